@@ -1,0 +1,252 @@
+/*
+ * wcfe.h — C ABI of the GB300 (sm_103a) per-step mechanics engine for the
+ * wholeCellFE 2-D cell-adhesion model.
+ *
+ * Everything crosses this boundary as plain pointers and sizes.  Host arrays
+ * use the reference's own memory order so a caller can pass the storage of a
+ * std::vector<Vec3d> (3 contiguous doubles per vertex) without repacking:
+ *
+ *   positions / velocities / accelerations / bond vectors : double[n][3]
+ *   Euler-Almansi strain (Voigt xx, yy, zz, xy, xz, yz)     : double[n][6]
+ *   concentrations c_A, c_C                                  : double[n]
+ *   triangles                                                : int32[t][3]
+ *   vertex -> triangle map (CSR, in the mesh's own order)    : int32[n+1], int32[3t]
+ *
+ * Every entry point returns an int status (WCFE_OK == 0).  No C++ exception
+ * crosses the ABI.  An engine owns one CUDA stream on one device; calls on one
+ * engine are not re-entrant (the reference is single threaded too).
+ *
+ * Reference interfaces replaced (file:line inside dredremontes/wholeCellFE,
+ * variant directory wholeCellFE_kMD unless stated):
+ *   driverVelocities_Explicit      cellBP/UL_growth_explicit.cpp:103-124 (+ predict cellBP/main.cpp:227-231)
+ *   updateFA (full)                cellBP/UL_growth_explicit.cpp:2026-2174 (k1: wholeCellFE_k1/cellBP/UL_growth_explicit.cpp:2005-2090)
+ *   updateForces_Explicit (cell)   cellBP/UL_growth_explicit.cpp:508-630
+ *   updateForces_Explicit (subs)   cellBP/UL_growth_explicit.cpp:429-504
+ *   calculateRes / evalElementRe   cellBP/UL_growth_explicit.cpp:632-928 (subs 931-1176)
+ *   calculateForce_FA              cellBP/UL_growth_explicit.cpp:1198-1303
+ *   calculateForce_FA_subs         cellBP/UL_growth_explicit.cpp:1305-1475
+ *   calculateForce_AP              cellBP/UL_growth_explicit.cpp:1477-1568
+ *   calculateBendingForce2D        cellBP/UL_growth_explicit.cpp:1571-1660
+ *   calculateAreaTot               cellBP/UL_growth_explicit.cpp:1662-1688
+ *   calculateAreaConstraintForce   cellBP/UL_growth_explicit.cpp:1691-1784
+ * The reference declares these ad hoc in cellBP/main.cpp:69-87 and has no header.
+ */
+#ifndef WCFE_H
+#define WCFE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WCFE_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    WCFE_OK = 0,
+    WCFE_ERR_ARG = 1,        /* bad argument (null pointer, size, unknown id) */
+    WCFE_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+    WCFE_ERR_NOMEM = 3,      /* device allocation failed */
+    WCFE_ERR_TOPOLOGY = 4,   /* mesh cannot be processed (e.g. a one-ring too large for a patch) */
+    WCFE_ERR_STATE = 5,      /* a cell's state holds NaN/Inf after a step (see wcfe_cell_status) */
+    WCFE_ERR_BUDGET = 6,     /* request does not fit the engine's HBM budget */
+    WCFE_ERR_LIMIT = 8,      /* size beyond a documented maximum */
+    WCFE_ERR_NODEVICE = 9    /* no CUDA device visible */
+};
+
+/* ---- integrin force laws ------------------------------------------------ */
+enum {
+    WCFE_LAW_LINEAR = 0,     /* f = k (D - L0); wholeCellFE_k1 / wholeCellFE_k31 */
+    WCFE_LAW_MD_TABLE = 1,   /* piecewise-linear MD fit; wholeCellFE_kMD UL:1203-1214 */
+    WCFE_LAW_POLY = 2        /* tangent stiffness k0 (1 + (e/x0)^2): f = k0 (e + e^3/(3 x0^2)), e = D - L0 */
+};
+
+/* ---- arithmetic forms --------------------------------------------------- */
+enum {
+    WCFE_PREC_FP64 = 0,      /* element assembly and update in FP64 (the plain form) */
+    WCFE_PREC_MIXED = 1      /* element assembly in FP32 (increment form), state/update in FP64 */
+};
+
+/* Reference variants for wcfe_params_default. */
+enum { WCFE_VARIANT_KMD = 0, WCFE_VARIANT_K1 = 1, WCFE_VARIANT_K31 = 2 };
+
+/*
+ * Per-cell physical constants.  The reference hard-codes every one of these in
+ * UL_growth_explicit.cpp; wcfe_params_default fills the reference values.
+ * Units: um, pN, s (stress pN/um^2 = Pa).
+ */
+typedef struct wcfe_params {
+    /* membrane (evalElementRe, UL:710-928) */
+    double mu;            /* shear modulus, 1000 (cell, UL:724) */
+    double thick;         /* thickness, 1 (UL:768) */
+    double thetag_dot;    /* growth rate, 0 (UL:714) */
+    double kappa;         /* active-stress anisotropy, 0.5 (UL:872) */
+    double tact_rate;     /* active stress ramp 200 Pa/s ... (UL:744-757) */
+    double tact_t1;       /* ... until t = 2 s ... */
+    double tact_max;      /* ... then 400 Pa */
+    double D_A, D_C;      /* diffusion coefficients 1, 1e-10 (UL:920-921); only the diagnostic residual uses them */
+    /* integrins (calculateForce_FA UL:1198-1303, updateFA UL:2026-2174) */
+    int32_t force_law;    /* WCFE_LAW_* */
+    int32_t linear_norm2d;/* 1: Bell force of the linear law uses the in-plane norm (k1 UL:2077) */
+    double k_lin;         /* linear stiffness, pN/um (1000 = 1 pN/nm) */
+    double rest_len;      /* spring rest length, um (0 in the reference) */
+    double poly_k0;       /* WCFE_LAW_POLY stiffness at zero extension, pN/um */
+    double poly_x0;       /* WCFE_LAW_POLY stiffening length, um */
+    double rho_i_max;     /* integrin density 100 /um^2 (UL:1218) */
+    double k_on, ka, kb, Fa, Fb;   /* Bell model 1, 0.004, 10, 15, 15 (UL:2139-2143) */
+    /* boundary (UL:1477-1784) */
+    double k_bend;        /* 20 (UL:1653) */
+    double k_area;        /* 1 (UL:1776) */
+    double area0;         /* 10*10*3.1416 (UL:1777) */
+    double ap_rate;       /* actin polymerisation rate 10 1/s (UL:1549) */
+    double ap_force;      /* 5 pN per event (UL:1560) */
+    double ap_density;    /* 100: events counted for ii < ap_density*L/2 (UL:1551) */
+    int32_t ap_enable;    /* 1: apply calculateForce_AP */
+    uint32_t seed;        /* key word 0 of the counter-based AP stream */
+    uint32_t stream;      /* key word 1: a per-cell stream id chosen by the caller */
+    /* integrator (updateForces_Explicit UL:567-628) */
+    double drag;          /* 0.001 */
+    double damp;          /* 0.001 */
+    double rho;           /* 1 */
+} wcfe_params;
+
+void wcfe_params_default(wcfe_params* p, int32_t variant);
+
+/*
+ * Counter-based stream shared by the GPU path and the oracle for the actin
+ * push of calculateForce_AP (UL:1546), which the reference draws from libc
+ * rand() after srand(time(NULL)) (UL:1481).  The k-th boundary vertex (in
+ * vertex index order) at AP call `call` of stream (seed, stream) draws the
+ * 31-bit value philox4x32_10(key = {seed, stream},
+ * counter = {k, call & 0xffffffff, call >> 32, 0}).x >> 1, used as
+ * Pr = r / (RAND_MAX + 1.0) with RAND_MAX = 2^31 - 1.
+ */
+uint32_t wcfe_ap_draw(uint32_t seed, uint32_t stream, uint64_t call, uint32_t k);
+/* Raw Philox4x32-10 block (Salmon et al., SC'11), exposed for known-answer tests. */
+void wcfe_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* ---- engine --------------------------------------------------------------- */
+typedef struct wcfe_engine wcfe_engine;
+
+/* hbm_budget_bytes == 0: no budget (allocate on demand). */
+int wcfe_engine_create(int32_t device, int32_t precision, uint64_t hbm_budget_bytes, wcfe_engine** out);
+int wcfe_engine_destroy(wcfe_engine* eng);
+int wcfe_engine_precision(const wcfe_engine* eng);
+/* Bytes of the budget still free for new cells (0 when there is no budget). */
+uint64_t wcfe_engine_free_bytes(const wcfe_engine* eng);
+/* Device bytes a cell of this size would take (state, topology, work lists). */
+uint64_t wcfe_cell_bytes(int32_t n_vert, int32_t n_tri);
+int wcfe_engine_sync(wcfe_engine* eng);
+
+/* ---- cells -------------------------------------------------------------- */
+/*
+ * Create a cell from its triangle mesh.  vt_ptr/vt_idx give the vertex ->
+ * triangle map in the mesh's own order (NonDestructiveTriMesh::
+ * m_vertex_to_triangle_map); pass NULL to build it in ascending triangle order
+ * (what read_ecomsol's add_triangle sequence gives).  is_bnd may be NULL: then
+ * a vertex is on the boundary when one of its edges has an odd triangle count
+ * (NonDestructiveTriMesh::rebuild_auxiliary_structures).
+ * The state starts at zero with c_A = 100 (cellBP/main.cpp:674-677).
+ */
+int wcfe_cell_create(wcfe_engine* eng, int32_t n_vert, int32_t n_tri, const int32_t* tri,
+                     const int32_t* vt_ptr, const int32_t* vt_idx, const uint8_t* is_bnd,
+                     const wcfe_params* params, int32_t* cell_out);
+int wcfe_cell_destroy(wcfe_engine* eng, int32_t cell);
+int wcfe_cell_set_params(wcfe_engine* eng, int32_t cell, const wcfe_params* params);
+/* Replace the topology after El Topo remeshing; the state must be set again afterwards. */
+int wcfe_cell_set_topology(wcfe_engine* eng, int32_t cell, int32_t n_vert, int32_t n_tri, const int32_t* tri,
+                           const int32_t* vt_ptr, const int32_t* vt_idx, const uint8_t* is_bnd);
+/* Substrate mesh of the cell, at its previous (X_s) and current (x_s) positions.
+ * n_tri == 0 / tri == NULL: a flat rigid plane (the substrate displacement is 0). */
+int wcfe_cell_set_substrate(wcfe_engine* eng, int32_t cell, int32_t n_vert, int32_t n_tri,
+                            const int32_t* tri, const double* X_s, const double* x_s);
+/* Any pointer may be NULL (that array is left unchanged / not returned). */
+int wcfe_cell_set_state(wcfe_engine* eng, int32_t cell, const double* x, const double* V, const double* A,
+                        const double* ea, const double* c_A, const double* c_C, const double* fa_u);
+int wcfe_cell_get_state(wcfe_engine* eng, int32_t cell, double* x, double* V, double* A, double* ea,
+                        double* c_A, double* c_C, double* fa_u);
+/* Simulation time used for the active-stress ramp and the AP call counter. */
+int wcfe_cell_set_clock(wcfe_engine* eng, int32_t cell, double t_cur, uint64_t ap_calls);
+int wcfe_cell_get_clock(wcfe_engine* eng, int32_t cell, double* t_cur, uint64_t* ap_calls);
+/* Bit 0: NaN/Inf in the state after the last step. */
+int wcfe_cell_status(wcfe_engine* eng, int32_t cell, uint32_t* status);
+int wcfe_cell_sizes(wcfe_engine* eng, int32_t cell, int32_t* n_vert, int32_t* n_tri, int32_t* n_bnd, int32_t* n_patch);
+
+/* ---- drop-in step pieces (one cell; the order of cellBP/main.cpp:224-363) -- */
+/* driverVelocities_Explicit + new_positions: V_hlf = V + dt/2 A (z = 0), x_pred = x + dt V_hlf.
+ * Outputs to host arrays (either may be NULL); V_hlf also stays on the device. */
+int wcfe_cell_predict(wcfe_engine* eng, int32_t cell, double dt, double* x_pred, double* V_hlf);
+/* updateFA: X (NULL = device positions) are the positions before El Topo's
+ * integrate, x_new after it; X_s/x_s the substrate's (NULL = as set). */
+int wcfe_cell_update_fa(wcfe_engine* eng, int32_t cell, double dt_real, const double* X, const double* x_new,
+                        const double* X_s, const double* x_s);
+/* updateForces_Explicit (cell overload): residual, integrin, AP, drag, bending and
+ * area forces, then A, ea and V.  Positions x_new become the current positions. */
+int wcfe_cell_update_forces(wcfe_engine* eng, int32_t cell, double dt, double dt_real, double t_tot);
+
+/* ---- diagnostic mirrors of the reference's force functions ------------- */
+/* calculateRes (cell overload): outputs double[n][3], [n][6], [n], [n], [n] (any may be NULL).
+ * X and x_new are host positions; centroid and time as in the reference call. */
+int wcfe_cell_eval_residual(wcfe_engine* eng, int32_t cell, const double* X, const double* x_new,
+                            double dt_real, const double centroid[3], double t_tot,
+                            double* Res, double* Res_ea, double* MM, double* Res_Adif, double* Res_Cdif);
+/* calculateAreaTot + calculateForce_FA + calculateForce_AP + calculateBendingForce2D +
+ * calculateAreaConstraintForce at host positions x (outputs double[n][3], area4 = {A, cx, cy, cz}). */
+int wcfe_cell_eval_forces(wcfe_engine* eng, int32_t cell, const double* x, double dt_real,
+                          double* F_FA, double* F_AP, double* F_bend, double* F_area, double area4[4]);
+
+/* ---- synthetic stepping of every live cell (no El Topo) ----------------- */
+/* nsteps full explicit steps of every live cell: predict, updateFA, updateForces.
+ * All cells advance in one launch per phase; runs asynchronously on the engine stream. */
+int wcfe_engine_step(wcfe_engine* eng, int32_t nsteps, double dt);
+/* Same, restricted to the listed cells. */
+int wcfe_engine_step_cells(wcfe_engine* eng, const int32_t* cells, int32_t ncells, int32_t nsteps, double dt);
+/* Capture steps into CUDA graphs (1) or launch eagerly (0, default). */
+int wcfe_engine_set_graphs(wcfe_engine* eng, int32_t enable);
+/* Kernel shapes: threads per CTA of the patch kernel, max elements per patch.
+ * 0 = choose by the built-in autotuner (wcfe_engine_autotune). */
+int wcfe_engine_set_shape(wcfe_engine* eng, int32_t patch_threads, int32_t patch_elems);
+int wcfe_engine_get_shape(const wcfe_engine* eng, int32_t* patch_threads, int32_t* patch_elems);
+/* Time every candidate shape on the live cells (reps steps each) and keep the fastest. */
+int wcfe_engine_autotune(wcfe_engine* eng, double dt, int32_t reps);
+/* Device timing of the last wcfe_engine_step (ms per kernel phase, summed over steps). */
+int wcfe_engine_last_timing(wcfe_engine* eng, float* ms_vertex, float* ms_patch);
+/* Enable per-phase CUDA-event timing inside wcfe_engine_step (off by default). */
+int wcfe_engine_set_timing(wcfe_engine* eng, int32_t enable);
+/* Number of kernels this engine launched since creation. */
+uint64_t wcfe_engine_launches(const wcfe_engine* eng);
+
+/* ---- serving: continuous batching of whole cell simulations -------------- */
+typedef struct wcfe_server wcfe_server;
+/* A request: one cell mesh + initial state + number of steps. Arrays are copied at submit. */
+typedef struct wcfe_request {
+    int32_t n_vert, n_tri;
+    const int32_t* tri;
+    const double* x;          /* [n][3] initial positions */
+    const wcfe_params* params;
+    int32_t n_steps;
+    const int32_t* sub_tri;   /* optional substrate mesh (NULL = plane) */
+    const double* sub_X;
+    int32_t sub_n_vert, sub_n_tri;
+} wcfe_request;
+
+int wcfe_server_create(wcfe_engine* eng, double dt, wcfe_server** out);
+int wcfe_server_destroy(wcfe_server* srv);
+/* Queue a request; *req_id receives its id (monotonic from 0). */
+int wcfe_server_submit(wcfe_server* srv, const wcfe_request* req, int64_t* req_id);
+/* One serving iteration: admit queued requests that fit the free budget, advance
+ * every resident cell by one step in one batched launch per phase, retire the
+ * finished ones.  *n_active / *n_queued report the counts after the iteration. */
+int wcfe_server_iterate(wcfe_server* srv, int32_t* n_active, int32_t* n_queued);
+/* Fetch a finished request's final positions (double[n][3]) and latency stats.
+ * Returns WCFE_ERR_ARG while it is still running. */
+int wcfe_server_result(wcfe_server* srv, int64_t req_id, double* x_out, double* seconds_in_system);
+/* Per-iteration wall time samples (seconds) collected so far; returns count. */
+int64_t wcfe_server_step_times(wcfe_server* srv, double* out, int64_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WCFE_H */

@@ -1,0 +1,34 @@
+"""The oracle against the reference compiled from its sources (oracle/_ref), on
+fresh seeded inputs.  Runs only where oracle/build_ref.sh has built the
+reference (the container that holds the reference sources); skipped elsewhere."""
+import numpy as np
+import pytest
+
+from conftest import relerr
+from oracle import oracle_py as O
+from wholecellfe_gb300 import synth
+from wholecellfe_gb300.params import default_params, kint_for
+
+
+@pytest.mark.parametrize("variant", ["kMD", "k1", "k31"])
+@pytest.mark.parametrize("seed", [21, 22])
+def test_oracle_matches_reference_build(variant, seed):
+    if not O.ref_available(variant):
+        pytest.skip("reference not built here (oracle/build_ref.sh)")
+    R = O.Ref(variant)
+    p = default_params(variant)
+    x0, tri = synth.disk_mesh(500, seed=seed)
+    n = len(x0)
+    hc = R.mesh(tri, n)
+    ptr, idx, bnd = R.mesh_map(hc, n, len(tri))
+    m = O.OMesh(tri, n, ptr, idx, bnd)
+    Xs, tri_s = synth.square_substrate(40.0, 16)
+    hs = R.mesh(tri_s, len(Xs))
+    ms = O.OMesh(tri_s, len(Xs))
+    st = synth.initial_state(x0, perturb=1.0, seed=seed)
+    s_ref, t_ref, c_ref = R.steps(hc, st, hs, Xs, kint_for(variant), 5e-5, 25, 1.9, p.seed, p.stream, 3)
+    c = O.OCell(m, st, p, t=1.9, ap_call=3, sub=ms, Xs=Xs)
+    c.steps(25, 5e-5)
+    for a, b, s0 in zip(c.state(), s_ref, st):
+        assert relerr(a - s0, b - s0) <= 1e-12
+    assert c.t == t_ref and c.ap_call == c_ref
