@@ -1,0 +1,431 @@
+"""Benchmark: cell-steps/s of the batched mixed-precision form against the plain
+one-cell FP64 form on one GB300 (the metric of the wholeCellFE mechanics step).
+
+Workload (N = 1): 256 uneven cells, vertex counts log-uniform in [500, 20000]
+(seeded disk meshes), integrins on 0.4 x N vertices, stiffness model per cell
+drawn from {linear 1 pN/nm, linear 31 pN/nm, polynomial k0 = 31 pN/nm x0 = 5 nm},
+flat rigid substrate, dt = 5e-5 s, from rest.  One "step" advances every cell by
+one explicit step (A1-A9), so a step is 256 cell-steps.
+
+Reported on one JSON line: the headline value (batched mixed form, device-timed,
+inputs resident), e2e (the same loop through the batched drop-in exchange with
+pinned host buffers: per step the predicted positions go to the host and the
+integrated positions come back), the plain FP64 one-cell form (about 2000 vertices),
+the relative displacement error of the mixed form against the FP64 form, per-step
+p50/p99 latency, the roofline of the dominant kernel, GPU clocks sampled during the
+timed region, and the CPU baseline.
+
+--impl reference: the reference's CPU path on the host cores (the oracle port of
+cellBP/UL_growth_explicit.cpp, all threads), same workload, bounded sample.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-steps/s batched+mixed vs plain FP64 on 1 GB300 at <=1e-6 rel err; p50/p99"
+DT = 5e-5
+N_CELLS = 256
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ----------------------------------------------------------------------------- workload
+def make_workload(seed: int, ncells: int = N_CELLS):
+    from wholecellfe_gb300 import synth
+    from wholecellfe_gb300.params import default_params
+    rng = np.random.default_rng(seed)
+    cells = []
+    for i in range(ncells):
+        n = int(round(math.exp(rng.uniform(math.log(500), math.log(20000)))))
+        x0, tri = synth.disk_mesh(n, seed=seed * 100003 + i)
+        model = int(rng.integers(0, 3))
+        if model == 0:
+            p = default_params("k1")
+        elif model == 1:
+            p = default_params("k31")
+        else:
+            p = default_params("k31")
+            p.force_law, p.poly_k0, p.poly_x0, p.linear_norm2d = 2, 31000.0, 0.005, 0
+        p.seed, p.stream = seed & 0xffffffff, i
+        nv = len(x0)
+        rho = np.zeros(nv)
+        pick = rng.choice(nv, size=max(1, int(round(0.4 * nv))), replace=False)
+        rho[pick] = p.rho_i_max
+        cells.append(dict(x0=x0, tri=tri, p=p, rho=rho, model=model))
+    return cells
+
+
+def load_cells(eng, cells):
+    from wholecellfe_gb300 import synth
+    hs = []
+    for c in cells:
+        h = eng.add_cell(c["x0"], c["tri"], c["p"], state=synth.initial_state(c["x0"]))
+        h.set_integrins(c["rho"])
+        hs.append(h)
+    return hs
+
+
+# ----------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.rows = []
+        self.proc = None
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([s.strip() for s in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+# ----------------------------------------------------------------------------- CPU baseline
+def cpu_baseline(cells, steps: int, budget_s: float = 15.0):
+    """The oracle (C port of the reference's step) on the host cores, all threads, on a
+    bounded sample of the workload's cells; returns cell-steps/s and what was run."""
+    from oracle import oracle_py as O
+    from wholecellfe_gb300 import synth
+    nthreads = os.cpu_count() or 1
+    # probe one mid-size cell for one step to size the sample
+    probe = min(cells, key=lambda c: abs(len(c["x0"]) - 5000))
+    m = O.OMesh(probe["tri"], len(probe["x0"]))
+    oc = O.OCell(m, synth.initial_state(probe["x0"]), probe["p"], rho_w=probe["rho"])
+    t0 = time.perf_counter()
+    oc.steps(1, DT)
+    per_vertex_step = (time.perf_counter() - t0) / len(probe["x0"])
+    mean_nv = float(np.mean([len(c["x0"]) for c in cells]))
+    ncs = max(nthreads, min(len(cells), 64))
+    nsteps = max(1, int(budget_s * nthreads / (per_vertex_step * mean_nv * ncs)))
+    nsteps = min(nsteps, steps)
+    sample = cells[:ncs]
+    ocs = []
+    meshes = []
+    for c in sample:
+        mm = O.OMesh(c["tri"], len(c["x0"]))
+        meshes.append(mm)
+        ocs.append(O.OCell(mm, synth.initial_state(c["x0"]), c["p"], rho_w=c["rho"]))
+    t0 = time.perf_counter()
+    O.cells_steps_mt(ocs, nsteps, DT, nthreads)
+    dt = time.perf_counter() - t0
+    return {"value": len(sample) * nsteps / dt, "unit": "cell-steps/s", "cores": nthreads, "kind": "port",
+            "sample": f"{len(sample)} of the workload's cells (mean {np.mean([len(c['x0']) for c in sample]):.0f} "
+                      f"vertices) x {nsteps} steps, oracle/wcfe_oracle.c on {nthreads} host threads, {dt:.1f} s"}
+
+
+# ----------------------------------------------------------------------------- measurements
+def kernel_bytes_patch_mixed(nv_total: int, nt_total: int) -> float:
+    """Algorithmic DRAM bytes of one mixed patch-phase launch: per vertex it reads the FP32
+    element record (64 B), x (24), the bond vector (24), c_C (8), V and A (48), the strain
+    (48), the one-ring offsets and slot codes (4 + 2 per incidence), and writes V, A (48) and
+    the strain (48); per element it reads the triangle (12) and its patch entry (4)."""
+    per_v = 64 + 24 + 24 + 8 + 48 + 48 + 4 + 48 + 48
+    per_incidence = 2
+    per_t = 12 + 4
+    return per_v * nv_total + per_incidence * 3 * nt_total + per_t * nt_total
+
+
+def percentile(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = (len(xs) - 1) * q
+    f, c = math.floor(k), math.ceil(k)
+    return xs[f] if f == c else xs[f] + (xs[c] - xs[f]) * (k - f)
+
+
+def timed_steps(eng, steps, dt, ranks_barrier=None):
+    """Device-timed steps on the engine's own stream: the engine records CUDA events
+    before each phase of every step (no host synchronisation inside the timed region);
+    total = first event to last event, plus per-step and per-phase durations."""
+    import torch
+    eng.set_timing(True)
+    eng.sync()
+    torch.cuda.synchronize()
+    if ranks_barrier:
+        ranks_barrier()
+    t_host0 = time.perf_counter()
+    eng.step(steps, dt)          # returns after the last event completed
+    eng.sync()
+    wall = time.perf_counter() - t_host0
+    torch.cuda.synchronize()
+    per_step, span = eng.step_times()
+    ms_v, ms_p = eng.last_timing()
+    eng.set_timing(False)
+    return dict(total_ms=span, wall_s=wall, per_step=per_step, ms_v=ms_v, ms_p=ms_p)
+
+
+def run_ours(args):
+    import torch
+    from wholecellfe_gb300 import capi
+    from wholecellfe_gb300.params import default_params
+    from wholecellfe_gb300 import synth
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = local if world > 1 else 0
+    torch.cuda.init()
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    cells = make_workload(seed=1000 + rank, ncells=args.cells)
+    nv_total = sum(len(c["x0"]) for c in cells)
+    nt_total = sum(len(c["tri"]) for c in cells)
+    log(f"[bench] rank {rank}: {len(cells)} cells, {nv_total} vertices, {nt_total} triangles")
+
+    # ---- batched mixed form (headline) ----
+    eng = capi.Engine(capi.PREC_MIXED, device=device)
+    load_cells(eng, cells)
+    eng.autotune(DT, 3)
+    thr, emax = eng.shape()
+    for _ in range(args.warmup):
+        eng.step(1, DT)
+    eng.sync()
+    launches0 = eng.launches()
+    clocks = ClockSampler()
+    clocks.start()
+    res = timed_steps(eng, args.steps, DT, barrier)
+    clocks_info = clocks.stop()
+    launches = eng.launches() - launches0
+    t_s = res["total_ms"] / 1e3
+    if dist:
+        tt = torch.tensor([t_s], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_s = float(tt.item())
+    value = world * len(cells) * args.steps / t_s
+    p50 = percentile(res["per_step"], 0.5)
+    p99 = percentile(res["per_step"], 0.99)
+    avg_v = res["ms_v"] / args.steps
+    avg_p = res["ms_p"] / args.steps
+    log(f"[bench] mixed: {t_s * 1e3 / args.steps:.3f} ms/step (vertex {avg_v:.3f}, patch {avg_p:.3f}), "
+        f"{value:.3e} cell-steps/s, wall {res['wall_s']:.2f}s")
+
+    # ---- e2e through the batched drop-in exchange, pinned host buffers ----
+    ntot = eng.total_vertices()
+    host = torch.empty((ntot, 3), dtype=torch.float64, pin_memory=True)
+    xbuf = host.numpy()
+    for _ in range(2):
+        eng.predict_all(DT, xbuf)
+        eng.update_all(DT, DT, xbuf)
+    eng.sync()
+    barrier()
+    e_launch0 = eng.launches()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.predict_all(DT, xbuf)          # device step part 1 + D2H of the predicted positions
+        eng.update_all(DT, DT, xbuf)       # H2D of the integrated positions + device step part 2
+    eng.sync()
+    e2e_s = time.perf_counter() - t0
+    e2e_launches = eng.launches() - e_launch0
+    if dist:
+        tt = torch.tensor([e2e_s], device=f"cuda:{local}")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_s = float(tt.item())
+    e2e = {"value": world * len(cells) * args.steps / e2e_s, "unit": "cell-steps/s",
+           "h2d_bytes_per_step": int(ntot * 24), "d2h_bytes_per_step": int(ntot * 24),
+           "api": "wcfe_engine_predict + wcfe_engine_update (include/wcfe.h), pinned host buffers",
+           "gpu_launches": int(e2e_launches)}
+    log(f"[bench] e2e: {e2e['value']:.3e} cell-steps/s")
+    eng.close()
+
+    out = None
+    if rank == 0:
+        # ---- error of the mixed form against the FP64 form (same workload, same steps) ----
+        err_steps = min(args.steps, 300)
+        finals = {}
+        for prec in (capi.PREC_MIXED, capi.PREC_FP64):
+            e = capi.Engine(prec, device=device)
+            hs = load_cells(e, cells)
+            e.step(err_steps, DT)
+            e.sync()
+            finals[prec] = [h.get_state()[0] for h in hs]
+            e.close()
+        errs = []
+        for c, xm, xd in zip(cells, finals[capi.PREC_MIXED], finals[capi.PREC_FP64]):
+            u = xd - c["x0"]
+            errs.append(float(np.max(np.abs(xm - xd)) / max(float(np.max(np.abs(u))), 1e-300)))
+        max_err = max(errs)
+        log(f"[bench] mixed vs FP64 relative displacement error after {err_steps} steps: max {max_err:.2e}")
+
+        # ---- plain one-cell FP64 form (config 1 size) ----
+        x0, tri = synth.disk_mesh(2000, seed=1)
+        p = default_params("k1")
+        ep = capi.Engine(capi.PREC_FP64, device=device)
+        hp = ep.add_cell(x0, tri, p, state=synth.initial_state(x0))
+        for _ in range(args.warmup):
+            ep.step(1, DT)
+        plain_steps = 200
+        pr = timed_steps(ep, plain_steps, DT)
+        ep.close()
+        plain_value = plain_steps / (pr["total_ms"] / 1e3)
+        plain_wall = plain_steps / pr["wall_s"]
+        log(f"[bench] plain FP64 one cell: {pr['total_ms'] / plain_steps * 1e3:.1f} us/step device, "
+            f"{plain_value:.3e} cell-steps/s device, {plain_wall:.3e} wall")
+
+        # ---- roofline of the dominant kernel ----
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except OSError:
+            pass
+        hbm = peaks.get("hbm_gbs", 6800.0)
+        kbytes = kernel_bytes_patch_mixed(nv_total, nt_total)
+        achieved = kbytes / (avg_p * 1e-3) / 1e9
+        traffic = None
+        prof = os.path.join(ROOT, "profiles", "k_patch_phase_mixed.md")
+        if os.path.exists(prof):
+            for line in open(prof):
+                if line.startswith("dram_bytes_per_vertex:"):
+                    traffic = float(line.split(":")[1]) * nv_total
+        roofline = {"bound": "hbm", "kernel": "k_patch_phase_mixed", "achieved": round(achieved, 1),
+                    "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                    "traffic": traffic, "algorithmic_bytes_per_launch": int(kbytes),
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
+                    "avg_launch_ms": round(avg_p, 4), "vertex_phase_avg_launch_ms": round(avg_v, 4)}
+
+        cpu = cpu_baseline(cells, args.steps) if not args.no_cpu else None
+        out = {
+            "metric": METRIC, "value": round(value, 1), "unit": "cell-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_s * 1e3 / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32-assembly+fp64-update",
+            "data": "synthetic: seeded disk meshes, random-init state from rest",
+            "config": {"workload": f"{len(cells)} uneven cells per GPU, vertices log-uniform [500, 20000], "
+                                   "integrins 0.4 x vertices, stiffness {linear 1, linear 31, poly 31 pN/nm x0 5 nm}, "
+                                   "flat rigid substrate, dt 5e-5 s, explicit step A1-A9",
+                       "cells": len(cells), "vertices": nv_total, "triangles": nt_total,
+                       "l2": f"state {nv_total * 600 / 1e9:.2f} GB resident > 129 MB L2 (inputs larger than L2)",
+                       "patch_threads": thr, "patch_elems": emax, "autotuned": True,
+                       "parallelism": f"replicas x{world}"},
+            "p50_ms_per_step": round(p50, 4), "p99_ms_per_step": round(p99, 4),
+            "plain_fp64": {"value": round(plain_value, 1), "unit": "cell-steps/s", "cell_vertices": len(x0),
+                           "p50_ms_per_step": round(percentile(pr["per_step"], 0.5), 4),
+                           "p99_ms_per_step": round(percentile(pr["per_step"], 0.99), 4),
+                           "wall_cell_steps_per_s": round(plain_wall, 1)},
+            "ratio_vs_plain_fp64": round(value / world / plain_value, 2),
+            "mixed_vs_fp64_rel_displacement_error": max_err, "error_steps": err_steps,
+            "element_assemblies_per_s": round(value / len(cells) * nt_total / world, 1),
+            "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
+            "clocks": clocks_info,
+        }
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    if out:
+        print(json.dumps(out), flush=True)
+
+
+def run_reference(args):
+    """The reference's CPU implementation of the step (the oracle port; the reference's own
+    sources are not on this machine) on all host cores, bounded sample of the workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle_py as O
+    from wholecellfe_gb300 import synth
+    cells = make_workload(seed=1000, ncells=args.cells)
+    nthreads = os.cpu_count() or 1
+    # one timed "step" = every sampled cell advanced by a few explicit steps, sized to finish in minutes
+    sample = cells[:max(nthreads, 32)]
+    ocs = [O.OCell(O.OMesh(c["tri"], len(c["x0"])), synth.initial_state(c["x0"]), c["p"], rho_w=c["rho"])
+           for c in sample]
+    per = 2
+    for _ in range(min(args.warmup, 1)):
+        O.cells_steps_mt(ocs, 1, DT, nthreads)
+    times = []
+    steps = min(args.steps, 10)
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        O.cells_steps_mt(ocs, per, DT, nthreads)
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = len(sample) * per * steps / tot
+    cpu = {"value": round(value, 1), "unit": "cell-steps/s", "cores": nthreads, "kind": "port",
+           "sample": f"{len(sample)} of the {len(cells)} workload cells x {per} explicit steps per timed step, "
+                     f"{steps} timed steps, oracle/wcfe_oracle.c (C port of cellBP/UL_growth_explicit.cpp)"}
+    out = {"metric": METRIC, "value": round(value, 1), "unit": "cell-steps/s", "n_gpus": 0, "steps": steps,
+           "warmup": args.warmup, "ms_per_step": round(tot / steps * 1e3, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+           "config": {"workload": "same 256-cell workload, CPU sample", "cells_sampled": len(sample)},
+           "impl": "reference", "cpu_baseline": cpu,
+           "e2e": {"value": round(value, 1), "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "p50_ms_per_step": round(percentile(times, 0.5) * 1e3, 3),
+           "p99_ms_per_step": round(percentile(times, 0.99) * 1e3, 3)}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=N_CELLS)
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        args.warmup = 3
+    from oracle import oracle_py
+    oracle_py.build()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

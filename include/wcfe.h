@@ -114,6 +114,9 @@ typedef struct wcfe_params {
 
 void wcfe_params_default(wcfe_params* p, int32_t variant);
 
+/* Message of the last failing call on this thread ("" if none). */
+const char* wcfe_last_error(void);
+
 /*
  * Counter-based stream shared by the GPU path and the oracle for the actin
  * push of calculateForce_AP (UL:1546), which the reference draws from libc
@@ -203,6 +206,19 @@ int wcfe_cell_eval_forces(wcfe_engine* eng, int32_t cell, const double* x, doubl
 int wcfe_engine_step(wcfe_engine* eng, int32_t nsteps, double dt);
 /* Same, restricted to the listed cells. */
 int wcfe_engine_step_cells(wcfe_engine* eng, const int32_t* cells, int32_t ncells, int32_t nsteps, double dt);
+/* Batched drop-in exchange for cells coupled to a host-side integrator (El Topo):
+ * positions of every live cell packed [sum n][3] in ascending cell-id order.
+ * wcfe_engine_predict: driverVelocities_Explicit + predict of every cell, predicted
+ *   positions copied to x_pred (returns when the copy is done);
+ * wcfe_engine_update: the integrated positions x_new (dt_real = the step El Topo took)
+ *   drive updateFA and updateForces_Explicit of every cell in one launch per phase;
+ *   x_new is read asynchronously: keep it unchanged until the next synchronising call. */
+int64_t wcfe_engine_total_vertices(wcfe_engine* eng);
+int wcfe_engine_predict(wcfe_engine* eng, double dt, double* x_pred);
+int wcfe_engine_update(wcfe_engine* eng, double dt, double dt_real, const double* x_new);
+/* Per-vertex integrin density (#/um^2) replacing rho_i_max (UL:1218); NULL restores the
+ * uniform density.  A zero entry is a vertex without integrins. */
+int wcfe_cell_set_integrins(wcfe_engine* eng, int32_t cell, const double* rho);
 /* Capture steps into CUDA graphs (1) or launch eagerly (0, default). */
 int wcfe_engine_set_graphs(wcfe_engine* eng, int32_t enable);
 /* Kernel shapes: threads per CTA of the patch kernel, max elements per patch.
@@ -213,7 +229,11 @@ int wcfe_engine_get_shape(const wcfe_engine* eng, int32_t* patch_threads, int32_
 int wcfe_engine_autotune(wcfe_engine* eng, double dt, int32_t reps);
 /* Device timing of the last wcfe_engine_step (ms per kernel phase, summed over steps). */
 int wcfe_engine_last_timing(wcfe_engine* eng, float* ms_vertex, float* ms_patch);
-/* Enable per-phase CUDA-event timing inside wcfe_engine_step (off by default). */
+/* Per-step device time (ms, events on the engine stream) of the last timed wcfe_engine_step;
+ * *span_ms receives the time from the first step's start to the last step's end. Returns the count. */
+int64_t wcfe_engine_step_times(wcfe_engine* eng, float* out, int64_t cap, float* span_ms);
+/* Enable per-phase CUDA-event timing inside wcfe_engine_step (off by default); a timed
+ * call launches eagerly (no graph) and records three events per step without host sync. */
 int wcfe_engine_set_timing(wcfe_engine* eng, int32_t enable);
 /* Number of kernels this engine launched since creation. */
 uint64_t wcfe_engine_launches(const wcfe_engine* eng);
@@ -245,6 +265,15 @@ int wcfe_server_iterate(wcfe_server* srv, int32_t* n_active, int32_t* n_queued);
 int wcfe_server_result(wcfe_server* srv, int64_t req_id, double* x_out, double* seconds_in_system);
 /* Per-iteration wall time samples (seconds) collected so far; returns count. */
 int64_t wcfe_server_step_times(wcfe_server* srv, double* out, int64_t cap);
+
+/* ---- host-only inspection of the connectivity preprocessing (no device) --- */
+/* Boundary ranks and neighbour candidates (the scan of UL:1500-1531), patches and
+ * one-ring slot codes, exactly as the engine builds them.  Capacities in int32 units. */
+int wcfe_debug_topology(int32_t n_vert, int32_t n_tri, const int32_t* tri, const int32_t* vt_ptr,
+                        const int32_t* vt_idx, const uint8_t* is_bnd, int32_t patch_elems_max, int32_t* nb_out,
+                        int32_t* bnd_rank, int32_t* bnd_cptr, int32_t* bnd_cand, int32_t cand_cap, int32_t* np_out,
+                        int32_t* patch, int32_t patch_cap, int32_t* patch_elems, int32_t elems_cap,
+                        uint16_t* vc_code);
 
 #ifdef __cplusplus
 }

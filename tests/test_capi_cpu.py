@@ -1,0 +1,134 @@
+"""The C-ABI library on the CPU: it loads, exports every function include/wcfe.h
+declares, and its host-side integer bookkeeping matches the reference's mesh
+structures and the oracle.  No kernel runs here."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from oracle import oracle_py as O
+from wholecellfe_gb300 import capi, synth
+from wholecellfe_gb300.params import Params, default_params
+
+
+def header_functions():
+    src = open(os.path.join(ROOT, "include", "wcfe.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(wcfe_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = capi.load()
+    names = header_functions()
+    assert len(names) >= 40
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the Python mirror binds each of them with a signature
+    assert set(names) <= set(capi.SIGNATURES), set(names) - set(capi.SIGNATURES)
+
+
+def test_engine_without_device_fails_cleanly():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is visible")
+    h = C.c_void_p()
+    rc = capi.load().wcfe_engine_create(0, 0, 0, C.byref(h))
+    assert rc == 9  # WCFE_ERR_NODEVICE
+
+
+def test_params_layout_and_defaults():
+    for v, name in ((0, "kMD"), (1, "k1"), (2, "k31")):
+        a = Params()
+        capi.load().wcfe_params_default(C.byref(a), v)
+        b = default_params(name)
+        assert bytes(a) == bytes(b)
+        c = Params()
+        O.lib().wo_params_default(C.byref(c), v)
+        assert bytes(a) == bytes(c)
+
+
+def test_philox_and_ap_stream_match_oracle():
+    L = capi.load()
+    c = (C.c_uint32 * 4)(0, 0, 0, 0)
+    k = (C.c_uint32 * 2)(0, 0)
+    o = (C.c_uint32 * 4)()
+    L.wcfe_philox4x32_10(c, k, o)
+    assert tuple(o) == (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)
+    rng = np.random.default_rng(3)
+    for _ in range(200):
+        s, st, call, kk = (int(rng.integers(0, 2**32)), int(rng.integers(0, 2**32)), int(rng.integers(0, 2**40)),
+                           int(rng.integers(0, 2**20)))
+        assert L.wcfe_ap_draw(s, st, call, kk) == O.lib().wo_ap_draw(s, st, call, kk)
+
+
+def _j1j2_from_candidates(x, rank, cptr, cand, v):
+    """Evaluate the engine's candidate list with the reference's sign rule (UL:1517-1525)."""
+    r = rank[v]
+    j1 = j2 = -1
+    for nj, ni in cand[cptr[r]:cptr[r + 1]]:
+        d1 = x[v] - x[nj]
+        d2 = x[ni] - x[v]
+        ncz = d1[0] * d2[1] - d1[1] * d2[0]
+        if ncz > 0:
+            j1 = nj
+        else:
+            j2 = nj
+    return j1, j2
+
+
+@pytest.mark.parametrize("n", [60, 500, 3000])
+def test_boundary_candidates_reproduce_reference_scan(n):
+    x, tri = synth.disk_mesh(n, seed=n)
+    t = capi.debug_topology(tri, len(x))
+    m = O.OMesh(tri, len(x))
+    j1o, j2o, cto = O.bnd_table(m, x)
+    bnd = m.bnd
+    assert t["nb"] == int(bnd.sum())
+    assert np.array_equal(t["rank"] >= 0, bnd.astype(bool))
+    for v in np.nonzero(bnd)[0]:
+        j1, j2 = _j1j2_from_candidates(x, t["rank"], t["cptr"], t["cand"], v)
+        assert (j1, j2) == (j1o[v], j2o[v])
+        assert t["cptr"][t["rank"][v] + 1] - t["cptr"][t["rank"][v]] == cto[v]
+
+
+def test_topology_matches_reference_mesh_structures(golden):
+    g = golden
+    n = len(g["x0"])
+    t = capi.debug_topology(g["tri"], n, vt_ptr=g["vt_ptr"], vt_idx=g["vt_idx"], bnd=g["bnd"])
+    t2 = capi.debug_topology(g["tri"], n)   # map and flags derived by the engine itself
+    for k in ("rank", "cptr", "cand", "patch", "elems", "codes"):
+        assert np.array_equal(t[k], t2[k]), k
+
+
+@pytest.mark.parametrize("emax", [24, 96, 320, 1024])
+def test_patches_cover_each_one_ring(emax):
+    x, tri = synth.disk_mesh(2000, seed=4)
+    n = len(x)
+    vt_ptr, vt_idx = synth.vertex_triangle_map(n, tri)
+    t = capi.debug_topology(tri, n, emax=emax)
+    P = t["patch"]
+    assert P[0, 0] == 0 and P[-1, 0] + P[-1, 1] == n and (P[1:, 0] == P[:-1, 0] + P[:-1, 1]).all()
+    assert (P[:, 3] <= emax).all()
+    for p in range(t["np"]):
+        v0, nvp, e0, ne = P[p]
+        elems = t["elems"][e0:e0 + ne]
+        assert len(set(elems.tolist())) == ne
+        for v in range(v0, v0 + nvp):
+            for k in range(vt_ptr[v], vt_ptr[v + 1]):
+                code = int(t["codes"][k])
+                slot, corner = code >> 2, code & 3
+                assert elems[slot] == vt_idx[k]
+                assert tri[vt_idx[k], corner] == v
+
+
+def test_topology_rejects_bad_meshes():
+    L = capi.load()
+    tri = np.array([[0, 1, 5]], np.int32)
+    with pytest.raises(capi.WcfeError):
+        capi.debug_topology(tri, 3)
+    with pytest.raises(capi.WcfeError):   # a vertex with no triangle
+        capi.debug_topology(np.array([[0, 1, 2]], np.int32), 4)
+    assert L is not None

@@ -1,0 +1,130 @@
+"""GPU: the mixed-precision form (FP32 increment-form assembly, FP64 state and
+update) against the FP64 form, and the batched drop-in exchange path.
+
+Mixed-form tolerance: relative displacement error <= 1e-6 against the FP64 form
+after 300 steps (max|x_mixed - x_fp64| / max|x_fp64 - x0| per cell)."""
+import numpy as np
+import pytest
+
+from wholecellfe_gb300 import capi, synth
+from wholecellfe_gb300.params import default_params
+
+pytestmark = pytest.mark.gpu
+MIXED_TOL = 1e-6
+
+
+def _law(p, k):
+    if k == 2:
+        p.force_law, p.poly_k0, p.poly_x0, p.linear_norm2d = 2, 31000.0, 0.005, 0
+    return p
+
+
+@pytest.mark.parametrize("variant,law", [("k1", 0), ("k31", 0), ("k31", 2)])
+def test_mixed_matches_fp64_300_steps(variant, law):
+    x0, tri = synth.disk_mesh(3000, seed=31)
+    p = _law(default_params(variant), law)
+    st = synth.initial_state(x0)
+    out = {}
+    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+        e = capi.Engine(prec)
+        h = e.add_cell(x0, tri, p, state=st)
+        e.step(300, 5e-5)
+        out[prec] = h.get_state()
+        assert h.status() == 0
+        e.close()
+    u = out[capi.PREC_FP64][0] - x0
+    err = np.max(np.abs(out[capi.PREC_MIXED][0] - out[capi.PREC_FP64][0])) / np.max(np.abs(u))
+    assert np.max(np.abs(u)) > 0
+    assert err <= MIXED_TOL, err
+
+
+def test_mixed_moving_state_matches_fp64():
+    """From a moving, pre-strained state (strain ~1e-2, bonds formed)."""
+    x0, tri = synth.disk_mesh(2000, seed=32)
+    p = default_params("k1")
+    st = synth.initial_state(x0, perturb=1.0, seed=4)
+    out = {}
+    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+        e = capi.Engine(prec)
+        h = e.add_cell(x0, tri, p, state=st, t=0.3)
+        e.step(100, 5e-5)
+        out[prec] = h.get_state()
+        e.close()
+    u = out[capi.PREC_FP64][0] - st[0]
+    err = np.max(np.abs(out[capi.PREC_MIXED][0] - out[capi.PREC_FP64][0])) / np.max(np.abs(u))
+    assert err <= MIXED_TOL, err
+
+
+def test_mixed_batched_equals_alone():
+    sizes = [700, 2500, 180]
+    cells = []
+    for i, n in enumerate(sizes):
+        x0, tri = synth.disk_mesh(n, seed=200 + i)
+        p = _law(default_params(["k1", "k31", "k31"][i]), [0, 0, 2][i])
+        p.stream = i
+        cells.append((x0, tri, p))
+    eb = capi.Engine(capi.PREC_MIXED)
+    hs = [eb.add_cell(x, t, p, state=synth.initial_state(x)) for x, t, p in cells]
+    eb.step(40, 5e-5)
+    batched = [h.get_state() for h in hs]
+    eb.close()
+    for (x, t, p), b in zip(cells, batched):
+        ea = capi.Engine(capi.PREC_MIXED)
+        h = ea.add_cell(x, t, p, state=synth.initial_state(x))
+        ea.step(40, 5e-5)
+        for u, w in zip(b, h.get_state()):
+            assert np.array_equal(u, w)
+        ea.close()
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
+def test_exchange_path_equals_internal_steps(prec):
+    """wcfe_engine_predict / wcfe_engine_update with the host returning the predicted
+    positions unchanged is the same computation as wcfe_engine_step: bit-identical."""
+    cells = [synth.disk_mesh(n, seed=300 + n) for n in (400, 1300)]
+    res = []
+    for mode in ("internal", "exchange"):
+        e = capi.Engine(prec)
+        hs = []
+        for i, (x0, tri) in enumerate(cells):
+            p = default_params("k31")
+            p.stream = i
+            hs.append(e.add_cell(x0, tri, p, state=synth.initial_state(x0, perturb=1.0, seed=i)))
+        if mode == "internal":
+            e.step(15, 5e-5)
+        else:
+            buf = np.zeros((e.total_vertices(), 3))
+            for _ in range(15):
+                e.predict_all(5e-5, buf)
+                e.update_all(5e-5, 5e-5, buf)
+            e.sync()
+        res.append([h.get_state() for h in hs])
+        e.close()
+    for a, b in zip(*res):
+        for u, w in zip(a, b):
+            assert np.array_equal(u, w)
+
+
+def test_integrin_density_mask():
+    """Per-vertex integrin density: zero density removes the integrin force exactly;
+    uniform rho_i_max reproduces the default."""
+    x0, tri = synth.disk_mesh(900, seed=5)
+    p = default_params("k1")
+    st = synth.initial_state(x0, perturb=1.0, seed=5)
+    outs = []
+    for rho in (None, np.full(len(x0), 100.0)):
+        e = capi.Engine(capi.PREC_FP64)
+        h = e.add_cell(x0, tri, p, state=st)
+        if rho is not None:
+            h.set_integrins(rho)
+        e.step(5, 5e-5)
+        outs.append(h.get_state())
+        e.close()
+    for u, w in zip(*outs):
+        assert np.array_equal(u, w)
+    e = capi.Engine(capi.PREC_FP64)
+    h = e.add_cell(x0, tri, p, state=st)
+    h.set_integrins(np.zeros(len(x0)))
+    F = h.eval_forces(st[0], 5e-5)[0]
+    assert np.all(F == 0)
+    e.close()

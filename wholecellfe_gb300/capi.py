@@ -1,0 +1,332 @@
+"""Python mirror of the C ABI (include/wcfe.h) over ctypes.
+
+This is host-side plumbing for tests, the benchmark and Python callers; the
+compute path is the sm_103a library ``libwcfe.so`` built in-tree by
+``wholecellfe_gb300/build.py``.  There is no CPU fallback: if the library is
+missing or no CUDA device is visible, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .params import Params
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libwcfe.so")
+
+_d = C.POINTER(C.c_double)
+_i = C.POINTER(C.c_int32)
+_u8 = C.POINTER(C.c_uint8)
+PREC_FP64, PREC_MIXED = 0, 1
+
+# exported symbols and their signatures (checked against include/wcfe.h by the tests)
+SIGNATURES = {
+    "wcfe_params_default": (None, [C.POINTER(Params), C.c_int32]),
+    "wcfe_last_error": (C.c_char_p, []),
+    "wcfe_ap_draw": (C.c_uint32, [C.c_uint32, C.c_uint32, C.c_uint64, C.c_uint32]),
+    "wcfe_philox4x32_10": (None, [C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
+    "wcfe_engine_create": (C.c_int, [C.c_int32, C.c_int32, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "wcfe_engine_destroy": (C.c_int, [C.c_void_p]),
+    "wcfe_engine_precision": (C.c_int, [C.c_void_p]),
+    "wcfe_engine_free_bytes": (C.c_uint64, [C.c_void_p]),
+    "wcfe_cell_bytes": (C.c_uint64, [C.c_int32, C.c_int32]),
+    "wcfe_engine_sync": (C.c_int, [C.c_void_p]),
+    "wcfe_cell_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _i, _i, _i, _u8, C.POINTER(Params),
+                                   C.POINTER(C.c_int32)]),
+    "wcfe_cell_destroy": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_cell_set_params": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(Params)]),
+    "wcfe_cell_set_topology": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _i, _i, _i, _u8]),
+    "wcfe_cell_set_substrate": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _i, _d, _d]),
+    "wcfe_cell_set_state": (C.c_int, [C.c_void_p, C.c_int32, _d, _d, _d, _d, _d, _d, _d]),
+    "wcfe_cell_get_state": (C.c_int, [C.c_void_p, C.c_int32, _d, _d, _d, _d, _d, _d, _d]),
+    "wcfe_cell_set_clock": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_uint64]),
+    "wcfe_cell_get_clock": (C.c_int, [C.c_void_p, C.c_int32, _d, C.POINTER(C.c_uint64)]),
+    "wcfe_cell_status": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_uint32)]),
+    "wcfe_cell_sizes": (C.c_int, [C.c_void_p, C.c_int32, _i, _i, _i, _i]),
+    "wcfe_cell_predict": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _d, _d]),
+    "wcfe_cell_update_fa": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _d, _d, _d, _d]),
+    "wcfe_cell_update_forces": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_double]),
+    "wcfe_cell_eval_residual": (C.c_int, [C.c_void_p, C.c_int32, _d, _d, C.c_double, _d, C.c_double, _d, _d, _d,
+                                          _d, _d]),
+    "wcfe_cell_eval_forces": (C.c_int, [C.c_void_p, C.c_int32, _d, C.c_double, _d, _d, _d, _d, _d]),
+    "wcfe_engine_step": (C.c_int, [C.c_void_p, C.c_int32, C.c_double]),
+    "wcfe_engine_step_cells": (C.c_int, [C.c_void_p, _i, C.c_int32, C.c_int32, C.c_double]),
+    "wcfe_engine_set_graphs": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_engine_set_shape": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "wcfe_engine_get_shape": (C.c_int, [C.c_void_p, _i, _i]),
+    "wcfe_engine_autotune": (C.c_int, [C.c_void_p, C.c_double, C.c_int32]),
+    "wcfe_engine_last_timing": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
+    "wcfe_engine_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_engine_launches": (C.c_uint64, [C.c_void_p]),
+    "wcfe_engine_step_times": (C.c_int64, [C.c_void_p, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float)]),
+    "wcfe_engine_total_vertices": (C.c_int64, [C.c_void_p]),
+    "wcfe_engine_predict": (C.c_int, [C.c_void_p, C.c_double, _d]),
+    "wcfe_engine_update": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _d]),
+    "wcfe_cell_set_integrins": (C.c_int, [C.c_void_p, C.c_int32, _d]),
+    "wcfe_server_create": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_void_p)]),
+    "wcfe_server_destroy": (C.c_int, [C.c_void_p]),
+    "wcfe_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
+    "wcfe_server_iterate": (C.c_int, [C.c_void_p, _i, _i]),
+    "wcfe_server_result": (C.c_int, [C.c_void_p, C.c_int64, _d, _d]),
+    "wcfe_server_step_times": (C.c_int64, [C.c_void_p, _d, C.c_int64]),
+    "wcfe_debug_topology": (C.c_int, [C.c_int32, C.c_int32, _i, _i, _i, _u8, C.c_int32, _i, _i, _i, _i, C.c_int32, _i,
+                                      _i, C.c_int32, _i, C.c_int32, C.POINTER(C.c_uint16)]),
+}
+
+
+def debug_topology(tri, n_vert, emax=320, vt_ptr=None, vt_idx=None, bnd=None):
+    """The engine's host preprocessing (boundary candidates, patches, slot codes); no device needed."""
+    tri = i32(tri)
+    nt = len(tri)
+    nb = C.c_int32()
+    npatch = C.c_int32()
+    rank = np.zeros(n_vert, np.int32)
+    cptr = np.zeros(n_vert + 1, np.int32)
+    cand = np.zeros(2 * 12 * n_vert + 16, np.int32)
+    patch = np.zeros(4 * n_vert + 16, np.int32)
+    elems = np.zeros(6 * nt + 16, np.int32)
+    codes = np.zeros(3 * nt, np.uint16)
+    check(load().wcfe_debug_topology(n_vert, nt, ip(tri), ip(None if vt_ptr is None else i32(vt_ptr)),
+                                     ip(None if vt_idx is None else i32(vt_idx)),
+                                     None if bnd is None else np.ascontiguousarray(bnd, np.uint8).ctypes.data_as(_u8),
+                                     emax, C.byref(nb), ip(rank), ip(cptr), ip(cand), len(cand), C.byref(npatch),
+                                     ip(patch), len(patch), ip(elems), len(elems),
+                                     codes.ctypes.data_as(C.POINTER(C.c_uint16))), "wcfe_debug_topology")
+    nbv, npv = nb.value, npatch.value
+    cptr = cptr[:nbv + 1]
+    patch = patch[:4 * npv].reshape(npv, 4)
+    return dict(nb=nbv, rank=rank, cptr=cptr, cand=cand[:2 * cptr[-1]].reshape(-1, 2), np=npv, patch=patch,
+                elems=elems[:patch[:, 3].sum()], codes=codes)
+
+
+class WcfeError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libwcfe.so (raises when it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise WcfeError(f"{path} is missing: build it with wholecellfe_gb300/build.py (no CPU fallback exists)")
+        lib = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def check(rc: int, what: str = ""):
+    if rc != 0:
+        msg = load().wcfe_last_error().decode()
+        raise WcfeError(f"{what} failed with status {rc}: {msg}")
+
+
+def dp(a):
+    return None if a is None else a.ctypes.data_as(_d)
+
+
+def ip(a):
+    return None if a is None else a.ctypes.data_as(_i)
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Request(C.Structure):
+    _fields_ = [("n_vert", C.c_int32), ("n_tri", C.c_int32), ("tri", _i), ("x", _d), ("params", C.POINTER(Params)),
+                ("n_steps", C.c_int32), ("sub_tri", _i), ("sub_X", _d), ("sub_n_vert", C.c_int32),
+                ("sub_n_tri", C.c_int32)]
+
+
+class Engine:
+    """One device, one stream, many cells (wcfe_engine)."""
+
+    def __init__(self, precision: int = PREC_FP64, device: int = 0, budget_bytes: int = 0):
+        L = load()
+        h = C.c_void_p()
+        check(L.wcfe_engine_create(device, precision, budget_bytes, C.byref(h)), "wcfe_engine_create")
+        self.h = h
+        self.precision = precision
+        self.cells: dict[int, "Cell"] = {}
+
+    def close(self):
+        if self.h:
+            load().wcfe_engine_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_cell(self, x, tri, params: Params, vt_ptr=None, vt_idx=None, bnd=None, state=None, t=0.0, ap_calls=0,
+                 substrate=None) -> "Cell":
+        tri = i32(tri)
+        n = len(x)
+        cid = C.c_int32()
+        check(load().wcfe_cell_create(self.h, n, len(tri), ip(tri), ip(None if vt_ptr is None else i32(vt_ptr)),
+                                      ip(None if vt_idx is None else i32(vt_idx)),
+                                      None if bnd is None else np.ascontiguousarray(bnd, np.uint8).ctypes.data_as(_u8),
+                                      C.byref(params), C.byref(cid)), "wcfe_cell_create")
+        c = Cell(self, cid.value, n, len(tri))
+        if state is None:
+            c.set_state(x=x)
+        else:
+            c.set_state(*state)
+        c.set_clock(t, ap_calls)
+        if substrate is not None:
+            c.set_substrate(*substrate)
+        self.cells[c.id] = c
+        return c
+
+    def step(self, nsteps: int, dt: float):
+        check(load().wcfe_engine_step(self.h, nsteps, dt), "wcfe_engine_step")
+
+    def step_cells(self, cells, nsteps: int, dt: float):
+        ids = i32([c.id for c in cells])
+        check(load().wcfe_engine_step_cells(self.h, ip(ids), len(ids), nsteps, dt), "wcfe_engine_step_cells")
+
+    def sync(self):
+        check(load().wcfe_engine_sync(self.h), "wcfe_engine_sync")
+
+    def set_graphs(self, on: bool):
+        check(load().wcfe_engine_set_graphs(self.h, int(on)), "wcfe_engine_set_graphs")
+
+    def set_timing(self, on: bool):
+        check(load().wcfe_engine_set_timing(self.h, int(on)), "wcfe_engine_set_timing")
+
+    def last_timing(self):
+        a, b = C.c_float(), C.c_float()
+        check(load().wcfe_engine_last_timing(self.h, C.byref(a), C.byref(b)), "wcfe_engine_last_timing")
+        return a.value, b.value
+
+    def step_times(self):
+        """(per-step device ms list, span ms) of the last timed step() call."""
+        n = load().wcfe_engine_step_times(self.h, None, 0, None)
+        buf = (C.c_float * max(n, 1))()
+        span = C.c_float()
+        load().wcfe_engine_step_times(self.h, buf, n, C.byref(span))
+        return list(buf)[:n], span.value
+
+    def set_shape(self, threads: int, emax: int):
+        check(load().wcfe_engine_set_shape(self.h, threads, emax), "wcfe_engine_set_shape")
+
+    def shape(self):
+        a, b = C.c_int32(), C.c_int32()
+        check(load().wcfe_engine_get_shape(self.h, C.byref(a), C.byref(b)), "wcfe_engine_get_shape")
+        return a.value, b.value
+
+    def autotune(self, dt: float, reps: int = 3):
+        check(load().wcfe_engine_autotune(self.h, dt, reps), "wcfe_engine_autotune")
+
+    def launches(self) -> int:
+        return int(load().wcfe_engine_launches(self.h))
+
+    def total_vertices(self) -> int:
+        return int(load().wcfe_engine_total_vertices(self.h))
+
+    def predict_all(self, dt: float, x_pred: np.ndarray):
+        check(load().wcfe_engine_predict(self.h, dt, dp(x_pred)), "wcfe_engine_predict")
+
+    def update_all(self, dt: float, dt_real: float, x_new: np.ndarray):
+        check(load().wcfe_engine_update(self.h, dt, dt_real, dp(x_new)), "wcfe_engine_update")
+
+    def free_bytes(self) -> int:
+        return int(load().wcfe_engine_free_bytes(self.h))
+
+
+class Cell:
+    def __init__(self, eng: Engine, cid: int, n: int, nt: int):
+        self.eng, self.id, self.n, self.nt = eng, cid, n, nt
+
+    def destroy(self):
+        check(load().wcfe_cell_destroy(self.eng.h, self.id), "wcfe_cell_destroy")
+        self.eng.cells.pop(self.id, None)
+
+    def set_state(self, x=None, V=None, A=None, ea=None, cA=None, cC=None, fau=None):
+        arrs = [None if a is None else f64(a) for a in (x, V, A, ea, cA, cC, fau)]
+        check(load().wcfe_cell_set_state(self.eng.h, self.id, *[dp(a) for a in arrs]), "wcfe_cell_set_state")
+
+    def get_state(self):
+        n = self.n
+        out = [np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 3)), np.zeros((n, 6)), np.zeros(n), np.zeros(n),
+               np.zeros((n, 3))]
+        check(load().wcfe_cell_get_state(self.eng.h, self.id, *[dp(a) for a in out]), "wcfe_cell_get_state")
+        return tuple(out)
+
+    def set_params(self, p: Params):
+        check(load().wcfe_cell_set_params(self.eng.h, self.id, C.byref(p)), "wcfe_cell_set_params")
+
+    def set_integrins(self, rho):
+        check(load().wcfe_cell_set_integrins(self.eng.h, self.id, dp(None if rho is None else f64(rho))),
+              "wcfe_cell_set_integrins")
+
+    def set_clock(self, t: float, ap_calls: int):
+        check(load().wcfe_cell_set_clock(self.eng.h, self.id, t, ap_calls), "wcfe_cell_set_clock")
+
+    def clock(self):
+        t = C.c_double()
+        k = C.c_uint64()
+        check(load().wcfe_cell_get_clock(self.eng.h, self.id, C.byref(t), C.byref(k)), "wcfe_cell_get_clock")
+        return t.value, k.value
+
+    def status(self) -> int:
+        s = C.c_uint32()
+        check(load().wcfe_cell_status(self.eng.h, self.id, C.byref(s)), "wcfe_cell_status")
+        return s.value
+
+    def sizes(self):
+        v = [C.c_int32() for _ in range(4)]
+        check(load().wcfe_cell_sizes(self.eng.h, self.id, *[C.byref(a) for a in v]), "wcfe_cell_sizes")
+        return tuple(a.value for a in v)
+
+    def set_substrate(self, Xs, tri_s, xs=None):
+        tri_s = i32(tri_s)
+        Xs = f64(Xs)
+        check(load().wcfe_cell_set_substrate(self.eng.h, self.id, len(Xs), len(tri_s), ip(tri_s), dp(Xs),
+                                             dp(None if xs is None else f64(xs))), "wcfe_cell_set_substrate")
+
+    # drop-in pieces
+    def predict(self, dt: float):
+        xp = np.zeros((self.n, 3))
+        vh = np.zeros((self.n, 3))
+        check(load().wcfe_cell_predict(self.eng.h, self.id, dt, dp(xp), dp(vh)), "wcfe_cell_predict")
+        return vh, xp
+
+    def update_fa(self, dt_real: float, x_new, X=None, Xs=None, xs=None):
+        check(load().wcfe_cell_update_fa(self.eng.h, self.id, dt_real, dp(None if X is None else f64(X)),
+                                         dp(f64(x_new)), dp(None if Xs is None else f64(Xs)),
+                                         dp(None if xs is None else f64(xs))), "wcfe_cell_update_fa")
+
+    def update_forces(self, dt: float, dt_real: float, t_tot: float):
+        check(load().wcfe_cell_update_forces(self.eng.h, self.id, dt, dt_real, t_tot), "wcfe_cell_update_forces")
+
+    def eval_residual(self, X, x_new, dt_real, centroid, t_tot):
+        n = self.n
+        out = [np.zeros((n, 3)), np.zeros((n, 6)), np.zeros(n), np.zeros(n), np.zeros(n)]
+        cen = f64(centroid)
+        check(load().wcfe_cell_eval_residual(self.eng.h, self.id, dp(f64(X)), dp(f64(x_new)), dt_real, dp(cen), t_tot,
+                                             *[dp(a) for a in out]), "wcfe_cell_eval_residual")
+        return tuple(out)
+
+    def eval_forces(self, x, dt_real):
+        n = self.n
+        out = [np.zeros((n, 3)) for _ in range(4)] + [np.zeros(4)]
+        check(load().wcfe_cell_eval_forces(self.eng.h, self.id, dp(f64(x)), dt_real, *[dp(a) for a in out]),
+              "wcfe_cell_eval_forces")
+        return tuple(out)

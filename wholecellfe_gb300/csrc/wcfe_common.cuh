@@ -1,0 +1,142 @@
+// wcfe_common.cuh — device helpers shared by the FP64 and mixed-precision kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "wcfe_device.cuh"
+
+namespace wcfe {
+
+// ---------------------------------------------------------------------------
+// unfused arithmetic for reproduced decisions
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double xm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xa(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double xs(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double xnorm3(double x, double y, double z) {
+    return __dsqrt_rn(xa(xa(xm(x, x), xm(y, y)), xm(z, z)));
+}
+
+__device__ __forceinline__ double4 ld4(const double4* p) {
+    double4 r;
+    const double2* q = reinterpret_cast<const double2*>(p);
+    double2 a = __ldg(q), b = __ldg(q + 1);
+    r.x = a.x; r.y = a.y; r.z = b.x; r.w = b.y;
+    return r;
+}
+__device__ __forceinline__ double4 ld4v(const double4* p) {  // plain (coherent) load for data written this launch
+    const double2* q = reinterpret_cast<const double2*>(p);
+    double2 a = q[0], b = q[1];
+    return make_double4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ void st4(double4* p, double x, double y, double z) {
+    double2* q = reinterpret_cast<double2*>(p);
+    q[0] = make_double2(x, y);
+    q[1] = make_double2(z, 0.0);
+}
+
+// predicted velocity and position, bit-identical wherever they are recomputed
+__device__ __forceinline__ void predict_vertex(const double4& x, const double4& V, const double4& A, double dt,
+                                               double hdt, double vh[3], double xn[3]) {
+    vh[0] = xa(V.x, xm(hdt, A.x));
+    vh[1] = xa(V.y, xm(hdt, A.y));
+    vh[2] = 0.0;
+    xn[0] = xa(x.x, xm(dt, vh[0]));
+    xn[1] = xa(x.y, xm(dt, vh[1]));
+    xn[2] = xa(x.z, xm(dt, vh[2]));
+}
+
+// MD force-extension fit, UL:1203-1214
+static __constant__ double c_md_px[6] = {0., 2.51250583e-03, 4.40265201e-03, 5.91408228e-03, 11.76817302e-03, 17.001e-03};
+static __constant__ double c_md_py[6] = {-7.15514497, 71.80501308, 356.62420075, 356.96656556, 126.21811585, 528.40481124};
+static __constant__ double c_md_k[6] = {31426.8556, 99485.86235, 67080.67086, -7908.39043, 21978.66923, 76858.39733};
+
+// Spring force vector of bond u and the Bell force magnitude (UL:1245-1264, :2112-2137; k1 :1259, :2077)
+__device__ __forceinline__ void spring_force(const wcfe_params& p, double ux, double uy, double uz, double fs[3],
+                                             double* bell) {
+    double D = xnorm3(ux, uy, uz);
+    if (p.force_law == WCFE_LAW_LINEAR && p.rest_len == 0.0) {
+        fs[0] = p.k_lin * ux; fs[1] = p.k_lin * uy; fs[2] = p.k_lin * uz;
+        *bell = p.linear_norm2d ? p.k_lin * __dsqrt_rn(xa(xm(ux, ux), xm(uy, uy))) : p.k_lin * D;
+        return;
+    }
+    double dx = 0, dy = 0, dz = 0;
+    if (D != 0) { dx = ux / D; dy = uy / D; dz = uz / D; }
+    double mag = 0.0;
+    if (p.force_law == WCFE_LAW_MD_TABLE) {
+        int j = -1;
+        if (D >= c_md_px[5]) j = 5;
+        else {
+#pragma unroll
+            for (int q = 0; q < 5; ++q)
+                if (D < c_md_px[q + 1] && D >= c_md_px[q]) j = q;
+        }
+        if (j >= 0) mag = c_md_py[j] + c_md_k[j] * xs(D, c_md_px[j]);
+    } else if (p.force_law == WCFE_LAW_LINEAR) {
+        mag = p.k_lin * (D - p.rest_len);
+    } else {
+        double e = D - p.rest_len;
+        mag = p.poly_k0 * (e + e * e * e / (3.0 * p.poly_x0 * p.poly_x0));
+    }
+    fs[0] = mag * dx; fs[1] = mag * dy; fs[2] = mag * dz;
+    if (p.force_law == WCFE_LAW_LINEAR && p.linear_norm2d) {
+        double D2 = __dsqrt_rn(xa(xm(ux, ux), xm(uy, uy)));
+        *bell = fabs(p.k_lin * (D2 - p.rest_len));
+    } else {
+        *bell = sqrt(fs[0] * fs[0] + fs[1] * fs[1] + fs[2] * fs[2]);
+    }
+}
+
+// Point location in the substrate (UL:2061-2100): the last containing triangle wins.
+__device__ __forceinline__ int locate(const SubDev& s, double px, double py, double pz, double w[3]) {
+    int gx = (int)floor((px - s.ox) * s.inv_h), gy = (int)floor((py - s.oy) * s.inv_h);
+    if (!(gx >= 0 && gx < s.gx && gy >= 0 && gy < s.gy)) return -1;
+    int g = gy * s.gx + gx;
+    int found = -1;
+    for (int k = s.cell_ptr[g]; k < s.cell_ptr[g + 1]; ++k) {
+        int e = s.cell_tri[k];
+        int4 t = s.tri[e];
+        double4 p1 = ld4(s.X + t.x), p2 = ld4(s.X + t.y), p3 = ld4(s.X + t.z);
+        double e1x = xs(p2.x, p1.x), e1y = xs(p2.y, p1.y), e1z = xs(p2.z, p1.z);
+        double e2x = xs(p3.x, p1.x), e2y = xs(p3.y, p1.y), e2z = xs(p3.z, p1.z);
+        double nx = xs(xm(e1y, e2z), xm(e1z, e2y)), ny = xs(xm(e1z, e2x), xm(e1x, e2z)), nz = xs(xm(e1x, e2y), xm(e1y, e2x));
+        double At = xm(0.5, xnorm3(nx, ny, nz));
+        double epx = xs(px, p1.x), epy = xs(py, p1.y), epz = xs(pz, p1.z);
+        double ax = xs(xm(e1y, epz), xm(e1z, epy)), ay = xs(xm(e1z, epx), xm(e1x, epz)), az = xs(xm(e1x, epy), xm(e1y, epx));
+        double A3 = -1;
+        if (az >= 0) A3 = xm(0.5, xnorm3(ax, ay, az));
+        double bx = xs(xm(epy, e2z), xm(epz, e2y)), by = xs(xm(epz, e2x), xm(epx, e2z)), bz = xs(xm(epx, e2y), xm(epy, e2x));
+        double A2 = -1;
+        if (bz >= 0) A2 = xm(0.5, xnorm3(bx, by, bz));
+        double A1 = xs(xs(At, A2), A3);
+        if (A1 >= 0 && A2 >= 0 && A3 >= 0) {
+            found = e;
+            w[0] = A1 / At; w[1] = A2 / At; w[2] = A3 / At;
+        }
+    }
+    return found;
+}
+
+// boundary neighbours and outward normal (UL:1489-1543)
+__device__ __forceinline__ bool boundary_frame(const CellDev& c, const double4* __restrict__ xp, int rank,
+                                               const double xi[3], double x1[3], double x2[3]) {
+    int j1 = -1, j2 = -1;
+    for (int k = c.bnd_cptr[rank]; k < c.bnd_cptr[rank + 1]; ++k) {
+        int2 cd = c.bnd_cand[k];
+        double4 pb = ld4v(xp + cd.x), pi = ld4v(xp + cd.y);
+        double d1x = xs(xi[0], pb.x), d1y = xs(xi[1], pb.y);
+        double d2x = xs(pi.x, xi[0]), d2y = xs(pi.y, xi[1]);
+        double ncz = xs(xm(d1x, d2y), xm(d1y, d2x));
+        if (ncz > 0) j1 = cd.x;
+        else j2 = cd.x;
+    }
+    if (j1 < 0 || j2 < 0) return false;
+    double4 a = ld4v(xp + j1), bq = ld4v(xp + j2);
+    x1[0] = a.x; x1[1] = a.y; x1[2] = a.z;
+    x2[0] = bq.x; x2[1] = bq.y; x2[2] = bq.z;
+    return true;
+}
+
+}  // namespace wcfe

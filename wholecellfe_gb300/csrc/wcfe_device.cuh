@@ -1,0 +1,101 @@
+// wcfe_device.cuh — device-side data layout and math of the per-step
+// mechanics (sm_103a).  Shared by the kernels (wcfe_kernels.cu) and by the host
+// engine (wcfe_engine.cu) for the layout structs.
+//
+// Layout in HBM, per cell (one arena block per cell, 256-B aligned arrays):
+//   pos[2][nv]   double4 (x, y, z, 0)  ping-pong: pos[par] = X (step start), pos[par^1] = x (step end)
+//   vel, acc, vhl [nv] double4         V, A, and V_hlf of the last drop-in predict
+//   ea[2][nv][6] double                ping-pong Euler-Almansi strain (Voigt xx yy zz xy xz yz)
+//   cA, cC [nv] double, fau [nv] double4
+//   tri [nt] int4 (a, b, c, 0); vt_ptr [nv+1], vc_code [3nt] uint16 one-ring in mesh order
+//   patches: patch [np] int4 (v0, nv, e0, ne), patch_elems [sum ne] int32
+//   boundary: bnd_rank [nv] int32 (-1 interior), bnd_cptr [nb+1], bnd_cand [..] int2 (nj, nint)
+//   k1_part [nk1][4] double: per-block partial sums of area and area-weighted centroid
+#pragma once
+#include <cstdint>
+
+#include "../../include/wcfe.h"
+
+namespace wcfe {
+
+constexpr int kVB = 256;        // vertices per vertex-phase block
+constexpr int kEB = 512;        // elements per vertex-phase block
+constexpr int kK1Threads = 256;
+
+struct SubDev {                 // substrate mesh + uniform grid for point location
+    int32_t nv, nt;
+    const double4* X;           // previous positions (point location)
+    const double4* x;           // current positions (displacement interpolation)
+    const int4* tri;
+    const int32_t* cell_ptr;    // [gx*gy+1]
+    const int32_t* cell_tri;    // triangle ids, ascending within a grid cell
+    double ox, oy, inv_h;
+    int32_t gx, gy;
+    int32_t moving;             // 0: x == X (rigid), the interpolated displacement is exactly 0
+};
+
+struct CellDev {
+    int32_t nv, nt, nb, np, nk1;
+    int32_t has_sub;
+    int64_t hoff;               // first vertex of this cell in the engine's packed host exchange arrays
+    double4* pos[2];
+    double4* vel;
+    double4* acc;
+    double4* vhl;
+    double* ea[2];
+    double* cA;
+    double* cC;
+    double4* fau;
+    const double* rho_w;        // optional per-vertex integrin density (nullptr: rho_i_max)
+    const int4* tri;
+    const int32_t* vt_ptr;
+    const uint16_t* vc_code;    // (slot << 2) | corner, slot local to the owner's patch
+    const int4* patch;
+    const int32_t* patch_elems;
+    const int32_t* bnd_rank;
+    const int32_t* bnd_cptr;
+    const int2* bnd_cand;
+    double* k1_part;
+    float4* rec;                // mixed form: per-vertex FP32 element inputs [nv][4] (see wcfe_mixed.cu)
+    // control words, advanced by the last patch-phase CTA of the cell to finish a step:
+    int32_t* ctl;               // [0] parity (which pos/ea buffer holds the step-start state), [1] CTA ticket
+    double* clk;                // [0] simulation time at the start of the next step
+    unsigned long long* ap;     // [0] calculateForce_AP calls made (the AP counter of the next step)
+    uint32_t* status;
+    double ap_thresh;           // ap_rate dt exp(-ap_rate dt) for the engine's current dt (UL:1552)
+    SubDev sub;
+    wcfe_params prm;
+};
+
+struct WorkItem {               // one block of a phase: (cell index into the table, block/patch index)
+    int32_t cell, idx;
+};
+
+// Philox4x32-10, Salmon et al. SC'11 (the counter-based stream of include/wcfe.h)
+__host__ __device__ inline void philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3], k0 = key[0], k1 = key[1];
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+        uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+#else
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0, hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+#endif
+        uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+        k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+__host__ __device__ inline uint32_t ap_draw(uint32_t seed, uint32_t stream, unsigned long long call, uint32_t k) {
+    uint32_t ctr[4] = {k, (uint32_t)call, (uint32_t)(call >> 32), 0u};
+    uint32_t key[2] = {seed, stream};
+    uint32_t o[4];
+    philox4x32_10(ctr, key, o);
+    return o[0] >> 1;
+}
+
+}  // namespace wcfe

@@ -1,0 +1,1232 @@
+// wcfe_engine.cu — host engine behind the C ABI (include/wcfe.h): cells in
+// HBM, batched work lists, CUDA-graph replay, the shape autotuner and the
+// serving loop.  Single device, one stream per engine.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <limits>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/wcfe.h"
+#include "wcfe_device.cuh"
+#include "wcfe_topology.h"
+
+namespace wcfe {
+struct PatchArgs;
+void launch_vertex_phase(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
+                         cudaStream_t st, const double* stage_in = nullptr, double* stage_out = nullptr);
+void launch_predict(const CellDev* cells, int cell, double dt, double* xout, double* vhout, int nv, cudaStream_t st);
+cudaError_t configure_kernels(size_t max_smem);
+size_t patch_smem_bytes(int prec, int mode, int emax);
+int patch_occupancy(int prec, int threads, size_t smem);
+int vertex_occupancy();
+bool mixed_available();
+void launch_patch(int prec, int mode, const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt,
+                  double dt_real, double ap_thresh, double t_override, int vh_from_buf, const double* centroid_dev,
+                  double* o0, double* o1, double* o2, double* o3, double* o4, int threads, int grid, cudaStream_t st);
+}  // namespace wcfe
+
+using namespace wcfe;
+
+namespace {
+
+enum { VP_PREDICT = 1, VP_UPDATE_FA = 2, VP_RECORD = 4, VP_EXPORT = 8, VP_IMPORT = 16, VP_NOAREA = 32 };
+enum { PP_STEP = 0, PP_RESIDUAL = 1, PP_FORCES = 2 };
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
+
+thread_local std::string g_last_error;
+#define CK(call)                                                                                        \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess) {                                                                        \
+            g_last_error = std::string(#call) + ": " + cudaGetErrorString(e_);                          \
+            return WCFE_ERR_CUDA;                                                                       \
+        }                                                                                               \
+    } while (0)
+
+double ap_threshold(const wcfe_params& p, double dt_real) { return p.ap_rate * dt_real * std::exp(-p.ap_rate * dt_real); }
+
+// ---------------------------------------------------------------------------
+struct Cell {
+    int32_t id = -1;
+    Topology topo;
+    Patches patches;
+    wcfe_params prm{};
+    // device memory
+    void* state_block = nullptr;
+    size_t state_bytes = 0;
+    void* patch_block = nullptr;
+    size_t patch_bytes = 0;
+    void* sub_block = nullptr;
+    size_t sub_bytes = 0;
+    double* rho_dev = nullptr;
+    CellDev dev{};
+    int32_t sub_nv = 0, sub_nt = 0;
+    std::vector<int32_t> sub_tri;
+    std::vector<double> sub_X, sub_x;
+    bool sub_moving = false;
+};
+
+struct Graph {
+    cudaGraphExec_t exec = nullptr;
+    double dt = 0;
+    int steps = 0;
+    uint64_t version = 0;
+};
+
+}  // namespace
+
+struct wcfe_engine {
+    int device = 0;
+    int prec = WCFE_PREC_FP64;
+    uint64_t budget = 0;
+    uint64_t used = 0;
+    cudaStream_t stream = nullptr;
+    int num_sms = 0;
+    std::map<int32_t, std::unique_ptr<Cell>> cells;
+    int32_t next_id = 0;
+    // batched tables
+    uint64_t version = 1;         // bumps on any change of the live set / topology / params
+    uint64_t table_version = 0;
+    double table_dt = -1.0;       // dt the per-cell AP thresholds in the table were computed for
+    std::vector<int32_t> order;   // table index -> cell id
+    std::vector<CellDev> table;
+    std::vector<WorkItem> k1, k2;
+    int64_t total_nv = 0;         // vertices of all live cells (packed exchange arrays)
+    double* d_xchg = nullptr;     // packed [total_nv][3] exchange buffer on the device
+    size_t d_xchg_cap = 0;
+    CellDev* d_table = nullptr;
+    size_t d_table_cap = 0;
+    WorkItem* d_k1 = nullptr;
+    size_t d_k1_cap = 0;
+    WorkItem* d_k2 = nullptr;
+    size_t d_k2_cap = 0;
+    // per-cell single-cell work lists for the drop-in calls (rebuilt on demand)
+    WorkItem* d_one = nullptr;
+    size_t d_one_cap = 0;
+    // staging
+    double* d_stage = nullptr;
+    size_t d_stage_cap = 0;
+    void* h_stage = nullptr;
+    size_t h_stage_cap = 0;
+    // shapes
+    int patch_threads = 128;
+    int patch_emax = 320;
+    bool tuned = false;
+    // graphs
+    bool use_graphs = false;
+    Graph graph;
+    // timing
+    bool timing = false;
+    cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+    std::vector<cudaEvent_t> tev;  // per-step events of the last timed wcfe_engine_step: 3 per step
+    int timed_steps = 0;
+    float ms_v = 0, ms_p = 0, ms_span = 0;
+    std::vector<float> step_ms;
+    uint64_t launches = 0;
+};
+
+namespace {
+
+int fail(const std::string& msg, int code) {
+    g_last_error = msg;
+    return code;
+}
+
+Cell* find(wcfe_engine* e, int32_t id) {
+    auto it = e->cells.find(id);
+    return it == e->cells.end() ? nullptr : it->second.get();
+}
+
+// ---- device memory of a cell -------------------------------------------------
+size_t state_layout(int32_t nv, int32_t nt, int32_t nb, int32_t ncand, int32_t nk1, bool rec, size_t* off /* 24 */) {
+    size_t o = 0;
+    int i = 0;
+    auto put = [&](size_t bytes) { off[i++] = o; o = align_up(o + bytes); };
+    put(sizeof(double4) * nv);   // 0 pos0
+    put(sizeof(double4) * nv);   // 1 pos1
+    put(sizeof(double4) * nv);   // 2 vel
+    put(sizeof(double4) * nv);   // 3 acc
+    put(sizeof(double4) * nv);   // 4 vhl
+    put(sizeof(double) * 6 * nv);  // 5 ea0
+    put(sizeof(double) * 6 * nv);  // 6 ea1
+    put(sizeof(double) * nv);    // 7 cA
+    put(sizeof(double) * nv);    // 8 cC
+    put(sizeof(double4) * nv);   // 9 fau
+    put(sizeof(int4) * nt);      // 10 tri
+    put(sizeof(int32_t) * (nv + 1));  // 11 vt_ptr
+    put(sizeof(int32_t) * nv);   // 12 bnd_rank
+    put(sizeof(int32_t) * (nb + 1));  // 13 bnd_cptr
+    put(sizeof(int2) * std::max(ncand, 1));  // 14 bnd_cand
+    put(sizeof(double) * 4 * nk1);  // 15 k1_part
+    put(sizeof(int32_t) * 4);    // 16 ctl
+    put(sizeof(double) * 2);     // 17 clk
+    put(sizeof(unsigned long long) * 2);  // 18 ap
+    put(sizeof(uint32_t) * 2);   // 19 status
+    put(rec ? sizeof(float4) * 4 * (size_t)nv : 0);  // 20 mixed-form element records
+    return o;
+}
+
+size_t patch_layout(int32_t np, size_t nelems, size_t ncodes, size_t* off /* 3 */) {
+    size_t o = 0;
+    int i = 0;
+    auto put = [&](size_t bytes) { off[i++] = o; o = align_up(o + bytes); };
+    put(sizeof(int4) * np);
+    put(sizeof(int32_t) * std::max<size_t>(nelems, 1));
+    put(sizeof(uint16_t) * std::max<size_t>(ncodes, 1));
+    return o;
+}
+
+int32_t nk1_of(int32_t nv, int32_t nt) {
+    return std::max((nv + kVB - 1) / kVB, (nt + kEB - 1) / kEB);
+}
+
+int dev_alloc(wcfe_engine* e, void** p, size_t bytes) {
+    if (e->budget && e->used + bytes > e->budget) return fail("HBM budget exceeded", WCFE_ERR_BUDGET);
+    cudaError_t r = cudaMallocAsync(p, bytes, e->stream);
+    if (r != cudaSuccess) {
+        cudaGetLastError();
+        return fail(std::string("cudaMallocAsync: ") + cudaGetErrorString(r), WCFE_ERR_NOMEM);
+    }
+    e->used += bytes;
+    return WCFE_OK;
+}
+void dev_free(wcfe_engine* e, void*& p, size_t& bytes) {
+    if (p) {
+        cudaFreeAsync(p, e->stream);
+        e->used -= bytes;
+    }
+    p = nullptr;
+    bytes = 0;
+}
+
+void* host_stage(wcfe_engine* e, size_t bytes) {
+    if (bytes > e->h_stage_cap) {
+        if (e->h_stage) cudaFreeHost(e->h_stage);
+        e->h_stage = nullptr;
+        if (cudaMallocHost(&e->h_stage, bytes) != cudaSuccess) {
+            e->h_stage_cap = 0;
+            return nullptr;
+        }
+        e->h_stage_cap = bytes;
+    }
+    return e->h_stage;
+}
+double* dev_stage(wcfe_engine* e, size_t bytes) {
+    if (bytes > e->d_stage_cap) {
+        if (e->d_stage) cudaFree(e->d_stage);
+        e->d_stage = nullptr;
+        if (cudaMalloc(&e->d_stage, bytes) != cudaSuccess) {
+            e->d_stage_cap = 0;
+            return nullptr;
+        }
+        e->d_stage_cap = bytes;
+    }
+    return e->d_stage;
+}
+
+// upload the whole static part of a cell (topology) and zero the state
+int upload_cell_topology(wcfe_engine* e, Cell* c) {
+    const Topology& T = c->topo;
+    int32_t ncand = (int32_t)(T.bnd_cand.size() / 2);
+    int32_t nk1 = nk1_of(T.nv, T.nt);
+    size_t off[24];
+    size_t bytes = state_layout(T.nv, T.nt, T.nb, ncand, nk1, e->prec == WCFE_PREC_MIXED, off);
+    if (c->state_block && c->state_bytes != bytes) dev_free(e, c->state_block, c->state_bytes);
+    if (!c->state_block) {
+        int r = dev_alloc(e, &c->state_block, bytes);
+        if (r) return r;
+        c->state_bytes = bytes;
+    }
+    char* b = (char*)c->state_block;
+    CK(cudaMemsetAsync(b, 0, bytes, e->stream));
+    CellDev& d = c->dev;
+    d.nv = T.nv;
+    d.nt = T.nt;
+    d.nb = T.nb;
+    d.nk1 = nk1;
+    d.pos[0] = (double4*)(b + off[0]);
+    d.pos[1] = (double4*)(b + off[1]);
+    d.vel = (double4*)(b + off[2]);
+    d.acc = (double4*)(b + off[3]);
+    d.vhl = (double4*)(b + off[4]);
+    d.ea[0] = (double*)(b + off[5]);
+    d.ea[1] = (double*)(b + off[6]);
+    d.cA = (double*)(b + off[7]);
+    d.cC = (double*)(b + off[8]);
+    d.fau = (double4*)(b + off[9]);
+    d.tri = (const int4*)(b + off[10]);
+    d.vt_ptr = (const int32_t*)(b + off[11]);
+    d.bnd_rank = (const int32_t*)(b + off[12]);
+    d.bnd_cptr = (const int32_t*)(b + off[13]);
+    d.bnd_cand = (const int2*)(b + off[14]);
+    d.k1_part = (double*)(b + off[15]);
+    d.ctl = (int32_t*)(b + off[16]);
+    d.clk = (double*)(b + off[17]);
+    d.ap = (unsigned long long*)(b + off[18]);
+    d.status = (uint32_t*)(b + off[19]);
+    d.rec = e->prec == WCFE_PREC_MIXED ? (float4*)(b + off[20]) : nullptr;
+    // topology arrays, staged through pinned memory
+    std::vector<int4> t4(T.nt);
+    for (int t = 0; t < T.nt; ++t) t4[t] = make_int4(T.tri[3 * t], T.tri[3 * t + 1], T.tri[3 * t + 2], 0);
+    CK(cudaMemcpyAsync((void*)d.tri, t4.data(), sizeof(int4) * T.nt, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync((void*)d.vt_ptr, T.vt_ptr.data(), sizeof(int32_t) * (T.nv + 1), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync((void*)d.bnd_rank, T.bnd_rank.data(), sizeof(int32_t) * T.nv, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync((void*)d.bnd_cptr, T.bnd_cptr.data(), sizeof(int32_t) * (T.nb + 1), cudaMemcpyHostToDevice, e->stream));
+    if (ncand)
+        CK(cudaMemcpyAsync((void*)d.bnd_cand, T.bnd_cand.data(), sizeof(int2) * ncand, cudaMemcpyHostToDevice, e->stream));
+    // reference start state: c_A = 100 (cellBP/main.cpp:674-677)
+    std::vector<double> ca(T.nv, 100.0);
+    CK(cudaMemcpyAsync(d.cA, ca.data(), sizeof(double) * T.nv, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int upload_cell_patches(wcfe_engine* e, Cell* c) {
+    std::string err = build_patches(c->patches, c->topo, e->patch_emax);
+    if (!err.empty()) return fail(err, WCFE_ERR_TOPOLOGY);
+    const Patches& P = c->patches;
+    size_t off[3];
+    size_t bytes = patch_layout(P.np, P.elems.size(), P.vc_code.size(), off);
+    if (c->patch_block && c->patch_bytes != bytes) dev_free(e, c->patch_block, c->patch_bytes);
+    if (!c->patch_block) {
+        int r = dev_alloc(e, &c->patch_block, bytes);
+        if (r) return r;
+        c->patch_bytes = bytes;
+    }
+    char* b = (char*)c->patch_block;
+    c->dev.np = P.np;
+    c->dev.patch = (const int4*)(b + off[0]);
+    c->dev.patch_elems = (const int32_t*)(b + off[1]);
+    c->dev.vc_code = (const uint16_t*)(b + off[2]);
+    CK(cudaMemcpyAsync((void*)c->dev.patch, P.patch.data(), sizeof(int32_t) * P.patch.size(), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync((void*)c->dev.patch_elems, P.elems.data(), sizeof(int32_t) * P.elems.size(), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync((void*)c->dev.vc_code, P.vc_code.data(), sizeof(uint16_t) * P.vc_code.size(), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int upload_substrate(wcfe_engine* e, Cell* c) {
+    dev_free(e, c->sub_block, c->sub_bytes);
+    c->dev.has_sub = 0;
+    std::memset(&c->dev.sub, 0, sizeof(SubDev));
+    if (c->sub_nt <= 0) return WCFE_OK;
+    SubGrid G;
+    build_subgrid(G, c->sub_nv, c->sub_nt, c->sub_tri.data(), c->sub_X.data());
+    size_t o = 0, off[6];
+    auto put = [&](int i, size_t bytes) { off[i] = o; o = align_up(o + bytes); };
+    put(0, sizeof(double4) * c->sub_nv);
+    put(1, sizeof(double4) * c->sub_nv);
+    put(2, sizeof(int4) * c->sub_nt);
+    put(3, sizeof(int32_t) * G.cell_ptr.size());
+    put(4, sizeof(int32_t) * std::max<size_t>(G.cell_tri.size(), 1));
+    int r = dev_alloc(e, &c->sub_block, o);
+    if (r) return r;
+    c->sub_bytes = o;
+    char* b = (char*)c->sub_block;
+    SubDev& s = c->dev.sub;
+    s.nv = c->sub_nv;
+    s.nt = c->sub_nt;
+    s.X = (const double4*)(b + off[0]);
+    s.x = (const double4*)(b + off[1]);
+    s.tri = (const int4*)(b + off[2]);
+    s.cell_ptr = (const int32_t*)(b + off[3]);
+    s.cell_tri = (const int32_t*)(b + off[4]);
+    s.ox = G.ox;
+    s.oy = G.oy;
+    s.inv_h = G.inv_h;
+    s.gx = G.gx;
+    s.gy = G.gy;
+    CK(cudaMemcpy2DAsync((void*)s.X, sizeof(double4), c->sub_X.data(), 3 * sizeof(double), 3 * sizeof(double), c->sub_nv,
+                         cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpy2DAsync((void*)s.x, sizeof(double4), c->sub_x.data(), 3 * sizeof(double), 3 * sizeof(double), c->sub_nv,
+                         cudaMemcpyHostToDevice, e->stream));
+    std::vector<int4> t4(c->sub_nt);
+    for (int t = 0; t < c->sub_nt; ++t) t4[t] = make_int4(c->sub_tri[3 * t], c->sub_tri[3 * t + 1], c->sub_tri[3 * t + 2], 0);
+    CK(cudaMemcpyAsync((void*)s.tri, t4.data(), sizeof(int4) * c->sub_nt, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync((void*)s.cell_ptr, G.cell_ptr.data(), sizeof(int32_t) * G.cell_ptr.size(), cudaMemcpyHostToDevice, e->stream));
+    if (!G.cell_tri.empty())
+        CK(cudaMemcpyAsync((void*)s.cell_tri, G.cell_tri.data(), sizeof(int32_t) * G.cell_tri.size(), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    s.moving = c->sub_moving ? 1 : 0;
+    c->dev.has_sub = 1;
+    return WCFE_OK;
+}
+
+void free_cell(wcfe_engine* e, Cell* c) {
+    dev_free(e, c->state_block, c->state_bytes);
+    dev_free(e, c->patch_block, c->patch_bytes);
+    dev_free(e, c->sub_block, c->sub_bytes);
+    if (c->rho_dev) {
+        size_t b = sizeof(double) * c->topo.nv;
+        void* p = c->rho_dev;
+        dev_free(e, p, b);
+        c->rho_dev = nullptr;
+    }
+}
+
+// ---- batched tables -----------------------------------------------------------
+void invalidate_graph(wcfe_engine* e);
+
+template <class T>
+int ensure_dev(T** p, size_t* cap, size_t n) {
+    if (n > *cap) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+        size_t c = std::max<size_t>(n, 2 * *cap);
+        if (cudaMalloc((void**)p, sizeof(T) * c) != cudaSuccess) {
+            *cap = 0;
+            return fail("cudaMalloc of a work list failed", WCFE_ERR_NOMEM);
+        }
+        *cap = c;
+    }
+    return WCFE_OK;
+}
+
+int sync_tables(wcfe_engine* e, double dt = -1.0) {
+    if (dt > 0 && dt != e->table_dt) {
+        e->table_dt = dt;
+        e->version++;
+        invalidate_graph(e);
+    }
+    if (e->table_version == e->version) return WCFE_OK;
+    e->order.clear();
+    e->table.clear();
+    e->total_nv = 0;
+    e->k1.clear();
+    e->k2.clear();
+    for (auto& kv : e->cells) {
+        Cell* c = kv.second.get();
+        c->dev.prm = c->prm;
+        c->dev.rho_w = c->rho_dev;
+        c->dev.ap_thresh = e->table_dt > 0 ? ap_threshold(c->prm, e->table_dt) : 0.0;
+        c->dev.hoff = e->total_nv;
+        e->total_nv += c->topo.nv;
+        int32_t ti = (int32_t)e->table.size();
+        e->order.push_back(c->id);
+        e->table.push_back(c->dev);
+        for (int b = 0; b < c->dev.nk1; ++b) e->k1.push_back({ti, b});
+        for (int p = 0; p < c->dev.np; ++p) e->k2.push_back({ti, p});
+    }
+    int r;
+    if ((r = ensure_dev(&e->d_table, &e->d_table_cap, std::max<size_t>(e->table.size(), 1)))) return r;
+    if ((r = ensure_dev(&e->d_k1, &e->d_k1_cap, std::max<size_t>(e->k1.size(), 1)))) return r;
+    if ((r = ensure_dev(&e->d_k2, &e->d_k2_cap, std::max<size_t>(e->k2.size(), 1)))) return r;
+    if (!e->table.empty())
+        CK(cudaMemcpyAsync(e->d_table, e->table.data(), sizeof(CellDev) * e->table.size(), cudaMemcpyHostToDevice, e->stream));
+    if (!e->k1.empty())
+        CK(cudaMemcpyAsync(e->d_k1, e->k1.data(), sizeof(WorkItem) * e->k1.size(), cudaMemcpyHostToDevice, e->stream));
+    if (!e->k2.empty())
+        CK(cudaMemcpyAsync(e->d_k2, e->k2.data(), sizeof(WorkItem) * e->k2.size(), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    e->table_version = e->version;
+    return WCFE_OK;
+}
+
+int table_index(wcfe_engine* e, int32_t id) {
+    for (size_t i = 0; i < e->order.size(); ++i)
+        if (e->order[i] == id) return (int)i;
+    return -1;
+}
+
+int rec_flag(const wcfe_engine* e) { return e->prec == WCFE_PREC_MIXED ? VP_RECORD : 0; }
+
+int grid_for(wcfe_engine* e, int nwork, int per_sm) {
+    int g = e->num_sms * std::max(per_sm, 1);
+    return std::max(1, std::min(nwork, g));
+}
+
+void invalidate_graph(wcfe_engine* e) {
+    if (e->graph.exec) cudaGraphExecDestroy(e->graph.exec);
+    e->graph.exec = nullptr;
+}
+
+// one explicit step of the cells listed in (k1, k2) device lists
+int enqueue_step(wcfe_engine* e, const WorkItem* k1, int n1, const WorkItem* k2, int n2, double dt) {
+    const double apt = std::numeric_limits<double>::quiet_NaN();  // per-cell thresholds from the table
+    int g1 = grid_for(e, n1, vertex_occupancy());
+    size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
+    int g2 = grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem));
+    cudaEvent_t* tv = (e->timing && e->tev.size() >= 3) ? &e->tev[3 * (size_t)e->timed_steps] : nullptr;
+    if (tv) cudaEventRecord(tv[0], e->stream);
+    launch_vertex_phase(e->d_table, k1, n1, dt, VP_PREDICT | VP_UPDATE_FA | rec_flag(e), g1, e->stream);
+    if (tv) cudaEventRecord(tv[1], e->stream);
+    launch_patch(e->prec, PP_STEP, e->d_table, k2, n2, e->patch_emax, dt, dt, apt,
+                 std::numeric_limits<double>::quiet_NaN(), 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                 e->patch_threads, g2, e->stream);
+    if (tv) {
+        cudaEventRecord(tv[2], e->stream);
+        e->timed_steps++;
+    }
+    e->launches += 2;
+    CK(cudaGetLastError());
+    return WCFE_OK;
+}
+
+// single-cell work lists for the drop-in entry points
+int one_cell_lists(wcfe_engine* e, Cell* c, int ti, int* n1, int* n2) {
+    std::vector<WorkItem> w;
+    for (int b = 0; b < c->dev.nk1; ++b) w.push_back({ti, b});
+    for (int p = 0; p < c->dev.np; ++p) w.push_back({ti, p});
+    int r = ensure_dev(&e->d_one, &e->d_one_cap, w.size());
+    if (r) return r;
+    CK(cudaMemcpyAsync(e->d_one, w.data(), sizeof(WorkItem) * w.size(), cudaMemcpyHostToDevice, e->stream));
+    *n1 = c->dev.nk1;
+    *n2 = c->dev.np;
+    return WCFE_OK;
+}
+
+int read_parity(wcfe_engine* e, Cell* c, int* par) {
+    int32_t ctl[2];
+    CK(cudaMemcpyAsync(ctl, c->dev.ctl, sizeof ctl, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    *par = ctl[0] & 1;
+    return WCFE_OK;
+}
+
+// host [n][3] <-> device double4 (strided 2-D copy, no kernel)
+int put3(wcfe_engine* e, double4* d, const double* h, int n) {
+    CK(cudaMemcpy2DAsync(d, sizeof(double4), h, 3 * sizeof(double), 3 * sizeof(double), n, cudaMemcpyHostToDevice, e->stream));
+    return WCFE_OK;
+}
+int get3(wcfe_engine* e, double* h, const double4* d, int n) {
+    CK(cudaMemcpy2DAsync(h, 3 * sizeof(double), d, sizeof(double4), 3 * sizeof(double), n, cudaMemcpyDeviceToHost, e->stream));
+    return WCFE_OK;
+}
+
+}  // namespace
+
+// =============================================================================
+// C ABI
+// =============================================================================
+extern "C" {
+
+void wcfe_params_default(wcfe_params* p, int32_t variant) {
+    std::memset(p, 0, sizeof *p);
+    p->mu = 1000.0; p->thick = 1.0; p->thetag_dot = 0.0; p->kappa = 0.5;
+    p->tact_rate = 200.0; p->tact_t1 = 2.0; p->tact_max = 400.0;
+    p->D_A = 1.0; p->D_C = 1e-10;
+    if (variant == WCFE_VARIANT_KMD) { p->force_law = WCFE_LAW_MD_TABLE; p->k_lin = 31000.0; p->linear_norm2d = 0; }
+    else if (variant == WCFE_VARIANT_K1) { p->force_law = WCFE_LAW_LINEAR; p->k_lin = 1000.0; p->linear_norm2d = 1; }
+    else { p->force_law = WCFE_LAW_LINEAR; p->k_lin = 31000.0; p->linear_norm2d = 1; }
+    p->rest_len = 0.0; p->poly_k0 = 31000.0; p->poly_x0 = 0.005;
+    p->rho_i_max = 100.0;
+    p->k_on = 1.0; p->ka = 0.004; p->kb = 10.0; p->Fa = 15.0; p->Fb = 15.0;
+    p->k_bend = 20.0; p->k_area = 1.0; p->area0 = 10 * 10 * 3.1416;
+    p->ap_rate = 10.0; p->ap_force = 5.0; p->ap_density = 100.0; p->ap_enable = 1;
+    p->seed = 1u; p->stream = 0u;
+    p->drag = 0.001; p->damp = 0.001; p->rho = 1.0;
+}
+
+uint32_t wcfe_ap_draw(uint32_t seed, uint32_t stream, uint64_t call, uint32_t k) {
+    return ap_draw(seed, stream, (unsigned long long)call, k);
+}
+void wcfe_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) { philox4x32_10(ctr, key, out); }
+
+const char* wcfe_last_error(void) { return g_last_error.c_str(); }
+
+int wcfe_engine_create(int32_t device, int32_t precision, uint64_t hbm_budget_bytes, wcfe_engine** out) {
+    if (!out || (precision != WCFE_PREC_FP64 && precision != WCFE_PREC_MIXED)) return fail("bad argument", WCFE_ERR_ARG);
+    if (precision == WCFE_PREC_MIXED && !mixed_available()) return fail("mixed-precision kernels not built", WCFE_ERR_ARG);
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n <= device) {
+        cudaGetLastError();
+        return fail("no CUDA device", WCFE_ERR_NODEVICE);
+    }
+    std::unique_ptr<wcfe_engine> e(new wcfe_engine());
+    e->device = device;
+    e->prec = precision;
+    e->budget = hbm_budget_bytes;
+    CK(cudaSetDevice(device));
+    CK(cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device));
+    CK(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    int max_optin = 0;
+    CK(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+    CK(configure_kernels((size_t)max_optin));
+    for (auto& ev : e->ev) CK(cudaEventCreate(&ev));
+    if (precision == WCFE_PREC_MIXED) { e->patch_threads = 128; e->patch_emax = 512; }
+    *out = e.release();
+    return WCFE_OK;
+}
+
+int wcfe_engine_destroy(wcfe_engine* e) {
+    if (!e) return WCFE_ERR_ARG;
+    cudaSetDevice(e->device);
+    cudaStreamSynchronize(e->stream);
+    for (auto& kv : e->cells) free_cell(e, kv.second.get());
+    e->cells.clear();
+    invalidate_graph(e);
+    cudaStreamSynchronize(e->stream);
+    if (e->d_table) cudaFree(e->d_table);
+    if (e->d_k1) cudaFree(e->d_k1);
+    if (e->d_k2) cudaFree(e->d_k2);
+    if (e->d_one) cudaFree(e->d_one);
+    if (e->d_xchg) cudaFree(e->d_xchg);
+    if (e->d_stage) cudaFree(e->d_stage);
+    if (e->h_stage) cudaFreeHost(e->h_stage);
+    for (auto& ev : e->ev)
+        if (ev) cudaEventDestroy(ev);
+    for (auto& ev : e->tev) cudaEventDestroy(ev);
+    cudaStreamDestroy(e->stream);
+    delete e;
+    return WCFE_OK;
+}
+
+int wcfe_engine_precision(const wcfe_engine* e) { return e ? e->prec : -1; }
+uint64_t wcfe_engine_free_bytes(const wcfe_engine* e) {
+    if (!e || !e->budget) return 0;
+    return e->budget > e->used ? e->budget - e->used : 0;
+}
+uint64_t wcfe_cell_bytes(int32_t nv, int32_t nt) {
+    size_t off[24];
+    int32_t nb = (int32_t)(4 * std::sqrt((double)std::max(nv, 1)) + 16);
+    size_t s = state_layout(nv, nt, nb, 3 * nb, nk1_of(nv, nt), true, off);
+    size_t p3[3];
+    size_t p = patch_layout(nv / 64 + 2, (size_t)(1.6 * nt) + 64, 3 * (size_t)nt, p3);
+    return (uint64_t)(s + p + sizeof(double) * nv);
+}
+int wcfe_engine_sync(wcfe_engine* e) {
+    if (!e) return WCFE_ERR_ARG;
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_cell_create(wcfe_engine* e, int32_t nv, int32_t nt, const int32_t* tri, const int32_t* vt_ptr,
+                     const int32_t* vt_idx, const uint8_t* is_bnd, const wcfe_params* params, int32_t* cell_out) {
+    if (!e || !tri || !params || !cell_out || nv <= 0 || nt <= 0) return fail("bad argument", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    std::unique_ptr<Cell> c(new Cell());
+    std::string err = build_topology(c->topo, nv, nt, tri, vt_ptr, vt_idx, is_bnd);
+    if (!err.empty()) return fail(err, WCFE_ERR_TOPOLOGY);
+    c->prm = *params;
+    int r = upload_cell_topology(e, c.get());
+    if (!r) r = upload_cell_patches(e, c.get());
+    if (r) {
+        free_cell(e, c.get());
+        return r;
+    }
+    c->id = e->next_id++;
+    *cell_out = c->id;
+    e->cells[c->id] = std::move(c);
+    e->version++;
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
+int wcfe_cell_destroy(wcfe_engine* e, int32_t id) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    free_cell(e, c);
+    e->cells.erase(id);
+    e->version++;
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
+int wcfe_cell_set_params(wcfe_engine* e, int32_t id, const wcfe_params* p) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c || !p) return fail("bad argument", WCFE_ERR_ARG);
+    c->prm = *p;
+    e->version++;
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
+int wcfe_cell_set_topology(wcfe_engine* e, int32_t id, int32_t nv, int32_t nt, const int32_t* tri,
+                           const int32_t* vt_ptr, const int32_t* vt_idx, const uint8_t* is_bnd) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c || !tri) return fail("bad argument", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    Topology T;
+    std::string err = build_topology(T, nv, nt, tri, vt_ptr, vt_idx, is_bnd);
+    if (!err.empty()) return fail(err, WCFE_ERR_TOPOLOGY);
+    c->topo = std::move(T);
+    int r = upload_cell_topology(e, c);
+    if (!r) r = upload_cell_patches(e, c);
+    if (c->rho_dev) {
+        void* p = c->rho_dev;
+        size_t b = sizeof(double) * nv;
+        dev_free(e, p, b);
+        c->rho_dev = nullptr;
+    }
+    e->version++;
+    invalidate_graph(e);
+    return r;
+}
+
+int wcfe_cell_set_substrate(wcfe_engine* e, int32_t id, int32_t nv, int32_t nt, const int32_t* tri, const double* Xs,
+                            const double* xs) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    if (nt <= 0 || !tri) {
+        c->sub_nt = 0;
+        c->sub_nv = 0;
+    } else {
+        if (!Xs || nv <= 0) return fail("substrate positions missing", WCFE_ERR_ARG);
+        for (int64_t k = 0; k < 3 * (int64_t)nt; ++k)
+            if (tri[k] < 0 || tri[k] >= nv) return fail("substrate index out of range", WCFE_ERR_TOPOLOGY);
+        c->sub_nv = nv;
+        c->sub_nt = nt;
+        c->sub_tri.assign(tri, tri + 3 * (size_t)nt);
+        c->sub_X.assign(Xs, Xs + 3 * (size_t)nv);
+        c->sub_x.assign(xs ? xs : Xs, (xs ? xs : Xs) + 3 * (size_t)nv);
+        c->sub_moving = std::memcmp(c->sub_X.data(), c->sub_x.data(), sizeof(double) * 3 * nv) != 0;
+    }
+    int r = upload_substrate(e, c);
+    e->version++;
+    invalidate_graph(e);
+    return r;
+}
+
+int wcfe_cell_set_state(wcfe_engine* e, int32_t id, const double* x, const double* V, const double* A, const double* ea,
+                        const double* cA, const double* cC, const double* fau) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    int par;
+    int r = read_parity(e, c, &par);
+    if (r) return r;
+    const int n = c->topo.nv;
+    CellDev& d = c->dev;
+    if (x && (r = put3(e, d.pos[par], x, n))) return r;
+    if (V && (r = put3(e, d.vel, V, n))) return r;
+    if (A && (r = put3(e, d.acc, A, n))) return r;
+    if (fau && (r = put3(e, d.fau, fau, n))) return r;
+    if (ea) CK(cudaMemcpyAsync(d.ea[par], ea, sizeof(double) * 6 * n, cudaMemcpyHostToDevice, e->stream));
+    if (cA) CK(cudaMemcpyAsync(d.cA, cA, sizeof(double) * n, cudaMemcpyHostToDevice, e->stream));
+    if (cC) CK(cudaMemcpyAsync(d.cC, cC, sizeof(double) * n, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_cell_get_state(wcfe_engine* e, int32_t id, double* x, double* V, double* A, double* ea, double* cA,
+                        double* cC, double* fau) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    int par;
+    int r = read_parity(e, c, &par);
+    if (r) return r;
+    const int n = c->topo.nv;
+    CellDev& d = c->dev;
+    if (x && (r = get3(e, x, d.pos[par], n))) return r;
+    if (V && (r = get3(e, V, d.vel, n))) return r;
+    if (A && (r = get3(e, A, d.acc, n))) return r;
+    if (fau && (r = get3(e, fau, d.fau, n))) return r;
+    if (ea) CK(cudaMemcpyAsync(ea, d.ea[par], sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, e->stream));
+    if (cA) CK(cudaMemcpyAsync(cA, d.cA, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+    if (cC) CK(cudaMemcpyAsync(cC, d.cC, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_cell_set_clock(wcfe_engine* e, int32_t id, double t, uint64_t calls) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    unsigned long long ap = calls;
+    CK(cudaMemcpyAsync(c->dev.clk, &t, sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync(c->dev.ap, &ap, sizeof ap, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_cell_get_clock(wcfe_engine* e, int32_t id, double* t, uint64_t* calls) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    double tt;
+    unsigned long long ap;
+    CK(cudaMemcpyAsync(&tt, c->dev.clk, sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaMemcpyAsync(&ap, c->dev.ap, sizeof ap, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    if (t) *t = tt;
+    if (calls) *calls = ap;
+    return WCFE_OK;
+}
+
+int wcfe_cell_status(wcfe_engine* e, int32_t id, uint32_t* status) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c || !status) return fail("bad argument", WCFE_ERR_ARG);
+    CK(cudaMemcpyAsync(status, c->dev.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_cell_sizes(wcfe_engine* e, int32_t id, int32_t* nv, int32_t* nt, int32_t* nb, int32_t* np) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    if (nv) *nv = c->topo.nv;
+    if (nt) *nt = c->topo.nt;
+    if (nb) *nb = c->topo.nb;
+    if (np) *np = c->patches.np;
+    return WCFE_OK;
+}
+
+// ---- drop-in pieces -------------------------------------------------------
+int wcfe_cell_predict(wcfe_engine* e, int32_t id, double dt, double* x_pred, double* V_hlf) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    int r = sync_tables(e);
+    if (r) return r;
+    int ti = table_index(e, id);
+    const int n = c->topo.nv;
+    double* st = dev_stage(e, sizeof(double) * 6 * n);
+    if (!st) return fail("staging allocation failed", WCFE_ERR_NOMEM);
+    launch_predict(e->d_table, ti, dt, x_pred ? st : nullptr, V_hlf ? st + 3 * n : nullptr, n, e->stream);
+    e->launches++;
+    CK(cudaGetLastError());
+    if (x_pred) CK(cudaMemcpyAsync(x_pred, st, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
+    if (V_hlf) CK(cudaMemcpyAsync(V_hlf, st + 3 * n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_cell_update_fa(wcfe_engine* e, int32_t id, double dt_real, const double* X, const double* x_new,
+                        const double* X_s, const double* x_s) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c || !x_new) return fail("bad argument", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    if ((X_s || x_s) && c->sub_nt > 0) {
+        bool changedX = X_s && std::memcmp(X_s, c->sub_X.data(), sizeof(double) * 3 * c->sub_nv) != 0;
+        if (X_s) c->sub_X.assign(X_s, X_s + 3 * (size_t)c->sub_nv);
+        if (x_s) c->sub_x.assign(x_s, x_s + 3 * (size_t)c->sub_nv);
+        bool moving = std::memcmp(c->sub_X.data(), c->sub_x.data(), sizeof(double) * 3 * c->sub_nv) != 0;
+        if (changedX) {
+            c->sub_moving = moving;
+            int r = upload_substrate(e, c);
+            if (r) return r;
+        } else {
+            int r = put3(e, (double4*)c->dev.sub.x, c->sub_x.data(), c->sub_nv);
+            if (r) return r;
+            if (moving != c->sub_moving) {
+                c->sub_moving = moving;
+                c->dev.sub.moving = moving ? 1 : 0;
+            }
+        }
+        e->version++;
+        invalidate_graph(e);
+    }
+    int r = sync_tables(e);
+    if (r) return r;
+    int par;
+    if ((r = read_parity(e, c, &par))) return r;
+    const int n = c->topo.nv;
+    if (X && (r = put3(e, c->dev.pos[par], X, n))) return r;
+    if ((r = put3(e, c->dev.pos[par ^ 1], x_new, n))) return r;
+    int ti = table_index(e, id), n1, n2;
+    if ((r = one_cell_lists(e, c, ti, &n1, &n2))) return r;
+    launch_vertex_phase(e->d_table, e->d_one, n1, dt_real, VP_UPDATE_FA | rec_flag(e), grid_for(e, n1, vertex_occupancy()),
+                        e->stream);
+    e->launches++;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_cell_update_forces(wcfe_engine* e, int32_t id, double dt, double dt_real, double t_tot) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    int r = sync_tables(e);
+    if (r) return r;
+    int ti = table_index(e, id), n1, n2;
+    if ((r = one_cell_lists(e, c, ti, &n1, &n2))) return r;
+    // area and centroid of the current positions (calculateAreaTot, UL:531), then the patch phase
+    launch_vertex_phase(e->d_table, e->d_one, n1, dt_real, rec_flag(e), grid_for(e, n1, vertex_occupancy()), e->stream);
+    size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
+    launch_patch(e->prec, PP_STEP, e->d_table, e->d_one + n1, n2, e->patch_emax, dt, dt_real, ap_threshold(c->prm, dt_real),
+                 t_tot, 1, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, e->patch_threads,
+                 grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem)), e->stream);
+    e->launches += 2;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_cell_eval_residual(wcfe_engine* e, int32_t id, const double* X, const double* x_new, double dt_real,
+                            const double centroid[3], double t_tot, double* Res, double* Res_ea, double* MM,
+                            double* Res_Adif, double* Res_Cdif) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c || !X || !x_new || !centroid) return fail("bad argument", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    int r = sync_tables(e);
+    if (r) return r;
+    int par;
+    if ((r = read_parity(e, c, &par))) return r;
+    const int n = c->topo.nv;
+    if ((r = put3(e, c->dev.pos[par], X, n))) return r;
+    if ((r = put3(e, c->dev.pos[par ^ 1], x_new, n))) return r;
+    double* st = dev_stage(e, sizeof(double) * (13 * (size_t)n + 4));
+    if (!st) return fail("staging allocation failed", WCFE_ERR_NOMEM);
+    double* dR = st;
+    double* dE = dR + 3 * n;
+    double* dM = dE + 6 * n;
+    double* dA = dM + n;
+    double* dC = dA + n;
+    double* dcen = dC + n;
+    CK(cudaMemcpyAsync(dcen, centroid, 3 * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    int ti = table_index(e, id), n1, n2;
+    if ((r = one_cell_lists(e, c, ti, &n1, &n2))) return r;
+    // partials for area (unused by the residual itself but keeps the kernel's prologue well defined)
+    launch_vertex_phase(e->d_table, e->d_one, n1, dt_real, 0, grid_for(e, n1, vertex_occupancy()), e->stream);
+    size_t smem = patch_smem_bytes(e->prec, PP_RESIDUAL, e->patch_emax);
+    launch_patch(e->prec, PP_RESIDUAL, e->d_table, e->d_one + n1, n2, e->patch_emax, dt_real, dt_real, 0.0, t_tot, 0, dcen,
+                 dR, dE, dM, dA, dC, e->patch_threads, grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem)),
+                 e->stream);
+    e->launches += 2;
+    CK(cudaGetLastError());
+    if (Res) CK(cudaMemcpyAsync(Res, dR, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
+    if (Res_ea) CK(cudaMemcpyAsync(Res_ea, dE, sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, e->stream));
+    if (MM) CK(cudaMemcpyAsync(MM, dM, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+    if (Res_Adif) CK(cudaMemcpyAsync(Res_Adif, dA, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+    if (Res_Cdif) CK(cudaMemcpyAsync(Res_Cdif, dC, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_cell_eval_forces(wcfe_engine* e, int32_t id, const double* x, double dt_real, double* F_FA, double* F_AP,
+                          double* F_bend, double* F_area, double area4[4]) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c || !x) return fail("bad argument", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    int r = sync_tables(e);
+    if (r) return r;
+    int par;
+    if ((r = read_parity(e, c, &par))) return r;
+    const int n = c->topo.nv;
+    // the element pass reads X too: use x for both so the residual part is defined
+    if ((r = put3(e, c->dev.pos[par], x, n))) return r;
+    if ((r = put3(e, c->dev.pos[par ^ 1], x, n))) return r;
+    double* st = dev_stage(e, sizeof(double) * 12 * (size_t)n);
+    if (!st) return fail("staging allocation failed", WCFE_ERR_NOMEM);
+    int ti = table_index(e, id), n1, n2;
+    if ((r = one_cell_lists(e, c, ti, &n1, &n2))) return r;
+    launch_vertex_phase(e->d_table, e->d_one, n1, dt_real, 0, grid_for(e, n1, vertex_occupancy()), e->stream);
+    size_t smem = patch_smem_bytes(e->prec, PP_FORCES, e->patch_emax);
+    launch_patch(e->prec, PP_FORCES, e->d_table, e->d_one + n1, n2, e->patch_emax, dt_real, dt_real,
+                 ap_threshold(c->prm, dt_real), std::numeric_limits<double>::quiet_NaN(), 0, nullptr, st, st + 3 * n,
+                 st + 6 * n, st + 9 * n, nullptr, e->patch_threads,
+                 grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem)), e->stream);
+    e->launches += 2;
+    CK(cudaGetLastError());
+    if (F_FA) CK(cudaMemcpyAsync(F_FA, st, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
+    if (F_AP) CK(cudaMemcpyAsync(F_AP, st + 3 * n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
+    if (F_bend) CK(cudaMemcpyAsync(F_bend, st + 6 * n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
+    if (F_area) CK(cudaMemcpyAsync(F_area, st + 9 * n, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, e->stream));
+    if (area4) {
+        std::vector<double> part(4 * (size_t)c->dev.nk1);
+        CK(cudaMemcpyAsync(part.data(), c->dev.k1_part, sizeof(double) * part.size(), cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        double s[4] = {0, 0, 0, 0};
+        for (int b = 0; b < c->dev.nk1; ++b)
+            for (int q = 0; q < 4; ++q) s[q] += part[4 * b + q];
+        area4[0] = s[0];
+        for (int q = 1; q < 4; ++q) area4[q] = s[q] / s[0];
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+// ---- batched stepping -------------------------------------------------------
+int wcfe_engine_step(wcfe_engine* e, int32_t nsteps, double dt) {
+    if (!e || nsteps < 0 || !(dt > 0)) return fail("bad argument", WCFE_ERR_ARG);
+    if (e->cells.empty() || nsteps == 0) return WCFE_OK;
+    CK(cudaSetDevice(e->device));
+    int r = sync_tables(e, dt);
+    if (r) return r;
+    const int n1 = (int)e->k1.size(), n2 = (int)e->k2.size();
+    if (e->use_graphs && !e->timing) {
+        const int chunk = std::min(nsteps, 8);
+        if (!e->graph.exec || e->graph.dt != dt || e->graph.version != e->version || e->graph.steps != chunk) {
+            invalidate_graph(e);
+            cudaGraph_t g;
+            CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+            for (int s = 0; s < chunk; ++s) {
+                r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt);
+                if (r) {
+                    cudaStreamEndCapture(e->stream, &g);
+                    return r;
+                }
+            }
+            e->launches -= 2 * chunk;  // counted at replay
+            CK(cudaStreamEndCapture(e->stream, &g));
+            CK(cudaGraphInstantiate(&e->graph.exec, g, 0));
+            cudaGraphDestroy(g);
+            e->graph.dt = dt;
+            e->graph.version = e->version;
+            e->graph.steps = chunk;
+        }
+        int done = 0;
+        while (done + chunk <= nsteps) {
+            CK(cudaGraphLaunch(e->graph.exec, e->stream));
+            e->launches += 2 * chunk;
+            done += chunk;
+        }
+        for (; done < nsteps; ++done)
+            if ((r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt))) return r;
+        return WCFE_OK;
+    }
+    if (e->timing) {
+        // events for every step, recorded on the engine stream without host synchronisation;
+        // read back by wcfe_engine_last_timing / wcfe_engine_step_times
+        while (e->tev.size() < 3 * (size_t)nsteps) {
+            cudaEvent_t ev;
+            CK(cudaEventCreate(&ev));
+            e->tev.push_back(ev);
+        }
+        e->timed_steps = 0;
+    }
+    for (int s = 0; s < nsteps; ++s)
+        if ((r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt))) return r;
+    if (e->timing) {
+        CK(cudaEventSynchronize(e->tev[3 * (size_t)e->timed_steps - 1]));
+        e->ms_v = e->ms_p = 0;
+        e->step_ms.assign(e->timed_steps, 0.f);
+        for (int s = 0; s < e->timed_steps; ++s) {
+            float a = 0, b = 0;
+            cudaEventElapsedTime(&a, e->tev[3 * s], e->tev[3 * s + 1]);
+            cudaEventElapsedTime(&b, e->tev[3 * s + 1], e->tev[3 * s + 2]);
+            e->ms_v += a;
+            e->ms_p += b;
+            e->step_ms[s] = a + b;
+        }
+        cudaEventElapsedTime(&e->ms_span, e->tev[0], e->tev[3 * (size_t)e->timed_steps - 1]);
+    }
+    return WCFE_OK;
+}
+
+int wcfe_engine_step_cells(wcfe_engine* e, const int32_t* ids, int32_t ncells, int32_t nsteps, double dt) {
+    if (!e || !ids || ncells <= 0 || nsteps < 0 || !(dt > 0)) return fail("bad argument", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    int r = sync_tables(e, dt);
+    if (r) return r;
+    std::vector<WorkItem> w1, w2;
+    for (int i = 0; i < ncells; ++i) {
+        Cell* c = find(e, ids[i]);
+        if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+        int ti = table_index(e, ids[i]);
+        for (int b = 0; b < c->dev.nk1; ++b) w1.push_back({ti, b});
+        for (int p = 0; p < c->dev.np; ++p) w2.push_back({ti, p});
+    }
+    std::vector<WorkItem> w(w1);
+    w.insert(w.end(), w2.begin(), w2.end());
+    if ((r = ensure_dev(&e->d_one, &e->d_one_cap, w.size()))) return r;
+    CK(cudaMemcpyAsync(e->d_one, w.data(), sizeof(WorkItem) * w.size(), cudaMemcpyHostToDevice, e->stream));
+    for (int s = 0; s < nsteps; ++s)
+        if ((r = enqueue_step(e, e->d_one, (int)w1.size(), e->d_one + w1.size(), (int)w2.size(), dt))) return r;
+    return WCFE_OK;
+}
+
+int wcfe_engine_set_graphs(wcfe_engine* e, int32_t enable) {
+    if (!e) return WCFE_ERR_ARG;
+    e->use_graphs = enable != 0;
+    if (!e->use_graphs) invalidate_graph(e);
+    return WCFE_OK;
+}
+
+int wcfe_engine_set_shape(wcfe_engine* e, int32_t threads, int32_t emax) {
+    if (!e) return WCFE_ERR_ARG;
+    if (threads == 0) threads = e->patch_threads;
+    if (emax == 0) emax = e->patch_emax;
+    if (threads % 32 || threads < 32 || threads > 512 || emax < 32 || emax > 4096) return fail("bad shape", WCFE_ERR_ARG);
+    int max_optin = 0;
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
+    if (patch_smem_bytes(e->prec, PP_RESIDUAL, emax) + 1024 > (size_t)max_optin) return fail("shape exceeds shared memory", WCFE_ERR_LIMIT);
+    CK(cudaStreamSynchronize(e->stream));
+    e->patch_threads = threads;
+    if (emax != e->patch_emax) {
+        e->patch_emax = emax;
+        for (auto& kv : e->cells) {
+            int r = upload_cell_patches(e, kv.second.get());
+            if (r) return r;
+        }
+        e->version++;
+    }
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
+int wcfe_engine_get_shape(const wcfe_engine* e, int32_t* threads, int32_t* emax) {
+    if (!e) return WCFE_ERR_ARG;
+    if (threads) *threads = e->patch_threads;
+    if (emax) *emax = e->patch_emax;
+    return WCFE_OK;
+}
+
+int wcfe_engine_set_timing(wcfe_engine* e, int32_t enable) {
+    if (!e) return WCFE_ERR_ARG;
+    e->timing = enable != 0;
+    return WCFE_OK;
+}
+
+int64_t wcfe_engine_step_times(wcfe_engine* e, float* out, int64_t cap, float* span_ms) {
+    if (!e) return -1;
+    for (int64_t i = 0; out && i < cap && i < (int64_t)e->step_ms.size(); ++i) out[i] = e->step_ms[i];
+    if (span_ms) *span_ms = e->ms_span;
+    return (int64_t)e->step_ms.size();
+}
+
+int wcfe_engine_last_timing(wcfe_engine* e, float* ms_v, float* ms_p) {
+    if (!e) return WCFE_ERR_ARG;
+    if (ms_v) *ms_v = e->ms_v;
+    if (ms_p) *ms_p = e->ms_p;
+    return WCFE_OK;
+}
+
+uint64_t wcfe_engine_launches(const wcfe_engine* e) { return e ? e->launches : 0; }
+
+int wcfe_debug_topology(int32_t nv, int32_t nt, const int32_t* tri, const int32_t* vt_ptr, const int32_t* vt_idx,
+                        const uint8_t* is_bnd, int32_t emax, int32_t* nb_out, int32_t* bnd_rank, int32_t* bnd_cptr,
+                        int32_t* bnd_cand, int32_t cand_cap, int32_t* np_out, int32_t* patch, int32_t patch_cap,
+                        int32_t* patch_elems, int32_t elems_cap, uint16_t* vc_code) {
+    Topology T;
+    std::string err = build_topology(T, nv, nt, tri, vt_ptr, vt_idx, is_bnd);
+    if (!err.empty()) return fail(err, WCFE_ERR_TOPOLOGY);
+    Patches P;
+    err = build_patches(P, T, emax);
+    if (!err.empty()) return fail(err, WCFE_ERR_TOPOLOGY);
+    if ((int64_t)T.bnd_cand.size() > cand_cap || (int64_t)P.patch.size() > patch_cap ||
+        (int64_t)P.elems.size() > elems_cap)
+        return fail("output capacity too small", WCFE_ERR_LIMIT);
+    if (nb_out) *nb_out = T.nb;
+    if (bnd_rank) std::memcpy(bnd_rank, T.bnd_rank.data(), sizeof(int32_t) * nv);
+    if (bnd_cptr) std::memcpy(bnd_cptr, T.bnd_cptr.data(), sizeof(int32_t) * T.bnd_cptr.size());
+    if (bnd_cand && !T.bnd_cand.empty()) std::memcpy(bnd_cand, T.bnd_cand.data(), sizeof(int32_t) * T.bnd_cand.size());
+    if (np_out) *np_out = P.np;
+    if (patch) std::memcpy(patch, P.patch.data(), sizeof(int32_t) * P.patch.size());
+    if (patch_elems) std::memcpy(patch_elems, P.elems.data(), sizeof(int32_t) * P.elems.size());
+    if (vc_code) std::memcpy(vc_code, P.vc_code.data(), sizeof(uint16_t) * P.vc_code.size());
+    return WCFE_OK;
+}
+
+int64_t wcfe_engine_total_vertices(wcfe_engine* e) {
+    if (!e) return -1;
+    if (sync_tables(e)) return -1;
+    return e->total_nv;
+}
+
+int wcfe_engine_predict(wcfe_engine* e, double dt, double* x_pred) {
+    if (!e || !x_pred || !(dt > 0)) return fail("bad argument", WCFE_ERR_ARG);
+    if (e->cells.empty()) return WCFE_OK;
+    CK(cudaSetDevice(e->device));
+    int r = sync_tables(e, dt);
+    if (r) return r;
+    if ((r = ensure_dev(&e->d_xchg, &e->d_xchg_cap, 3 * (size_t)e->total_nv))) return r;
+    const int n1 = (int)e->k1.size();
+    launch_vertex_phase(e->d_table, e->d_k1, n1, dt, VP_PREDICT | VP_EXPORT | VP_NOAREA, grid_for(e, n1, vertex_occupancy()),
+                        e->stream, nullptr, e->d_xchg);
+    e->launches++;
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(x_pred, e->d_xchg, sizeof(double) * 3 * e->total_nv, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_engine_update(wcfe_engine* e, double dt, double dt_real, const double* x_new) {
+    if (!e || !x_new || !(dt > 0) || !(dt_real > 0)) return fail("bad argument", WCFE_ERR_ARG);
+    if (e->cells.empty()) return WCFE_OK;
+    CK(cudaSetDevice(e->device));
+    int r = sync_tables(e, dt_real);
+    if (r) return r;
+    if ((r = ensure_dev(&e->d_xchg, &e->d_xchg_cap, 3 * (size_t)e->total_nv))) return r;
+    CK(cudaMemcpyAsync(e->d_xchg, x_new, sizeof(double) * 3 * e->total_nv, cudaMemcpyHostToDevice, e->stream));
+    const int n1 = (int)e->k1.size(), n2 = (int)e->k2.size();
+    launch_vertex_phase(e->d_table, e->d_k1, n1, dt_real, VP_IMPORT | VP_UPDATE_FA | rec_flag(e),
+                        grid_for(e, n1, vertex_occupancy()), e->stream, e->d_xchg, nullptr);
+    size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
+    launch_patch(e->prec, PP_STEP, e->d_table, e->d_k2, n2, e->patch_emax, dt, dt_real,
+                 std::numeric_limits<double>::quiet_NaN(), std::numeric_limits<double>::quiet_NaN(), 1, nullptr, nullptr,
+                 nullptr, nullptr, nullptr, nullptr, e->patch_threads,
+                 grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem)), e->stream);
+    e->launches += 2;
+    CK(cudaGetLastError());
+    return WCFE_OK;
+}
+
+int wcfe_cell_set_integrins(wcfe_engine* e, int32_t id, const double* rho) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    const size_t bytes = sizeof(double) * c->topo.nv;
+    if (!rho) {
+        if (c->rho_dev) {
+            void* p = c->rho_dev;
+            size_t b = bytes;
+            dev_free(e, p, b);
+            c->rho_dev = nullptr;
+        }
+    } else {
+        if (!c->rho_dev) {
+            void* p = nullptr;
+            int r = dev_alloc(e, &p, bytes);
+            if (r) return r;
+            c->rho_dev = (double*)p;
+        }
+        CK(cudaMemcpyAsync(c->rho_dev, rho, bytes, cudaMemcpyHostToDevice, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    e->version++;
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
+// Autotuner: time every candidate (threads, emax) on the live cells.  The state
+// is saved and restored around the trials so tuning does not advance the cells.
+int wcfe_engine_autotune(wcfe_engine* e, double dt, int32_t reps) {
+    if (!e || !(dt > 0) || reps < 1) return fail("bad argument", WCFE_ERR_ARG);
+    if (e->cells.empty()) return WCFE_OK;
+    CK(cudaSetDevice(e->device));
+    // save all state blocks
+    std::vector<std::pair<Cell*, void*>> saved;
+    for (auto& kv : e->cells) {
+        Cell* c = kv.second.get();
+        void* copy = nullptr;
+        CK(cudaMalloc(&copy, c->state_bytes));
+        CK(cudaMemcpyAsync(copy, c->state_block, c->state_bytes, cudaMemcpyDeviceToDevice, e->stream));
+        saved.push_back({c, copy});
+    }
+    const int threads_c[] = {64, 128, 256};
+    const int emax_c[] = {192, 256, 320, 384, 512, 768};
+    int max_optin = 0;
+    cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
+    float best = 1e30f;
+    int bt = e->patch_threads, be = e->patch_emax;
+    bool was_timing = e->timing;
+    e->timing = true;
+    for (int em : emax_c) {
+        if (patch_smem_bytes(e->prec, PP_RESIDUAL, em) + 1024 > (size_t)max_optin) continue;
+        for (int th : threads_c) {
+            int r = wcfe_engine_set_shape(e, th, em);
+            if (r) continue;
+            wcfe_engine_step(e, 1, dt);  // warm
+            r = wcfe_engine_step(e, reps, dt);
+            if (r) continue;
+            float t = e->ms_v + e->ms_p;
+            if (t < best) { best = t; bt = th; be = em; }
+            for (auto& s : saved)
+                CK(cudaMemcpyAsync(s.first->state_block, s.second, s.first->state_bytes, cudaMemcpyDeviceToDevice, e->stream));
+        }
+    }
+    e->timing = was_timing;
+    int r = wcfe_engine_set_shape(e, bt, be);
+    for (auto& s : saved) {
+        cudaMemcpyAsync(s.first->state_block, s.second, s.first->state_bytes, cudaMemcpyDeviceToDevice, e->stream);
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    for (auto& s : saved) cudaFree(s.second);
+    e->tuned = true;
+    return r;
+}
+
+}  // extern "C"
