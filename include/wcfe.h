@@ -266,6 +266,21 @@ int wcfe_server_result(wcfe_server* srv, int64_t req_id, double* x_out, double* 
 /* Per-iteration wall time samples (seconds) collected so far; returns count. */
 int64_t wcfe_server_step_times(wcfe_server* srv, double* out, int64_t cap);
 
+/* ---- allocation-free area reduction ------------------------------------- */
+/* No counterpart in the reference: the same total area and area-weighted
+ * centroid as calculateAreaTot (computed inside every engine step), as a
+ * single call that allocates no device memory, for host codes that reserve
+ * all their device memory up front or must not synchronise on cudaMalloc /
+ * cudaFree mid-loop.  Inputs and output are the caller's device memory:
+ * x double[n][3], tri int32[t][3], area4 double[4] = {A, cx, cy, cz}.  The
+ * scratch is a 128 KiB file-scope device array that every GPU loading the
+ * library keeps until exit; t <= 4,194,304 (else WCFE_ERR_LIMIT).  The first
+ * call on a device resolves the array's address (do it before any stream
+ * capture).  Calls overlapping on the GPU race on the shared array.  An index
+ * outside [0, n) yields NaN.  stream: a cudaStream_t, or NULL. */
+int wcfe_area_tot_noalloc(const double* x_dev, int32_t n_vert, const int32_t* tri_dev, int32_t n_tri,
+                          double* area4_dev, void* stream);
+
 /* ---- host-only inspection of the connectivity preprocessing (no device) --- */
 /* Boundary ranks and neighbour candidates (the scan of UL:1500-1531), patches and
  * one-ring slot codes, exactly as the engine builds them.  Capacities in int32 units. */

@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 LIB = os.path.join(HERE, "libwcfe.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["wcfe_kernels.cu", "wcfe_mixed.cu", "wcfe_engine.cu", "wcfe_server.cu", "wcfe_topology.cpp"]
+SOURCES = ["wcfe_kernels.cu", "wcfe_mixed.cu", "wcfe_engine.cu", "wcfe_server.cu", "wcfe_topology.cpp",
+           "wcfe_noalloc.cu"]
 
 
 def nvcc() -> str:

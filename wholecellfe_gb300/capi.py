@@ -72,6 +72,7 @@ SIGNATURES = {
     "wcfe_server_iterate": (C.c_int, [C.c_void_p, _i, _i]),
     "wcfe_server_result": (C.c_int, [C.c_void_p, C.c_int64, _d, _d]),
     "wcfe_server_step_times": (C.c_int64, [C.c_void_p, _d, C.c_int64]),
+    "wcfe_area_tot_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "wcfe_debug_topology": (C.c_int, [C.c_int32, C.c_int32, _i, _i, _i, _u8, C.c_int32, _i, _i, _i, _i, C.c_int32, _i,
                                       _i, C.c_int32, _i, C.c_int32, C.POINTER(C.c_uint16)]),
 }
