@@ -163,10 +163,10 @@ def cpu_baseline(cells, steps: int, budget_s: float = 15.0):
 # ----------------------------------------------------------------------------- measurements
 def kernel_bytes_patch_mixed(nv_total: int, nt_total: int) -> float:
     """Algorithmic DRAM bytes of one mixed patch-phase launch: per vertex it reads the FP32
-    element record (64 B), x (24), the bond vector (24), c_C (8), V and A (48), the strain
-    (48), the one-ring offsets and slot codes (4 + 2 per incidence), and writes V, A (48) and
-    the strain (48); per element it reads the triangle (12) and its patch entry (4)."""
-    per_v = 64 + 24 + 24 + 8 + 48 + 48 + 4 + 48 + 48
+    element record (48 B), the bond vector (24), c_C (8), V and A (48), the strain (48), the
+    one-ring offsets and slot codes (4 + 2 per incidence), and writes V, A (48) and the strain
+    (48); per element it reads the triangle (12) and its patch entry (4)."""
+    per_v = 48 + 24 + 8 + 48 + 48 + 4 + 48 + 48
     per_incidence = 2
     per_t = 12 + 4
     return per_v * nv_total + per_incidence * 3 * nt_total + per_t * nt_total
@@ -307,6 +307,8 @@ def run_ours(args):
         p = default_params("k1")
         ep = capi.Engine(capi.PREC_FP64, device=device)
         hp = ep.add_cell(x0, tri, p, state=synth.initial_state(x0))
+        ep.autotune(DT, 5)
+        plain_shape = ep.shape()
         for _ in range(args.warmup):
             ep.step(1, DT)
         plain_steps = 200
@@ -353,6 +355,7 @@ def run_ours(args):
                        "parallelism": f"replicas x{world}"},
             "p50_ms_per_step": round(p50, 4), "p99_ms_per_step": round(p99, 4),
             "plain_fp64": {"value": round(plain_value, 1), "unit": "cell-steps/s", "cell_vertices": len(x0),
+                           "shape": list(plain_shape),
                            "p50_ms_per_step": round(percentile(pr["per_step"], 0.5), 4),
                            "p99_ms_per_step": round(percentile(pr["per_step"], 0.99), 4),
                            "wall_cell_steps_per_s": round(plain_wall, 1)},
@@ -367,6 +370,33 @@ def run_ours(args):
         dist.destroy_process_group()
     if out:
         print(json.dumps(out), flush=True)
+
+
+def run_phase(args):
+    """One timed loop only, for profiling: the batched mixed or FP64 form on the workload
+    (--cells of them), or the plain one-cell FP64 form."""
+    import torch
+    from wholecellfe_gb300 import capi, synth
+    from wholecellfe_gb300.params import default_params
+    torch.cuda.init()
+    if args.phase == "plain":
+        x0, tri = synth.disk_mesh(2000, seed=1)
+        eng = capi.Engine(capi.PREC_FP64)
+        eng.add_cell(x0, tri, default_params("k1"), state=synth.initial_state(x0))
+        ncells = 1
+    else:
+        cells = make_workload(seed=1000, ncells=args.cells)
+        eng = capi.Engine(capi.PREC_MIXED if args.phase == "mixed" else capi.PREC_FP64)
+        load_cells(eng, cells)
+        ncells = len(cells)
+    for _ in range(args.warmup):
+        eng.step(1, DT)
+    r = timed_steps(eng, args.steps, DT)
+    thr, emax = eng.shape()
+    print(json.dumps({"phase": args.phase, "cells": ncells, "ms_per_step": r["total_ms"] / args.steps,
+                      "vertex_ms": r["ms_v"] / args.steps, "patch_ms": r["ms_p"] / args.steps,
+                      "cell_steps_per_s": ncells * args.steps / (r["total_ms"] / 1e3), "shape": [thr, emax]}))
+    eng.close()
 
 
 def run_reference(args):
@@ -416,6 +446,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells", type=int, default=N_CELLS)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain"],
+                    help="profiling aid: run only one timed loop (default shape, no autotune) and print its timing")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -423,6 +455,8 @@ def main():
     oracle_py.build()
     if args.impl == "reference":
         run_reference(args)
+    elif args.phase != "all":
+        run_phase(args)
     else:
         run_ours(args)
 

@@ -63,7 +63,10 @@ __device__ __forceinline__ void spring_force(const wcfe_params& p, double ux, do
         return;
     }
     double dx = 0, dy = 0, dz = 0;
-    if (D != 0) { dx = ux / D; dy = uy / D; dz = uz / D; }
+    if (D != 0) {
+        const double iD = 1.0 / D;
+        dx = ux * iD; dy = uy * iD; dz = uz * iD;
+    }
     double mag = 0.0;
     if (p.force_law == WCFE_LAW_MD_TABLE) {
         int j = -1;

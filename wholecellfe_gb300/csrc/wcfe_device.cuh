@@ -18,9 +18,7 @@
 
 namespace wcfe {
 
-constexpr int kVB = 256;        // vertices per vertex-phase block
-constexpr int kEB = 512;        // elements per vertex-phase block
-constexpr int kK1Threads = 256;
+constexpr int kK1Threads = 256;  // largest vertex-phase block (vertices per block = threads = CellDev::vb)
 
 struct SubDev {                 // substrate mesh + uniform grid for point location
     int32_t nv, nt;
@@ -36,6 +34,7 @@ struct SubDev {                 // substrate mesh + uniform grid for point locat
 
 struct CellDev {
     int32_t nv, nt, nb, np, nk1;
+    int32_t vb;                 // vertices per vertex-phase block (= its thread count); 2 vb elements per block
     int32_t has_sub;
     int64_t hoff;               // first vertex of this cell in the engine's packed host exchange arrays
     double4* pos[2];
@@ -55,6 +54,8 @@ struct CellDev {
     const int32_t* bnd_rank;
     const int32_t* bnd_cptr;
     const int2* bnd_cand;
+    const int32_t* bnd_optr;    // [nb+1] directed boundary edges leaving each boundary vertex
+    const int32_t* bnd_out;     //        and their end vertices (the boundary loop, mixed-form area)
     double* k1_part;
     float4* rec;                // mixed form: per-vertex FP32 element inputs [nv][4] (see wcfe_mixed.cu)
     // control words, advanced by the last patch-phase CTA of the cell to finish a step:

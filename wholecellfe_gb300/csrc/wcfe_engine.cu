@@ -22,13 +22,15 @@
 namespace wcfe {
 struct PatchArgs;
 void launch_vertex_phase(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
-                         cudaStream_t st, const double* stage_in = nullptr, double* stage_out = nullptr);
+                         int threads, cudaStream_t st, const double* stage_in = nullptr, double* stage_out = nullptr);
 void launch_predict(const CellDev* cells, int cell, double dt, double* xout, double* vhout, int nv, cudaStream_t st);
 cudaError_t configure_kernels(size_t max_smem);
 size_t patch_smem_bytes(int prec, int mode, int emax);
 int patch_occupancy(int prec, int threads, size_t smem);
-int vertex_occupancy();
+int vertex_occupancy(int threads);
 bool mixed_available();
+void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
+                         int threads, cudaStream_t st, const double* stage_in, double* stage_out);
 void launch_patch(int prec, int mode, const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt,
                   double dt_real, double ap_thresh, double t_override, int vh_from_buf, const double* centroid_dev,
                   double* o0, double* o1, double* o2, double* o3, double* o4, int threads, int grid, cudaStream_t st);
@@ -122,6 +124,7 @@ struct wcfe_engine {
     // shapes
     int patch_threads = 128;
     int patch_emax = 320;
+    int vblock = 256;             // vertices (threads) per vertex-phase block
     bool tuned = false;
     // graphs
     bool use_graphs = false;
@@ -173,7 +176,9 @@ size_t state_layout(int32_t nv, int32_t nt, int32_t nb, int32_t ncand, int32_t n
     put(sizeof(double) * 2);     // 17 clk
     put(sizeof(unsigned long long) * 2);  // 18 ap
     put(sizeof(uint32_t) * 2);   // 19 status
-    put(rec ? sizeof(float4) * 4 * (size_t)nv : 0);  // 20 mixed-form element records
+    put(rec ? sizeof(float4) * 3 * (size_t)nv : 0);  // 20 mixed-form element records (3 float4 per vertex)
+    put(sizeof(int32_t) * (nb + 1));  // 21 bnd_optr
+    put(sizeof(int32_t) * std::max(2 * nb, 1));  // 22 bnd_out (at most a few edges per boundary vertex)
     return o;
 }
 
@@ -187,8 +192,8 @@ size_t patch_layout(int32_t np, size_t nelems, size_t ncodes, size_t* off /* 3 *
     return o;
 }
 
-int32_t nk1_of(int32_t nv, int32_t nt) {
-    return std::max((nv + kVB - 1) / kVB, (nt + kEB - 1) / kEB);
+int32_t nk1_of(int32_t nv, int32_t nt, int32_t vb) {
+    return std::max((nv + vb - 1) / vb, (nt + 2 * vb - 1) / (2 * vb));
 }
 
 int dev_alloc(wcfe_engine* e, void** p, size_t bytes) {
@@ -239,7 +244,7 @@ double* dev_stage(wcfe_engine* e, size_t bytes) {
 int upload_cell_topology(wcfe_engine* e, Cell* c) {
     const Topology& T = c->topo;
     int32_t ncand = (int32_t)(T.bnd_cand.size() / 2);
-    int32_t nk1 = nk1_of(T.nv, T.nt);
+    int32_t nk1 = nk1_of(T.nv, T.nt, e->vblock);
     size_t off[24];
     size_t bytes = state_layout(T.nv, T.nt, T.nb, ncand, nk1, e->prec == WCFE_PREC_MIXED, off);
     if (c->state_block && c->state_bytes != bytes) dev_free(e, c->state_block, c->state_bytes);
@@ -255,6 +260,7 @@ int upload_cell_topology(wcfe_engine* e, Cell* c) {
     d.nt = T.nt;
     d.nb = T.nb;
     d.nk1 = nk1;
+    d.vb = e->vblock;
     d.pos[0] = (double4*)(b + off[0]);
     d.pos[1] = (double4*)(b + off[1]);
     d.vel = (double4*)(b + off[2]);
@@ -276,6 +282,12 @@ int upload_cell_topology(wcfe_engine* e, Cell* c) {
     d.ap = (unsigned long long*)(b + off[18]);
     d.status = (uint32_t*)(b + off[19]);
     d.rec = e->prec == WCFE_PREC_MIXED ? (float4*)(b + off[20]) : nullptr;
+    d.bnd_optr = (const int32_t*)(b + off[21]);
+    d.bnd_out = (const int32_t*)(b + off[22]);
+    if ((int64_t)T.bnd_out.size() > std::max<int64_t>(2 * (int64_t)T.nb, 1)) return fail("non-manifold boundary", WCFE_ERR_TOPOLOGY);
+    CK(cudaMemcpyAsync((void*)d.bnd_optr, T.bnd_optr.data(), sizeof(int32_t) * (T.nb + 1), cudaMemcpyHostToDevice, e->stream));
+    if (!T.bnd_out.empty())
+        CK(cudaMemcpyAsync((void*)d.bnd_out, T.bnd_out.data(), sizeof(int32_t) * T.bnd_out.size(), cudaMemcpyHostToDevice, e->stream));
     // topology arrays, staged through pinned memory
     std::vector<int4> t4(T.nt);
     for (int t = 0; t < T.nt; ++t) t4[t] = make_int4(T.tri[3 * t], T.tri[3 * t + 1], T.tri[3 * t + 2], 0);
@@ -441,6 +453,13 @@ int table_index(wcfe_engine* e, int32_t id) {
 
 int rec_flag(const wcfe_engine* e) { return e->prec == WCFE_PREC_MIXED ? VP_RECORD : 0; }
 
+// vertex phase of the engine's arithmetic form (the mixed form has its own kernel)
+void vphase(const wcfe_engine* e, const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
+            cudaStream_t st, const double* stage_in = nullptr, double* stage_out = nullptr) {
+    if (e->prec == WCFE_PREC_MIXED) launch_vertex_mixed(cells, work, nwork, dt, flags, grid, e->vblock, st, stage_in, stage_out);
+    else launch_vertex_phase(cells, work, nwork, dt, flags, grid, e->vblock, st, stage_in, stage_out);
+}
+
 int grid_for(wcfe_engine* e, int nwork, int per_sm) {
     int g = e->num_sms * std::max(per_sm, 1);
     return std::max(1, std::min(nwork, g));
@@ -454,12 +473,12 @@ void invalidate_graph(wcfe_engine* e) {
 // one explicit step of the cells listed in (k1, k2) device lists
 int enqueue_step(wcfe_engine* e, const WorkItem* k1, int n1, const WorkItem* k2, int n2, double dt) {
     const double apt = std::numeric_limits<double>::quiet_NaN();  // per-cell thresholds from the table
-    int g1 = grid_for(e, n1, vertex_occupancy());
+    int g1 = grid_for(e, n1, vertex_occupancy(e->vblock));
     size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
     int g2 = grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem));
     cudaEvent_t* tv = (e->timing && e->tev.size() >= 3) ? &e->tev[3 * (size_t)e->timed_steps] : nullptr;
     if (tv) cudaEventRecord(tv[0], e->stream);
-    launch_vertex_phase(e->d_table, k1, n1, dt, VP_PREDICT | VP_UPDATE_FA | rec_flag(e), g1, e->stream);
+    vphase(e, e->d_table, k1, n1, dt, VP_PREDICT | VP_UPDATE_FA | rec_flag(e), g1, e->stream);
     if (tv) cudaEventRecord(tv[1], e->stream);
     launch_patch(e->prec, PP_STEP, e->d_table, k2, n2, e->patch_emax, dt, dt, apt,
                  std::numeric_limits<double>::quiet_NaN(), 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
@@ -554,7 +573,8 @@ int wcfe_engine_create(int32_t device, int32_t precision, uint64_t hbm_budget_by
     CK(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
     CK(configure_kernels((size_t)max_optin));
     for (auto& ev : e->ev) CK(cudaEventCreate(&ev));
-    if (precision == WCFE_PREC_MIXED) { e->patch_threads = 128; e->patch_emax = 512; }
+    if (precision == WCFE_PREC_MIXED) { e->patch_threads = 128; e->patch_emax = 512; e->vblock = 256; }
+    else { e->patch_threads = 64; e->patch_emax = 96; e->vblock = 64; }  // FP64: more, smaller blocks
     *out = e.release();
     return WCFE_OK;
 }
@@ -590,7 +610,7 @@ uint64_t wcfe_engine_free_bytes(const wcfe_engine* e) {
 uint64_t wcfe_cell_bytes(int32_t nv, int32_t nt) {
     size_t off[24];
     int32_t nb = (int32_t)(4 * std::sqrt((double)std::max(nv, 1)) + 16);
-    size_t s = state_layout(nv, nt, nb, 3 * nb, nk1_of(nv, nt), true, off);
+    size_t s = state_layout(nv, nt, nb, 3 * nb, nk1_of(nv, nt, 64), true, off);
     size_t p3[3];
     size_t p = patch_layout(nv / 64 + 2, (size_t)(1.6 * nt) + 64, 3 * (size_t)nt, p3);
     return (uint64_t)(s + p + sizeof(double) * nv);
@@ -699,6 +719,20 @@ int wcfe_cell_set_state(wcfe_engine* e, int32_t id, const double* x, const doubl
     if (r) return r;
     const int n = c->topo.nv;
     CellDev& d = c->dev;
+    if (x && e->prec == WCFE_PREC_MIXED) {
+        // the mixed form assumes a planar membrane with counter-clockwise triangles (its
+        // element inputs drop z and its area comes from the boundary loop)
+        for (int v = 0; v < n; ++v)
+            if (x[3 * v + 2] != 0.0) return fail("the mixed form needs a planar membrane (z = 0)", WCFE_ERR_ARG);
+        const std::vector<int32_t>& T = c->topo.tri;
+        for (int t = 0; t < c->topo.nt; ++t) {
+            const double* a = x + 3 * T[3 * t];
+            const double* b = x + 3 * T[3 * t + 1];
+            const double* q = x + 3 * T[3 * t + 2];
+            if ((b[0] - a[0]) * (q[1] - a[1]) - (b[1] - a[1]) * (q[0] - a[0]) <= 0)
+                return fail("the mixed form needs counter-clockwise, non-degenerate triangles", WCFE_ERR_ARG);
+        }
+    }
     if (x && (r = put3(e, d.pos[par], x, n))) return r;
     if (V && (r = put3(e, d.vel, V, n))) return r;
     if (A && (r = put3(e, d.acc, A, n))) return r;
@@ -826,8 +860,8 @@ int wcfe_cell_update_fa(wcfe_engine* e, int32_t id, double dt_real, const double
     if ((r = put3(e, c->dev.pos[par ^ 1], x_new, n))) return r;
     int ti = table_index(e, id), n1, n2;
     if ((r = one_cell_lists(e, c, ti, &n1, &n2))) return r;
-    launch_vertex_phase(e->d_table, e->d_one, n1, dt_real, VP_UPDATE_FA | rec_flag(e), grid_for(e, n1, vertex_occupancy()),
-                        e->stream);
+    vphase(e, e->d_table, e->d_one, n1, dt_real, VP_UPDATE_FA | rec_flag(e), grid_for(e, n1, vertex_occupancy(e->vblock)),
+           e->stream);
     e->launches++;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(e->stream));
@@ -843,7 +877,7 @@ int wcfe_cell_update_forces(wcfe_engine* e, int32_t id, double dt, double dt_rea
     int ti = table_index(e, id), n1, n2;
     if ((r = one_cell_lists(e, c, ti, &n1, &n2))) return r;
     // area and centroid of the current positions (calculateAreaTot, UL:531), then the patch phase
-    launch_vertex_phase(e->d_table, e->d_one, n1, dt_real, rec_flag(e), grid_for(e, n1, vertex_occupancy()), e->stream);
+    vphase(e, e->d_table, e->d_one, n1, dt_real, rec_flag(e), grid_for(e, n1, vertex_occupancy(e->vblock)), e->stream);
     size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
     launch_patch(e->prec, PP_STEP, e->d_table, e->d_one + n1, n2, e->patch_emax, dt, dt_real, ap_threshold(c->prm, dt_real),
                  t_tot, 1, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, e->patch_threads,
@@ -879,7 +913,8 @@ int wcfe_cell_eval_residual(wcfe_engine* e, int32_t id, const double* X, const d
     int ti = table_index(e, id), n1, n2;
     if ((r = one_cell_lists(e, c, ti, &n1, &n2))) return r;
     // partials for area (unused by the residual itself but keeps the kernel's prologue well defined)
-    launch_vertex_phase(e->d_table, e->d_one, n1, dt_real, 0, grid_for(e, n1, vertex_occupancy()), e->stream);
+    launch_vertex_phase(e->d_table, e->d_one, n1, dt_real, 0, grid_for(e, n1, vertex_occupancy(e->vblock)), e->vblock,
+                        e->stream);
     size_t smem = patch_smem_bytes(e->prec, PP_RESIDUAL, e->patch_emax);
     launch_patch(e->prec, PP_RESIDUAL, e->d_table, e->d_one + n1, n2, e->patch_emax, dt_real, dt_real, 0.0, t_tot, 0, dcen,
                  dR, dE, dM, dA, dC, e->patch_threads, grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem)),
@@ -912,7 +947,8 @@ int wcfe_cell_eval_forces(wcfe_engine* e, int32_t id, const double* x, double dt
     if (!st) return fail("staging allocation failed", WCFE_ERR_NOMEM);
     int ti = table_index(e, id), n1, n2;
     if ((r = one_cell_lists(e, c, ti, &n1, &n2))) return r;
-    launch_vertex_phase(e->d_table, e->d_one, n1, dt_real, 0, grid_for(e, n1, vertex_occupancy()), e->stream);
+    launch_vertex_phase(e->d_table, e->d_one, n1, dt_real, 0, grid_for(e, n1, vertex_occupancy(e->vblock)), e->vblock,
+                        e->stream);
     size_t smem = patch_smem_bytes(e->prec, PP_FORCES, e->patch_emax);
     launch_patch(e->prec, PP_FORCES, e->d_table, e->d_one + n1, n2, e->patch_emax, dt_real, dt_real,
                  ap_threshold(c->prm, dt_real), std::numeric_limits<double>::quiet_NaN(), 0, nullptr, st, st + 3 * n,
@@ -1124,8 +1160,8 @@ int wcfe_engine_predict(wcfe_engine* e, double dt, double* x_pred) {
     if (r) return r;
     if ((r = ensure_dev(&e->d_xchg, &e->d_xchg_cap, 3 * (size_t)e->total_nv))) return r;
     const int n1 = (int)e->k1.size();
-    launch_vertex_phase(e->d_table, e->d_k1, n1, dt, VP_PREDICT | VP_EXPORT | VP_NOAREA, grid_for(e, n1, vertex_occupancy()),
-                        e->stream, nullptr, e->d_xchg);
+    vphase(e, e->d_table, e->d_k1, n1, dt, VP_PREDICT | VP_EXPORT | VP_NOAREA, grid_for(e, n1, vertex_occupancy(e->vblock)),
+           e->stream, nullptr, e->d_xchg);
     e->launches++;
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(x_pred, e->d_xchg, sizeof(double) * 3 * e->total_nv, cudaMemcpyDeviceToHost, e->stream));
@@ -1142,8 +1178,8 @@ int wcfe_engine_update(wcfe_engine* e, double dt, double dt_real, const double* 
     if ((r = ensure_dev(&e->d_xchg, &e->d_xchg_cap, 3 * (size_t)e->total_nv))) return r;
     CK(cudaMemcpyAsync(e->d_xchg, x_new, sizeof(double) * 3 * e->total_nv, cudaMemcpyHostToDevice, e->stream));
     const int n1 = (int)e->k1.size(), n2 = (int)e->k2.size();
-    launch_vertex_phase(e->d_table, e->d_k1, n1, dt_real, VP_IMPORT | VP_UPDATE_FA | rec_flag(e),
-                        grid_for(e, n1, vertex_occupancy()), e->stream, e->d_xchg, nullptr);
+    vphase(e, e->d_table, e->d_k1, n1, dt_real, VP_IMPORT | VP_UPDATE_FA | rec_flag(e), grid_for(e, n1, vertex_occupancy(e->vblock)),
+           e->stream, e->d_xchg, nullptr);
     size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
     launch_patch(e->prec, PP_STEP, e->d_table, e->d_k2, n2, e->patch_emax, dt, dt_real,
                  std::numeric_limits<double>::quiet_NaN(), std::numeric_limits<double>::quiet_NaN(), 1, nullptr, nullptr,
@@ -1196,8 +1232,8 @@ int wcfe_engine_autotune(wcfe_engine* e, double dt, int32_t reps) {
         CK(cudaMemcpyAsync(copy, c->state_block, c->state_bytes, cudaMemcpyDeviceToDevice, e->stream));
         saved.push_back({c, copy});
     }
-    const int threads_c[] = {64, 128, 256};
-    const int emax_c[] = {192, 256, 320, 384, 512, 768};
+    const int threads_c[] = {32, 64, 128, 256};
+    const int emax_c[] = {48, 64, 96, 128, 192, 256, 384, 512, 768};
     int max_optin = 0;
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
     float best = 1e30f;

@@ -70,8 +70,9 @@ __global__ void __launch_bounds__(kK1Threads) k_vertex_phase(const CellDev* __re
         double4* __restrict__ X = c.pos[par];
         double4* __restrict__ xo = c.pos[par ^ 1];
         // ---- vertices ----
-        const int v = b * kVB + threadIdx.x;
-        if (v < nv && threadIdx.x < kVB) {
+        const int VB = c.vb;
+        const int v = b * VB + threadIdx.x;
+        if (v < nv && (int)threadIdx.x < VB) {
             const double4 Xv = ld4(X + v);
             double xn[3];
             if (flags & VP_IMPORT) {
@@ -144,8 +145,8 @@ __global__ void __launch_bounds__(kK1Threads) k_vertex_phase(const CellDev* __re
         if (flags & VP_NOAREA) continue;
         // ---- area and area-weighted centroid of this block's elements ----
         double acc[4] = {0, 0, 0, 0};
-        const int e_end = min(nt, (b + 1) * kEB);
-        for (int e = b * kEB + threadIdx.x; e < e_end; e += blockDim.x) {
+        const int e_end = min(nt, (b + 1) * 2 * VB);
+        for (int e = b * 2 * VB + threadIdx.x; e < e_end; e += blockDim.x) {
             int4 t = __ldg(c.tri + e);
             double p[3][3];
             const int id[3] = {t.x, t.y, t.z};
@@ -164,8 +165,13 @@ __global__ void __launch_bounds__(kK1Threads) k_vertex_phase(const CellDev* __re
             }
             double e1x = p[1][0] - p[0][0], e1y = p[1][1] - p[0][1], e1z = p[1][2] - p[0][2];
             double e2x = p[2][0] - p[0][0], e2y = p[2][1] - p[0][1], e2z = p[2][2] - p[0][2];
-            double cx = 0.5 * (e1y * e2z - e1z * e2y), cy = 0.5 * (e1z * e2x - e1x * e2z), cz = 0.5 * (e1x * e2y - e1y * e2x);
-            double a = sqrt(cx * cx + cy * cy + cz * cz);
+            double a;
+            if (e1z == 0.0 && e2z == 0.0) {
+                a = fabs(0.5 * (e1x * e2y - e1y * e2x));  // planar element: the norm of (0, 0, cz) is |cz| exactly
+            } else {
+                double cx = 0.5 * (e1y * e2z - e1z * e2y), cy = 0.5 * (e1z * e2x - e1x * e2z), cz = 0.5 * (e1x * e2y - e1y * e2x);
+                a = sqrt(cx * cx + cy * cy + cz * cz);
+            }
             const double third = 1. / 3.;
             acc[0] += a;
             acc[1] += third * (p[0][0] + p[1][0] + p[2][0]) * a;
@@ -224,8 +230,9 @@ __device__ __forceinline__ void element_fp64(const double X[3][3], const double 
     double gc[3] = {g1[1] * g2[2] - g1[2] * g2[1], g1[2] * g2[0] - g1[0] * g2[2], g1[0] * g2[1] - g1[1] * g2[0]};
     double nG = sqrt(Gc[0] * Gc[0] + Gc[1] * Gc[1] + Gc[2] * Gc[2]);
     double ng = sqrt(gc[0] * gc[0] + gc[1] * gc[1] + gc[2] * gc[2]);
+    const double inG = 1.0 / nG, ing = 1.0 / ng;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) { N[k] = Gc[k] / nG; n[k] = gc[k] / ng; }
+    for (int k = 0; k < 3; ++k) { N[k] = Gc[k] * inG; n[k] = gc[k] * ing; }
 
     const double third = 1.0 / 3.0;
     double ev[6];
@@ -532,11 +539,11 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
             }
             const double Vo[3] = {V4.x, V4.y, V4.z};
             double An[3], Vn[3];
-            const double md = p.damp * MM * p.rho, mr = MM * p.rho;
+            const double md = p.damp * MM * p.rho, imr = 1.0 / (MM * p.rho), iMM = 1.0 / MM;
 #pragma unroll
             for (int r = 0; r < 3; ++r) {
                 double f = -p.drag * vh[r] + Fb[r] + Fap[r] + Ffa[r] + Far[r] - R[r];
-                An[r] = (f - md * Vo[r]) / mr;
+                An[r] = (f - md * Vo[r]) * imr;
             }
             const bool half = a.dt_real > a.dt / 2.0;
 #pragma unroll
@@ -544,9 +551,9 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
             const double2* eo = reinterpret_cast<const double2*>(eao + 6 * (size_t)v);
             double2* en = reinterpret_cast<double2*>(c.ea[par ^ 1] + 6 * (size_t)v);
             double2 e0 = eo[0], e1 = eo[1], e2 = eo[2];
-            double2 n0 = make_double2(e0.x + Rq[0] / MM, e0.y + Rq[1] / MM);
-            double2 n1 = make_double2(e1.x + Rq[2] / MM, e1.y + Rq[3] / MM);
-            double2 n2 = make_double2(e2.x + Rq[4] / MM, e2.y + Rq[5] / MM);
+            double2 n0 = make_double2(e0.x + Rq[0] * iMM, e0.y + Rq[1] * iMM);
+            double2 n1 = make_double2(e1.x + Rq[2] * iMM, e1.y + Rq[3] * iMM);
+            double2 n2 = make_double2(e2.x + Rq[4] * iMM, e2.y + Rq[5] * iMM);
             en[0] = n0; en[1] = n1; en[2] = n2;
             st4(c.acc + v, An[0], An[1], An[2]);
             st4(c.vel + v, Vn[0], Vn[1], Vn[2]);
@@ -588,9 +595,9 @@ __global__ void k_predict(const CellDev* __restrict__ cells, int cell, double dt
 // ---------------------------------------------------------------------------
 
 void launch_vertex_phase(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
-                         cudaStream_t st, const double* stage_in, double* stage_out) {
+                         int threads, cudaStream_t st, const double* stage_in, double* stage_out) {
     if (nwork <= 0) return;
-    k_vertex_phase<<<grid, kK1Threads, 0, st>>>(cells, work, nwork, dt, dt / 2.0, flags, stage_in, stage_out);
+    k_vertex_phase<<<grid, threads, 0, st>>>(cells, work, nwork, dt, dt / 2.0, flags, stage_in, stage_out);
 }
 
 // mixed-precision patch phase (wcfe_mixed.cu)
@@ -625,9 +632,9 @@ int patch_occupancy(int prec, int threads, size_t smem) {
 
 bool mixed_available() { return true; }
 
-int vertex_occupancy() {
+int vertex_occupancy(int threads) {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)k_vertex_phase, kK1Threads, 0) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)k_vertex_phase, threads, 0) != cudaSuccess) {
         cudaGetLastError();
         return 1;
     }

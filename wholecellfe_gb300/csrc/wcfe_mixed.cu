@@ -1,26 +1,34 @@
-// wcfe_mixed.cu — the mixed-precision patch phase (WCFE_PREC_MIXED).
+// wcfe_mixed.cu — the mixed-precision form (WCFE_PREC_MIXED) of the step.
 //
-// Element assembly runs in FP32 in an increment form of evalElementRe
-// (UL:710-928); the state, the per-vertex accumulation of boundary terms and
-// the explicit update stay in FP64.  With F = I + H, E the nodal-average
-// strain and P = I - N N, the reference's stress is rewritten exactly as
+// The cell is a planar membrane (z = 0) with counter-clockwise triangles, as
+// the reference's cell path is: read_ecomsol forces z = 0 (cellBP/iomesh.cpp:519)
+// and driverVelocities_Explicit zeroes the normal velocity (UL:119).  Then
+// N = n = e3 and every tensor of evalElementRe (UL:710-928) is an in-plane 2x2
+// block plus a decoupled zz entry; this form computes the 2x2 blocks.
+//
+// Element assembly runs in FP32 in an increment form that is algebraically the
+// reference's.  With F = I + H, E the integration-point strain and P the
+// in-plane identity, the stress is
 //     S_pas = mu [c0 P + beta / theta_g - theta_g (1 + eta) gamma]
 //     beta  = be_t - I   = 2 E (I - 2E)^-1
 //     gamma = C^-1 - I   = -c C^-1,  c = H + H^T + H^T H
 //     eta   = lambda_N^2 - 1 = (theta_g^2 (1 + de) - (1 + dth)^2) / (1 + dth)^2
 //     c0    = -(theta_g^2 - 1 + theta_g^2 eta) / theta_g
-// (de = det(I - 2E) - 1 and dth = det F - 1 from the invariants), so every
-// FP32 quantity is a small number carried at full relative precision instead
-// of a difference of two O(1) numbers.  The isotropic part kappa t_act I of the
-// active stress contributes w b_i per element corner; on a closed one-ring
-// these sum to exactly zero, so it is left out of the FP32 element and added in
-// FP64 for boundary vertices as (1/2) kappa t_act thick N x (X_end - X_start)
-// summed over the one-ring.  The strain update uses K = F^-1 - I = -H F^-1:
-//     ea_s = E + K^T E + E K + K^T E K - (K + K^T + K^T K)/2     (theta_g = 1)
+// with de = det(I - 2E) - 1 and dth = det F - 1 from the invariants.  Every
+// FP32 quantity is thus a small number at full relative precision, not a
+// difference of two O(1) numbers.  The isotropic active stress kappa t_act I
+// contributes w b_i per element corner; on a closed one-ring these sum to
+// exactly zero, so it stays out of the FP32 element and is added in FP64 for
+// boundary vertices: (1/2) kappa t_act thick e3 x sum (X_k - X_j).  The strain
+// update uses K = F^-1 - I = -H F^-1:
+//     ea_s - E = theta_g^2 D + (theta_g^2 - 1)(E - I/2),
+//     D = K^T E + E K + K^T E K - (K + K^T + K^T K)/2.
 //
-// The element inputs come from a per-vertex FP32 record written by the vertex
-// phase: positions as float-float (hi, lo), the step displacement u = x - X,
-// and the strain, so the element loop performs no FP64 arithmetic at all.
+// The vertex phase packs each vertex's element inputs into an FP32 record:
+// the position as float-float (hi, lo), the step displacement u = x - X and
+// the strain.  The element loop therefore does no FP64 arithmetic.  The state
+// and every accumulation (x, V, the strain, c_C, the bond vector) stay FP64; the
+// per-step force and acceleration are FP32.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -30,8 +38,6 @@
 
 namespace wcfe {
 
-struct PatchArgs;  // defined in wcfe_kernels.cu; the mixed kernel takes its own argument block
-
 struct MixedArgs {
     const CellDev* cells;
     const WorkItem* work;
@@ -40,218 +46,161 @@ struct MixedArgs {
     int vh_from_buf;
 };
 
+constexpr int kRec = 3;      // float4 per vertex record
+constexpr int kSlot32 = 20;  // floats per element slot in shared memory
 
-// 3x3 helpers in FP32 (row-major)
-__device__ __forceinline__ void adj3f(const float m[9], float o[9], float* det) {
-    float c00 = m[4] * m[8] - m[5] * m[7];
-    float c10 = m[5] * m[6] - m[3] * m[8];
-    float c20 = m[3] * m[7] - m[4] * m[6];
-    *det = c00 * m[0] + c10 * m[1] + c20 * m[2];
-    o[0] = c00; o[3] = c10; o[6] = c20;
-    o[1] = m[2] * m[7] - m[1] * m[8];
-    o[4] = m[0] * m[8] - m[2] * m[6];
-    o[7] = m[1] * m[6] - m[0] * m[7];
-    o[2] = m[1] * m[5] - m[2] * m[4];
-    o[5] = m[2] * m[3] - m[0] * m[5];
-    o[8] = m[0] * m[4] - m[1] * m[3];
-}
-__device__ __forceinline__ void mm3f(const float a[9], const float b[9], float o[9]) {
+// MD force-extension fit (UL:1203-1214) in FP32
+static __constant__ float c_md_px32[6] = {0.f, 2.51250583e-03f, 4.40265201e-03f, 5.91408228e-03f, 11.76817302e-03f, 17.001e-03f};
+static __constant__ float c_md_py32[6] = {-7.15514497f, 71.80501308f, 356.62420075f, 356.96656556f, 126.21811585f, 528.40481124f};
+static __constant__ float c_md_k32[6] = {31426.8556f, 99485.86235f, 67080.67086f, -7908.39043f, 21978.66923f, 76858.39733f};
+
+// Spring force of bond u in FP32 (UL:1245-1264; k1 UL:1259-1261; the polynomial extension)
+// and the Bell force magnitude of updateFA (UL:2137; k1 UL:2077).
+__device__ __forceinline__ void spring_force32(const wcfe_params& p, float ux, float uy, float uz, float fs[3],
+                                               float* bell) {
+    const float D = sqrtf(ux * ux + uy * uy + uz * uz);
+    const float k = (float)p.k_lin, L0 = (float)p.rest_len;
+    if (p.force_law == WCFE_LAW_LINEAR && p.rest_len == 0.0) {
+        fs[0] = k * ux; fs[1] = k * uy; fs[2] = k * uz;
+        *bell = p.linear_norm2d ? k * sqrtf(ux * ux + uy * uy) : k * D;
+        return;
+    }
+    const float iD = D != 0.0f ? 1.0f / D : 0.0f;
+    float mag = 0.0f;
+    if (p.force_law == WCFE_LAW_MD_TABLE) {
+        int j = -1;
+        if (D >= c_md_px32[5]) j = 5;
+        else {
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) o[i * 3 + j] = a[i * 3] * b[j] + a[i * 3 + 1] * b[3 + j] + a[i * 3 + 2] * b[6 + j];
-}
-// det(I + M) - 1 from the invariants of M
-__device__ __forceinline__ float detp1m1(const float m[9]) {
-    float tr = m[0] + m[4] + m[8];
-    float i2 = (m[0] * m[4] - m[1] * m[3]) + (m[0] * m[8] - m[2] * m[6]) + (m[4] * m[8] - m[5] * m[7]);
-    float d = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) + m[2] * (m[3] * m[7] - m[4] * m[6]);
-    return tr + i2 + d;
+            for (int q = 0; q < 5; ++q)
+                if (D < c_md_px32[q + 1] && D >= c_md_px32[q]) j = q;
+        }
+        if (j >= 0) mag = c_md_py32[j] + c_md_k32[j] * (D - c_md_px32[j]);
+    } else if (p.force_law == WCFE_LAW_LINEAR) {
+        mag = k * (D - L0);
+    } else {
+        const float e = D - L0, x0 = (float)p.poly_x0;
+        mag = (float)p.poly_k0 * (e + e * e * e / (3.0f * x0 * x0));
+    }
+    fs[0] = mag * ux * iD; fs[1] = mag * uy * iD; fs[2] = mag * uz * iD;
+    if (p.force_law == WCFE_LAW_LINEAR && p.linear_norm2d) *bell = fabsf(k * (sqrtf(ux * ux + uy * uy) - L0));
+    else *bell = fabsf(mag) * (D != 0.0f ? 1.0f : 0.0f);
 }
 
-// per-vertex record: float4 r0 = (Xhi.x, Xhi.y, Xhi.z, u.x), r1 = (Xlo.x, Xlo.y, Xlo.z, u.y),
-//                    r2 = (u.z, ea0, ea1, ea2), r3 = (ea3, ea4, ea5, 0)
-struct ElemOut32 {
-    float re[3][3];
-    float rea[3][6];
+struct ElemParams {   // per-cell constants of the element, hoisted out of the element loop
+    float mu, thick, grow, s_iso, t_an, cx, cy;
+};
+
+// planar element in the increment form; outputs per corner: Re (x, y), Re_ea (xx, yy, xy, zz)
+struct Elem2 {
+    float re[3][2];
+    float rea[3][4];
     float mm, acur;
 };
 
-__device__ __forceinline__ void element_mixed(const float4 r[3][4], const wcfe_params& p, float mu, float s_iso,
-                                              float t_an, float grow, const float cen[3], ElemOut32& o) {
-    float Xh[3][3], Xl[3][3], u[3][3], ea[3][6];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        Xh[k][0] = r[k][0].x; Xh[k][1] = r[k][0].y; Xh[k][2] = r[k][0].z;
-        Xl[k][0] = r[k][1].x; Xl[k][1] = r[k][1].y; Xl[k][2] = r[k][1].z;
-        u[k][0] = r[k][0].w; u[k][1] = r[k][1].w; u[k][2] = r[k][2].x;
-        ea[k][0] = r[k][2].y; ea[k][1] = r[k][2].z; ea[k][2] = r[k][2].w;
-        ea[k][3] = r[k][3].x; ea[k][4] = r[k][3].y; ea[k][5] = r[k][3].z;
-    }
-    float G1[3], G2[3], d1[3], d2[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        G1[k] = (Xh[1][k] - Xh[0][k]) + (Xl[1][k] - Xl[0][k]);
-        G2[k] = (Xh[2][k] - Xh[0][k]) + (Xl[2][k] - Xl[0][k]);
-        d1[k] = u[1][k] - u[0][k];
-        d2[k] = u[2][k] - u[0][k];
-    }
-    float Gc[3] = {G1[1] * G2[2] - G1[2] * G2[1], G1[2] * G2[0] - G1[0] * G2[2], G1[0] * G2[1] - G1[1] * G2[0]};
-    float nG = sqrtf(Gc[0] * Gc[0] + Gc[1] * Gc[1] + Gc[2] * Gc[2]);
-    float inG = 1.0f / nG;
-    float N[3] = {Gc[0] * inG, Gc[1] * inG, Gc[2] * inG};
-    // dual basis: G1inv = (G2 x N)/|GxG|, G2inv = (N x G1)/|GxG|
-    float b1[3] = {(G2[1] * N[2] - G2[2] * N[1]) * inG, (G2[2] * N[0] - G2[0] * N[2]) * inG, (G2[0] * N[1] - G2[1] * N[0]) * inG};
-    float b2[3] = {(N[1] * G1[2] - N[2] * G1[1]) * inG, (N[2] * G1[0] - N[0] * G1[2]) * inG, (N[0] * G1[1] - N[1] * G1[0]) * inG};
-    float g1[3] = {G1[0] + d1[0], G1[1] + d1[1], G1[2] + d1[2]};
-    float g2[3] = {G2[0] + d2[0], G2[1] + d2[1], G2[2] + d2[2]};
-    float gc[3] = {g1[1] * g2[2] - g1[2] * g2[1], g1[2] * g2[0] - g1[0] * g2[2], g1[0] * g2[1] - g1[1] * g2[0]};
-    float ng = sqrtf(gc[0] * gc[0] + gc[1] * gc[1] + gc[2] * gc[2]);
-    // n - N = dgc/ng - Gc (ng - nG)/(ng nG) with ng - nG = dgc.(gc + Gc)/(ng + nG): no cancellation
-    float dgc[3] = {gc[0] - Gc[0], gc[1] - Gc[1], gc[2] - Gc[2]};
-    float ing = 1.0f / ng;
-    float dng = (dgc[0] * (gc[0] + Gc[0]) + dgc[1] * (gc[1] + Gc[1]) + dgc[2] * (gc[2] + Gc[2])) / (ng + nG);
-    float dn[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) dn[k] = dgc[k] * ing - Gc[k] * (dng * ing * inG);
-    float H[9];
-#pragma unroll
-    for (int rr = 0; rr < 3; ++rr)
-#pragma unroll
-        for (int cc = 0; cc < 3; ++cc) H[rr * 3 + cc] = d1[rr] * b1[cc] + d2[rr] * b2[cc] + dn[rr] * N[cc];
+__device__ __forceinline__ void element2d(const float4 r[3][kRec], const ElemParams& q, Elem2& o) {
+    // r0 = (Xhi.x, Xhi.y, Xlo.x, Xlo.y), r1 = (u.x, u.y, exx, eyy), r2 = (exy, ezz, -, -)
+    const float G1x = (r[1][0].x - r[0][0].x) + (r[1][0].z - r[0][0].z);
+    const float G1y = (r[1][0].y - r[0][0].y) + (r[1][0].w - r[0][0].w);
+    const float G2x = (r[2][0].x - r[0][0].x) + (r[2][0].z - r[0][0].z);
+    const float G2y = (r[2][0].y - r[0][0].y) + (r[2][0].w - r[0][0].w);
+    const float d1x = r[1][1].x - r[0][1].x, d1y = r[1][1].y - r[0][1].y;
+    const float d2x = r[2][1].x - r[0][1].x, d2y = r[2][1].y - r[0][1].y;
+    const float Gc = G1x * G2y - G1y * G2x;  // > 0: counter-clockwise
+    const float iG = 1.0f / Gc;
+    // shape gradients in the reference configuration: b1 = (G2 x e3)/Gc, b2 = (e3 x G1)/Gc
+    const float b1x = G2y * iG, b1y = -G2x * iG;
+    const float b2x = -G1y * iG, b2y = G1x * iG;
+    const float b0x = -b1x - b2x, b0y = -b1y - b2y;
+    // H = d1 (x) b1 + d2 (x) b2
+    const float H00 = d1x * b1x + d2x * b2x, H01 = d1x * b1y + d2x * b2y;
+    const float H10 = d1y * b1x + d2y * b2x, H11 = d1y * b1y + d2y * b2y;
+    const float gc = (G1x + d1x) * (G2y + d2y) - (G1y + d1y) * (G2x + d2x);
     // strain at the integration point
     const float third = 1.0f / 3.0f;
-    float ev[6];
-#pragma unroll
-    for (int q = 0; q < 6; ++q) ev[q] = third * (ea[0][q] + ea[1][q] + ea[2][q]);
-    float E[9] = {ev[0], ev[3], ev[4], ev[3], ev[1], ev[5], ev[4], ev[5], ev[2]};
-    float M2[9], aM[9], dM;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) M2[k] = -2.0f * E[k];
-    M2[0] += 1.0f; M2[4] += 1.0f; M2[8] += 1.0f;
-    adj3f(M2, aM, &dM);
-    float idM = 1.0f / dM;
-    float Minv[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) Minv[k] = aM[k] * idM;
-    float beta[9];
-    mm3f(E, Minv, beta);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) beta[k] *= 2.0f;
-    float m2E[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) m2E[k] = -2.0f * E[k];
-    float de = detp1m1(m2E);
-    // C = I + c, c = H + H^T + H^T H
-    float cmat[9], Cm[9], aC[9], dC;
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-            cmat[i * 3 + j] = H[i * 3 + j] + H[j * 3 + i] + (H[i] * H[j] + H[3 + i] * H[3 + j] + H[6 + i] * H[6 + j]);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) Cm[k] = cmat[k];
-    Cm[0] += 1.0f; Cm[4] += 1.0f; Cm[8] += 1.0f;
-    adj3f(Cm, aC, &dC);
-    float idC = 1.0f / dC;
-    float Cinv[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) Cinv[k] = aC[k] * idC;
-    float gam[9];
-    mm3f(cmat, Cinv, gam);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) gam[k] = -gam[k];
-    float dth = detp1m1(H);
-    const float g = grow;            // theta_g - 1 = thetag_dot dt_real (UL:847)
-    const float thg = 1.0f + g;
-    float one_dth = 1.0f + dth;
-    float eta = ((2.0f * g + g * g) + thg * thg * de - 2.0f * dth - dth * dth) / (one_dth * one_dth);
-    float c0 = -((2.0f * g + g * g) + thg * thg * eta) / thg;
-    float S[9];
-#pragma unroll
-    for (int rr = 0; rr < 3; ++rr)
-#pragma unroll
-        for (int cc = 0; cc < 3; ++cc) {
-            float P = (rr == cc ? 1.0f : 0.0f) - N[rr] * N[cc];
-            S[rr * 3 + cc] = mu * (c0 * P + beta[rr * 3 + cc] / thg - thg * (1.0f + eta) * gam[rr * 3 + cc]);
-        }
-    // anisotropic active part t_act (1 - 2 kappa) a0 a0^T (zero for kappa = 1/2)
-    if (t_an != 0.0f) {
-        float a0[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-            a0[k] = third * ((Xh[0][k] + Xh[1][k] + Xh[2][k]) + (Xl[0][k] + Xl[1][k] + Xl[2][k]) +
-                             (u[0][k] + u[1][k] + u[2][k])) - cen[k];
-        float ia = rsqrtf(a0[0] * a0[0] + a0[1] * a0[1] + a0[2] * a0[2]);
-#pragma unroll
-        for (int rr = 0; rr < 3; ++rr)
-#pragma unroll
-            for (int cc = 0; cc < 3; ++cc) S[rr * 3 + cc] += t_an * (a0[rr] * ia) * (a0[cc] * ia);
+    const float exx = third * (r[0][1].z + r[1][1].z + r[2][1].z);
+    const float eyy = third * (r[0][1].w + r[1][1].w + r[2][1].w);
+    const float exy = third * (r[0][2].x + r[1][2].x + r[2][2].x);
+    const float ezz = third * (r[0][2].y + r[1][2].y + r[2][2].y);
+    // beta = 2 E (I - 2E)^-1 ; de = det(I - 2E) - 1 (with the zz factor 1 - 2 ezz)
+    const float m00 = 1.0f - 2.0f * exx, m11 = 1.0f - 2.0f * eyy, m01 = -2.0f * exy;
+    const float dm1 = -2.0f * (exx + eyy) + 4.0f * (exx * eyy - exy * exy);  // det(I - 2E_2) - 1
+    const float idM = 1.0f / (1.0f + dm1);
+    const float i00 = m11 * idM, i01 = -m01 * idM, i11 = m00 * idM;  // (I - 2E)^-1, symmetric
+    const float be00 = 2.0f * (exx * i00 + exy * i01), be01 = 2.0f * (exx * i01 + exy * i11);
+    const float be11 = 2.0f * (exy * i01 + eyy * i11);
+    const float de = dm1 - 2.0f * ezz * (1.0f + dm1);
+    // gamma = -c (I + c)^-1, c = H + H^T + H^T H
+    const float c00 = 2.0f * H00 + (H00 * H00 + H10 * H10);
+    const float c11 = 2.0f * H11 + (H01 * H01 + H11 * H11);
+    const float c01 = H01 + H10 + (H00 * H01 + H10 * H11);
+    const float dC = (1.0f + c00) * (1.0f + c11) - c01 * c01;
+    const float iC = 1.0f / dC;
+    const float ci00 = (1.0f + c11) * iC, ci01 = -c01 * iC, ci11 = (1.0f + c00) * iC;
+    const float ga00 = -(c00 * ci00 + c01 * ci01), ga01 = -(c00 * ci01 + c01 * ci11);
+    const float ga11 = -(c01 * ci01 + c11 * ci11);
+    // dth = det F - 1 = tr H + det H
+    const float dth = (H00 + H11) + (H00 * H11 - H01 * H10);
+    const float g = q.grow, thg = 1.0f + g, gg2 = 2.0f * g + g * g;
+    const float one_dth = 1.0f + dth;
+    const float eta = (gg2 + thg * thg * de - 2.0f * dth - dth * dth) / (one_dth * one_dth);
+    const float c0 = -(gg2 + thg * thg * eta) / thg;
+    const float ith = 1.0f / thg, tge = thg * (1.0f + eta);
+    float S00 = q.mu * (c0 + be00 * ith - tge * ga00);
+    float S01 = q.mu * (be01 * ith - tge * ga01);
+    float S11 = q.mu * (c0 + be11 * ith - tge * ga11);
+    if (q.t_an != 0.0f) {  // anisotropic active stress t_act (1 - 2 kappa) a0 a0^T
+        float ax = third * ((r[0][0].x + r[1][0].x + r[2][0].x) + (r[0][0].z + r[1][0].z + r[2][0].z) +
+                            (r[0][1].x + r[1][1].x + r[2][1].x)) - q.cx;
+        float ay = third * ((r[0][0].y + r[1][0].y + r[2][0].y) + (r[0][0].w + r[1][0].w + r[2][0].w) +
+                            (r[0][1].y + r[1][1].y + r[2][1].y)) - q.cy;
+        const float ia = rsqrtf(ax * ax + ay * ay);
+        ax *= ia; ay *= ia;
+        S00 += q.t_an * ax * ax; S01 += q.t_an * ax * ay; S11 += q.t_an * ay * ay;
     }
-    // T = s_iso H + (I + H) S   (the isotropic part s_iso I is handled per vertex in FP64)
-    float HS[9];
-    mm3f(H, S, HS);
-    float T[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) T[k] = s_iso * H[k] + S[k] + HS[k];
-    const float wA = 0.5f * nG * (float)p.thick;
-    float b0[3] = {-b1[0] - b2[0], -b1[1] - b2[1], -b1[2] - b2[2]};
-    const float* bb[3] = {b0, b1, b2};
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int rr = 0; rr < 3; ++rr) o.re[i][rr] = wA * (T[rr * 3] * bb[i][0] + T[rr * 3 + 1] * bb[i][1] + T[rr * 3 + 2] * bb[i][2]);
-    // strain: K = F^-1 - I = -H F^-1
-    float Fm[9], aF[9], dF;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) Fm[k] = H[k];
-    Fm[0] += 1.0f; Fm[4] += 1.0f; Fm[8] += 1.0f;
-    adj3f(Fm, aF, &dF);
-    float idF = 1.0f / dF;
-    float Finv[9];
-#pragma unroll
-    for (int k = 0; k < 9; ++k) Finv[k] = aF[k] * idF;
-    float K[9];
-    mm3f(H, Finv, K);
-#pragma unroll
-    for (int k = 0; k < 9; ++k) K[k] = -K[k];
-    float EK[9], KtE[9], KtEK[9], KtK[9];
-    mm3f(E, K, EK);
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            KtE[i * 3 + j] = K[i] * E[j] + K[3 + i] * E[3 + j] + K[6 + i] * E[6 + j];
-            KtK[i * 3 + j] = K[i] * K[j] + K[3 + i] * K[3 + j] + K[6 + i] * K[6 + j];
-        }
-    mm3f(KtE, K, KtEK);
-    float D[9];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j)
-            D[i * 3 + j] = KtE[i * 3 + j] + EK[i * 3 + j] + KtEK[i * 3 + j] - 0.5f * (K[i * 3 + j] + K[j * 3 + i] + KtK[i * 3 + j]);
-    // theta_g != 1: ea_s = (1 - thg^2)/2 I + thg^2 (E + D), written as E + [(1 - thg^2)/2 I + (thg^2 - 1) E + thg^2 D]
+    // T = s_iso H + (I + H) S
+    const float T00 = q.s_iso * H00 + S00 + (H00 * S00 + H01 * S01);
+    const float T01 = q.s_iso * H01 + S01 + (H00 * S01 + H01 * S11);
+    const float T10 = q.s_iso * H10 + S01 + (H10 * S00 + H11 * S01);
+    const float T11 = q.s_iso * H11 + S11 + (H10 * S01 + H11 * S11);
+    const float wA = 0.5f * Gc * q.thick;
+    o.re[0][0] = wA * (T00 * b0x + T01 * b0y); o.re[0][1] = wA * (T10 * b0x + T11 * b0y);
+    o.re[1][0] = wA * (T00 * b1x + T01 * b1y); o.re[1][1] = wA * (T10 * b1x + T11 * b1y);
+    o.re[2][0] = wA * (T00 * b2x + T01 * b2y); o.re[2][1] = wA * (T10 * b2x + T11 * b2y);
+    // strain: K = -H (I + H)^-1
+    const float iF = 1.0f / one_dth;  // det(I + H) = 1 + dth
+    const float f00 = (1.0f + H11) * iF, f01 = -H01 * iF, f10 = -H10 * iF, f11 = (1.0f + H00) * iF;
+    const float K00 = -(H00 * f00 + H01 * f10), K01 = -(H00 * f01 + H01 * f11);
+    const float K10 = -(H10 * f00 + H11 * f10), K11 = -(H10 * f01 + H11 * f11);
+    // E K and K^T E K
+    const float EK00 = exx * K00 + exy * K10, EK01 = exx * K01 + exy * K11;
+    const float EK10 = exy * K00 + eyy * K10, EK11 = exy * K01 + eyy * K11;
+    const float KEK00 = K00 * EK00 + K10 * EK10, KEK01 = K00 * EK01 + K10 * EK11;
+    const float KEK11 = K01 * EK01 + K11 * EK11;
+    const float KK00 = K00 * K00 + K10 * K10, KK01 = K00 * K01 + K10 * K11, KK11 = K01 * K01 + K11 * K11;
+    // D = K^T E + E K + K^T E K - (K + K^T + K^T K)/2; (K^T E)_ij = (E K)_ji
+    const float D00 = 2.0f * EK00 + KEK00 - 0.5f * (2.0f * K00 + KK00);
+    const float D11 = 2.0f * EK11 + KEK11 - 0.5f * (2.0f * K11 + KK11);
+    const float D01 = (EK10 + EK01) + KEK01 - 0.5f * (K01 + K10 + KK01);
     const float tg2 = thg * thg, gg = tg2 - 1.0f;
-    float dv[6] = {tg2 * D[0] + gg * (ev[0] - 0.5f), tg2 * D[4] + gg * (ev[1] - 0.5f), tg2 * D[8] + gg * (ev[2] - 0.5f),
-                   tg2 * D[1] + gg * ev[3], tg2 * D[2] + gg * ev[4], tg2 * D[5] + gg * ev[5]};
+    const float dvxx = tg2 * D00 + gg * (exx - 0.5f), dvyy = tg2 * D11 + gg * (eyy - 0.5f);
+    const float dvxy = tg2 * D01 + gg * exy, dvzz = gg * (ezz - 0.5f);
+    const float w3 = third * wA;
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int q = 0; q < 6; ++q) o.rea[i][q] = third * wA * ((ev[q] - ea[i][q]) + dv[q]);
-    o.mm = third * wA;
-    o.acur = 0.5f * ng;
+    for (int i = 0; i < 3; ++i) {
+        o.rea[i][0] = w3 * ((exx - r[i][1].z) + dvxx);
+        o.rea[i][1] = w3 * ((eyy - r[i][1].w) + dvyy);
+        o.rea[i][2] = w3 * ((exy - r[i][2].x) + dvxy);
+        o.rea[i][3] = w3 * ((ezz - r[i][2].y) + dvzz);
+    }
+    o.mm = w3;
+    o.acur = 0.5f * fabsf(gc);
 }
-
-constexpr int kSlot32 = 29;
 
 __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
     extern __shared__ float smf[];
     const int emax = a.emax;
-    float* s_re = smf;
-    float* s_rea = s_re + 9 * emax;
-    float* s_mm = s_rea + 18 * emax;
-    float* s_ac = s_mm + emax;
+    // structure of arrays: field k of slot j at smf[k * emax + j]
     __shared__ double s_red[4];
     for (int w = blockIdx.x; w < a.nwork; w += gridDim.x) {
         const WorkItem it = a.work[w];
@@ -278,160 +227,158 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
         }
         __syncthreads();
         const double area_tot = s_red[0];
-        const float cen[3] = {(float)s_red[1], (float)s_red[2], (float)s_red[3]};
         const double t = isnan(a.t_override) ? c.clk[0] : a.t_override;
         const unsigned long long ap_call = c.ap[0];
         const double t_act = t < p.tact_t1 ? t * p.tact_rate : p.tact_max;
         const double s_iso = p.kappa * t_act;
-        const float t_an = (float)((1.0 - 2.0 * p.kappa) * t_act);
+        ElemParams q;
+        q.mu = (float)p.mu;
+        q.thick = (float)p.thick;
+        q.grow = (float)(p.thetag_dot * a.dt_real);
+        q.s_iso = (float)s_iso;
+        q.t_an = (float)((1.0 - 2.0 * p.kappa) * t_act);
+        q.cx = (float)s_red[1];
+        q.cy = (float)s_red[2];
+        // ---- elements of the patch -> shared memory ----
         for (int j = threadIdx.x; j < pt.w; j += blockDim.x) {
             const int e = c.patch_elems[pt.z + j];
             const int4 t4 = __ldg(c.tri + e);
             const int id[3] = {t4.x, t4.y, t4.z};
-            float4 r[3][4];
+            float4 r[3][kRec];
 #pragma unroll
             for (int k = 0; k < 3; ++k)
 #pragma unroll
-                for (int q = 0; q < 4; ++q) r[k][q] = rec[4 * (size_t)id[k] + q];
-            ElemOut32 o;
-            element_mixed(r, p, (float)p.mu, (float)s_iso, t_an, (float)(p.thetag_dot * a.dt_real), cen, o);
+                for (int m = 0; m < kRec; ++m) r[k][m] = rec[kRec * (size_t)id[k] + m];
+            Elem2 o;
+            element2d(r, q, o);
 #pragma unroll
-            for (int k = 0; k < 3; ++k)
+            for (int k = 0; k < 3; ++k) {
+                smf[(2 * k + 0) * emax + j] = o.re[k][0];
+                smf[(2 * k + 1) * emax + j] = o.re[k][1];
 #pragma unroll
-                for (int rr = 0; rr < 3; ++rr) s_re[j * 9 + k * 3 + rr] = o.re[k][rr];
-#pragma unroll
-            for (int k = 0; k < 3; ++k)
-#pragma unroll
-                for (int q = 0; q < 6; ++q) s_rea[j * 18 + k * 6 + q] = o.rea[k][q];
-            s_mm[j] = o.mm;
-            s_ac[j] = o.acur;
+                for (int m = 0; m < 4; ++m) smf[(6 + 4 * k + m) * emax + j] = o.rea[k][m];
+            }
+            smf[18 * emax + j] = o.mm;
+            smf[19 * emax + j] = o.acur;
         }
         __syncthreads();
+        // ---- owned vertices: forces and the acceleration in FP32, accumulations in FP64 ----
+        const float drag = (float)p.drag, damp = (float)p.damp, rhom = (float)p.rho;
+        const double hdt = a.hdt, cdt = a.dt_real - a.dt / 2.0;
+        const bool half = a.dt_real > a.dt / 2.0;
         for (int i = threadIdx.x; i < pt.y; i += blockDim.x) {
             const int v = pt.x + i;
-            float R[3] = {0, 0, 0}, Rq[6] = {0, 0, 0, 0, 0, 0}, MMf = 0, Asf = 0;
+            float R0 = 0, R1 = 0, Q0 = 0, Q1 = 0, Q2 = 0, Q3 = 0, MMf = 0, Asf = 0;
             for (int k = c.vt_ptr[v]; k < c.vt_ptr[v + 1]; ++k) {
                 const int code = c.vc_code[k];
                 const int sl = code >> 2, cn = code & 3;
-#pragma unroll
-                for (int r = 0; r < 3; ++r) R[r] += s_re[sl * 9 + cn * 3 + r];
-#pragma unroll
-                for (int q = 0; q < 6; ++q) Rq[q] += s_rea[sl * 18 + cn * 6 + q];
-                MMf += s_mm[sl];
-                Asf += s_ac[sl];
+                R0 += smf[(2 * cn) * emax + sl];
+                R1 += smf[(2 * cn + 1) * emax + sl];
+                Q0 += smf[(6 + 4 * cn) * emax + sl];
+                Q1 += smf[(7 + 4 * cn) * emax + sl];
+                Q2 += smf[(8 + 4 * cn) * emax + sl];
+                Q3 += smf[(9 + 4 * cn) * emax + sl];
+                MMf += smf[18 * emax + sl];
+                Asf += smf[19 * emax + sl];
             }
-            const double MM = (double)MMf;
-            const double Asum = (double)Asf / 3.0;
-            const double4 xv4 = ld4v(xp + v);
-            const double xi[3] = {xv4.x, xv4.y, xv4.z};
-            double Rd[3] = {(double)R[0], (double)R[1], (double)R[2]};
+            const float Asum = Asf * (1.0f / 3.0f);
+            // integrin force (UL:1241-1269) in FP32
             const double4 f4 = ld4v(c.fau + v);
-            double fs[3], bell;
-            spring_force(p, f4.x, f4.y, f4.z, fs, &bell);
-            const double rho = c.rho_w ? c.rho_w[v] : p.rho_i_max;
-            const double cCv = c.cC[v];
-            double Ffa[3];
-#pragma unroll
-            for (int r = 0; r < 3; ++r) Ffa[r] = -cCv * fs[r] * Asum * rho;
-            double Fap[3] = {0, 0, 0}, Fb[3] = {0, 0, 0}, Far[3] = {0, 0, 0};
+            float fs[3], bell;
+            spring_force32(p, (float)f4.x, (float)f4.y, (float)f4.z, fs, &bell);
+            const float rho = c.rho_w ? (float)c.rho_w[v] : (float)p.rho_i_max;
+            const float kfa = -(float)c.cC[v] * Asum * rho;
+            float F0 = kfa * fs[0] - R0, F1 = kfa * fs[1] - R1;
             const int rank = c.bnd_rank[v];
             if (rank >= 0) {
-                // isotropic active stress on the open one-ring: (1/2) s_iso thick sum N x (X_k - X_j)
-                double sx = 0, sy = 0, sz = 0;
+                const double4 xv4 = ld4v(xp + v);
+                const double xi[3] = {xv4.x, xv4.y, xv4.z};
+                // isotropic active stress on the open one-ring: (1/2) s_iso thick e3 x sum (X_k - X_j)
+                double sx = 0, sy = 0;
                 for (int k = c.vt_ptr[v]; k < c.vt_ptr[v + 1]; ++k) {
                     const int code = c.vc_code[k];
                     const int cn = code & 3;
                     const int e = c.patch_elems[pt.z + (code >> 2)];
                     const int4 t4 = c.tri[e];
                     const int ids[3] = {t4.x, t4.y, t4.z};
-                    const double4 Xi = ld4v(X + ids[cn]);
                     const double4 Xj = ld4v(X + ids[(cn + 1) % 3]), Xk = ld4v(X + ids[(cn + 2) % 3]);
-                    // orientation of the element (its normal N = +-e3 for a planar membrane)
-                    const double oz = (Xj.x - Xi.x) * (Xk.y - Xi.y) - (Xj.y - Xi.y) * (Xk.x - Xi.x);
-                    const double sg = oz >= 0 ? 1.0 : -1.0;
-                    sx += sg * (Xk.x - Xj.x); sy += sg * (Xk.y - Xj.y); sz += sg * (Xk.z - Xj.z);
+                    sx += Xk.x - Xj.x;
+                    sy += Xk.y - Xj.y;
                 }
-                // planar membrane: N = e3, so N x (sx, sy) = (-sy, sx)
                 const double w = 0.5 * s_iso * p.thick;
-                Rd[0] += w * (-sy);
-                Rd[1] += w * sx;
-                (void)sz;
+                double Fb0 = w * sy, Fb1 = -w * sx;  // minus the residual term w e3 x s
                 double x1[3], x2[3];
                 if (boundary_frame(c, xp, rank, xi, x1, x2)) {
-                    double d1[3] = {xi[0] - x1[0], xi[1] - x1[1], xi[2] - x1[2]};
-                    double d2[3] = {x2[0] - xi[0], x2[1] - xi[1], x2[2] - xi[2]};
-                    double n1[3] = {d1[1], -d1[0], 0.0}, n2[3] = {d2[1], -d2[0], 0.0};
-                    double nn1 = sqrt(n1[0] * n1[0] + n1[1] * n1[1]), nn2 = sqrt(n2[0] * n2[0] + n2[1] * n2[1]);
-                    double l1 = sqrt(d1[0] * d1[0] + d1[1] * d1[1] + d1[2] * d1[2]);
-                    double l2 = sqrt(d2[0] * d2[0] + d2[1] * d2[1] + d2[2] * d2[2]);
-                    double L = l1 + l2;
-                    double nrm[3];
-#pragma unroll
-                    for (int r = 0; r < 3; ++r) nrm[r] = l1 / L * (n1[r] / nn1) + l2 / L * (n2[r] / nn2);
+                    const double d1x = xi[0] - x1[0], d1y = xi[1] - x1[1], d2x = x2[0] - xi[0], d2y = x2[1] - xi[1];
+                    const double d1z = xi[2] - x1[2], d2z = x2[2] - xi[2];
+                    const double nn1 = sqrt(d1y * d1y + d1x * d1x), nn2 = sqrt(d2y * d2y + d2x * d2x);
+                    const double l1 = sqrt(d1x * d1x + d1y * d1y + d1z * d1z), l2 = sqrt(d2x * d2x + d2y * d2y + d2z * d2z);
+                    const double L = l1 + l2;
+                    const double nx = l1 / L * (d1y / nn1) + l2 / L * (d2y / nn2);
+                    const double ny = l1 / L * (-d1x / nn1) + l2 / L * (-d2x / nn2);
+                    double fb = 0.0;
                     if (p.ap_enable) {
-                        uint32_t r31 = ap_draw(p.seed, p.stream, ap_call, (uint32_t)rank);
-                        double Pr = (double)r31 / ((double)2147483647 + 1.);
-                        double lim = p.ap_density * L / 2;
-                        double cnt = lim > 0 ? ceil(lim) : 0.0;
+                        const uint32_t r31 = ap_draw(p.seed, p.stream, ap_call, (uint32_t)rank);
+                        const double Pr = (double)r31 / ((double)2147483647 + 1.);
+                        const double lim = p.ap_density * L / 2;
+                        const double cnt = lim > 0 ? ceil(lim) : 0.0;
                         const double apt = isnan(a.ap_thresh) ? c.ap_thresh : a.ap_thresh;
-                        double fsc = (Pr < apt) ? p.ap_force * cnt : 0.0;
-#pragma unroll
-                        for (int r = 0; r < 3; ++r) Fap[r] = fsc * nrm[r];
+                        fb += (Pr < apt) ? p.ap_force * cnt : 0.0;
                     }
-                    double ed1[3] = {d1[0] / l1, d1[1] / l1, d1[2] / l1}, ed2[3] = {d2[0] / l2, d2[1] / l2, d2[2] / l2};
-                    double cost = ed1[0] * ed2[0] + ed1[1] * ed2[1] + ed1[2] * ed2[2];
-                    double ez = xs(xm(ed1[0], ed2[1]), xm(ed1[1], ed2[0]));
-                    double turna = ez > 0 ? cost - 1 : 1 - cost;
-                    double kap = turna * 2 / L;
-#pragma unroll
-                    for (int r = 0; r < 3; ++r) Fb[r] = p.k_bend * kap * nrm[r];
-                    double sc = -p.k_area * (area_tot - p.area0) / 2 * L;
-#pragma unroll
-                    for (int r = 0; r < 3; ++r) Far[r] = sc * nrm[r];
+                    const double e1x = d1x / l1, e1y = d1y / l1, e1z = d1z / l1, e2x = d2x / l2, e2y = d2y / l2, e2z = d2z / l2;
+                    const double cost = e1x * e2x + e1y * e2y + e1z * e2z;
+                    const double ez = xs(xm(e1x, e2y), xm(e1y, e2x));
+                    const double turna = ez > 0 ? cost - 1 : 1 - cost;
+                    fb += p.k_bend * (turna * 2 / L);
+                    fb += -p.k_area * (area_tot - p.area0) / 2 * L;
+                    Fb0 += fb * nx;
+                    Fb1 += fb * ny;
                 }
+                F0 += (float)Fb0;
+                F1 += (float)Fb1;
             }
+            // explicit update (UL:592-628): A in FP32 from the FP32 force; V and the strain in FP64
             const double4 V4 = ld4v(c.vel + v), A4 = ld4v(c.acc + v);
-            double vh[3];
+            double vh0, vh1;
             if (a.vh_from_buf) {
-                double4 h = ld4v(c.vhl + v);
-                vh[0] = h.x; vh[1] = h.y; vh[2] = h.z;
+                const double4 h = ld4v(c.vhl + v);
+                vh0 = h.x; vh1 = h.y;
             } else {
-                const double4 Xv = ld4v(X + v);
-                vh[0] = xa(V4.x, xm(a.hdt, A4.x));
-                vh[1] = xa(V4.y, xm(a.hdt, A4.y));
-                vh[2] = 0.0;
-                (void)Xv;
+                vh0 = fma(hdt, A4.x, V4.x);
+                vh1 = fma(hdt, A4.y, V4.y);
             }
-            const double Vo[3] = {V4.x, V4.y, V4.z};
-            double An[3], Vn[3];
-            const double md = p.damp * MM * p.rho, mr = MM * p.rho;
-#pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                double f = -p.drag * vh[r] + Fb[r] + Fap[r] + Ffa[r] + Far[r] - Rd[r];
-                An[r] = (f - md * Vo[r]) / mr;
+            const float iM = 1.0f / (MMf * rhom);
+            const float damp_m = damp * MMf * rhom;
+            const float An0 = (F0 - drag * (float)vh0 - damp_m * (float)V4.x) * iM;
+            const float An1 = (F1 - drag * (float)vh1 - damp_m * (float)V4.y) * iM;
+            const float An2 = (-damp_m * (float)V4.z) * iM;  // no force normal to the plane
+            double Vn0, Vn1, Vn2;
+            if (half) {
+                Vn0 = fma(cdt, (double)An0, vh0);
+                Vn1 = fma(cdt, (double)An1, vh1);
+                Vn2 = cdt * (double)An2;
+            } else {
+                Vn0 = fma(a.dt_real, (double)An0, V4.x);
+                Vn1 = fma(a.dt_real, (double)An1, V4.y);
+                Vn2 = fma(a.dt_real, (double)An2, V4.z);
             }
-            const bool half = a.dt_real > a.dt / 2.0;
-#pragma unroll
-            for (int r = 0; r < 3; ++r) Vn[r] = half ? vh[r] + (a.dt_real - a.dt / 2.0) * An[r] : Vo[r] + a.dt_real * An[r];
-            const double* eao = c.ea[par] + 6 * (size_t)v;
-            double* en = c.ea[par ^ 1] + 6 * (size_t)v;
-            const float iM = 1.0f / MMf;
-            double chk = 0;
-#pragma unroll
-            for (int q = 0; q < 6; ++q) {
-                double nv = eao[q] + (double)(Rq[q] * iM);
-                en[q] = nv;
-                chk += nv;
-            }
-            st4(c.acc + v, An[0], An[1], An[2]);
-            st4(c.vel + v, Vn[0], Vn[1], Vn[2]);
-            chk += An[0] + An[1] + An[2] + Vn[0] + Vn[1] + Vn[2] + xi[0] + xi[1];
+            const double2* eo = reinterpret_cast<const double2*>(c.ea[par] + 6 * (size_t)v);
+            double2* en = reinterpret_cast<double2*>(c.ea[par ^ 1] + 6 * (size_t)v);
+            const float iMM = 1.0f / MMf;
+            const double2 e0 = eo[0], e1 = eo[1], e2 = eo[2];  // (xx, yy), (zz, xy), (xz, yz)
+            en[0] = make_double2(e0.x + (double)(Q0 * iMM), e0.y + (double)(Q1 * iMM));
+            en[1] = make_double2(e1.x + (double)(Q3 * iMM), e1.y + (double)(Q2 * iMM));
+            en[2] = e2;
+            st4(c.acc + v, (double)An0, (double)An1, (double)An2);
+            st4(c.vel + v, Vn0, Vn1, Vn2);
+            // NaN/Inf in the state shows up in the FP32 quantities derived from it
+            const float chk = An0 + An1 + Q0 + Q1 + Q2 + (float)vh0 + (float)vh1;
             if (!isfinite(chk)) atomicOr(c.status, 1u);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             __threadfence();
-            unsigned int done = atomicAdd(reinterpret_cast<unsigned int*>(c.ctl + 1), 1u);
+            const unsigned int done = atomicAdd(reinterpret_cast<unsigned int*>(c.ctl + 1), 1u);
             if ((int)done == c.np - 1) {
                 c.ctl[1] = 0;
                 c.ctl[0] = par ^ 1;
@@ -440,6 +387,165 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             }
         }
     }
+}
+
+// ===========================================================================
+// mixed-form vertex phase: predict (FP64), bond kinetics with FP32 rates and
+// FP64 accumulation, the FP32 element records, and the cell area and
+// area-weighted centroid from the boundary loop (shoelace over the directed
+// boundary edges).  For a planar mesh without inverted elements that equals
+// calculateAreaTot's sum of element areas.
+// ===========================================================================
+enum { VM_PREDICT = 1, VM_UPDATE_FA = 2, VM_EXPORT = 8, VM_IMPORT = 16, VM_NOAREA = 32 };
+
+__device__ __forceinline__ void predict_mixed(const double4& X, const double4& V, const double4& A, double dt,
+                                              double hdt, double vh[2], double xn[3]) {
+    vh[0] = fma(hdt, A.x, V.x);
+    vh[1] = fma(hdt, A.y, V.y);
+    xn[0] = fma(dt, vh[0], X.x);
+    xn[1] = fma(dt, vh[1], X.y);
+    xn[2] = X.z;  // V_hlf.z = 0 (UL:119)
+}
+
+__global__ void __launch_bounds__(kK1Threads) k_vertex_phase_mixed(const CellDev* __restrict__ cells,
+                                                                 const WorkItem* __restrict__ work, int nwork,
+                                                                 double dt, double hdt, int flags,
+                                                                 const double* __restrict__ stage_in,
+                                                                 double* __restrict__ stage_out) {
+    __shared__ double red[3 * kK1Threads];
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const WorkItem it = work[w];
+        const CellDev& c = cells[it.cell];
+        const int b = it.idx;
+        const int par = c.ctl[0];
+        const double4* __restrict__ X = c.pos[par];
+        double4* __restrict__ xo = c.pos[par ^ 1];
+        const int v = b * c.vb + threadIdx.x;
+        double acc[3] = {0, 0, 0};
+        bool has = false;
+        if (v < c.nv) {
+            const double4 Xv = ld4(X + v);
+            double xn[3];
+            if (flags & VM_IMPORT) {
+                const double* qq = stage_in + 3 * (size_t)(c.hoff + v);
+                xn[0] = qq[0]; xn[1] = qq[1]; xn[2] = qq[2];
+                st4(xo + v, xn[0], xn[1], xn[2]);
+            } else if (flags & VM_PREDICT) {
+                double vh[2];
+                predict_mixed(Xv, ld4(c.vel + v), ld4(c.acc + v), dt, hdt, vh, xn);
+                st4(xo + v, xn[0], xn[1], xn[2]);
+                if (flags & VM_EXPORT) {
+                    st4(c.vhl + v, vh[0], vh[1], 0.0);
+                    double* qq = stage_out + 3 * (size_t)(c.hoff + v);
+                    qq[0] = xn[0]; qq[1] = xn[1]; qq[2] = xn[2];
+                }
+            } else {
+                const double4 t = ld4v(xo + v);
+                xn[0] = t.x; xn[1] = t.y; xn[2] = t.z;
+            }
+            const double cu0 = xn[0] - Xv.x, cu1 = xn[1] - Xv.y;  // exact differences
+            if (flags & VM_UPDATE_FA) {
+                const wcfe_params& p = c.prm;
+                const double4 f = ld4v(c.fau + v);
+                double su0 = 0, su1 = 0, su2 = 0;
+                if (c.has_sub && c.sub.moving) {
+                    double wgt[3];
+                    const int e = locate(c.sub, xs(Xv.x, f.x), xs(Xv.y, f.y), xs(Xv.z, f.z), wgt);
+                    if (e >= 0) {
+                        const int4 t = c.sub.tri[e];
+                        const double4 a0 = ld4(c.sub.x + t.x), a1 = ld4(c.sub.x + t.y), a2 = ld4(c.sub.x + t.z);
+                        const double4 b0 = ld4(c.sub.X + t.x), b1 = ld4(c.sub.X + t.y), b2 = ld4(c.sub.X + t.z);
+                        su0 = wgt[0] * (a0.x - b0.x) + wgt[1] * (a1.x - b1.x) + wgt[2] * (a2.x - b2.x);
+                        su1 = wgt[0] * (a0.y - b0.y) + wgt[1] * (a1.y - b1.y) + wgt[2] * (a2.y - b2.y);
+                        su2 = wgt[0] * (a0.z - b0.z) + wgt[1] * (a1.z - b1.z) + wgt[2] * (a2.z - b2.z);
+                    }
+                }
+                const double u0 = (f.x + cu0) - su0, u1 = (f.y + cu1) - su1, u2 = f.z - su2;
+                float fs[3], force;
+                spring_force32(p, (float)u0, (float)u1, (float)u2, fs, &force);
+                const float koff = (float)p.ka * __expf(force / (float)p.Fa) + (float)p.kb * __expf(-force / (float)p.Fb);
+                const double cold = c.cC[v];
+                const float coldf = (float)cold, dtf = (float)dt, kon = (float)p.k_on;
+                double cn = cold + (double)(dtf * (kon * (1.0f - coldf) - koff * coldf));
+                if (cn < 0) cn = 0;
+                if (c.cA[v] < 0) c.cA[v] = 0;
+                double n0, n1, n2;
+                const bool keep_pos = cold > 0 && (1.0f - dtf * koff) > 0.0f;
+                if (keep_pos && cn > 0) {
+                    // keep / c_new = 1 + ds with ds = -dt k_on (1 - c_old) / c_new exactly
+                    const double ds = (double)(-dtf * kon * (1.0f - coldf) / (float)cn);
+                    n0 = fma(u0, ds, u0); n1 = fma(u1, ds, u1); n2 = fma(u2, ds, u2);
+                } else {
+                    n0 = 0.0 * u0; n1 = 0.0 * u1; n2 = 0.0 * u2;
+                }
+                c.cC[v] = cn;
+                st4(c.fau + v, n0, n1, n2);
+            }
+            if (!(flags & VM_EXPORT)) {
+                const float hx = (float)Xv.x, hy = (float)Xv.y;
+                const float lx = (float)(Xv.x - (double)hx), ly = (float)(Xv.y - (double)hy);
+                const double2* e2 = reinterpret_cast<const double2*>(c.ea[par] + 6 * (size_t)v);
+                const double2 q0 = e2[0], q1 = e2[1];  // (xx, yy), (zz, xy)
+                float4* r = c.rec + kRec * (size_t)v;
+                r[0] = make_float4(hx, hy, lx, ly);
+                r[1] = make_float4((float)cu0, (float)cu1, (float)q0.x, (float)q0.y);
+                r[2] = make_float4((float)q1.y, (float)q1.x, 0.0f, 0.0f);
+            }
+            const int rank = c.bnd_rank[v];
+            if (!(flags & VM_NOAREA) && rank >= 0) {
+                for (int k = c.bnd_optr[rank]; k < c.bnd_optr[rank + 1]; ++k) {
+                    const int j = c.bnd_out[k];
+                    double xj[3];
+                    if (flags & VM_IMPORT) {
+                        const double* qq = stage_in + 3 * (size_t)(c.hoff + j);
+                        xj[0] = qq[0]; xj[1] = qq[1];
+                    } else if (flags & VM_PREDICT) {
+                        double vhj[2];
+                        predict_mixed(ld4(X + j), ld4(c.vel + j), ld4(c.acc + j), dt, hdt, vhj, xj);
+                    } else {
+                        const double4 t = ld4v(xo + j);
+                        xj[0] = t.x; xj[1] = t.y;
+                    }
+                    const double cr = xn[0] * xj[1] - xj[0] * xn[1];
+                    acc[0] += 0.5 * cr;
+                    acc[1] += (1.0 / 6.0) * (xn[0] + xj[0]) * cr;
+                    acc[2] += (1.0 / 6.0) * (xn[1] + xj[1]) * cr;
+                    has = true;
+                }
+            }
+        }
+        if (flags & VM_NOAREA) continue;
+        // block partial over its boundary edges, fixed order, only in blocks that have any
+        if (__syncthreads_or(has)) {
+            for (int k = 0; k < 3; ++k) red[3 * threadIdx.x + k] = acc[k];
+            __syncthreads();
+            if (threadIdx.x < 32) {
+                double s[3] = {0, 0, 0};
+                for (int t = threadIdx.x; t < (int)blockDim.x; t += 32)
+                    for (int k = 0; k < 3; ++k) s[k] += red[3 * t + k];
+#pragma unroll
+                for (int k = 0; k < 3; ++k)
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
+                if (threadIdx.x == 0) {
+                    c.k1_part[4 * b + 0] = s[0];
+                    c.k1_part[4 * b + 1] = s[1];
+                    c.k1_part[4 * b + 2] = s[2];
+                    c.k1_part[4 * b + 3] = 0.0;
+                }
+            }
+        } else if (threadIdx.x == 0) {
+            c.k1_part[4 * b + 0] = 0.0; c.k1_part[4 * b + 1] = 0.0;
+            c.k1_part[4 * b + 2] = 0.0; c.k1_part[4 * b + 3] = 0.0;
+        }
+        __syncthreads();
+    }
+}
+
+void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
+                         int threads, cudaStream_t st, const double* stage_in, double* stage_out) {
+    if (nwork <= 0) return;
+    k_vertex_phase_mixed<<<grid, threads, 0, st>>>(cells, work, nwork, dt, dt / 2.0, flags, stage_in, stage_out);
 }
 
 size_t mixed_smem_bytes(int emax) { return sizeof(float) * (size_t)emax * kSlot32; }

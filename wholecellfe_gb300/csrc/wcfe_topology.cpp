@@ -84,6 +84,30 @@ std::string build_topology(Topology& T, int32_t nv, int32_t nt, const int32_t* t
         T.bnd_cptr.push_back((int32_t)(T.bnd_cand.size() / 2));
     }
     T.nb = nb;
+    // directed boundary edges: an edge of odd triangle count, oriented as in its triangle
+    {
+        std::unordered_map<int64_t, int32_t> ecount;
+        ecount.reserve(3 * (size_t)nt);
+        for (int t = 0; t < nt; ++t)
+            for (int a = 0; a < 3; ++a) {
+                int64_t u = T.tri[3 * t + a], w = T.tri[3 * t + (a + 1) % 3];
+                if (u > w) std::swap(u, w);
+                ecount[u * nv + w]++;
+            }
+        std::vector<std::vector<int32_t>> outs(nb);
+        for (int t = 0; t < nt; ++t)
+            for (int a = 0; a < 3; ++a) {
+                int32_t u = T.tri[3 * t + a], w = T.tri[3 * t + (a + 1) % 3];
+                int64_t lo = std::min(u, w), hi = std::max(u, w);
+                if (ecount[lo * nv + hi] % 2 && T.bnd_rank[u] >= 0) outs[T.bnd_rank[u]].push_back(w);
+            }
+        T.bnd_optr.assign(1, 0);
+        T.bnd_out.clear();
+        for (int r = 0; r < nb; ++r) {
+            T.bnd_out.insert(T.bnd_out.end(), outs[r].begin(), outs[r].end());
+            T.bnd_optr.push_back((int32_t)T.bnd_out.size());
+        }
+    }
     return "";
 }
 

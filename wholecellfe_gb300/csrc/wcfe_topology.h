@@ -17,6 +17,8 @@ struct Topology {
     std::vector<int32_t> bnd_rank;   // [nv] index among boundary vertices in vertex order, -1 interior
     std::vector<int32_t> bnd_cptr;   // [nb+1]
     std::vector<int32_t> bnd_cand;   // [2 * bnd_cptr[nb]] (nj, nint) pairs, UL:1500-1531 scan order
+    std::vector<int32_t> bnd_optr;   // [nb+1] directed boundary edges leaving each boundary vertex
+    std::vector<int32_t> bnd_out;    // their end vertices (edge direction as in its triangle)
 };
 
 struct Patches {
