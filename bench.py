@@ -340,6 +340,9 @@ def run_ours(args):
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
                     "avg_launch_ms": round(avg_p, 4), "vertex_phase_avg_launch_ms": round(avg_v, 4)}
 
+        serving = run_serving(args.serve_seconds) if args.serve_seconds > 0 else None
+        if serving:
+            log(f"[bench] serving: {serving}")
         cpu = cpu_baseline(cells, args.steps) if not args.no_cpu else None
         out = {
             "metric": METRIC, "value": round(value, 1), "unit": "cell-steps/s", "n_gpus": world,
@@ -362,7 +365,7 @@ def run_ours(args):
             "ratio_vs_plain_fp64": round(value / world / plain_value, 2),
             "mixed_vs_fp64_rel_displacement_error": max_err, "error_steps": err_steps,
             "element_assemblies_per_s": round(value / len(cells) * nt_total / world, 1),
-            "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "serving": serving,
             "clocks": clocks_info,
         }
     if dist:
@@ -370,6 +373,80 @@ def run_ours(args):
         dist.destroy_process_group()
     if out:
         print(json.dumps(out), flush=True)
+
+
+def run_serving(seconds: float, rate: float = 200.0, budget_gb: float = 16.0, seed: int = 7):
+    """Config 5, bounded: Poisson arrivals (rate per second) of cell simulations with 1k-50k
+    vertices (log-uniform), 50-2000 steps (uniform) and a random stiffness model, admitted by
+    an HBM budget into one mixed-precision engine (wcfe_server_*).  Arrivals stop after
+    `seconds`; the loop then drains.  Meshes come from a pool of 24 seeded disks."""
+    import ctypes as C
+    from wholecellfe_gb300 import capi, synth
+    from wholecellfe_gb300.params import default_params
+    L = capi.load()
+    rng = np.random.default_rng(seed)
+    pool = []
+    for i in range(24):
+        n = int(round(math.exp(rng.uniform(math.log(1000), math.log(50000)))))
+        x0, tri = synth.disk_mesh(n, seed=9000 + i)
+        pool.append((np.ascontiguousarray(x0), np.ascontiguousarray(tri, np.int32)))
+    params = []
+    for law in range(3):
+        p = default_params("k31" if law else "k1")
+        if law == 2:
+            p.force_law, p.poly_k0, p.poly_x0, p.linear_norm2d = 2, 31000.0, 0.005, 0
+        params.append(p)
+    eng = capi.Engine(capi.PREC_MIXED, budget_bytes=int(budget_gb * 2**30))
+    srv = C.c_void_p()
+    capi.check(L.wcfe_server_create(eng.h, DT, C.byref(srv)), "wcfe_server_create")
+    keep, ids, steps_of, nv_of = [], [], [], []
+    t0 = time.perf_counter()
+    next_arrival = rng.exponential(1.0 / rate)
+    na, nq = C.c_int32(), C.c_int32()
+    cell_steps = 0
+    active_hist = []
+    while True:
+        now = time.perf_counter() - t0
+        while next_arrival <= now and next_arrival < seconds:
+            x0, tri = pool[int(rng.integers(0, len(pool)))]
+            p = params[int(rng.integers(0, 3))]
+            steps = int(rng.integers(50, 2001))
+            rq = capi.Request(len(x0), len(tri), capi.ip(tri), capi.dp(x0), C.pointer(p), steps, None, None, 0, 0)
+            rid = C.c_int64()
+            capi.check(L.wcfe_server_submit(srv, C.byref(rq), C.byref(rid)), "wcfe_server_submit")
+            ids.append(rid.value)
+            steps_of.append(steps)
+            nv_of.append(len(x0))
+            next_arrival += rng.exponential(1.0 / rate)
+        capi.check(L.wcfe_server_iterate(srv, C.byref(na), C.byref(nq)), "wcfe_server_iterate")
+        active_hist.append(na.value)
+        if now >= seconds and na.value == 0 and nq.value == 0:
+            break
+        if now > seconds + 120:   # drain bound
+            break
+    wall = time.perf_counter() - t0
+    n = L.wcfe_server_step_times(srv, None, 0)
+    buf = (C.c_double * max(n, 1))()
+    L.wcfe_server_step_times(srv, buf, n)
+    it_ms = [b * 1e3 for b in list(buf)[:n]]
+    lat = []
+    done_steps = 0
+    for rid, st in zip(ids, steps_of):
+        t = C.c_double()
+        if L.wcfe_server_result(srv, rid, None, C.byref(t)) == 0:
+            lat.append(t.value)
+            done_steps += st
+    L.wcfe_server_destroy(srv)
+    eng.close()
+    return {"arrival_rate_per_s": rate, "arrival_seconds": seconds, "requests": len(ids), "completed": len(lat),
+            "vertices_per_request": "log-uniform [1000, 50000] (pool of 24 meshes)", "steps_per_request": "uniform [50, 2000]",
+            "hbm_budget_gb": budget_gb, "wall_s": round(wall, 2),
+            "cell_steps_per_s": round(done_steps / wall, 1),
+            "p50_step_ms": round(percentile(it_ms, 0.5), 4) if it_ms else None,
+            "p99_step_ms": round(percentile(it_ms, 0.99), 4) if it_ms else None,
+            "p50_request_s": round(percentile(lat, 0.5), 3) if lat else None,
+            "p99_request_s": round(percentile(lat, 0.99), 3) if lat else None,
+            "max_resident_cells": max(active_hist) if active_hist else 0}
 
 
 def run_phase(args):
@@ -446,6 +523,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells", type=int, default=N_CELLS)
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
+                    help="length of the Poisson arrival window of the serving measurement (0: skip)")
     ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain"],
                     help="profiling aid: run only one timed loop (default shape, no autotune) and print its timing")
     args = ap.parse_args()

@@ -22,6 +22,12 @@ _i = C.POINTER(C.c_int32)
 _u8 = C.POINTER(C.c_uint8)
 PREC_FP64, PREC_MIXED = 0, 1
 
+class Request(C.Structure):
+    _fields_ = [("n_vert", C.c_int32), ("n_tri", C.c_int32), ("tri", _i), ("x", _d), ("params", C.POINTER(Params)),
+                ("n_steps", C.c_int32), ("sub_tri", _i), ("sub_X", _d), ("sub_n_vert", C.c_int32),
+                ("sub_n_tri", C.c_int32)]
+
+
 # exported symbols and their signatures (checked against include/wcfe.h by the tests)
 SIGNATURES = {
     "wcfe_params_default": (None, [C.POINTER(Params), C.c_int32]),
@@ -68,7 +74,7 @@ SIGNATURES = {
     "wcfe_cell_set_integrins": (C.c_int, [C.c_void_p, C.c_int32, _d]),
     "wcfe_server_create": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_void_p)]),
     "wcfe_server_destroy": (C.c_int, [C.c_void_p]),
-    "wcfe_server_submit": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int64)]),
+    "wcfe_server_submit": (C.c_int, [C.c_void_p, C.POINTER(Request), C.POINTER(C.c_int64)]),
     "wcfe_server_iterate": (C.c_int, [C.c_void_p, _i, _i]),
     "wcfe_server_result": (C.c_int, [C.c_void_p, C.c_int64, _d, _d]),
     "wcfe_server_step_times": (C.c_int64, [C.c_void_p, _d, C.c_int64]),
@@ -145,12 +151,6 @@ def f64(a):
 
 def i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
-
-
-class Request(C.Structure):
-    _fields_ = [("n_vert", C.c_int32), ("n_tri", C.c_int32), ("tri", _i), ("x", _d), ("params", C.POINTER(Params)),
-                ("n_steps", C.c_int32), ("sub_tri", _i), ("sub_X", _d), ("sub_n_vert", C.c_int32),
-                ("sub_n_tri", C.c_int32)]
 
 
 class Engine:
