@@ -142,4 +142,35 @@ __device__ __forceinline__ bool boundary_frame(const CellDev& c, const double4* 
     return true;
 }
 
+
+// The last vertex-phase block of a cell (an atomic ticket in ctl[2]) reduces the
+// cell's per-block area partials in a fixed order into area4 = {A, cx, cy, cz}.
+__device__ __forceinline__ void finish_area(const CellDev& c) {
+    __shared__ int s_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned int t = atomicAdd(reinterpret_cast<unsigned int*>(c.ctl + 2), 1u);
+        s_last = ((int)t == c.nk1 - 1);
+    }
+    __syncthreads();
+    if (s_last && threadIdx.x < 32) {
+        double s4[4] = {0, 0, 0, 0};
+        for (int k = threadIdx.x; k < c.nk1; k += 32)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) s4[q] += __ldcg(c.k1_part + 4 * k + q);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s4[q] += __shfl_xor_sync(0xffffffffu, s4[q], o);
+        if (threadIdx.x == 0) {
+            c.area4[0] = s4[0];
+            c.area4[1] = s4[1] / s4[0];
+            c.area4[2] = s4[2] / s4[0];
+            c.area4[3] = s4[3] / s4[0];
+            c.ctl[2] = 0;
+        }
+    }
+}
+
 }  // namespace wcfe

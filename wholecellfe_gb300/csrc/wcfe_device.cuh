@@ -32,6 +32,17 @@ struct SubDev {                 // substrate mesh + uniform grid for point locat
     int32_t moving;             // 0: x == X (rigid), the interpolated displacement is exactly 0
 };
 
+// FP32 copies of the per-cell constants the mixed form uses per vertex, converted
+// once on the host so that the kernels do no FP64 -> FP32 parameter conversions.
+enum { PF_LINEAR0 = 0, PF_MD = 1, PF_LINEAR = 2, PF_POLY = 3 };
+struct ParamF {
+    float k_lin, rest_len, poly_k0, poly_c3;   // poly_c3 = 1 / (3 x0^2)
+    float ka, kb, iFa, iFb, k_on, rho_i_max;
+    float drag, damp, rho;
+    int32_t law;                               // PF_*: linear with zero rest length, MD table, linear, polynomial
+    int32_t norm2d;
+};
+
 struct CellDev {
     int32_t nv, nt, nb, np, nk1;
     int32_t vb;                 // vertices per vertex-phase block (= its thread count); 2 vb elements per block
@@ -57,16 +68,42 @@ struct CellDev {
     const int32_t* bnd_optr;    // [nb+1] directed boundary edges leaving each boundary vertex
     const int32_t* bnd_out;     //        and their end vertices (the boundary loop, mixed-form area)
     double* k1_part;
+    double* area4;              // {A, cx, cy, cz} of the positions after predict, reduced by the vertex phase
     float4* rec;                // mixed form: per-vertex FP32 element inputs [nv][4] (see wcfe_mixed.cu)
+    double4* bnd_part;          // mixed form: [nb] shoelace terms {A, A cx, A cy, 0} of each boundary vertex
     // control words, advanced by the last patch-phase CTA of the cell to finish a step:
-    int32_t* ctl;               // [0] parity (which pos/ea buffer holds the step-start state), [1] CTA ticket
+    int32_t* ctl;               // [0] parity (which pos/ea buffer holds the step-start state), [1] patch-phase
+                                //     CTA ticket, [2] vertex-phase block ticket
     double* clk;                // [0] simulation time at the start of the next step
     unsigned long long* ap;     // [0] calculateForce_AP calls made (the AP counter of the next step)
     uint32_t* status;
     double ap_thresh;           // ap_rate dt exp(-ap_rate dt) for the engine's current dt (UL:1552)
     SubDev sub;
     wcfe_params prm;
+    ParamF pf;
 };
+
+inline ParamF make_paramf(const wcfe_params& p) {
+    ParamF f{};
+    f.k_lin = (float)p.k_lin;
+    f.rest_len = (float)p.rest_len;
+    f.poly_k0 = (float)p.poly_k0;
+    f.poly_c3 = (float)(1.0 / (3.0 * p.poly_x0 * p.poly_x0));
+    f.ka = (float)p.ka;
+    f.kb = (float)p.kb;
+    f.iFa = (float)(1.0 / p.Fa);
+    f.iFb = (float)(1.0 / p.Fb);
+    f.k_on = (float)p.k_on;
+    f.rho_i_max = (float)p.rho_i_max;
+    f.drag = (float)p.drag;
+    f.damp = (float)p.damp;
+    f.rho = (float)p.rho;
+    f.law = p.force_law == WCFE_LAW_MD_TABLE ? PF_MD
+          : p.force_law == WCFE_LAW_LINEAR ? (p.rest_len == 0.0 ? PF_LINEAR0 : PF_LINEAR)
+          : PF_POLY;
+    f.norm2d = p.linear_norm2d ? 1 : 0;
+    return f;
+}
 
 struct WorkItem {               // one block of a phase: (cell index into the table, block/patch index)
     int32_t cell, idx;

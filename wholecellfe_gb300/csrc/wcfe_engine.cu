@@ -179,6 +179,8 @@ size_t state_layout(int32_t nv, int32_t nt, int32_t nb, int32_t ncand, int32_t n
     put(rec ? sizeof(float4) * 3 * (size_t)nv : 0);  // 20 mixed-form element records (3 float4 per vertex)
     put(sizeof(int32_t) * (nb + 1));  // 21 bnd_optr
     put(sizeof(int32_t) * std::max(2 * nb, 1));  // 22 bnd_out (at most a few edges per boundary vertex)
+    put(sizeof(double) * 4);     // 23 area4
+    put(rec ? sizeof(double4) * (size_t)nb : 0);  // 24 mixed form: shoelace terms per boundary vertex
     return o;
 }
 
@@ -245,7 +247,7 @@ int upload_cell_topology(wcfe_engine* e, Cell* c) {
     const Topology& T = c->topo;
     int32_t ncand = (int32_t)(T.bnd_cand.size() / 2);
     int32_t nk1 = nk1_of(T.nv, T.nt, e->vblock);
-    size_t off[24];
+    size_t off[32];
     size_t bytes = state_layout(T.nv, T.nt, T.nb, ncand, nk1, e->prec == WCFE_PREC_MIXED, off);
     if (c->state_block && c->state_bytes != bytes) dev_free(e, c->state_block, c->state_bytes);
     if (!c->state_block) {
@@ -282,6 +284,8 @@ int upload_cell_topology(wcfe_engine* e, Cell* c) {
     d.ap = (unsigned long long*)(b + off[18]);
     d.status = (uint32_t*)(b + off[19]);
     d.rec = e->prec == WCFE_PREC_MIXED ? (float4*)(b + off[20]) : nullptr;
+    d.area4 = (double*)(b + off[23]);
+    d.bnd_part = e->prec == WCFE_PREC_MIXED ? (double4*)(b + off[24]) : nullptr;
     d.bnd_optr = (const int32_t*)(b + off[21]);
     d.bnd_out = (const int32_t*)(b + off[22]);
     if ((int64_t)T.bnd_out.size() > std::max<int64_t>(2 * (int64_t)T.nb, 1)) return fail("non-manifold boundary", WCFE_ERR_TOPOLOGY);
@@ -420,6 +424,7 @@ int sync_tables(wcfe_engine* e, double dt = -1.0) {
     for (auto& kv : e->cells) {
         Cell* c = kv.second.get();
         c->dev.prm = c->prm;
+        c->dev.pf = make_paramf(c->prm);
         c->dev.rho_w = c->rho_dev;
         c->dev.ap_thresh = e->table_dt > 0 ? ap_threshold(c->prm, e->table_dt) : 0.0;
         c->dev.hoff = e->total_nv;
@@ -608,7 +613,7 @@ uint64_t wcfe_engine_free_bytes(const wcfe_engine* e) {
     return e->budget > e->used ? e->budget - e->used : 0;
 }
 uint64_t wcfe_cell_bytes(int32_t nv, int32_t nt) {
-    size_t off[24];
+    size_t off[32];
     int32_t nb = (int32_t)(4 * std::sqrt((double)std::max(nv, 1)) + 16);
     size_t s = state_layout(nv, nt, nb, 3 * nb, nk1_of(nv, nt, 64), true, off);
     size_t p3[3];

@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(kK1Threads) k_vertex_phase(const CellDev* __re
         block_sum4(acc, red);
         if (threadIdx.x == 0)
             for (int k = 0; k < 4; ++k) c.k1_part[4 * b + k] = acc[k];
+        finish_area(c);
         __syncthreads();
     }
 }
@@ -374,7 +375,6 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
     double* s_ac = s_mm + emax;            // [emax]
     double* s_dA = s_ac + emax;            // [emax][3] diffusion (residual diagnostics only)
     double* s_dC = s_dA + (MODE == PP_RESIDUAL ? 3 * emax : 0);
-    __shared__ double s_red[8];
     for (int w = blockIdx.x; w < a.nwork; w += gridDim.x) {
         const WorkItem it = a.work[w];
         const CellDev& c = a.cells[it.cell];
@@ -384,24 +384,8 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
         const double4* __restrict__ X = c.pos[par];
         const double4* __restrict__ xp = c.pos[par ^ 1];
         const double* __restrict__ eao = c.ea[par];
-        // cell area and centroid from the vertex-phase partials, fixed reduction order
-        if (threadIdx.x < 32) {
-            double s4[4] = {0, 0, 0, 0};
-            for (int k = threadIdx.x; k < c.nk1; k += 32)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) s4[q] += c.k1_part[4 * k + q];
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) s4[q] += __shfl_xor_sync(0xffffffffu, s4[q], o);
-            if (threadIdx.x == 0) {
-                s_red[0] = s4[0];
-                s_red[1] = s4[1] / s4[0]; s_red[2] = s4[2] / s4[0]; s_red[3] = s4[3] / s4[0];
-            }
-        }
-        __syncthreads();
-        const double area_tot = s_red[0];
-        double cen[3] = {s_red[1], s_red[2], s_red[3]};
+        const double area_tot = c.area4[0];
+        double cen[3] = {c.area4[1], c.area4[2], c.area4[3]};
         if (MODE == PP_RESIDUAL && a.centroid_override) {
             cen[0] = a.centroid_override[0]; cen[1] = a.centroid_override[1]; cen[2] = a.centroid_override[2];
         }

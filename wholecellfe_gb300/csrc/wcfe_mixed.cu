@@ -35,6 +35,7 @@
 #include <cstdint>
 
 #include "wcfe_common.cuh"
+#include "wcfe_cvt.h"
 
 namespace wcfe {
 
@@ -42,9 +43,20 @@ struct MixedArgs {
     const CellDev* cells;
     const WorkItem* work;
     int nwork, emax;
-    double dt, dt_real, hdt, ap_thresh, t_override;
-    int vh_from_buf;
+    double dt, dt_real, hdt, cdt, ap_thresh, t_override;
+    int vh_from_buf, half;   // cdt = dt_real - dt/2; half = dt_real > dt/2
 };
+
+// sign tests of doubles on the integer pipe (the FP64 pipe is the scarce one)
+__device__ __forceinline__ bool dzero(double x) { return (dbits(x) << 1) == 0; }
+__device__ __forceinline__ bool dneg(double x) {   // x < 0
+    const uint64_t b = dbits(x);
+    return (int64_t)b < 0 && (b << 1) != 0 && (b << 1) <= (0x7FF0000000000000ull << 1);
+}
+__device__ __forceinline__ bool dpos(double x) {   // x > 0
+    const uint64_t b = dbits(x);
+    return (int64_t)b > 0 && b <= 0x7FF0000000000000ull;
+}
 
 constexpr int kRec = 3;      // float4 per vertex record
 constexpr int kSlot32 = 20;  // floats per element slot in shared memory
@@ -56,18 +68,18 @@ static __constant__ float c_md_k32[6] = {31426.8556f, 99485.86235f, 67080.67086f
 
 // Spring force of bond u in FP32 (UL:1245-1264; k1 UL:1259-1261; the polynomial extension)
 // and the Bell force magnitude of updateFA (UL:2137; k1 UL:2077).
-__device__ __forceinline__ void spring_force32(const wcfe_params& p, float ux, float uy, float uz, float fs[3],
+__device__ __forceinline__ void spring_force32(const ParamF& p, float ux, float uy, float uz, float fs[3],
                                                float* bell) {
     const float D = sqrtf(ux * ux + uy * uy + uz * uz);
-    const float k = (float)p.k_lin, L0 = (float)p.rest_len;
-    if (p.force_law == WCFE_LAW_LINEAR && p.rest_len == 0.0) {
+    const float k = p.k_lin, L0 = p.rest_len;
+    if (p.law == PF_LINEAR0) {
         fs[0] = k * ux; fs[1] = k * uy; fs[2] = k * uz;
-        *bell = p.linear_norm2d ? k * sqrtf(ux * ux + uy * uy) : k * D;
+        *bell = p.norm2d ? k * sqrtf(ux * ux + uy * uy) : k * D;
         return;
     }
     const float iD = D != 0.0f ? 1.0f / D : 0.0f;
     float mag = 0.0f;
-    if (p.force_law == WCFE_LAW_MD_TABLE) {
+    if (p.law == PF_MD) {
         int j = -1;
         if (D >= c_md_px32[5]) j = 5;
         else {
@@ -76,14 +88,14 @@ __device__ __forceinline__ void spring_force32(const wcfe_params& p, float ux, f
                 if (D < c_md_px32[q + 1] && D >= c_md_px32[q]) j = q;
         }
         if (j >= 0) mag = c_md_py32[j] + c_md_k32[j] * (D - c_md_px32[j]);
-    } else if (p.force_law == WCFE_LAW_LINEAR) {
+    } else if (p.law == PF_LINEAR) {
         mag = k * (D - L0);
     } else {
-        const float e = D - L0, x0 = (float)p.poly_x0;
-        mag = (float)p.poly_k0 * (e + e * e * e / (3.0f * x0 * x0));
+        const float e = D - L0;
+        mag = p.poly_k0 * (e + e * e * e * p.poly_c3);
     }
     fs[0] = mag * ux * iD; fs[1] = mag * uy * iD; fs[2] = mag * uz * iD;
-    if (p.force_law == WCFE_LAW_LINEAR && p.linear_norm2d) *bell = fabsf(k * (sqrtf(ux * ux + uy * uy) - L0));
+    if (p.law == PF_LINEAR && p.norm2d) *bell = fabsf(k * (sqrtf(ux * ux + uy * uy) - L0));
     else *bell = fabsf(mag) * (D != 0.0f ? 1.0f : 0.0f);
 }
 
@@ -201,44 +213,30 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
     extern __shared__ float smf[];
     const int emax = a.emax;
     // structure of arrays: field k of slot j at smf[k * emax + j]
-    __shared__ double s_red[4];
+    __shared__ ElemParams s_q;
     for (int w = blockIdx.x; w < a.nwork; w += gridDim.x) {
         const WorkItem it = a.work[w];
         const CellDev& c = a.cells[it.cell];
-        const wcfe_params& p = c.prm;
         const int4 pt = c.patch[it.idx];
         const int par = c.ctl[0];
         const double4* __restrict__ X = c.pos[par];
         const double4* __restrict__ xp = c.pos[par ^ 1];
         const float4* __restrict__ rec = c.rec;
-        if (threadIdx.x < 32) {
-            double s4[4] = {0, 0, 0, 0};
-            for (int k = threadIdx.x; k < c.nk1; k += 32)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) s4[q] += c.k1_part[4 * k + q];
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) s4[q] += __shfl_xor_sync(0xffffffffu, s4[q], o);
-            if (threadIdx.x == 0) {
-                s_red[0] = s4[0];
-                s_red[1] = s4[1] / s4[0]; s_red[2] = s4[2] / s4[0]; s_red[3] = s4[3] / s4[0];
-            }
+        const unsigned long long ap_call = c.ap[0];
+        if (threadIdx.x == 0) {   // the element constants of this cell and step, once per CTA
+            const wcfe_params& p = c.prm;
+            const double t = isnan(a.t_override) ? c.clk[0] : a.t_override;
+            const double t_act = t < p.tact_t1 ? t * p.tact_rate : p.tact_max;
+            s_q.mu = (float)p.mu;
+            s_q.thick = (float)p.thick;
+            s_q.grow = (float)(p.thetag_dot * a.dt_real);
+            s_q.s_iso = (float)(p.kappa * t_act);
+            s_q.t_an = (float)((1.0 - 2.0 * p.kappa) * t_act);
+            s_q.cx = (float)c.area4[1];
+            s_q.cy = (float)c.area4[2];
         }
         __syncthreads();
-        const double area_tot = s_red[0];
-        const double t = isnan(a.t_override) ? c.clk[0] : a.t_override;
-        const unsigned long long ap_call = c.ap[0];
-        const double t_act = t < p.tact_t1 ? t * p.tact_rate : p.tact_max;
-        const double s_iso = p.kappa * t_act;
-        ElemParams q;
-        q.mu = (float)p.mu;
-        q.thick = (float)p.thick;
-        q.grow = (float)(p.thetag_dot * a.dt_real);
-        q.s_iso = (float)s_iso;
-        q.t_an = (float)((1.0 - 2.0 * p.kappa) * t_act);
-        q.cx = (float)s_red[1];
-        q.cy = (float)s_red[2];
+        const ElemParams q = s_q;
         // ---- elements of the patch -> shared memory ----
         for (int j = threadIdx.x; j < pt.w; j += blockDim.x) {
             const int e = c.patch_elems[pt.z + j];
@@ -263,9 +261,10 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
         }
         __syncthreads();
         // ---- owned vertices: forces and the acceleration in FP32, accumulations in FP64 ----
-        const float drag = (float)p.drag, damp = (float)p.damp, rhom = (float)p.rho;
-        const double hdt = a.hdt, cdt = a.dt_real - a.dt / 2.0;
-        const bool half = a.dt_real > a.dt / 2.0;
+        const ParamF& pf = c.pf;
+        const float drag = pf.drag, damp = pf.damp, rhom = pf.rho, rho_max = pf.rho_i_max;
+        const double hdt = a.hdt, cdt = a.cdt;
+        const bool half = a.half;
         for (int i = threadIdx.x; i < pt.y; i += blockDim.x) {
             const int v = pt.x + i;
             float R0 = 0, R1 = 0, Q0 = 0, Q1 = 0, Q2 = 0, Q3 = 0, MMf = 0, Asf = 0;
@@ -285,12 +284,16 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             // integrin force (UL:1241-1269) in FP32
             const double4 f4 = ld4v(c.fau + v);
             float fs[3], bell;
-            spring_force32(p, (float)f4.x, (float)f4.y, (float)f4.z, fs, &bell);
-            const float rho = c.rho_w ? (float)c.rho_w[v] : (float)p.rho_i_max;
-            const float kfa = -(float)c.cC[v] * Asum * rho;
+            spring_force32(pf, f64_to_f32_rn(f4.x), f64_to_f32_rn(f4.y), f64_to_f32_rn(f4.z), fs, &bell);
+            const float rho = c.rho_w ? f64_to_f32_rn(c.rho_w[v]) : rho_max;
+            const float kfa = -f64_to_f32_rn(c.cC[v]) * Asum * rho;
             float F0 = kfa * fs[0] - R0, F1 = kfa * fs[1] - R1;
             const int rank = c.bnd_rank[v];
             if (rank >= 0) {
+                const wcfe_params& p = c.prm;
+                const double t = isnan(a.t_override) ? c.clk[0] : a.t_override;
+                const double s_iso = p.kappa * (t < p.tact_t1 ? t * p.tact_rate : p.tact_max);
+                const double area_tot = c.area4[0];
                 const double4 xv4 = ld4v(xp + v);
                 const double xi[3] = {xv4.x, xv4.y, xv4.z};
                 // isotropic active stress on the open one-ring: (1/2) s_iso thick e3 x sum (X_k - X_j)
@@ -349,30 +352,32 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             }
             const float iM = 1.0f / (MMf * rhom);
             const float damp_m = damp * MMf * rhom;
-            const float An0 = (F0 - drag * (float)vh0 - damp_m * (float)V4.x) * iM;
-            const float An1 = (F1 - drag * (float)vh1 - damp_m * (float)V4.y) * iM;
-            const float An2 = (-damp_m * (float)V4.z) * iM;  // no force normal to the plane
+            const float vh0f = f64_to_f32_rn(vh0), vh1f = f64_to_f32_rn(vh1);
+            const float An0 = (F0 - drag * vh0f - damp_m * f64_to_f32_rn(V4.x)) * iM;
+            const float An1 = (F1 - drag * vh1f - damp_m * f64_to_f32_rn(V4.y)) * iM;
+            const float An2 = dzero(V4.z) ? 0.0f : (-damp_m * f64_to_f32_rn(V4.z)) * iM;  // no force normal to the plane
+            const double An0d = f32_to_f64(An0), An1d = f32_to_f64(An1), An2d = f32_to_f64(An2);
             double Vn0, Vn1, Vn2;
             if (half) {
-                Vn0 = fma(cdt, (double)An0, vh0);
-                Vn1 = fma(cdt, (double)An1, vh1);
-                Vn2 = cdt * (double)An2;
+                Vn0 = fma(cdt, An0d, vh0);
+                Vn1 = fma(cdt, An1d, vh1);
+                Vn2 = cdt * An2d;
             } else {
-                Vn0 = fma(a.dt_real, (double)An0, V4.x);
-                Vn1 = fma(a.dt_real, (double)An1, V4.y);
-                Vn2 = fma(a.dt_real, (double)An2, V4.z);
+                Vn0 = fma(a.dt_real, An0d, V4.x);
+                Vn1 = fma(a.dt_real, An1d, V4.y);
+                Vn2 = fma(a.dt_real, An2d, V4.z);
             }
             const double2* eo = reinterpret_cast<const double2*>(c.ea[par] + 6 * (size_t)v);
             double2* en = reinterpret_cast<double2*>(c.ea[par ^ 1] + 6 * (size_t)v);
             const float iMM = 1.0f / MMf;
             const double2 e0 = eo[0], e1 = eo[1], e2 = eo[2];  // (xx, yy), (zz, xy), (xz, yz)
-            en[0] = make_double2(e0.x + (double)(Q0 * iMM), e0.y + (double)(Q1 * iMM));
-            en[1] = make_double2(e1.x + (double)(Q3 * iMM), e1.y + (double)(Q2 * iMM));
+            en[0] = make_double2(e0.x + f32_to_f64(Q0 * iMM), e0.y + f32_to_f64(Q1 * iMM));
+            en[1] = make_double2(e1.x + f32_to_f64(Q3 * iMM), e1.y + f32_to_f64(Q2 * iMM));
             en[2] = e2;
-            st4(c.acc + v, (double)An0, (double)An1, (double)An2);
+            st4(c.acc + v, An0d, An1d, An2d);
             st4(c.vel + v, Vn0, Vn1, Vn2);
             // NaN/Inf in the state shows up in the FP32 quantities derived from it
-            const float chk = An0 + An1 + Q0 + Q1 + Q2 + (float)vh0 + (float)vh1;
+            const float chk = An0 + An1 + Q0 + Q1 + Q2 + vh0f + vh1f;
             if (!isfinite(chk)) atomicOr(c.status, 1u);
         }
         __syncthreads();
@@ -407,145 +412,164 @@ __device__ __forceinline__ void predict_mixed(const double4& X, const double4& V
     xn[2] = X.z;  // V_hlf.z = 0 (UL:119)
 }
 
-__global__ void __launch_bounds__(kK1Threads) k_vertex_phase_mixed(const CellDev* __restrict__ cells,
-                                                                 const WorkItem* __restrict__ work, int nwork,
-                                                                 double dt, double hdt, int flags,
-                                                                 const double* __restrict__ stage_in,
-                                                                 double* __restrict__ stage_out) {
-    __shared__ double red[3 * kK1Threads];
-    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
-        const WorkItem it = work[w];
-        const CellDev& c = cells[it.cell];
-        const int b = it.idx;
+// The cell area and centroid of the mixed form: every boundary vertex writes its
+// shoelace terms to bnd_part[rank]; the last block of the cell to finish (ticket
+// ctl[2]) sums them in rank order, so the result does not depend on block timing.
+__device__ __forceinline__ void finish_area_boundary(const CellDev& c) {
+    __shared__ int s_last;
+    __shared__ double s_w[kK1Threads / 32][3];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned int t = atomicAdd(reinterpret_cast<unsigned int*>(c.ctl + 2), 1u);
+        s_last = ((int)t == c.nk1 - 1);
+    }
+    __syncthreads();
+    if (!s_last) return;   // block-uniform
+    __threadfence();
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int r = threadIdx.x; r < c.nb; r += blockDim.x) {
+        const double2* q = reinterpret_cast<const double2*>(c.bnd_part + r);
+        const double2 a = __ldcg(q), b = __ldcg(q + 1);
+        s0 += a.x; s1 += a.y; s2 += b.x;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    const int wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_w[wid][0] = s0; s_w[wid][1] = s1; s_w[wid][2] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double A = 0, Ax = 0, Ay = 0;
+        for (int w = 0; w < nw; ++w) {
+            A += s_w[w][0]; Ax += s_w[w][1]; Ay += s_w[w][2];
+        }
+        c.area4[0] = A;
+        c.area4[1] = Ax / A;
+        c.area4[2] = Ay / A;
+        c.area4[3] = 0.0;
+        c.ctl[2] = 0;
+    }
+}
+
+// One block per work item (a block of c.vb consecutive vertices of one cell).
+__global__ void __launch_bounds__(kK1Threads, 3) k_vertex_phase_mixed(const CellDev* __restrict__ cells,
+                                                                    const WorkItem* __restrict__ work,
+                                                                    double dt, double hdt, float dtf, int flags,
+                                                                    const double* __restrict__ stage_in,
+                                                                    double* __restrict__ stage_out) {
+    const WorkItem it = work[blockIdx.x];
+    const CellDev& c = cells[it.cell];
+    const int v = it.idx * c.vb + threadIdx.x;
+    if (v < c.nv) {
         const int par = c.ctl[0];
         const double4* __restrict__ X = c.pos[par];
         double4* __restrict__ xo = c.pos[par ^ 1];
-        const int v = b * c.vb + threadIdx.x;
-        double acc[3] = {0, 0, 0};
-        bool has = false;
-        if (v < c.nv) {
-            const double4 Xv = ld4(X + v);
-            double xn[3];
-            if (flags & VM_IMPORT) {
-                const double* qq = stage_in + 3 * (size_t)(c.hoff + v);
-                xn[0] = qq[0]; xn[1] = qq[1]; xn[2] = qq[2];
-                st4(xo + v, xn[0], xn[1], xn[2]);
-            } else if (flags & VM_PREDICT) {
-                double vh[2];
-                predict_mixed(Xv, ld4(c.vel + v), ld4(c.acc + v), dt, hdt, vh, xn);
-                st4(xo + v, xn[0], xn[1], xn[2]);
-                if (flags & VM_EXPORT) {
-                    st4(c.vhl + v, vh[0], vh[1], 0.0);
-                    double* qq = stage_out + 3 * (size_t)(c.hoff + v);
-                    qq[0] = xn[0]; qq[1] = xn[1]; qq[2] = xn[2];
+        const double4 Xv = ld4(X + v);
+        const int rank = c.bnd_rank[v];
+        double xn[3];
+        if (flags & VM_IMPORT) {
+            const double* qq = stage_in + 3 * (size_t)(c.hoff + v);
+            xn[0] = qq[0]; xn[1] = qq[1]; xn[2] = qq[2];
+            st4(xo + v, xn[0], xn[1], xn[2]);
+        } else if (flags & VM_PREDICT) {
+            double vh[2];
+            predict_mixed(Xv, ld4(c.vel + v), ld4(c.acc + v), dt, hdt, vh, xn);
+            st4(xo + v, xn[0], xn[1], xn[2]);
+            if (flags & VM_EXPORT) {
+                st4(c.vhl + v, vh[0], vh[1], 0.0);
+                double* qq = stage_out + 3 * (size_t)(c.hoff + v);
+                qq[0] = xn[0]; qq[1] = xn[1]; qq[2] = xn[2];
+            }
+        } else {
+            const double4 t = ld4v(xo + v);
+            xn[0] = t.x; xn[1] = t.y; xn[2] = t.z;
+        }
+        const double cu0 = xn[0] - Xv.x, cu1 = xn[1] - Xv.y;  // exact differences
+        if (flags & VM_UPDATE_FA) {
+            const ParamF& pf = c.pf;
+            const double4 f = ld4(c.fau + v);
+            const double cold = c.cC[v], cAv = c.cA[v];
+            double u0 = f.x + cu0, u1 = f.y + cu1, u2 = f.z;
+            if (c.has_sub && c.sub.moving) {
+                double wgt[3];
+                const int e = locate(c.sub, xs(Xv.x, f.x), xs(Xv.y, f.y), xs(Xv.z, f.z), wgt);
+                if (e >= 0) {
+                    const int4 t = c.sub.tri[e];
+                    const double4 a0 = ld4(c.sub.x + t.x), a1 = ld4(c.sub.x + t.y), a2 = ld4(c.sub.x + t.z);
+                    const double4 b0 = ld4(c.sub.X + t.x), b1 = ld4(c.sub.X + t.y), b2 = ld4(c.sub.X + t.z);
+                    u0 -= wgt[0] * (a0.x - b0.x) + wgt[1] * (a1.x - b1.x) + wgt[2] * (a2.x - b2.x);
+                    u1 -= wgt[0] * (a0.y - b0.y) + wgt[1] * (a1.y - b1.y) + wgt[2] * (a2.y - b2.y);
+                    u2 -= wgt[0] * (a0.z - b0.z) + wgt[1] * (a1.z - b1.z) + wgt[2] * (a2.z - b2.z);
                 }
+            }
+            float fs[3], force;
+            spring_force32(pf, f64_to_f32_rn(u0), f64_to_f32_rn(u1), f64_to_f32_rn(u2), fs, &force);
+            const float koff = pf.ka * __expf(force * pf.iFa) + pf.kb * __expf(-force * pf.iFb);
+            const float coldf = f64_to_f32_rn(cold), kon = pf.k_on;
+            double cn = cold + f32_to_f64(dtf * (kon * (1.0f - coldf) - koff * coldf));
+            if (dneg(cn)) cn = 0;
+            if (dneg(cAv)) c.cA[v] = 0;
+            double n0, n1, n2;
+            const bool keep_pos = dpos(cold) && (1.0f - dtf * koff) > 0.0f;
+            if (keep_pos && dpos(cn)) {
+                // keep / c_new = 1 + ds with ds = -dt k_on (1 - c_old) / c_new exactly
+                const double ds = f32_to_f64(-dtf * kon * (1.0f - coldf) / f64_to_f32_rn(cn));
+                n0 = fma(u0, ds, u0); n1 = fma(u1, ds, u1); n2 = fma(u2, ds, u2);
             } else {
-                const double4 t = ld4v(xo + v);
-                xn[0] = t.x; xn[1] = t.y; xn[2] = t.z;
+                n0 = 0.0 * u0; n1 = 0.0 * u1; n2 = 0.0 * u2;
             }
-            const double cu0 = xn[0] - Xv.x, cu1 = xn[1] - Xv.y;  // exact differences
-            if (flags & VM_UPDATE_FA) {
-                const wcfe_params& p = c.prm;
-                const double4 f = ld4v(c.fau + v);
-                double su0 = 0, su1 = 0, su2 = 0;
-                if (c.has_sub && c.sub.moving) {
-                    double wgt[3];
-                    const int e = locate(c.sub, xs(Xv.x, f.x), xs(Xv.y, f.y), xs(Xv.z, f.z), wgt);
-                    if (e >= 0) {
-                        const int4 t = c.sub.tri[e];
-                        const double4 a0 = ld4(c.sub.x + t.x), a1 = ld4(c.sub.x + t.y), a2 = ld4(c.sub.x + t.z);
-                        const double4 b0 = ld4(c.sub.X + t.x), b1 = ld4(c.sub.X + t.y), b2 = ld4(c.sub.X + t.z);
-                        su0 = wgt[0] * (a0.x - b0.x) + wgt[1] * (a1.x - b1.x) + wgt[2] * (a2.x - b2.x);
-                        su1 = wgt[0] * (a0.y - b0.y) + wgt[1] * (a1.y - b1.y) + wgt[2] * (a2.y - b2.y);
-                        su2 = wgt[0] * (a0.z - b0.z) + wgt[1] * (a1.z - b1.z) + wgt[2] * (a2.z - b2.z);
-                    }
-                }
-                const double u0 = (f.x + cu0) - su0, u1 = (f.y + cu1) - su1, u2 = f.z - su2;
-                float fs[3], force;
-                spring_force32(p, (float)u0, (float)u1, (float)u2, fs, &force);
-                const float koff = (float)p.ka * __expf(force / (float)p.Fa) + (float)p.kb * __expf(-force / (float)p.Fb);
-                const double cold = c.cC[v];
-                const float coldf = (float)cold, dtf = (float)dt, kon = (float)p.k_on;
-                double cn = cold + (double)(dtf * (kon * (1.0f - coldf) - koff * coldf));
-                if (cn < 0) cn = 0;
-                if (c.cA[v] < 0) c.cA[v] = 0;
-                double n0, n1, n2;
-                const bool keep_pos = cold > 0 && (1.0f - dtf * koff) > 0.0f;
-                if (keep_pos && cn > 0) {
-                    // keep / c_new = 1 + ds with ds = -dt k_on (1 - c_old) / c_new exactly
-                    const double ds = (double)(-dtf * kon * (1.0f - coldf) / (float)cn);
-                    n0 = fma(u0, ds, u0); n1 = fma(u1, ds, u1); n2 = fma(u2, ds, u2);
+            c.cC[v] = cn;
+            st4(c.fau + v, n0, n1, n2);
+        }
+        if (!(flags & VM_EXPORT)) {
+            const double2* e2 = reinterpret_cast<const double2*>(c.ea[par] + 6 * (size_t)v);
+            const double2 q0 = __ldg(e2), q1 = __ldg(e2 + 1);  // (xx, yy), (zz, xy)
+            const float hx = f64_to_f32_rn(Xv.x), hy = f64_to_f32_rn(Xv.y);
+            const float lx = f64_to_f32_rn(Xv.x - f32_to_f64(hx)), ly = f64_to_f32_rn(Xv.y - f32_to_f64(hy));
+            float4* r = c.rec + kRec * (size_t)v;
+            r[0] = make_float4(hx, hy, lx, ly);
+            r[1] = make_float4(f64_to_f32_rn(cu0), f64_to_f32_rn(cu1), f64_to_f32_rn(q0.x), f64_to_f32_rn(q0.y));
+            r[2] = make_float4(f64_to_f32_rn(q1.y), f64_to_f32_rn(q1.x), 0.0f, 0.0f);
+        }
+        if (!(flags & VM_NOAREA) && rank >= 0) {
+            // shoelace terms of the directed boundary edges leaving v
+            double s0 = 0, s1 = 0, s2 = 0;
+            for (int k = c.bnd_optr[rank]; k < c.bnd_optr[rank + 1]; ++k) {
+                const int j = c.bnd_out[k];
+                double xj[3];
+                if (flags & VM_IMPORT) {
+                    const double* qq = stage_in + 3 * (size_t)(c.hoff + j);
+                    xj[0] = qq[0]; xj[1] = qq[1];
+                } else if (flags & VM_PREDICT) {
+                    double vhj[2];
+                    predict_mixed(ld4(X + j), ld4(c.vel + j), ld4(c.acc + j), dt, hdt, vhj, xj);
                 } else {
-                    n0 = 0.0 * u0; n1 = 0.0 * u1; n2 = 0.0 * u2;
+                    const double4 t = ld4v(xo + j);
+                    xj[0] = t.x; xj[1] = t.y;
                 }
-                c.cC[v] = cn;
-                st4(c.fau + v, n0, n1, n2);
+                const double cr = xn[0] * xj[1] - xj[0] * xn[1];
+                s0 += 0.5 * cr;
+                s1 += (1.0 / 6.0) * (xn[0] + xj[0]) * cr;
+                s2 += (1.0 / 6.0) * (xn[1] + xj[1]) * cr;
             }
-            if (!(flags & VM_EXPORT)) {
-                const float hx = (float)Xv.x, hy = (float)Xv.y;
-                const float lx = (float)(Xv.x - (double)hx), ly = (float)(Xv.y - (double)hy);
-                const double2* e2 = reinterpret_cast<const double2*>(c.ea[par] + 6 * (size_t)v);
-                const double2 q0 = e2[0], q1 = e2[1];  // (xx, yy), (zz, xy)
-                float4* r = c.rec + kRec * (size_t)v;
-                r[0] = make_float4(hx, hy, lx, ly);
-                r[1] = make_float4((float)cu0, (float)cu1, (float)q0.x, (float)q0.y);
-                r[2] = make_float4((float)q1.y, (float)q1.x, 0.0f, 0.0f);
-            }
-            const int rank = c.bnd_rank[v];
-            if (!(flags & VM_NOAREA) && rank >= 0) {
-                for (int k = c.bnd_optr[rank]; k < c.bnd_optr[rank + 1]; ++k) {
-                    const int j = c.bnd_out[k];
-                    double xj[3];
-                    if (flags & VM_IMPORT) {
-                        const double* qq = stage_in + 3 * (size_t)(c.hoff + j);
-                        xj[0] = qq[0]; xj[1] = qq[1];
-                    } else if (flags & VM_PREDICT) {
-                        double vhj[2];
-                        predict_mixed(ld4(X + j), ld4(c.vel + j), ld4(c.acc + j), dt, hdt, vhj, xj);
-                    } else {
-                        const double4 t = ld4v(xo + j);
-                        xj[0] = t.x; xj[1] = t.y;
-                    }
-                    const double cr = xn[0] * xj[1] - xj[0] * xn[1];
-                    acc[0] += 0.5 * cr;
-                    acc[1] += (1.0 / 6.0) * (xn[0] + xj[0]) * cr;
-                    acc[2] += (1.0 / 6.0) * (xn[1] + xj[1]) * cr;
-                    has = true;
-                }
-            }
+            st4(c.bnd_part + rank, s0, s1, s2);
+            __threadfence();
         }
-        if (flags & VM_NOAREA) continue;
-        // block partial over its boundary edges, fixed order, only in blocks that have any
-        if (__syncthreads_or(has)) {
-            for (int k = 0; k < 3; ++k) red[3 * threadIdx.x + k] = acc[k];
-            __syncthreads();
-            if (threadIdx.x < 32) {
-                double s[3] = {0, 0, 0};
-                for (int t = threadIdx.x; t < (int)blockDim.x; t += 32)
-                    for (int k = 0; k < 3; ++k) s[k] += red[3 * t + k];
-#pragma unroll
-                for (int k = 0; k < 3; ++k)
-#pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_xor_sync(0xffffffffu, s[k], o);
-                if (threadIdx.x == 0) {
-                    c.k1_part[4 * b + 0] = s[0];
-                    c.k1_part[4 * b + 1] = s[1];
-                    c.k1_part[4 * b + 2] = s[2];
-                    c.k1_part[4 * b + 3] = 0.0;
-                }
-            }
-        } else if (threadIdx.x == 0) {
-            c.k1_part[4 * b + 0] = 0.0; c.k1_part[4 * b + 1] = 0.0;
-            c.k1_part[4 * b + 2] = 0.0; c.k1_part[4 * b + 3] = 0.0;
-        }
-        __syncthreads();
     }
+    if (!(flags & VM_NOAREA)) finish_area_boundary(c);
 }
 
 void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
                          int threads, cudaStream_t st, const double* stage_in, double* stage_out) {
     if (nwork <= 0) return;
-    k_vertex_phase_mixed<<<grid, threads, 0, st>>>(cells, work, nwork, dt, dt / 2.0, flags, stage_in, stage_out);
+    (void)grid;   // one block per work item
+    k_vertex_phase_mixed<<<nwork, threads, 0, st>>>(cells, work, dt, dt / 2.0, (float)dt, flags, stage_in, stage_out);
 }
 
 size_t mixed_smem_bytes(int emax) { return sizeof(float) * (size_t)emax * kSlot32; }
@@ -578,6 +602,8 @@ void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, i
     a.dt = dt;
     a.dt_real = dt_real;
     a.hdt = dt / 2.0;
+    a.cdt = dt_real - dt / 2.0;
+    a.half = dt_real > dt / 2.0;
     a.ap_thresh = ap_thresh;
     a.t_override = t_override;
     a.vh_from_buf = vh_from_buf;
