@@ -10,7 +10,10 @@
 //   tri [nt] int4 (a, b, c, 0); vt_ptr [nv+1], vc_code [3nt] uint16 one-ring in mesh order
 //   patches: patch [np] int4 (v0, nv, e0, ne), patch_elems [sum ne] int32
 //   boundary: bnd_rank [nv] int32 (-1 interior), bnd_cptr [nb+1], bnd_cand [..] int2 (nj, nint)
+//   bnd_optr [nb+1], bnd_out: directed boundary edges; bnd_vert [nb] boundary vertices by rank
 //   k1_part [nk1][4] double: per-block partial sums of area and area-weighted centroid
+//   area4 [4] double: cell area and centroid of the predicted positions (written by the vertex phase)
+//   rec [nv][3] float4: mixed form only, the FP32 element inputs of each vertex
 #pragma once
 #include <cstdint>
 
@@ -70,7 +73,7 @@ struct CellDev {
     double* k1_part;
     double* area4;              // {A, cx, cy, cz} of the positions after predict, reduced by the vertex phase
     float4* rec;                // mixed form: per-vertex FP32 element inputs [nv][4] (see wcfe_mixed.cu)
-    double4* bnd_part;          // mixed form: [nb] shoelace terms {A, A cx, A cy, 0} of each boundary vertex
+    const int32_t* bnd_vert;    // [nb] boundary vertices in rank order (the inverse of bnd_rank)
     // control words, advanced by the last patch-phase CTA of the cell to finish a step:
     int32_t* ctl;               // [0] parity (which pos/ea buffer holds the step-start state), [1] patch-phase
                                 //     CTA ticket, [2] vertex-phase block ticket

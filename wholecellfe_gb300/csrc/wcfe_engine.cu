@@ -180,7 +180,7 @@ size_t state_layout(int32_t nv, int32_t nt, int32_t nb, int32_t ncand, int32_t n
     put(sizeof(int32_t) * (nb + 1));  // 21 bnd_optr
     put(sizeof(int32_t) * std::max(2 * nb, 1));  // 22 bnd_out (at most a few edges per boundary vertex)
     put(sizeof(double) * 4);     // 23 area4
-    put(rec ? sizeof(double4) * (size_t)nb : 0);  // 24 mixed form: shoelace terms per boundary vertex
+    put(sizeof(int32_t) * std::max(nb, 1));  // 24 bnd_vert: boundary vertices in rank order
     return o;
 }
 
@@ -285,14 +285,20 @@ int upload_cell_topology(wcfe_engine* e, Cell* c) {
     d.status = (uint32_t*)(b + off[19]);
     d.rec = e->prec == WCFE_PREC_MIXED ? (float4*)(b + off[20]) : nullptr;
     d.area4 = (double*)(b + off[23]);
-    d.bnd_part = e->prec == WCFE_PREC_MIXED ? (double4*)(b + off[24]) : nullptr;
+    d.bnd_vert = (const int32_t*)(b + off[24]);
     d.bnd_optr = (const int32_t*)(b + off[21]);
     d.bnd_out = (const int32_t*)(b + off[22]);
     if ((int64_t)T.bnd_out.size() > std::max<int64_t>(2 * (int64_t)T.nb, 1)) return fail("non-manifold boundary", WCFE_ERR_TOPOLOGY);
     CK(cudaMemcpyAsync((void*)d.bnd_optr, T.bnd_optr.data(), sizeof(int32_t) * (T.nb + 1), cudaMemcpyHostToDevice, e->stream));
     if (!T.bnd_out.empty())
         CK(cudaMemcpyAsync((void*)d.bnd_out, T.bnd_out.data(), sizeof(int32_t) * T.bnd_out.size(), cudaMemcpyHostToDevice, e->stream));
-    // topology arrays, staged through pinned memory
+    if (T.nb > 0) {
+        std::vector<int32_t> bv(T.nb);
+        for (int v = 0; v < T.nv; ++v)
+            if (T.bnd_rank[v] >= 0) bv[T.bnd_rank[v]] = v;
+        CK(cudaMemcpyAsync((void*)d.bnd_vert, bv.data(), sizeof(int32_t) * T.nb, cudaMemcpyHostToDevice, e->stream));
+    }
+    // topology arrays
     std::vector<int4> t4(T.nt);
     for (int t = 0; t < T.nt; ++t) t4[t] = make_int4(T.tri[3 * t], T.tri[3 * t + 1], T.tri[3 * t + 2], 0);
     CK(cudaMemcpyAsync((void*)d.tri, t4.data(), sizeof(int4) * T.nt, cudaMemcpyHostToDevice, e->stream));

@@ -209,11 +209,119 @@ __device__ __forceinline__ void element2d(const float4 r[3][kRec], const ElemPar
     o.acur = 0.5f * fabsf(gc);
 }
 
+constexpr int kBndSlots = 128;   // boundary vertices a patch CTA queues for its second loop
+
+// Boundary terms of vertex v (rank `rank`) in FP64, added to (F0, F1): the isotropic
+// active stress of the open one-ring, AP push (calculateForce_AP UL:1477-1569),
+// bending (calculateBendingForce2D UL:1571-1689) and area constraint
+// (calculateAreaConstraintForce UL:1691-1784), on the neighbour frame of UL:1500-1531.
+__device__ __forceinline__ void boundary_force(const CellDev& c, const MixedArgs& a, const int4& pt,
+                                               const double4* __restrict__ X, const double4* __restrict__ xp, int v,
+                                               int rank, unsigned long long ap_call, float& F0, float& F1) {
+    const wcfe_params& p = c.prm;
+    const double t = isnan(a.t_override) ? c.clk[0] : a.t_override;
+    const double s_iso = p.kappa * (t < p.tact_t1 ? t * p.tact_rate : p.tact_max);
+    const double area_tot = c.area4[0];
+    const double4 xv4 = ld4v(xp + v);
+    const double xi[3] = {xv4.x, xv4.y, xv4.z};
+    // isotropic active stress on the open one-ring: (1/2) s_iso thick e3 x sum (X_k - X_j)
+    double sx = 0, sy = 0;
+    for (int k = c.vt_ptr[v]; k < c.vt_ptr[v + 1]; ++k) {
+        const int code = c.vc_code[k];
+        const int cn = code & 3;
+        const int e = c.patch_elems[pt.z + (code >> 2)];
+        const int4 t4 = c.tri[e];
+        const int ids[3] = {t4.x, t4.y, t4.z};
+        const double4 Xj = ld4v(X + ids[(cn + 1) % 3]), Xk = ld4v(X + ids[(cn + 2) % 3]);
+        sx += Xk.x - Xj.x;
+        sy += Xk.y - Xj.y;
+    }
+    const double w = 0.5 * s_iso * p.thick;
+    double Fb0 = w * sy, Fb1 = -w * sx;  // minus the residual term w e3 x s
+    double x1[3], x2[3];
+    if (boundary_frame(c, xp, rank, xi, x1, x2)) {
+        const double d1x = xi[0] - x1[0], d1y = xi[1] - x1[1], d2x = x2[0] - xi[0], d2y = x2[1] - xi[1];
+        const double d1z = xi[2] - x1[2], d2z = x2[2] - xi[2];
+        const double nn1 = sqrt(d1y * d1y + d1x * d1x), nn2 = sqrt(d2y * d2y + d2x * d2x);
+        const double l1 = sqrt(d1x * d1x + d1y * d1y + d1z * d1z), l2 = sqrt(d2x * d2x + d2y * d2y + d2z * d2z);
+        const double L = l1 + l2;
+        const double nx = l1 / L * (d1y / nn1) + l2 / L * (d2y / nn2);
+        const double ny = l1 / L * (-d1x / nn1) + l2 / L * (-d2x / nn2);
+        double fb = 0.0;
+        if (p.ap_enable) {
+            const uint32_t r31 = ap_draw(p.seed, p.stream, ap_call, (uint32_t)rank);
+            const double Pr = (double)r31 / ((double)2147483647 + 1.);
+            const double lim = p.ap_density * L / 2;
+            const double cnt = lim > 0 ? ceil(lim) : 0.0;
+            const double apt = isnan(a.ap_thresh) ? c.ap_thresh : a.ap_thresh;
+            fb += (Pr < apt) ? p.ap_force * cnt : 0.0;
+        }
+        const double e1x = d1x / l1, e1y = d1y / l1, e1z = d1z / l1, e2x = d2x / l2, e2y = d2y / l2, e2z = d2z / l2;
+        const double cost = e1x * e2x + e1y * e2y + e1z * e2z;
+        const double ez = xs(xm(e1x, e2y), xm(e1y, e2x));
+        const double turna = ez > 0 ? cost - 1 : 1 - cost;
+        fb += p.k_bend * (turna * 2 / L);
+        fb += -p.k_area * (area_tot - p.area0) / 2 * L;
+        Fb0 += fb * nx;
+        Fb1 += fb * ny;
+    }
+    F0 += (float)Fb0;
+    F1 += (float)Fb1;
+}
+
+// Explicit update of vertex v (UL:592-628): A in FP32 from the FP32 force; V and the
+// strain accumulate in FP64.
+__device__ __forceinline__ void finish_vertex(const CellDev& c, const MixedArgs& a, int par, int v, float F0, float F1,
+                                              float Q0, float Q1, float Q2, float Q3, float MMf) {
+    const ParamF& pf = c.pf;
+    const double4 V4 = ld4v(c.vel + v), A4 = ld4v(c.acc + v);
+    double vh0, vh1;
+    if (a.vh_from_buf) {
+        const double4 h = ld4v(c.vhl + v);
+        vh0 = h.x; vh1 = h.y;
+    } else {
+        vh0 = fma(a.hdt, A4.x, V4.x);
+        vh1 = fma(a.hdt, A4.y, V4.y);
+    }
+    const float rhom = pf.rho;
+    const float iM = 1.0f / (MMf * rhom);
+    const float damp_m = pf.damp * MMf * rhom;
+    const float vh0f = f64_to_f32_rn(vh0), vh1f = f64_to_f32_rn(vh1);
+    const float An0 = (F0 - pf.drag * vh0f - damp_m * f64_to_f32_rn(V4.x)) * iM;
+    const float An1 = (F1 - pf.drag * vh1f - damp_m * f64_to_f32_rn(V4.y)) * iM;
+    const float An2 = dzero(V4.z) ? 0.0f : (-damp_m * f64_to_f32_rn(V4.z)) * iM;  // no force normal to the plane
+    const double An0d = f32_to_f64(An0), An1d = f32_to_f64(An1), An2d = f32_to_f64(An2);
+    double Vn0, Vn1, Vn2;
+    if (a.half) {
+        Vn0 = fma(a.cdt, An0d, vh0);
+        Vn1 = fma(a.cdt, An1d, vh1);
+        Vn2 = a.cdt * An2d;
+    } else {
+        Vn0 = fma(a.dt_real, An0d, V4.x);
+        Vn1 = fma(a.dt_real, An1d, V4.y);
+        Vn2 = fma(a.dt_real, An2d, V4.z);
+    }
+    const double2* eo = reinterpret_cast<const double2*>(c.ea[par] + 6 * (size_t)v);
+    double2* en = reinterpret_cast<double2*>(c.ea[par ^ 1] + 6 * (size_t)v);
+    const float iMM = 1.0f / MMf;
+    const double2 e0 = eo[0], e1 = eo[1], e2 = eo[2];  // (xx, yy), (zz, xy), (xz, yz)
+    en[0] = make_double2(e0.x + f32_to_f64(Q0 * iMM), e0.y + f32_to_f64(Q1 * iMM));
+    en[1] = make_double2(e1.x + f32_to_f64(Q3 * iMM), e1.y + f32_to_f64(Q2 * iMM));
+    en[2] = e2;
+    st4(c.acc + v, An0d, An1d, An2d);
+    st4(c.vel + v, Vn0, Vn1, Vn2);
+    // NaN/Inf in the state shows up in the FP32 quantities derived from it
+    const float chk = An0 + An1 + Q0 + Q1 + Q2 + vh0f + vh1f;
+    if (!isfinite(chk)) atomicOr(c.status, 1u);
+}
+
 __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
     extern __shared__ float smf[];
     const int emax = a.emax;
     // structure of arrays: field k of slot j at smf[k * emax + j]
     __shared__ ElemParams s_q;
+    __shared__ int s_nbnd;
+    __shared__ float s_bnd[8 * kBndSlots];
     for (int w = blockIdx.x; w < a.nwork; w += gridDim.x) {
         const WorkItem it = a.work[w];
         const CellDev& c = a.cells[it.cell];
@@ -224,6 +332,7 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
         const float4* __restrict__ rec = c.rec;
         const unsigned long long ap_call = c.ap[0];
         if (threadIdx.x == 0) {   // the element constants of this cell and step, once per CTA
+            s_nbnd = 0;
             const wcfe_params& p = c.prm;
             const double t = isnan(a.t_override) ? c.clk[0] : a.t_override;
             const double t_act = t < p.tact_t1 ? t * p.tact_rate : p.tact_max;
@@ -261,10 +370,11 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
         }
         __syncthreads();
         // ---- owned vertices: forces and the acceleration in FP32, accumulations in FP64 ----
+        // Interior vertices finish here.  Boundary vertices queue their FP32 sums in shared
+        // memory and finish in a second loop over consecutive threads, so that the FP64
+        // boundary terms run on full warps instead of one or two lanes of many warps.
         const ParamF& pf = c.pf;
-        const float drag = pf.drag, damp = pf.damp, rhom = pf.rho, rho_max = pf.rho_i_max;
-        const double hdt = a.hdt, cdt = a.cdt;
-        const bool half = a.half;
+        const float rho_max = pf.rho_i_max;
         for (int i = threadIdx.x; i < pt.y; i += blockDim.x) {
             const int v = pt.x + i;
             float R0 = 0, R1 = 0, Q0 = 0, Q1 = 0, Q2 = 0, Q3 = 0, MMf = 0, Asf = 0;
@@ -290,95 +400,25 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             float F0 = kfa * fs[0] - R0, F1 = kfa * fs[1] - R1;
             const int rank = c.bnd_rank[v];
             if (rank >= 0) {
-                const wcfe_params& p = c.prm;
-                const double t = isnan(a.t_override) ? c.clk[0] : a.t_override;
-                const double s_iso = p.kappa * (t < p.tact_t1 ? t * p.tact_rate : p.tact_max);
-                const double area_tot = c.area4[0];
-                const double4 xv4 = ld4v(xp + v);
-                const double xi[3] = {xv4.x, xv4.y, xv4.z};
-                // isotropic active stress on the open one-ring: (1/2) s_iso thick e3 x sum (X_k - X_j)
-                double sx = 0, sy = 0;
-                for (int k = c.vt_ptr[v]; k < c.vt_ptr[v + 1]; ++k) {
-                    const int code = c.vc_code[k];
-                    const int cn = code & 3;
-                    const int e = c.patch_elems[pt.z + (code >> 2)];
-                    const int4 t4 = c.tri[e];
-                    const int ids[3] = {t4.x, t4.y, t4.z};
-                    const double4 Xj = ld4v(X + ids[(cn + 1) % 3]), Xk = ld4v(X + ids[(cn + 2) % 3]);
-                    sx += Xk.x - Xj.x;
-                    sy += Xk.y - Xj.y;
+                const int slot = atomicAdd(&s_nbnd, 1);
+                if (slot < kBndSlots) {
+                    float* b = s_bnd + 8 * slot;
+                    b[0] = __int_as_float(i); b[1] = F0; b[2] = F1; b[3] = Q0;
+                    b[4] = Q1; b[5] = Q2; b[6] = Q3; b[7] = MMf;
+                    continue;
                 }
-                const double w = 0.5 * s_iso * p.thick;
-                double Fb0 = w * sy, Fb1 = -w * sx;  // minus the residual term w e3 x s
-                double x1[3], x2[3];
-                if (boundary_frame(c, xp, rank, xi, x1, x2)) {
-                    const double d1x = xi[0] - x1[0], d1y = xi[1] - x1[1], d2x = x2[0] - xi[0], d2y = x2[1] - xi[1];
-                    const double d1z = xi[2] - x1[2], d2z = x2[2] - xi[2];
-                    const double nn1 = sqrt(d1y * d1y + d1x * d1x), nn2 = sqrt(d2y * d2y + d2x * d2x);
-                    const double l1 = sqrt(d1x * d1x + d1y * d1y + d1z * d1z), l2 = sqrt(d2x * d2x + d2y * d2y + d2z * d2z);
-                    const double L = l1 + l2;
-                    const double nx = l1 / L * (d1y / nn1) + l2 / L * (d2y / nn2);
-                    const double ny = l1 / L * (-d1x / nn1) + l2 / L * (-d2x / nn2);
-                    double fb = 0.0;
-                    if (p.ap_enable) {
-                        const uint32_t r31 = ap_draw(p.seed, p.stream, ap_call, (uint32_t)rank);
-                        const double Pr = (double)r31 / ((double)2147483647 + 1.);
-                        const double lim = p.ap_density * L / 2;
-                        const double cnt = lim > 0 ? ceil(lim) : 0.0;
-                        const double apt = isnan(a.ap_thresh) ? c.ap_thresh : a.ap_thresh;
-                        fb += (Pr < apt) ? p.ap_force * cnt : 0.0;
-                    }
-                    const double e1x = d1x / l1, e1y = d1y / l1, e1z = d1z / l1, e2x = d2x / l2, e2y = d2y / l2, e2z = d2z / l2;
-                    const double cost = e1x * e2x + e1y * e2y + e1z * e2z;
-                    const double ez = xs(xm(e1x, e2y), xm(e1y, e2x));
-                    const double turna = ez > 0 ? cost - 1 : 1 - cost;
-                    fb += p.k_bend * (turna * 2 / L);
-                    fb += -p.k_area * (area_tot - p.area0) / 2 * L;
-                    Fb0 += fb * nx;
-                    Fb1 += fb * ny;
-                }
-                F0 += (float)Fb0;
-                F1 += (float)Fb1;
+                boundary_force(c, a, pt, X, xp, v, rank, ap_call, F0, F1);   // queue full: finish in place
             }
-            // explicit update (UL:592-628): A in FP32 from the FP32 force; V and the strain in FP64
-            const double4 V4 = ld4v(c.vel + v), A4 = ld4v(c.acc + v);
-            double vh0, vh1;
-            if (a.vh_from_buf) {
-                const double4 h = ld4v(c.vhl + v);
-                vh0 = h.x; vh1 = h.y;
-            } else {
-                vh0 = fma(hdt, A4.x, V4.x);
-                vh1 = fma(hdt, A4.y, V4.y);
-            }
-            const float iM = 1.0f / (MMf * rhom);
-            const float damp_m = damp * MMf * rhom;
-            const float vh0f = f64_to_f32_rn(vh0), vh1f = f64_to_f32_rn(vh1);
-            const float An0 = (F0 - drag * vh0f - damp_m * f64_to_f32_rn(V4.x)) * iM;
-            const float An1 = (F1 - drag * vh1f - damp_m * f64_to_f32_rn(V4.y)) * iM;
-            const float An2 = dzero(V4.z) ? 0.0f : (-damp_m * f64_to_f32_rn(V4.z)) * iM;  // no force normal to the plane
-            const double An0d = f32_to_f64(An0), An1d = f32_to_f64(An1), An2d = f32_to_f64(An2);
-            double Vn0, Vn1, Vn2;
-            if (half) {
-                Vn0 = fma(cdt, An0d, vh0);
-                Vn1 = fma(cdt, An1d, vh1);
-                Vn2 = cdt * An2d;
-            } else {
-                Vn0 = fma(a.dt_real, An0d, V4.x);
-                Vn1 = fma(a.dt_real, An1d, V4.y);
-                Vn2 = fma(a.dt_real, An2d, V4.z);
-            }
-            const double2* eo = reinterpret_cast<const double2*>(c.ea[par] + 6 * (size_t)v);
-            double2* en = reinterpret_cast<double2*>(c.ea[par ^ 1] + 6 * (size_t)v);
-            const float iMM = 1.0f / MMf;
-            const double2 e0 = eo[0], e1 = eo[1], e2 = eo[2];  // (xx, yy), (zz, xy), (xz, yz)
-            en[0] = make_double2(e0.x + f32_to_f64(Q0 * iMM), e0.y + f32_to_f64(Q1 * iMM));
-            en[1] = make_double2(e1.x + f32_to_f64(Q3 * iMM), e1.y + f32_to_f64(Q2 * iMM));
-            en[2] = e2;
-            st4(c.acc + v, An0d, An1d, An2d);
-            st4(c.vel + v, Vn0, Vn1, Vn2);
-            // NaN/Inf in the state shows up in the FP32 quantities derived from it
-            const float chk = An0 + An1 + Q0 + Q1 + Q2 + vh0f + vh1f;
-            if (!isfinite(chk)) atomicOr(c.status, 1u);
+            finish_vertex(c, a, par, v, F0, F1, Q0, Q1, Q2, Q3, MMf);
+        }
+        __syncthreads();
+        const int nq = min(s_nbnd, kBndSlots);
+        for (int j = threadIdx.x; j < nq; j += blockDim.x) {
+            const float* b = s_bnd + 8 * j;
+            const int v = pt.x + __float_as_int(b[0]);
+            float F0 = b[1], F1 = b[2];
+            boundary_force(c, a, pt, X, xp, v, c.bnd_rank[v], ap_call, F0, F1);
+            finish_vertex(c, a, par, v, F0, F1, b[3], b[4], b[5], b[6], b[7]);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -412,10 +452,13 @@ __device__ __forceinline__ void predict_mixed(const double4& X, const double4& V
     xn[2] = X.z;  // V_hlf.z = 0 (UL:119)
 }
 
-// The cell area and centroid of the mixed form: every boundary vertex writes its
-// shoelace terms to bnd_part[rank]; the last block of the cell to finish (ticket
-// ctl[2]) sums them in rank order, so the result does not depend on block timing.
-__device__ __forceinline__ void finish_area_boundary(const CellDev& c) {
+// The cell area and centroid of the mixed form, from the predicted positions of
+// the boundary loop (shoelace over the directed boundary edges).  The last block
+// of the cell to finish (ticket ctl[2]) reads the positions the other blocks
+// wrote (through L2) and sums the terms in a fixed order: boundary ranks strided
+// over the threads, then lanes, then warps.  Only that block runs the FP64
+// shoelace, with all of its lanes busy.
+__device__ __forceinline__ void finish_area_boundary(const CellDev& c, const double4* xo) {
     __shared__ int s_last;
     __shared__ double s_w[kK1Threads / 32][3];
     __syncthreads();
@@ -429,9 +472,14 @@ __device__ __forceinline__ void finish_area_boundary(const CellDev& c) {
     __threadfence();
     double s0 = 0, s1 = 0, s2 = 0;
     for (int r = threadIdx.x; r < c.nb; r += blockDim.x) {
-        const double2* q = reinterpret_cast<const double2*>(c.bnd_part + r);
-        const double2 a = __ldcg(q), b = __ldcg(q + 1);
-        s0 += a.x; s1 += a.y; s2 += b.x;
+        const double2 xi = __ldcg(reinterpret_cast<const double2*>(xo + c.bnd_vert[r]));
+        for (int k = c.bnd_optr[r]; k < c.bnd_optr[r + 1]; ++k) {
+            const double2 xj = __ldcg(reinterpret_cast<const double2*>(xo + c.bnd_out[k]));
+            const double cr = xi.x * xj.y - xj.x * xi.y;
+            s0 += 0.5 * cr;
+            s1 += (1.0 / 6.0) * (xi.x + xj.x) * cr;
+            s2 += (1.0 / 6.0) * (xi.y + xj.y) * cr;
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -471,7 +519,6 @@ __global__ void __launch_bounds__(kK1Threads, 3) k_vertex_phase_mixed(const Cell
         const double4* __restrict__ X = c.pos[par];
         double4* __restrict__ xo = c.pos[par ^ 1];
         const double4 Xv = ld4(X + v);
-        const int rank = c.bnd_rank[v];
         double xn[3];
         if (flags & VM_IMPORT) {
             const double* qq = stage_in + 3 * (size_t)(c.hoff + v);
@@ -537,32 +584,10 @@ __global__ void __launch_bounds__(kK1Threads, 3) k_vertex_phase_mixed(const Cell
             r[1] = make_float4(f64_to_f32_rn(cu0), f64_to_f32_rn(cu1), f64_to_f32_rn(q0.x), f64_to_f32_rn(q0.y));
             r[2] = make_float4(f64_to_f32_rn(q1.y), f64_to_f32_rn(q1.x), 0.0f, 0.0f);
         }
-        if (!(flags & VM_NOAREA) && rank >= 0) {
-            // shoelace terms of the directed boundary edges leaving v
-            double s0 = 0, s1 = 0, s2 = 0;
-            for (int k = c.bnd_optr[rank]; k < c.bnd_optr[rank + 1]; ++k) {
-                const int j = c.bnd_out[k];
-                double xj[3];
-                if (flags & VM_IMPORT) {
-                    const double* qq = stage_in + 3 * (size_t)(c.hoff + j);
-                    xj[0] = qq[0]; xj[1] = qq[1];
-                } else if (flags & VM_PREDICT) {
-                    double vhj[2];
-                    predict_mixed(ld4(X + j), ld4(c.vel + j), ld4(c.acc + j), dt, hdt, vhj, xj);
-                } else {
-                    const double4 t = ld4v(xo + j);
-                    xj[0] = t.x; xj[1] = t.y;
-                }
-                const double cr = xn[0] * xj[1] - xj[0] * xn[1];
-                s0 += 0.5 * cr;
-                s1 += (1.0 / 6.0) * (xn[0] + xj[0]) * cr;
-                s2 += (1.0 / 6.0) * (xn[1] + xj[1]) * cr;
-            }
-            st4(c.bnd_part + rank, s0, s1, s2);
-            __threadfence();
-        }
+        // boundary positions are read by the block that finishes the area
+        if (!(flags & VM_NOAREA) && c.bnd_rank[v] >= 0) __threadfence();
     }
-    if (!(flags & VM_NOAREA)) finish_area_boundary(c);
+    if (!(flags & VM_NOAREA)) finish_area_boundary(c, c.pos[c.ctl[0] ^ 1]);
 }
 
 void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
