@@ -72,29 +72,53 @@ inline float f64_to_f32_slow(double x) { return (float)x; }
 inline double f32_to_f64_slow(float f) { return (double)f; }
 #endif
 
-// binary64 -> binary32, round to nearest even
+WCFE_HD uint32_t dhi(double x) {
+#if defined(__CUDA_ARCH__)
+    return (uint32_t)__double2hiint(x);
+#else
+    return (uint32_t)(dbits(x) >> 32);
+#endif
+}
+WCFE_HD uint32_t dlo(double x) {
+#if defined(__CUDA_ARCH__)
+    return (uint32_t)__double2loint(x);
+#else
+    return (uint32_t)dbits(x);
+#endif
+}
+WCFE_HD double dmake(uint32_t hi, uint32_t lo) {
+#if defined(__CUDA_ARCH__)
+    return __hiloint2double((int)hi, (int)lo);
+#else
+    return bitsd(((uint64_t)hi << 32) | lo);
+#endif
+}
+
+// binary64 -> binary32, round to nearest even.  32-bit integer operations only.
 WCFE_HD float f64_to_f32_rn(double x) {
-    const uint64_t b = dbits(x);
-    const uint64_t s = b & 0x8000000000000000ull;
-    const uint64_t a = b ^ s;
+    const uint32_t hi = dhi(x), lo = dlo(x);
+    const uint32_t s = hi & 0x80000000u;
+    const uint32_t ah = hi ^ s;
     // normal binary32 results: biased binary64 exponent in [897, 1150]
-    if (a - (897ull << 52) < (254ull << 52)) {
-        uint64_t r = a - (896ull << 52);            // rebias the exponent to binary32's
-        r += 0x0FFFFFFFull + ((r >> 29) & 1ull);    // round the 52-bit fraction to 23 bits, ties to even
-        return bitsf((uint32_t)(r >> 29) | (uint32_t)(s >> 32));
+    if (ah - (897u << 20) < (254u << 20)) {
+        const uint32_t rh = ah - (896u << 20);        // rebias the exponent to binary32's
+        // round the 52-bit fraction to 23 bits (ties to even): add 2^28 - 1 + bit 29, carry into the high word
+        const uint32_t t = lo + 0x0FFFFFFFu + ((lo >> 29) & 1u);
+        const uint32_t rh2 = rh + (t < lo ? 1u : 0u);
+        return bitsf(((rh2 << 3) | (t >> 29)) | s);
     }
     // |x| < 2^-150 (exponent <= 872) rounds to a signed zero
-    if (a < (873ull << 52)) return bitsf((uint32_t)(s >> 32));
+    if (ah < (873u << 20)) return bitsf(s);
     return f64_to_f32_slow(x);                     // subnormal results, overflow, inf, NaN
 }
 
-// binary32 -> binary64, exact
+// binary32 -> binary64, exact.  32-bit integer operations only.
 WCFE_HD double f32_to_f64(float f) {
     const uint32_t b = fbits(f);
     const uint32_t s = b & 0x80000000u;
     const uint32_t a = b ^ s;
-    if (a - 0x00800000u < 0x7f000000u) return bitsd((((uint64_t)a << 29) + (896ull << 52)) | ((uint64_t)s << 32));
-    if (a == 0) return bitsd((uint64_t)s << 32);  // signed zero
+    if (a - 0x00800000u < 0x7f000000u) return dmake(((a >> 3) + (896u << 20)) | s, a << 29);
+    if (a == 0) return dmake(s, 0u);               // signed zero
     return f32_to_f64_slow(f);                     // subnormal, inf, NaN
 }
 
