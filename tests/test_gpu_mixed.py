@@ -1,5 +1,6 @@
-"""GPU: the mixed-precision form (FP32 increment-form assembly, FP64 state and
-update) against the FP64 form, and the batched drop-in exchange path.
+"""GPU: the mixed-precision form (FP32 increment-form assembly and forces,
+float-float state and accumulation) against the FP64 form, and the batched
+drop-in exchange path.
 
 Mixed-form tolerance: relative displacement error <= 1e-6 against the FP64 form
 after 300 steps (max|x_mixed - x_fp64| / max|x_fp64 - x0| per cell)."""
@@ -80,7 +81,10 @@ def test_mixed_batched_equals_alone():
 @pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
 def test_exchange_path_equals_internal_steps(prec):
     """wcfe_engine_predict / wcfe_engine_update with the host returning the predicted
-    positions unchanged is the same computation as wcfe_engine_step: bit-identical."""
+    positions unchanged is the same computation as wcfe_engine_step: bit-identical for
+    the FP64 form.  The mixed form keeps positions as float-float pairs (about 48
+    bits) and the exchange carries them as binary64, which can round a pair's low
+    part; its results agree to 1e-9 of each array's magnitude."""
     cells = [synth.disk_mesh(n, seed=300 + n) for n in (400, 1300)]
     res = []
     for mode in ("internal", "exchange"):
@@ -102,7 +106,35 @@ def test_exchange_path_equals_internal_steps(prec):
         e.close()
     for a, b in zip(*res):
         for u, w in zip(a, b):
-            assert np.array_equal(u, w)
+            if prec == capi.PREC_FP64:
+                assert np.array_equal(u, w)
+            else:
+                assert np.max(np.abs(u - w)) <= 1e-9 * max(np.max(np.abs(w)), 1e-12)
+
+
+def test_mixed_engine_refuses_per_function_entry_points():
+    """The reference-function mirrors run on FP64 engines; a mixed engine says so."""
+    x0, tri = synth.disk_mesh(300, seed=8)
+    e = capi.Engine(capi.PREC_MIXED)
+    h = e.add_cell(x0, tri, default_params("k1"), state=synth.initial_state(x0))
+    with pytest.raises(capi.WcfeError):
+        h.predict(5e-5)
+    with pytest.raises(capi.WcfeError):
+        h.eval_forces(x0, 5e-5)
+    e.close()
+
+
+def test_mixed_state_round_trip():
+    """set_state / get_state of a mixed engine: float-float storage keeps 48 bits."""
+    x0, tri = synth.disk_mesh(500, seed=9)
+    st = synth.initial_state(x0, perturb=1.0, seed=3)
+    e = capi.Engine(capi.PREC_MIXED)
+    h = e.add_cell(x0, tri, default_params("k31"), state=st)
+    got = h.get_state()
+    for k, (a, b) in enumerate(zip(got, st)):
+        tol = 2.0 ** -23 if k == 2 else 2.0 ** -47   # the acceleration is stored in FP32
+        assert np.all(np.abs(a - b) <= tol * np.abs(b) + 1e-300), k
+    e.close()
 
 
 def test_integrin_density_mask():

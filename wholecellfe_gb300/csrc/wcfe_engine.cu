@@ -534,6 +534,62 @@ int get3(wcfe_engine* e, double* h, const double4* d, int n) {
     return WCFE_OK;
 }
 
+// A mixed engine keeps its state as float-float pairs (hi = RN(x), lo = RN(x - hi))
+// in the same slots (wcfe_ff.cuh): pos, vel, fau as {hi.xyz0, lo.xyz0}; acc as the
+// FP32 acceleration; ea as {hi xx yy zz xy, lo xx yy zz xy, hi xz yz, lo xz yz};
+// cA, cC as {hi, lo}.  These convert on the host.
+inline void split_ff(double x, float* hi, float* lo) {
+    const float h = (float)x;
+    *hi = h;
+    *lo = (float)(x - (double)h);
+}
+int put_ff(wcfe_engine* e, void* d, const double* h, int n, int kind) {
+    std::vector<float> b;
+    if (kind == 0 || kind == 1) {          // [n][3] vectors -> ff4 (kind 1: acceleration, hi only)
+        b.assign((size_t)8 * n, 0.0f);
+        for (int v = 0; v < n; ++v)
+            for (int k = 0; k < 3; ++k) {
+                if (kind == 1) b[8 * (size_t)v + k] = (float)h[3 * (size_t)v + k];
+                else split_ff(h[3 * (size_t)v + k], &b[8 * (size_t)v + k], &b[8 * (size_t)v + 4 + k]);
+            }
+    } else if (kind == 2) {                // [n][6] strain (xx yy zz xy xz yz) -> ffea
+        b.assign((size_t)12 * n, 0.0f);
+        for (int v = 0; v < n; ++v) {
+            const double* q = h + 6 * (size_t)v;
+            float* o = &b[12 * (size_t)v];
+            for (int k = 0; k < 4; ++k) split_ff(q[k], &o[k], &o[4 + k]);
+            split_ff(q[4], &o[8], &o[10]);
+            split_ff(q[5], &o[9], &o[11]);
+        }
+    } else {                               // [n] scalars -> ff
+        b.assign((size_t)2 * n, 0.0f);
+        for (int v = 0; v < n; ++v) split_ff(h[v], &b[2 * (size_t)v], &b[2 * (size_t)v + 1]);
+    }
+    CK(cudaMemcpyAsync(d, b.data(), sizeof(float) * b.size(), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+int get_ff(wcfe_engine* e, double* h, const void* d, int n, int kind) {
+    const size_t per = kind <= 1 ? 8 : kind == 2 ? 12 : 2;
+    std::vector<float> b(per * (size_t)n);
+    CK(cudaMemcpyAsync(b.data(), d, sizeof(float) * b.size(), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    auto ffd = [](float hi, float lo) { return (double)hi + (double)lo; };
+    for (int v = 0; v < n; ++v) {
+        const float* o = &b[per * (size_t)v];
+        if (kind == 0) for (int k = 0; k < 3; ++k) h[3 * (size_t)v + k] = ffd(o[k], o[4 + k]);
+        else if (kind == 1) for (int k = 0; k < 3; ++k) h[3 * (size_t)v + k] = (double)o[k];
+        else if (kind == 2) {
+            double* q = h + 6 * (size_t)v;
+            for (int k = 0; k < 4; ++k) q[k] = ffd(o[k], o[4 + k]);
+            q[4] = ffd(o[8], o[10]);
+            q[5] = ffd(o[9], o[11]);
+        } else h[v] = ffd(o[0], o[1]);
+    }
+    return WCFE_OK;
+}
+enum { FF_VEC = 0, FF_ACC = 1, FF_EA = 2, FF_SCALAR = 3 };
+
 }  // namespace
 
 // =============================================================================
@@ -744,6 +800,17 @@ int wcfe_cell_set_state(wcfe_engine* e, int32_t id, const double* x, const doubl
                 return fail("the mixed form needs counter-clockwise, non-degenerate triangles", WCFE_ERR_ARG);
         }
     }
+    if (e->prec == WCFE_PREC_MIXED) {
+        if (x && (r = put_ff(e, d.pos[par], x, n, FF_VEC))) return r;
+        if (V && (r = put_ff(e, d.vel, V, n, FF_VEC))) return r;
+        if (A && (r = put_ff(e, d.acc, A, n, FF_ACC))) return r;
+        if (fau && (r = put_ff(e, d.fau, fau, n, FF_VEC))) return r;
+        // both strain buffers: the mixed step carries xz, yz (zero rates in the plane) unchanged
+        if (ea && ((r = put_ff(e, d.ea[par], ea, n, FF_EA)) || (r = put_ff(e, d.ea[par ^ 1], ea, n, FF_EA)))) return r;
+        if (cA && (r = put_ff(e, d.cA, cA, n, FF_SCALAR))) return r;
+        if (cC && (r = put_ff(e, d.cC, cC, n, FF_SCALAR))) return r;
+        return WCFE_OK;
+    }
     if (x && (r = put3(e, d.pos[par], x, n))) return r;
     if (V && (r = put3(e, d.vel, V, n))) return r;
     if (A && (r = put3(e, d.acc, A, n))) return r;
@@ -765,6 +832,16 @@ int wcfe_cell_get_state(wcfe_engine* e, int32_t id, double* x, double* V, double
     if (r) return r;
     const int n = c->topo.nv;
     CellDev& d = c->dev;
+    if (e->prec == WCFE_PREC_MIXED) {
+        if (x && (r = get_ff(e, x, d.pos[par], n, FF_VEC))) return r;
+        if (V && (r = get_ff(e, V, d.vel, n, FF_VEC))) return r;
+        if (A && (r = get_ff(e, A, d.acc, n, FF_ACC))) return r;
+        if (fau && (r = get_ff(e, fau, d.fau, n, FF_VEC))) return r;
+        if (ea && (r = get_ff(e, ea, d.ea[par], n, FF_EA))) return r;
+        if (cA && (r = get_ff(e, cA, d.cA, n, FF_SCALAR))) return r;
+        if (cC && (r = get_ff(e, cC, d.cC, n, FF_SCALAR))) return r;
+        return WCFE_OK;
+    }
     if (x && (r = get3(e, x, d.pos[par], n))) return r;
     if (V && (r = get3(e, V, d.vel, n))) return r;
     if (A && (r = get3(e, A, d.acc, n))) return r;
@@ -821,6 +898,8 @@ int wcfe_cell_sizes(wcfe_engine* e, int32_t id, int32_t* nv, int32_t* nt, int32_
 int wcfe_cell_predict(wcfe_engine* e, int32_t id, double dt, double* x_pred, double* V_hlf) {
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    if (e->prec == WCFE_PREC_MIXED)
+        return fail("the per-function entry points run on an FP64 engine (WCFE_PREC_FP64)", WCFE_ERR_STATE);
     CK(cudaSetDevice(e->device));
     int r = sync_tables(e);
     if (r) return r;
@@ -841,6 +920,8 @@ int wcfe_cell_update_fa(wcfe_engine* e, int32_t id, double dt_real, const double
                         const double* X_s, const double* x_s) {
     Cell* c = e ? find(e, id) : nullptr;
     if (!c || !x_new) return fail("bad argument", WCFE_ERR_ARG);
+    if (e->prec == WCFE_PREC_MIXED)
+        return fail("the per-function entry points run on an FP64 engine (WCFE_PREC_FP64)", WCFE_ERR_STATE);
     CK(cudaSetDevice(e->device));
     if ((X_s || x_s) && c->sub_nt > 0) {
         bool changedX = X_s && std::memcmp(X_s, c->sub_X.data(), sizeof(double) * 3 * c->sub_nv) != 0;
@@ -882,6 +963,8 @@ int wcfe_cell_update_fa(wcfe_engine* e, int32_t id, double dt_real, const double
 int wcfe_cell_update_forces(wcfe_engine* e, int32_t id, double dt, double dt_real, double t_tot) {
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    if (e->prec == WCFE_PREC_MIXED)
+        return fail("the per-function entry points run on an FP64 engine (WCFE_PREC_FP64)", WCFE_ERR_STATE);
     CK(cudaSetDevice(e->device));
     int r = sync_tables(e);
     if (r) return r;
@@ -904,6 +987,8 @@ int wcfe_cell_eval_residual(wcfe_engine* e, int32_t id, const double* X, const d
                             double* Res_Adif, double* Res_Cdif) {
     Cell* c = e ? find(e, id) : nullptr;
     if (!c || !X || !x_new || !centroid) return fail("bad argument", WCFE_ERR_ARG);
+    if (e->prec == WCFE_PREC_MIXED)
+        return fail("the per-function entry points run on an FP64 engine (WCFE_PREC_FP64)", WCFE_ERR_STATE);
     CK(cudaSetDevice(e->device));
     int r = sync_tables(e);
     if (r) return r;
@@ -945,6 +1030,8 @@ int wcfe_cell_eval_forces(wcfe_engine* e, int32_t id, const double* x, double dt
                           double* F_bend, double* F_area, double area4[4]) {
     Cell* c = e ? find(e, id) : nullptr;
     if (!c || !x) return fail("bad argument", WCFE_ERR_ARG);
+    if (e->prec == WCFE_PREC_MIXED)
+        return fail("the per-function entry points run on an FP64 engine (WCFE_PREC_FP64)", WCFE_ERR_STATE);
     CK(cudaSetDevice(e->device));
     int r = sync_tables(e);
     if (r) return r;

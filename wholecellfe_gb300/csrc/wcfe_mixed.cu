@@ -36,6 +36,7 @@
 
 #include "wcfe_common.cuh"
 #include "wcfe_cvt.h"
+#include "wcfe_ff.cuh"
 
 namespace wcfe {
 
@@ -43,19 +44,49 @@ struct MixedArgs {
     const CellDev* cells;
     const WorkItem* work;
     int nwork, emax;
-    double dt, dt_real, hdt, cdt, ap_thresh, t_override;
-    int vh_from_buf, half;   // cdt = dt_real - dt/2; half = dt_real > dt/2
+    double dt_real, ap_thresh, t_override;
+    ff hdt, cdt, dtr;        // dt/2, dt_real - dt/2, dt_real as float-float
+    int vh_from_buf, half;   // half = dt_real > dt/2
 };
 
-// sign tests of doubles on the integer pipe (the FP64 pipe is the scarce one)
-__device__ __forceinline__ bool dzero(double x) { return (dbits(x) << 1) == 0; }
-__device__ __forceinline__ bool dneg(double x) {   // x < 0
-    const uint64_t b = dbits(x);
-    return (int64_t)b < 0 && (b << 1) != 0 && (b << 1) <= (0x7FF0000000000000ull << 1);
+// The mixed engine's state arrays hold float-float values (wcfe_ff.cuh) in the
+// slots the FP64 engine uses for doubles: pos, vel, fau and vhl as ff4 (32 B),
+// ea as ffea (48 B), cA and cC as ff (8 B); acc holds the FP32 acceleration as a
+// float4 in the first half of its 32-B slot.
+__device__ __forceinline__ ff4 ldg_ff4(const double4* base, int v) {
+    const float4* q = reinterpret_cast<const float4*>(base + v);
+    const float4 h = __ldg(q), l = __ldg(q + 1);
+    return {h.x, h.y, h.z, h.w, l.x, l.y, l.z, l.w};
 }
-__device__ __forceinline__ bool dpos(double x) {   // x > 0
-    const uint64_t b = dbits(x);
-    return (int64_t)b > 0 && b <= 0x7FF0000000000000ull;
+__device__ __forceinline__ ff4 ld_ff4(const double4* base, int v) {   // coherent: written in this launch
+    const float4* q = reinterpret_cast<const float4*>(base + v);
+    const float4 h = __ldcg(q), l = __ldcg(q + 1);
+    return {h.x, h.y, h.z, h.w, l.x, l.y, l.z, l.w};
+}
+__device__ __forceinline__ void st_ff4(double4* base, int v, const ff4& a) {
+    float4* q = reinterpret_cast<float4*>(base + v);
+    q[0] = make_float4(a.hx, a.hy, a.hz, a.hw);
+    q[1] = make_float4(a.lx, a.ly, a.lz, a.lw);
+}
+__device__ __forceinline__ ff ld_ff(const double* base, int v) {
+    const float2 t = __ldg(reinterpret_cast<const float2*>(base) + v);
+    return {t.x, t.y};
+}
+__device__ __forceinline__ void st_ff(double* base, int v, ff a) {
+    reinterpret_cast<float2*>(base)[v] = make_float2(a.hi, a.lo);
+}
+__device__ __forceinline__ float4 ld_acc(const double4* base, int v) {
+    return __ldg(reinterpret_cast<const float4*>(base + v));
+}
+// positions as doubles (boundary terms, area, exchange)
+__device__ __forceinline__ void pos_d(const ff4& a, double x[3]) {
+    x[0] = ff_to_d(ffx(a)); x[1] = ff_to_d(ffy(a)); x[2] = ff_to_d(ffz(a));
+}
+// predicted velocity and position of one in-plane component:
+// vh = V + (dt/2) A, x = X + dt vh (the z component does not move, UL:119)
+__device__ __forceinline__ void predict_ff(ff X, ff V, float A, ff hdt, ff dt, ff& vh, ff& x) {
+    vh = ff_add(V, ff_mul_f(hdt, A));
+    x = ff_add(X, ff_mul(dt, vh));
 }
 
 constexpr int kRec = 3;      // float4 per vertex record
@@ -211,6 +242,29 @@ __device__ __forceinline__ void element2d(const float4 r[3][kRec], const ElemPar
 
 constexpr int kBndSlots = 128;   // boundary vertices a patch CTA queues for its second loop
 
+// The neighbour frame of a boundary vertex (UL:1500-1531) on float-float positions:
+// the same candidate scan and orientation test as boundary_frame, on the positions
+// converted to binary64.
+__device__ __forceinline__ bool boundary_frame_ff(const CellDev& c, const double4* __restrict__ xp, int rank,
+                                                  const double xi[3], double x1[3], double x2[3]) {
+    int j1 = -1, j2 = -1;
+    for (int k = c.bnd_cptr[rank]; k < c.bnd_cptr[rank + 1]; ++k) {
+        const int2 cd = c.bnd_cand[k];
+        double pb[3], pi[3];
+        pos_d(ldg_ff4(xp, cd.x), pb);
+        pos_d(ldg_ff4(xp, cd.y), pi);
+        const double d1x = xs(xi[0], pb[0]), d1y = xs(xi[1], pb[1]);
+        const double d2x = xs(pi[0], xi[0]), d2y = xs(pi[1], xi[1]);
+        const double ncz = xs(xm(d1x, d2y), xm(d1y, d2x));
+        if (ncz > 0) j1 = cd.x;
+        else j2 = cd.x;
+    }
+    if (j1 < 0 || j2 < 0) return false;
+    pos_d(ldg_ff4(xp, j1), x1);
+    pos_d(ldg_ff4(xp, j2), x2);
+    return true;
+}
+
 // Boundary terms of vertex v (rank `rank`) in FP64, added to (F0, F1): the isotropic
 // active stress of the open one-ring, AP push (calculateForce_AP UL:1477-1569),
 // bending (calculateBendingForce2D UL:1571-1689) and area constraint
@@ -222,24 +276,24 @@ __device__ __forceinline__ void boundary_force(const CellDev& c, const MixedArgs
     const double t = isnan(a.t_override) ? c.clk[0] : a.t_override;
     const double s_iso = p.kappa * (t < p.tact_t1 ? t * p.tact_rate : p.tact_max);
     const double area_tot = c.area4[0];
-    const double4 xv4 = ld4v(xp + v);
-    const double xi[3] = {xv4.x, xv4.y, xv4.z};
+    double xi[3];
+    pos_d(ldg_ff4(xp, v), xi);
     // isotropic active stress on the open one-ring: (1/2) s_iso thick e3 x sum (X_k - X_j)
-    double sx = 0, sy = 0;
+    ff sx = {0.0f, 0.0f}, sy = {0.0f, 0.0f};
     for (int k = c.vt_ptr[v]; k < c.vt_ptr[v + 1]; ++k) {
         const int code = c.vc_code[k];
         const int cn = code & 3;
         const int e = c.patch_elems[pt.z + (code >> 2)];
         const int4 t4 = c.tri[e];
         const int ids[3] = {t4.x, t4.y, t4.z};
-        const double4 Xj = ld4v(X + ids[(cn + 1) % 3]), Xk = ld4v(X + ids[(cn + 2) % 3]);
-        sx += Xk.x - Xj.x;
-        sy += Xk.y - Xj.y;
+        const ff4 Xj = ldg_ff4(X, ids[(cn + 1) % 3]), Xk = ldg_ff4(X, ids[(cn + 2) % 3]);
+        sx = ff_add(sx, ff_sub(ffx(Xk), ffx(Xj)));
+        sy = ff_add(sy, ff_sub(ffy(Xk), ffy(Xj)));
     }
     const double w = 0.5 * s_iso * p.thick;
-    double Fb0 = w * sy, Fb1 = -w * sx;  // minus the residual term w e3 x s
+    double Fb0 = w * ff_to_d(sy), Fb1 = -w * ff_to_d(sx);  // minus the residual term w e3 x s
     double x1[3], x2[3];
-    if (boundary_frame(c, xp, rank, xi, x1, x2)) {
+    if (boundary_frame_ff(c, xp, rank, xi, x1, x2)) {
         const double d1x = xi[0] - x1[0], d1y = xi[1] - x1[1], d2x = x2[0] - xi[0], d2y = x2[1] - xi[1];
         const double d1z = xi[2] - x1[2], d2z = x2[2] - xi[2];
         const double nn1 = sqrt(d1y * d1y + d1x * d1x), nn2 = sqrt(d2y * d2y + d2x * d2x);
@@ -265,53 +319,53 @@ __device__ __forceinline__ void boundary_force(const CellDev& c, const MixedArgs
         Fb0 += fb * nx;
         Fb1 += fb * ny;
     }
-    F0 += (float)Fb0;
-    F1 += (float)Fb1;
+    F0 += f64_to_f32_rn(Fb0);
+    F1 += f64_to_f32_rn(Fb1);
 }
 
-// Explicit update of vertex v (UL:592-628): A in FP32 from the FP32 force; V and the
-// strain accumulate in FP64.
+// Explicit update of vertex v (UL:592-628): the acceleration in FP32 from the FP32
+// force; the velocity and the strain accumulate in float-float.
 __device__ __forceinline__ void finish_vertex(const CellDev& c, const MixedArgs& a, int par, int v, float F0, float F1,
                                               float Q0, float Q1, float Q2, float Q3, float MMf) {
     const ParamF& pf = c.pf;
-    const double4 V4 = ld4v(c.vel + v), A4 = ld4v(c.acc + v);
-    double vh0, vh1;
+    const ff4 V = ldg_ff4(c.vel, v);
+    ff vh0, vh1;
     if (a.vh_from_buf) {
-        const double4 h = ld4v(c.vhl + v);
-        vh0 = h.x; vh1 = h.y;
+        const ff4 h = ldg_ff4(c.vhl, v);
+        vh0 = ffx(h); vh1 = ffy(h);
     } else {
-        vh0 = fma(a.hdt, A4.x, V4.x);
-        vh1 = fma(a.hdt, A4.y, V4.y);
+        const float4 A = ld_acc(c.acc, v);
+        vh0 = ff_add(ffx(V), ff_mul_f(a.hdt, A.x));
+        vh1 = ff_add(ffy(V), ff_mul_f(a.hdt, A.y));
     }
     const float rhom = pf.rho;
     const float iM = 1.0f / (MMf * rhom);
     const float damp_m = pf.damp * MMf * rhom;
-    const float vh0f = f64_to_f32_rn(vh0), vh1f = f64_to_f32_rn(vh1);
-    const float An0 = (F0 - pf.drag * vh0f - damp_m * f64_to_f32_rn(V4.x)) * iM;
-    const float An1 = (F1 - pf.drag * vh1f - damp_m * f64_to_f32_rn(V4.y)) * iM;
-    const float An2 = dzero(V4.z) ? 0.0f : (-damp_m * f64_to_f32_rn(V4.z)) * iM;  // no force normal to the plane
-    const double An0d = f32_to_f64(An0), An1d = f32_to_f64(An1), An2d = f32_to_f64(An2);
-    double Vn0, Vn1, Vn2;
+    const float An0 = (F0 - pf.drag * vh0.hi - damp_m * V.hx) * iM;
+    const float An1 = (F1 - pf.drag * vh1.hi - damp_m * V.hy) * iM;
+    const float An2 = V.hz == 0.0f ? 0.0f : (-damp_m * V.hz) * iM;  // no force normal to the plane
+    ff Vn0, Vn1, Vn2;
     if (a.half) {
-        Vn0 = fma(a.cdt, An0d, vh0);
-        Vn1 = fma(a.cdt, An1d, vh1);
-        Vn2 = a.cdt * An2d;
+        Vn0 = ff_add(vh0, ff_mul_f(a.cdt, An0));
+        Vn1 = ff_add(vh1, ff_mul_f(a.cdt, An1));
+        Vn2 = ff_mul_f(a.cdt, An2);
     } else {
-        Vn0 = fma(a.dt_real, An0d, V4.x);
-        Vn1 = fma(a.dt_real, An1d, V4.y);
-        Vn2 = fma(a.dt_real, An2d, V4.z);
+        Vn0 = ff_add(ffx(V), ff_mul_f(a.dtr, An0));
+        Vn1 = ff_add(ffy(V), ff_mul_f(a.dtr, An1));
+        Vn2 = ff_add(ffz(V), ff_mul_f(a.dtr, An2));
     }
-    const double2* eo = reinterpret_cast<const double2*>(c.ea[par] + 6 * (size_t)v);
-    double2* en = reinterpret_cast<double2*>(c.ea[par ^ 1] + 6 * (size_t)v);
+    const float4* eo = reinterpret_cast<const float4*>(c.ea[par] + 6 * (size_t)v);
+    float4* en = reinterpret_cast<float4*>(c.ea[par ^ 1] + 6 * (size_t)v);
+    const float4 eh = __ldg(eo), el = __ldg(eo + 1);   // (xx, yy, zz, xy) hi and lo; (xz, yz) stay as set
     const float iMM = 1.0f / MMf;
-    const double2 e0 = eo[0], e1 = eo[1], e2 = eo[2];  // (xx, yy), (zz, xy), (xz, yz)
-    en[0] = make_double2(e0.x + f32_to_f64(Q0 * iMM), e0.y + f32_to_f64(Q1 * iMM));
-    en[1] = make_double2(e1.x + f32_to_f64(Q3 * iMM), e1.y + f32_to_f64(Q2 * iMM));
-    en[2] = e2;
-    st4(c.acc + v, An0d, An1d, An2d);
-    st4(c.vel + v, Vn0, Vn1, Vn2);
+    const ff exx = ff_add_f({eh.x, el.x}, Q0 * iMM), eyy = ff_add_f({eh.y, el.y}, Q1 * iMM);
+    const ff ezz = ff_add_f({eh.z, el.z}, Q3 * iMM), exy = ff_add_f({eh.w, el.w}, Q2 * iMM);
+    en[0] = make_float4(exx.hi, eyy.hi, ezz.hi, exy.hi);
+    en[1] = make_float4(exx.lo, eyy.lo, ezz.lo, exy.lo);
+    *reinterpret_cast<float4*>(c.acc + v) = make_float4(An0, An1, An2, 0.0f);
+    st_ff4(c.vel, v, make_ff4(Vn0, Vn1, Vn2));
     // NaN/Inf in the state shows up in the FP32 quantities derived from it
-    const float chk = An0 + An1 + Q0 + Q1 + Q2 + vh0f + vh1f;
+    const float chk = An0 + An1 + Q0 + Q1 + Q2 + vh0.hi + vh1.hi;
     if (!isfinite(chk)) atomicOr(c.status, 1u);
 }
 
@@ -392,11 +446,11 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             }
             const float Asum = Asf * (1.0f / 3.0f);
             // integrin force (UL:1241-1269) in FP32
-            const double4 f4 = ld4v(c.fau + v);
+            const ff4 f4 = ldg_ff4(c.fau, v);
             float fs[3], bell;
-            spring_force32(pf, f64_to_f32_rn(f4.x), f64_to_f32_rn(f4.y), f64_to_f32_rn(f4.z), fs, &bell);
+            spring_force32(pf, f4.hx, f4.hy, f4.hz, fs, &bell);
             const float rho = c.rho_w ? f64_to_f32_rn(c.rho_w[v]) : rho_max;
-            const float kfa = -f64_to_f32_rn(c.cC[v]) * Asum * rho;
+            const float kfa = -ld_ff(c.cC, v).hi * Asum * rho;
             float F0 = kfa * fs[0] - R0, F1 = kfa * fs[1] - R1;
             const int rank = c.bnd_rank[v];
             if (rank >= 0) {
@@ -443,15 +497,6 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
 // ===========================================================================
 enum { VM_PREDICT = 1, VM_UPDATE_FA = 2, VM_EXPORT = 8, VM_IMPORT = 16, VM_NOAREA = 32 };
 
-__device__ __forceinline__ void predict_mixed(const double4& X, const double4& V, const double4& A, double dt,
-                                              double hdt, double vh[2], double xn[3]) {
-    vh[0] = fma(hdt, A.x, V.x);
-    vh[1] = fma(hdt, A.y, V.y);
-    xn[0] = fma(dt, vh[0], X.x);
-    xn[1] = fma(dt, vh[1], X.y);
-    xn[2] = X.z;  // V_hlf.z = 0 (UL:119)
-}
-
 // The cell area and centroid of the mixed form, from the predicted positions of
 // the boundary loop (shoelace over the directed boundary edges).  The last block
 // of the cell to finish (ticket ctl[2]) reads the positions the other blocks
@@ -472,13 +517,15 @@ __device__ __forceinline__ void finish_area_boundary(const CellDev& c, const dou
     __threadfence();
     double s0 = 0, s1 = 0, s2 = 0;
     for (int r = threadIdx.x; r < c.nb; r += blockDim.x) {
-        const double2 xi = __ldcg(reinterpret_cast<const double2*>(xo + c.bnd_vert[r]));
+        double xi[3];
+        pos_d(ld_ff4(xo, c.bnd_vert[r]), xi);
         for (int k = c.bnd_optr[r]; k < c.bnd_optr[r + 1]; ++k) {
-            const double2 xj = __ldcg(reinterpret_cast<const double2*>(xo + c.bnd_out[k]));
-            const double cr = xi.x * xj.y - xj.x * xi.y;
+            double xj[3];
+            pos_d(ld_ff4(xo, c.bnd_out[k]), xj);
+            const double cr = xi[0] * xj[1] - xj[0] * xi[1];
             s0 += 0.5 * cr;
-            s1 += (1.0 / 6.0) * (xi.x + xj.x) * cr;
-            s2 += (1.0 / 6.0) * (xi.y + xj.y) * cr;
+            s1 += (1.0 / 6.0) * (xi[0] + xj[0]) * cr;
+            s2 += (1.0 / 6.0) * (xi[1] + xj[1]) * cr;
         }
     }
 #pragma unroll
@@ -505,96 +552,115 @@ __device__ __forceinline__ void finish_area_boundary(const CellDev& c, const dou
     }
 }
 
-// One block per work item (a block of c.vb consecutive vertices of one cell).
+struct VertexArgs {
+    ff dt, hdt;
+    float dtf;
+    int flags;
+    const double* stage_in;
+    double* stage_out;
+};
+
+// Mixed-form vertex phase, one block per work item (c.vb consecutive vertices of
+// one cell): predict, bond kinetics with FP32 rates and float-float accumulation,
+// and the FP32 element records.  No FP64 arithmetic outside the exchange
+// conversions and the area of the finishing block.
 __global__ void __launch_bounds__(kK1Threads, 3) k_vertex_phase_mixed(const CellDev* __restrict__ cells,
                                                                     const WorkItem* __restrict__ work,
-                                                                    double dt, double hdt, float dtf, int flags,
-                                                                    const double* __restrict__ stage_in,
-                                                                    double* __restrict__ stage_out) {
+                                                                    const VertexArgs va) {
     const WorkItem it = work[blockIdx.x];
     const CellDev& c = cells[it.cell];
     const int v = it.idx * c.vb + threadIdx.x;
+    const int flags = va.flags;
+    const int par = c.ctl[0];
+    double4* __restrict__ xo = c.pos[par ^ 1];
     if (v < c.nv) {
-        const int par = c.ctl[0];
         const double4* __restrict__ X = c.pos[par];
-        double4* __restrict__ xo = c.pos[par ^ 1];
-        const double4 Xv = ld4(X + v);
-        double xn[3];
+        const ff4 Xv = ldg_ff4(X, v);
+        ff xn0, xn1, xn2 = ffz(Xv);
         if (flags & VM_IMPORT) {
-            const double* qq = stage_in + 3 * (size_t)(c.hoff + v);
-            xn[0] = qq[0]; xn[1] = qq[1]; xn[2] = qq[2];
-            st4(xo + v, xn[0], xn[1], xn[2]);
+            const double* qq = va.stage_in + 3 * (size_t)(c.hoff + v);
+            xn0 = ff_from_d(qq[0]); xn1 = ff_from_d(qq[1]); xn2 = ff_from_d(qq[2]);
+            st_ff4(xo, v, make_ff4(xn0, xn1, xn2));
         } else if (flags & VM_PREDICT) {
-            double vh[2];
-            predict_mixed(Xv, ld4(c.vel + v), ld4(c.acc + v), dt, hdt, vh, xn);
-            st4(xo + v, xn[0], xn[1], xn[2]);
+            const ff4 V = ldg_ff4(c.vel, v);
+            const float4 A = ld_acc(c.acc, v);
+            ff vh0, vh1;
+            predict_ff(ffx(Xv), ffx(V), A.x, va.hdt, va.dt, vh0, xn0);
+            predict_ff(ffy(Xv), ffy(V), A.y, va.hdt, va.dt, vh1, xn1);
+            st_ff4(xo, v, make_ff4(xn0, xn1, xn2));
             if (flags & VM_EXPORT) {
-                st4(c.vhl + v, vh[0], vh[1], 0.0);
-                double* qq = stage_out + 3 * (size_t)(c.hoff + v);
-                qq[0] = xn[0]; qq[1] = xn[1]; qq[2] = xn[2];
+                st_ff4(c.vhl, v, make_ff4(vh0, vh1, {0.0f, 0.0f}));
+                double* qq = va.stage_out + 3 * (size_t)(c.hoff + v);
+                qq[0] = ff_to_d(xn0); qq[1] = ff_to_d(xn1); qq[2] = ff_to_d(xn2);
             }
         } else {
-            const double4 t = ld4v(xo + v);
-            xn[0] = t.x; xn[1] = t.y; xn[2] = t.z;
+            const ff4 t = ld_ff4(xo, v);
+            xn0 = ffx(t); xn1 = ffy(t); xn2 = ffz(t);
         }
-        const double cu0 = xn[0] - Xv.x, cu1 = xn[1] - Xv.y;  // exact differences
+        const ff cu0 = ff_sub(xn0, ffx(Xv)), cu1 = ff_sub(xn1, ffy(Xv));   // step displacement
         if (flags & VM_UPDATE_FA) {
             const ParamF& pf = c.pf;
-            const double4 f = ld4(c.fau + v);
-            const double cold = c.cC[v], cAv = c.cA[v];
-            double u0 = f.x + cu0, u1 = f.y + cu1, u2 = f.z;
+            const ff4 f = ldg_ff4(c.fau, v);
+            const ff cold = ld_ff(c.cC, v), cAv = ld_ff(c.cA, v);
+            ff u0 = ff_add(ffx(f), cu0), u1 = ff_add(ffy(f), cu1), u2 = ffz(f);
             if (c.has_sub && c.sub.moving) {
-                double wgt[3];
-                const int e = locate(c.sub, xs(Xv.x, f.x), xs(Xv.y, f.y), xs(Xv.z, f.z), wgt);
+                double wgt[3], Xd[3], fd[3];
+                pos_d(Xv, Xd);
+                pos_d(f, fd);
+                const int e = locate(c.sub, xs(Xd[0], fd[0]), xs(Xd[1], fd[1]), xs(Xd[2], fd[2]), wgt);
                 if (e >= 0) {
                     const int4 t = c.sub.tri[e];
                     const double4 a0 = ld4(c.sub.x + t.x), a1 = ld4(c.sub.x + t.y), a2 = ld4(c.sub.x + t.z);
                     const double4 b0 = ld4(c.sub.X + t.x), b1 = ld4(c.sub.X + t.y), b2 = ld4(c.sub.X + t.z);
-                    u0 -= wgt[0] * (a0.x - b0.x) + wgt[1] * (a1.x - b1.x) + wgt[2] * (a2.x - b2.x);
-                    u1 -= wgt[0] * (a0.y - b0.y) + wgt[1] * (a1.y - b1.y) + wgt[2] * (a2.y - b2.y);
-                    u2 -= wgt[0] * (a0.z - b0.z) + wgt[1] * (a1.z - b1.z) + wgt[2] * (a2.z - b2.z);
+                    u0 = ff_sub(u0, ff_from_d(wgt[0] * (a0.x - b0.x) + wgt[1] * (a1.x - b1.x) + wgt[2] * (a2.x - b2.x)));
+                    u1 = ff_sub(u1, ff_from_d(wgt[0] * (a0.y - b0.y) + wgt[1] * (a1.y - b1.y) + wgt[2] * (a2.y - b2.y)));
+                    u2 = ff_sub(u2, ff_from_d(wgt[0] * (a0.z - b0.z) + wgt[1] * (a1.z - b1.z) + wgt[2] * (a2.z - b2.z)));
                 }
             }
             float fs[3], force;
-            spring_force32(pf, f64_to_f32_rn(u0), f64_to_f32_rn(u1), f64_to_f32_rn(u2), fs, &force);
+            spring_force32(pf, u0.hi, u1.hi, u2.hi, fs, &force);
             const float koff = pf.ka * __expf(force * pf.iFa) + pf.kb * __expf(-force * pf.iFb);
-            const float coldf = f64_to_f32_rn(cold), kon = pf.k_on;
-            double cn = cold + f32_to_f64(dtf * (kon * (1.0f - coldf) - koff * coldf));
-            if (dneg(cn)) cn = 0;
-            if (dneg(cAv)) c.cA[v] = 0;
-            double n0, n1, n2;
-            const bool keep_pos = dpos(cold) && (1.0f - dtf * koff) > 0.0f;
-            if (keep_pos && dpos(cn)) {
+            const float coldf = cold.hi, kon = pf.k_on, dtf = va.dtf;
+            ff cn = ff_add_f(cold, dtf * (kon * (1.0f - coldf) - koff * coldf));
+            if (cn.hi < 0.0f) cn = {0.0f, 0.0f};
+            if (cAv.hi < 0.0f) st_ff(c.cA, v, {0.0f, 0.0f});
+            ff n0, n1, n2;
+            const bool keep_pos = coldf > 0.0f && (1.0f - dtf * koff) > 0.0f;
+            if (keep_pos && cn.hi > 0.0f) {
                 // keep / c_new = 1 + ds with ds = -dt k_on (1 - c_old) / c_new exactly
-                const double ds = f32_to_f64(-dtf * kon * (1.0f - coldf) / f64_to_f32_rn(cn));
-                n0 = fma(u0, ds, u0); n1 = fma(u1, ds, u1); n2 = fma(u2, ds, u2);
+                const float ds = -dtf * kon * (1.0f - coldf) / cn.hi;
+                n0 = ff_add(u0, ff_mul_f(u0, ds)); n1 = ff_add(u1, ff_mul_f(u1, ds)); n2 = ff_add(u2, ff_mul_f(u2, ds));
             } else {
-                n0 = 0.0 * u0; n1 = 0.0 * u1; n2 = 0.0 * u2;
+                n0 = {0.0f * u0.hi, 0.0f}; n1 = {0.0f * u1.hi, 0.0f}; n2 = {0.0f * u2.hi, 0.0f};
             }
-            c.cC[v] = cn;
-            st4(c.fau + v, n0, n1, n2);
+            st_ff(c.cC, v, cn);
+            st_ff4(c.fau, v, make_ff4(n0, n1, n2));
         }
         if (!(flags & VM_EXPORT)) {
-            const double2* e2 = reinterpret_cast<const double2*>(c.ea[par] + 6 * (size_t)v);
-            const double2 q0 = __ldg(e2), q1 = __ldg(e2 + 1);  // (xx, yy), (zz, xy)
-            const float hx = f64_to_f32_rn(Xv.x), hy = f64_to_f32_rn(Xv.y);
-            const float lx = f64_to_f32_rn(Xv.x - f32_to_f64(hx)), ly = f64_to_f32_rn(Xv.y - f32_to_f64(hy));
+            const float4 eh = __ldg(reinterpret_cast<const float4*>(c.ea[par] + 6 * (size_t)v));  // (xx, yy, zz, xy)
             float4* r = c.rec + kRec * (size_t)v;
-            r[0] = make_float4(hx, hy, lx, ly);
-            r[1] = make_float4(f64_to_f32_rn(cu0), f64_to_f32_rn(cu1), f64_to_f32_rn(q0.x), f64_to_f32_rn(q0.y));
-            r[2] = make_float4(f64_to_f32_rn(q1.y), f64_to_f32_rn(q1.x), 0.0f, 0.0f);
+            r[0] = make_float4(Xv.hx, Xv.hy, Xv.lx, Xv.ly);
+            r[1] = make_float4(cu0.hi, cu1.hi, eh.x, eh.y);
+            r[2] = make_float4(eh.w, eh.z, 0.0f, 0.0f);
         }
         // boundary positions are read by the block that finishes the area
         if (!(flags & VM_NOAREA) && c.bnd_rank[v] >= 0) __threadfence();
     }
-    if (!(flags & VM_NOAREA)) finish_area_boundary(c, c.pos[c.ctl[0] ^ 1]);
+    if (!(flags & VM_NOAREA)) finish_area_boundary(c, xo);
 }
 
 void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
                          int threads, cudaStream_t st, const double* stage_in, double* stage_out) {
     if (nwork <= 0) return;
     (void)grid;   // one block per work item
-    k_vertex_phase_mixed<<<nwork, threads, 0, st>>>(cells, work, dt, dt / 2.0, (float)dt, flags, stage_in, stage_out);
+    VertexArgs va;
+    va.dt = ff_from_d(dt);
+    va.hdt = ff_from_d(dt / 2.0);
+    va.dtf = (float)dt;
+    va.flags = flags;
+    va.stage_in = stage_in;
+    va.stage_out = stage_out;
+    k_vertex_phase_mixed<<<nwork, threads, 0, st>>>(cells, work, va);
 }
 
 size_t mixed_smem_bytes(int emax) { return sizeof(float) * (size_t)emax * kSlot32; }
@@ -624,10 +690,10 @@ void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, i
     a.work = work;
     a.nwork = nwork;
     a.emax = emax;
-    a.dt = dt;
     a.dt_real = dt_real;
-    a.hdt = dt / 2.0;
-    a.cdt = dt_real - dt / 2.0;
+    a.hdt = ff_from_d(dt / 2.0);
+    a.cdt = ff_from_d(dt_real - dt / 2.0);
+    a.dtr = ff_from_d(dt_real);
     a.half = dt_real > dt / 2.0;
     a.ap_thresh = ap_thresh;
     a.t_override = t_override;
