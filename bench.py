@@ -7,8 +7,9 @@ drawn from {linear 1 pN/nm, linear 31 pN/nm, polynomial k0 = 31 pN/nm x0 = 5 nm}
 flat rigid substrate, dt = 5e-5 s, from rest.  One "step" advances every cell by
 one explicit step (A1-A9), so a step is 256 cell-steps.
 
-Reported on one JSON line: the headline value (batched mixed form, device-timed,
-inputs resident), e2e (the same loop through the batched drop-in exchange with
+Reported on one JSON line: the headline value (batched mixed form: FP32 element
+assembly and forces, float-float state and accumulation; device-timed, inputs
+resident), e2e (the same loop through the batched drop-in exchange with
 pinned host buffers: per step the predicted positions go to the host and the
 integrated positions come back), the plain FP64 one-cell form (about 2000 vertices),
 the relative displacement error of the mixed form against the FP64 form, per-step
@@ -95,7 +96,7 @@ def load_cells(eng, cells):
 
 # ----------------------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks and throttle reasons sampled every 100 ms while running."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -108,7 +109,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
             return
@@ -175,14 +176,16 @@ def cpu_baseline(cells, steps: int, budget_s: float = 15.0):
 
 # ----------------------------------------------------------------------------- measurements
 def kernel_bytes_patch_mixed(nv_total: int, nt_total: int) -> float:
-    """Algorithmic DRAM bytes of one mixed patch-phase launch: per vertex it reads the FP32
-    element record (48 B), the bond vector (24), c_C (8), V and A (48), the strain (48), the
-    one-ring offsets and slot codes (4 + 2 per incidence), and writes V, A (48) and the strain
-    (48); per element it reads the triangle (12) and its patch entry (4)."""
-    per_v = 48 + 24 + 8 + 48 + 48 + 4 + 48 + 48
-    per_incidence = 2
-    per_t = 12 + 4
-    return per_v * nv_total + per_incidence * 3 * nt_total + per_t * nt_total
+    """Algorithmic DRAM bytes of one mixed patch-phase launch (float-float state).
+    Per owned vertex it reads the FP32 element record (48 B), the high half of the
+    bond vector (16), c_C (4, its high word), the integrin density (8), V (32), the
+    FP32 acceleration (16), the strain xx yy zz xy (32), the one-ring offset and
+    boundary rank (8) and 2 B of slot code per incidence (3 per triangle); it writes
+    A (16), V (32) and the strain (32).  Per element it reads the triangle (16) and
+    its patch entry (4)."""
+    per_v = 48 + 16 + 4 + 8 + 32 + 16 + 32 + 8 + 16 + 32 + 32
+    per_t = 16 + 4 + 3 * 2
+    return per_v * nv_total + per_t * nt_total
 
 
 def percentile(xs, q):
@@ -357,7 +360,7 @@ def run_ours(args):
         out = {
             "metric": METRIC, "value": round(value, 1), "unit": "cell-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_s * 1e3 / args.steps, 4),
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32-assembly+fp64-update",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (assembly, forces) + float-float (state, accumulation)",
             "data": "synthetic: seeded disk meshes, random-init state from rest",
             "config": {"workload": f"{len(cells)} uneven cells per GPU, vertices log-uniform [500, 20000], "
                                    "integrins 0.4 x vertices, stiffness {linear 1, linear 31, poly 31 pN/nm x0 5 nm}, "
@@ -529,7 +532,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cells", type=int, default=N_CELLS)
