@@ -478,6 +478,8 @@ def run_phase(args):
     else:
         cells = make_workload(seed=1000, ncells=args.cells)
         eng = capi.Engine(capi.PREC_MIXED if args.phase == "mixed" else capi.PREC_FP64)
+        if args.phase == "mixed":
+            eng.set_patch_kernel(args.patch_kernel)
         load_cells(eng, cells)
         ncells = len(cells)
     for _ in range(args.warmup):
@@ -486,7 +488,8 @@ def run_phase(args):
     thr, emax = eng.shape()
     print(json.dumps({"phase": args.phase, "cells": ncells, "ms_per_step": r["total_ms"] / args.steps,
                       "vertex_ms": r["ms_v"] / args.steps, "patch_ms": r["ms_p"] / args.steps,
-                      "cell_steps_per_s": ncells * args.steps / (r["total_ms"] / 1e3), "shape": [thr, emax]}))
+                      "cell_steps_per_s": ncells * args.steps / (r["total_ms"] / 1e3), "shape": [thr, emax],
+                      "patch_kernel": args.patch_kernel}))
     eng.close()
 
 
@@ -541,6 +544,8 @@ def main():
                     help="length of the Poisson arrival window of the serving measurement (0: skip)")
     ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain"],
                     help="profiling aid: run only one timed loop (default shape, no autotune) and print its timing")
+    ap.add_argument("--patch-kernel", type=int, default=0, choices=[0, 1],
+                    help="with --phase mixed: 0 staged patch kernel (default), 1 plain")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

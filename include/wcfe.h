@@ -200,6 +200,13 @@ int wcfe_cell_eval_residual(wcfe_engine* eng, int32_t cell, const double* X, con
 int wcfe_cell_eval_forces(wcfe_engine* eng, int32_t cell, const double* x, double dt_real,
                           double* F_FA, double* F_AP, double* F_bend, double* F_area, double area4[4]);
 
+/* Mixed engines: which patch-phase kernel a step uses.  0 (default): the staged
+ * kernel (each patch's records and owned-vertex state copied into shared memory
+ * one patch ahead with bulk asynchronous copies) wherever its shared-memory plan
+ * fits, else the plain kernel; 1: always the plain kernel.  Results are identical.
+ * No counterpart in the reference. */
+int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind);
+
 /* ---- synthetic stepping of every live cell (no El Topo) ----------------- */
 /* nsteps full explicit steps of every live cell: predict, updateFA, updateForces.
  * All cells advance in one launch per phase; runs asynchronously on the engine stream. */
@@ -289,6 +296,16 @@ int wcfe_debug_topology(int32_t n_vert, int32_t n_tri, const int32_t* tri, const
                         int32_t* bnd_rank, int32_t* bnd_cptr, int32_t* bnd_cand, int32_t cand_cap, int32_t* np_out,
                         int32_t* patch, int32_t patch_cap, int32_t* patch_elems, int32_t elems_cap,
                         uint16_t* vc_code);
+
+/* The staging description the mixed form's patch kernel copies per patch: for
+ * each patch (h0, nh, c0, nc) = its halo list (vertices of its elements outside
+ * its owned range, ascending) and its one-ring code range; the corners of every
+ * element slot as patch-local vertex indices (owned v -> v - v0, halo k -> nvp + k,
+ * 4 uint16 per slot, each patch's rows padded to an even count); maxima_out[4] =
+ * largest (ne, nvp, nh, nc) over the patches.  No counterpart in the reference. */
+int wcfe_debug_patch_staging(int32_t n_vert, int32_t n_tri, const int32_t* tri, int32_t patch_elems_max,
+                             int32_t* np_out, int32_t* xinfo, int32_t xinfo_cap, int32_t* halo, int32_t halo_cap,
+                             uint16_t* loc, int32_t loc_cap, int32_t* maxima_out);
 
 #ifdef __cplusplus
 }

@@ -132,3 +132,32 @@ def test_topology_rejects_bad_meshes():
     with pytest.raises(capi.WcfeError):   # a vertex with no triangle
         capi.debug_topology(np.array([[0, 1, 2]], np.int32), 4)
     assert L is not None
+
+
+@pytest.mark.parametrize("emax", [24, 96, 512])
+def test_patch_staging_description(emax):
+    """Halo lists, patch-local corners and code ranges of the mixed form's staged patches."""
+    x, tri = synth.disk_mesh(1500, seed=6)
+    n = len(x)
+    vt_ptr, vt_idx = synth.vertex_triangle_map(n, tri)
+    t = capi.debug_topology(tri, n, emax=emax)
+    s = capi.debug_patch_staging(tri, n, emax=emax)
+    assert s["np"] == t["np"]
+    mx = np.zeros(4, np.int64)
+    for p in range(t["np"]):
+        v0, nvp, e0, ne = t["patch"][p]
+        h0, nh, c0, nc = s["xinfo"][p]
+        assert e0 % 2 == 0
+        assert c0 == vt_ptr[v0] and nc == vt_ptr[v0 + nvp] - vt_ptr[v0]
+        halo = s["halo"][h0:h0 + nh]
+        assert (np.diff(halo) > 0).all()
+        assert ((halo < v0) | (halo >= v0 + nvp)).all()
+        corners = tri[t["elems"][e0:e0 + ne]]
+        want = np.unique(corners[(corners < v0) | (corners >= v0 + nvp)])
+        assert np.array_equal(halo, want)
+        loc = s["loc"][e0:e0 + ne].astype(np.int64)
+        assert (loc[:, 3] == 0).all()
+        local = np.where(loc[:, :3] < nvp, v0 + loc[:, :3], halo[np.clip(loc[:, :3] - nvp, 0, max(nh - 1, 0))])
+        assert np.array_equal(local, corners)
+        mx = np.maximum(mx, [ne, nvp, nh, nc])
+    assert list(mx) == [s["max_ne"], s["max_nvp"], s["max_nh"], s["max_nc"]]

@@ -39,10 +39,12 @@ def test_mixed_matches_fp64_300_steps(variant, law):
     assert err <= MIXED_TOL, err
 
 
-def test_mixed_moving_state_matches_fp64():
-    """From a moving, pre-strained state (strain ~1e-2, bonds formed)."""
+@pytest.mark.parametrize("variant,law", [("k1", 0), ("k31", 0), ("k31", 2)])
+def test_mixed_moving_state_matches_fp64(variant, law):
+    """From a moving, pre-strained state (strain ~1e-2, bonds formed, some bonds
+    stretched far enough that the Bell off-rate exceeds the FP32 range)."""
     x0, tri = synth.disk_mesh(2000, seed=32)
-    p = default_params("k1")
+    p = _law(default_params(variant), law)
     st = synth.initial_state(x0, perturb=1.0, seed=4)
     out = {}
     for prec in (capi.PREC_FP64, capi.PREC_MIXED):
@@ -160,3 +162,34 @@ def test_integrin_density_mask():
     F = h.eval_forces(st[0], 5e-5)[0]
     assert np.all(F == 0)
     e.close()
+
+
+def test_staged_patch_kernel_equals_plain():
+    """The staged patch kernel (bulk copies into shared memory) computes exactly what
+    the plain kernel computes: bit-identical state after 30 steps, several cells and
+    patch shapes, with integrin masks."""
+    cells = []
+    for i, n in enumerate([250, 1700, 5200]):
+        x0, tri = synth.disk_mesh(n, seed=400 + i)
+        p = _law(default_params(["k1", "k31", "k31"][i]), [0, 0, 2][i])
+        p.stream = i
+        rho = np.where(np.random.default_rng(i).random(len(x0)) < 0.4, p.rho_i_max, 0.0)
+        cells.append((x0, tri, p, rho))
+    for emax in (96, 512):
+        res = []
+        for kind in (0, 1):
+            e = capi.Engine(capi.PREC_MIXED)
+            e.set_shape(128, emax)
+            e.set_patch_kernel(kind)
+            hs = []
+            for x0, tri, p, rho in cells:
+                h = e.add_cell(x0, tri, p, state=synth.initial_state(x0, perturb=1.0, seed=7))
+                h.set_integrins(rho)
+                hs.append(h)
+            e.step(30, 5e-5)
+            res.append([h.get_state() for h in hs])
+            assert all(h.status() == 0 for h in hs)
+            e.close()
+        for a, b in zip(*res):
+            for u, w in zip(a, b):
+                assert np.array_equal(u, w)

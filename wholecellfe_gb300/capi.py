@@ -78,9 +78,12 @@ SIGNATURES = {
     "wcfe_server_iterate": (C.c_int, [C.c_void_p, _i, _i]),
     "wcfe_server_result": (C.c_int, [C.c_void_p, C.c_int64, _d, _d]),
     "wcfe_server_step_times": (C.c_int64, [C.c_void_p, _d, C.c_int64]),
+    "wcfe_engine_set_patch_kernel": (C.c_int, [C.c_void_p, C.c_int32]),
     "wcfe_area_tot_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "wcfe_debug_topology": (C.c_int, [C.c_int32, C.c_int32, _i, _i, _i, _u8, C.c_int32, _i, _i, _i, _i, C.c_int32, _i,
                                       _i, C.c_int32, _i, C.c_int32, C.POINTER(C.c_uint16)]),
+    "wcfe_debug_patch_staging": (C.c_int, [C.c_int32, C.c_int32, _i, C.c_int32, _i, _i, C.c_int32, _i, C.c_int32,
+                                           C.POINTER(C.c_uint16), C.c_int32, _i]),
 }
 
 
@@ -105,8 +108,27 @@ def debug_topology(tri, n_vert, emax=320, vt_ptr=None, vt_idx=None, bnd=None):
     nbv, npv = nb.value, npatch.value
     cptr = cptr[:nbv + 1]
     patch = patch[:4 * npv].reshape(npv, 4)
+    n_el = int(patch[-1, 2] + patch[-1, 3] + (patch[-1, 3] & 1)) if npv else 0
     return dict(nb=nbv, rank=rank, cptr=cptr, cand=cand[:2 * cptr[-1]].reshape(-1, 2), np=npv, patch=patch,
-                elems=elems[:patch[:, 3].sum()], codes=codes)
+                elems=elems[:n_el], codes=codes)
+
+
+def debug_patch_staging(tri, n_vert, emax=320):
+    """Staging description of each patch (halo lists, patch-local corners, code ranges)."""
+    tri = i32(tri)
+    nt = len(tri)
+    npatch = C.c_int32()
+    xinfo = np.zeros(4 * n_vert + 16, np.int32)
+    halo = np.zeros(8 * n_vert + 64, np.int32)
+    loc = np.zeros(4 * (6 * nt + 16), np.uint16)
+    mx = np.zeros(4, np.int32)
+    check(load().wcfe_debug_patch_staging(n_vert, nt, ip(tri), emax, C.byref(npatch), ip(xinfo), len(xinfo), ip(halo),
+                                          len(halo), loc.ctypes.data_as(C.POINTER(C.c_uint16)), len(loc), ip(mx)),
+          "wcfe_debug_patch_staging")
+    npv = npatch.value
+    xinfo = xinfo[:4 * npv].reshape(npv, 4)
+    return dict(np=npv, xinfo=xinfo, halo=halo, loc=loc.reshape(-1, 4),
+                max_ne=int(mx[0]), max_nvp=int(mx[1]), max_nh=int(mx[2]), max_nc=int(mx[3]))
 
 
 class WcfeError(RuntimeError):
@@ -226,6 +248,10 @@ class Engine:
 
     def set_shape(self, threads: int, emax: int):
         check(load().wcfe_engine_set_shape(self.h, threads, emax), "wcfe_engine_set_shape")
+
+    def set_patch_kernel(self, kind: int):
+        """Mixed engines: 0 staged patch kernel where it fits (default), 1 plain."""
+        check(load().wcfe_engine_set_patch_kernel(self.h, kind), "wcfe_engine_set_patch_kernel")
 
     def shape(self):
         a, b = C.c_int32(), C.c_int32()

@@ -44,6 +44,8 @@ struct ParamF {
     float drag, damp, rho;
     int32_t law;                               // PF_*: linear with zero rest length, MD table, linear, polynomial
     int32_t norm2d;
+    // low parts (x - RN(x)) of the constants the Bell force and rate use in float-float
+    float k_lin_lo, rest_len_lo, poly_k0_lo, poly_c3_lo, iFa_lo, iFb_lo;
 };
 
 struct CellDev {
@@ -59,12 +61,15 @@ struct CellDev {
     double* cA;
     double* cC;
     double4* fau;
-    const double* rho_w;        // optional per-vertex integrin density (nullptr: rho_i_max)
+    const double* rho_w;        // optional per-vertex integrin density (nullptr: rho_i_max); floats in a mixed engine
     const int4* tri;
     const int32_t* vt_ptr;
     const uint16_t* vc_code;    // (slot << 2) | corner, slot local to the owner's patch
     const int4* patch;
     const int32_t* patch_elems;
+    const int4* patch_x;        // per patch (h0, nh, c0, nc): halo list and one-ring code range (mixed form staging)
+    const int32_t* patch_halo;  // halo vertices of each patch, ascending
+    const uint16_t* patch_loc;  // [4 per element slot] corners as patch-local vertex indices
     const int32_t* bnd_rank;
     const int32_t* bnd_cptr;
     const int2* bnd_cand;
@@ -105,6 +110,13 @@ inline ParamF make_paramf(const wcfe_params& p) {
           : p.force_law == WCFE_LAW_LINEAR ? (p.rest_len == 0.0 ? PF_LINEAR0 : PF_LINEAR)
           : PF_POLY;
     f.norm2d = p.linear_norm2d ? 1 : 0;
+    auto lo = [](double x) { return (float)(x - (double)(float)x); };
+    f.k_lin_lo = lo(p.k_lin);
+    f.rest_len_lo = lo(p.rest_len);
+    f.poly_k0_lo = lo(p.poly_k0);
+    f.poly_c3_lo = lo(1.0 / (3.0 * p.poly_x0 * p.poly_x0));
+    f.iFa_lo = lo(1.0 / p.Fa);
+    f.iFb_lo = lo(1.0 / p.Fb);
     return f;
 }
 

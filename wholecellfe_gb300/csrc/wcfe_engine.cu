@@ -25,6 +25,9 @@ void launch_vertex_phase(const CellDev* cells, const WorkItem* work, int nwork, 
                          int threads, cudaStream_t st, const double* stage_in = nullptr, double* stage_out = nullptr);
 void launch_predict(const CellDev* cells, int cell, double dt, double* xout, double* vhout, int nv, cudaStream_t st);
 cudaError_t configure_kernels(size_t max_smem);
+bool launch_patch_staged(const CellDev* cells, const WorkItem* work, int nwork, int cap_ne, int cap_nvp, int cap_nh,
+                         int cap_nc, double dt, double dt_real, double ap_thresh, double t_override, int vh_from_buf,
+                         int num_sms, cudaStream_t st);
 size_t patch_smem_bytes(int prec, int mode, int emax);
 int patch_occupancy(int prec, int threads, size_t smem);
 int vertex_occupancy(int threads);
@@ -71,7 +74,8 @@ struct Cell {
     size_t patch_bytes = 0;
     void* sub_block = nullptr;
     size_t sub_bytes = 0;
-    double* rho_dev = nullptr;
+    double* rho_dev = nullptr;      // integrin density (floats for a mixed engine)
+    size_t rho_size = 0;            // its allocation
     CellDev dev{};
     int32_t sub_nv = 0, sub_nt = 0;
     std::vector<int32_t> sub_tri;
@@ -125,6 +129,8 @@ struct wcfe_engine {
     int patch_threads = 128;
     int patch_emax = 320;
     int vblock = 256;             // vertices (threads) per vertex-phase block
+    int patch_kernel = 0;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
+    int cap_ne = 0, cap_nvp = 0, cap_nh = 0, cap_nc = 0;   // largest patch over the cells (staging plan)
     bool tuned = false;
     // graphs
     bool use_graphs = false;
@@ -181,18 +187,26 @@ size_t state_layout(int32_t nv, int32_t nt, int32_t nb, int32_t ncand, int32_t n
     put(sizeof(int32_t) * std::max(2 * nb, 1));  // 22 bnd_out (at most a few edges per boundary vertex)
     put(sizeof(double) * 4);     // 23 area4
     put(sizeof(int32_t) * std::max(nb, 1));  // 24 bnd_vert: boundary vertices in rank order
+    put(64);                     // 25 slack: 16-B-rounded bulk copies of the last arrays stay in the block
     return o;
 }
 
-size_t patch_layout(int32_t np, size_t nelems, size_t ncodes, size_t* off /* 3 */) {
+// patch arrays; every array ends with 64 B of slack so that 16-B-rounded bulk copies stay in the block
+size_t patch_layout(int32_t np, size_t nelems, size_t ncodes, size_t nhalo, size_t* off /* 6 */) {
     size_t o = 0;
     int i = 0;
-    auto put = [&](size_t bytes) { off[i++] = o; o = align_up(o + bytes); };
-    put(sizeof(int4) * np);
-    put(sizeof(int32_t) * std::max<size_t>(nelems, 1));
-    put(sizeof(uint16_t) * std::max<size_t>(ncodes, 1));
+    auto put = [&](size_t bytes) { off[i++] = o; o = align_up(o + bytes + 64); };
+    put(sizeof(int4) * np);                               // 0 patch (v0, nvp, e0, ne)
+    put(sizeof(int32_t) * std::max<size_t>(nelems, 1));   // 1 element ids
+    put(sizeof(uint16_t) * std::max<size_t>(ncodes, 1));  // 2 one-ring slot codes
+    put(sizeof(int4) * np);                               // 3 staging info (h0, nh, c0, nc)
+    put(sizeof(int32_t) * std::max<size_t>(nhalo, 1));    // 4 halo vertices
+    put(sizeof(uint16_t) * 4 * std::max<size_t>(nelems, 1));  // 5 element corners, patch-local
     return o;
 }
+
+// per-vertex integrin density (double for FP64 engines, float for mixed ones) + slack
+size_t rho_bytes(int32_t nv) { return sizeof(double) * (size_t)nv + 64; }
 
 int32_t nk1_of(int32_t nv, int32_t nt, int32_t vb) {
     return std::max((nv + vb - 1) / vb, (nt + 2 * vb - 1) / (2 * vb));
@@ -318,8 +332,8 @@ int upload_cell_patches(wcfe_engine* e, Cell* c) {
     std::string err = build_patches(c->patches, c->topo, e->patch_emax);
     if (!err.empty()) return fail(err, WCFE_ERR_TOPOLOGY);
     const Patches& P = c->patches;
-    size_t off[3];
-    size_t bytes = patch_layout(P.np, P.elems.size(), P.vc_code.size(), off);
+    size_t off[6];
+    size_t bytes = patch_layout(P.np, P.elems.size(), P.vc_code.size(), P.halo.size(), off);
     if (c->patch_block && c->patch_bytes != bytes) dev_free(e, c->patch_block, c->patch_bytes);
     if (!c->patch_block) {
         int r = dev_alloc(e, &c->patch_block, bytes);
@@ -327,13 +341,21 @@ int upload_cell_patches(wcfe_engine* e, Cell* c) {
         c->patch_bytes = bytes;
     }
     char* b = (char*)c->patch_block;
+    CK(cudaMemsetAsync(b, 0, bytes, e->stream));
     c->dev.np = P.np;
     c->dev.patch = (const int4*)(b + off[0]);
     c->dev.patch_elems = (const int32_t*)(b + off[1]);
     c->dev.vc_code = (const uint16_t*)(b + off[2]);
+    c->dev.patch_x = (const int4*)(b + off[3]);
+    c->dev.patch_halo = (const int32_t*)(b + off[4]);
+    c->dev.patch_loc = (const uint16_t*)(b + off[5]);
     CK(cudaMemcpyAsync((void*)c->dev.patch, P.patch.data(), sizeof(int32_t) * P.patch.size(), cudaMemcpyHostToDevice, e->stream));
     CK(cudaMemcpyAsync((void*)c->dev.patch_elems, P.elems.data(), sizeof(int32_t) * P.elems.size(), cudaMemcpyHostToDevice, e->stream));
     CK(cudaMemcpyAsync((void*)c->dev.vc_code, P.vc_code.data(), sizeof(uint16_t) * P.vc_code.size(), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync((void*)c->dev.patch_x, P.xinfo.data(), sizeof(int32_t) * P.xinfo.size(), cudaMemcpyHostToDevice, e->stream));
+    if (!P.halo.empty())
+        CK(cudaMemcpyAsync((void*)c->dev.patch_halo, P.halo.data(), sizeof(int32_t) * P.halo.size(), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync((void*)c->dev.patch_loc, P.loc.data(), sizeof(uint16_t) * P.loc.size(), cudaMemcpyHostToDevice, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return WCFE_OK;
 }
@@ -390,7 +412,7 @@ void free_cell(wcfe_engine* e, Cell* c) {
     dev_free(e, c->patch_block, c->patch_bytes);
     dev_free(e, c->sub_block, c->sub_bytes);
     if (c->rho_dev) {
-        size_t b = sizeof(double) * c->topo.nv;
+        size_t b = c->rho_size;
         void* p = c->rho_dev;
         dev_free(e, p, b);
         c->rho_dev = nullptr;
@@ -427,6 +449,14 @@ int sync_tables(wcfe_engine* e, double dt = -1.0) {
     e->total_nv = 0;
     e->k1.clear();
     e->k2.clear();
+    e->cap_ne = e->cap_nvp = e->cap_nh = e->cap_nc = 0;
+    for (auto& kv : e->cells) {
+        const Patches& P = kv.second->patches;
+        e->cap_ne = std::max(e->cap_ne, P.max_ne);
+        e->cap_nvp = std::max(e->cap_nvp, P.max_nvp);
+        e->cap_nh = std::max(e->cap_nh, P.max_nh);
+        e->cap_nc = std::max(e->cap_nc, P.max_nc);
+    }
     for (auto& kv : e->cells) {
         Cell* c = kv.second.get();
         c->dev.prm = c->prm;
@@ -481,19 +511,28 @@ void invalidate_graph(wcfe_engine* e) {
     e->graph.exec = nullptr;
 }
 
+// the patch phase of a step (STEP mode): the staged mixed kernel where it applies
+void patch_step(wcfe_engine* e, const WorkItem* k2, int n2, double dt, double dt_real, double apt, double t_override,
+                int vh_from_buf) {
+    if (e->prec == WCFE_PREC_MIXED && e->patch_kernel == 0 &&
+        launch_patch_staged(e->d_table, k2, n2, e->cap_ne, e->cap_nvp, e->cap_nh, e->cap_nc, dt, dt_real, apt,
+                            t_override, vh_from_buf, e->num_sms, e->stream))
+        return;
+    size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
+    launch_patch(e->prec, PP_STEP, e->d_table, k2, n2, e->patch_emax, dt, dt_real, apt, t_override, vh_from_buf,
+                 nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, e->patch_threads,
+                 grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem)), e->stream);
+}
+
 // one explicit step of the cells listed in (k1, k2) device lists
 int enqueue_step(wcfe_engine* e, const WorkItem* k1, int n1, const WorkItem* k2, int n2, double dt) {
     const double apt = std::numeric_limits<double>::quiet_NaN();  // per-cell thresholds from the table
     int g1 = grid_for(e, n1, vertex_occupancy(e->vblock));
-    size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
-    int g2 = grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem));
     cudaEvent_t* tv = (e->timing && e->tev.size() >= 3) ? &e->tev[3 * (size_t)e->timed_steps] : nullptr;
     if (tv) cudaEventRecord(tv[0], e->stream);
     vphase(e, e->d_table, k1, n1, dt, VP_PREDICT | VP_UPDATE_FA | rec_flag(e), g1, e->stream);
     if (tv) cudaEventRecord(tv[1], e->stream);
-    launch_patch(e->prec, PP_STEP, e->d_table, k2, n2, e->patch_emax, dt, dt, apt,
-                 std::numeric_limits<double>::quiet_NaN(), 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-                 e->patch_threads, g2, e->stream);
+    patch_step(e, k2, n2, dt, dt, apt, std::numeric_limits<double>::quiet_NaN(), 0);
     if (tv) {
         cudaEventRecord(tv[2], e->stream);
         e->timed_steps++;
@@ -535,56 +574,58 @@ int get3(wcfe_engine* e, double* h, const double4* d, int n) {
 }
 
 // A mixed engine keeps its state as float-float pairs (hi = RN(x), lo = RN(x - hi))
-// in the same slots (wcfe_ff.cuh): pos, vel, fau as {hi.xyz0, lo.xyz0}; acc as the
-// FP32 acceleration; ea as {hi xx yy zz xy, lo xx yy zz xy, hi xz yz, lo xz yz};
-// cA, cC as {hi, lo}.  These convert on the host.
+// in the same slots, as structures of arrays over the cell's n vertices
+// (wcfe_mixed.cu): pos, vel, fau, vhl as hi float4[n] then lo float4[n]; acc as the
+// FP32 acceleration float4[n]; ea as hi float4[n] (xx yy zz xy), lo float4[n],
+// then float4[n] (xz hi, yz hi, xz lo, yz lo); cA, cC as hi float[n] then lo float[n].
+// These convert on the host.
 inline void split_ff(double x, float* hi, float* lo) {
     const float h = (float)x;
     *hi = h;
     *lo = (float)(x - (double)h);
 }
 int put_ff(wcfe_engine* e, void* d, const double* h, int n, int kind) {
+    const size_t N = (size_t)n;
     std::vector<float> b;
-    if (kind == 0 || kind == 1) {          // [n][3] vectors -> ff4 (kind 1: acceleration, hi only)
-        b.assign((size_t)8 * n, 0.0f);
-        for (int v = 0; v < n; ++v)
+    if (kind == 0 || kind == 1) {          // [n][3] vectors
+        b.assign((kind == 1 ? 4 : 8) * N, 0.0f);
+        for (size_t v = 0; v < N; ++v)
             for (int k = 0; k < 3; ++k) {
-                if (kind == 1) b[8 * (size_t)v + k] = (float)h[3 * (size_t)v + k];
-                else split_ff(h[3 * (size_t)v + k], &b[8 * (size_t)v + k], &b[8 * (size_t)v + 4 + k]);
+                if (kind == 1) b[4 * v + k] = (float)h[3 * v + k];
+                else split_ff(h[3 * v + k], &b[4 * v + k], &b[4 * (N + v) + k]);
             }
-    } else if (kind == 2) {                // [n][6] strain (xx yy zz xy xz yz) -> ffea
-        b.assign((size_t)12 * n, 0.0f);
-        for (int v = 0; v < n; ++v) {
-            const double* q = h + 6 * (size_t)v;
-            float* o = &b[12 * (size_t)v];
-            for (int k = 0; k < 4; ++k) split_ff(q[k], &o[k], &o[4 + k]);
-            split_ff(q[4], &o[8], &o[10]);
-            split_ff(q[5], &o[9], &o[11]);
+    } else if (kind == 2) {                // [n][6] strain (xx yy zz xy xz yz)
+        b.assign(12 * N, 0.0f);
+        for (size_t v = 0; v < N; ++v) {
+            const double* q = h + 6 * v;
+            for (int k = 0; k < 4; ++k) split_ff(q[k], &b[4 * v + k], &b[4 * (N + v) + k]);
+            split_ff(q[4], &b[4 * (2 * N + v) + 0], &b[4 * (2 * N + v) + 2]);
+            split_ff(q[5], &b[4 * (2 * N + v) + 1], &b[4 * (2 * N + v) + 3]);
         }
-    } else {                               // [n] scalars -> ff
-        b.assign((size_t)2 * n, 0.0f);
-        for (int v = 0; v < n; ++v) split_ff(h[v], &b[2 * (size_t)v], &b[2 * (size_t)v + 1]);
+    } else {                               // [n] scalars
+        b.assign(2 * N, 0.0f);
+        for (size_t v = 0; v < N; ++v) split_ff(h[v], &b[v], &b[N + v]);
     }
     CK(cudaMemcpyAsync(d, b.data(), sizeof(float) * b.size(), cudaMemcpyHostToDevice, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return WCFE_OK;
 }
 int get_ff(wcfe_engine* e, double* h, const void* d, int n, int kind) {
-    const size_t per = kind <= 1 ? 8 : kind == 2 ? 12 : 2;
-    std::vector<float> b(per * (size_t)n);
+    const size_t N = (size_t)n;
+    const size_t per = kind == 0 ? 8 : kind == 1 ? 4 : kind == 2 ? 12 : 2;
+    std::vector<float> b(per * N);
     CK(cudaMemcpyAsync(b.data(), d, sizeof(float) * b.size(), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     auto ffd = [](float hi, float lo) { return (double)hi + (double)lo; };
-    for (int v = 0; v < n; ++v) {
-        const float* o = &b[per * (size_t)v];
-        if (kind == 0) for (int k = 0; k < 3; ++k) h[3 * (size_t)v + k] = ffd(o[k], o[4 + k]);
-        else if (kind == 1) for (int k = 0; k < 3; ++k) h[3 * (size_t)v + k] = (double)o[k];
+    for (size_t v = 0; v < N; ++v) {
+        if (kind == 0) for (int k = 0; k < 3; ++k) h[3 * v + k] = ffd(b[4 * v + k], b[4 * (N + v) + k]);
+        else if (kind == 1) for (int k = 0; k < 3; ++k) h[3 * v + k] = (double)b[4 * v + k];
         else if (kind == 2) {
-            double* q = h + 6 * (size_t)v;
-            for (int k = 0; k < 4; ++k) q[k] = ffd(o[k], o[4 + k]);
-            q[4] = ffd(o[8], o[10]);
-            q[5] = ffd(o[9], o[11]);
-        } else h[v] = ffd(o[0], o[1]);
+            double* q = h + 6 * v;
+            for (int k = 0; k < 4; ++k) q[k] = ffd(b[4 * v + k], b[4 * (N + v) + k]);
+            q[4] = ffd(b[4 * (2 * N + v) + 0], b[4 * (2 * N + v) + 2]);
+            q[5] = ffd(b[4 * (2 * N + v) + 1], b[4 * (2 * N + v) + 3]);
+        } else h[v] = ffd(b[v], b[N + v]);
     }
     return WCFE_OK;
 }
@@ -678,9 +719,9 @@ uint64_t wcfe_cell_bytes(int32_t nv, int32_t nt) {
     size_t off[32];
     int32_t nb = (int32_t)(4 * std::sqrt((double)std::max(nv, 1)) + 16);
     size_t s = state_layout(nv, nt, nb, 3 * nb, nk1_of(nv, nt, 64), true, off);
-    size_t p3[3];
-    size_t p = patch_layout(nv / 64 + 2, (size_t)(1.6 * nt) + 64, 3 * (size_t)nt, p3);
-    return (uint64_t)(s + p + sizeof(double) * nv);
+    size_t p6[6];
+    size_t p = patch_layout(nv / 64 + 2, (size_t)(1.6 * nt) + 64, 3 * (size_t)nt, (size_t)(0.6 * nv) + 64, p6);
+    return (uint64_t)(s + p + rho_bytes(nv));
 }
 int wcfe_engine_sync(wcfe_engine* e) {
     if (!e) return WCFE_ERR_ARG;
@@ -742,7 +783,7 @@ int wcfe_cell_set_topology(wcfe_engine* e, int32_t id, int32_t nv, int32_t nt, c
     if (!r) r = upload_cell_patches(e, c);
     if (c->rho_dev) {
         void* p = c->rho_dev;
-        size_t b = sizeof(double) * nv;
+        size_t b = c->rho_size;
         dev_free(e, p, b);
         c->rho_dev = nullptr;
     }
@@ -1191,6 +1232,13 @@ int wcfe_engine_set_shape(wcfe_engine* e, int32_t threads, int32_t emax) {
     return WCFE_OK;
 }
 
+int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind) {
+    if (!e || kind < 0 || kind > 1) return fail("bad argument", WCFE_ERR_ARG);
+    e->patch_kernel = kind;
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
 int wcfe_engine_get_shape(const wcfe_engine* e, int32_t* threads, int32_t* emax) {
     if (!e) return WCFE_ERR_ARG;
     if (threads) *threads = e->patch_threads;
@@ -1244,6 +1292,30 @@ int wcfe_debug_topology(int32_t nv, int32_t nt, const int32_t* tri, const int32_
     return WCFE_OK;
 }
 
+int wcfe_debug_patch_staging(int32_t nv, int32_t nt, const int32_t* tri, int32_t emax, int32_t* np_out, int32_t* xinfo,
+                             int32_t xinfo_cap, int32_t* halo, int32_t halo_cap, uint16_t* loc, int32_t loc_cap,
+                             int32_t* maxima_out) {
+    Topology T;
+    std::string err = build_topology(T, nv, nt, tri, nullptr, nullptr, nullptr);
+    if (!err.empty()) return fail(err, WCFE_ERR_TOPOLOGY);
+    Patches P;
+    err = build_patches(P, T, emax);
+    if (!err.empty()) return fail(err, WCFE_ERR_TOPOLOGY);
+    if ((int64_t)P.xinfo.size() > xinfo_cap || (int64_t)P.halo.size() > halo_cap || (int64_t)P.loc.size() > loc_cap)
+        return fail("output capacity too small", WCFE_ERR_LIMIT);
+    if (np_out) *np_out = P.np;
+    if (xinfo) std::memcpy(xinfo, P.xinfo.data(), sizeof(int32_t) * P.xinfo.size());
+    if (halo && !P.halo.empty()) std::memcpy(halo, P.halo.data(), sizeof(int32_t) * P.halo.size());
+    if (loc) std::memcpy(loc, P.loc.data(), sizeof(uint16_t) * P.loc.size());
+    if (maxima_out) {
+        maxima_out[0] = P.max_ne;
+        maxima_out[1] = P.max_nvp;
+        maxima_out[2] = P.max_nh;
+        maxima_out[3] = P.max_nc;
+    }
+    return WCFE_OK;
+}
+
 int64_t wcfe_engine_total_vertices(wcfe_engine* e) {
     if (!e) return -1;
     if (sync_tables(e)) return -1;
@@ -1278,11 +1350,8 @@ int wcfe_engine_update(wcfe_engine* e, double dt, double dt_real, const double* 
     const int n1 = (int)e->k1.size(), n2 = (int)e->k2.size();
     vphase(e, e->d_table, e->d_k1, n1, dt_real, VP_IMPORT | VP_UPDATE_FA | rec_flag(e), grid_for(e, n1, vertex_occupancy(e->vblock)),
            e->stream, e->d_xchg, nullptr);
-    size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
-    launch_patch(e->prec, PP_STEP, e->d_table, e->d_k2, n2, e->patch_emax, dt, dt_real,
-                 std::numeric_limits<double>::quiet_NaN(), std::numeric_limits<double>::quiet_NaN(), 1, nullptr, nullptr,
-                 nullptr, nullptr, nullptr, nullptr, e->patch_threads,
-                 grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem)), e->stream);
+    patch_step(e, e->d_k2, n2, dt, dt_real, std::numeric_limits<double>::quiet_NaN(),
+               std::numeric_limits<double>::quiet_NaN(), 1);
     e->launches += 2;
     CK(cudaGetLastError());
     return WCFE_OK;
@@ -1292,22 +1361,29 @@ int wcfe_cell_set_integrins(wcfe_engine* e, int32_t id, const double* rho) {
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     CK(cudaSetDevice(e->device));
-    const size_t bytes = sizeof(double) * c->topo.nv;
+    const int n = c->topo.nv;
     if (!rho) {
         if (c->rho_dev) {
             void* p = c->rho_dev;
-            size_t b = bytes;
+            size_t b = c->rho_size;
             dev_free(e, p, b);
             c->rho_dev = nullptr;
         }
     } else {
         if (!c->rho_dev) {
             void* p = nullptr;
-            int r = dev_alloc(e, &p, bytes);
+            int r = dev_alloc(e, &p, rho_bytes(n));
             if (r) return r;
             c->rho_dev = (double*)p;
+            c->rho_size = rho_bytes(n);
         }
-        CK(cudaMemcpyAsync(c->rho_dev, rho, bytes, cudaMemcpyHostToDevice, e->stream));
+        if (e->prec == WCFE_PREC_MIXED) {   // FP32 densities
+            std::vector<float> f(n);
+            for (int v = 0; v < n; ++v) f[v] = (float)rho[v];
+            CK(cudaMemcpyAsync(c->rho_dev, f.data(), sizeof(float) * n, cudaMemcpyHostToDevice, e->stream));
+        } else {
+            CK(cudaMemcpyAsync(c->rho_dev, rho, sizeof(double) * n, cudaMemcpyHostToDevice, e->stream));
+        }
         CK(cudaStreamSynchronize(e->stream));
     }
     e->version++;

@@ -76,6 +76,15 @@ WCFE_HD ff ff_mul(ff a, ff b) {
 WCFE_HD ff ff_fma_f(ff a, ff b, float c) { return ff_add(a, ff_mul_f(b, c)); }
 // a + b * c, both products' factors float-float
 WCFE_HD ff ff_fma(ff a, ff b, ff c) { return ff_add(a, ff_mul(b, c)); }
+// square root: s = sqrt(hi) corrected by one Newton step on the exact residual
+WCFE_HD ff ff_sqrt(ff a) {
+    if (!(a.hi > 0.0f)) return {0.0f, 0.0f};
+    const float s = sqrtf(a.hi);
+    const float r = FF_ADD(FF_FMA(-s, s, a.hi), a.lo);   // a - s^2
+    return fast_two_sum(s, r / (2.0f * s));
+}
+WCFE_HD ff ff_abs(ff a) { return a.hi < 0.0f ? ff{-a.hi, -a.lo} : a; }
+WCFE_HD bool ff_lt(ff a, ff b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 // the float nearest to the value (hi, for a normalised pair)
 WCFE_HD float ff_f(ff a) { return a.hi; }
 

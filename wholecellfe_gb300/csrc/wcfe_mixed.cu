@@ -31,12 +31,14 @@
 // per-step force and acceleration are FP32.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 
 #include "wcfe_common.cuh"
 #include "wcfe_cvt.h"
 #include "wcfe_ff.cuh"
+#include "wcfe_tma.cuh"
 
 namespace wcfe {
 
@@ -50,34 +52,40 @@ struct MixedArgs {
 };
 
 // The mixed engine's state arrays hold float-float values (wcfe_ff.cuh) in the
-// slots the FP64 engine uses for doubles: pos, vel, fau and vhl as ff4 (32 B),
-// ea as ffea (48 B), cA and cC as ff (8 B); acc holds the FP32 acceleration as a
-// float4 in the first half of its 32-B slot.
-__device__ __forceinline__ ff4 ldg_ff4(const double4* base, int v) {
-    const float4* q = reinterpret_cast<const float4*>(base + v);
-    const float4 h = __ldg(q), l = __ldg(q + 1);
+// slots the FP64 engine uses for doubles, as structures of arrays over the cell's
+// n vertices: pos, vel, fau and vhl as hi float4[n] then lo float4[n] (32n B);
+// ea as hi float4[n] (xx, yy, zz, xy), lo float4[n], then float4[n] (xz hi,
+// yz hi, xz lo, yz lo) (48n B); cA and cC as hi float[n] then lo float[n] (8n B);
+// acc holds the FP32 acceleration as float4[n]; the integrin density is float[n].
+__device__ __forceinline__ ff4 ldg_ff4(const double4* base, int n, int v) {
+    const float4* q = reinterpret_cast<const float4*>(base);
+    const float4 h = __ldg(q + v), l = __ldg(q + n + v);
     return {h.x, h.y, h.z, h.w, l.x, l.y, l.z, l.w};
 }
-__device__ __forceinline__ ff4 ld_ff4(const double4* base, int v) {   // coherent: written in this launch
-    const float4* q = reinterpret_cast<const float4*>(base + v);
-    const float4 h = __ldcg(q), l = __ldcg(q + 1);
+__device__ __forceinline__ ff4 ld_ff4(const double4* base, int n, int v) {   // coherent: written in this launch
+    const float4* q = reinterpret_cast<const float4*>(base);
+    const float4 h = __ldcg(q + v), l = __ldcg(q + n + v);
     return {h.x, h.y, h.z, h.w, l.x, l.y, l.z, l.w};
 }
-__device__ __forceinline__ void st_ff4(double4* base, int v, const ff4& a) {
-    float4* q = reinterpret_cast<float4*>(base + v);
-    q[0] = make_float4(a.hx, a.hy, a.hz, a.hw);
-    q[1] = make_float4(a.lx, a.ly, a.lz, a.lw);
+__device__ __forceinline__ void st_ff4(double4* base, int n, int v, const ff4& a) {
+    float4* q = reinterpret_cast<float4*>(base);
+    q[v] = make_float4(a.hx, a.hy, a.hz, a.hw);
+    q[n + v] = make_float4(a.lx, a.ly, a.lz, a.lw);
 }
-__device__ __forceinline__ ff ld_ff(const double* base, int v) {
-    const float2 t = __ldg(reinterpret_cast<const float2*>(base) + v);
-    return {t.x, t.y};
+__device__ __forceinline__ ff ld_ff(const double* base, int n, int v) {
+    const float* q = reinterpret_cast<const float*>(base);
+    return {__ldg(q + v), __ldg(q + n + v)};
 }
-__device__ __forceinline__ void st_ff(double* base, int v, ff a) {
-    reinterpret_cast<float2*>(base)[v] = make_float2(a.hi, a.lo);
+__device__ __forceinline__ void st_ff(double* base, int n, int v, ff a) {
+    float* q = reinterpret_cast<float*>(base);
+    q[v] = a.hi;
+    q[n + v] = a.lo;
 }
 __device__ __forceinline__ float4 ld_acc(const double4* base, int v) {
-    return __ldg(reinterpret_cast<const float4*>(base + v));
+    return __ldg(reinterpret_cast<const float4*>(base) + v);
 }
+__device__ __forceinline__ void st_acc(double4* base, int v, float4 a) { reinterpret_cast<float4*>(base)[v] = a; }
+__device__ __forceinline__ float ld_rho(const double* base, int v) { return __ldg(reinterpret_cast<const float*>(base) + v); }
 // positions as doubles (boundary terms, area, exchange)
 __device__ __forceinline__ void pos_d(const ff4& a, double x[3]) {
     x[0] = ff_to_d(ffx(a)); x[1] = ff_to_d(ffy(a)); x[2] = ff_to_d(ffz(a));
@@ -128,6 +136,53 @@ __device__ __forceinline__ void spring_force32(const ParamF& p, float ux, float 
     fs[0] = mag * ux * iD; fs[1] = mag * uy * iD; fs[2] = mag * uz * iD;
     if (p.law == PF_LINEAR && p.norm2d) *bell = fabsf(k * (sqrtf(ux * ux + uy * uy) - L0));
     else *bell = fabsf(mag) * (D != 0.0f ? 1.0f : 0.0f);
+}
+
+// kfa * f - R, with kfa * f exact (FMA TwoProduct) and R float-float: one final rounding
+__device__ __forceinline__ float net_force(float kfa, float f, ff R) {
+    const float p = kfa * f;
+    const ff prod = {p, __fmaf_rn(kfa, f, -p)};
+    return ff_sub(prod, R).hi;
+}
+
+// MD force-extension fit (UL:1203-1214) as float-float constants (hi, lo)
+#define FFH(x) ((float)(x))
+#define FFL(x) ((float)((x) - (double)(float)(x)))
+#define FF6(m, a, b, c, d, e, f) {m(a), m(b), m(c), m(d), m(e), m(f)}
+#define MD_PX 0., 2.51250583e-03, 4.40265201e-03, 5.91408228e-03, 11.76817302e-03, 17.001e-03
+#define MD_PY -7.15514497, 71.80501308, 356.62420075, 356.96656556, 126.21811585, 528.40481124
+#define MD_K 31426.8556, 99485.86235, 67080.67086, -7908.39043, 21978.66923, 76858.39733
+#define FF6H(...) FF6(FFH, __VA_ARGS__)
+#define FF6L(...) FF6(FFL, __VA_ARGS__)
+static __constant__ float c_md_pxh[6] = FF6H(MD_PX), c_md_pxl[6] = FF6L(MD_PX);
+static __constant__ float c_md_pyh[6] = FF6H(MD_PY), c_md_pyl[6] = FF6L(MD_PY);
+static __constant__ float c_md_kh[6] = FF6H(MD_K), c_md_kl[6] = FF6L(MD_K);
+__device__ __forceinline__ ff md_px(int j) { return {c_md_pxh[j], c_md_pxl[j]}; }
+__device__ __forceinline__ ff md_py(int j) { return {c_md_pyh[j], c_md_pyl[j]}; }
+__device__ __forceinline__ ff md_k(int j) { return {c_md_kh[j], c_md_kl[j]}; }
+
+// Bell force magnitude of updateFA (UL:2137; k1 UL:2077) in float-float.  The off-rate
+// k_a exp(F / F_a) turns a relative error e of F into (F / F_a) e, so F is carried
+// to about 48 bits.
+__device__ __forceinline__ ff bell_ff(const ParamF& p, ff ux, ff uy, ff uz) {
+    const ff k = {p.k_lin, p.k_lin_lo}, L0 = {p.rest_len, p.rest_len_lo};
+    const ff d2xy = ff_add(ff_mul(ux, ux), ff_mul(uy, uy));
+    const ff d2 = ff_add(d2xy, ff_mul(uz, uz));
+    if (p.law == PF_LINEAR0) return ff_mul(k, ff_sqrt(p.norm2d ? d2xy : d2));
+    if (p.law == PF_LINEAR) return ff_abs(ff_mul(k, ff_sub(ff_sqrt(p.norm2d ? d2xy : d2), L0)));
+    const ff D = ff_sqrt(d2);
+    if (p.law == PF_MD) {
+        int j = -1;
+        if (!ff_lt(D, md_px(5))) j = 5;
+        else
+            for (int q = 0; q < 5; ++q)
+                if (ff_lt(D, md_px(q + 1)) && !ff_lt(D, md_px(q))) j = q;
+        if (j < 0 || D.hi == 0.0f) return {0.0f, 0.0f};
+        return ff_abs(ff_add(md_py(j), ff_mul(md_k(j), ff_sub(D, md_px(j)))));
+    }
+    const ff e = ff_sub(D, L0);
+    const ff c3 = {p.poly_c3, p.poly_c3_lo}, k0 = {p.poly_k0, p.poly_k0_lo};
+    return ff_abs(ff_mul(k0, ff_add(e, ff_mul(ff_mul(ff_mul(e, e), e), c3))));
 }
 
 struct ElemParams {   // per-cell constants of the element, hoisted out of the element loop
@@ -251,8 +306,8 @@ __device__ __forceinline__ bool boundary_frame_ff(const CellDev& c, const double
     for (int k = c.bnd_cptr[rank]; k < c.bnd_cptr[rank + 1]; ++k) {
         const int2 cd = c.bnd_cand[k];
         double pb[3], pi[3];
-        pos_d(ldg_ff4(xp, cd.x), pb);
-        pos_d(ldg_ff4(xp, cd.y), pi);
+        pos_d(ldg_ff4(xp, c.nv, cd.x), pb);
+        pos_d(ldg_ff4(xp, c.nv, cd.y), pi);
         const double d1x = xs(xi[0], pb[0]), d1y = xs(xi[1], pb[1]);
         const double d2x = xs(pi[0], xi[0]), d2y = xs(pi[1], xi[1]);
         const double ncz = xs(xm(d1x, d2y), xm(d1y, d2x));
@@ -260,8 +315,8 @@ __device__ __forceinline__ bool boundary_frame_ff(const CellDev& c, const double
         else j2 = cd.x;
     }
     if (j1 < 0 || j2 < 0) return false;
-    pos_d(ldg_ff4(xp, j1), x1);
-    pos_d(ldg_ff4(xp, j2), x2);
+    pos_d(ldg_ff4(xp, c.nv, j1), x1);
+    pos_d(ldg_ff4(xp, c.nv, j2), x2);
     return true;
 }
 
@@ -277,7 +332,7 @@ __device__ __forceinline__ void boundary_force(const CellDev& c, const MixedArgs
     const double s_iso = p.kappa * (t < p.tact_t1 ? t * p.tact_rate : p.tact_max);
     const double area_tot = c.area4[0];
     double xi[3];
-    pos_d(ldg_ff4(xp, v), xi);
+    pos_d(ldg_ff4(xp, c.nv, v), xi);
     // isotropic active stress on the open one-ring: (1/2) s_iso thick e3 x sum (X_k - X_j)
     ff sx = {0.0f, 0.0f}, sy = {0.0f, 0.0f};
     for (int k = c.vt_ptr[v]; k < c.vt_ptr[v + 1]; ++k) {
@@ -286,7 +341,7 @@ __device__ __forceinline__ void boundary_force(const CellDev& c, const MixedArgs
         const int e = c.patch_elems[pt.z + (code >> 2)];
         const int4 t4 = c.tri[e];
         const int ids[3] = {t4.x, t4.y, t4.z};
-        const ff4 Xj = ldg_ff4(X, ids[(cn + 1) % 3]), Xk = ldg_ff4(X, ids[(cn + 2) % 3]);
+        const ff4 Xj = ldg_ff4(X, c.nv, ids[(cn + 1) % 3]), Xk = ldg_ff4(X, c.nv, ids[(cn + 2) % 3]);
         sx = ff_add(sx, ff_sub(ffx(Xk), ffx(Xj)));
         sy = ff_add(sy, ff_sub(ffy(Xk), ffy(Xj)));
     }
@@ -324,17 +379,17 @@ __device__ __forceinline__ void boundary_force(const CellDev& c, const MixedArgs
 }
 
 // Explicit update of vertex v (UL:592-628): the acceleration in FP32 from the FP32
-// force; the velocity and the strain accumulate in float-float.
-__device__ __forceinline__ void finish_vertex(const CellDev& c, const MixedArgs& a, int par, int v, float F0, float F1,
-                                              float Q0, float Q1, float Q2, float Q3, float MMf) {
+// force; the velocity and the strain accumulate in float-float.  V, A and the strain
+// (xx yy zz xy, hi and lo) come in from the caller (global memory or a staged copy).
+__device__ __forceinline__ void finish_vertex_core(const CellDev& c, const MixedArgs& a, int par, int v, float F0,
+                                                   float F1, float Q0, float Q1, float Q2, float Q3, float MMf,
+                                                   const ff4& V, const float4& A, const float4& eh, const float4& el) {
     const ParamF& pf = c.pf;
-    const ff4 V = ldg_ff4(c.vel, v);
     ff vh0, vh1;
     if (a.vh_from_buf) {
-        const ff4 h = ldg_ff4(c.vhl, v);
+        const ff4 h = ldg_ff4(c.vhl, c.nv, v);
         vh0 = ffx(h); vh1 = ffy(h);
     } else {
-        const float4 A = ld_acc(c.acc, v);
         vh0 = ff_add(ffx(V), ff_mul_f(a.hdt, A.x));
         vh1 = ff_add(ffy(V), ff_mul_f(a.hdt, A.y));
     }
@@ -354,19 +409,25 @@ __device__ __forceinline__ void finish_vertex(const CellDev& c, const MixedArgs&
         Vn1 = ff_add(ffy(V), ff_mul_f(a.dtr, An1));
         Vn2 = ff_add(ffz(V), ff_mul_f(a.dtr, An2));
     }
-    const float4* eo = reinterpret_cast<const float4*>(c.ea[par] + 6 * (size_t)v);
-    float4* en = reinterpret_cast<float4*>(c.ea[par ^ 1] + 6 * (size_t)v);
-    const float4 eh = __ldg(eo), el = __ldg(eo + 1);   // (xx, yy, zz, xy) hi and lo; (xz, yz) stay as set
+    float4* en = reinterpret_cast<float4*>(c.ea[par ^ 1]);   // (xz, yz) stay as set
     const float iMM = 1.0f / MMf;
     const ff exx = ff_add_f({eh.x, el.x}, Q0 * iMM), eyy = ff_add_f({eh.y, el.y}, Q1 * iMM);
     const ff ezz = ff_add_f({eh.z, el.z}, Q3 * iMM), exy = ff_add_f({eh.w, el.w}, Q2 * iMM);
-    en[0] = make_float4(exx.hi, eyy.hi, ezz.hi, exy.hi);
-    en[1] = make_float4(exx.lo, eyy.lo, ezz.lo, exy.lo);
-    *reinterpret_cast<float4*>(c.acc + v) = make_float4(An0, An1, An2, 0.0f);
-    st_ff4(c.vel, v, make_ff4(Vn0, Vn1, Vn2));
+    en[v] = make_float4(exx.hi, eyy.hi, ezz.hi, exy.hi);
+    en[c.nv + v] = make_float4(exx.lo, eyy.lo, ezz.lo, exy.lo);
+    st_acc(c.acc, v, make_float4(An0, An1, An2, 0.0f));
+    st_ff4(c.vel, c.nv, v, make_ff4(Vn0, Vn1, Vn2));
     // NaN/Inf in the state shows up in the FP32 quantities derived from it
     const float chk = An0 + An1 + Q0 + Q1 + Q2 + vh0.hi + vh1.hi;
     if (!isfinite(chk)) atomicOr(c.status, 1u);
+}
+
+__device__ __forceinline__ void finish_vertex(const CellDev& c, const MixedArgs& a, int par, int v, float F0, float F1,
+                                              float Q0, float Q1, float Q2, float Q3, float MMf) {
+    const float4* eo = reinterpret_cast<const float4*>(c.ea[par]);
+    const float4 A = a.vh_from_buf ? make_float4(0.f, 0.f, 0.f, 0.f) : ld_acc(c.acc, v);
+    finish_vertex_core(c, a, par, v, F0, F1, Q0, Q1, Q2, Q3, MMf, ldg_ff4(c.vel, c.nv, v), A, __ldg(eo + v),
+                       __ldg(eo + c.nv + v));
 }
 
 __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
@@ -431,12 +492,13 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
         const float rho_max = pf.rho_i_max;
         for (int i = threadIdx.x; i < pt.y; i += blockDim.x) {
             const int v = pt.x + i;
-            float R0 = 0, R1 = 0, Q0 = 0, Q1 = 0, Q2 = 0, Q3 = 0, MMf = 0, Asf = 0;
+            float Q0 = 0, Q1 = 0, Q2 = 0, Q3 = 0, MMf = 0, Asf = 0;
+            ff R0 = {0.0f, 0.0f}, R1 = {0.0f, 0.0f};   // compensated: the corner forces largely cancel
             for (int k = c.vt_ptr[v]; k < c.vt_ptr[v + 1]; ++k) {
                 const int code = c.vc_code[k];
                 const int sl = code >> 2, cn = code & 3;
-                R0 += smf[(2 * cn) * emax + sl];
-                R1 += smf[(2 * cn + 1) * emax + sl];
+                R0 = ff_add_f(R0, smf[(2 * cn) * emax + sl]);
+                R1 = ff_add_f(R1, smf[(2 * cn + 1) * emax + sl]);
                 Q0 += smf[(6 + 4 * cn) * emax + sl];
                 Q1 += smf[(7 + 4 * cn) * emax + sl];
                 Q2 += smf[(8 + 4 * cn) * emax + sl];
@@ -446,12 +508,13 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             }
             const float Asum = Asf * (1.0f / 3.0f);
             // integrin force (UL:1241-1269) in FP32
-            const ff4 f4 = ldg_ff4(c.fau, v);
+            const ff4 f4 = ldg_ff4(c.fau, c.nv, v);
             float fs[3], bell;
             spring_force32(pf, f4.hx, f4.hy, f4.hz, fs, &bell);
-            const float rho = c.rho_w ? f64_to_f32_rn(c.rho_w[v]) : rho_max;
-            const float kfa = -ld_ff(c.cC, v).hi * Asum * rho;
-            float F0 = kfa * fs[0] - R0, F1 = kfa * fs[1] - R1;
+            const float rho = c.rho_w ? ld_rho(c.rho_w, v) : rho_max;
+            const float kfa = -ld_ff(c.cC, c.nv, v).hi * Asum * rho;
+            // F = kfa fs - R with the product exact (TwoProduct) and one rounding at the end
+            float F0 = net_force(kfa, fs[0], R0), F1 = net_force(kfa, fs[1], R1);
             const int rank = c.bnd_rank[v];
             if (rank >= 0) {
                 const int slot = atomicAdd(&s_nbnd, 1);
@@ -518,10 +581,10 @@ __device__ __forceinline__ void finish_area_boundary(const CellDev& c, const dou
     double s0 = 0, s1 = 0, s2 = 0;
     for (int r = threadIdx.x; r < c.nb; r += blockDim.x) {
         double xi[3];
-        pos_d(ld_ff4(xo, c.bnd_vert[r]), xi);
+        pos_d(ld_ff4(xo, c.nv, c.bnd_vert[r]), xi);
         for (int k = c.bnd_optr[r]; k < c.bnd_optr[r + 1]; ++k) {
             double xj[3];
-            pos_d(ld_ff4(xo, c.bnd_out[k]), xj);
+            pos_d(ld_ff4(xo, c.nv, c.bnd_out[k]), xj);
             const double cr = xi[0] * xj[1] - xj[0] * xi[1];
             s0 += 0.5 * cr;
             s1 += (1.0 / 6.0) * (xi[0] + xj[0]) * cr;
@@ -575,33 +638,33 @@ __global__ void __launch_bounds__(kK1Threads, 3) k_vertex_phase_mixed(const Cell
     double4* __restrict__ xo = c.pos[par ^ 1];
     if (v < c.nv) {
         const double4* __restrict__ X = c.pos[par];
-        const ff4 Xv = ldg_ff4(X, v);
+        const ff4 Xv = ldg_ff4(X, c.nv, v);
         ff xn0, xn1, xn2 = ffz(Xv);
         if (flags & VM_IMPORT) {
             const double* qq = va.stage_in + 3 * (size_t)(c.hoff + v);
             xn0 = ff_from_d(qq[0]); xn1 = ff_from_d(qq[1]); xn2 = ff_from_d(qq[2]);
-            st_ff4(xo, v, make_ff4(xn0, xn1, xn2));
+            st_ff4(xo, c.nv, v, make_ff4(xn0, xn1, xn2));
         } else if (flags & VM_PREDICT) {
-            const ff4 V = ldg_ff4(c.vel, v);
+            const ff4 V = ldg_ff4(c.vel, c.nv, v);
             const float4 A = ld_acc(c.acc, v);
             ff vh0, vh1;
             predict_ff(ffx(Xv), ffx(V), A.x, va.hdt, va.dt, vh0, xn0);
             predict_ff(ffy(Xv), ffy(V), A.y, va.hdt, va.dt, vh1, xn1);
-            st_ff4(xo, v, make_ff4(xn0, xn1, xn2));
+            st_ff4(xo, c.nv, v, make_ff4(xn0, xn1, xn2));
             if (flags & VM_EXPORT) {
-                st_ff4(c.vhl, v, make_ff4(vh0, vh1, {0.0f, 0.0f}));
+                st_ff4(c.vhl, c.nv, v, make_ff4(vh0, vh1, {0.0f, 0.0f}));
                 double* qq = va.stage_out + 3 * (size_t)(c.hoff + v);
                 qq[0] = ff_to_d(xn0); qq[1] = ff_to_d(xn1); qq[2] = ff_to_d(xn2);
             }
         } else {
-            const ff4 t = ld_ff4(xo, v);
+            const ff4 t = ld_ff4(xo, c.nv, v);
             xn0 = ffx(t); xn1 = ffy(t); xn2 = ffz(t);
         }
         const ff cu0 = ff_sub(xn0, ffx(Xv)), cu1 = ff_sub(xn1, ffy(Xv));   // step displacement
         if (flags & VM_UPDATE_FA) {
             const ParamF& pf = c.pf;
-            const ff4 f = ldg_ff4(c.fau, v);
-            const ff cold = ld_ff(c.cC, v), cAv = ld_ff(c.cA, v);
+            const ff4 f = ldg_ff4(c.fau, c.nv, v);
+            const ff cold = ld_ff(c.cC, c.nv, v), cAv = ld_ff(c.cA, c.nv, v);
             ff u0 = ff_add(ffx(f), cu0), u1 = ff_add(ffy(f), cu1), u2 = ffz(f);
             if (c.has_sub && c.sub.moving) {
                 double wgt[3], Xd[3], fd[3];
@@ -617,13 +680,17 @@ __global__ void __launch_bounds__(kK1Threads, 3) k_vertex_phase_mixed(const Cell
                     u2 = ff_sub(u2, ff_from_d(wgt[0] * (a0.z - b0.z) + wgt[1] * (a1.z - b1.z) + wgt[2] * (a2.z - b2.z)));
                 }
             }
-            float fs[3], force;
-            spring_force32(pf, u0.hi, u1.hi, u2.hi, fs, &force);
-            const float koff = pf.ka * __expf(force * pf.iFa) + pf.kb * __expf(-force * pf.iFb);
+            // Bell kinetics (UL:2137-2171): k_off from the float-float force, the c_C update in float-float
+            const ff F = bell_ff(pf, u0, u1, u2);
+            const ff xa = ff_mul(F, {pf.iFa, pf.iFa_lo}), xb = ff_mul(F, {pf.iFb, pf.iFb_lo});
+            // the exponent is capped below FP32 overflow (e^88 ~ 1.7e38): any force that large already
+            // gives dt k_off >> 1, i.e. the same decisions as the unbounded FP64 rate
+            const float koff = pf.ka * expf(fminf(xa.hi, 88.0f)) * (1.0f + xa.lo) + pf.kb * expf(-xb.hi) * (1.0f - xb.lo);
             const float coldf = cold.hi, kon = pf.k_on, dtf = va.dtf;
-            ff cn = ff_add_f(cold, dtf * (kon * (1.0f - coldf) - koff * coldf));
+            const ff rate = ff_sub(ff_mul_f(ff_sub({1.0f, 0.0f}, cold), kon), ff_mul_f(cold, koff));
+            ff cn = ff_add(cold, ff_mul(va.dt, rate));
             if (cn.hi < 0.0f) cn = {0.0f, 0.0f};
-            if (cAv.hi < 0.0f) st_ff(c.cA, v, {0.0f, 0.0f});
+            if (cAv.hi < 0.0f) st_ff(c.cA, c.nv, v, {0.0f, 0.0f});
             ff n0, n1, n2;
             const bool keep_pos = coldf > 0.0f && (1.0f - dtf * koff) > 0.0f;
             if (keep_pos && cn.hi > 0.0f) {
@@ -633,11 +700,11 @@ __global__ void __launch_bounds__(kK1Threads, 3) k_vertex_phase_mixed(const Cell
             } else {
                 n0 = {0.0f * u0.hi, 0.0f}; n1 = {0.0f * u1.hi, 0.0f}; n2 = {0.0f * u2.hi, 0.0f};
             }
-            st_ff(c.cC, v, cn);
-            st_ff4(c.fau, v, make_ff4(n0, n1, n2));
+            st_ff(c.cC, c.nv, v, cn);
+            st_ff4(c.fau, c.nv, v, make_ff4(n0, n1, n2));
         }
         if (!(flags & VM_EXPORT)) {
-            const float4 eh = __ldg(reinterpret_cast<const float4*>(c.ea[par] + 6 * (size_t)v));  // (xx, yy, zz, xy)
+            const float4 eh = __ldg(reinterpret_cast<const float4*>(c.ea[par]) + v);  // (xx, yy, zz, xy) hi
             float4* r = c.rec + kRec * (size_t)v;
             r[0] = make_float4(Xv.hx, Xv.hy, Xv.lx, Xv.ly);
             r[1] = make_float4(cu0.hi, cu1.hi, eh.x, eh.y);
@@ -663,6 +730,348 @@ void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, 
     k_vertex_phase_mixed<<<nwork, threads, 0, st>>>(cells, work, va);
 }
 
+// ===========================================================================
+// Staged patch phase: a persistent CTA walks its patches and, one patch ahead,
+// copies everything the patch reads into shared memory with bulk asynchronous
+// copies completing on an mbarrier (two stages).  Element records of the owned
+// range and the owned vertices' state are contiguous ranges (one copy each); the
+// halo records are one 48-B copy per halo vertex, issued by the lanes of warp 0.
+// The arithmetic is that of k_patch_phase_mixed.
+// ===========================================================================
+struct StageLayout {
+    uint32_t stage_bytes;   // bytes per stage
+    uint32_t o_hdr, o_loc, o_rec, o_vt, o_code, o_fau, o_cc, o_rho, o_vhi, o_vlo, o_acc, o_eahi, o_ealo, o_rank;
+    uint32_t smf_off;       // element outputs, after the two stages
+    int32_t cap_ne, cap_nvp, cap_nh, cap_nc;
+};
+
+struct StageHdr {
+    int32_t cell, idx, par, bad;
+    int4 pt;                // (v0, nvp, e0, ne)
+    int4 px;                // (h0, nh, c0, nc)
+    int32_t vt_off, code_base, s_off, has_rho;
+    unsigned long long ap_call;
+    ElemParams q;
+};
+
+constexpr long long kWaitLimit = 4000000000ll;   // SM clocks (about 2 s) before a stage wait gives up
+
+__device__ __forceinline__ void stage_issue(const MixedArgs& a, const StageLayout& L, unsigned char* sm, int w, int s,
+                                            uint64_t* bar) {
+    unsigned char* st = sm + (size_t)s * L.stage_bytes;
+    StageHdr* h = reinterpret_cast<StageHdr*>(st + L.o_hdr);
+    const int lane = threadIdx.x & 31;
+    fence_proxy_async_smem();   // the stage was last read through the generic proxy
+    if (lane == 0) {
+        const WorkItem it = a.work[w];
+        const CellDev& c = a.cells[it.cell];
+        const int4 pt = c.patch[it.idx];
+        const int4 px = c.patch_x[it.idx];
+        const int n = c.nv;
+        const int par = c.ctl[0];
+        h->cell = it.cell;
+        h->idx = it.idx;
+        h->par = par;
+        h->pt = pt;
+        h->px = px;
+        h->ap_call = c.ap[0];
+        h->has_rho = c.rho_w != nullptr;
+        {   // element constants of this cell and step
+            const wcfe_params& p = c.prm;
+            const double t = isnan(a.t_override) ? c.clk[0] : a.t_override;
+            const double t_act = t < p.tact_t1 ? t * p.tact_rate : p.tact_max;
+            h->q.mu = (float)p.mu;
+            h->q.thick = (float)p.thick;
+            h->q.grow = (float)(p.thetag_dot * a.dt_real);
+            h->q.s_iso = (float)(p.kappa * t_act);
+            h->q.t_an = (float)((1.0 - 2.0 * p.kappa) * t_act);
+            h->q.cx = (float)c.area4[1];
+            h->q.cy = (float)c.area4[2];
+        }
+        const bool bad = pt.w > L.cap_ne || pt.y > L.cap_nvp || px.y > L.cap_nh || px.w > L.cap_nc;
+        h->bad = bad;
+        if (bad) {
+            atomicOr(c.status, 4u);
+            mbar_arrive_expect_tx(bar + s, 0);
+        } else {
+            const int v0 = pt.x, nvp = pt.y;
+            const int a4 = v0 & ~3;                  // 16-B aligned start of the 4-byte per-vertex arrays
+            const int cb = px.z & ~7;                // 16-B aligned start of the 2-byte codes
+            h->vt_off = v0 - a4;
+            h->s_off = v0 - a4;
+            h->code_base = cb;
+            const uint32_t b_loc = align16(8u * (uint32_t)pt.w);
+            const uint32_t b_rec = 48u * (uint32_t)nvp;
+            const uint32_t b_vt = align16(4u * (uint32_t)(v0 + nvp + 1 - a4));
+            const uint32_t b_code = align16(2u * (uint32_t)(px.z + px.w - cb));
+            const uint32_t b_v16 = 16u * (uint32_t)nvp;
+            const uint32_t b_s4 = align16(4u * (uint32_t)(v0 + nvp - a4));
+            const uint32_t total = b_loc + b_rec + b_vt + b_code + 6u * b_v16 + (h->has_rho ? 3u : 2u) * b_s4 +
+                                   48u * (uint32_t)px.y;
+            mbar_arrive_expect_tx(bar + s, total);
+            const float4* fau = reinterpret_cast<const float4*>(c.fau);
+            const float4* vel = reinterpret_cast<const float4*>(c.vel);
+            const float4* ea = reinterpret_cast<const float4*>(c.ea[par]);
+            bulk_g2s(st + L.o_loc, c.patch_loc + 4 * (size_t)pt.z, b_loc, bar + s);
+            if (b_rec) bulk_g2s(st + L.o_rec, c.rec + 3 * (size_t)v0, b_rec, bar + s);
+            bulk_g2s(st + L.o_vt, c.vt_ptr + a4, b_vt, bar + s);
+            if (b_code) bulk_g2s(st + L.o_code, c.vc_code + cb, b_code, bar + s);
+            if (b_v16) {
+                bulk_g2s(st + L.o_fau, fau + v0, b_v16, bar + s);
+                bulk_g2s(st + L.o_vhi, vel + v0, b_v16, bar + s);
+                bulk_g2s(st + L.o_vlo, vel + n + v0, b_v16, bar + s);
+                bulk_g2s(st + L.o_acc, reinterpret_cast<const float4*>(c.acc) + v0, b_v16, bar + s);
+                bulk_g2s(st + L.o_eahi, ea + v0, b_v16, bar + s);
+                bulk_g2s(st + L.o_ealo, ea + n + v0, b_v16, bar + s);
+            }
+            if (b_s4) {
+                bulk_g2s(st + L.o_cc, reinterpret_cast<const float*>(c.cC) + a4, b_s4, bar + s);
+                bulk_g2s(st + L.o_rank, c.bnd_rank + a4, b_s4, bar + s);
+                if (h->has_rho) bulk_g2s(st + L.o_rho, reinterpret_cast<const float*>(c.rho_w) + a4, b_s4, bar + s);
+            }
+        }
+    }
+    __syncwarp();
+    if (!h->bad) {
+        const CellDev& c = a.cells[h->cell];
+        const int nvp = h->pt.y, h0 = h->px.x, nh = h->px.y;
+        unsigned char* rec_s = st + L.o_rec;
+        for (int k = lane; k < nh; k += 32) {
+            const int u = c.patch_halo[h0 + k];
+            bulk_g2s(rec_s + 48 * (size_t)(nvp + k), c.rec + 3 * (size_t)u, 48u, bar + s);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_patch_mixed_staged(MixedArgs a, StageLayout L) {
+    extern __shared__ __align__(128) unsigned char sm[];
+    __shared__ uint64_t bar[2];
+    __shared__ int s_nbnd, s_ok;
+    __shared__ float s_bnd[8 * kBndSlots];
+    float* smf = reinterpret_cast<float*>(sm + L.smf_off);
+    const int emax = L.cap_ne;   // field stride of the element outputs
+    if (threadIdx.x == 0) {
+        mbar_init(bar, 1);
+        mbar_init(bar + 1, 1);
+        mbar_init_fence();
+    }
+    __syncthreads();
+    if ((int)blockIdx.x < a.nwork && threadIdx.x < 32) stage_issue(a, L, sm, blockIdx.x, 0, bar);
+    int k = 0;
+    for (int w = blockIdx.x; w < a.nwork; w += gridDim.x, ++k) {
+        const int s = k & 1;
+        const int wn = w + gridDim.x;
+        if (wn < a.nwork && threadIdx.x < 32) stage_issue(a, L, sm, wn, s ^ 1, bar);
+        if (threadIdx.x == 0) {
+            s_nbnd = 0;
+            s_ok = mbar_wait_bounded(bar + s, (uint32_t)(k >> 1) & 1u, kWaitLimit) ? 1 : 0;
+        }
+        __syncthreads();
+        if (!s_ok) {
+            // a copy did not complete: flag the cell, wait (bounded) for this CTA's copies, leave
+            if (threadIdx.x == 0) {
+                atomicOr(a.cells[a.work[w].cell].status, 8u);
+                mbar_wait_bounded(bar + s, (uint32_t)(k >> 1) & 1u, kWaitLimit);
+                if (wn < a.nwork) mbar_wait_bounded(bar + (s ^ 1), (uint32_t)((k + 1) >> 1) & 1u, kWaitLimit);
+            }
+            return;
+        }
+        const unsigned char* st = sm + (size_t)s * L.stage_bytes;
+        const StageHdr* h = reinterpret_cast<const StageHdr*>(st + L.o_hdr);
+        if (h->bad) {   // capacity exceeded: status already flagged
+            __syncthreads();
+            continue;
+        }
+        const CellDev& c = a.cells[h->cell];
+        const int4 pt = h->pt;
+        const int par = h->par;
+        const ElemParams q = h->q;
+        const float4* rec_s = reinterpret_cast<const float4*>(st + L.o_rec);
+        const uint2* loc_s = reinterpret_cast<const uint2*>(st + L.o_loc);
+        // ---- elements of the patch -> shared memory ----
+        for (int j = threadIdx.x; j < pt.w; j += blockDim.x) {
+            const uint2 l2 = loc_s[j];
+            const int id[3] = {(int)(l2.x & 0xffffu), (int)(l2.x >> 16), (int)(l2.y & 0xffffu)};
+            float4 r[3][kRec];
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk)
+#pragma unroll
+                for (int m = 0; m < kRec; ++m) r[kk][m] = rec_s[kRec * id[kk] + m];
+            Elem2 o;
+            element2d(r, q, o);
+#pragma unroll
+            for (int kk = 0; kk < 3; ++kk) {
+                smf[(2 * kk + 0) * emax + j] = o.re[kk][0];
+                smf[(2 * kk + 1) * emax + j] = o.re[kk][1];
+#pragma unroll
+                for (int m = 0; m < 4; ++m) smf[(6 + 4 * kk + m) * emax + j] = o.rea[kk][m];
+            }
+            smf[18 * emax + j] = o.mm;
+            smf[19 * emax + j] = o.acur;
+        }
+        __syncthreads();
+        // ---- owned vertices (as k_patch_phase_mixed, state from the stage) ----
+        const int32_t* vt_s = reinterpret_cast<const int32_t*>(st + L.o_vt) + h->vt_off;
+        const uint16_t* code_s = reinterpret_cast<const uint16_t*>(st + L.o_code) - h->code_base;
+        const float4* fau_s = reinterpret_cast<const float4*>(st + L.o_fau);
+        const float* cc_s = reinterpret_cast<const float*>(st + L.o_cc) + h->s_off;
+        const float* rho_s = reinterpret_cast<const float*>(st + L.o_rho) + h->s_off;
+        const int32_t* rank_s = reinterpret_cast<const int32_t*>(st + L.o_rank) + h->s_off;
+        const float4* vhi_s = reinterpret_cast<const float4*>(st + L.o_vhi);
+        const float4* vlo_s = reinterpret_cast<const float4*>(st + L.o_vlo);
+        const float4* acc_s = reinterpret_cast<const float4*>(st + L.o_acc);
+        const float4* eahi_s = reinterpret_cast<const float4*>(st + L.o_eahi);
+        const float4* ealo_s = reinterpret_cast<const float4*>(st + L.o_ealo);
+        const ParamF& pf = c.pf;
+        const float rho_max = pf.rho_i_max;
+        const bool has_rho = h->has_rho;
+        const double4* __restrict__ X = c.pos[par];
+        const double4* __restrict__ xp = c.pos[par ^ 1];
+        for (int i = threadIdx.x; i < pt.y; i += blockDim.x) {
+            const int v = pt.x + i;
+            float Q0 = 0, Q1 = 0, Q2 = 0, Q3 = 0, MMf = 0, Asf = 0;
+            ff R0 = {0.0f, 0.0f}, R1 = {0.0f, 0.0f};   // compensated: the corner forces largely cancel
+            for (int kk = vt_s[i]; kk < vt_s[i + 1]; ++kk) {
+                const int code = code_s[kk];
+                const int sl = code >> 2, cn = code & 3;
+                R0 = ff_add_f(R0, smf[(2 * cn) * emax + sl]);
+                R1 = ff_add_f(R1, smf[(2 * cn + 1) * emax + sl]);
+                Q0 += smf[(6 + 4 * cn) * emax + sl];
+                Q1 += smf[(7 + 4 * cn) * emax + sl];
+                Q2 += smf[(8 + 4 * cn) * emax + sl];
+                Q3 += smf[(9 + 4 * cn) * emax + sl];
+                MMf += smf[18 * emax + sl];
+                Asf += smf[19 * emax + sl];
+            }
+            const float Asum = Asf * (1.0f / 3.0f);
+            const float4 f4 = fau_s[i];
+            float fs[3], bell;
+            spring_force32(pf, f4.x, f4.y, f4.z, fs, &bell);
+            const float rho = has_rho ? rho_s[i] : rho_max;
+            const float kfa = -cc_s[i] * Asum * rho;
+            // F = kfa fs - R with the product exact (TwoProduct) and one rounding at the end
+            float F0 = net_force(kfa, fs[0], R0), F1 = net_force(kfa, fs[1], R1);
+            const int rank = rank_s[i];
+            if (rank >= 0) {
+                const int slot = atomicAdd(&s_nbnd, 1);
+                if (slot < kBndSlots) {
+                    float* b = s_bnd + 8 * slot;
+                    b[0] = __int_as_float(i); b[1] = F0; b[2] = F1; b[3] = Q0;
+                    b[4] = Q1; b[5] = Q2; b[6] = Q3; b[7] = MMf;
+                    continue;
+                }
+                boundary_force(c, a, pt, X, xp, v, rank, h->ap_call, F0, F1);   // queue full: finish in place
+            }
+            const float4 vh = vhi_s[i], vl = vlo_s[i];
+            finish_vertex_core(c, a, par, v, F0, F1, Q0, Q1, Q2, Q3, MMf,
+                               {vh.x, vh.y, vh.z, vh.w, vl.x, vl.y, vl.z, vl.w}, acc_s[i], eahi_s[i], ealo_s[i]);
+        }
+        __syncthreads();
+        const int nq = min(s_nbnd, kBndSlots);
+        for (int j = threadIdx.x; j < nq; j += blockDim.x) {
+            const float* b = s_bnd + 8 * j;
+            const int i = __float_as_int(b[0]);
+            const int v = pt.x + i;
+            float F0 = b[1], F1 = b[2];
+            boundary_force(c, a, pt, X, xp, v, rank_s[i], h->ap_call, F0, F1);
+            const float4 vh = vhi_s[i], vl = vlo_s[i];
+            finish_vertex_core(c, a, par, v, F0, F1, b[3], b[4], b[5], b[6], b[7],
+                               {vh.x, vh.y, vh.z, vh.w, vl.x, vl.y, vl.z, vl.w}, acc_s[i], eahi_s[i], ealo_s[i]);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            const unsigned int done = atomicAdd(reinterpret_cast<unsigned int*>(c.ctl + 1), 1u);
+            if ((int)done == c.np - 1) {
+                c.ctl[1] = 0;
+                c.ctl[0] = par ^ 1;
+                c.clk[0] = c.clk[0] + a.dt_real;
+                c.ap[0] = h->ap_call + 1ull;
+            }
+        }
+    }
+}
+
+// Shared-memory plan of the staged kernel for the given capacities; false if it
+// does not fit in max_smem bytes.
+bool staged_layout(int cap_ne, int cap_nvp, int cap_nh, int cap_nc, size_t max_smem, StageLayout* L,
+                   size_t* total) {
+    cap_ne = (cap_ne + 1) & ~1;
+    uint32_t o = 0;
+    auto put = [&](uint32_t bytes) {
+        const uint32_t at = o;
+        o = (o + bytes + 127u) & ~127u;
+        return at;
+    };
+    L->o_hdr = put((uint32_t)sizeof(StageHdr));
+    L->o_loc = put(8u * cap_ne + 16u);
+    L->o_rec = put(48u * (uint32_t)(cap_nvp + cap_nh));
+    L->o_vt = put(4u * (uint32_t)(cap_nvp + 8));
+    L->o_code = put(2u * (uint32_t)(cap_nc + 16));
+    L->o_fau = put(16u * cap_nvp);
+    L->o_vhi = put(16u * cap_nvp);
+    L->o_vlo = put(16u * cap_nvp);
+    L->o_acc = put(16u * cap_nvp);
+    L->o_eahi = put(16u * cap_nvp);
+    L->o_ealo = put(16u * cap_nvp);
+    L->o_cc = put(4u * (uint32_t)(cap_nvp + 8));
+    L->o_rho = put(4u * (uint32_t)(cap_nvp + 8));
+    L->o_rank = put(4u * (uint32_t)(cap_nvp + 8));
+    L->stage_bytes = o;
+    L->smf_off = 2u * o;
+    L->cap_ne = cap_ne;
+    L->cap_nvp = cap_nvp;
+    L->cap_nh = cap_nh;
+    L->cap_nc = cap_nc;
+    *total = (size_t)L->smf_off + sizeof(float) * (size_t)cap_ne * kSlot32;
+    return *total <= max_smem;
+}
+
+static size_t g_staged_optin = 0;   // dynamic shared memory the staged kernel may use
+
+cudaError_t configure_staged(size_t max_smem) {
+    cudaFuncAttributes at;
+    cudaError_t e = cudaFuncGetAttributes(&at, (const void*)k_patch_mixed_staged);
+    if (e != cudaSuccess) return e;
+    size_t dyn = max_smem > at.sharedSizeBytes + 1024 ? max_smem - at.sharedSizeBytes - 1024 : 0;
+    g_staged_optin = dyn;
+    return cudaFuncSetAttribute((const void*)k_patch_mixed_staged, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)dyn);
+}
+
+// Launch the staged kernel if its plan fits; returns false (nothing launched) otherwise.
+bool launch_patch_staged(const CellDev* cells, const WorkItem* work, int nwork, int cap_ne, int cap_nvp, int cap_nh,
+                         int cap_nc, double dt, double dt_real, double ap_thresh, double t_override, int vh_from_buf,
+                         int num_sms, cudaStream_t st) {
+    if (nwork <= 0) return true;
+    StageLayout L;
+    size_t smem = 0;
+    if (!staged_layout(cap_ne, cap_nvp, cap_nh, cap_nc, g_staged_optin, &L, &smem)) return false;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_patch_mixed_staged, 256, smem) !=
+            cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return false;
+    }
+    MixedArgs a;
+    a.cells = cells;
+    a.work = work;
+    a.nwork = nwork;
+    a.emax = L.cap_ne;
+    a.dt_real = dt_real;
+    a.hdt = ff_from_d(dt / 2.0);
+    a.cdt = ff_from_d(dt_real - dt / 2.0);
+    a.dtr = ff_from_d(dt_real);
+    a.half = dt_real > dt / 2.0;
+    a.ap_thresh = ap_thresh;
+    a.t_override = t_override;
+    a.vh_from_buf = vh_from_buf;
+    const int grid = std::min(nwork, per_sm * num_sms);
+    k_patch_mixed_staged<<<grid, 256, smem, st>>>(a, L);
+    return true;
+}
+
 size_t mixed_smem_bytes(int emax) { return sizeof(float) * (size_t)emax * kSlot32; }
 
 cudaError_t configure_mixed(size_t max_smem) {
@@ -670,7 +1079,9 @@ cudaError_t configure_mixed(size_t max_smem) {
     cudaError_t e = cudaFuncGetAttributes(&at, (const void*)k_patch_phase_mixed);
     if (e != cudaSuccess) return e;
     size_t dyn = max_smem > at.sharedSizeBytes ? max_smem - at.sharedSizeBytes : 0;
-    return cudaFuncSetAttribute((const void*)k_patch_phase_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    e = cudaFuncSetAttribute((const void*)k_patch_phase_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+    if (e != cudaSuccess) return e;
+    return configure_staged(max_smem);
 }
 
 int mixed_occupancy(int threads, size_t smem) {

@@ -116,6 +116,10 @@ std::string build_patches(Patches& P, const Topology& T, int32_t emax) {
     P.emax = emax;
     P.patch.clear();
     P.elems.clear();
+    P.xinfo.clear();
+    P.halo.clear();
+    P.loc.clear();
+    P.max_nvp = P.max_nh = P.max_nc = 0;
     P.vc_code.assign(T.vt_idx.size(), 0);
     P.max_ne = 0;
     std::vector<int32_t> mark(T.nt, -1), slot(T.nt, 0);
@@ -149,11 +153,45 @@ std::string build_patches(Patches& P, const Topology& T, int32_t emax) {
                 int corner = (T.tri[3 * t] == u) ? 0 : (T.tri[3 * t + 1] == u ? 1 : 2);
                 P.vc_code[k] = (uint16_t)((slot[t] << 2) | corner);
             }
+        // halo: vertices of the patch's elements outside [v0, v), ascending
+        const int nvp = v - v0;
+        std::vector<int32_t> hl;
+        for (int j = 0; j < ne; ++j)
+            for (int q = 0; q < 3; ++q) {
+                const int u = T.tri[3 * P.elems[e0 + j] + q];
+                if (u < v0 || u >= v) hl.push_back(u);
+            }
+        std::sort(hl.begin(), hl.end());
+        hl.erase(std::unique(hl.begin(), hl.end()), hl.end());
+        if (nvp + (int)hl.size() > 65535) return "a patch touches more than 65535 vertices";
+        const int h0 = (int)P.halo.size();
+        P.halo.insert(P.halo.end(), hl.begin(), hl.end());
+        for (int j = 0; j < ne; ++j) {
+            for (int q = 0; q < 3; ++q) {
+                const int u = T.tri[3 * P.elems[e0 + j] + q];
+                const int l = (u >= v0 && u < v) ? u - v0
+                                                 : nvp + (int)(std::lower_bound(hl.begin(), hl.end(), u) - hl.begin());
+                P.loc.push_back((uint16_t)l);
+            }
+            P.loc.push_back(0);
+        }
+        if (ne & 1) {   // keep every patch's element list at an even offset (16-B aligned loc rows)
+            P.elems.push_back(P.elems[e0 + ne - 1]);
+            for (int q = 0; q < 4; ++q) P.loc.push_back(0);
+        }
         P.patch.push_back(v0);
-        P.patch.push_back(v - v0);
+        P.patch.push_back(nvp);
         P.patch.push_back(e0);
         P.patch.push_back(ne);
+        const int c0 = T.vt_ptr[v0], nc = T.vt_ptr[v] - T.vt_ptr[v0];
+        P.xinfo.push_back(h0);
+        P.xinfo.push_back((int)hl.size());
+        P.xinfo.push_back(c0);
+        P.xinfo.push_back(nc);
         P.max_ne = std::max(P.max_ne, ne);
+        P.max_nvp = std::max(P.max_nvp, nvp);
+        P.max_nh = std::max(P.max_nh, (int)hl.size());
+        P.max_nc = std::max(P.max_nc, nc);
         ++np;
     }
     P.np = np;

@@ -23,9 +23,16 @@ struct Topology {
 
 struct Patches {
     int32_t np = 0, emax = 0, max_ne = 0;
+    int32_t max_nvp = 0, max_nh = 0, max_nc = 0;
     std::vector<int32_t> patch;      // [4 np] (v0, nvp, e0, ne)
-    std::vector<int32_t> elems;      // element ids of each patch
+    std::vector<int32_t> elems;      // element ids of each patch (each patch's list padded to an even length)
     std::vector<uint16_t> vc_code;   // aligned with vt_idx: (slot << 2) | corner
+    // staging description of each patch (the mixed form's pipelined patch kernel):
+    std::vector<int32_t> xinfo;      // [4 np] (h0, nh, c0, nc): halo list offset and count; one-ring codes
+                                     //        vc_code[c0 .. c0 + nc) of the owned vertices
+    std::vector<int32_t> halo;       // vertices of a patch's elements outside its owned range, ascending
+    std::vector<uint16_t> loc;       // [4 per elems entry] corners as patch-local vertex indices:
+                                     //        owned v -> v - v0, halo k -> nvp + k; 4th entry 0
 };
 
 // Returns "" on success or an error message.
