@@ -480,6 +480,9 @@ def run_phase(args):
         eng = capi.Engine(capi.PREC_MIXED if args.phase == "mixed" else capi.PREC_FP64)
         if args.phase == "mixed":
             eng.set_patch_kernel(args.patch_kernel)
+        if args.shape:
+            t, e_ = (int(x) for x in args.shape.split(","))
+            eng.set_shape(t, e_)
         load_cells(eng, cells)
         ncells = len(cells)
     for _ in range(args.warmup):
@@ -544,8 +547,9 @@ def main():
                     help="length of the Poisson arrival window of the serving measurement (0: skip)")
     ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain"],
                     help="profiling aid: run only one timed loop (default shape, no autotune) and print its timing")
-    ap.add_argument("--patch-kernel", type=int, default=0, choices=[0, 1],
-                    help="with --phase mixed: 0 staged patch kernel (default), 1 plain")
+    ap.add_argument("--shape", default="", help="with --phase: patch threads,elements (default: the engine's)")
+    ap.add_argument("--patch-kernel", type=int, default=1, choices=[0, 1],
+                    help="with --phase mixed: 0 staged patch kernel, 1 plain (default)")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

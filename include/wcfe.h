@@ -200,11 +200,11 @@ int wcfe_cell_eval_residual(wcfe_engine* eng, int32_t cell, const double* X, con
 int wcfe_cell_eval_forces(wcfe_engine* eng, int32_t cell, const double* x, double dt_real,
                           double* F_FA, double* F_AP, double* F_bend, double* F_area, double area4[4]);
 
-/* Mixed engines: which patch-phase kernel a step uses.  0 (default): the staged
- * kernel (each patch's records and owned-vertex state copied into shared memory
- * one patch ahead with bulk asynchronous copies) wherever its shared-memory plan
- * fits, else the plain kernel; 1: always the plain kernel.  Results are identical.
- * No counterpart in the reference. */
+/* Mixed engines: which patch-phase kernel a step uses.  0: the staged kernel (a
+ * producer warp copies each patch's records and owned-vertex state into shared
+ * memory one patch ahead with bulk asynchronous copies) wherever its shared-memory
+ * plan fits, else the plain kernel; 1 (default): the plain kernel.  Results are
+ * identical; wcfe_engine_autotune times both.  No counterpart in the reference. */
 int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind);
 
 /* ---- synthetic stepping of every live cell (no El Topo) ----------------- */

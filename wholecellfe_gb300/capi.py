@@ -250,7 +250,7 @@ class Engine:
         check(load().wcfe_engine_set_shape(self.h, threads, emax), "wcfe_engine_set_shape")
 
     def set_patch_kernel(self, kind: int):
-        """Mixed engines: 0 staged patch kernel where it fits (default), 1 plain."""
+        """Mixed engines: 0 staged patch kernel where it fits, 1 plain (default)."""
         check(load().wcfe_engine_set_patch_kernel(self.h, kind), "wcfe_engine_set_patch_kernel")
 
     def shape(self):

@@ -129,7 +129,7 @@ struct wcfe_engine {
     int patch_threads = 128;
     int patch_emax = 320;
     int vblock = 256;             // vertices (threads) per vertex-phase block
-    int patch_kernel = 0;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
+    int patch_kernel = 1;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
     int cap_ne = 0, cap_nvp = 0, cap_nh = 0, cap_nc = 0;   // largest patch over the cells (staging plan)
     bool tuned = false;
     // graphs
@@ -1411,24 +1411,32 @@ int wcfe_engine_autotune(wcfe_engine* e, double dt, int32_t reps) {
     int max_optin = 0;
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
     float best = 1e30f;
-    int bt = e->patch_threads, be = e->patch_emax;
+    int bt = e->patch_threads, be = e->patch_emax, bk = e->patch_kernel;
     bool was_timing = e->timing;
     e->timing = true;
-    for (int em : emax_c) {
-        if (patch_smem_bytes(e->prec, PP_RESIDUAL, em) + 1024 > (size_t)max_optin) continue;
-        for (int th : threads_c) {
-            int r = wcfe_engine_set_shape(e, th, em);
-            if (r) continue;
-            wcfe_engine_step(e, 1, dt);  // warm
-            r = wcfe_engine_step(e, reps, dt);
-            if (r) continue;
-            float t = e->ms_v + e->ms_p;
-            if (t < best) { best = t; bt = th; be = em; }
-            for (auto& s : saved)
-                CK(cudaMemcpyAsync(s.first->state_block, s.second, s.first->state_bytes, cudaMemcpyDeviceToDevice, e->stream));
+    // mixed engines also try the staged patch kernel (its block shape is fixed; it uses emax)
+    const int nkinds = e->prec == WCFE_PREC_MIXED ? 2 : 1;
+    for (int kind = 1; kind >= 2 - nkinds; --kind) {
+        e->patch_kernel = kind;
+        for (int em : emax_c) {
+            if (patch_smem_bytes(e->prec, PP_RESIDUAL, em) + 1024 > (size_t)max_optin) continue;
+            for (int th : threads_c) {
+                if (kind == 0 && th != threads_c[0]) continue;
+                int r = wcfe_engine_set_shape(e, kind == 0 ? e->patch_threads : th, em);
+                if (r) continue;
+                wcfe_engine_step(e, 1, dt);  // warm
+                r = wcfe_engine_step(e, reps, dt);
+                if (r) continue;
+                float t = e->ms_v + e->ms_p;
+                if (t < best) { best = t; bt = e->patch_threads; be = em; bk = kind; }
+                for (auto& s : saved)
+                    CK(cudaMemcpyAsync(s.first->state_block, s.second, s.first->state_bytes, cudaMemcpyDeviceToDevice,
+                                       e->stream));
+            }
         }
     }
     e->timing = was_timing;
+    e->patch_kernel = bk;
     int r = wcfe_engine_set_shape(e, bt, be);
     for (auto& s : saved) {
         cudaMemcpyAsync(s.first->state_block, s.second, s.first->state_bytes, cudaMemcpyDeviceToDevice, e->stream);

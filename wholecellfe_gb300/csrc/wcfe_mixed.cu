@@ -297,42 +297,69 @@ __device__ __forceinline__ void element2d(const float4 r[3][kRec], const ElemPar
 
 constexpr int kBndSlots = 128;   // boundary vertices a patch CTA queues for its second loop
 
-// The neighbour frame of a boundary vertex (UL:1500-1531) on float-float positions:
-// the same candidate scan and orientation test as boundary_frame, on the positions
-// converted to binary64.
-__device__ __forceinline__ bool boundary_frame_ff(const CellDev& c, const double4* __restrict__ xp, int rank,
-                                                  const double xi[3], double x1[3], double x2[3]) {
-    int j1 = -1, j2 = -1;
-    for (int k = c.bnd_cptr[rank]; k < c.bnd_cptr[rank + 1]; ++k) {
-        const int2 cd = c.bnd_cand[k];
-        double pb[3], pi[3];
-        pos_d(ldg_ff4(xp, c.nv, cd.x), pb);
-        pos_d(ldg_ff4(xp, c.nv, cd.y), pi);
-        const double d1x = xs(xi[0], pb[0]), d1y = xs(xi[1], pb[1]);
-        const double d2x = xs(pi[0], xi[0]), d2y = xs(pi[1], xi[1]);
-        const double ncz = xs(xm(d1x, d2y), xm(d1y, d2x));
-        if (ncz > 0) j1 = cd.x;
-        else j2 = cd.x;
-    }
-    if (j1 < 0 || j2 < 0) return false;
-    pos_d(ldg_ff4(xp, c.nv, j1), x1);
-    pos_d(ldg_ff4(xp, c.nv, j2), x2);
-    return true;
-}
+// Per-cell, per-step constants of the boundary terms (computed once per patch CTA).
+struct BndConst {
+    float w;              // (1/2) kappa t_act thick: isotropic active stress on the open one-ring
+    float area_term;      // -k_area (A - A_0) / 2 (calculateAreaConstraintForce)
+    float k_bend, ap_force;
+    ff half_density;      // ap_density / 2
+    uint32_t ap_thr;      // r31 < ap_thr  <=>  r31 / 2^31 < ap_rate dt exp(-ap_rate dt)
+    int32_t ap_enable;
+    uint32_t seed, stream;
+    unsigned long long ap_call;
+};
 
-// Boundary terms of vertex v (rank `rank`) in FP64, added to (F0, F1): the isotropic
-// active stress of the open one-ring, AP push (calculateForce_AP UL:1477-1569),
-// bending (calculateBendingForce2D UL:1571-1689) and area constraint
-// (calculateAreaConstraintForce UL:1691-1784), on the neighbour frame of UL:1500-1531.
-__device__ __forceinline__ void boundary_force(const CellDev& c, const MixedArgs& a, const int4& pt,
-                                               const double4* __restrict__ X, const double4* __restrict__ xp, int v,
-                                               int rank, unsigned long long ap_call, float& F0, float& F1) {
+__device__ __forceinline__ BndConst make_bnd_const(const CellDev& c, const MixedArgs& a, unsigned long long ap_call) {
     const wcfe_params& p = c.prm;
     const double t = isnan(a.t_override) ? c.clk[0] : a.t_override;
     const double s_iso = p.kappa * (t < p.tact_t1 ? t * p.tact_rate : p.tact_max);
-    const double area_tot = c.area4[0];
-    double xi[3];
-    pos_d(ldg_ff4(xp, c.nv, v), xi);
+    const double apt = isnan(a.ap_thresh) ? c.ap_thresh : a.ap_thresh;
+    BndConst b;
+    b.w = (float)(0.5 * s_iso * p.thick);
+    b.area_term = (float)(-p.k_area * (c.area4[0] - p.area0) / 2);
+    b.k_bend = (float)p.k_bend;
+    b.ap_force = (float)p.ap_force;
+    b.half_density = ff_from_d(p.ap_density / 2);
+    const double thr = ceil(apt * 2147483648.0);
+    b.ap_thr = thr <= 0.0 ? 0u : (thr >= 4294967295.0 ? 4294967295u : (uint32_t)thr);
+    b.ap_enable = p.ap_enable;
+    b.seed = p.seed;
+    b.stream = p.stream;
+    b.ap_call = ap_call;
+    return b;
+}
+
+// The neighbour frame of a boundary vertex (UL:1500-1531): the candidate scan of
+// boundary_frame, with the orientation test on float-float differences.
+__device__ __forceinline__ bool boundary_frame_ff(const CellDev& c, const double4* __restrict__ xp, int rank,
+                                                  const ff4& xi, ff4& x1, ff4& x2) {
+    int j1 = -1, j2 = -1;
+    for (int k = c.bnd_cptr[rank]; k < c.bnd_cptr[rank + 1]; ++k) {
+        const int2 cd = c.bnd_cand[k];
+        const ff4 pb = ldg_ff4(xp, c.nv, cd.x), pi = ldg_ff4(xp, c.nv, cd.y);
+        const ff d1x = ff_sub(ffx(xi), ffx(pb)), d1y = ff_sub(ffy(xi), ffy(pb));
+        const ff d2x = ff_sub(ffx(pi), ffx(xi)), d2y = ff_sub(ffy(pi), ffy(xi));
+        const ff ncz = ff_sub(ff_mul(d1x, d2y), ff_mul(d1y, d2x));
+        if (ncz.hi > 0.0f) j1 = cd.x;
+        else j2 = cd.x;
+    }
+    if (j1 < 0 || j2 < 0) return false;
+    x1 = ldg_ff4(xp, c.nv, j1);
+    x2 = ldg_ff4(xp, c.nv, j2);
+    return true;
+}
+
+// Boundary terms of vertex v (rank `rank`) added to (F0, F1), in FP32 on float-float
+// positions: the isotropic active stress of the open one-ring, AP push
+// (calculateForce_AP UL:1477-1569), bending (calculateBendingForce2D UL:1571-1689) and
+// area constraint (calculateAreaConstraintForce UL:1691-1784), on the neighbour frame of
+// UL:1500-1531.  The turning-angle term cos(theta) - 1 is evaluated as -|e1 - e2|^2 / 2,
+// free of the cancellation that FP32 would suffer on a nearly straight boundary, and
+// the AP bond count ceil(density L / 2) is taken on a float-float L.
+__device__ __forceinline__ void boundary_force(const CellDev& c, const BndConst& bc, const int4& pt,
+                                               const double4* __restrict__ X, const double4* __restrict__ xp, int v,
+                                               int rank, float& F0, float& F1) {
+    const ff4 xi = ldg_ff4(xp, c.nv, v);
     // isotropic active stress on the open one-ring: (1/2) s_iso thick e3 x sum (X_k - X_j)
     ff sx = {0.0f, 0.0f}, sy = {0.0f, 0.0f};
     for (int k = c.vt_ptr[v]; k < c.vt_ptr[v + 1]; ++k) {
@@ -345,37 +372,43 @@ __device__ __forceinline__ void boundary_force(const CellDev& c, const MixedArgs
         sx = ff_add(sx, ff_sub(ffx(Xk), ffx(Xj)));
         sy = ff_add(sy, ff_sub(ffy(Xk), ffy(Xj)));
     }
-    const double w = 0.5 * s_iso * p.thick;
-    double Fb0 = w * ff_to_d(sy), Fb1 = -w * ff_to_d(sx);  // minus the residual term w e3 x s
-    double x1[3], x2[3];
+    float Fb0 = bc.w * sy.hi, Fb1 = -bc.w * sx.hi;  // minus the residual term w e3 x s
+    ff4 x1, x2;
     if (boundary_frame_ff(c, xp, rank, xi, x1, x2)) {
-        const double d1x = xi[0] - x1[0], d1y = xi[1] - x1[1], d2x = x2[0] - xi[0], d2y = x2[1] - xi[1];
-        const double d1z = xi[2] - x1[2], d2z = x2[2] - xi[2];
-        const double nn1 = sqrt(d1y * d1y + d1x * d1x), nn2 = sqrt(d2y * d2y + d2x * d2x);
-        const double l1 = sqrt(d1x * d1x + d1y * d1y + d1z * d1z), l2 = sqrt(d2x * d2x + d2y * d2y + d2z * d2z);
-        const double L = l1 + l2;
-        const double nx = l1 / L * (d1y / nn1) + l2 / L * (d2y / nn2);
-        const double ny = l1 / L * (-d1x / nn1) + l2 / L * (-d2x / nn2);
-        double fb = 0.0;
-        if (p.ap_enable) {
-            const uint32_t r31 = ap_draw(p.seed, p.stream, ap_call, (uint32_t)rank);
-            const double Pr = (double)r31 / ((double)2147483647 + 1.);
-            const double lim = p.ap_density * L / 2;
-            const double cnt = lim > 0 ? ceil(lim) : 0.0;
-            const double apt = isnan(a.ap_thresh) ? c.ap_thresh : a.ap_thresh;
-            fb += (Pr < apt) ? p.ap_force * cnt : 0.0;
+        const float d1x = ff_sub(ffx(xi), ffx(x1)).hi, d1y = ff_sub(ffy(xi), ffy(x1)).hi;
+        const float d1z = ff_sub(ffz(xi), ffz(x1)).hi;
+        const float d2x = ff_sub(ffx(x2), ffx(xi)).hi, d2y = ff_sub(ffy(x2), ffy(xi)).hi;
+        const float d2z = ff_sub(ffz(x2), ffz(xi)).hi;
+        const float nn1 = sqrtf(d1y * d1y + d1x * d1x), nn2 = sqrtf(d2y * d2y + d2x * d2x);
+        const float l1 = sqrtf(d1x * d1x + d1y * d1y + d1z * d1z), l2 = sqrtf(d2x * d2x + d2y * d2y + d2z * d2z);
+        const ff Lf = two_sum(l1, l2);
+        const float L = Lf.hi;
+        const float nx = l1 / L * (d1y / nn1) + l2 / L * (d2y / nn2);
+        const float ny = l1 / L * (-d1x / nn1) + l2 / L * (-d2x / nn2);
+        float fb = 0.0f;
+        if (bc.ap_enable) {
+            const uint32_t r31 = ap_draw(bc.seed, bc.stream, bc.ap_call, (uint32_t)rank);
+            const ff lim = ff_mul(Lf, bc.half_density);
+            float cnt = 0.0f;
+            if (lim.hi > 0.0f || (lim.hi == 0.0f && lim.lo > 0.0f)) {
+                cnt = ceilf(lim.hi);
+                if (cnt == lim.hi && lim.lo > 0.0f) cnt += 1.0f;
+            }
+            fb += (r31 < bc.ap_thr) ? bc.ap_force * cnt : 0.0f;
         }
-        const double e1x = d1x / l1, e1y = d1y / l1, e1z = d1z / l1, e2x = d2x / l2, e2y = d2y / l2, e2z = d2z / l2;
-        const double cost = e1x * e2x + e1y * e2y + e1z * e2z;
-        const double ez = xs(xm(e1x, e2y), xm(e1y, e2x));
-        const double turna = ez > 0 ? cost - 1 : 1 - cost;
-        fb += p.k_bend * (turna * 2 / L);
-        fb += -p.k_area * (area_tot - p.area0) / 2 * L;
+        const float i1 = 1.0f / l1, i2 = 1.0f / l2;
+        const float e1x = d1x * i1, e1y = d1y * i1, e1z = d1z * i1, e2x = d2x * i2, e2y = d2y * i2, e2z = d2z * i2;
+        const float gx = e1x - e2x, gy = e1y - e2y, gz = e1z - e2z;
+        const float q = 0.5f * (gx * gx + gy * gy + gz * gz);   // 1 - cos(theta)
+        const float ez = e1x * e2y - e1y * e2x;
+        const float turna = ez > 0.0f ? -q : q;
+        fb += bc.k_bend * (turna * 2.0f / L);
+        fb += bc.area_term * L;
         Fb0 += fb * nx;
         Fb1 += fb * ny;
     }
-    F0 += f64_to_f32_rn(Fb0);
-    F1 += f64_to_f32_rn(Fb1);
+    F0 += Fb0;
+    F1 += Fb1;
 }
 
 // Explicit update of vertex v (UL:592-628): the acceleration in FP32 from the FP32
@@ -435,6 +468,7 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
     const int emax = a.emax;
     // structure of arrays: field k of slot j at smf[k * emax + j]
     __shared__ ElemParams s_q;
+    __shared__ BndConst s_bc;
     __shared__ int s_nbnd;
     __shared__ float s_bnd[8 * kBndSlots];
     for (int w = blockIdx.x; w < a.nwork; w += gridDim.x) {
@@ -458,6 +492,7 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             s_q.t_an = (float)((1.0 - 2.0 * p.kappa) * t_act);
             s_q.cx = (float)c.area4[1];
             s_q.cy = (float)c.area4[2];
+            s_bc = make_bnd_const(c, a, ap_call);
         }
         __syncthreads();
         const ElemParams q = s_q;
@@ -524,7 +559,7 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
                     b[4] = Q1; b[5] = Q2; b[6] = Q3; b[7] = MMf;
                     continue;
                 }
-                boundary_force(c, a, pt, X, xp, v, rank, ap_call, F0, F1);   // queue full: finish in place
+                boundary_force(c, s_bc, pt, X, xp, v, rank, F0, F1);   // queue full: finish in place
             }
             finish_vertex(c, a, par, v, F0, F1, Q0, Q1, Q2, Q3, MMf);
         }
@@ -534,7 +569,7 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             const float* b = s_bnd + 8 * j;
             const int v = pt.x + __float_as_int(b[0]);
             float F0 = b[1], F1 = b[2];
-            boundary_force(c, a, pt, X, xp, v, c.bnd_rank[v], ap_call, F0, F1);
+            boundary_force(c, s_bc, pt, X, xp, v, c.bnd_rank[v], F0, F1);
             finish_vertex(c, a, par, v, F0, F1, b[3], b[4], b[5], b[6], b[7]);
         }
         __syncthreads();
@@ -734,8 +769,9 @@ void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, 
 // Staged patch phase: a persistent CTA walks its patches and, one patch ahead,
 // copies everything the patch reads into shared memory with bulk asynchronous
 // copies completing on an mbarrier (two stages).  Element records of the owned
-// range and the owned vertices' state are contiguous ranges (one copy each); the
-// halo records are one 48-B copy per halo vertex, issued by the lanes of warp 0.
+// range and the owned vertices' state are contiguous ranges (one bulk copy each);
+// the halo records are scattered 48-B rows, copied with 16-B cp.async by the lanes
+// of warp 0, whose completion arrives on the same barrier.
 // The arithmetic is that of k_patch_phase_mixed.
 // ===========================================================================
 struct StageLayout {
@@ -752,6 +788,7 @@ struct StageHdr {
     int32_t vt_off, code_base, s_off, has_rho;
     unsigned long long ap_call;
     ElemParams q;
+    BndConst bc;
 };
 
 constexpr long long kWaitLimit = 4000000000ll;   // SM clocks (about 2 s) before a stage wait gives up
@@ -787,6 +824,7 @@ __device__ __forceinline__ void stage_issue(const MixedArgs& a, const StageLayou
             h->q.t_an = (float)((1.0 - 2.0 * p.kappa) * t_act);
             h->q.cx = (float)c.area4[1];
             h->q.cy = (float)c.area4[2];
+            h->bc = make_bnd_const(c, a, h->ap_call);
         }
         const bool bad = pt.w > L.cap_ne || pt.y > L.cap_nvp || px.y > L.cap_nh || px.w > L.cap_nc;
         h->bad = bad;
@@ -806,8 +844,7 @@ __device__ __forceinline__ void stage_issue(const MixedArgs& a, const StageLayou
             const uint32_t b_code = align16(2u * (uint32_t)(px.z + px.w - cb));
             const uint32_t b_v16 = 16u * (uint32_t)nvp;
             const uint32_t b_s4 = align16(4u * (uint32_t)(v0 + nvp - a4));
-            const uint32_t total = b_loc + b_rec + b_vt + b_code + 6u * b_v16 + (h->has_rho ? 3u : 2u) * b_s4 +
-                                   48u * (uint32_t)px.y;
+            const uint32_t total = b_loc + b_rec + b_vt + b_code + 6u * b_v16 + (h->has_rho ? 3u : 2u) * b_s4;
             mbar_arrive_expect_tx(bar + s, total);
             const float4* fau = reinterpret_cast<const float4*>(c.fau);
             const float4* vel = reinterpret_cast<const float4*>(c.vel);
@@ -832,54 +869,83 @@ __device__ __forceinline__ void stage_issue(const MixedArgs& a, const StageLayou
         }
     }
     __syncwarp();
+    // halo records: scattered 48-B rows, three 16-B cp.async each, spread over the lanes; every
+    // lane then arrives on the stage barrier when its copies have landed (32 of its 33 arrivals)
     if (!h->bad) {
         const CellDev& c = a.cells[h->cell];
         const int nvp = h->pt.y, h0 = h->px.x, nh = h->px.y;
-        unsigned char* rec_s = st + L.o_rec;
+        float4* rec_s = reinterpret_cast<float4*>(st + L.o_rec) + kRec * (size_t)nvp;
         for (int k = lane; k < nh; k += 32) {
-            const int u = c.patch_halo[h0 + k];
-            bulk_g2s(rec_s + 48 * (size_t)(nvp + k), c.rec + 3 * (size_t)u, 48u, bar + s);
+            const float4* src = c.rec + kRec * (size_t)c.patch_halo[h0 + k];
+#pragma unroll
+            for (int m = 0; m < kRec; ++m) cp_async16(rec_s + kRec * (size_t)k + m, src + m);
         }
     }
+    cp_async_mbar_arrive(bar + s);
 }
 
-__global__ void __launch_bounds__(256) k_patch_mixed_staged(MixedArgs a, StageLayout L) {
+constexpr int kConsumers = 256;   // 8 consumer warps; warp 8 produces (stage_issue)
+
+__device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
+// Warp-specialised: warp 8 walks the CTA's patches and fills stage k & 1 for patch k as
+// soon as the consumers have released it (barrier empty[s]); warps 0-7 wait for the
+// stage (barrier full[s]), compute, and release it.
+__global__ void __launch_bounds__(kConsumers + 32) k_patch_mixed_staged(MixedArgs a, StageLayout L) {
     extern __shared__ __align__(128) unsigned char sm[];
-    __shared__ uint64_t bar[2];
+    __shared__ uint64_t full[2], empty[2];
     __shared__ int s_nbnd, s_ok;
     __shared__ float s_bnd[8 * kBndSlots];
     float* smf = reinterpret_cast<float*>(sm + L.smf_off);
     const int emax = L.cap_ne;   // field stride of the element outputs
     if (threadIdx.x == 0) {
-        mbar_init(bar, 1);
-        mbar_init(bar + 1, 1);
+        // full: the producer lane 0's expect-tx arrival + one cp.async arrival per producer lane
+        mbar_init(full, 33);
+        mbar_init(full + 1, 33);
+        mbar_init(empty, 1);
+        mbar_init(empty + 1, 1);
         mbar_init_fence();
     }
     __syncthreads();
-    if ((int)blockIdx.x < a.nwork && threadIdx.x < 32) stage_issue(a, L, sm, blockIdx.x, 0, bar);
+    if (threadIdx.x >= kConsumers) {   // ---- producer warp ----
+        int k = 0;
+        for (int w = blockIdx.x; w < a.nwork; w += gridDim.x, ++k) {
+            const int s = k & 1;
+            if (k >= 2) {   // wait until the consumers released this stage (patch k - 2)
+                int ok = 1;
+                if ((threadIdx.x & 31) == 0)
+                    ok = mbar_wait_bounded(empty + s, (uint32_t)((k >> 1) - 1) & 1u, kWaitLimit) ? 1 : 0;
+                if (!__shfl_sync(0xffffffffu, ok, 0)) return;   // the consumers stopped (and flagged it)
+            }
+            stage_issue(a, L, sm, w, s, full);
+        }
+        return;
+    }
+    // ---- consumer warps ----
     int k = 0;
     for (int w = blockIdx.x; w < a.nwork; w += gridDim.x, ++k) {
         const int s = k & 1;
-        const int wn = w + gridDim.x;
-        if (wn < a.nwork && threadIdx.x < 32) stage_issue(a, L, sm, wn, s ^ 1, bar);
         if (threadIdx.x == 0) {
             s_nbnd = 0;
-            s_ok = mbar_wait_bounded(bar + s, (uint32_t)(k >> 1) & 1u, kWaitLimit) ? 1 : 0;
+            s_ok = mbar_wait_bounded(full + s, (uint32_t)(k >> 1) & 1u, kWaitLimit) ? 1 : 0;
         }
-        __syncthreads();
+        consumer_sync();
         if (!s_ok) {
-            // a copy did not complete: flag the cell, wait (bounded) for this CTA's copies, leave
+            // a copy did not complete: flag the cell, wait (bounded) once more for the stage's copies, leave
             if (threadIdx.x == 0) {
                 atomicOr(a.cells[a.work[w].cell].status, 8u);
-                mbar_wait_bounded(bar + s, (uint32_t)(k >> 1) & 1u, kWaitLimit);
-                if (wn < a.nwork) mbar_wait_bounded(bar + (s ^ 1), (uint32_t)((k + 1) >> 1) & 1u, kWaitLimit);
+                mbar_wait_bounded(full + s, (uint32_t)(k >> 1) & 1u, kWaitLimit);
             }
             return;
         }
         const unsigned char* st = sm + (size_t)s * L.stage_bytes;
         const StageHdr* h = reinterpret_cast<const StageHdr*>(st + L.o_hdr);
         if (h->bad) {   // capacity exceeded: status already flagged
-            __syncthreads();
+            consumer_sync();
+            if (threadIdx.x == 0) mbar_arrive(empty + s);
             continue;
         }
         const CellDev& c = a.cells[h->cell];
@@ -889,7 +955,7 @@ __global__ void __launch_bounds__(256) k_patch_mixed_staged(MixedArgs a, StageLa
         const float4* rec_s = reinterpret_cast<const float4*>(st + L.o_rec);
         const uint2* loc_s = reinterpret_cast<const uint2*>(st + L.o_loc);
         // ---- elements of the patch -> shared memory ----
-        for (int j = threadIdx.x; j < pt.w; j += blockDim.x) {
+        for (int j = threadIdx.x; j < pt.w; j += kConsumers) {
             const uint2 l2 = loc_s[j];
             const int id[3] = {(int)(l2.x & 0xffffu), (int)(l2.x >> 16), (int)(l2.y & 0xffffu)};
             float4 r[3][kRec];
@@ -909,7 +975,7 @@ __global__ void __launch_bounds__(256) k_patch_mixed_staged(MixedArgs a, StageLa
             smf[18 * emax + j] = o.mm;
             smf[19 * emax + j] = o.acur;
         }
-        __syncthreads();
+        consumer_sync();
         // ---- owned vertices (as k_patch_phase_mixed, state from the stage) ----
         const int32_t* vt_s = reinterpret_cast<const int32_t*>(st + L.o_vt) + h->vt_off;
         const uint16_t* code_s = reinterpret_cast<const uint16_t*>(st + L.o_code) - h->code_base;
@@ -927,7 +993,7 @@ __global__ void __launch_bounds__(256) k_patch_mixed_staged(MixedArgs a, StageLa
         const bool has_rho = h->has_rho;
         const double4* __restrict__ X = c.pos[par];
         const double4* __restrict__ xp = c.pos[par ^ 1];
-        for (int i = threadIdx.x; i < pt.y; i += blockDim.x) {
+        for (int i = threadIdx.x; i < pt.y; i += kConsumers) {
             const int v = pt.x + i;
             float Q0 = 0, Q1 = 0, Q2 = 0, Q3 = 0, MMf = 0, Asf = 0;
             ff R0 = {0.0f, 0.0f}, R1 = {0.0f, 0.0f};   // compensated: the corner forces largely cancel
@@ -960,33 +1026,35 @@ __global__ void __launch_bounds__(256) k_patch_mixed_staged(MixedArgs a, StageLa
                     b[4] = Q1; b[5] = Q2; b[6] = Q3; b[7] = MMf;
                     continue;
                 }
-                boundary_force(c, a, pt, X, xp, v, rank, h->ap_call, F0, F1);   // queue full: finish in place
+                boundary_force(c, h->bc, pt, X, xp, v, rank, F0, F1);   // queue full: finish in place
             }
             const float4 vh = vhi_s[i], vl = vlo_s[i];
             finish_vertex_core(c, a, par, v, F0, F1, Q0, Q1, Q2, Q3, MMf,
                                {vh.x, vh.y, vh.z, vh.w, vl.x, vl.y, vl.z, vl.w}, acc_s[i], eahi_s[i], ealo_s[i]);
         }
-        __syncthreads();
+        consumer_sync();
         const int nq = min(s_nbnd, kBndSlots);
-        for (int j = threadIdx.x; j < nq; j += blockDim.x) {
+        for (int j = threadIdx.x; j < nq; j += kConsumers) {
             const float* b = s_bnd + 8 * j;
             const int i = __float_as_int(b[0]);
             const int v = pt.x + i;
             float F0 = b[1], F1 = b[2];
-            boundary_force(c, a, pt, X, xp, v, rank_s[i], h->ap_call, F0, F1);
+            boundary_force(c, h->bc, pt, X, xp, v, rank_s[i], F0, F1);
             const float4 vh = vhi_s[i], vl = vlo_s[i];
             finish_vertex_core(c, a, par, v, F0, F1, b[3], b[4], b[5], b[6], b[7],
                                {vh.x, vh.y, vh.z, vh.w, vl.x, vl.y, vl.z, vl.w}, acc_s[i], eahi_s[i], ealo_s[i]);
         }
-        __syncthreads();
+        consumer_sync();
         if (threadIdx.x == 0) {
+            const unsigned long long ap_call = h->ap_call;
+            mbar_arrive(empty + s);   // stage s is free (everything it holds has been read)
             __threadfence();
             const unsigned int done = atomicAdd(reinterpret_cast<unsigned int*>(c.ctl + 1), 1u);
             if ((int)done == c.np - 1) {
                 c.ctl[1] = 0;
                 c.ctl[0] = par ^ 1;
                 c.clk[0] = c.clk[0] + a.dt_real;
-                c.ap[0] = h->ap_call + 1ull;
+                c.ap[0] = ap_call + 1ull;
             }
         }
     }
@@ -1048,7 +1116,7 @@ bool launch_patch_staged(const CellDev* cells, const WorkItem* work, int nwork, 
     size_t smem = 0;
     if (!staged_layout(cap_ne, cap_nvp, cap_nh, cap_nc, g_staged_optin, &L, &smem)) return false;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_patch_mixed_staged, 256, smem) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_patch_mixed_staged, kConsumers + 32, smem) !=
             cudaSuccess ||
         per_sm < 1) {
         cudaGetLastError();
@@ -1068,7 +1136,7 @@ bool launch_patch_staged(const CellDev* cells, const WorkItem* work, int nwork, 
     a.t_override = t_override;
     a.vh_from_buf = vh_from_buf;
     const int grid = std::min(nwork, per_sm * num_sms);
-    k_patch_mixed_staged<<<grid, 256, smem, st>>>(a, L);
+    k_patch_mixed_staged<<<grid, kConsumers + 32, smem, st>>>(a, L);
     return true;
 }
 
