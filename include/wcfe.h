@@ -288,6 +288,38 @@ int64_t wcfe_server_step_times(wcfe_server* srv, double* out, int64_t cap);
 int wcfe_area_tot_noalloc(const double* x_dev, int32_t n_vert, const int32_t* tri_dev, int32_t n_tri,
                           double* area4_dev, void* stream);
 
+/* ---- implicit (Newton) step: no counterpart in the reference -------------
+ * Backward Euler of the explicit step's equations of motion (UL:592-628) with the
+ * membrane implicit and the adhesion and boundary forces (A4, A6-A8) taken at the
+ * predicted positions (A1, after the bond kinetics A5):
+ *   G(x) = m (x - X)/dt^2 - m V/dt + (drag + damp m)(x - X)/dt - F_ext + Res(X, x, ea) = 0
+ * in the plane (2N unknowns; planar cells).  Per Newton iteration: G in FP64, the
+ * dense 2N x 2N tangent from FP32 element tangents, its LU factorisation (trailing
+ * updates on the tensor cores, TF32), and the solve refined in FP64 until its
+ * residual is 1e-10 of |G|.  Converged when |G|inf <= newton_rtol * (force scale).
+ * After the step V = (x - X)/dt, A = (V - V_old)/dt, ea += Res_ea/MM.  FP64 engines
+ * only.  Dense factors take 4 (2N)^2 bytes per cell on the device. */
+typedef struct wcfe_newton_stats {
+    int32_t newton_iters;              /* Newton updates summed over steps (all cells together) */
+    int32_t max_refine_iters;          /* largest number of refinement passes of one linear solve */
+    int32_t unconverged;               /* cell-steps that hit max_newton without converging */
+    int32_t pad;
+    double max_rel_residual;           /* largest final |G|inf / force scale */
+    double max_refine_rel_residual;    /* largest final |J dx + G|inf / |G|inf of a linear solve */
+} wcfe_newton_stats;
+
+int wcfe_engine_step_implicit(wcfe_engine* e, int32_t nsteps, double dt, double newton_rtol, int32_t max_newton,
+                              wcfe_newton_stats* stats);
+
+/* Factor the dense m x m matrix A (row-major, FP32, m even) with the implicit step's
+ * LU (no pivoting; TF32 tensor-core trailing updates) and solve A x = b once
+ * (unrefined).  Device 0; for tests of the factorisation itself. */
+int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x);
+
+/* The dense tangent J (2N x 2N, row-major, FP32) of cell `id` at positions x [n][3]
+ * with the cell's state as step start, and the mass/damping diagonal [n]. */
+int wcfe_cell_newton_tangent(wcfe_engine* e, int32_t id, double dt, const double* x, float* J_out, double* diag_out);
+
 /* ---- host-only inspection of the connectivity preprocessing (no device) --- */
 /* Boundary ranks and neighbour candidates (the scan of UL:1500-1531), patches and
  * one-ring slot codes, exactly as the engine builds them.  Capacities in int32 units. */

@@ -22,6 +22,11 @@ _i = C.POINTER(C.c_int32)
 _u8 = C.POINTER(C.c_uint8)
 PREC_FP64, PREC_MIXED = 0, 1
 
+class NewtonStats(C.Structure):
+    _fields_ = [("newton_iters", C.c_int32), ("max_refine_iters", C.c_int32), ("unconverged", C.c_int32),
+                ("pad", C.c_int32), ("max_rel_residual", C.c_double), ("max_refine_rel_residual", C.c_double)]
+
+
 class Request(C.Structure):
     _fields_ = [("n_vert", C.c_int32), ("n_tri", C.c_int32), ("tri", _i), ("x", _d), ("params", C.POINTER(Params)),
                 ("n_steps", C.c_int32), ("sub_tri", _i), ("sub_X", _d), ("sub_n_vert", C.c_int32),
@@ -79,6 +84,9 @@ SIGNATURES = {
     "wcfe_server_result": (C.c_int, [C.c_void_p, C.c_int64, _d, _d]),
     "wcfe_server_step_times": (C.c_int64, [C.c_void_p, _d, C.c_int64]),
     "wcfe_engine_set_patch_kernel": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_engine_step_implicit": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_void_p]),
+    "wcfe_cell_newton_tangent": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _d, C.POINTER(C.c_float), _d]),
+    "wcfe_debug_lu_solve": (C.c_int, [C.c_int32, C.POINTER(C.c_float), _d, C.POINTER(C.c_float)]),
     "wcfe_area_tot_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "wcfe_debug_topology": (C.c_int, [C.c_int32, C.c_int32, _i, _i, _i, _u8, C.c_int32, _i, _i, _i, _i, C.c_int32, _i,
                                       _i, C.c_int32, _i, C.c_int32, C.POINTER(C.c_uint16)]),
@@ -129,6 +137,16 @@ def debug_patch_staging(tri, n_vert, emax=320):
     xinfo = xinfo[:4 * npv].reshape(npv, 4)
     return dict(np=npv, xinfo=xinfo, halo=halo, loc=loc.reshape(-1, 4),
                 max_ne=int(mx[0]), max_nvp=int(mx[1]), max_nh=int(mx[2]), max_nc=int(mx[3]))
+
+
+def debug_lu_solve(A, b):
+    """The implicit step's dense LU (TF32 trailing updates) and one unrefined solve."""
+    A = np.ascontiguousarray(A, np.float32)
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.zeros(len(b), np.float32)
+    check(load().wcfe_debug_lu_solve(len(b), A.ctypes.data_as(C.POINTER(C.c_float)), dp(b),
+                                     x.ctypes.data_as(C.POINTER(C.c_float))), "wcfe_debug_lu_solve")
+    return x
 
 
 class WcfeError(RuntimeError):
@@ -219,6 +237,13 @@ class Engine:
 
     def step(self, nsteps: int, dt: float):
         check(load().wcfe_engine_step(self.h, nsteps, dt), "wcfe_engine_step")
+
+    def step_implicit(self, nsteps: int, dt: float, rtol: float = 1e-10, max_newton: int = 8):
+        """Backward-Euler steps (FP64 engines); returns the Newton statistics."""
+        st = NewtonStats()
+        check(load().wcfe_engine_step_implicit(self.h, nsteps, dt, rtol, max_newton, C.byref(st)),
+              "wcfe_engine_step_implicit")
+        return {k: getattr(st, k) for k, _ in NewtonStats._fields_ if k != "pad"}
 
     def step_cells(self, cells, nsteps: int, dt: float):
         ids = i32([c.id for c in cells])
@@ -350,6 +375,15 @@ class Cell:
         check(load().wcfe_cell_eval_residual(self.eng.h, self.id, dp(f64(X)), dp(f64(x_new)), dt_real, dp(cen), t_tot,
                                              *[dp(a) for a in out]), "wcfe_cell_eval_residual")
         return tuple(out)
+
+    def newton_tangent(self, x, dt):
+        """Dense implicit-step tangent (2n x 2n, FP32) at positions x, and the mass diagonal."""
+        n = self.n
+        J = np.zeros((2 * n, 2 * n), np.float32)
+        d = np.zeros(n)
+        check(load().wcfe_cell_newton_tangent(self.eng.h, self.id, dt, dp(f64(x)),
+                                              J.ctypes.data_as(C.POINTER(C.c_float)), dp(d)), "wcfe_cell_newton_tangent")
+        return J, d
 
     def eval_forces(self, x, dt_real):
         n = self.n

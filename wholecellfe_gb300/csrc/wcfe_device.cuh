@@ -120,6 +120,24 @@ inline ParamF make_paramf(const wcfe_params& p) {
     return f;
 }
 
+// Newton work of one cell (implicit step, wcfe_newton.cu); device array, one entry per cell
+struct NewtonCell {
+    float* J;            // dense 2n x 2n tangent, row-major, leading dimension ld (FP32); LU factors in place
+    float* Ke;           // [nt][36] element tangents: (2 k + i) * 6 + 2 l + j = d re[k][i] / d u[l][j]
+    double* diag;        // [n] mass and damping diagonal m / dt^2 + (drag + damp m) / dt
+    double* G;           // [2n] Newton residual
+    double* dx;          // [2n] Newton correction
+    double* d;           // [2n] the iterate as displacement x - X (keeps the inertia term free of the
+                         //      rounding of x: m / dt^2 times ulp(x) would floor |G|)
+    double* r;           // [2n] residual of the linear solve
+    float* z;            // [2n] FP32 solve workspace
+    const double* Fext;  // [3n] external forces at the predicted positions
+    const double* Res;   // [3n] membrane residual at the iterate
+    const double* MM;    // [n] lumped mass
+    double* norms;       // [4]: |G|inf, force scale, |r|inf, non-finite or zero pivot flag
+    int n, ld, active, pad;
+};
+
 struct WorkItem {               // one block of a phase: (cell index into the table, block/patch index)
     int32_t cell, idx;
 };

@@ -36,7 +36,25 @@ void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, 
                          int threads, cudaStream_t st, const double* stage_in, double* stage_out);
 void launch_patch(int prec, int mode, const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt,
                   double dt_real, double ap_thresh, double t_override, int vh_from_buf, const double* centroid_dev,
-                  double* o0, double* o1, double* o2, double* o3, double* o4, int threads, int grid, cudaStream_t st);
+                  double* o0, double* o1, double* o2, double* o3, double* o4, int threads, int grid, cudaStream_t st,
+                  int packed = 0);
+cudaError_t configure_newton(size_t max_smem, int num_sms);
+size_t newton_tangent_smem(int emax);
+void launch_newton_residual(const CellDev* cells, const NewtonCell* nc, const int* cell_of_slot, int nslots, int max_n,
+                            double dt, cudaStream_t st);
+void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int* cell_slot, const WorkItem* work,
+                           int nwork, int emax, double dt, cudaStream_t st);
+void launch_newton_lu(NewtonCell* nc, int nslots, int max_m, cudaStream_t st);
+void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, cudaStream_t st);
+void launch_newton_refine(const CellDev* cells, NewtonCell* nc, const int* cell_slot, const WorkItem* work, int nwork,
+                          int add_z, cudaStream_t st);
+void launch_newton_accumulate(NewtonCell* nc, int nslots, int max_n, cudaStream_t st);
+void launch_newton_apply(const CellDev* cells, NewtonCell* nc, const int* cell_of_slot, int nslots, int max_n, int init,
+                         cudaStream_t st);
+void launch_newton_finish(const CellDev* cells, NewtonCell* nc, const int* cell_of_slot, int nslots, int max_n,
+                          const double* res_ea, double dt, unsigned int* tickets, cudaStream_t st);
+void launch_sum4(const double* a, const double* b, const double* c, const double* d, double* o, size_t n,
+                 cudaStream_t st);
 }  // namespace wcfe
 
 using namespace wcfe;
@@ -680,6 +698,7 @@ int wcfe_engine_create(int32_t device, int32_t precision, uint64_t hbm_budget_by
     int max_optin = 0;
     CK(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
     CK(configure_kernels((size_t)max_optin));
+    CK(configure_newton((size_t)max_optin, e->num_sms > 0 ? e->num_sms : 1));
     for (auto& ev : e->ev) CK(cudaEventCreate(&ev));
     if (precision == WCFE_PREC_MIXED) { e->patch_threads = 128; e->patch_emax = 512; e->vblock = 256; }
     else { e->patch_threads = 64; e->patch_emax = 96; e->vblock = 64; }  // FP64: more, smaller blocks
@@ -1354,6 +1373,332 @@ int wcfe_engine_update(wcfe_engine* e, double dt, double dt_real, const double* 
                std::numeric_limits<double>::quiet_NaN(), 1);
     e->launches += 2;
     CK(cudaGetLastError());
+    return WCFE_OK;
+}
+
+// ---------------------------------------------------------------------------- implicit (Newton) step
+namespace {
+struct NewtonPlan {
+    void* block = nullptr;
+    size_t bytes = 0;
+    std::vector<NewtonCell> cells;   // host copy
+    NewtonCell* d_cells = nullptr;
+    int* d_ident = nullptr;          // slot s <-> table index s
+    unsigned int* d_tickets = nullptr;
+    double* norms = nullptr;         // [nslots][4]
+    double *res = nullptr, *rea = nullptr, *mm = nullptr, *f4 = nullptr, *fext = nullptr;
+    int max_n = 0;
+};
+
+size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// one device block for every cell of the table: packed residual and force arrays, per cell
+// J, element tangents and vectors
+int newton_plan(wcfe_engine* e, NewtonPlan& P) {
+    const int ns = (int)e->order.size();
+    const size_t NV = (size_t)e->total_nv;
+    size_t o = 0;
+    auto put = [&](size_t bytes) { const size_t at = o; o = al256(o + bytes); return at; };
+    const size_t o_res = put(sizeof(double) * 3 * NV), o_rea = put(sizeof(double) * 6 * NV), o_mm = put(sizeof(double) * NV);
+    const size_t o_f4 = put(sizeof(double) * 12 * NV), o_fext = put(sizeof(double) * 3 * NV);
+    const size_t o_norm = put(sizeof(double) * 4 * ns), o_nc = put(sizeof(NewtonCell) * ns);
+    const size_t o_id = put(sizeof(int) * ns), o_tk = put(sizeof(unsigned int) * ns);
+    struct Off { size_t J, Ke, diag, G, dx, d, r, z; int n, ld; };
+    std::vector<Off> off(ns);
+    P.max_n = 0;
+    for (int sl = 0; sl < ns; ++sl) {
+        const Cell* c = e->cells.at(e->order[sl]).get();
+        const int n = c->topo.nv, m = 2 * n, ld = (m + 3) & ~3;
+        Off& f = off[sl];
+        f.n = n;
+        f.ld = ld;
+        f.J = put(sizeof(float) * (size_t)m * ld);
+        f.Ke = put(sizeof(float) * 36 * (size_t)c->topo.nt);
+        f.diag = put(sizeof(double) * n);
+        f.G = put(sizeof(double) * m);
+        f.dx = put(sizeof(double) * m);
+        f.d = put(sizeof(double) * m);
+        f.r = put(sizeof(double) * m);
+        f.z = put(sizeof(float) * m);
+        P.max_n = std::max(P.max_n, n);
+    }
+    int r = dev_alloc(e, &P.block, o);
+    if (r) return r;
+    P.bytes = o;
+    char* b = (char*)P.block;
+    CK(cudaMemsetAsync(b, 0, o, e->stream));
+    P.res = (double*)(b + o_res);
+    P.rea = (double*)(b + o_rea);
+    P.mm = (double*)(b + o_mm);
+    P.f4 = (double*)(b + o_f4);
+    P.fext = (double*)(b + o_fext);
+    P.norms = (double*)(b + o_norm);
+    P.d_cells = (NewtonCell*)(b + o_nc);
+    P.d_ident = (int*)(b + o_id);
+    P.d_tickets = (unsigned int*)(b + o_tk);
+    P.cells.resize(ns);
+    std::vector<int> ident(ns);
+    for (int sl = 0; sl < ns; ++sl) {
+        const Cell* c = e->cells.at(e->order[sl]).get();
+        const size_t h = (size_t)c->dev.hoff;
+        const Off& f = off[sl];
+        NewtonCell& N = P.cells[sl];
+        N.J = (float*)(b + f.J);
+        N.Ke = (float*)(b + f.Ke);
+        N.diag = (double*)(b + f.diag);
+        N.G = (double*)(b + f.G);
+        N.dx = (double*)(b + f.dx);
+        N.d = (double*)(b + f.d);
+        N.r = (double*)(b + f.r);
+        N.z = (float*)(b + f.z);
+        N.Fext = P.fext + 3 * h;
+        N.Res = P.res + 3 * h;
+        N.MM = P.mm + h;
+        N.norms = P.norms + 4 * (size_t)sl;
+        N.n = f.n;
+        N.ld = f.ld;
+        N.active = 1;
+        N.pad = 0;
+        ident[sl] = sl;
+    }
+    CK(cudaMemcpyAsync(P.d_ident, ident.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync(P.d_cells, P.cells.data(), sizeof(NewtonCell) * ns, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+void newton_free(wcfe_engine* e, NewtonPlan& P) {
+    if (P.block) {
+        cudaStreamSynchronize(e->stream);
+        dev_free(e, P.block, P.bytes);
+    }
+}
+
+int newton_upload_active(wcfe_engine* e, NewtonPlan& P) {
+    CK(cudaMemcpyAsync(P.d_cells, P.cells.data(), sizeof(NewtonCell) * P.cells.size(), cudaMemcpyHostToDevice,
+                       e->stream));
+    return WCFE_OK;
+}
+
+int newton_read_norms(wcfe_engine* e, NewtonPlan& P, std::vector<double>& h) {
+    h.resize(4 * P.cells.size());
+    CK(cudaMemcpyAsync(h.data(), P.norms, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+// the FP64 membrane residual, lumped mass and strain residual at the iterate (packed arrays)
+void newton_membrane(wcfe_engine* e, NewtonPlan& P, double dt) {
+    const int n2 = (int)e->k2.size();
+    const size_t smem = patch_smem_bytes(WCFE_PREC_FP64, PP_RESIDUAL, e->patch_emax);
+    launch_patch(WCFE_PREC_FP64, PP_RESIDUAL, e->d_table, e->d_k2, n2, e->patch_emax, dt, dt, 0.0,
+                 std::numeric_limits<double>::quiet_NaN(), 0, nullptr, P.res, P.rea, P.mm, nullptr, nullptr,
+                 e->patch_threads, grid_for(e, n2, patch_occupancy(WCFE_PREC_FP64, e->patch_threads, smem)), e->stream, 1);
+}
+
+int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_newton, wcfe_newton_stats* st) {
+    const int ns = (int)P.cells.size();
+    const int n1 = (int)e->k1.size(), n2 = (int)e->k2.size();
+    const size_t NV = (size_t)e->total_nv;
+    std::vector<double> hn;
+    // A1 + A5: predicted positions, bond kinetics, area and centroid of the predicted positions
+    vphase(e, e->d_table, e->d_k1, n1, dt, VP_PREDICT | VP_UPDATE_FA, grid_for(e, n1, vertex_occupancy(e->vblock)),
+           e->stream);
+    // external forces at the predicted positions
+    {
+        const size_t smem = patch_smem_bytes(WCFE_PREC_FP64, PP_FORCES, e->patch_emax);
+        launch_patch(WCFE_PREC_FP64, PP_FORCES, e->d_table, e->d_k2, n2, e->patch_emax, dt, dt,
+                     std::numeric_limits<double>::quiet_NaN(), std::numeric_limits<double>::quiet_NaN(), 0, nullptr,
+                     P.f4, P.f4 + 3 * NV, P.f4 + 6 * NV, P.f4 + 9 * NV, nullptr, e->patch_threads,
+                     grid_for(e, n2, patch_occupancy(WCFE_PREC_FP64, e->patch_threads, smem)), e->stream, 1);
+        launch_sum4(P.f4, P.f4 + 3 * NV, P.f4 + 6 * NV, P.f4 + 9 * NV, P.fext, 3 * NV, e->stream);
+    }
+    for (auto& N : P.cells) N.active = 1;
+    int r = newton_upload_active(e, P);
+    if (r) return r;
+    launch_newton_apply(e->d_table, P.d_cells, P.d_ident, ns, P.max_n, 1, e->stream);   // d = x_pred - X
+    e->launches += 3;
+    for (int it = 0;; ++it) {
+        newton_membrane(e, P, dt);
+        CK(cudaMemsetAsync(P.norms, 0, sizeof(double) * 4 * ns, e->stream));
+        launch_newton_residual(e->d_table, P.d_cells, P.d_ident, ns, P.max_n, dt, e->stream);
+        e->launches += 2;
+        if ((r = newton_read_norms(e, P, hn))) return r;
+        int nact = 0;
+        for (int sl = 0; sl < ns; ++sl) {
+            const double g = hn[4 * sl], f = std::max(hn[4 * sl + 1], 1e-300);
+            const bool bad = !std::isfinite(g) || hn[4 * sl + 3] != 0.0;
+            const bool conv = g <= rtol * f;
+            P.cells[sl].active = (!bad && !conv && it < max_newton) ? 1 : 0;
+            nact += P.cells[sl].active;
+            if (!P.cells[sl].active) {   // final for this step
+                if (st) {
+                    st->max_rel_residual = std::max(st->max_rel_residual, std::isfinite(g) ? g / f : INFINITY);
+                    if (!conv) st->unconverged += 1;
+                }
+                if (bad) {   // non-finite residual or zero pivot: flag the cell (status bit 16)
+                    Cell* c = e->cells.at(e->order[sl]).get();
+                    uint32_t s0 = 0;
+                    CK(cudaMemcpyAsync(&s0, c->dev.status, sizeof s0, cudaMemcpyDeviceToHost, e->stream));
+                    CK(cudaStreamSynchronize(e->stream));
+                    s0 |= 16u;
+                    CK(cudaMemcpyAsync(c->dev.status, &s0, sizeof s0, cudaMemcpyHostToDevice, e->stream));
+                }
+            }
+        }
+        if (!nact) break;
+        if ((r = newton_upload_active(e, P))) return r;
+        if (st) st->newton_iters += 1;
+        // tangent, LU
+        for (const auto& N : P.cells)
+            if (N.active) CK(cudaMemsetAsync(N.J, 0, sizeof(float) * 2 * (size_t)N.n * N.ld, e->stream));
+        launch_newton_tangent(e->d_table, P.d_cells, P.d_ident, e->d_k2, n2, e->patch_emax, dt, e->stream);
+        launch_newton_lu(P.d_cells, ns, 2 * P.max_n, e->stream);
+        // J dx = -G, refined in FP64
+        for (const auto& N : P.cells)
+            if (N.active) {
+                CK(cudaMemsetAsync(N.dx, 0, sizeof(double) * 2 * (size_t)N.n, e->stream));
+                CK(cudaMemsetAsync(N.z, 0, sizeof(float) * 2 * (size_t)N.n, e->stream));
+            }
+        launch_newton_refine(e->d_table, P.d_cells, P.d_ident, e->d_k2, n2, 0, e->stream);
+        int q = 0;
+        double final_ratio = 0.0;
+        for (; q < 16; ++q) {
+            launch_newton_solve(P.d_cells, ns, P.max_n, e->stream);
+            CK(cudaMemsetAsync(P.norms, 0, sizeof(double) * 4 * ns, e->stream));   // G's norm is kept on the host
+            launch_newton_refine(e->d_table, P.d_cells, P.d_ident, e->d_k2, n2, 1, e->stream);
+            launch_newton_accumulate(P.d_cells, ns, P.max_n, e->stream);
+            e->launches += 3;
+            std::vector<double> hr;
+            if ((r = newton_read_norms(e, P, hr))) return r;
+            bool done = true;
+            final_ratio = 0.0;
+            for (int sl = 0; sl < ns; ++sl) {
+                if (!P.cells[sl].active) continue;
+                const double ratio = hr[4 * sl + 2] / std::max(hn[4 * sl], 1e-300);
+                if (!(ratio <= 1e-10)) done = false;
+                final_ratio = std::max(final_ratio, ratio);
+            }
+            if (done) break;
+        }
+        if (st) {
+            st->max_refine_iters = std::max(st->max_refine_iters, q + 1);
+            st->max_refine_rel_residual = std::max(st->max_refine_rel_residual, final_ratio);
+        }
+        launch_newton_apply(e->d_table, P.d_cells, P.d_ident, ns, P.max_n, 0, e->stream);
+        e->launches += 4 + 3 * ((2 * P.max_n + 63) / 64);
+        CK(cudaGetLastError());
+    }
+    // finish at the converged x: strain residual, V, A, ea; advance parity, clock, AP counter
+    newton_membrane(e, P, dt);
+    launch_newton_finish(e->d_table, P.d_cells, P.d_ident, ns, P.max_n, P.rea, dt, P.d_tickets, e->stream);
+    e->launches += 2;
+    CK(cudaGetLastError());
+    return WCFE_OK;
+}
+}  // namespace
+
+int wcfe_engine_step_implicit(wcfe_engine* e, int32_t nsteps, double dt, double newton_rtol, int32_t max_newton,
+                              wcfe_newton_stats* stats) {
+    if (!e || nsteps < 0 || !(dt > 0) || !(newton_rtol > 0) || max_newton < 1) return fail("bad argument", WCFE_ERR_ARG);
+    if (e->prec != WCFE_PREC_FP64)
+        return fail("the implicit step runs on an FP64 engine (WCFE_PREC_FP64)", WCFE_ERR_STATE);
+    if (stats) std::memset(stats, 0, sizeof *stats);
+    if (e->cells.empty() || nsteps == 0) return WCFE_OK;
+    CK(cudaSetDevice(e->device));
+    int r = sync_tables(e, dt);
+    if (r) return r;
+    NewtonPlan P;
+    if ((r = newton_plan(e, P))) return r;
+    for (int s = 0; s < nsteps && !r; ++s) r = newton_step(e, P, dt, newton_rtol, max_newton, stats);
+    if (!r) {
+        cudaError_t ce = cudaStreamSynchronize(e->stream);
+        if (ce != cudaSuccess) r = fail(std::string("CUDA: ") + cudaGetErrorString(ce), WCFE_ERR_CUDA);
+    }
+    newton_free(e, P);
+    return r;
+}
+
+int wcfe_cell_newton_tangent(wcfe_engine* e, int32_t id, double dt, const double* x, float* J_out, double* diag_out) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c || !x || !J_out || !(dt > 0)) return fail("bad argument", WCFE_ERR_ARG);
+    if (e->prec != WCFE_PREC_FP64)
+        return fail("the implicit step runs on an FP64 engine (WCFE_PREC_FP64)", WCFE_ERR_STATE);
+    CK(cudaSetDevice(e->device));
+    int r = sync_tables(e, dt);
+    if (r) return r;
+    int par;
+    if ((r = read_parity(e, c, &par))) return r;
+    const int n = c->topo.nv;
+    if ((r = put3(e, c->dev.pos[par ^ 1], x, n))) return r;
+    NewtonPlan P;
+    if ((r = newton_plan(e, P))) return r;
+    const int ti = table_index(e, id);
+    int n1, n2;
+    if ((r = one_cell_lists(e, c, ti, &n1, &n2)) == 0) {
+        // area and centroid of x, then the lumped mass, then J
+        launch_vertex_phase(e->d_table, e->d_one, n1, dt, 0, grid_for(e, n1, vertex_occupancy(e->vblock)), e->vblock,
+                            e->stream);
+        const size_t smem = patch_smem_bytes(WCFE_PREC_FP64, PP_RESIDUAL, e->patch_emax);
+        launch_patch(WCFE_PREC_FP64, PP_RESIDUAL, e->d_table, e->d_one + n1, n2, e->patch_emax, dt, dt, 0.0,
+                     std::numeric_limits<double>::quiet_NaN(), 0, nullptr, P.res, P.rea, P.mm, nullptr, nullptr,
+                     e->patch_threads, grid_for(e, n2, patch_occupancy(WCFE_PREC_FP64, e->patch_threads, smem)),
+                     e->stream, 1);
+        launch_newton_tangent(e->d_table, P.d_cells, P.d_ident, e->d_one + n1, n2, e->patch_emax, dt, e->stream);
+        const NewtonCell& N = P.cells[ti];
+        CK(cudaMemcpy2DAsync(J_out, sizeof(float) * 2 * n, N.J, sizeof(float) * N.ld, sizeof(float) * 2 * n, 2 * n,
+                             cudaMemcpyDeviceToHost, e->stream));
+        if (diag_out) CK(cudaMemcpyAsync(diag_out, N.diag, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+        CK(cudaStreamSynchronize(e->stream));
+        e->launches += 3;
+    }
+    newton_free(e, P);
+    return r;
+}
+
+int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x) {
+    if (m <= 0 || (m & 1) || !A || !b || !x) return fail("bad argument", WCFE_ERR_ARG);
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        cudaGetLastError();
+        return fail("no CUDA device", WCFE_ERR_NODEVICE);
+    }
+    int max_optin = 0, sms = 0;
+    CK(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0));
+    CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
+    CK(configure_newton((size_t)max_optin, sms));
+    const int ld = (m + 3) & ~3;
+    const size_t bytes = sizeof(float) * (size_t)m * ld + sizeof(double) * m + sizeof(float) * m +
+                         sizeof(double) * 4 + sizeof(NewtonCell) + 1024;
+    char* blk = nullptr;
+    CK(cudaMalloc(&blk, bytes));
+    size_t o = 0;
+    auto take = [&](size_t n) { char* p = blk + o; o = (o + n + 255) & ~(size_t)255; return p; };
+    NewtonCell N{};
+    N.J = (float*)take(sizeof(float) * (size_t)m * ld);
+    N.r = (double*)take(sizeof(double) * m);
+    N.z = (float*)take(sizeof(float) * m);
+    N.norms = (double*)take(sizeof(double) * 4);
+    N.n = m / 2;
+    N.ld = ld;
+    N.active = 1;
+    NewtonCell* d_nc = (NewtonCell*)take(sizeof(NewtonCell));
+    cudaError_t ce = cudaMemcpy2D(N.J, sizeof(float) * ld, A, sizeof(float) * m, sizeof(float) * m, m,
+                                  cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemcpy(N.r, b, sizeof(double) * m, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) ce = cudaMemset(N.norms, 0, sizeof(double) * 4);
+    if (ce == cudaSuccess) ce = cudaMemcpy(d_nc, &N, sizeof N, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) {
+        launch_newton_lu(d_nc, 1, m, 0);
+        launch_newton_solve(d_nc, 1, m / 2, 0);
+        ce = cudaDeviceSynchronize();
+    }
+    double flag = 0;
+    if (ce == cudaSuccess) ce = cudaMemcpy(x, N.z, sizeof(float) * m, cudaMemcpyDeviceToHost);
+    if (ce == cudaSuccess) ce = cudaMemcpy(&flag, N.norms + 3, sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(blk);
+    if (ce != cudaSuccess) return fail(std::string("CUDA: ") + cudaGetErrorString(ce), WCFE_ERR_CUDA);
+    if (flag != 0.0) return fail("zero or non-finite pivot", WCFE_ERR_STATE);
     return WCFE_OK;
 }
 

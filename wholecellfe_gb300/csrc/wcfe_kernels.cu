@@ -361,6 +361,7 @@ struct PatchArgs {
     double* out2;
     double* out3;
     double* out4;
+    int packed;                       // 1: outputs indexed by the cell's offset in the packed arrays (hoff + v)
 };
 
 constexpr int kSlot64 = 29;  // re 9, rea 18, mm, acur
@@ -445,12 +446,13 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
                 Asum += s_ac[sl] / 3;
                 if (MODE == PP_RESIDUAL) { dA += s_dA[sl * 3 + cn]; dC += s_dC[sl * 3 + cn]; }
             }
+            const size_t ov = a.packed ? (size_t)c.hoff + v : (size_t)v;   // output row
             if (MODE == PP_RESIDUAL) {
-                if (a.out0) for (int r = 0; r < 3; ++r) a.out0[3 * (size_t)v + r] = R[r];
-                if (a.out1) for (int q = 0; q < 6; ++q) a.out1[6 * (size_t)v + q] = Rq[q];
-                if (a.out2) a.out2[v] = MM;
-                if (a.out3) a.out3[v] = dA;
-                if (a.out4) a.out4[v] = dC;
+                if (a.out0) for (int r = 0; r < 3; ++r) a.out0[3 * ov + r] = R[r];
+                if (a.out1) for (int q = 0; q < 6; ++q) a.out1[6 * ov + q] = Rq[q];
+                if (a.out2) a.out2[ov] = MM;
+                if (a.out3) a.out3[ov] = dA;
+                if (a.out4) a.out4[ov] = dC;
                 continue;
             }
             const double4 xv4 = ld4v(xp + v);
@@ -504,10 +506,10 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
             }
             if (MODE == PP_FORCES) {
                 for (int r = 0; r < 3; ++r) {
-                    if (a.out0) a.out0[3 * (size_t)v + r] = Ffa[r];
-                    if (a.out1) a.out1[3 * (size_t)v + r] = Fap[r];
-                    if (a.out2) a.out2[3 * (size_t)v + r] = Fb[r];
-                    if (a.out3) a.out3[3 * (size_t)v + r] = Far[r];
+                    if (a.out0) a.out0[3 * ov + r] = Ffa[r];
+                    if (a.out1) a.out1[3 * ov + r] = Fap[r];
+                    if (a.out2) a.out2[3 * ov + r] = Fb[r];
+                    if (a.out3) a.out3[3 * ov + r] = Far[r];
                 }
                 continue;
             }
@@ -627,7 +629,8 @@ int vertex_occupancy(int threads) {
 
 void launch_patch(int prec, int mode, const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt,
                   double dt_real, double ap_thresh, double t_override, int vh_from_buf, const double* centroid_dev,
-                  double* o0, double* o1, double* o2, double* o3, double* o4, int threads, int grid, cudaStream_t st) {
+                  double* o0, double* o1, double* o2, double* o3, double* o4, int threads, int grid, cudaStream_t st,
+                  int packed) {
     if (nwork <= 0) return;
     if (prec == WCFE_PREC_MIXED && mode == PP_STEP) {
         launch_patch_mixed(cells, work, nwork, emax, dt, dt_real, ap_thresh, t_override, vh_from_buf, threads, grid, st);
@@ -646,6 +649,7 @@ void launch_patch(int prec, int mode, const CellDev* cells, const WorkItem* work
     a.vh_from_buf = vh_from_buf;
     a.centroid_override = centroid_dev;
     a.out0 = o0; a.out1 = o1; a.out2 = o2; a.out3 = o3; a.out4 = o4;
+    a.packed = packed;
     size_t smem = patch_smem_bytes(WCFE_PREC_FP64, mode, emax);
     if (mode == PP_STEP) k_patch_phase_fp64<PP_STEP><<<grid, threads, smem, st>>>(a);
     else if (mode == PP_RESIDUAL) k_patch_phase_fp64<PP_RESIDUAL><<<grid, threads, smem, st>>>(a);

@@ -1,0 +1,788 @@
+// wcfe_newton.cu — implicit (Newton) step of the membrane on FP64 engines.
+//
+// There is no counterpart in the reference, which integrates explicitly
+// (UL:889).  The step is backward Euler of the same equations of motion the
+// explicit step integrates (UL:592-628), with the membrane implicit and the
+// adhesion and boundary forces evaluated at the predicted positions:
+//
+//   G(x) = m (x - X) / dt^2 - m V / dt + (drag + damp m)(x - X) / dt - F_ext + Res(X, x, ea) = 0
+//   J(x) = diag(m / dt^2 + (drag + damp m) / dt) + dRes/dx          (in-plane, 2N x 2N)
+//
+// with m = MM rho the lumped mass, F_ext = F_FA + F_AP + F_bend + F_area at the
+// predicted positions and Res the FP64 membrane residual (calculateRes,
+// UL:632-707).  Per Newton iteration: the FP64 residual G, the FP32 element
+// tangents (forward-mode derivatives of the planar increment-form element, six
+// directions at once), a dense FP32 J assembled row by row in one-ring order
+// (deterministic), its LU factorisation with the trailing updates on the tensor
+// cores in TF32, and the solve J d = -G refined in FP64 against the sparse
+// element-by-element J until the correction's residual is 1e-10 of |G|.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+
+#include "wcfe_common.cuh"
+
+namespace wcfe {
+
+// ===========================================================================
+// forward-mode derivatives: value + ND directional derivatives
+// ===========================================================================
+template <int ND>
+struct Dual {
+    float v;
+    float d[ND];
+};
+template <int ND>
+__device__ __forceinline__ Dual<ND> dconst(float a) {
+    Dual<ND> r;
+    r.v = a;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) r.d[i] = 0.0f;
+    return r;
+}
+template <int ND>
+__device__ __forceinline__ Dual<ND> operator+(const Dual<ND>& a, const Dual<ND>& b) {
+    Dual<ND> r;
+    r.v = a.v + b.v;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] + b.d[i];
+    return r;
+}
+template <int ND>
+__device__ __forceinline__ Dual<ND> operator-(const Dual<ND>& a, const Dual<ND>& b) {
+    Dual<ND> r;
+    r.v = a.v - b.v;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] - b.d[i];
+    return r;
+}
+template <int ND>
+__device__ __forceinline__ Dual<ND> operator-(const Dual<ND>& a) {
+    Dual<ND> r;
+    r.v = -a.v;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) r.d[i] = -a.d[i];
+    return r;
+}
+template <int ND>
+__device__ __forceinline__ Dual<ND> operator*(const Dual<ND>& a, const Dual<ND>& b) {
+    Dual<ND> r;
+    r.v = a.v * b.v;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] * b.v + a.v * b.d[i];
+    return r;
+}
+template <int ND>
+__device__ __forceinline__ Dual<ND> operator*(const Dual<ND>& a, float b) {
+    Dual<ND> r;
+    r.v = a.v * b;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] * b;
+    return r;
+}
+template <int ND>
+__device__ __forceinline__ Dual<ND> operator*(float b, const Dual<ND>& a) { return a * b; }
+template <int ND>
+__device__ __forceinline__ Dual<ND> operator+(const Dual<ND>& a, float b) {
+    Dual<ND> r = a;
+    r.v += b;
+    return r;
+}
+template <int ND>
+__device__ __forceinline__ Dual<ND> operator+(float b, const Dual<ND>& a) { return a + b; }
+template <int ND>
+__device__ __forceinline__ Dual<ND> operator-(const Dual<ND>& a, float b) {
+    Dual<ND> r = a;
+    r.v -= b;
+    return r;
+}
+template <int ND>
+__device__ __forceinline__ Dual<ND> operator-(float b, const Dual<ND>& a) {
+    Dual<ND> r;
+    r.v = b - a.v;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) r.d[i] = -a.d[i];
+    return r;
+}
+template <int ND>
+__device__ __forceinline__ Dual<ND> inv(const Dual<ND>& a) {   // 1 / a
+    Dual<ND> r;
+    r.v = 1.0f / a.v;
+    const float s = -r.v * r.v;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] * s;
+    return r;
+}
+template <int ND>
+__device__ __forceinline__ Dual<ND> rsqrt(const Dual<ND>& a) {   // a^-1/2
+    Dual<ND> r;
+    r.v = rsqrtf(a.v);
+    const float s = -0.5f * r.v / a.v;
+#pragma unroll
+    for (int i = 0; i < ND; ++i) r.d[i] = a.d[i] * s;
+    return r;
+}
+__device__ __forceinline__ float inv(float a) { return 1.0f / a; }
+__device__ __forceinline__ float rsqrt(float a) { return rsqrtf(a); }
+
+struct TanParams {   // per-cell constants of the planar element
+    float mu, thick, grow, s_iso, t_an;
+};
+
+// In-plane element residual of the planar increment form (the re part of the mixed
+// form's element; UL:710-928 restated with F = I + H):
+//   G1, G2 reference edges; d1, d2 the edge increments of the displacement x - X;
+//   e = strain (xx, yy, xy, zz) at the integration point; (ax, ay) the element
+//   centroid minus the cell centroid (direction of the anisotropic active stress).
+template <class T>
+__device__ __forceinline__ void element_re_planar(float G1x, float G1y, float G2x, float G2y, const T& d1x,
+                                                  const T& d1y, const T& d2x, const T& d2y, const float e[4],
+                                                  const T& ax_in, const T& ay_in, const TanParams& q, T re[3][2]) {
+    const float Gc = G1x * G2y - G1y * G2x;
+    const float iG = 1.0f / Gc;
+    const float b1x = G2y * iG, b1y = -G2x * iG;
+    const float b2x = -G1y * iG, b2y = G1x * iG;
+    const float b0x = -b1x - b2x, b0y = -b1y - b2y;
+    const T H00 = d1x * b1x + d2x * b2x, H01 = d1x * b1y + d2x * b2y;
+    const T H10 = d1y * b1x + d2y * b2x, H11 = d1y * b1y + d2y * b2y;
+    const float exx = e[0], eyy = e[1], exy = e[2], ezz = e[3];
+    const float m00 = 1.0f - 2.0f * exx, m11 = 1.0f - 2.0f * eyy, m01 = -2.0f * exy;
+    const float dm1 = -2.0f * (exx + eyy) + 4.0f * (exx * eyy - exy * exy);
+    const float idM = 1.0f / (1.0f + dm1);
+    const float i00 = m11 * idM, i01 = -m01 * idM, i11 = m00 * idM;
+    const float be00 = 2.0f * (exx * i00 + exy * i01), be01 = 2.0f * (exx * i01 + exy * i11);
+    const float be11 = 2.0f * (exy * i01 + eyy * i11);
+    const float de = dm1 - 2.0f * ezz * (1.0f + dm1);
+    const T c00 = 2.0f * H00 + (H00 * H00 + H10 * H10);
+    const T c11 = 2.0f * H11 + (H01 * H01 + H11 * H11);
+    const T c01 = H01 + H10 + (H00 * H01 + H10 * H11);
+    const T dC = (1.0f + c00) * (1.0f + c11) - c01 * c01;
+    const T iC = inv(dC);
+    const T ci00 = (1.0f + c11) * iC, ci01 = -c01 * iC, ci11 = (1.0f + c00) * iC;
+    const T ga00 = -(c00 * ci00 + c01 * ci01), ga01 = -(c00 * ci01 + c01 * ci11);
+    const T ga11 = -(c01 * ci01 + c11 * ci11);
+    const T dth = (H00 + H11) + (H00 * H11 - H01 * H10);
+    const float g = q.grow, thg = 1.0f + g, gg2 = 2.0f * g + g * g;
+    const T one_dth = 1.0f + dth;
+    const T eta = (gg2 + thg * thg * de - 2.0f * dth - dth * dth) * inv(one_dth * one_dth);
+    const T c0 = -(gg2 + thg * thg * eta) * (1.0f / thg);
+    const float ith = 1.0f / thg;
+    const T tge = thg * (1.0f + eta);
+    T S00 = q.mu * (c0 + be00 * ith - tge * ga00);
+    T S01 = q.mu * (be01 * ith - tge * ga01);
+    T S11 = q.mu * (c0 + be11 * ith - tge * ga11);
+    if (q.t_an != 0.0f) {
+        const T ia = rsqrt(ax_in * ax_in + ay_in * ay_in);
+        const T ax = ax_in * ia, ay = ay_in * ia;
+        S00 = S00 + q.t_an * (ax * ax);
+        S01 = S01 + q.t_an * (ax * ay);
+        S11 = S11 + q.t_an * (ay * ay);
+    }
+    const T T00 = q.s_iso * H00 + S00 + (H00 * S00 + H01 * S01);
+    const T T01 = q.s_iso * H01 + S01 + (H00 * S01 + H01 * S11);
+    const T T10 = q.s_iso * H10 + S01 + (H10 * S00 + H11 * S01);
+    const T T11 = q.s_iso * H11 + S11 + (H10 * S01 + H11 * S11);
+    const float wA = 0.5f * Gc * q.thick;
+    re[0][0] = wA * (T00 * b0x + T01 * b0y); re[0][1] = wA * (T10 * b0x + T11 * b0y);
+    re[1][0] = wA * (T00 * b1x + T01 * b1y); re[1][1] = wA * (T10 * b1x + T11 * b1y);
+    re[2][0] = wA * (T00 * b2x + T01 * b2y); re[2][1] = wA * (T10 * b2x + T11 * b2y);
+}
+
+// element tangents and dense assembly, one CTA per patch of a cell (work list of
+// the patch phase); elements computed once per patch into shared memory
+constexpr int kTanThreads = 128;
+
+__global__ void __launch_bounds__(kTanThreads) k_newton_tangent(const CellDev* __restrict__ cells,
+                                                               const NewtonCell* __restrict__ nc,
+                                                               const int* __restrict__ cell_slot,
+                                                               const WorkItem* __restrict__ work, int nwork, int emax,
+                                                               double dt) {
+    extern __shared__ float ke_s[];   // [emax][36]
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const WorkItem it = work[w];
+        const int slot = cell_slot[it.cell];
+        if (slot < 0) continue;
+        const NewtonCell& N = nc[slot];
+        if (!N.active) continue;
+        const CellDev& c = cells[it.cell];
+        const wcfe_params& p = c.prm;
+        const int4 pt = c.patch[it.idx];
+        const int par = c.ctl[0];
+        const double4* __restrict__ X = c.pos[par];
+        const double4* __restrict__ xp = c.pos[par ^ 1];
+        const double* __restrict__ ea = c.ea[par];
+        const double t = c.clk[0];
+        const double t_act = t < p.tact_t1 ? t * p.tact_rate : p.tact_max;
+        TanParams q;
+        q.mu = (float)p.mu;
+        q.thick = (float)p.thick;
+        q.grow = (float)(p.thetag_dot * dt);
+        q.s_iso = (float)(p.kappa * t_act);
+        q.t_an = (float)((1.0 - 2.0 * p.kappa) * t_act);
+        const double cx = c.area4[1], cy = c.area4[2];
+        for (int j = threadIdx.x; j < pt.w; j += blockDim.x) {
+            const int e = c.patch_elems[pt.z + j];
+            const int4 t4 = c.tri[e];
+            const int id[3] = {t4.x, t4.y, t4.z};
+            double Xd[3][2], ud[3][2];
+            float ev[4] = {0, 0, 0, 0};
+            double axd = 0, ayd = 0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double4 a = ld4(X + id[k]), b = ld4v(xp + id[k]);
+                Xd[k][0] = a.x; Xd[k][1] = a.y;
+                ud[k][0] = b.x - a.x; ud[k][1] = b.y - a.y;
+                axd += b.x; ayd += b.y;
+                const double* q6 = ea + 6 * (size_t)id[k];
+                ev[0] += (float)q6[0]; ev[1] += (float)q6[1]; ev[2] += (float)q6[3]; ev[3] += (float)q6[2];
+            }
+#pragma unroll
+            for (int m = 0; m < 4; ++m) ev[m] *= (1.0f / 3.0f);
+            // seeds: direction 2k + i is the displacement of corner k, component i
+            Dual<6> u[3][2];
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int i = 0; i < 2; ++i) {
+                    u[k][i] = dconst<6>((float)ud[k][i]);
+                    u[k][i].d[2 * k + i] = 1.0f;
+                }
+            const Dual<6> d1x = u[1][0] - u[0][0], d1y = u[1][1] - u[0][1];
+            const Dual<6> d2x = u[2][0] - u[0][0], d2y = u[2][1] - u[0][1];
+            Dual<6> ax = dconst<6>((float)(axd / 3.0 - cx)), ay = dconst<6>((float)(ayd / 3.0 - cy));
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                ax.d[2 * k] = 1.0f / 3.0f;
+                ay.d[2 * k + 1] = 1.0f / 3.0f;
+            }
+            Dual<6> re[3][2];
+            element_re_planar((float)(Xd[1][0] - Xd[0][0]), (float)(Xd[1][1] - Xd[0][1]), (float)(Xd[2][0] - Xd[0][0]),
+                              (float)(Xd[2][1] - Xd[0][1]), d1x, d1y, d2x, d2y, ev, ax, ay, q, re);
+            float* o = ke_s + 36 * j;
+#pragma unroll
+            for (int k = 0; k < 3; ++k)
+#pragma unroll
+                for (int i = 0; i < 2; ++i)
+#pragma unroll
+                    for (int l = 0; l < 6; ++l) o[(2 * k + i) * 6 + l] = re[k][i].d[l];
+            float* og = N.Ke + 36 * (size_t)e;   // duplicates across patches carry the same values
+#pragma unroll 4
+            for (int l = 0; l < 36; ++l) og[l] = o[l];
+        }
+        __syncthreads();
+        // rows 2v, 2v+1 of the owned vertices: diagonal, then the one-ring in mesh order
+        const double idt = 1.0 / dt;
+        for (int i = threadIdx.x; i < pt.y; i += blockDim.x) {
+            const int v = pt.x + i;
+            const double m = N.MM[v] * p.rho;
+            const double dg = m * idt * idt + (p.drag + p.damp * m) * idt;
+            N.diag[v] = dg;
+            float* row0 = N.J + (size_t)(2 * v) * N.ld;
+            float* row1 = row0 + N.ld;
+            row0[2 * v] += (float)dg;
+            row1[2 * v + 1] += (float)dg;
+            for (int k = c.vt_ptr[v]; k < c.vt_ptr[v + 1]; ++k) {
+                const int code = c.vc_code[k];
+                const int sl = code >> 2, cv = code & 3;
+                const int e = c.patch_elems[pt.z + sl];
+                const int4 t4 = c.tri[e];
+                const int id[3] = {t4.x, t4.y, t4.z};
+                const float* o = ke_s + 36 * sl;
+#pragma unroll
+                for (int l = 0; l < 3; ++l) {
+                    const int col = 2 * id[l];
+                    row0[col] += o[(2 * cv) * 6 + 2 * l];
+                    row0[col + 1] += o[(2 * cv) * 6 + 2 * l + 1];
+                    row1[col] += o[(2 * cv + 1) * 6 + 2 * l];
+                    row1[col + 1] += o[(2 * cv + 1) * 6 + 2 * l + 1];
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// Newton residual G (FP64) per owned vertex, and per cell |G|inf and the force scale
+__global__ void k_newton_residual(const CellDev* __restrict__ cells, const NewtonCell* __restrict__ nc,
+                                  const int* __restrict__ cell_of_slot, int nslots, double dt) {
+    const int slot = blockIdx.y;
+    if (slot >= nslots) return;
+    const NewtonCell& N = nc[slot];
+    if (!N.active) return;
+    const CellDev& c = cells[cell_of_slot[slot]];
+    const wcfe_params& p = c.prm;
+    const double idt = 1.0 / dt;
+    double gmax = 0.0, fscale = 0.0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N.n; v += gridDim.x * blockDim.x) {
+        const double m = N.MM[v] * p.rho;
+        const double4 Vv = ld4(c.vel + v);
+        const double dx[2] = {N.d[2 * (size_t)v], N.d[2 * (size_t)v + 1]}, V[2] = {Vv.x, Vv.y};
+#pragma unroll
+        for (int i = 0; i < 2; ++i) {
+            const double f = N.Fext[3 * (size_t)v + i], res = N.Res[3 * (size_t)v + i];
+            const double inert = m * dx[i] * idt * idt, mom = m * V[i] * idt;
+            const double g = inert - mom + (p.drag + p.damp * m) * dx[i] * idt - f + res;
+            N.G[2 * (size_t)v + i] = g;
+            gmax = fmax(gmax, fabs(g));
+            // the scale of the terms G sums (its rounding floor is relative to the largest)
+            fscale = fmax(fscale, fmax(fmax(fabs(f), fabs(res)), fmax(fabs(inert), fabs(mom))));
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        gmax = fmax(gmax, __shfl_xor_sync(0xffffffffu, gmax, o));
+        fscale = fmax(fscale, __shfl_xor_sync(0xffffffffu, fscale, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(reinterpret_cast<unsigned long long*>(N.norms + 0), (unsigned long long)__double_as_longlong(gmax));
+        atomicMax(reinterpret_cast<unsigned long long*>(N.norms + 1), (unsigned long long)__double_as_longlong(fscale));
+    }
+}
+
+// ===========================================================================
+// Dense LU without pivoting (J is strongly diagonally dominant: the mass term
+// m / dt^2 exceeds the membrane stiffness by orders of magnitude for explicit-size
+// steps; a pivot that is not finite or not above 1e-30 of the diagonal's scale
+// flags the cell).  Right-looking, 64-wide blocks; the trailing update
+// A22 -= L21 U12 runs on the tensor cores (mma m16n8k8, TF32 in, FP32 accumulate).
+// ===========================================================================
+constexpr int kNb = 64;
+
+__global__ void __launch_bounds__(256) k_lu_diag(NewtonCell* nc, int nslots, int k0) {
+    NewtonCell& N = nc[blockIdx.x];
+    const int m = 2 * N.n;
+    if (blockIdx.x >= nslots || !N.active || k0 >= m) return;
+    const int kb = min(kNb, m - k0);
+    __shared__ float A[kNb][kNb + 1];
+    for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
+        const int i = idx / kb, j = idx % kb;
+        A[i][j] = N.J[(size_t)(k0 + i) * N.ld + k0 + j];
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; ++j) {
+        const float piv = A[j][j];
+        if (threadIdx.x == 0 && !(fabsf(piv) > 1e-30f)) N.norms[3] = 1.0;
+        for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x) A[i][j] /= piv;
+        __syncthreads();
+        const int rest = kb - j - 1;
+        for (int idx = threadIdx.x; idx < rest * rest; idx += blockDim.x) {
+            const int i = j + 1 + idx / rest, k = j + 1 + idx % rest;
+            A[i][k] -= A[i][j] * A[j][k];
+        }
+        __syncthreads();
+    }
+    for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
+        const int i = idx / kb, j = idx % kb;
+        N.J[(size_t)(k0 + i) * N.ld + k0 + j] = A[i][j];
+    }
+}
+
+// U12 = L11^-1 A12 (block x: column chunks) and L21 = A21 U11^-1 (block x: row chunks
+// after the column chunks); one column or one row per thread, in place
+__global__ void __launch_bounds__(256) k_lu_panels(NewtonCell* nc, int nslots, int k0, int nchunks) {
+    const int slot = blockIdx.y;
+    if (slot >= nslots) return;
+    NewtonCell& N = nc[slot];
+    const int m = 2 * N.n;
+    if (!N.active || k0 >= m) return;
+    const int kb = min(kNb, m - k0);
+    const int r0 = k0 + kb;
+    if (r0 >= m) return;
+    __shared__ float D[kNb][kNb + 1];
+    for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
+        const int i = idx / kb, j = idx % kb;
+        D[i][j] = N.J[(size_t)(k0 + i) * N.ld + k0 + j];
+    }
+    __syncthreads();
+    const int half = nchunks / 2;
+    if ((int)blockIdx.x < half) {   // columns: forward substitution with the unit lower L11
+        for (int col = r0 + blockIdx.x * blockDim.x + threadIdx.x; col < m; col += half * blockDim.x) {
+            float x[kNb];
+#pragma unroll 8
+            for (int i = 0; i < kNb; ++i) {
+                if (i >= kb) break;
+                float a = N.J[(size_t)(k0 + i) * N.ld + col];
+                for (int j = 0; j < i; ++j) a -= D[i][j] * x[j];
+                x[i] = a;
+                N.J[(size_t)(k0 + i) * N.ld + col] = a;
+            }
+        }
+    } else {                         // rows: x U11 = a
+        for (int row = r0 + (blockIdx.x - half) * blockDim.x + threadIdx.x; row < m; row += half * blockDim.x) {
+            float* a = N.J + (size_t)row * N.ld + k0;
+            float x[kNb];
+#pragma unroll 8
+            for (int j = 0; j < kNb; ++j) {
+                if (j >= kb) break;
+                float s = a[j];
+                for (int i = 0; i < j; ++i) s -= x[i] * D[i][j];
+                x[j] = s / D[j][j];
+                a[j] = x[j];
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ uint32_t to_tf32(float f) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(f));
+    return r;
+}
+
+// A22 -= L21 U12 for one 128 x 128 tile of the trailing matrix; 8 warps as 2 x 4,
+// each a 64 x 32 block of 4 x 4 m16n8 tiles; K = the block width (<= 64).
+constexpr int kTile = 128;
+__global__ void __launch_bounds__(256) k_lu_update(NewtonCell* nc, int nslots, int k0) {
+    const int slot = blockIdx.z;
+    if (slot >= nslots) return;
+    NewtonCell& N = nc[slot];
+    const int m = 2 * N.n;
+    if (!N.active || k0 >= m) return;
+    const int kb = min(kNb, m - k0);
+    const int r0 = k0 + kb;
+    const int tm = r0 + blockIdx.y * kTile, tn = r0 + blockIdx.x * kTile;
+    if (tm >= m || tn >= m) return;
+    extern __shared__ float smu[];
+    float* As = smu;                       // [128][kNb + 4]: L21 rows tm.., columns k0..
+    float* Bs = smu + kTile * (kNb + 4);   // [kNb][128 + 8]: U12 rows k0.., columns tn..
+    const int lda = kNb + 4, ldb = kTile + 8;
+    for (int idx = threadIdx.x; idx < kTile * kNb; idx += blockDim.x) {
+        const int i = idx / kNb, k = idx % kNb;
+        const int row = tm + i;
+        As[i * lda + k] = (row < m && k < kb) ? N.J[(size_t)row * N.ld + k0 + k] : 0.0f;
+    }
+    for (int idx = threadIdx.x; idx < kNb * kTile; idx += blockDim.x) {
+        const int k = idx / kTile, j = idx % kTile;
+        const int col = tn + j;
+        Bs[k * ldb + j] = (col < m && k < kb) ? N.J[(size_t)(k0 + k) * N.ld + col] : 0.0f;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = (warp >> 2) * 64, wn = (warp & 3) * 32;   // warp block origin in the tile
+    const int g = lane >> 2, t = lane & 3;
+    float acc[4][4][4];
+    // load C (the trailing entries) into the accumulators
+#pragma unroll
+    for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni) {
+            const int rA = tm + wm + mi * 16 + g, cA = tn + wn + ni * 8 + 2 * t;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int row = rA + 8 * h;
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int col = cA + q;
+                    acc[mi][ni][2 * h + q] = (row < m && col < m) ? N.J[(size_t)row * N.ld + col] : 0.0f;
+                }
+            }
+        }
+    for (int ks = 0; ks < kNb; ks += 8) {
+        uint32_t af[4][4], bf[4][2];
+#pragma unroll
+        for (int mi = 0; mi < 4; ++mi) {
+            const float* a = As + (wm + mi * 16) * lda + ks;
+            // -L21: the product is subtracted
+            af[mi][0] = to_tf32(-a[g * lda + t]);
+            af[mi][1] = to_tf32(-a[(g + 8) * lda + t]);
+            af[mi][2] = to_tf32(-a[g * lda + t + 4]);
+            af[mi][3] = to_tf32(-a[(g + 8) * lda + t + 4]);
+        }
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni) {
+            const float* b = Bs + ks * ldb + wn + ni * 8;
+            bf[ni][0] = to_tf32(b[t * ldb + g]);
+            bf[ni][1] = to_tf32(b[(t + 4) * ldb + g]);
+        }
+#pragma unroll
+        for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+            for (int ni = 0; ni < 4; ++ni) {
+                float* d = acc[mi][ni];
+                asm volatile(
+                    "mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                    "{%0,%1,%2,%3};"
+                    : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+                    : "r"(af[mi][0]), "r"(af[mi][1]), "r"(af[mi][2]), "r"(af[mi][3]), "r"(bf[ni][0]), "r"(bf[ni][1]));
+            }
+    }
+#pragma unroll
+    for (int mi = 0; mi < 4; ++mi)
+#pragma unroll
+        for (int ni = 0; ni < 4; ++ni) {
+            const int rA = tm + wm + mi * 16 + g, cA = tn + wn + ni * 8 + 2 * t;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int row = rA + 8 * h;
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int col = cA + q;
+                    if (row < m && col < m) N.J[(size_t)row * N.ld + col] = acc[mi][ni][2 * h + q];
+                }
+            }
+        }
+}
+
+// ===========================================================================
+// Triangular solves with the LU factors, z = U^-1 L^-1 r (FP32), one CTA per cell:
+// within a 64-row block the substitution runs on warp 0; the rows outside the
+// block are updated by the whole CTA
+// ===========================================================================
+constexpr int kSolveThreads = 512;
+__global__ void __launch_bounds__(kSolveThreads) k_lu_solve(NewtonCell* nc, int nslots) {
+    extern __shared__ float y[];   // [2n]
+    NewtonCell& N = nc[blockIdx.x];
+    const int m = 2 * N.n;
+    if (blockIdx.x >= nslots || !N.active) return;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) y[i] = (float)N.r[i];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // forward: L (unit lower)
+    for (int b0 = 0; b0 < m; b0 += kNb) {
+        const int kb = min(kNb, m - b0);
+        if (warp == 0) {
+            for (int i = 1; i < kb; ++i) {
+                const float* Li = N.J + (size_t)(b0 + i) * N.ld + b0;
+                float s = 0.0f;
+                for (int j = lane; j < i; j += 32) s += Li[j] * y[b0 + j];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                if (lane == 0) y[b0 + i] -= s;
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        for (int i = b0 + kb + threadIdx.x; i < m; i += blockDim.x) {
+            const float* Li = N.J + (size_t)i * N.ld + b0;
+            float s = 0.0f;
+            for (int j = 0; j < kb; ++j) s += Li[j] * y[b0 + j];
+            y[i] -= s;
+        }
+        __syncthreads();
+    }
+    // backward: U
+    const int nblk = (m + kNb - 1) / kNb;
+    for (int bi = nblk - 1; bi >= 0; --bi) {
+        const int b0 = bi * kNb, kb = min(kNb, m - b0);
+        if (warp == 0) {
+            for (int i = kb - 1; i >= 0; --i) {
+                const float* Ui = N.J + (size_t)(b0 + i) * N.ld + b0;
+                float s = 0.0f;
+                for (int j = i + 1 + lane; j < kb; j += 32) s += Ui[j] * y[b0 + j];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                if (lane == 0) y[b0 + i] = (y[b0 + i] - s) / Ui[i];
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < b0; i += blockDim.x) {
+            const float* Ui = N.J + (size_t)i * N.ld + b0;
+            float s = 0.0f;
+            for (int j = 0; j < kb; ++j) s += Ui[j] * y[b0 + j];
+            y[i] -= s;
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < m; i += blockDim.x) N.z[i] = y[i];
+}
+
+// dx += z; r = -G - J dx in FP64 with J element by element (diagonal + the FP32 element
+// tangents promoted), one CTA per patch; |r|inf per cell
+__global__ void __launch_bounds__(kTanThreads) k_newton_refine(const CellDev* __restrict__ cells, NewtonCell* nc,
+                                                              const int* __restrict__ cell_slot,
+                                                              const WorkItem* __restrict__ work, int nwork,
+                                                              int add_z) {
+    for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
+        const WorkItem it = work[w];
+        const int slot = cell_slot[it.cell];
+        if (slot < 0) continue;
+        NewtonCell& N = nc[slot];
+        if (!N.active) continue;
+        const CellDev& c = cells[it.cell];
+        const int4 pt = c.patch[it.idx];
+        double rmax = 0.0;
+        for (int i = threadIdx.x; i < pt.y; i += blockDim.x) {
+            const int v = pt.x + i;
+            double jd[2] = {0.0, 0.0};
+            for (int k = c.vt_ptr[v]; k < c.vt_ptr[v + 1]; ++k) {
+                const int code = c.vc_code[k];
+                const int cv = code & 3;
+                const int e = c.patch_elems[pt.z + (code >> 2)];
+                const int4 t4 = c.tri[e];
+                const int id[3] = {t4.x, t4.y, t4.z};
+                const float* o = N.Ke + 36 * (size_t)e;
+#pragma unroll
+                for (int l = 0; l < 3; ++l)
+#pragma unroll
+                    for (int j = 0; j < 2; ++j) {
+                        const int col = 2 * id[l] + j;
+                        const double dcol = N.dx[col] + (add_z ? (double)N.z[col] : 0.0);
+                        jd[0] += (double)o[(2 * cv) * 6 + 2 * l + j] * dcol;
+                        jd[1] += (double)o[(2 * cv + 1) * 6 + 2 * l + j] * dcol;
+                    }
+            }
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int row = 2 * v + q;
+                const double dr = N.dx[row] + (add_z ? (double)N.z[row] : 0.0);
+                const double rr = -N.G[row] - (N.diag[v] * dr + jd[q]);
+                N.r[row] = rr;
+                rmax = fmax(rmax, fabs(rr));
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+        if ((threadIdx.x & 31) == 0)
+            atomicMax(reinterpret_cast<unsigned long long*>(N.norms + 2), (unsigned long long)__double_as_longlong(rmax));
+    }
+}
+
+// dx += z (after every refine pass reads it)
+__global__ void k_newton_accumulate(NewtonCell* nc, int nslots) {
+    NewtonCell& N = nc[blockIdx.y];
+    if (blockIdx.y >= nslots || !N.active) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * N.n; i += gridDim.x * blockDim.x) N.dx[i] += (double)N.z[i];
+}
+
+// d += dx (in-plane displacement), x = X + d in pos[par ^ 1]; init: d = x_pred - X
+__global__ void k_newton_apply(const CellDev* __restrict__ cells, NewtonCell* nc, const int* __restrict__ cell_of_slot,
+                               int nslots, int init) {
+    NewtonCell& N = nc[blockIdx.y];
+    if (blockIdx.y >= nslots || (!init && !N.active)) return;
+    const CellDev& c = cells[cell_of_slot[blockIdx.y]];
+    const int par = c.ctl[0];
+    const double4* X = c.pos[par];
+    double4* xp = c.pos[par ^ 1];
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N.n; v += gridDim.x * blockDim.x) {
+        const double4 Xv = ld4(X + v);
+        double4 q = ld4v(xp + v);
+        if (init) {
+            N.d[2 * v] = q.x - Xv.x;
+            N.d[2 * v + 1] = q.y - Xv.y;
+            continue;
+        }
+        const double d0 = N.d[2 * v] + N.dx[2 * v], d1 = N.d[2 * v + 1] + N.dx[2 * v + 1];
+        N.d[2 * v] = d0;
+        N.d[2 * v + 1] = d1;
+        st4(xp + v, Xv.x + d0, Xv.y + d1, q.z);
+    }
+}
+
+// Finish the step at the converged x: V = (x - X)/dt, A = (V - V_old)/dt, ea += Res_ea / MM;
+// the last block of a cell advances parity, clock and AP counter
+__global__ void k_newton_finish(const CellDev* __restrict__ cells, NewtonCell* nc, const int* __restrict__ cell_of_slot,
+                                int nslots, const double* __restrict__ res_ea, double dt, unsigned int* tickets) {
+    const int slot = blockIdx.y;
+    if (slot >= nslots) return;
+    NewtonCell& N = nc[slot];
+    const CellDev& c = cells[cell_of_slot[slot]];
+    const int par = c.ctl[0];
+    const double* eo = c.ea[par];
+    double* en = c.ea[par ^ 1];
+    const double* Rq = res_ea + 6 * (size_t)c.hoff;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N.n; v += gridDim.x * blockDim.x) {
+        const double4 Vo = ld4(c.vel + v);
+        const double Vn[2] = {N.d[2 * (size_t)v] / dt, N.d[2 * (size_t)v + 1] / dt};
+        st4(c.acc + v, (Vn[0] - Vo.x) / dt, (Vn[1] - Vo.y) / dt, 0.0);
+        st4(c.vel + v, Vn[0], Vn[1], 0.0);
+        const double iMM = 1.0 / N.MM[v];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) en[6 * (size_t)v + q] = eo[6 * (size_t)v + q] + Rq[6 * (size_t)v + q] * iMM;
+        if (!isfinite(Vn[0] + Vn[1])) atomicOr(c.status, 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned int done = atomicAdd(tickets + slot, 1u);
+        if ((int)done == (int)gridDim.x - 1) {
+            tickets[slot] = 0;
+            c.ctl[0] = par ^ 1;
+            c.clk[0] = c.clk[0] + dt;
+            c.ap[0] = c.ap[0] + 1ull;
+        }
+    }
+}
+
+// F_ext = F_FA + F_AP + F_bend + F_area (packed [3 n_total])
+__global__ void k_sum4(const double* __restrict__ a, const double* __restrict__ b, const double* __restrict__ c,
+                       const double* __restrict__ d, double* __restrict__ o, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        o[i] = a[i] + b[i] + c[i] + d[i];
+}
+
+// ---------------------------------------------------------------------------- host launchers
+static int g_num_sms = 0;
+
+cudaError_t configure_newton(size_t max_smem, int num_sms) {
+    g_num_sms = num_sms;
+    cudaError_t e = cudaFuncSetAttribute((const void*)k_lu_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)(sizeof(float) * (kTile * (kNb + 4) + kNb * (kTile + 8))));
+    if (e != cudaSuccess) return e;
+    cudaFuncAttributes at;
+    if ((e = cudaFuncGetAttributes(&at, (const void*)k_lu_solve)) != cudaSuccess) return e;
+    if ((e = cudaFuncSetAttribute((const void*)k_lu_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(max_smem - at.sharedSizeBytes - 1024))) != cudaSuccess)
+        return e;
+    if ((e = cudaFuncGetAttributes(&at, (const void*)k_newton_tangent)) != cudaSuccess) return e;
+    return cudaFuncSetAttribute((const void*)k_newton_tangent, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(max_smem - at.sharedSizeBytes - 1024));
+}
+
+size_t newton_solve_smem(int max_n) { return sizeof(float) * 2 * (size_t)max_n; }
+size_t newton_tangent_smem(int emax) { return sizeof(float) * 36 * (size_t)emax; }
+
+void launch_newton_residual(const CellDev* cells, const NewtonCell* nc, const int* cell_of_slot, int nslots, int max_n,
+                            double dt, cudaStream_t st) {
+    dim3 grid((unsigned)std::max(1, std::min((max_n + 255) / 256, 64)), (unsigned)nslots);
+    k_newton_residual<<<grid, 256, 0, st>>>(cells, nc, cell_of_slot, nslots, dt);
+}
+void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int* cell_slot, const WorkItem* work,
+                           int nwork, int emax, double dt, cudaStream_t st) {
+    if (nwork <= 0) return;
+    const int grid = std::min(nwork, std::max(1, g_num_sms) * 8);
+    k_newton_tangent<<<grid, kTanThreads, newton_tangent_smem(emax), st>>>(cells, nc, cell_slot, work, nwork, emax, dt);
+}
+void launch_newton_lu(NewtonCell* nc, int nslots, int max_m, cudaStream_t st) {
+    const size_t usm = sizeof(float) * (kTile * (kNb + 4) + kNb * (kTile + 8));
+    for (int k0 = 0; k0 < max_m; k0 += kNb) {
+        k_lu_diag<<<nslots, 256, 0, st>>>(nc, nslots, k0);
+        const int rest = max_m - k0 - kNb;
+        if (rest <= 0) break;
+        const int half = std::max(1, std::min((rest + 255) / 256, 32));
+        k_lu_panels<<<dim3(2 * half, nslots), 256, 0, st>>>(nc, nslots, k0, 2 * half);
+        const int tiles = (rest + kTile - 1) / kTile;
+        k_lu_update<<<dim3(tiles, tiles, nslots), 256, usm, st>>>(nc, nslots, k0);
+    }
+}
+void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, cudaStream_t st) {
+    k_lu_solve<<<nslots, kSolveThreads, newton_solve_smem(max_n), st>>>(nc, nslots);
+}
+void launch_newton_refine(const CellDev* cells, NewtonCell* nc, const int* cell_slot, const WorkItem* work, int nwork,
+                          int add_z, cudaStream_t st) {
+    if (nwork <= 0) return;
+    const int grid = std::min(nwork, std::max(1, g_num_sms) * 8);
+    k_newton_refine<<<grid, kTanThreads, 0, st>>>(cells, nc, cell_slot, work, nwork, add_z);
+}
+void launch_newton_accumulate(NewtonCell* nc, int nslots, int max_n, cudaStream_t st) {
+    dim3 grid((unsigned)std::max(1, std::min((2 * max_n + 255) / 256, 64)), (unsigned)nslots);
+    k_newton_accumulate<<<grid, 256, 0, st>>>(nc, nslots);
+}
+void launch_newton_apply(const CellDev* cells, NewtonCell* nc, const int* cell_of_slot, int nslots, int max_n, int init,
+                         cudaStream_t st) {
+    dim3 grid((unsigned)std::max(1, std::min((max_n + 255) / 256, 64)), (unsigned)nslots);
+    k_newton_apply<<<grid, 256, 0, st>>>(cells, nc, cell_of_slot, nslots, init);
+}
+void launch_newton_finish(const CellDev* cells, NewtonCell* nc, const int* cell_of_slot, int nslots, int max_n,
+                          const double* res_ea, double dt, unsigned int* tickets, cudaStream_t st) {
+    dim3 grid((unsigned)std::max(1, std::min((max_n + 255) / 256, 64)), (unsigned)nslots);
+    k_newton_finish<<<grid, 256, 0, st>>>(cells, nc, cell_of_slot, nslots, res_ea, dt, tickets);
+}
+void launch_sum4(const double* a, const double* b, const double* c, const double* d, double* o, size_t n,
+                 cudaStream_t st) {
+    if (n == 0) return;
+    const int grid = (int)std::min<size_t>((n + 255) / 256, 4096);
+    k_sum4<<<grid, 256, 0, st>>>(a, b, c, d, o, n);
+}
+
+}  // namespace wcfe
