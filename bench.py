@@ -353,6 +353,9 @@ def run_ours(args):
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
                     "avg_launch_ms": round(avg_p, 4), "vertex_phase_avg_launch_ms": round(avg_v, 4)}
 
+        newton = run_newton(args.newton_cells) if args.newton_cells > 0 else None
+        if newton:
+            log(f"[bench] newton: {newton}")
         serving = run_serving(args.serve_seconds) if args.serve_seconds > 0 else None
         if serving:
             log(f"[bench] serving: {serving}")
@@ -380,6 +383,7 @@ def run_ours(args):
             "mixed_vs_fp64_rel_displacement_error": max_err, "error_steps": err_steps,
             "element_assemblies_per_s": round(value / len(cells) * nt_total / world, 1),
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "serving": serving,
+            "newton": newton,
             "clocks": clocks_info,
         }
     if dist:
@@ -463,6 +467,45 @@ def run_serving(seconds: float, rate: float = 200.0, budget_gb: float = 16.0, se
             "max_resident_cells": max(active_hist) if active_hist else 0}
 
 
+def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4):
+    """Config 4, bounded: implicit (Newton) steps of `ncells` cells with 1000-4000 vertices
+    (uniform), dense 2N x 2N tangents, LU with TF32 tensor-core trailing updates, FP64
+    residual and refinement to 1e-10.  Reports cell-steps/s, Newton iterations, the
+    residuals reached and the LU's FLOP rate over the timed steps."""
+    import torch
+    from wholecellfe_gb300 import capi, synth
+    from wholecellfe_gb300.params import default_params
+    rng = np.random.default_rng(seed)
+    eng = capi.Engine(capi.PREC_FP64)
+    sizes = []
+    for i in range(ncells):
+        n = int(rng.integers(1000, 4001))
+        x0, tri = synth.disk_mesh(n, seed=7000 + i)
+        p = default_params(["k1", "k31", "k31"][i % 3])
+        if i % 3 == 2:
+            p.force_law, p.poly_k0, p.poly_x0, p.linear_norm2d = 2, 31000.0, 0.005, 0
+        p.stream = i
+        eng.add_cell(x0, tri, p, state=synth.initial_state(x0))
+        sizes.append(len(x0))
+    eng.step_implicit(1, DT, rtol=1e-10, max_newton=8)   # warm-up (and first allocations)
+    eng.sync()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    st = eng.step_implicit(steps, DT, rtol=1e-10, max_newton=8)
+    eng.sync()
+    wall = time.perf_counter() - t0
+    eng.close()
+    lu_flops_per_iter = sum((2.0 / 3.0) * (2 * n) ** 3 for n in sizes)
+    iters = st["newton_iters"]   # Newton updates over the timed steps (all cells in lockstep)
+    return {"cells": ncells, "vertices": "uniform [1000, 4000]", "steps": steps,
+            "cell_steps_per_s": round(ncells * steps / wall, 2), "ms_per_step": round(wall / steps * 1e3, 2),
+            "newton_iters_per_step": iters / steps, "max_refine_passes": st["max_refine_iters"],
+            "max_rel_residual": st["max_rel_residual"], "max_refine_rel_residual": st["max_refine_rel_residual"],
+            "unconverged_cell_steps": st["unconverged"], "rounding_floor_exits": st["floor_exits"],
+            "lu_tflop_per_s": round(lu_flops_per_iter * iters / wall / 1e12, 2),
+            "timing": "host wall clock around wcfe_engine_step_implicit (it synchronises per Newton iteration)"}
+
+
 def run_phase(args):
     """One timed loop only, for profiling: the batched mixed or FP64 form on the workload
     (--cells of them), or the plain one-cell FP64 form."""
@@ -470,6 +513,9 @@ def run_phase(args):
     from wholecellfe_gb300 import capi, synth
     from wholecellfe_gb300.params import default_params
     torch.cuda.init()
+    if args.phase == "newton":
+        print(json.dumps(run_newton(args.cells if args.cells != N_CELLS else 64, max(1, min(args.steps, 5)))))
+        return
     if args.phase == "plain":
         x0, tri = synth.disk_mesh(2000, seed=1)
         eng = capi.Engine(capi.PREC_FP64)
@@ -545,8 +591,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the Poisson arrival window of the serving measurement (0: skip)")
-    ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain"],
+    ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain", "newton"],
                     help="profiling aid: run only one timed loop (default shape, no autotune) and print its timing")
+    ap.add_argument("--newton-cells", type=int, default=64,
+                    help="cells of the bounded implicit-step (Newton, dense LU) measurement (0: skip)")
     ap.add_argument("--shape", default="", help="with --phase: patch threads,elements (default: the engine's)")
     ap.add_argument("--patch-kernel", type=int, default=1, choices=[0, 1],
                     help="with --phase mixed: 0 staged patch kernel, 1 plain (default)")

@@ -296,14 +296,17 @@ int wcfe_area_tot_noalloc(const double* x_dev, int32_t n_vert, const int32_t* tr
  * in the plane (2N unknowns; planar cells).  Per Newton iteration: G in FP64, the
  * dense 2N x 2N tangent from FP32 element tangents, its LU factorisation (trailing
  * updates on the tensor cores, TF32), and the solve refined in FP64 until its
- * residual is 1e-10 of |G|.  Converged when |G|inf <= newton_rtol * (force scale).
+ * residual is 1e-10 of |G|.  Converged when |G|inf <= newton_rtol * (the largest
+ * term G sums), or at the residual's rounding floor, |dRes/dx| ulp(x) with FP64
+ * positions: the last correction below 1e-13 of the displacement, or no further
+ * reduction of |G| (more than 1/4 of the previous) once below 1e-6 of the scale.
  * After the step V = (x - X)/dt, A = (V - V_old)/dt, ea += Res_ea/MM.  FP64 engines
  * only.  Dense factors take 4 (2N)^2 bytes per cell on the device. */
 typedef struct wcfe_newton_stats {
     int32_t newton_iters;              /* Newton updates summed over steps (all cells together) */
     int32_t max_refine_iters;          /* largest number of refinement passes of one linear solve */
     int32_t unconverged;               /* cell-steps that hit max_newton without converging */
-    int32_t pad;
+    int32_t floor_exits;               /* cell-steps that stopped at the residual's rounding floor above rtol */
     double max_rel_residual;           /* largest final |G|inf / force scale */
     double max_refine_rel_residual;    /* largest final |J dx + G|inf / |G|inf of a linear solve */
 } wcfe_newton_stats;

@@ -24,7 +24,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 
 class NewtonStats(C.Structure):
     _fields_ = [("newton_iters", C.c_int32), ("max_refine_iters", C.c_int32), ("unconverged", C.c_int32),
-                ("pad", C.c_int32), ("max_rel_residual", C.c_double), ("max_refine_rel_residual", C.c_double)]
+                ("floor_exits", C.c_int32), ("max_rel_residual", C.c_double), ("max_refine_rel_residual", C.c_double)]
 
 
 class Request(C.Structure):
@@ -243,7 +243,7 @@ class Engine:
         st = NewtonStats()
         check(load().wcfe_engine_step_implicit(self.h, nsteps, dt, rtol, max_newton, C.byref(st)),
               "wcfe_engine_step_implicit")
-        return {k: getattr(st, k) for k, _ in NewtonStats._fields_ if k != "pad"}
+        return {k: getattr(st, k) for k, _ in NewtonStats._fields_}
 
     def step_cells(self, cells, nsteps: int, dt: float):
         ids = i32([c.id for c in cells])

@@ -134,7 +134,8 @@ struct NewtonCell {
     const double* Fext;  // [3n] external forces at the predicted positions
     const double* Res;   // [3n] membrane residual at the iterate
     const double* MM;    // [n] lumped mass
-    double* norms;       // [4]: |G|inf, force scale, |r|inf, non-finite or zero pivot flag
+    double* norms;       // [8]: |G|inf, force scale, |r|inf, non-finite or zero pivot flag, |dx|inf of the
+                         //      last update, |d|inf
     int n, ld, active, pad;
 };
 

@@ -1401,7 +1401,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
     auto put = [&](size_t bytes) { const size_t at = o; o = al256(o + bytes); return at; };
     const size_t o_res = put(sizeof(double) * 3 * NV), o_rea = put(sizeof(double) * 6 * NV), o_mm = put(sizeof(double) * NV);
     const size_t o_f4 = put(sizeof(double) * 12 * NV), o_fext = put(sizeof(double) * 3 * NV);
-    const size_t o_norm = put(sizeof(double) * 4 * ns), o_nc = put(sizeof(NewtonCell) * ns);
+    const size_t o_norm = put(sizeof(double) * 8 * ns), o_nc = put(sizeof(NewtonCell) * ns);
     const size_t o_id = put(sizeof(int) * ns), o_tk = put(sizeof(unsigned int) * ns);
     struct Off { size_t J, Ke, diag, G, dx, d, r, z; int n, ld; };
     std::vector<Off> off(ns);
@@ -1454,7 +1454,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         N.Fext = P.fext + 3 * h;
         N.Res = P.res + 3 * h;
         N.MM = P.mm + h;
-        N.norms = P.norms + 4 * (size_t)sl;
+        N.norms = P.norms + 8 * (size_t)sl;
         N.n = f.n;
         N.ld = f.ld;
         N.active = 1;
@@ -1481,7 +1481,7 @@ int newton_upload_active(wcfe_engine* e, NewtonPlan& P) {
 }
 
 int newton_read_norms(wcfe_engine* e, NewtonPlan& P, std::vector<double>& h) {
-    h.resize(4 * P.cells.size());
+    h.resize(8 * P.cells.size());
     CK(cudaMemcpyAsync(h.data(), P.norms, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return WCFE_OK;
@@ -1514,21 +1514,31 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
         launch_sum4(P.f4, P.f4 + 3 * NV, P.f4 + 6 * NV, P.f4 + 9 * NV, P.fext, 3 * NV, e->stream);
     }
     for (auto& N : P.cells) N.active = 1;
+    std::vector<double> gprev(ns, INFINITY);
     int r = newton_upload_active(e, P);
     if (r) return r;
     launch_newton_apply(e->d_table, P.d_cells, P.d_ident, ns, P.max_n, 1, e->stream);   // d = x_pred - X
     e->launches += 3;
     for (int it = 0;; ++it) {
         newton_membrane(e, P, dt);
-        CK(cudaMemsetAsync(P.norms, 0, sizeof(double) * 4 * ns, e->stream));
+        // |G| and the force scale (entries 0, 1) are rebuilt; entries 4, 5 hold the last update
+        for (int sl = 0; sl < ns; ++sl) CK(cudaMemsetAsync(P.norms + 8 * (size_t)sl, 0, sizeof(double) * 4, e->stream));
         launch_newton_residual(e->d_table, P.d_cells, P.d_ident, ns, P.max_n, dt, e->stream);
         e->launches += 2;
         if ((r = newton_read_norms(e, P, hn))) return r;
         int nact = 0;
         for (int sl = 0; sl < ns; ++sl) {
-            const double g = hn[4 * sl], f = std::max(hn[4 * sl + 1], 1e-300);
-            const bool bad = !std::isfinite(g) || hn[4 * sl + 3] != 0.0;
-            const bool conv = g <= rtol * f;
+            const double g = hn[8 * sl], f = std::max(hn[8 * sl + 1], 1e-300);
+            const bool bad = !std::isfinite(g) || hn[8 * sl + 3] != 0.0;
+            // converged: the residual at rtol of the force scale, or the iteration has reached the
+            // residual's rounding floor, about |dRes/dx| ulp(x) (the positions are FP64): the last
+            // correction was at the rounding level of the displacement, or Newton, which otherwise
+            // converges quadratically here, stopped reducing |G| (below 1e-6 of the scale)
+            const bool floor = it > 0 && (hn[8 * sl + 4] <= 1e-13 * hn[8 * sl + 5] ||
+                                          (it > 1 && g > 0.25 * gprev[sl] && g <= 1e-6 * f));
+            const bool conv = g <= rtol * f || floor;
+            if (floor && !(g <= rtol * f) && st && P.cells[sl].active) st->floor_exits += 1;
+            gprev[sl] = g;
             P.cells[sl].active = (!bad && !conv && it < max_newton) ? 1 : 0;
             nact += P.cells[sl].active;
             if (!P.cells[sl].active) {   // final for this step
@@ -1565,7 +1575,8 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
         double final_ratio = 0.0;
         for (; q < 16; ++q) {
             launch_newton_solve(P.d_cells, ns, P.max_n, e->stream);
-            CK(cudaMemsetAsync(P.norms, 0, sizeof(double) * 4 * ns, e->stream));   // G's norm is kept on the host
+            for (int sl = 0; sl < ns; ++sl)   // |r| only (G's norm is kept on the host)
+                CK(cudaMemsetAsync(P.norms + 8 * (size_t)sl + 2, 0, sizeof(double), e->stream));
             launch_newton_refine(e->d_table, P.d_cells, P.d_ident, e->d_k2, n2, 1, e->stream);
             launch_newton_accumulate(P.d_cells, ns, P.max_n, e->stream);
             e->launches += 3;
@@ -1575,7 +1586,7 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
             final_ratio = 0.0;
             for (int sl = 0; sl < ns; ++sl) {
                 if (!P.cells[sl].active) continue;
-                const double ratio = hr[4 * sl + 2] / std::max(hn[4 * sl], 1e-300);
+                const double ratio = hr[8 * sl + 2] / std::max(hn[8 * sl], 1e-300);
                 if (!(ratio <= 1e-10)) done = false;
                 final_ratio = std::max(final_ratio, ratio);
             }
@@ -1585,6 +1596,7 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
             st->max_refine_iters = std::max(st->max_refine_iters, q + 1);
             st->max_refine_rel_residual = std::max(st->max_refine_rel_residual, final_ratio);
         }
+        for (int sl = 0; sl < ns; ++sl) CK(cudaMemsetAsync(P.norms + 8 * (size_t)sl + 4, 0, sizeof(double) * 2, e->stream));
         launch_newton_apply(e->d_table, P.d_cells, P.d_ident, ns, P.max_n, 0, e->stream);
         e->launches += 4 + 3 * ((2 * P.max_n + 63) / 64);
         CK(cudaGetLastError());
@@ -1669,7 +1681,7 @@ int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x) {
     CK(configure_newton((size_t)max_optin, sms));
     const int ld = (m + 3) & ~3;
     const size_t bytes = sizeof(float) * (size_t)m * ld + sizeof(double) * m + sizeof(float) * m +
-                         sizeof(double) * 4 + sizeof(NewtonCell) + 1024;
+                         sizeof(double) * 8 + sizeof(NewtonCell) + 1024;
     char* blk = nullptr;
     CK(cudaMalloc(&blk, bytes));
     size_t o = 0;
@@ -1678,7 +1690,7 @@ int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x) {
     N.J = (float*)take(sizeof(float) * (size_t)m * ld);
     N.r = (double*)take(sizeof(double) * m);
     N.z = (float*)take(sizeof(float) * m);
-    N.norms = (double*)take(sizeof(double) * 4);
+    N.norms = (double*)take(sizeof(double) * 8);
     N.n = m / 2;
     N.ld = ld;
     N.active = 1;
@@ -1686,7 +1698,7 @@ int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x) {
     cudaError_t ce = cudaMemcpy2D(N.J, sizeof(float) * ld, A, sizeof(float) * m, sizeof(float) * m, m,
                                   cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(N.r, b, sizeof(double) * m, cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess) ce = cudaMemset(N.norms, 0, sizeof(double) * 4);
+    if (ce == cudaSuccess) ce = cudaMemset(N.norms, 0, sizeof(double) * 8);
     if (ce == cudaSuccess) ce = cudaMemcpy(d_nc, &N, sizeof N, cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) {
         launch_newton_lu(d_nc, 1, m, 0);

@@ -654,6 +654,7 @@ __global__ void k_newton_apply(const CellDev* __restrict__ cells, NewtonCell* nc
     const int par = c.ctl[0];
     const double4* X = c.pos[par];
     double4* xp = c.pos[par ^ 1];
+    double dxm = 0.0, dm = 0.0;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < N.n; v += gridDim.x * blockDim.x) {
         const double4 Xv = ld4(X + v);
         double4 q = ld4v(xp + v);
@@ -666,6 +667,17 @@ __global__ void k_newton_apply(const CellDev* __restrict__ cells, NewtonCell* nc
         N.d[2 * v] = d0;
         N.d[2 * v + 1] = d1;
         st4(xp + v, Xv.x + d0, Xv.y + d1, q.z);
+        dxm = fmax(dxm, fmax(fabs(N.dx[2 * v]), fabs(N.dx[2 * v + 1])));
+        dm = fmax(dm, fmax(fabs(d0), fabs(d1)));
+    }
+    if (init) return;
+    for (int o = 16; o > 0; o >>= 1) {
+        dxm = fmax(dxm, __shfl_xor_sync(0xffffffffu, dxm, o));
+        dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(reinterpret_cast<unsigned long long*>(N.norms + 4), (unsigned long long)__double_as_longlong(dxm));
+        atomicMax(reinterpret_cast<unsigned long long*>(N.norms + 5), (unsigned long long)__double_as_longlong(dm));
     }
 }
 
