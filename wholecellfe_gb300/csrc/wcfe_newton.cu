@@ -349,37 +349,42 @@ __global__ void k_newton_residual(const CellDev* __restrict__ cells, const Newto
 // ===========================================================================
 constexpr int kNb = 64;
 
+// The diagonal block, padded to 64 x 64 with the identity, factored in shared memory
+// by a 16 x 16 thread grid (no divisions or modulos in the inner loops).
+__device__ __forceinline__ void load_block_padded(const NewtonCell& N, int k0, int kb, float (*A)[kNb + 1]) {
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    for (int i = ty; i < kNb; i += 16)
+        for (int j = tx; j < kNb; j += 16)
+            A[i][j] = (i < kb && j < kb) ? N.J[(size_t)(k0 + i) * N.ld + k0 + j] : (i == j ? 1.0f : 0.0f);
+}
+
 __global__ void __launch_bounds__(256) k_lu_diag(NewtonCell* nc, int nslots, int k0) {
     NewtonCell& N = nc[blockIdx.x];
     const int m = 2 * N.n;
     if (blockIdx.x >= nslots || !N.active || k0 >= m) return;
     const int kb = min(kNb, m - k0);
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     __shared__ float A[kNb][kNb + 1];
-    for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
-        const int i = idx / kb, j = idx % kb;
-        A[i][j] = N.J[(size_t)(k0 + i) * N.ld + k0 + j];
-    }
+    load_block_padded(N, k0, kb, A);
     __syncthreads();
-    for (int j = 0; j < kb; ++j) {
+    for (int j = 0; j < kNb; ++j) {
         const float piv = A[j][j];
-        if (threadIdx.x == 0 && !(fabsf(piv) > 1e-30f)) N.norms[3] = 1.0;
-        for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x) A[i][j] /= piv;
+        if (threadIdx.x == 0 && j < kb && !(fabsf(piv) > 1e-30f)) N.norms[3] = 1.0;
+        if (threadIdx.x > j && threadIdx.x < kNb) A[threadIdx.x][j] /= piv;
         __syncthreads();
-        const int rest = kb - j - 1;
-        for (int idx = threadIdx.x; idx < rest * rest; idx += blockDim.x) {
-            const int i = j + 1 + idx / rest, k = j + 1 + idx % rest;
-            A[i][k] -= A[i][j] * A[j][k];
+        for (int i = j + 1 + ty; i < kNb; i += 16) {
+            const float l = A[i][j];
+            for (int k = j + 1 + tx; k < kNb; k += 16) A[i][k] -= l * A[j][k];
         }
         __syncthreads();
     }
-    for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
-        const int i = idx / kb, j = idx % kb;
-        N.J[(size_t)(k0 + i) * N.ld + k0 + j] = A[i][j];
-    }
+    for (int i = ty; i < kb; i += 16)
+        for (int j = tx; j < kb; j += 16) N.J[(size_t)(k0 + i) * N.ld + k0 + j] = A[i][j];
 }
 
 // U12 = L11^-1 A12 (block x: column chunks) and L21 = A21 U11^-1 (block x: row chunks
-// after the column chunks); one column or one row per thread, in place
+// after the column chunks); one column or one row per thread, held in registers (the
+// padded 64-step substitutions are fully unrolled), in place
 __global__ void __launch_bounds__(256) k_lu_panels(NewtonCell* nc, int nslots, int k0, int nchunks) {
     const int slot = blockIdx.y;
     if (slot >= nslots) return;
@@ -390,36 +395,40 @@ __global__ void __launch_bounds__(256) k_lu_panels(NewtonCell* nc, int nslots, i
     const int r0 = k0 + kb;
     if (r0 >= m) return;
     __shared__ float D[kNb][kNb + 1];
-    for (int idx = threadIdx.x; idx < kb * kb; idx += blockDim.x) {
-        const int i = idx / kb, j = idx % kb;
-        D[i][j] = N.J[(size_t)(k0 + i) * N.ld + k0 + j];
-    }
+    load_block_padded(N, k0, kb, D);
     __syncthreads();
     const int half = nchunks / 2;
+    float x[kNb];
     if ((int)blockIdx.x < half) {   // columns: forward substitution with the unit lower L11
         for (int col = r0 + blockIdx.x * blockDim.x + threadIdx.x; col < m; col += half * blockDim.x) {
-            float x[kNb];
-#pragma unroll 8
-            for (int i = 0; i < kNb; ++i) {
-                if (i >= kb) break;
-                float a = N.J[(size_t)(k0 + i) * N.ld + col];
+#pragma unroll
+            for (int i = 0; i < kNb; ++i) x[i] = i < kb ? N.J[(size_t)(k0 + i) * N.ld + col] : 0.0f;
+#pragma unroll
+            for (int i = 1; i < kNb; ++i) {
+                float a = x[i];
+#pragma unroll
                 for (int j = 0; j < i; ++j) a -= D[i][j] * x[j];
                 x[i] = a;
-                N.J[(size_t)(k0 + i) * N.ld + col] = a;
             }
+#pragma unroll
+            for (int i = 0; i < kNb; ++i)
+                if (i < kb) N.J[(size_t)(k0 + i) * N.ld + col] = x[i];
         }
     } else {                         // rows: x U11 = a
         for (int row = r0 + (blockIdx.x - half) * blockDim.x + threadIdx.x; row < m; row += half * blockDim.x) {
-            float* a = N.J + (size_t)row * N.ld + k0;
-            float x[kNb];
-#pragma unroll 8
+            float* ar = N.J + (size_t)row * N.ld + k0;
+#pragma unroll
+            for (int j = 0; j < kNb; ++j) x[j] = j < kb ? ar[j] : 0.0f;
+#pragma unroll
             for (int j = 0; j < kNb; ++j) {
-                if (j >= kb) break;
-                float s = a[j];
+                float s = x[j];
+#pragma unroll
                 for (int i = 0; i < j; ++i) s -= x[i] * D[i][j];
                 x[j] = s / D[j][j];
-                a[j] = x[j];
             }
+#pragma unroll
+            for (int j = 0; j < kNb; ++j)
+                if (j < kb) ar[j] = x[j];
         }
     }
 }
@@ -430,9 +439,9 @@ __device__ __forceinline__ uint32_t to_tf32(float f) {
     return r;
 }
 
-// A22 -= L21 U12 for one 128 x 128 tile of the trailing matrix; 8 warps as 2 x 4,
-// each a 64 x 32 block of 4 x 4 m16n8 tiles; K = the block width (<= 64).
-constexpr int kTile = 128;
+// A22 -= L21 U12 for one 64 x 128 tile of the trailing matrix; 8 warps as 2 x 4, each
+// a 32 x 32 block of 2 x 4 m16n8 tiles; K = the block width (<= 64).
+constexpr int kTileM = 64, kTileN = 128;
 __global__ void __launch_bounds__(256) k_lu_update(NewtonCell* nc, int nslots, int k0) {
     const int slot = blockIdx.z;
     if (slot >= nslots) return;
@@ -441,30 +450,29 @@ __global__ void __launch_bounds__(256) k_lu_update(NewtonCell* nc, int nslots, i
     if (!N.active || k0 >= m) return;
     const int kb = min(kNb, m - k0);
     const int r0 = k0 + kb;
-    const int tm = r0 + blockIdx.y * kTile, tn = r0 + blockIdx.x * kTile;
+    const int tm = r0 + blockIdx.y * kTileM, tn = r0 + blockIdx.x * kTileN;
     if (tm >= m || tn >= m) return;
     extern __shared__ float smu[];
-    float* As = smu;                       // [128][kNb + 4]: L21 rows tm.., columns k0..
-    float* Bs = smu + kTile * (kNb + 4);   // [kNb][128 + 8]: U12 rows k0.., columns tn..
-    const int lda = kNb + 4, ldb = kTile + 8;
-    for (int idx = threadIdx.x; idx < kTile * kNb; idx += blockDim.x) {
-        const int i = idx / kNb, k = idx % kNb;
+    const int lda = kNb + 4, ldb = kTileN + 8;
+    float* As = smu;                 // [64][kNb + 4]: L21 rows tm.., columns k0..
+    float* Bs = smu + kTileM * lda;  // [kNb][128 + 8]: U12 rows k0.., columns tn..
+    for (int idx = threadIdx.x; idx < kTileM * kNb; idx += blockDim.x) {
+        const int i = idx >> 6, k = idx & (kNb - 1);
         const int row = tm + i;
         As[i * lda + k] = (row < m && k < kb) ? N.J[(size_t)row * N.ld + k0 + k] : 0.0f;
     }
-    for (int idx = threadIdx.x; idx < kNb * kTile; idx += blockDim.x) {
-        const int k = idx / kTile, j = idx % kTile;
+    for (int idx = threadIdx.x; idx < kNb * kTileN; idx += blockDim.x) {
+        const int k = idx >> 7, j = idx & (kTileN - 1);
         const int col = tn + j;
         Bs[k * ldb + j] = (col < m && k < kb) ? N.J[(size_t)(k0 + k) * N.ld + col] : 0.0f;
     }
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int wm = (warp >> 2) * 64, wn = (warp & 3) * 32;   // warp block origin in the tile
+    const int wm = (warp >> 2) * 32, wn = (warp & 3) * 32;   // warp block origin in the tile
     const int g = lane >> 2, t = lane & 3;
-    float acc[4][4][4];
-    // load C (the trailing entries) into the accumulators
+    float acc[2][4][4];
 #pragma unroll
-    for (int mi = 0; mi < 4; ++mi)
+    for (int mi = 0; mi < 2; ++mi)
 #pragma unroll
         for (int ni = 0; ni < 4; ++ni) {
             const int rA = tm + wm + mi * 16 + g, cA = tn + wn + ni * 8 + 2 * t;
@@ -478,10 +486,11 @@ __global__ void __launch_bounds__(256) k_lu_update(NewtonCell* nc, int nslots, i
                 }
             }
         }
-    for (int ks = 0; ks < kNb; ks += 8) {
-        uint32_t af[4][4], bf[4][2];
 #pragma unroll
-        for (int mi = 0; mi < 4; ++mi) {
+    for (int ks = 0; ks < kNb; ks += 8) {
+        uint32_t af[2][4], bf[4][2];
+#pragma unroll
+        for (int mi = 0; mi < 2; ++mi) {
             const float* a = As + (wm + mi * 16) * lda + ks;
             // -L21: the product is subtracted
             af[mi][0] = to_tf32(-a[g * lda + t]);
@@ -496,7 +505,7 @@ __global__ void __launch_bounds__(256) k_lu_update(NewtonCell* nc, int nslots, i
             bf[ni][1] = to_tf32(b[(t + 4) * ldb + g]);
         }
 #pragma unroll
-        for (int mi = 0; mi < 4; ++mi)
+        for (int mi = 0; mi < 2; ++mi)
 #pragma unroll
             for (int ni = 0; ni < 4; ++ni) {
                 float* d = acc[mi][ni];
@@ -508,7 +517,7 @@ __global__ void __launch_bounds__(256) k_lu_update(NewtonCell* nc, int nslots, i
             }
     }
 #pragma unroll
-    for (int mi = 0; mi < 4; ++mi)
+    for (int mi = 0; mi < 2; ++mi)
 #pragma unroll
         for (int ni = 0; ni < 4; ++ni) {
             const int rA = tm + wm + mi * 16 + g, cA = tn + wn + ni * 8 + 2 * t;
@@ -525,67 +534,72 @@ __global__ void __launch_bounds__(256) k_lu_update(NewtonCell* nc, int nslots, i
 }
 
 // ===========================================================================
-// Triangular solves with the LU factors, z = U^-1 L^-1 r (FP32), one CTA per cell:
-// within a 64-row block the substitution runs on warp 0; the rows outside the
-// block are updated by the whole CTA
+// Triangular solves with the LU factors, z = U^-1 L^-1 r (FP32), blocked by 64 rows:
+// per block one CTA per cell solves the diagonal block, then a grid of CTAs
+// subtracts the block's contribution from the remaining rows (one warp per row,
+// the row's 64 entries read coalesced).
 // ===========================================================================
-constexpr int kSolveThreads = 512;
-__global__ void __launch_bounds__(kSolveThreads) k_lu_solve(NewtonCell* nc, int nslots) {
-    extern __shared__ float y[];   // [2n]
+__global__ void k_trsv_init(NewtonCell* nc, int nslots) {
+    NewtonCell& N = nc[blockIdx.y];
+    if (blockIdx.y >= nslots || !N.active) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * N.n; i += gridDim.x * blockDim.x) N.z[i] = (float)N.r[i];
+}
+
+// diagonal block b0: lower (unit) forward or upper backward substitution; the block is
+// staged in shared memory by the CTA, the substitution runs on warp 0
+__global__ void __launch_bounds__(256) k_trsv_diag(NewtonCell* nc, int nslots, int b0, int upper) {
     NewtonCell& N = nc[blockIdx.x];
     const int m = 2 * N.n;
-    if (blockIdx.x >= nslots || !N.active) return;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) y[i] = (float)N.r[i];
+    if (blockIdx.x >= nslots || !N.active || b0 >= m) return;
+    const int kb = min(kNb, m - b0), lane = threadIdx.x & 31;
+    __shared__ float T[kNb][kNb + 1];
+    __shared__ float y[kNb];
+    load_block_padded(N, b0, kb, T);
+    if (threadIdx.x < kNb) y[threadIdx.x] = threadIdx.x < kb ? N.z[b0 + threadIdx.x] : 0.0f;
+    __syncthreads();
+    if (threadIdx.x >= 32) return;
+    if (!upper) {
+        for (int i = 1; i < kb; ++i) {
+            float s = (lane < i ? T[i][lane] * y[lane] : 0.0f) + (lane + 32 < i ? T[i][lane + 32] * y[lane + 32] : 0.0f);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) y[i] -= s;
+            __syncwarp();
+        }
+    } else {
+        for (int i = kb - 1; i >= 0; --i) {
+            float s = (lane > i && lane < kb ? T[i][lane] * y[lane] : 0.0f) +
+                      (lane + 32 > i && lane + 32 < kb ? T[i][lane + 32] * y[lane + 32] : 0.0f);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) y[i] = (y[i] - s) / T[i][i];
+            __syncwarp();
+        }
+    }
+    for (int i = lane; i < kb; i += 32) N.z[b0 + i] = y[i];
+}
+
+// rows outside block b0 (below it for L, above it for U) -= their 64 entries of the block times y_block
+constexpr int kTrsvRows = 64;
+__global__ void __launch_bounds__(256) k_trsv_update(NewtonCell* nc, int nslots, int b0, int upper) {
+    NewtonCell& N = nc[blockIdx.y];
+    const int m = 2 * N.n;
+    if (blockIdx.y >= nslots || !N.active || b0 >= m) return;
+    const int kb = min(kNb, m - b0);
+    const int lo = upper ? 0 : b0 + kb, hi = upper ? b0 : m;
+    const int r0 = lo + blockIdx.x * kTrsvRows;
+    if (r0 >= hi) return;
+    __shared__ float yb[kNb];
+    if (threadIdx.x < kNb) yb[threadIdx.x] = threadIdx.x < kb ? N.z[b0 + threadIdx.x] : 0.0f;
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // forward: L (unit lower)
-    for (int b0 = 0; b0 < m; b0 += kNb) {
-        const int kb = min(kNb, m - b0);
-        if (warp == 0) {
-            for (int i = 1; i < kb; ++i) {
-                const float* Li = N.J + (size_t)(b0 + i) * N.ld + b0;
-                float s = 0.0f;
-                for (int j = lane; j < i; j += 32) s += Li[j] * y[b0 + j];
+    for (int i = r0 + warp; i < min(r0 + kTrsvRows, hi); i += 8) {
+        const float* Ai = N.J + (size_t)i * N.ld + b0;
+        float s = (lane < kb ? Ai[lane] * yb[lane] : 0.0f) + (lane + 32 < kb ? Ai[lane + 32] * yb[lane + 32] : 0.0f);
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                if (lane == 0) y[b0 + i] -= s;
-                __syncwarp();
-            }
-        }
-        __syncthreads();
-        for (int i = b0 + kb + threadIdx.x; i < m; i += blockDim.x) {
-            const float* Li = N.J + (size_t)i * N.ld + b0;
-            float s = 0.0f;
-            for (int j = 0; j < kb; ++j) s += Li[j] * y[b0 + j];
-            y[i] -= s;
-        }
-        __syncthreads();
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) N.z[i] -= s;
     }
-    // backward: U
-    const int nblk = (m + kNb - 1) / kNb;
-    for (int bi = nblk - 1; bi >= 0; --bi) {
-        const int b0 = bi * kNb, kb = min(kNb, m - b0);
-        if (warp == 0) {
-            for (int i = kb - 1; i >= 0; --i) {
-                const float* Ui = N.J + (size_t)(b0 + i) * N.ld + b0;
-                float s = 0.0f;
-                for (int j = i + 1 + lane; j < kb; j += 32) s += Ui[j] * y[b0 + j];
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                if (lane == 0) y[b0 + i] = (y[b0 + i] - s) / Ui[i];
-                __syncwarp();
-            }
-        }
-        __syncthreads();
-        for (int i = threadIdx.x; i < b0; i += blockDim.x) {
-            const float* Ui = N.J + (size_t)i * N.ld + b0;
-            float s = 0.0f;
-            for (int j = 0; j < kb; ++j) s += Ui[j] * y[b0 + j];
-            y[i] -= s;
-        }
-        __syncthreads();
-    }
-    for (int i = threadIdx.x; i < m; i += blockDim.x) N.z[i] = y[i];
 }
 
 // dx += z; r = -G - J dx in FP64 with J element by element (diagonal + the FP32 element
@@ -729,19 +743,14 @@ static int g_num_sms = 0;
 cudaError_t configure_newton(size_t max_smem, int num_sms) {
     g_num_sms = num_sms;
     cudaError_t e = cudaFuncSetAttribute((const void*)k_lu_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)(sizeof(float) * (kTile * (kNb + 4) + kNb * (kTile + 8))));
+                                         (int)(sizeof(float) * (kTileM * (kNb + 4) + kNb * (kTileN + 8))));
     if (e != cudaSuccess) return e;
     cudaFuncAttributes at;
-    if ((e = cudaFuncGetAttributes(&at, (const void*)k_lu_solve)) != cudaSuccess) return e;
-    if ((e = cudaFuncSetAttribute((const void*)k_lu_solve, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)(max_smem - at.sharedSizeBytes - 1024))) != cudaSuccess)
-        return e;
     if ((e = cudaFuncGetAttributes(&at, (const void*)k_newton_tangent)) != cudaSuccess) return e;
     return cudaFuncSetAttribute((const void*)k_newton_tangent, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)(max_smem - at.sharedSizeBytes - 1024));
 }
 
-size_t newton_solve_smem(int max_n) { return sizeof(float) * 2 * (size_t)max_n; }
 size_t newton_tangent_smem(int emax) { return sizeof(float) * 36 * (size_t)emax; }
 
 void launch_newton_residual(const CellDev* cells, const NewtonCell* nc, const int* cell_of_slot, int nslots, int max_n,
@@ -756,19 +765,34 @@ void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int
     k_newton_tangent<<<grid, kTanThreads, newton_tangent_smem(emax), st>>>(cells, nc, cell_slot, work, nwork, emax, dt);
 }
 void launch_newton_lu(NewtonCell* nc, int nslots, int max_m, cudaStream_t st) {
-    const size_t usm = sizeof(float) * (kTile * (kNb + 4) + kNb * (kTile + 8));
+    const size_t usm = sizeof(float) * (kTileM * (kNb + 4) + kNb * (kTileN + 8));
     for (int k0 = 0; k0 < max_m; k0 += kNb) {
         k_lu_diag<<<nslots, 256, 0, st>>>(nc, nslots, k0);
         const int rest = max_m - k0 - kNb;
         if (rest <= 0) break;
         const int half = std::max(1, std::min((rest + 255) / 256, 32));
         k_lu_panels<<<dim3(2 * half, nslots), 256, 0, st>>>(nc, nslots, k0, 2 * half);
-        const int tiles = (rest + kTile - 1) / kTile;
-        k_lu_update<<<dim3(tiles, tiles, nslots), 256, usm, st>>>(nc, nslots, k0);
+        k_lu_update<<<dim3((rest + kTileN - 1) / kTileN, (rest + kTileM - 1) / kTileM, nslots), 256, usm, st>>>(
+            nc, nslots, k0);
     }
 }
 void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, cudaStream_t st) {
-    k_lu_solve<<<nslots, kSolveThreads, newton_solve_smem(max_n), st>>>(nc, nslots);
+    const int m = 2 * max_n, nblk = (m + kNb - 1) / kNb;
+    k_trsv_init<<<dim3((unsigned)std::max(1, std::min((m + 255) / 256, 32)), (unsigned)nslots), 256, 0, st>>>(nc, nslots);
+    for (int b = 0; b < nblk; ++b) {   // forward, L
+        k_trsv_diag<<<nslots, 256, 0, st>>>(nc, nslots, b * kNb, 0);
+        const int rows = m - (b + 1) * kNb;
+        if (rows > 0)
+            k_trsv_update<<<dim3((unsigned)((rows + kTrsvRows - 1) / kTrsvRows), (unsigned)nslots), 256, 0, st>>>(
+                nc, nslots, b * kNb, 0);
+    }
+    for (int b = nblk - 1; b >= 0; --b) {   // backward, U
+        k_trsv_diag<<<nslots, 256, 0, st>>>(nc, nslots, b * kNb, 1);
+        const int rows = b * kNb;
+        if (rows > 0)
+            k_trsv_update<<<dim3((unsigned)((rows + kTrsvRows - 1) / kTrsvRows), (unsigned)nslots), 256, 0, st>>>(
+                nc, nslots, b * kNb, 1);
+    }
 }
 void launch_newton_refine(const CellDev* cells, NewtonCell* nc, const int* cell_slot, const WorkItem* work, int nwork,
                           int add_z, cudaStream_t st) {
