@@ -353,6 +353,8 @@ def run_ours(args):
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
                     "avg_launch_ms": round(avg_p, 4), "vertex_phase_avg_launch_ms": round(avg_v, 4)}
 
+        config2 = run_config2()
+        log(f"[bench] config 2: {config2}")
         newton = run_newton(args.newton_cells) if args.newton_cells > 0 else None
         if newton:
             log(f"[bench] newton: {newton}")
@@ -383,7 +385,7 @@ def run_ours(args):
             "mixed_vs_fp64_rel_displacement_error": max_err, "error_steps": err_steps,
             "element_assemblies_per_s": round(value / len(cells) * nt_total / world, 1),
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "serving": serving,
-            "newton": newton,
+            "newton": newton, "config2": config2,
             "clocks": clocks_info,
         }
     if dist:
@@ -467,6 +469,39 @@ def run_serving(seconds: float, rate: float = 200.0, budget_gb: float = 16.0, se
             "max_resident_cells": max(active_hist) if active_hist else 0}
 
 
+def run_config2(steps: int = 500, seed: int = 2):
+    """Config 2: one 20,000-vertex cell, 8,000 integrins with k(x) = k0 (1 + (x/x0)^2), k0 = 31 pN/nm,
+    x0 = 5 nm, shear modulus log-normal per element (median mu, sigma 0.3), 500 steps, in the FP64
+    form and in the mixed form (FP32 assembly); device time per step of each and the mixed
+    form's relative displacement error against the FP64 form."""
+    import torch
+    from wholecellfe_gb300 import capi, synth
+    from wholecellfe_gb300.params import default_params
+    rng = np.random.default_rng(seed)
+    x0, tri = synth.disk_mesh(20000, seed=seed)
+    p = default_params("k31")
+    p.force_law, p.poly_k0, p.poly_x0, p.linear_norm2d = 2, 31000.0, 0.005, 0
+    rho = np.zeros(len(x0))
+    rho[rng.choice(len(x0), size=8000, replace=False)] = p.rho_i_max
+    mu = p.mu * np.exp(0.3 * rng.standard_normal(len(tri)))
+    out = {}
+    for name, prec in (("fp64", capi.PREC_FP64), ("mixed", capi.PREC_MIXED)):
+        eng = capi.Engine(prec)
+        h = eng.add_cell(x0, tri, p, state=synth.initial_state(x0))
+        h.set_integrins(rho)
+        h.set_element_mu(mu)
+        eng.autotune(DT, 3)
+        r = timed_steps(eng, steps, DT)
+        out[name] = (h.get_state()[0], r["total_ms"] / steps, h.status())
+        eng.close()
+    u = out["fp64"][0] - x0
+    err = float(np.max(np.abs(out["mixed"][0] - out["fp64"][0])) / np.max(np.abs(u)))
+    return {"vertices": len(x0), "triangles": len(tri), "integrins": 8000, "steps": steps,
+            "fp64_ms_per_step": round(out["fp64"][1], 4), "mixed_ms_per_step": round(out["mixed"][1], 4),
+            "mixed_vs_fp64_rel_displacement_error": err,
+            "status": [out["fp64"][2], out["mixed"][2]]}
+
+
 def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4):
     """Config 4, bounded: implicit (Newton) steps of `ncells` cells with 1000-4000 vertices
     (uniform), dense 2N x 2N tangents, LU with TF32 tensor-core trailing updates, FP64
@@ -513,6 +548,9 @@ def run_phase(args):
     from wholecellfe_gb300 import capi, synth
     from wholecellfe_gb300.params import default_params
     torch.cuda.init()
+    if args.phase == "config2":
+        print(json.dumps(run_config2(max(1, min(args.steps, 500)))))
+        return
     if args.phase == "newton":
         print(json.dumps(run_newton(args.cells if args.cells != N_CELLS else 64, max(1, min(args.steps, 5)))))
         return
@@ -591,7 +629,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the Poisson arrival window of the serving measurement (0: skip)")
-    ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain", "newton"],
+    ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain", "newton", "config2"],
                     help="profiling aid: run only one timed loop (default shape, no autotune) and print its timing")
     ap.add_argument("--newton-cells", type=int, default=64,
                     help="cells of the bounded implicit-step (Newton, dense LU) measurement (0: skip)")

@@ -207,6 +207,11 @@ int wcfe_cell_eval_forces(wcfe_engine* eng, int32_t cell, const double* x, doubl
  * identical; wcfe_engine_autotune times both.  No counterpart in the reference. */
 int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind);
 
+/* Per-element shear modulus mu of the membrane [n_tri] (NULL restores params.mu for
+ * every element).  An extension without counterpart in the reference, which has one
+ * mu per material (UL:721-728); dropped when the topology changes. */
+int wcfe_cell_set_element_mu(wcfe_engine* e, int32_t id, const double* mu);
+
 /* ---- synthetic stepping of every live cell (no El Topo) ----------------- */
 /* nsteps full explicit steps of every live cell: predict, updateFA, updateForces.
  * All cells advance in one launch per phase; runs asynchronously on the engine stream. */

@@ -31,7 +31,8 @@ def build(force: bool = False) -> str:
 
 
 class Mesh(C.Structure):
-    _fields_ = [("nv", C.c_int32), ("nt", C.c_int32), ("tri", _i), ("vt_ptr", _i), ("vt_idx", _i), ("bnd", _u8)]
+    _fields_ = [("nv", C.c_int32), ("nt", C.c_int32), ("tri", _i), ("vt_ptr", _i), ("vt_idx", _i), ("bnd", _u8),
+                ("mu_e", _d)]
 
 
 class Cell(C.Structure):
@@ -74,7 +75,8 @@ def lib():
 class OMesh:
     """Mesh arrays kept alive together with the ctypes struct that points into them."""
 
-    def __init__(self, tri, n_vert, vt_ptr=None, vt_idx=None, bnd=None):
+    def __init__(self, tri, n_vert, vt_ptr=None, vt_idx=None, bnd=None, mu_e=None):
+        """mu_e: optional per-element shear modulus (an extension: the reference has one per material)."""
         from wholecellfe_gb300 import synth
         self.tri = np.ascontiguousarray(tri, dtype=np.int32)
         self.nv = int(n_vert)
@@ -85,8 +87,9 @@ class OMesh:
         self.vt_ptr = np.ascontiguousarray(vt_ptr, dtype=np.int32)
         self.vt_idx = np.ascontiguousarray(vt_idx, dtype=np.int32)
         self.bnd = np.ascontiguousarray(bnd, dtype=np.uint8)
+        self.mu_e = None if mu_e is None else f64(mu_e).copy()
         self.s = Mesh(self.nv, len(self.tri), ip(self.tri), ip(self.vt_ptr), ip(self.vt_idx),
-                      self.bnd.ctypes.data_as(_u8))
+                      self.bnd.ctypes.data_as(_u8), dp(self.mu_e))
 
 
 # ---- thin wrappers ----------------------------------------------------------

@@ -44,6 +44,9 @@ typedef struct wo_mesh {
     const int32_t* vt_ptr;  /* [nv+1] vertex -> triangle map, mesh order */
     const int32_t* vt_idx;
     const uint8_t* bnd;     /* [nv] NonDestructiveTriMesh::m_is_boundary_vertex */
+    const double* mu_e;     /* [nt] optional per-element shear modulus of a cell (NULL: p->mu); an
+                               extension without reference counterpart (the reference has one mu per
+                               material, UL:721-728) */
 } wo_mesh;
 
 /* ------------------------------------------------------------------ */
@@ -372,8 +375,9 @@ WO_API void wo_calc_res(const wo_mesh* m, const double* X, const double* x, cons
         if (cA) { cAe[0] = cA[a]; cAe[1] = cA[b]; cAe[2] = cA[c]; }
         if (cC) { cCe[0] = cC[a]; cCe[1] = cC[b]; cCe[2] = cC[c]; }
         wo_elem_out o;
+        const double mu_el = (mat == 1 && m->mu_e) ? m->mu_e[e] : mu;
         wo_element(X + 3 * a, X + 3 * b, X + 3 * c, x + 3 * a, x + 3 * b, x + 3 * c, ea + 6 * a, ea + 6 * b, ea + 6 * c,
-                   cAe, cCe, dt_real, mat, mu, p, t_act, centroid ? centroid : zero3, &o);
+                   cAe, cCe, dt_real, mat, mu_el, p, t_act, centroid ? centroid : zero3, &o);
         int idx[3] = {a, b, c};
         for (int i = 0; i < 3; ++i) {
             for (int k = 0; k < 3; ++k) Res[idx[i] * 3 + k] += o.Re[i * 3 + k];

@@ -123,3 +123,19 @@ def test_philox_known_answers():
         o = (C.c_uint32 * 4)()
         L.wo_philox4x32_10(c, k, o)
         assert tuple(o) == want
+
+
+def test_oracle_per_element_mu_uniform_equals_params_mu():
+    """The per-element modulus of the oracle with every element at params.mu is the
+    uniform-modulus oracle, bit for bit (the extension does not move the pinned path)."""
+    from wholecellfe_gb300 import synth
+    from wholecellfe_gb300.params import default_params
+    x0, tri = synth.disk_mesh(300, seed=3)
+    p = default_params("k1")
+    st = synth.initial_state(x0, perturb=1.0, seed=3)
+    a = O.OCell(O.OMesh(tri, len(x0)), st, p, t=0.3)
+    b = O.OCell(O.OMesh(tri, len(x0), mu_e=np.full(len(tri), p.mu)), st, p, t=0.3)
+    a.steps(5, 5e-5)
+    b.steps(5, 5e-5)
+    for u, w in zip(a.state(), b.state()):
+        assert np.array_equal(u, w)

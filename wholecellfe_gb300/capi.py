@@ -84,6 +84,7 @@ SIGNATURES = {
     "wcfe_server_result": (C.c_int, [C.c_void_p, C.c_int64, _d, _d]),
     "wcfe_server_step_times": (C.c_int64, [C.c_void_p, _d, C.c_int64]),
     "wcfe_engine_set_patch_kernel": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_cell_set_element_mu": (C.c_int, [C.c_void_p, C.c_int32, _d]),
     "wcfe_engine_step_implicit": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_void_p]),
     "wcfe_cell_newton_tangent": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _d, C.POINTER(C.c_float), _d]),
     "wcfe_debug_lu_solve": (C.c_int, [C.c_int32, C.POINTER(C.c_float), _d, C.POINTER(C.c_float)]),
@@ -323,6 +324,11 @@ class Cell:
 
     def set_params(self, p: Params):
         check(load().wcfe_cell_set_params(self.eng.h, self.id, C.byref(p)), "wcfe_cell_set_params")
+
+    def set_element_mu(self, mu):
+        """Per-element shear modulus [n_tri] (None: the cell's params.mu everywhere)."""
+        check(load().wcfe_cell_set_element_mu(self.eng.h, self.id, None if mu is None else dp(f64(mu))),
+              "wcfe_cell_set_element_mu")
 
     def set_integrins(self, rho):
         check(load().wcfe_cell_set_integrins(self.eng.h, self.id, dp(None if rho is None else f64(rho))),

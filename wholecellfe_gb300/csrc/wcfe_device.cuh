@@ -62,6 +62,7 @@ struct CellDev {
     double* cC;
     double4* fau;
     const double* rho_w;        // optional per-vertex integrin density (nullptr: rho_i_max); floats in a mixed engine
+    const double* mu_e;         // optional per-element shear modulus (nullptr: prm.mu); floats in a mixed engine
     const int4* tri;
     const int32_t* vt_ptr;
     const uint16_t* vc_code;    // (slot << 2) | corner, slot local to the owner's patch

@@ -94,6 +94,8 @@ struct Cell {
     size_t sub_bytes = 0;
     double* rho_dev = nullptr;      // integrin density (floats for a mixed engine)
     size_t rho_size = 0;            // its allocation
+    double* mu_dev = nullptr;       // per-element shear modulus (floats for a mixed engine)
+    size_t mu_size = 0;
     CellDev dev{};
     int32_t sub_nv = 0, sub_nt = 0;
     std::vector<int32_t> sub_tri;
@@ -426,6 +428,12 @@ int upload_substrate(wcfe_engine* e, Cell* c) {
 }
 
 void free_cell(wcfe_engine* e, Cell* c) {
+    if (c->mu_dev) {
+        void* p = c->mu_dev;
+        size_t b = c->mu_size;
+        dev_free(e, p, b);
+        c->mu_dev = nullptr;
+    }
     dev_free(e, c->state_block, c->state_bytes);
     dev_free(e, c->patch_block, c->patch_bytes);
     dev_free(e, c->sub_block, c->sub_bytes);
@@ -480,6 +488,7 @@ int sync_tables(wcfe_engine* e, double dt = -1.0) {
         c->dev.prm = c->prm;
         c->dev.pf = make_paramf(c->prm);
         c->dev.rho_w = c->rho_dev;
+        c->dev.mu_e = c->mu_dev;
         c->dev.ap_thresh = e->table_dt > 0 ? ap_threshold(c->prm, e->table_dt) : 0.0;
         c->dev.hoff = e->total_nv;
         e->total_nv += c->topo.nv;
@@ -805,6 +814,12 @@ int wcfe_cell_set_topology(wcfe_engine* e, int32_t id, int32_t nv, int32_t nt, c
         size_t b = c->rho_size;
         dev_free(e, p, b);
         c->rho_dev = nullptr;
+    }
+    if (c->mu_dev) {
+        void* p = c->mu_dev;
+        size_t b = c->mu_size;
+        dev_free(e, p, b);
+        c->mu_dev = nullptr;
     }
     e->version++;
     invalidate_graph(e);
@@ -1711,6 +1726,42 @@ int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x) {
     cudaFree(blk);
     if (ce != cudaSuccess) return fail(std::string("CUDA: ") + cudaGetErrorString(ce), WCFE_ERR_CUDA);
     if (flag != 0.0) return fail("zero or non-finite pivot", WCFE_ERR_STATE);
+    return WCFE_OK;
+}
+
+int wcfe_cell_set_element_mu(wcfe_engine* e, int32_t id, const double* mu) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    const int nt = c->topo.nt;
+    if (!mu) {
+        if (c->mu_dev) {
+            void* p = c->mu_dev;
+            size_t b = c->mu_size;
+            dev_free(e, p, b);
+            c->mu_dev = nullptr;
+        }
+    } else {
+        for (int t = 0; t < nt; ++t)
+            if (!(mu[t] > 0) || !std::isfinite(mu[t])) return fail("shear moduli must be positive", WCFE_ERR_ARG);
+        if (!c->mu_dev) {
+            void* p = nullptr;
+            int r = dev_alloc(e, &p, rho_bytes(nt));
+            if (r) return r;
+            c->mu_dev = (double*)p;
+            c->mu_size = rho_bytes(nt);
+        }
+        if (e->prec == WCFE_PREC_MIXED) {
+            std::vector<float> f(nt);
+            for (int t = 0; t < nt; ++t) f[t] = (float)mu[t];
+            CK(cudaMemcpyAsync(c->mu_dev, f.data(), sizeof(float) * nt, cudaMemcpyHostToDevice, e->stream));
+        } else {
+            CK(cudaMemcpyAsync(c->mu_dev, mu, sizeof(double) * nt, cudaMemcpyHostToDevice, e->stream));
+        }
+        CK(cudaStreamSynchronize(e->stream));
+    }
+    e->version++;
+    invalidate_graph(e);
     return WCFE_OK;
 }
 

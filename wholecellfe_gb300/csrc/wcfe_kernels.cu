@@ -413,7 +413,8 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
                 }
                 ElemOut64 o;
                 double rA[3], rC[3];
-                element_fp64<MODE == PP_RESIDUAL>(Xe, xe, ee, cA3, cC3, p, p.mu, t_act, 0, cen, a.dt_real, o, rA, rC);
+                const double mu_el = c.mu_e ? c.mu_e[e] : p.mu;
+                element_fp64<MODE == PP_RESIDUAL>(Xe, xe, ee, cA3, cC3, p, mu_el, t_act, 0, cen, a.dt_real, o, rA, rC);
 #pragma unroll
                 for (int k = 0; k < 3; ++k)
 #pragma unroll

@@ -507,7 +507,9 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
 #pragma unroll
                 for (int m = 0; m < kRec; ++m) r[k][m] = rec[kRec * (size_t)id[k] + m];
             Elem2 o;
-            element2d(r, q, o);
+            ElemParams qe = q;
+            if (c.mu_e) qe.mu = __ldg(reinterpret_cast<const float*>(c.mu_e) + e);
+            element2d(r, qe, o);
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 smf[(2 * k + 0) * emax + j] = o.re[k][0];
@@ -964,7 +966,9 @@ __global__ void __launch_bounds__(kConsumers + 32) k_patch_mixed_staged(MixedArg
 #pragma unroll
                 for (int m = 0; m < kRec; ++m) r[kk][m] = rec_s[kRec * id[kk] + m];
             Elem2 o;
-            element2d(r, q, o);
+            ElemParams qe = q;
+            if (c.mu_e) qe.mu = __ldg(reinterpret_cast<const float*>(c.mu_e) + c.patch_elems[pt.z + j]);
+            element2d(r, qe, o);
 #pragma unroll
             for (int kk = 0; kk < 3; ++kk) {
                 smf[(2 * kk + 0) * emax + j] = o.re[kk][0];

@@ -258,8 +258,10 @@ __global__ void __launch_bounds__(kTanThreads) k_newton_tangent(const CellDev* _
                 ay.d[2 * k + 1] = 1.0f / 3.0f;
             }
             Dual<6> re[3][2];
+            TanParams qe = q;
+            if (c.mu_e) qe.mu = (float)c.mu_e[e];
             element_re_planar((float)(Xd[1][0] - Xd[0][0]), (float)(Xd[1][1] - Xd[0][1]), (float)(Xd[2][0] - Xd[0][0]),
-                              (float)(Xd[2][1] - Xd[0][1]), d1x, d1y, d2x, d2y, ev, ax, ay, q, re);
+                              (float)(Xd[2][1] - Xd[0][1]), d1x, d1y, d2x, d2y, ev, ax, ay, qe, re);
             float* o = ke_s + 36 * j;
 #pragma unroll
             for (int k = 0; k < 3; ++k)
