@@ -207,6 +207,23 @@ int wcfe_cell_eval_forces(wcfe_engine* eng, int32_t cell, const double* x, doubl
  * identical; wcfe_engine_autotune times both.  No counterpart in the reference. */
 int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind);
 
+/* Couple cell `cell` to a deformable substrate simulated by the same FP64 engine:
+ * `substrate` is another cell of the engine holding the substrate mesh and state
+ * (A10; its params.mu is the substrate modulus, 1e6 in the reference, UL:726; its
+ * other params give damp and rho; it has no active stress, integrins, boundary
+ * terms or drag).  Each wcfe_engine_step then runs, per step: the cell's bond
+ * kinetics on the substrate's step-start positions and predicted displacement
+ * (updateFA UL:2026-2174), the bond reactions onto every substrate triangle
+ * containing each anchor at the substrate's predicted positions
+ * (calculateForce_FA_subs UL:1305-1475, accumulated in 2^-40 fixed point so the
+ * sum is order-independent), and the substrate's update with them
+ * (updateForces_Explicit, substrate overload UL:429-504).  Point location uses a
+ * grid over the substrate's current positions; triangles that later move by more
+ * than grid_margin may be missed (couple again to rebuild).  substrate < 0
+ * uncouples.  The other stepping entry points refuse engines with coupled
+ * substrates.  Status bit 32: a reaction beyond the fixed-point range. */
+int wcfe_cell_couple_substrate(wcfe_engine* e, int32_t cell, int32_t substrate, double grid_margin);
+
 /* Per-element shear modulus mu of the membrane [n_tri] (NULL restores params.mu for
  * every element).  An extension without counterpart in the reference, which has one
  * mu per material (UL:721-728); dropped when the topology changes. */

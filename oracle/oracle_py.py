@@ -168,6 +168,17 @@ def update_forces(m: OMesh, X, x, V, Vh, A, ea, cA, cC, fau, dt, dt_real, t_tot,
     return V, A, ea, outs
 
 
+def update_forces_subs(ms: OMesh, Xs, xs, Vs, Vhs, As, eas, dt, dt_real, t_tot, fau, cC, xcell, mc: OMesh,
+                       p: Params, rho_w=None):
+    """Substrate overload of updateForces_Explicit (UL:429-504): returns updated (Vs, As, eas)."""
+    Vs = f64(Vs).copy(); As = f64(As).copy(); eas = f64(eas).copy()
+    lib().wo_update_forces_subs(C.byref(ms.s), dp(f64(Xs)), dp(f64(xs)), dp(Vs), dp(f64(Vhs)), dp(As), dp(eas),
+                                C.c_double(dt), C.c_double(dt_real), C.c_double(t_tot), dp(f64(fau)), dp(f64(cC)),
+                                dp(f64(xcell)), C.byref(mc.s), C.byref(p), dp(None if rho_w is None else f64(rho_w)),
+                                None, None)
+    return Vs, As, eas
+
+
 def force_fa_subs(ms: OMesh, Xs, xs, cC, xcell, fau, mc: OMesh, p: Params, rho_w=None):
     F = np.zeros((ms.nv, 3))
     lib().wo_force_fa_subs(C.byref(ms.s), dp(f64(Xs)), dp(f64(xs)), dp(f64(cC)), dp(f64(xcell)), dp(f64(fau)),

@@ -85,6 +85,7 @@ SIGNATURES = {
     "wcfe_server_step_times": (C.c_int64, [C.c_void_p, _d, C.c_int64]),
     "wcfe_engine_set_patch_kernel": (C.c_int, [C.c_void_p, C.c_int32]),
     "wcfe_cell_set_element_mu": (C.c_int, [C.c_void_p, C.c_int32, _d]),
+    "wcfe_cell_couple_substrate": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
     "wcfe_engine_step_implicit": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_void_p]),
     "wcfe_cell_newton_tangent": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _d, C.POINTER(C.c_float), _d]),
     "wcfe_debug_lu_solve": (C.c_int, [C.c_int32, C.POINTER(C.c_float), _d, C.POINTER(C.c_float)]),
@@ -324,6 +325,11 @@ class Cell:
 
     def set_params(self, p: Params):
         check(load().wcfe_cell_set_params(self.eng.h, self.id, C.byref(p)), "wcfe_cell_set_params")
+
+    def couple_substrate(self, sub, margin: float = 0.05):
+        """Couple this cell to a deformable substrate cell of the same engine (None: uncouple)."""
+        check(load().wcfe_cell_couple_substrate(self.eng.h, self.id, -1 if sub is None else sub.id, margin),
+              "wcfe_cell_couple_substrate")
 
     def set_element_mu(self, mu):
         """Per-element shear modulus [n_tri] (None: the cell's params.mu everywhere)."""

@@ -92,8 +92,33 @@ __device__ __forceinline__ void spring_force(const wcfe_params& p, double ux, do
     }
 }
 
+// Containment test of point (px, py, pz) in triangle (p1, p2, p3) with barycentric weights
+// (UL:2061-2100 and UL:1317-1465 use the same construction), unfused
+__device__ __forceinline__ bool tri_contains(const double4& p1, const double4& p2, const double4& p3, double px, double py,
+                                             double pz, double w[3]) {
+    double e1x = xs(p2.x, p1.x), e1y = xs(p2.y, p1.y), e1z = xs(p2.z, p1.z);
+    double e2x = xs(p3.x, p1.x), e2y = xs(p3.y, p1.y), e2z = xs(p3.z, p1.z);
+    double nx = xs(xm(e1y, e2z), xm(e1z, e2y)), ny = xs(xm(e1z, e2x), xm(e1x, e2z)), nz = xs(xm(e1x, e2y), xm(e1y, e2x));
+    double At = xm(0.5, xnorm3(nx, ny, nz));
+    double epx = xs(px, p1.x), epy = xs(py, p1.y), epz = xs(pz, p1.z);
+    double ax = xs(xm(e1y, epz), xm(e1z, epy)), ay = xs(xm(e1z, epx), xm(e1x, epz)), az = xs(xm(e1x, epy), xm(e1y, epx));
+    double A3 = -1;
+    if (az >= 0) A3 = xm(0.5, xnorm3(ax, ay, az));
+    double bx = xs(xm(epy, e2z), xm(epz, e2y)), by = xs(xm(epz, e2x), xm(epx, e2z)), bz = xs(xm(epx, e2y), xm(epy, e2x));
+    double A2 = -1;
+    if (bz >= 0) A2 = xm(0.5, xnorm3(bx, by, bz));
+    double A1 = xs(xs(At, A2), A3);
+    if (A1 >= 0 && A2 >= 0 && A3 >= 0) {
+        w[0] = A1 / At; w[1] = A2 / At; w[2] = A3 / At;
+        return true;
+    }
+    return false;
+}
+
 // Point location in the substrate (UL:2061-2100): the last containing triangle wins.
-__device__ __forceinline__ int locate(const SubDev& s, double px, double py, double pz, double w[3]) {
+// Positions P: the substrate's own X, or those of a coupled substrate cell.
+__device__ __forceinline__ int locate_in(const SubDev& s, const double4* __restrict__ P, double px, double py, double pz,
+                                         double w[3]) {
     int gx = (int)floor((px - s.ox) * s.inv_h), gy = (int)floor((py - s.oy) * s.inv_h);
     if (!(gx >= 0 && gx < s.gx && gy >= 0 && gy < s.gy)) return -1;
     int g = gy * s.gx + gx;
@@ -101,25 +126,16 @@ __device__ __forceinline__ int locate(const SubDev& s, double px, double py, dou
     for (int k = s.cell_ptr[g]; k < s.cell_ptr[g + 1]; ++k) {
         int e = s.cell_tri[k];
         int4 t = s.tri[e];
-        double4 p1 = ld4(s.X + t.x), p2 = ld4(s.X + t.y), p3 = ld4(s.X + t.z);
-        double e1x = xs(p2.x, p1.x), e1y = xs(p2.y, p1.y), e1z = xs(p2.z, p1.z);
-        double e2x = xs(p3.x, p1.x), e2y = xs(p3.y, p1.y), e2z = xs(p3.z, p1.z);
-        double nx = xs(xm(e1y, e2z), xm(e1z, e2y)), ny = xs(xm(e1z, e2x), xm(e1x, e2z)), nz = xs(xm(e1x, e2y), xm(e1y, e2x));
-        double At = xm(0.5, xnorm3(nx, ny, nz));
-        double epx = xs(px, p1.x), epy = xs(py, p1.y), epz = xs(pz, p1.z);
-        double ax = xs(xm(e1y, epz), xm(e1z, epy)), ay = xs(xm(e1z, epx), xm(e1x, epz)), az = xs(xm(e1x, epy), xm(e1y, epx));
-        double A3 = -1;
-        if (az >= 0) A3 = xm(0.5, xnorm3(ax, ay, az));
-        double bx = xs(xm(epy, e2z), xm(epz, e2y)), by = xs(xm(epz, e2x), xm(epx, e2z)), bz = xs(xm(epx, e2y), xm(epy, e2x));
-        double A2 = -1;
-        if (bz >= 0) A2 = xm(0.5, xnorm3(bx, by, bz));
-        double A1 = xs(xs(At, A2), A3);
-        if (A1 >= 0 && A2 >= 0 && A3 >= 0) {
+        double wk[3];
+        if (tri_contains(ld4(P + t.x), ld4(P + t.y), ld4(P + t.z), px, py, pz, wk)) {
             found = e;
-            w[0] = A1 / At; w[1] = A2 / At; w[2] = A3 / At;
+            w[0] = wk[0]; w[1] = wk[1]; w[2] = wk[2];
         }
     }
     return found;
+}
+__device__ __forceinline__ int locate(const SubDev& s, double px, double py, double pz, double w[3]) {
+    return locate_in(s, s.X, px, py, pz, w);
 }
 
 // boundary neighbours and outward normal (UL:1489-1543)

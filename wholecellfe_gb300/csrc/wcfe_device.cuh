@@ -23,6 +23,7 @@ namespace wcfe {
 
 constexpr int kK1Threads = 256;  // largest vertex-phase block (vertices per block = threads = CellDev::vb)
 
+struct CellDev;
 struct SubDev {                 // substrate mesh + uniform grid for point location
     int32_t nv, nt;
     const double4* X;           // previous positions (point location)
@@ -33,6 +34,10 @@ struct SubDev {                 // substrate mesh + uniform grid for point locat
     double ox, oy, inv_h;
     int32_t gx, gy;
     int32_t moving;             // 0: x == X (rigid), the interpolated displacement is exactly 0
+    // deformable substrate simulated by the same engine (A10): its table entry, whose step-start
+    // positions and predicted displacement replace X and x above, and its reaction accumulator
+    const CellDev* scell;
+    unsigned long long* fext;   // [nv_s][4] fixed-point (2^-40) reaction forces of the cell's bonds
 };
 
 // FP32 copies of the per-cell constants the mixed form uses per vertex, converted
@@ -52,6 +57,8 @@ struct CellDev {
     int32_t nv, nt, nb, np, nk1;
     int32_t vb;                 // vertices per vertex-phase block (= its thread count); 2 vb elements per block
     int32_t has_sub;
+    int32_t material;           // 1 cell membrane, 2 substrate (mat 2: no active stress, integrins, boundary
+                                // terms or drag; external forces from fext_in)
     int64_t hoff;               // first vertex of this cell in the engine's packed host exchange arrays
     double4* pos[2];
     double4* vel;
@@ -86,6 +93,7 @@ struct CellDev {
     double* clk;                // [0] simulation time at the start of the next step
     unsigned long long* ap;     // [0] calculateForce_AP calls made (the AP counter of the next step)
     uint32_t* status;
+    unsigned long long* fext_in;  // substrate cells: [nv][4] fixed-point reactions accumulated this step
     double ap_thresh;           // ap_rate dt exp(-ap_rate dt) for the engine's current dt (UL:1552)
     SubDev sub;
     wcfe_params prm;

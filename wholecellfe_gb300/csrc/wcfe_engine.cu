@@ -96,6 +96,15 @@ struct Cell {
     size_t rho_size = 0;            // its allocation
     double* mu_dev = nullptr;       // per-element shear modulus (floats for a mixed engine)
     size_t mu_size = 0;
+    // deformable substrate coupling (A10): a cell names its substrate cell; the substrate cell
+    // owns the reaction accumulator; the cell owns the point-location grid over the substrate
+    int32_t couple_sub = -1;
+    bool is_sub = false;
+    void* fext_block = nullptr;
+    size_t fext_bytes = 0;
+    void* cgrid_block = nullptr;
+    size_t cgrid_bytes = 0;
+    SubGrid cgrid;
     CellDev dev{};
     int32_t sub_nv = 0, sub_nt = 0;
     std::vector<int32_t> sub_tri;
@@ -151,6 +160,7 @@ struct wcfe_engine {
     int vblock = 256;             // vertices (threads) per vertex-phase block
     int patch_kernel = 1;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
     int cap_ne = 0, cap_nvp = 0, cap_nh = 0, cap_nc = 0;   // largest patch over the cells (staging plan)
+    int n2_sub = 0;               // patch work items of substrate cells, at the end of k2 (second launch)
     bool tuned = false;
     // graphs
     bool use_graphs = false;
@@ -428,6 +438,8 @@ int upload_substrate(wcfe_engine* e, Cell* c) {
 }
 
 void free_cell(wcfe_engine* e, Cell* c) {
+    dev_free(e, c->fext_block, c->fext_bytes);
+    dev_free(e, c->cgrid_block, c->cgrid_bytes);
     if (c->mu_dev) {
         void* p = c->mu_dev;
         size_t b = c->mu_size;
@@ -463,6 +475,8 @@ int ensure_dev(T** p, size_t* cap, size_t n) {
     return WCFE_OK;
 }
 
+int table_index(wcfe_engine* e, int32_t id);
+
 int sync_tables(wcfe_engine* e, double dt = -1.0) {
     if (dt > 0 && dt != e->table_dt) {
         e->table_dt = dt;
@@ -483,12 +497,15 @@ int sync_tables(wcfe_engine* e, double dt = -1.0) {
         e->cap_nh = std::max(e->cap_nh, P.max_nh);
         e->cap_nc = std::max(e->cap_nc, P.max_nc);
     }
+    std::vector<WorkItem> k2_sub;
     for (auto& kv : e->cells) {
         Cell* c = kv.second.get();
         c->dev.prm = c->prm;
         c->dev.pf = make_paramf(c->prm);
         c->dev.rho_w = c->rho_dev;
         c->dev.mu_e = c->mu_dev;
+        c->dev.material = c->is_sub ? 2 : 1;
+        c->dev.fext_in = (unsigned long long*)c->fext_block;
         c->dev.ap_thresh = e->table_dt > 0 ? ap_threshold(c->prm, e->table_dt) : 0.0;
         c->dev.hoff = e->total_nv;
         e->total_nv += c->topo.nv;
@@ -496,10 +513,24 @@ int sync_tables(wcfe_engine* e, double dt = -1.0) {
         e->order.push_back(c->id);
         e->table.push_back(c->dev);
         for (int b = 0; b < c->dev.nk1; ++b) e->k1.push_back({ti, b});
-        for (int p = 0; p < c->dev.np; ++p) e->k2.push_back({ti, p});
+        // substrate cells take their reactions after every cell's patch phase: a second launch
+        for (int p = 0; p < c->dev.np; ++p) (c->is_sub ? k2_sub : e->k2).push_back({ti, p});
     }
+    e->n2_sub = (int)k2_sub.size();
+    e->k2.insert(e->k2.end(), k2_sub.begin(), k2_sub.end());
     int r;
     if ((r = ensure_dev(&e->d_table, &e->d_table_cap, std::max<size_t>(e->table.size(), 1)))) return r;
+    // coupled cells point at their substrate's table entry (device address, known now)
+    for (size_t ti = 0; ti < e->table.size(); ++ti) {
+        const Cell* c = e->cells.at(e->order[ti]).get();
+        if (c->couple_sub < 0) continue;
+        auto it = e->cells.find(c->couple_sub);
+        if (it == e->cells.end()) return fail("coupled substrate cell no longer exists", WCFE_ERR_STATE);
+        const int ts = table_index(e, c->couple_sub);
+        SubDev& sd = e->table[ti].sub;
+        sd.scell = e->d_table + ts;
+        sd.fext = (unsigned long long*)it->second->fext_block;
+    }
     if ((r = ensure_dev(&e->d_k1, &e->d_k1_cap, std::max<size_t>(e->k1.size(), 1)))) return r;
     if ((r = ensure_dev(&e->d_k2, &e->d_k2_cap, std::max<size_t>(e->k2.size(), 1)))) return r;
     if (!e->table.empty())
@@ -559,7 +590,12 @@ int enqueue_step(wcfe_engine* e, const WorkItem* k1, int n1, const WorkItem* k2,
     if (tv) cudaEventRecord(tv[0], e->stream);
     vphase(e, e->d_table, k1, n1, dt, VP_PREDICT | VP_UPDATE_FA | rec_flag(e), g1, e->stream);
     if (tv) cudaEventRecord(tv[1], e->stream);
-    patch_step(e, k2, n2, dt, dt, apt, std::numeric_limits<double>::quiet_NaN(), 0);
+    const int nsub = (k2 == e->d_k2 && n2 == (int)e->k2.size()) ? e->n2_sub : 0;
+    patch_step(e, k2, n2 - nsub, dt, dt, apt, std::numeric_limits<double>::quiet_NaN(), 0);
+    if (nsub > 0) {   // substrate cells, after the reactions of their coupled cells
+        patch_step(e, k2 + (n2 - nsub), nsub, dt, dt, apt, std::numeric_limits<double>::quiet_NaN(), 0);
+        e->launches += 1;
+    }
     if (tv) {
         cudaEventRecord(tv[2], e->stream);
         e->timed_steps++;
@@ -782,6 +818,12 @@ int wcfe_cell_create(wcfe_engine* e, int32_t nv, int32_t nt, const int32_t* tri,
 int wcfe_cell_destroy(wcfe_engine* e, int32_t id) {
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    // drop substrate couplings that involve this cell
+    std::vector<int32_t> users;
+    for (auto& kv : e->cells)
+        if (kv.second->couple_sub == id) users.push_back(kv.first);
+    for (int32_t u : users) wcfe_cell_couple_substrate(e, u, -1, 0.0);
+    if (c->couple_sub >= 0) wcfe_cell_couple_substrate(e, id, -1, 0.0);
     free_cell(e, c);
     e->cells.erase(id);
     e->version++;
@@ -1217,6 +1259,8 @@ int wcfe_engine_step(wcfe_engine* e, int32_t nsteps, double dt) {
 
 int wcfe_engine_step_cells(wcfe_engine* e, const int32_t* ids, int32_t ncells, int32_t nsteps, double dt) {
     if (!e || !ids || ncells <= 0 || nsteps < 0 || !(dt > 0)) return fail("bad argument", WCFE_ERR_ARG);
+    if (e && std::any_of(e->cells.begin(), e->cells.end(), [](const auto& kv) { return kv.second->is_sub; }))
+        return fail("coupled substrates step only through wcfe_engine_step", WCFE_ERR_STATE);
     CK(cudaSetDevice(e->device));
     int r = sync_tables(e, dt);
     if (r) return r;
@@ -1357,6 +1401,8 @@ int64_t wcfe_engine_total_vertices(wcfe_engine* e) {
 }
 
 int wcfe_engine_predict(wcfe_engine* e, double dt, double* x_pred) {
+    if (e && std::any_of(e->cells.begin(), e->cells.end(), [](const auto& kv) { return kv.second->is_sub; }))
+        return fail("coupled substrates step only through wcfe_engine_step", WCFE_ERR_STATE);
     if (!e || !x_pred || !(dt > 0)) return fail("bad argument", WCFE_ERR_ARG);
     if (e->cells.empty()) return WCFE_OK;
     CK(cudaSetDevice(e->device));
@@ -1374,6 +1420,8 @@ int wcfe_engine_predict(wcfe_engine* e, double dt, double* x_pred) {
 }
 
 int wcfe_engine_update(wcfe_engine* e, double dt, double dt_real, const double* x_new) {
+    if (e && std::any_of(e->cells.begin(), e->cells.end(), [](const auto& kv) { return kv.second->is_sub; }))
+        return fail("coupled substrates step only through wcfe_engine_step", WCFE_ERR_STATE);
     if (!e || !x_new || !(dt > 0) || !(dt_real > 0)) return fail("bad argument", WCFE_ERR_ARG);
     if (e->cells.empty()) return WCFE_OK;
     CK(cudaSetDevice(e->device));
@@ -1630,6 +1678,8 @@ int wcfe_engine_step_implicit(wcfe_engine* e, int32_t nsteps, double dt, double 
     if (!e || nsteps < 0 || !(dt > 0) || !(newton_rtol > 0) || max_newton < 1) return fail("bad argument", WCFE_ERR_ARG);
     if (e->prec != WCFE_PREC_FP64)
         return fail("the implicit step runs on an FP64 engine (WCFE_PREC_FP64)", WCFE_ERR_STATE);
+    if (e && std::any_of(e->cells.begin(), e->cells.end(), [](const auto& kv) { return kv.second->is_sub; }))
+        return fail("coupled substrates step only through wcfe_engine_step", WCFE_ERR_STATE);
     if (stats) std::memset(stats, 0, sizeof *stats);
     if (e->cells.empty() || nsteps == 0) return WCFE_OK;
     CK(cudaSetDevice(e->device));
@@ -1762,6 +1812,76 @@ int wcfe_cell_set_element_mu(wcfe_engine* e, int32_t id, const double* mu) {
     }
     e->version++;
     invalidate_graph(e);
+    return WCFE_OK;
+}
+
+int wcfe_cell_couple_substrate(wcfe_engine* e, int32_t id, int32_t sub_id, double grid_margin) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    if (e->prec != WCFE_PREC_FP64) return fail("substrate coupling runs on an FP64 engine", WCFE_ERR_STATE);
+    CK(cudaSetDevice(e->device));
+    CK(cudaStreamSynchronize(e->stream));
+    // undo a previous coupling of this cell
+    if (c->couple_sub >= 0) {
+        const int32_t old = c->couple_sub;
+        c->couple_sub = -1;
+        dev_free(e, c->cgrid_block, c->cgrid_bytes);
+        std::memset(&c->dev.sub, 0, sizeof(SubDev));
+        c->dev.has_sub = 0;
+        bool still = false;
+        for (auto& kv : e->cells) still = still || kv.second->couple_sub == old;
+        auto it = e->cells.find(old);
+        if (!still && it != e->cells.end()) {
+            it->second->is_sub = false;
+            dev_free(e, it->second->fext_block, it->second->fext_bytes);
+        }
+    }
+    e->version++;
+    invalidate_graph(e);
+    if (sub_id < 0) return WCFE_OK;
+    Cell* s = find(e, sub_id);
+    if (!s || s == c) return fail("bad substrate cell", WCFE_ERR_ARG);
+    if (c->is_sub || s->couple_sub >= 0) return fail("a substrate cell cannot be coupled to a substrate", WCFE_ERR_ARG);
+    if (!(grid_margin >= 0)) return fail("bad grid margin", WCFE_ERR_ARG);
+    // point-location grid over the substrate's current positions
+    const int ns = s->topo.nv, nts = s->topo.nt;
+    std::vector<double> xs(3 * (size_t)ns);
+    int r = wcfe_cell_get_state(e, sub_id, xs.data(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr);
+    if (r) return r;
+    build_subgrid(c->cgrid, ns, nts, s->topo.tri.data(), xs.data(), grid_margin);
+    const SubGrid& G = c->cgrid;
+    const size_t b0 = align_up(sizeof(int32_t) * G.cell_ptr.size());
+    const size_t bytes = b0 + align_up(sizeof(int32_t) * std::max<size_t>(G.cell_tri.size(), 1));
+    if ((r = dev_alloc(e, &c->cgrid_block, bytes))) return r;
+    c->cgrid_bytes = bytes;
+    char* b = (char*)c->cgrid_block;
+    CK(cudaMemcpyAsync(b, G.cell_ptr.data(), sizeof(int32_t) * G.cell_ptr.size(), cudaMemcpyHostToDevice, e->stream));
+    if (!G.cell_tri.empty())
+        CK(cudaMemcpyAsync(b + b0, G.cell_tri.data(), sizeof(int32_t) * G.cell_tri.size(), cudaMemcpyHostToDevice,
+                           e->stream));
+    if (!s->fext_block) {
+        if ((r = dev_alloc(e, &s->fext_block, sizeof(unsigned long long) * 4 * (size_t)ns))) return r;
+        s->fext_bytes = sizeof(unsigned long long) * 4 * (size_t)ns;
+        CK(cudaMemsetAsync(s->fext_block, 0, s->fext_bytes, e->stream));
+    }
+    CK(cudaStreamSynchronize(e->stream));
+    SubDev& sd = c->dev.sub;
+    std::memset(&sd, 0, sizeof sd);
+    sd.nv = ns;
+    sd.nt = nts;
+    sd.tri = s->dev.tri;
+    sd.cell_ptr = (const int32_t*)b;
+    sd.cell_tri = (const int32_t*)(b + b0);
+    sd.ox = G.ox;
+    sd.oy = G.oy;
+    sd.inv_h = G.inv_h;
+    sd.gx = G.gx;
+    sd.gy = G.gy;
+    sd.moving = 1;
+    c->dev.has_sub = 1;
+    c->couple_sub = sub_id;
+    s->is_sub = true;
+    e->version++;
     return WCFE_OK;
 }
 

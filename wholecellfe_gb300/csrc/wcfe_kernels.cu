@@ -93,12 +93,34 @@ __global__ void __launch_bounds__(kK1Threads) k_vertex_phase(const CellDev* __re
                 double4 t = ld4v(xo + v);
                 xn[0] = t.x; xn[1] = t.y; xn[2] = t.z;
             }
-            if (flags & VP_UPDATE_FA) {
+            if ((flags & VP_UPDATE_FA) && c.material != 2) {
                 const wcfe_params& p = c.prm;
                 double4 f = ld4v(c.fau + v);
                 double cu0 = xs(xn[0], Xv.x), cu1 = xs(xn[1], Xv.y), cu2 = xs(xn[2], Xv.z);
                 double su0 = 0, su1 = 0, su2 = 0;
-                if (c.has_sub && c.sub.moving) {
+                if (c.has_sub && c.sub.scell) {
+                    // deformable substrate of the same engine: locate in its step-start positions; its
+                    // displacement over the step is its own predict (the same arithmetic as its vertex phase)
+                    const CellDev& sc = *c.sub.scell;
+                    const double4* __restrict__ Xs = sc.pos[sc.ctl[0]];
+                    double wgt[3];
+                    int e = locate_in(c.sub, Xs, xs(Xv.x, f.x), xs(Xv.y, f.y), xs(Xv.z, f.z), wgt);
+                    if (e >= 0) {
+                        int4 t = c.sub.tri[e];
+                        const int id[3] = {t.x, t.y, t.z};
+                        double d[3][3];
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) {
+                            const double4 Xk = ld4(Xs + id[k]);
+                            double vh[3], xk[3];
+                            predict_vertex(Xk, ld4(sc.vel + id[k]), ld4(sc.acc + id[k]), dt, hdt, vh, xk);
+                            d[k][0] = xk[0] - Xk.x; d[k][1] = xk[1] - Xk.y; d[k][2] = xk[2] - Xk.z;
+                        }
+                        su0 = wgt[0] * d[0][0] + wgt[1] * d[1][0] + wgt[2] * d[2][0];
+                        su1 = wgt[0] * d[0][1] + wgt[1] * d[1][1] + wgt[2] * d[2][1];
+                        su2 = wgt[0] * d[0][2] + wgt[1] * d[1][2] + wgt[2] * d[2][2];
+                    }
+                } else if (c.has_sub && c.sub.moving) {
                     double wgt[3];
                     int e = locate(c.sub, xs(Xv.x, f.x), xs(Xv.y, f.y), xs(Xv.z, f.z), wgt);
                     if (e >= 0) {
@@ -127,19 +149,6 @@ __global__ void __launch_bounds__(kK1Threads) k_vertex_phase(const CellDev* __re
                 }
                 c.cC[v] = cn;
                 st4(c.fau + v, u0, u1, u2);
-            }
-            if (flags & VP_RECORD) {
-                // FP32 element inputs of the mixed form: float-float X, the step displacement, the strain
-                const float hx = (float)Xv.x, hy = (float)Xv.y, hz = (float)Xv.z;
-                const float lx = (float)(Xv.x - (double)hx), ly = (float)(Xv.y - (double)hy), lz = (float)(Xv.z - (double)hz);
-                const float ux = (float)(xn[0] - Xv.x), uy = (float)(xn[1] - Xv.y), uz = (float)(xn[2] - Xv.z);
-                const double2* e2 = reinterpret_cast<const double2*>(c.ea[par] + 6 * (size_t)v);
-                const double2 q0 = e2[0], q1 = e2[1], q2 = e2[2];
-                float4* r = c.rec + 4 * (size_t)v;
-                r[0] = make_float4(hx, hy, hz, ux);
-                r[1] = make_float4(lx, ly, lz, uy);
-                r[2] = make_float4(uz, (float)q0.x, (float)q0.y, (float)q1.x);
-                r[3] = make_float4((float)q1.y, (float)q2.x, (float)q2.y, 0.0f);
             }
         }
         if (flags & VP_NOAREA) continue;
@@ -414,7 +423,9 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
                 ElemOut64 o;
                 double rA[3], rC[3];
                 const double mu_el = c.mu_e ? c.mu_e[e] : p.mu;
-                element_fp64<MODE == PP_RESIDUAL>(Xe, xe, ee, cA3, cC3, p, mu_el, t_act, 0, cen, a.dt_real, o, rA, rC);
+                // substrate (mat 2, UL:989-1176): no active stress
+                element_fp64<MODE == PP_RESIDUAL>(Xe, xe, ee, cA3, cC3, p, mu_el, c.material == 2 ? 0.0 : t_act,
+                                                  c.material == 2 ? 1 : 0, cen, a.dt_real, o, rA, rC);
 #pragma unroll
                 for (int k = 0; k < 3; ++k)
 #pragma unroll
@@ -464,11 +475,41 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
             spring_force(p, f4.x, f4.y, f4.z, fs, &bell);
             const double rho = c.rho_w ? c.rho_w[v] : p.rho_i_max;
             const double cCv = c.cC[v];
+            const bool subs = c.material == 2;
             double Ffa[3];
 #pragma unroll
-            for (int r = 0; r < 3; ++r) Ffa[r] = -cCv * fs[r] * Asum * rho;
+            for (int r = 0; r < 3; ++r) Ffa[r] = subs ? 0.0 : -cCv * fs[r] * Asum * rho;
+            if (MODE == PP_STEP && !subs && c.has_sub && c.sub.scell) {
+                // reaction of this vertex's bonds on a deformable substrate (calculateForce_FA_subs
+                // UL:1305-1475): at the anchor x - fa_u, onto every containing triangle of the
+                // substrate's predicted positions, by barycentric weight; fixed-point sums (2^-40) so
+                // the total does not depend on the order of the atomic adds
+                const CellDev& sc = *c.sub.scell;
+                const double4* __restrict__ xs_s = sc.pos[sc.ctl[0] ^ 1];
+                const double Px = xs(xi[0], f4.x), Py = xs(xi[1], f4.y), Pz = xs(xi[2], f4.z);
+                const SubDev& g = c.sub;
+                const int gx = (int)floor((Px - g.ox) * g.inv_h), gy = (int)floor((Py - g.oy) * g.inv_h);
+                if (gx >= 0 && gx < g.gx && gy >= 0 && gy < g.gy) {
+                    const int gc = gy * g.gx + gx;
+                    for (int k = g.cell_ptr[gc]; k < g.cell_ptr[gc + 1]; ++k) {
+                        const int4 t = g.tri[g.cell_tri[k]];
+                        double w[3];
+                        if (!tri_contains(ld4v(xs_s + t.x), ld4v(xs_s + t.y), ld4v(xs_s + t.z), Px, Py, Pz, w)) continue;
+                        const int id[3] = {t.x, t.y, t.z};
+#pragma unroll
+                        for (int q = 0; q < 3; ++q)
+#pragma unroll
+                            for (int r = 0; r < 3; ++r) {
+                                const double val = cCv * fs[r] * w[q] * Asum * rho;
+                                if (!(fabs(val) < 4.0e6)) atomicOr(c.status, 32u);
+                                atomicAdd(g.fext + 4 * (size_t)id[q] + r,
+                                          (unsigned long long)__double2ll_rn(val * 1099511627776.0));
+                            }
+                    }
+                }
+            }
             double Fap[3] = {0, 0, 0}, Fb[3] = {0, 0, 0}, Far[3] = {0, 0, 0};
-            const int rank = c.bnd_rank[v];
+            const int rank = subs ? -1 : c.bnd_rank[v];
             if (rank >= 0) {
                 double x1[3], x2[3];
                 if (boundary_frame(c, xp, rank, xi, x1, x2)) {
@@ -527,10 +568,22 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
             const double Vo[3] = {V4.x, V4.y, V4.z};
             double An[3], Vn[3];
             const double md = p.damp * MM * p.rho, imr = 1.0 / (MM * p.rho), iMM = 1.0 / MM;
+            if (subs) {
+                // substrate update (updateForces_Explicit, substrate overload UL:429-504):
+                // f = F_FA_subs - Res, no drag; the reactions are consumed and cleared
 #pragma unroll
-            for (int r = 0; r < 3; ++r) {
-                double f = -p.drag * vh[r] + Fb[r] + Fap[r] + Ffa[r] + Far[r] - R[r];
-                An[r] = (f - md * Vo[r]) * imr;
+                for (int r = 0; r < 3; ++r) {
+                    unsigned long long* q = c.fext_in + 4 * (size_t)v + r;
+                    const double fr = (double)(long long)*q * (1.0 / 1099511627776.0);
+                    *q = 0ull;
+                    An[r] = ((fr - R[r]) - md * Vo[r]) * imr;
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    double f = -p.drag * vh[r] + Fb[r] + Fap[r] + Ffa[r] + Far[r] - R[r];
+                    An[r] = (f - md * Vo[r]) * imr;
+                }
             }
             const bool half = a.dt_real > a.dt / 2.0;
 #pragma unroll

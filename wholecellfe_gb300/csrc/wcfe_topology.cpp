@@ -198,7 +198,9 @@ std::string build_patches(Patches& P, const Topology& T, int32_t emax) {
     return "";
 }
 
-void build_subgrid(SubGrid& G, int32_t nv, int32_t nt, const int32_t* tri, const double* X) {
+// margin: extra width around the domain and every triangle's box, so that triangles that
+// move by less than it are still found in the grid cells of the points they contain
+void build_subgrid(SubGrid& G, int32_t nv, int32_t nt, const int32_t* tri, const double* X, double margin) {
     double lo[2] = {1e300, 1e300}, hi[2] = {-1e300, -1e300};
     for (int v = 0; v < nv; ++v)
         for (int c = 0; c < 2; ++c) {
@@ -207,7 +209,7 @@ void build_subgrid(SubGrid& G, int32_t nv, int32_t nt, const int32_t* tri, const
         }
     double span = std::max(hi[0] - lo[0], hi[1] - lo[1]);
     if (!(span > 0)) span = 1.0;
-    double pad = 1e-9 * span;
+    double pad = 1e-9 * span + std::max(margin, 0.0);
     lo[0] -= pad; lo[1] -= pad; hi[0] += pad; hi[1] += pad;
     int g = std::max(1, (int)std::ceil(std::sqrt((double)nt) / 1.5));
     double h = std::max(hi[0] - lo[0], hi[1] - lo[1]) / g;

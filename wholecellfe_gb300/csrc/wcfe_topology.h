@@ -47,6 +47,6 @@ struct SubGrid {
     std::vector<int32_t> cell_ptr, cell_tri;
 };
 // Uniform grid over the substrate triangles' (slightly padded) bounding boxes.
-void build_subgrid(SubGrid& G, int32_t nv, int32_t nt, const int32_t* tri, const double* X);
+void build_subgrid(SubGrid& G, int32_t nv, int32_t nt, const int32_t* tri, const double* X, double margin = 0.0);
 
 }  // namespace wcfe
