@@ -502,7 +502,7 @@ def run_config2(steps: int = 500, seed: int = 2):
             "status": [out["fp64"][2], out["mixed"][2]]}
 
 
-def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4):
+def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(256, 0)):
     """Config 4, bounded: implicit (Newton) steps of `ncells` cells with 1000-4000 vertices
     (uniform), dense 2N x 2N tangents, LU with TF32 tensor-core trailing updates, FP64
     residual and refinement to 1e-10.  Reports cell-steps/s, Newton iterations, the
@@ -512,6 +512,7 @@ def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4):
     from wholecellfe_gb300.params import default_params
     rng = np.random.default_rng(seed)
     eng = capi.Engine(capi.PREC_FP64)
+    eng.set_lu(*lu)
     sizes = []
     for i in range(ncells):
         n = int(rng.integers(1000, 4001))
@@ -530,15 +531,18 @@ def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4):
     eng.sync()
     wall = time.perf_counter() - t0
     eng.close()
-    lu_flops_per_iter = sum((2.0 / 3.0) * (2 * n) ** 3 for n in sizes)
     iters = st["newton_iters"]   # Newton updates over the timed steps (all cells in lockstep)
     return {"cells": ncells, "vertices": "uniform [1000, 4000]", "steps": steps,
+            "lu": {"outer_block": lu[0], "updates": ["tcgen05", "mma.sync"][lu[1]]},
             "cell_steps_per_s": round(ncells * steps / wall, 2), "ms_per_step": round(wall / steps * 1e3, 2),
             "newton_iters_per_step": iters / steps, "max_refine_passes": st["max_refine_iters"],
             "max_rel_residual": st["max_rel_residual"], "max_refine_rel_residual": st["max_refine_rel_residual"],
             "unconverged_cell_steps": st["unconverged"], "rounding_floor_exits": st["floor_exits"],
-            "lu_tflop_per_s": round(lu_flops_per_iter * iters / wall / 1e12, 2),
-            "timing": "host wall clock around wcfe_engine_step_implicit (it synchronises per Newton iteration)"}
+            "lu_ms_per_step": round(st["lu_ms"] / steps, 2),
+            "lu_tflop_per_s": round(st["lu_gflop"] / st["lu_ms"], 2) if st["lu_ms"] > 0 else None,
+            "lu_share_of_step": round(st["lu_ms"] / (wall * 1e3), 3),
+            "timing": "host wall clock around wcfe_engine_step_implicit (it synchronises per Newton iteration); "
+                      "LU: CUDA events around each factorisation, TF32 flops 2/3 (2N)^3 per factored cell"}
 
 
 def run_phase(args):
@@ -552,7 +556,8 @@ def run_phase(args):
         print(json.dumps(run_config2(max(1, min(args.steps, 500)))))
         return
     if args.phase == "newton":
-        print(json.dumps(run_newton(args.cells if args.cells != N_CELLS else 64, max(1, min(args.steps, 5)))))
+        lu = tuple(int(v) for v in args.lu.split(","))
+        print(json.dumps(run_newton(args.cells if args.cells != N_CELLS else 64, max(1, min(args.steps, 5)), lu=lu)))
         return
     if args.phase == "plain":
         x0, tri = synth.disk_mesh(2000, seed=1)
@@ -631,6 +636,7 @@ def main():
                     help="length of the Poisson arrival window of the serving measurement (0: skip)")
     ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain", "newton", "config2"],
                     help="profiling aid: run only one timed loop (default shape, no autotune) and print its timing")
+    ap.add_argument("--lu", default="256,0", help="--phase newton: LU outer block and kind (0 tcgen05, 1 mma.sync)")
     ap.add_argument("--newton-cells", type=int, default=64,
                     help="cells of the bounded implicit-step (Newton, dense LU) measurement (0: skip)")
     ap.add_argument("--shape", default="", help="with --phase: patch threads,elements (default: the engine's)")

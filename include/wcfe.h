@@ -331,15 +331,26 @@ typedef struct wcfe_newton_stats {
     int32_t floor_exits;               /* cell-steps that stopped at the residual's rounding floor above rtol */
     double max_rel_residual;           /* largest final |G|inf / force scale */
     double max_refine_rel_residual;    /* largest final |J dx + G|inf / |G|inf of a linear solve */
+    double lu_ms;                      /* device time of the dense factorisations (CUDA events) */
+    double lu_gflop;                   /* their work, 2/3 (2N)^3 per factored cell, in GFLOP */
 } wcfe_newton_stats;
 
 int wcfe_engine_step_implicit(wcfe_engine* e, int32_t nsteps, double dt, double newton_rtol, int32_t max_newton,
                               wcfe_newton_stats* stats);
 
+/* The implicit step's dense LU.  block: the outer block width, 64 or 256 (default): the
+ * trailing matrix takes one update per outer block with K = block.  kind 0 (default):
+ * trailing updates on the tcgen05 tensor cores (TMA-fed, TF32, accumulators in TMEM);
+ * kind 1: the mma.sync TF32 updates (block must be 64).  FP64 engines; results agree
+ * to TF32 rounding, and the refinement takes every solve to the same tolerance. */
+int wcfe_engine_set_lu(wcfe_engine* e, int32_t block, int32_t kind);
+
 /* Factor the dense m x m matrix A (row-major, FP32, m even) with the implicit step's
  * LU (no pivoting; TF32 tensor-core trailing updates) and solve A x = b once
  * (unrefined).  Device 0; for tests of the factorisation itself. */
 int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x);
+/* The same with the LU variant of wcfe_engine_set_lu. */
+int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* x, int32_t block, int32_t kind);
 
 /* The dense tangent J (2N x 2N, row-major, FP32) of cell `id` at positions x [n][3]
  * with the cell's state as step start, and the mass/damping diagonal [n]. */

@@ -154,8 +154,12 @@ def test_implicit_refuses_mixed_engine():
     e.close()
 
 
+LU_VARIANTS = [(256, 0), (64, 0), (64, 1)]   # (outer block, kind): tcgen05 two-level, tcgen05, mma.sync
+
+
+@pytest.mark.parametrize("block,kind", LU_VARIANTS)
 @pytest.mark.parametrize("m", [2, 64, 130, 512, 2050])
-def test_dense_lu_solve(m):
+def test_dense_lu_solve(m, block, kind):
     """The LU factorisation on its own (no refinement): A = m I + U(-1, 1) has off-diagonal
     weight comparable to the diagonal's, so every block, panel and tensor-core tile of the
     factorisation shows in x; the error is at the TF32 level of the trailing updates."""
@@ -163,9 +167,42 @@ def test_dense_lu_solve(m):
     A = rng.uniform(-1.0, 1.0, (m, m)) + m * np.eye(m)
     A32 = A.astype(np.float32)
     b = rng.uniform(-1.0, 1.0, m)
-    x = capi.debug_lu_solve(A32, b).astype(np.float64)
+    x = capi.debug_lu_solve(A32, b, block, kind).astype(np.float64)
     ref = np.linalg.solve(A32.astype(np.float64), b)
     assert np.max(np.abs(x - ref)) / np.max(np.abs(ref)) < 3e-3
     # the off-diagonal part matters: dropping it is far off
     diag_only = b / np.diag(A32)
     assert np.max(np.abs(diag_only - ref)) / np.max(np.abs(ref)) > 1e-2
+
+
+@pytest.mark.parametrize("m", [258, 770])
+def test_dense_lu_tcgen05_matches_mma_sync(m):
+    """The tcgen05 updates (two-level, K = 256) and the mma.sync updates (K = 64) factor the
+    same matrix to the same solution within TF32 rounding; a matrix whose off-diagonal part
+    dominates x makes a wrong tile visible."""
+    rng = np.random.default_rng(m + 1)
+    A = (rng.uniform(-1.0, 1.0, (m, m)) + 0.25 * m * np.eye(m)).astype(np.float32)
+    b = rng.uniform(-1.0, 1.0, m)
+    ref = np.linalg.solve(A.astype(np.float64), b)
+    xs = [capi.debug_lu_solve(A, b, blk, kind).astype(np.float64) for blk, kind in LU_VARIANTS]
+    for x in xs:
+        assert np.max(np.abs(x - ref)) / np.max(np.abs(ref)) < 1e-2
+    assert np.max(np.abs(xs[0] - xs[2])) / np.max(np.abs(ref)) < 1e-2
+
+
+def test_implicit_step_lu_variants_agree():
+    """The implicit step with each LU variant: the refinement takes every solve to 1e-10, so
+    the converged states agree to the Newton tolerance."""
+    x0, tri, st, p, t = _cell(300, 31)
+    out = []
+    for block, kind in LU_VARIANTS:
+        e = capi.Engine(capi.PREC_FP64)
+        e.set_lu(block, kind)
+        h = e.add_cell(x0, tri, p, state=st, t=t)
+        stats = e.step_implicit(2, DT, rtol=1e-11, max_newton=8)
+        assert stats["unconverged"] == 0 and h.status() == 0, stats
+        out.append(h.get_state()[0])
+        e.close()
+    u = out[0] - st[0]
+    for x in out[1:]:
+        assert np.max(np.abs(x - out[0])) / np.max(np.abs(u)) < 1e-9

@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libwcfe.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["wcfe_kernels.cu", "wcfe_mixed.cu", "wcfe_engine.cu", "wcfe_server.cu", "wcfe_topology.cpp",
-           "wcfe_noalloc.cu", "wcfe_newton.cu"]
+           "wcfe_noalloc.cu", "wcfe_newton.cu", "wcfe_lu_tc.cu"]
 
 
 def nvcc() -> str:

@@ -24,7 +24,8 @@ PREC_FP64, PREC_MIXED = 0, 1
 
 class NewtonStats(C.Structure):
     _fields_ = [("newton_iters", C.c_int32), ("max_refine_iters", C.c_int32), ("unconverged", C.c_int32),
-                ("floor_exits", C.c_int32), ("max_rel_residual", C.c_double), ("max_refine_rel_residual", C.c_double)]
+                ("floor_exits", C.c_int32), ("max_rel_residual", C.c_double), ("max_refine_rel_residual", C.c_double),
+                ("lu_ms", C.c_double), ("lu_gflop", C.c_double)]
 
 
 class Request(C.Structure):
@@ -89,6 +90,9 @@ SIGNATURES = {
     "wcfe_engine_step_implicit": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_void_p]),
     "wcfe_cell_newton_tangent": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _d, C.POINTER(C.c_float), _d]),
     "wcfe_debug_lu_solve": (C.c_int, [C.c_int32, C.POINTER(C.c_float), _d, C.POINTER(C.c_float)]),
+    "wcfe_debug_lu_solve_with": (C.c_int, [C.c_int32, C.POINTER(C.c_float), _d, C.POINTER(C.c_float), C.c_int32,
+                                           C.c_int32]),
+    "wcfe_engine_set_lu": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "wcfe_area_tot_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "wcfe_debug_topology": (C.c_int, [C.c_int32, C.c_int32, _i, _i, _i, _u8, C.c_int32, _i, _i, _i, _i, C.c_int32, _i,
                                       _i, C.c_int32, _i, C.c_int32, C.POINTER(C.c_uint16)]),
@@ -141,13 +145,20 @@ def debug_patch_staging(tri, n_vert, emax=320):
                 max_ne=int(mx[0]), max_nvp=int(mx[1]), max_nh=int(mx[2]), max_nc=int(mx[3]))
 
 
-def debug_lu_solve(A, b):
-    """The implicit step's dense LU (TF32 trailing updates) and one unrefined solve."""
+def debug_lu_solve(A, b, block: int | None = None, kind: int = 0):
+    """The implicit step's dense LU (TF32 trailing updates) and one unrefined solve.
+    block None: the default LU; else the outer block width (64, 256) and kind (0 tcgen05,
+    1 mma.sync) of wcfe_engine_set_lu."""
     A = np.ascontiguousarray(A, np.float32)
     b = np.ascontiguousarray(b, np.float64)
     x = np.zeros(len(b), np.float32)
-    check(load().wcfe_debug_lu_solve(len(b), A.ctypes.data_as(C.POINTER(C.c_float)), dp(b),
-                                     x.ctypes.data_as(C.POINTER(C.c_float))), "wcfe_debug_lu_solve")
+    fp = C.POINTER(C.c_float)
+    if block is None:
+        check(load().wcfe_debug_lu_solve(len(b), A.ctypes.data_as(fp), dp(b), x.ctypes.data_as(fp)),
+              "wcfe_debug_lu_solve")
+    else:
+        check(load().wcfe_debug_lu_solve_with(len(b), A.ctypes.data_as(fp), dp(b), x.ctypes.data_as(fp), block, kind),
+              "wcfe_debug_lu_solve_with")
     return x
 
 
@@ -275,6 +286,10 @@ class Engine:
 
     def set_shape(self, threads: int, emax: int):
         check(load().wcfe_engine_set_shape(self.h, threads, emax), "wcfe_engine_set_shape")
+
+    def set_lu(self, block: int = 256, kind: int = 0):
+        """The implicit step's LU: outer block width 64 or 256; kind 0 tcgen05, 1 mma.sync (block 64)."""
+        check(load().wcfe_engine_set_lu(self.h, block, kind), "wcfe_engine_set_lu")
 
     def set_patch_kernel(self, kind: int):
         """Mixed engines: 0 staged patch kernel where it fits, 1 plain (default)."""

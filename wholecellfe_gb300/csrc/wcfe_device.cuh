@@ -17,6 +17,8 @@
 #pragma once
 #include <cstdint>
 
+#include <cuda.h>
+
 #include "../../include/wcfe.h"
 
 namespace wcfe {
@@ -146,6 +148,23 @@ struct NewtonCell {
     double* norms;       // [8]: |G|inf, force scale, |r|inf, non-finite or zero pivot flag, |dx|inf of the
                          //      last update, |d|inf
     int n, ld, active, pad;
+    float* Ut;           // [2n][utld] transposed U rows of the current outer LU block (tensor-core operand)
+    int utld, pad2;
+};
+
+// TMA descriptors of one cell's dense LU: J (fp32, 2n x 2n, row stride ld) and Ut
+// (2n rows x utld), both read as boxes of 32 columns x 128 rows, 128-byte swizzled
+struct LuMaps {
+    CUtensorMap jmap;
+    CUtensorMap umap;
+};
+
+// One trailing-update launch of the blocked LU: per cell, C[rows, cols] -= J[rows, ka:ka+K]
+// Ut[cols, kb:kb+K]^T over up to two regions, each bound clamped to the cell's 2n (a
+// negative upper bound means 2n)
+struct LuUpdateArgs {
+    int rlo[2], rhi[2], clo[2], chi[2];
+    int nreg, ka, kb, K;
 };
 
 struct WorkItem {               // one block of a phase: (cell index into the table, block/patch index)

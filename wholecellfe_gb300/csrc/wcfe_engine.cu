@@ -44,7 +44,17 @@ void launch_newton_residual(const CellDev* cells, const NewtonCell* nc, const in
                             double dt, cudaStream_t st);
 void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int* cell_slot, const WorkItem* work,
                            int nwork, int emax, double dt, cudaStream_t st);
-void launch_newton_lu(NewtonCell* nc, int nslots, int max_m, cudaStream_t st);
+const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots, int max_m, const LuMaps* maps,
+                             int* d_prefix, int nb, int kind, cudaStream_t st);
+void lu_tc_attributes(int* regs, int* max_threads);
+std::string lu_attr_note() {
+    int regs = 0, mt = 0;
+    lu_tc_attributes(&regs, &mt);
+    return " (tensor-core update kernel: " + std::to_string(regs) + " registers, at most " + std::to_string(mt) +
+           " threads per block)";
+}
+size_t lu_prefix_capacity(int nslots, int max_m);
+int encode_lu_maps(const NewtonCell* h, int nslots, LuMaps* out);
 void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, cudaStream_t st);
 void launch_newton_refine(const CellDev* cells, NewtonCell* nc, const int* cell_slot, const WorkItem* work, int nwork,
                           int add_z, cudaStream_t st);
@@ -159,6 +169,7 @@ struct wcfe_engine {
     int patch_emax = 320;
     int vblock = 256;             // vertices (threads) per vertex-phase block
     int patch_kernel = 1;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
+    int lu_nb = 256, lu_kind = 0; // implicit step's LU: outer block width, 0 tcgen05 / 1 mma.sync updates
     int cap_ne = 0, cap_nvp = 0, cap_nh = 0, cap_nc = 0;   // largest patch over the cells (staging plan)
     int n2_sub = 0;               // patch work items of substrate cells, at the end of k2 (second launch)
     bool tuned = false;
@@ -1310,6 +1321,14 @@ int wcfe_engine_set_shape(wcfe_engine* e, int32_t threads, int32_t emax) {
     return WCFE_OK;
 }
 
+int wcfe_engine_set_lu(wcfe_engine* e, int32_t block, int32_t kind) {
+    if (!e || (block != 64 && block != 256) || kind < 0 || kind > 1 || (kind == 1 && block != 64))
+        return fail("bad argument", WCFE_ERR_ARG);
+    e->lu_nb = block;
+    e->lu_kind = kind;
+    return WCFE_OK;
+}
+
 int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind) {
     if (!e || kind < 0 || kind > 1) return fail("bad argument", WCFE_ERR_ARG);
     e->patch_kernel = kind;
@@ -1448,12 +1467,15 @@ struct NewtonPlan {
     NewtonCell* d_cells = nullptr;
     int* d_ident = nullptr;          // slot s <-> table index s
     unsigned int* d_tickets = nullptr;
-    double* norms = nullptr;         // [nslots][4]
+    double* norms = nullptr;         // [nslots][8]
+    LuMaps* d_maps = nullptr;        // [nslots] TMA descriptors of J and Ut
+    int* d_prefix = nullptr;         // per-launch tile prefix sums of the LU's trailing updates
     double *res = nullptr, *rea = nullptr, *mm = nullptr, *f4 = nullptr, *fext = nullptr;
     int max_n = 0;
 };
 
 size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+constexpr int kLuUtld = 256;   // Ut row length: the widest outer LU block
 
 // one device block for every cell of the table: packed residual and force arrays, per cell
 // J, element tangents and vectors
@@ -1466,7 +1488,8 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
     const size_t o_f4 = put(sizeof(double) * 12 * NV), o_fext = put(sizeof(double) * 3 * NV);
     const size_t o_norm = put(sizeof(double) * 8 * ns), o_nc = put(sizeof(NewtonCell) * ns);
     const size_t o_id = put(sizeof(int) * ns), o_tk = put(sizeof(unsigned int) * ns);
-    struct Off { size_t J, Ke, diag, G, dx, d, r, z; int n, ld; };
+    const size_t o_maps = put(sizeof(LuMaps) * ns);
+    struct Off { size_t J, Ut, Ke, diag, G, dx, d, r, z; int n, ld; };
     std::vector<Off> off(ns);
     P.max_n = 0;
     for (int sl = 0; sl < ns; ++sl) {
@@ -1476,6 +1499,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         f.n = n;
         f.ld = ld;
         f.J = put(sizeof(float) * (size_t)m * ld);
+        f.Ut = put(sizeof(float) * (size_t)m * kLuUtld);
         f.Ke = put(sizeof(float) * 36 * (size_t)c->topo.nt);
         f.diag = put(sizeof(double) * n);
         f.G = put(sizeof(double) * m);
@@ -1485,6 +1509,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         f.z = put(sizeof(float) * m);
         P.max_n = std::max(P.max_n, n);
     }
+    const size_t o_pref = put(sizeof(int) * lu_prefix_capacity(ns, 2 * P.max_n));
     int r = dev_alloc(e, &P.block, o);
     if (r) return r;
     P.bytes = o;
@@ -1499,6 +1524,8 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
     P.d_cells = (NewtonCell*)(b + o_nc);
     P.d_ident = (int*)(b + o_id);
     P.d_tickets = (unsigned int*)(b + o_tk);
+    P.d_maps = (LuMaps*)(b + o_maps);
+    P.d_prefix = (int*)(b + o_pref);
     P.cells.resize(ns);
     std::vector<int> ident(ns);
     for (int sl = 0; sl < ns; ++sl) {
@@ -1507,6 +1534,9 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         const Off& f = off[sl];
         NewtonCell& N = P.cells[sl];
         N.J = (float*)(b + f.J);
+        N.Ut = (float*)(b + f.Ut);
+        N.utld = kLuUtld;
+        N.pad2 = 0;
         N.Ke = (float*)(b + f.Ke);
         N.diag = (double*)(b + f.diag);
         N.G = (double*)(b + f.G);
@@ -1524,6 +1554,9 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         N.pad = 0;
         ident[sl] = sl;
     }
+    std::vector<LuMaps> maps(ns);
+    if (encode_lu_maps(P.cells.data(), ns, maps.data())) return fail("tensor map encoding failed", WCFE_ERR_CUDA);
+    CK(cudaMemcpyAsync(P.d_maps, maps.data(), sizeof(LuMaps) * ns, cudaMemcpyHostToDevice, e->stream));
     CK(cudaMemcpyAsync(P.d_ident, ident.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, e->stream));
     CK(cudaMemcpyAsync(P.d_cells, P.cells.data(), sizeof(NewtonCell) * ns, cudaMemcpyHostToDevice, e->stream));
     CK(cudaStreamSynchronize(e->stream));
@@ -1626,7 +1659,15 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
         for (const auto& N : P.cells)
             if (N.active) CK(cudaMemsetAsync(N.J, 0, sizeof(float) * 2 * (size_t)N.n * N.ld, e->stream));
         launch_newton_tangent(e->d_table, P.d_cells, P.d_ident, e->d_k2, n2, e->patch_emax, dt, e->stream);
-        launch_newton_lu(P.d_cells, ns, 2 * P.max_n, e->stream);
+        if (st) CK(cudaEventRecord(e->ev[0], e->stream));
+        if (const char* k = launch_newton_lu(P.d_cells, P.cells.data(), ns, 2 * P.max_n, P.d_maps, P.d_prefix,
+                                             e->lu_nb, e->lu_kind, e->stream))
+            return fail(std::string("launch failed: ") + k + lu_attr_note(), WCFE_ERR_CUDA);
+        if (st) {
+            CK(cudaEventRecord(e->ev[1], e->stream));
+            for (const auto& N : P.cells)
+                if (N.active) st->lu_gflop += (2.0 / 3.0) * std::pow(2.0 * N.n, 3) * 1e-9;
+        }
         // J dx = -G, refined in FP64
         for (const auto& N : P.cells)
             if (N.active) {
@@ -1656,6 +1697,9 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
             if (done) break;
         }
         if (st) {
+            float lu = 0.0f;
+            CK(cudaEventElapsedTime(&lu, e->ev[0], e->ev[1]));   // both passed: the stream was synchronised
+            st->lu_ms += lu;
             st->max_refine_iters = std::max(st->max_refine_iters, q + 1);
             st->max_refine_rel_residual = std::max(st->max_refine_rel_residual, final_ratio);
         }
@@ -1734,7 +1778,13 @@ int wcfe_cell_newton_tangent(wcfe_engine* e, int32_t id, double dt, const double
 }
 
 int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x) {
+    return wcfe_debug_lu_solve_with(m, A, b, x, 256, 0);
+}
+
+int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* x, int32_t block, int32_t kind) {
     if (m <= 0 || (m & 1) || !A || !b || !x) return fail("bad argument", WCFE_ERR_ARG);
+    if ((block != 64 && block != 256) || kind < 0 || kind > 1 || (kind == 1 && block != 64))
+        return fail("bad argument", WCFE_ERR_ARG);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
         cudaGetLastError();
@@ -1745,14 +1795,18 @@ int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x) {
     CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0));
     CK(configure_newton((size_t)max_optin, sms));
     const int ld = (m + 3) & ~3;
-    const size_t bytes = sizeof(float) * (size_t)m * ld + sizeof(double) * m + sizeof(float) * m +
-                         sizeof(double) * 8 + sizeof(NewtonCell) + 1024;
+    const size_t npref = lu_prefix_capacity(1, m);
+    const size_t bytes = sizeof(float) * (size_t)m * ld + sizeof(float) * (size_t)m * kLuUtld + sizeof(double) * m +
+                         sizeof(float) * m + sizeof(double) * 8 + sizeof(NewtonCell) + sizeof(LuMaps) +
+                         sizeof(int) * npref + 8 * 256;
     char* blk = nullptr;
     CK(cudaMalloc(&blk, bytes));
     size_t o = 0;
     auto take = [&](size_t n) { char* p = blk + o; o = (o + n + 255) & ~(size_t)255; return p; };
     NewtonCell N{};
     N.J = (float*)take(sizeof(float) * (size_t)m * ld);
+    N.Ut = (float*)take(sizeof(float) * (size_t)m * kLuUtld);
+    N.utld = kLuUtld;
     N.r = (double*)take(sizeof(double) * m);
     N.z = (float*)take(sizeof(float) * m);
     N.norms = (double*)take(sizeof(double) * 8);
@@ -1760,21 +1814,33 @@ int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x) {
     N.ld = ld;
     N.active = 1;
     NewtonCell* d_nc = (NewtonCell*)take(sizeof(NewtonCell));
-    cudaError_t ce = cudaMemcpy2D(N.J, sizeof(float) * ld, A, sizeof(float) * m, sizeof(float) * m, m,
-                                  cudaMemcpyHostToDevice);
+    LuMaps* d_maps = (LuMaps*)take(sizeof(LuMaps));
+    int* d_pref = (int*)take(sizeof(int) * npref);
+    LuMaps maps{};
+    cudaError_t ce = encode_lu_maps(&N, 1, &maps) ? cudaErrorInvalidValue : cudaSuccess;
+    if (ce == cudaSuccess) ce = cudaMemset(blk, 0, bytes);
+    if (ce == cudaSuccess)
+        ce = cudaMemcpy2D(N.J, sizeof(float) * ld, A, sizeof(float) * m, sizeof(float) * m, m, cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(N.r, b, sizeof(double) * m, cudaMemcpyHostToDevice);
-    if (ce == cudaSuccess) ce = cudaMemset(N.norms, 0, sizeof(double) * 8);
+    if (ce == cudaSuccess) ce = cudaMemcpy(d_maps, &maps, sizeof maps, cudaMemcpyHostToDevice);
     if (ce == cudaSuccess) ce = cudaMemcpy(d_nc, &N, sizeof N, cudaMemcpyHostToDevice);
+    const char* failed = nullptr;
     if (ce == cudaSuccess) {
-        launch_newton_lu(d_nc, 1, m, 0);
+        failed = launch_newton_lu(d_nc, &N, 1, m, d_maps, d_pref, block, kind, 0);
         launch_newton_solve(d_nc, 1, m / 2, 0);
+        if (!failed && cudaGetLastError() != cudaSuccess) failed = "triangular solves";
         ce = cudaDeviceSynchronize();
+    }
+    if (failed) {
+        cudaFree(blk);
+        return fail(std::string("launch failed: ") + failed + lu_attr_note(), WCFE_ERR_CUDA);
     }
     double flag = 0;
     if (ce == cudaSuccess) ce = cudaMemcpy(x, N.z, sizeof(float) * m, cudaMemcpyDeviceToHost);
     if (ce == cudaSuccess) ce = cudaMemcpy(&flag, N.norms + 3, sizeof(double), cudaMemcpyDeviceToHost);
     cudaFree(blk);
     if (ce != cudaSuccess) return fail(std::string("CUDA: ") + cudaGetErrorString(ce), WCFE_ERR_CUDA);
+    if (flag == 2.0) return fail("tensor-core update timed out", WCFE_ERR_CUDA);
     if (flag != 0.0) return fail("zero or non-finite pivot", WCFE_ERR_STATE);
     return WCFE_OK;
 }

@@ -1,0 +1,326 @@
+// wcfe_lu_tc.cu — trailing updates of the implicit step's blocked LU on the
+// 5th-generation tensor cores (tcgen05, TF32 inputs, FP32 accumulation in TMEM).
+//
+// One launch updates, for every active cell, C[rows, cols] -= L Ut^T with
+// L = J[rows, ka:ka+K] (the L21 panel, K-major as stored) and Ut the transposed U rows
+// of the current outer block (Ut[c][k] = U[K0 + k][c], written by the panel kernel).
+// The MMA computes the transposed product D = Ut L^T with M = 128 columns of C and
+// N = 128 rows of C, so a TMEM lane is a column of C and a TMEM column is a row of C:
+// each epilogue thread owns one column of the tile and reads and writes C one row at a
+// time, a warp covering 32 consecutive floats (coalesced, no staging buffer).
+//
+// Persistent CTAs, one per SM, walk a flat list of 128 x 128 tiles over all cells (the
+// host gives the per-cell tile counts as a prefix sum).  Warp 0 streams the operand
+// boxes with TMA into a 4-stage ring (K = 32 per stage, 128-byte swizzled); one thread of
+// warp 1 issues the MMAs into two TMEM accumulators, so tile t + 1 multiplies while tile t
+// is written back; 16 epilogue warps, four per TMEM lane quadrant (32 rows of C each),
+// prefetch the tile's C values before its product is ready, then subtract and store.
+//
+// Every wait is bounded: on a timeout the CTA flags the cell it was working on (norms[3],
+// the LU's failure flag), stops issuing work, waits (bounded) for its copies and MMAs in
+// flight, frees its TMEM and exits.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "wcfe_device.cuh"
+#include "wcfe_tc.cuh"
+
+namespace wcfe {
+namespace {
+
+constexpr int kTile = 128;                         // tile rows and columns of C
+constexpr int kBK = 32;                            // K per pipeline stage (one 128-B swizzle atom of fp32)
+constexpr int kStages = 4;
+constexpr int kEpiWarps = 16;                     // four per TMEM lane quadrant, 32 rows of C each
+constexpr int kThreads = 32 * (2 + kEpiWarps);
+constexpr uint32_t kBoxBytes = 128u * 128u;        // 128 rows x 128 B
+constexpr uint32_t kStageBytes = 2 * kBoxBytes;    // Ut box, then L box
+constexpr uint32_t kTmemCols = 256;                // two 128-column fp32 accumulators
+constexpr long long kWait = 2000000000ll;          // SM clocks (about 1 s) before a wait gives up
+constexpr size_t kSmemBytes = 1024 + (size_t)kStages * kStageBytes + 256;
+
+struct Tile {
+    int slot, tm, tn, rhi, chi;
+};
+
+__device__ __forceinline__ void region_of(const LuUpdateArgs& a, int r, int m, int& rlo, int& rhi, int& clo,
+                                          int& chi) {
+    rlo = min(a.rlo[r], m);
+    rhi = a.rhi[r] < 0 ? m : min(a.rhi[r], m);
+    clo = min(a.clo[r], m);
+    chi = a.chi[r] < 0 ? m : min(a.chi[r], m);
+}
+
+// flat tile f -> cell, tile origin; groups are (cell, region) pairs in cell-major order
+__device__ __forceinline__ Tile decode_tile(const NewtonCell* nc, const int* __restrict__ prefix, int ngroups, const LuUpdateArgs& a,
+                            int f) {
+    int lo = 0, hi = ngroups;   // prefix[lo] <= f < prefix[hi]; empty groups are skipped
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(prefix + mid) <= f) lo = mid;
+        else hi = mid;
+    }
+    Tile t;
+    t.slot = lo / a.nreg;
+    const int reg = lo - t.slot * a.nreg;
+    const int m = 2 * nc[t.slot].n;
+    int rlo, rhi, clo, chi;
+    region_of(a, reg, m, rlo, rhi, clo, chi);
+    const int tiles_n = (chi - clo + kTile - 1) / kTile;
+    const int local = f - __ldg(prefix + lo);
+    t.tm = rlo + (local / tiles_n) * kTile;
+    t.tn = clo + (local % tiles_n) * kTile;
+    t.rhi = rhi;
+    t.chi = chi;
+    return t;
+}
+
+__global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, const LuMaps* __restrict__ maps,
+                                                             const int* __restrict__ prefix, int ngroups,
+                                                             LuUpdateArgs a) {
+    extern __shared__ uint8_t tc_smem_raw[];
+    uint8_t* sm = tc_smem_raw + ((1024u - (smem_addr(tc_smem_raw) & 1023u)) & 1023u);
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm + kStages * kStageBytes);
+    uint64_t* empty = full + kStages;
+    uint64_t* tfull = empty + kStages;
+    uint64_t* tempty = tfull + 2;
+    uint64_t* drain = tempty + 2;
+    uint32_t* tbase_s = reinterpret_cast<uint32_t*>(drain + 1);
+    volatile int* abort_s = reinterpret_cast<volatile int*>(tbase_s + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int total = __ldg(prefix + ngroups);
+    const int nch = a.K / kBK;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(tfull + b, 1);
+            mbar_init(tempty + b, kEpiWarps);
+        }
+        mbar_init(drain, 1);
+        *abort_s = 0;
+        mbar_init_fence();
+    }
+    if (warp == 1) {
+        tc_alloc(tbase_s, kTmemCols);
+        tc_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *tbase_s;
+
+    if (warp == 0) {
+        // ---------------------------------------------------------------- TMA producer
+        if (lane == 0) {
+            int g = 0;   // chunks issued so far
+            for (int f = blockIdx.x; f < total && !*abort_s; f += gridDim.x) {
+                const Tile t = decode_tile(nc, prefix, ngroups, a, f);
+                const LuMaps* mp = maps + t.slot;
+                tmap_acquire(&mp->umap);
+                tmap_acquire(&mp->jmap);
+                for (int c = 0; c < nch; ++c, ++g) {
+                    const int s = g % kStages;
+                    const uint32_t u = (uint32_t)(g / kStages);
+                    if (!mbar_wait_bounded(empty + s, (u & 1u) ^ 1u, kWait)) {
+                        *abort_s = 1;
+                        nc[t.slot].norms[3] = 2.0;
+                        break;
+                    }
+                    uint8_t* st = sm + s * kStageBytes;
+                    mbar_arrive_expect_tx(full + s, kStageBytes);
+                    tma_load_2d(st, &mp->umap, a.kb + c * kBK, t.tn, full + s);
+                    tma_load_2d(st + kBoxBytes, &mp->jmap, a.ka + c * kBK, t.tm, full + s);
+                }
+            }
+            // every stage's last fill has landed before the CTA may exit
+            for (int s = 0; s < kStages && s < g; ++s) {
+                const uint32_t ulast = (uint32_t)((g - 1 - s) / kStages);
+                mbar_wait_bounded(full + s, ulast & 1u, kWait);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------------------------------------------------------- MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = tc_idesc_tf32(kTile, kTile);
+            int g = 0, it = 0;
+            for (int f = blockIdx.x; f < total && !*abort_s; f += gridDim.x, ++it) {
+                const int b = it & 1;
+                const uint32_t v = (uint32_t)(it >> 1);
+                if (!mbar_wait_bounded(tempty + b, (v & 1u) ^ 1u, kWait)) {
+                    *abort_s = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tbase + (uint32_t)(b * kTile);
+                bool ok = true;
+                for (int c = 0; c < nch; ++c, ++g) {
+                    const int s = g % kStages;
+                    const uint32_t u = (uint32_t)(g / kStages);
+                    if (!mbar_wait_bounded(full + s, u & 1u, kWait)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = smem_addr(sm + s * kStageBytes);
+                    const uint64_t da = tc_desc_k_sw128(sa), db = tc_desc_k_sw128(sa + kBoxBytes);
+#pragma unroll
+                    for (int k = 0; k < kBK / 8; ++k)
+                        tc_mma_tf32(d, da + 2u * (uint32_t)k, db + 2u * (uint32_t)k, idesc, (uint32_t)(c | k));
+                    tc_commit(empty + s);   // the stage is free once these MMAs have read it
+                }
+                if (!ok) {
+                    *abort_s = 1;
+                    break;
+                }
+                tc_commit(tfull + b);
+            }
+            tc_commit(drain);   // all MMAs issued by this thread have completed
+            mbar_wait_bounded(drain, 0u, kWait);
+        }
+        __syncwarp();
+    } else {
+        // ---------------------------------------------------------------- epilogue: C -= D^T
+        const int q = warp & 3;                   // the TMEM lane quadrant this warp may access
+        const int i0 = 32 * ((warp - 2) >> 2);    // rows of the tile (TMEM columns) of this warp
+        const uint32_t lane_field = (uint32_t)(32 * q) << 16;
+        int it = 0;
+        for (int f = blockIdx.x; f < total; f += gridDim.x, ++it) {
+            const int b = it & 1;
+            const uint32_t v = (uint32_t)(it >> 1);
+            const Tile t = decode_tile(nc, prefix, ngroups, a, f);
+            const int col = t.tn + 32 * q + lane;
+            const int ld = nc[t.slot].ld;
+            // this warp's 32 rows of the tile: rows t.tm + i0 + r, r < nrows valid
+            const int nrows = col < t.chi ? min(32, t.rhi - (t.tm + i0)) : 0;
+            float* __restrict__ Cb = nc[t.slot].J + (size_t)(t.tm + i0) * ld + col;
+            float c[32];
+#pragma unroll
+            for (int r = 0; r < 32; ++r) c[r] = r < nrows ? Cb[r * ld] : 0.0f;
+            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(tfull + b, v & 1u, kWait));
+            if (!ok) {
+                if (lane == 0) nc[t.slot].norms[3] = 2.0;
+                *abort_s = 1;
+                break;
+            }
+            tc_fence_after();
+            float p[32];
+            tc_ld_32x32b_x32(tbase + (uint32_t)(b * kTile + i0) + lane_field, p);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty + b);   // the accumulator may be overwritten
+            // the row stride through a shuffle: the store addresses are recomputed here rather
+            // than kept live (in registers) from the loads across the wait
+            const int lds = __shfl_sync(0xffffffffu, ld, 0);
+            float* __restrict__ Cs = Cb;
+#pragma unroll
+            for (int r = 0; r < 32; ++r) {
+                if (r < nrows) *Cs = c[r] - p[r];
+                Cs += lds;
+            }
+            if (*abort_s) break;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tc_dealloc(tbase, kTmemCols);
+    }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+int g_sms = 0;
+int g_lu_tc_regs = 0, g_lu_tc_max_threads = 0;
+
+int encode_f32_2d(CUtensorMap* map, const float* base, uint64_t cols, uint64_t rows, uint64_t row_bytes) {
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {row_bytes};
+    const cuuint32_t box[2] = {32, 128};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box,
+                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? 0 : -1;
+}
+
+}  // namespace
+
+// driver entry point for tensor-map encoding, the kernel's shared-memory size, the SM count
+cudaError_t configure_lu_tc(int num_sms) {
+    g_sms = num_sms;
+    if (!g_encode) {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+        if (e != cudaSuccess) return e;
+        if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorSymbolNotFound;
+        g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    cudaError_t e = cudaFuncSetAttribute((const void*)k_lu_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kSmemBytes);
+    if (e != cudaSuccess) return e;
+    cudaFuncAttributes at;
+    if ((e = cudaFuncGetAttributes(&at, (const void*)k_lu_update_tc)) != cudaSuccess) return e;
+    g_lu_tc_regs = at.numRegs;
+    g_lu_tc_max_threads = at.maxThreadsPerBlock;
+    return cudaSuccess;
+}
+
+// registers per thread and the largest block the compiled update kernel can launch with
+void lu_tc_attributes(int* regs, int* max_threads) {
+    *regs = g_lu_tc_regs;
+    *max_threads = g_lu_tc_max_threads;
+}
+
+// tensor maps of J and Ut for every cell (host copies of the NewtonCell entries); cells of
+// 64 or fewer rows have no trailing update and get an empty entry.  0 on success.
+int encode_lu_maps(const NewtonCell* h, int nslots, LuMaps* out) {
+    if (!g_encode) return -1;
+    for (int s = 0; s < nslots; ++s) {
+        std::memset(&out[s], 0, sizeof(LuMaps));
+        const uint64_t m = 2 * (uint64_t)h[s].n;
+        if (m <= 64) continue;
+        if (!h[s].Ut || h[s].utld % 32 != 0) return -1;
+        if (encode_f32_2d(&out[s].jmap, h[s].J, m, m, sizeof(float) * (uint64_t)h[s].ld)) return -1;
+        if (encode_f32_2d(&out[s].umap, h[s].Ut, (uint64_t)h[s].utld, m, sizeof(float) * (uint64_t)h[s].utld))
+            return -1;
+    }
+    return 0;
+}
+
+// tiles of one update launch per (cell, region) group, as a prefix sum (ngroups + 1 entries);
+// returns the total
+int lu_update_prefix(const NewtonCell* h, int nslots, const LuUpdateArgs& a, int* pref) {
+    int acc = 0;
+    for (int s = 0; s < nslots; ++s)
+        for (int r = 0; r < a.nreg; ++r) {
+            pref[s * a.nreg + r] = acc;
+            if (!h[s].active) continue;
+            const int m = 2 * h[s].n;
+            const int rlo = std::min(a.rlo[r], m), rhi = a.rhi[r] < 0 ? m : std::min(a.rhi[r], m);
+            const int clo = std::min(a.clo[r], m), chi = a.chi[r] < 0 ? m : std::min(a.chi[r], m);
+            if (rhi > rlo && chi > clo) acc += ((rhi - rlo + kTile - 1) / kTile) * ((chi - clo + kTile - 1) / kTile);
+        }
+    pref[nslots * a.nreg] = acc;
+    return acc;
+}
+
+bool launch_lu_update_tc(NewtonCell* nc, const LuMaps* maps, const int* d_prefix, int nslots, int total,
+                         const LuUpdateArgs& a, cudaStream_t st) {
+    if (g_lu_tc_max_threads < kThreads) return false;
+    if (total <= 0) return true;
+    const int grid = std::max(1, std::min(total, g_sms > 0 ? g_sms : 1));
+    k_lu_update_tc<<<grid, kThreads, kSmemBytes, st>>>(nc, maps, d_prefix, nslots * a.nreg, a);
+    return cudaGetLastError() == cudaSuccess;
+}
+
+}  // namespace wcfe

@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <vector>
 
 #include "wcfe_common.cuh"
 
@@ -386,8 +387,9 @@ __global__ void __launch_bounds__(256) k_lu_diag(NewtonCell* nc, int nslots, int
 
 // U12 = L11^-1 A12 (block x: column chunks) and L21 = A21 U11^-1 (block x: row chunks
 // after the column chunks); one column or one row per thread, held in registers (the
-// padded 64-step substitutions are fully unrolled), in place
-__global__ void __launch_bounds__(256) k_lu_panels(NewtonCell* nc, int nslots, int k0, int nchunks) {
+// padded 64-step substitutions are fully unrolled), in place.  The U rows also go,
+// transposed, to Ut[col][kbase + i] (the tensor-core update's K-major operand).
+__global__ void __launch_bounds__(256) k_lu_panels(NewtonCell* nc, int nslots, int k0, int nchunks, int kbase) {
     const int slot = blockIdx.y;
     if (slot >= nslots) return;
     NewtonCell& N = nc[slot];
@@ -415,6 +417,11 @@ __global__ void __launch_bounds__(256) k_lu_panels(NewtonCell* nc, int nslots, i
 #pragma unroll
             for (int i = 0; i < kNb; ++i)
                 if (i < kb) N.J[(size_t)(k0 + i) * N.ld + col] = x[i];
+            if (N.Ut) {
+                float4* u = reinterpret_cast<float4*>(N.Ut + (size_t)col * N.utld + kbase);
+#pragma unroll
+                for (int i = 0; i < kNb / 4; ++i) u[i] = make_float4(x[4 * i], x[4 * i + 1], x[4 * i + 2], x[4 * i + 3]);
+            }
         }
     } else {                         // rows: x U11 = a
         for (int row = r0 + (blockIdx.x - half) * blockDim.x + threadIdx.x; row < m; row += half * blockDim.x) {
@@ -742,8 +749,15 @@ __global__ void k_sum4(const double* __restrict__ a, const double* __restrict__ 
 // ---------------------------------------------------------------------------- host launchers
 static int g_num_sms = 0;
 
+cudaError_t configure_lu_tc(int num_sms);
+int lu_update_prefix(const NewtonCell* h, int nslots, const LuUpdateArgs& a, int* pref);
+bool launch_lu_update_tc(NewtonCell* nc, const LuMaps* maps, const int* d_prefix, int nslots, int total,
+                         const LuUpdateArgs& a, cudaStream_t st);
+
 cudaError_t configure_newton(size_t max_smem, int num_sms) {
     g_num_sms = num_sms;
+    cudaError_t ce = configure_lu_tc(num_sms);
+    if (ce != cudaSuccess) return ce;
     cudaError_t e = cudaFuncSetAttribute((const void*)k_lu_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)(sizeof(float) * (kTileM * (kNb + 4) + kNb * (kTileN + 8))));
     if (e != cudaSuccess) return e;
@@ -766,17 +780,95 @@ void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int
     const int grid = std::min(nwork, std::max(1, g_num_sms) * 8);
     k_newton_tangent<<<grid, kTanThreads, newton_tangent_smem(emax), st>>>(cells, nc, cell_slot, work, nwork, emax, dt);
 }
-void launch_newton_lu(NewtonCell* nc, int nslots, int max_m, cudaStream_t st) {
-    const size_t usm = sizeof(float) * (kTileM * (kNb + 4) + kNb * (kTileN + 8));
-    for (int k0 = 0; k0 < max_m; k0 += kNb) {
-        k_lu_diag<<<nslots, 256, 0, st>>>(nc, nslots, k0);
+// The blocked LU of every active cell, in lockstep over the largest matrix.  kind 1: the
+// 64-wide right-looking algorithm with mma.sync updates (nb must be 64).  kind 0:
+// outer blocks of nb (64 or 256) columns; inside one, 64-wide steps factor the diagonal
+// block and the two panels and update only the rest of the outer block's column and
+// row strips; the trailing matrix then takes one update with K = nb on the tcgen05
+// tensor cores.  The per-launch tile counts go to the device in one copy (d_prefix,
+// lu_prefix_capacity ints).
+size_t lu_prefix_capacity(int nslots, int max_m) {
+    return (size_t)2 * ((size_t)(max_m + kNb - 1) / kNb + 1) * (2 * (size_t)nslots + 1);
+}
+
+const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots, int max_m, const LuMaps* maps,
+                             int* d_prefix, int nb, int kind, cudaStream_t st) {
+    const char* failed = nullptr;
+    auto checked = [&](const char* name) {
+        if (!failed && cudaGetLastError() != cudaSuccess) failed = name;
+    };
+    auto panels = [&](int k0, int kbase) {
         const int rest = max_m - k0 - kNb;
-        if (rest <= 0) break;
         const int half = std::max(1, std::min((rest + 255) / 256, 32));
-        k_lu_panels<<<dim3(2 * half, nslots), 256, 0, st>>>(nc, nslots, k0, 2 * half);
-        k_lu_update<<<dim3((rest + kTileN - 1) / kTileN, (rest + kTileM - 1) / kTileM, nslots), 256, usm, st>>>(
-            nc, nslots, k0);
+        k_lu_panels<<<dim3(2 * half, nslots), 256, 0, st>>>(nc, nslots, k0, 2 * half, kbase);
+    };
+    if (kind == 1) {
+        const size_t usm = sizeof(float) * (kTileM * (kNb + 4) + kNb * (kTileN + 8));
+        for (int k0 = 0; k0 < max_m; k0 += kNb) {
+            k_lu_diag<<<nslots, 256, 0, st>>>(nc, nslots, k0);
+            const int rest = max_m - k0 - kNb;
+            if (rest <= 0) break;
+            panels(k0, 0);
+            k_lu_update<<<dim3((rest + kTileN - 1) / kTileN, (rest + kTileM - 1) / kTileM, nslots), 256, usm, st>>>(
+                nc, nslots, k0);
+            checked("k_lu_diag, k_lu_panels or k_lu_update");
+        }
+        return failed;
     }
+    struct Op {
+        int type, k0, kbase, pref, total;   // type 0 diag, 1 panels, 2 update
+        LuUpdateArgs a;
+    };
+    std::vector<Op> ops;
+    std::vector<int> pref;
+    auto update = [&](const LuUpdateArgs& a) {
+        const size_t at = pref.size();
+        pref.resize(at + (size_t)nslots * a.nreg + 1);
+        const int total = lu_update_prefix(h_nc, nslots, a, pref.data() + at);
+        if (!total) {
+            pref.resize(at);
+            return;
+        }
+        ops.push_back({2, 0, 0, (int)at, total, a});
+    };
+    for (int K0 = 0; K0 < max_m; K0 += nb) {
+        for (int ib = 0; ib < nb / kNb && K0 + ib * kNb < max_m; ++ib) {
+            const int k0 = K0 + ib * kNb;
+            ops.push_back({0, k0, 0, 0, 0, {}});
+            if (max_m - k0 - kNb <= 0) break;
+            ops.push_back({1, k0, ib * kNb, 0, 0, {}});
+            LuUpdateArgs a{};   // the rest of the outer block's column strip, then of its row strip
+            a.nreg = 2;
+            a.rlo[0] = k0 + kNb; a.rhi[0] = -1; a.clo[0] = k0 + kNb; a.chi[0] = K0 + nb;
+            a.rlo[1] = k0 + kNb; a.rhi[1] = K0 + nb; a.clo[1] = K0 + nb; a.chi[1] = -1;
+            a.ka = k0;
+            a.kb = ib * kNb;
+            a.K = kNb;
+            update(a);
+        }
+        LuUpdateArgs a{};   // the trailing matrix, K = nb
+        a.nreg = 1;
+        a.rlo[0] = K0 + nb; a.rhi[0] = -1; a.clo[0] = K0 + nb; a.chi[0] = -1;
+        a.ka = K0;
+        a.kb = 0;
+        a.K = nb;
+        a.rlo[1] = a.rhi[1] = a.clo[1] = a.chi[1] = 0;
+        update(a);
+    }
+    if (!pref.empty()) cudaMemcpyAsync(d_prefix, pref.data(), sizeof(int) * pref.size(), cudaMemcpyHostToDevice, st);
+    for (const Op& o : ops) {
+        if (o.type == 0) {
+            k_lu_diag<<<nslots, 256, 0, st>>>(nc, nslots, o.k0);
+            checked("k_lu_diag");
+        } else if (o.type == 1) {
+            panels(o.k0, o.kbase);
+            checked("k_lu_panels");
+        } else {
+            if (!launch_lu_update_tc(nc, maps, d_prefix + o.pref, nslots, o.total, o.a, st) && !failed)
+                failed = "k_lu_update_tc";
+        }
+    }
+    return failed;
 }
 void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, cudaStream_t st) {
     const int m = 2 * max_n, nblk = (m + kNb - 1) / kNb;
