@@ -344,6 +344,10 @@ int wcfe_engine_step_implicit(wcfe_engine* e, int32_t nsteps, double dt, double 
  * kind 1: the mma.sync TF32 updates (block must be 64).  FP64 engines; results agree
  * to TF32 rounding, and the refinement takes every solve to the same tolerance. */
 int wcfe_engine_set_lu(wcfe_engine* e, int32_t block, int32_t kind);
+/* reuse 1 (default): one dense factorisation per implicit step, kept by its later Newton
+ * iterations (the refinement against the current tangent restores the exact correction);
+ * 0: a fresh factorisation every Newton iteration. */
+int wcfe_engine_set_lu_reuse(wcfe_engine* e, int32_t reuse);
 
 /* Factor the dense m x m matrix A (row-major, FP32, m even) with the implicit step's
  * LU (no pivoting; TF32 tensor-core trailing updates) and solve A x = b once

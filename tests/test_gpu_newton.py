@@ -206,3 +206,21 @@ def test_implicit_step_lu_variants_agree():
     u = out[0] - st[0]
     for x in out[1:]:
         assert np.max(np.abs(x - out[0])) / np.max(np.abs(u)) < 1e-9
+
+
+def test_implicit_step_factor_reuse_agrees():
+    """One factorisation per step (default) against a fresh one every Newton iteration: the
+    refinement restores the exact correction, so the converged states agree."""
+    x0, tri, st, p, t = _cell(400, 33)
+    out = []
+    for reuse in (True, False):
+        e = capi.Engine(capi.PREC_FP64)
+        e.set_lu_reuse(reuse)
+        h = e.add_cell(x0, tri, p, state=st, t=t)
+        stats = e.step_implicit(3, DT, rtol=1e-11, max_newton=8)
+        assert stats["unconverged"] == 0 and h.status() == 0, stats
+        assert stats["max_refine_rel_residual"] <= 1e-10, stats
+        out.append(h.get_state()[0])
+        e.close()
+    u = out[1] - st[0]
+    assert np.max(np.abs(out[0] - out[1])) / np.max(np.abs(u)) < 1e-9

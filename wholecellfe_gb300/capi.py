@@ -93,6 +93,7 @@ SIGNATURES = {
     "wcfe_debug_lu_solve_with": (C.c_int, [C.c_int32, C.POINTER(C.c_float), _d, C.POINTER(C.c_float), C.c_int32,
                                            C.c_int32]),
     "wcfe_engine_set_lu": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "wcfe_engine_set_lu_reuse": (C.c_int, [C.c_void_p, C.c_int32]),
     "wcfe_area_tot_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "wcfe_debug_topology": (C.c_int, [C.c_int32, C.c_int32, _i, _i, _i, _u8, C.c_int32, _i, _i, _i, _i, C.c_int32, _i,
                                       _i, C.c_int32, _i, C.c_int32, C.POINTER(C.c_uint16)]),
@@ -290,6 +291,10 @@ class Engine:
     def set_lu(self, block: int = 256, kind: int = 0):
         """The implicit step's LU: outer block width 64 or 256; kind 0 tcgen05, 1 mma.sync (block 64)."""
         check(load().wcfe_engine_set_lu(self.h, block, kind), "wcfe_engine_set_lu")
+
+    def set_lu_reuse(self, reuse: bool):
+        """Implicit step: True (default) factor once per step, False every Newton iteration."""
+        check(load().wcfe_engine_set_lu_reuse(self.h, int(reuse)), "wcfe_engine_set_lu_reuse")
 
     def set_patch_kernel(self, kind: int):
         """Mixed engines: 0 staged patch kernel where it fits, 1 plain (default)."""

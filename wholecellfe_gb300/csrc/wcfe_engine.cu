@@ -43,7 +43,7 @@ size_t newton_tangent_smem(int emax);
 void launch_newton_residual(const CellDev* cells, const NewtonCell* nc, const int* cell_of_slot, int nslots, int max_n,
                             double dt, cudaStream_t st);
 void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int* cell_slot, const WorkItem* work,
-                           int nwork, int emax, double dt, cudaStream_t st);
+                           int nwork, int emax, double dt, int dense, cudaStream_t st);
 const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots, int max_m, const LuMaps* maps,
                              int* d_prefix, int nb, int kind, cudaStream_t st);
 void lu_tc_attributes(int* regs, int* max_threads);
@@ -170,6 +170,7 @@ struct wcfe_engine {
     int vblock = 256;             // vertices (threads) per vertex-phase block
     int patch_kernel = 1;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
     int lu_nb = 256, lu_kind = 0; // implicit step's LU: outer block width, 0 tcgen05 / 1 mma.sync updates
+    int lu_reuse = 1;             // 1: factor once per implicit step, 0: every Newton iteration
     int cap_ne = 0, cap_nvp = 0, cap_nh = 0, cap_nc = 0;   // largest patch over the cells (staging plan)
     int n2_sub = 0;               // patch work items of substrate cells, at the end of k2 (second launch)
     bool tuned = false;
@@ -1329,6 +1330,12 @@ int wcfe_engine_set_lu(wcfe_engine* e, int32_t block, int32_t kind) {
     return WCFE_OK;
 }
 
+int wcfe_engine_set_lu_reuse(wcfe_engine* e, int32_t reuse) {
+    if (!e || reuse < 0 || reuse > 1) return fail("bad argument", WCFE_ERR_ARG);
+    e->lu_reuse = reuse;
+    return WCFE_OK;
+}
+
 int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind) {
     if (!e || kind < 0 || kind > 1) return fail("bad argument", WCFE_ERR_ARG);
     e->patch_kernel = kind;
@@ -1655,10 +1662,16 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
         if (!nact) break;
         if ((r = newton_upload_active(e, P))) return r;
         if (st) st->newton_iters += 1;
-        // tangent, LU
-        for (const auto& N : P.cells)
-            if (N.active) CK(cudaMemsetAsync(N.J, 0, sizeof(float) * 2 * (size_t)N.n * N.ld, e->stream));
-        launch_newton_tangent(e->d_table, P.d_cells, P.d_ident, e->d_k2, n2, e->patch_emax, dt, e->stream);
+        // tangent; the dense LU on the first iteration of the step (or every iteration without
+        // reuse).  Later iterations keep the factors: the FP64 refinement against the current
+        // sparse tangent still gives the Newton correction to 1e-10, in a pass or two more.
+        const bool factor = it == 0 || !e->lu_reuse;
+        if (factor)
+            for (const auto& N : P.cells)
+                if (N.active) CK(cudaMemsetAsync(N.J, 0, sizeof(float) * 2 * (size_t)N.n * N.ld, e->stream));
+        launch_newton_tangent(e->d_table, P.d_cells, P.d_ident, e->d_k2, n2, e->patch_emax, dt, factor ? 1 : 0,
+                              e->stream);
+        if (factor) {
         if (st) CK(cudaEventRecord(e->ev[0], e->stream));
         if (const char* k = launch_newton_lu(P.d_cells, P.cells.data(), ns, 2 * P.max_n, P.d_maps, P.d_prefix,
                                              e->lu_nb, e->lu_kind, e->stream))
@@ -1667,6 +1680,7 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
             CK(cudaEventRecord(e->ev[1], e->stream));
             for (const auto& N : P.cells)
                 if (N.active) st->lu_gflop += (2.0 / 3.0) * std::pow(2.0 * N.n, 3) * 1e-9;
+        }
         }
         // J dx = -G, refined in FP64
         for (const auto& N : P.cells)
@@ -1698,7 +1712,7 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
         }
         if (st) {
             float lu = 0.0f;
-            CK(cudaEventElapsedTime(&lu, e->ev[0], e->ev[1]));   // both passed: the stream was synchronised
+            if (factor) CK(cudaEventElapsedTime(&lu, e->ev[0], e->ev[1]));   // both passed: the stream was synchronised
             st->lu_ms += lu;
             st->max_refine_iters = std::max(st->max_refine_iters, q + 1);
             st->max_refine_rel_residual = std::max(st->max_refine_rel_residual, final_ratio);
@@ -1765,7 +1779,7 @@ int wcfe_cell_newton_tangent(wcfe_engine* e, int32_t id, double dt, const double
                      std::numeric_limits<double>::quiet_NaN(), 0, nullptr, P.res, P.rea, P.mm, nullptr, nullptr,
                      e->patch_threads, grid_for(e, n2, patch_occupancy(WCFE_PREC_FP64, e->patch_threads, smem)),
                      e->stream, 1);
-        launch_newton_tangent(e->d_table, P.d_cells, P.d_ident, e->d_one + n1, n2, e->patch_emax, dt, e->stream);
+        launch_newton_tangent(e->d_table, P.d_cells, P.d_ident, e->d_one + n1, n2, e->patch_emax, dt, 1, e->stream);
         const NewtonCell& N = P.cells[ti];
         CK(cudaMemcpy2DAsync(J_out, sizeof(float) * 2 * n, N.J, sizeof(float) * N.ld, sizeof(float) * 2 * n, 2 * n,
                              cudaMemcpyDeviceToHost, e->stream));

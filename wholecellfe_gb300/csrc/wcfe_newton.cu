@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kTanThreads) k_newton_tangent(const CellDev* _
                                                                const NewtonCell* __restrict__ nc,
                                                                const int* __restrict__ cell_slot,
                                                                const WorkItem* __restrict__ work, int nwork, int emax,
-                                                               double dt) {
+                                                               double dt, int dense) {
     extern __shared__ float ke_s[];   // [emax][36]
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
         const WorkItem it = work[w];
@@ -282,6 +282,7 @@ __global__ void __launch_bounds__(kTanThreads) k_newton_tangent(const CellDev* _
             const double m = N.MM[v] * p.rho;
             const double dg = m * idt * idt + (p.drag + p.damp * m) * idt;
             N.diag[v] = dg;
+            if (!dense) continue;   // element tangents and the diagonal only (the factors are reused)
             float* row0 = N.J + (size_t)(2 * v) * N.ld;
             float* row1 = row0 + N.ld;
             row0[2 * v] += (float)dg;
@@ -775,10 +776,11 @@ void launch_newton_residual(const CellDev* cells, const NewtonCell* nc, const in
     k_newton_residual<<<grid, 256, 0, st>>>(cells, nc, cell_of_slot, nslots, dt);
 }
 void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int* cell_slot, const WorkItem* work,
-                           int nwork, int emax, double dt, cudaStream_t st) {
+                           int nwork, int emax, double dt, int dense, cudaStream_t st) {
     if (nwork <= 0) return;
     const int grid = std::min(nwork, std::max(1, g_num_sms) * 8);
-    k_newton_tangent<<<grid, kTanThreads, newton_tangent_smem(emax), st>>>(cells, nc, cell_slot, work, nwork, emax, dt);
+    k_newton_tangent<<<grid, kTanThreads, newton_tangent_smem(emax), st>>>(cells, nc, cell_slot, work, nwork, emax, dt,
+                                                                               dense);
 }
 // The blocked LU of every active cell, in lockstep over the largest matrix.  kind 1: the
 // 64-wide right-looking algorithm with mma.sync updates (nb must be 64).  kind 0:
