@@ -541,6 +541,7 @@ def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(256, 0)):
             "lu_ms_per_step": round(st["lu_ms"] / steps, 2),
             "lu_tflop_per_s": round(st["lu_gflop"] / st["lu_ms"], 2) if st["lu_ms"] > 0 else None,
             "lu_share_of_step": round(st["lu_ms"] / (wall * 1e3), 3),
+            "solve_ms_per_step": round(st["solve_ms"] / steps, 2),
             "timing": "host wall clock around wcfe_engine_step_implicit (it synchronises per Newton iteration); "
                       "LU: CUDA events around each factorisation, TF32 flops 2/3 (2N)^3 per factored cell"}
 

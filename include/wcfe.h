@@ -333,6 +333,7 @@ typedef struct wcfe_newton_stats {
     double max_refine_rel_residual;    /* largest final |J dx + G|inf / |G|inf of a linear solve */
     double lu_ms;                      /* device time of the dense factorisations (CUDA events) */
     double lu_gflop;                   /* their work, 2/3 (2N)^3 per factored cell, in GFLOP */
+    double solve_ms;                   /* device time of the triangular solves with the factors */
 } wcfe_newton_stats;
 
 int wcfe_engine_step_implicit(wcfe_engine* e, int32_t nsteps, double dt, double newton_rtol, int32_t max_newton,

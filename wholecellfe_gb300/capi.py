@@ -25,7 +25,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 class NewtonStats(C.Structure):
     _fields_ = [("newton_iters", C.c_int32), ("max_refine_iters", C.c_int32), ("unconverged", C.c_int32),
                 ("floor_exits", C.c_int32), ("max_rel_residual", C.c_double), ("max_refine_rel_residual", C.c_double),
-                ("lu_ms", C.c_double), ("lu_gflop", C.c_double)]
+                ("lu_ms", C.c_double), ("lu_gflop", C.c_double), ("solve_ms", C.c_double)]
 
 
 class Request(C.Structure):

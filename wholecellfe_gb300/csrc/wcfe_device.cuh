@@ -150,6 +150,9 @@ struct NewtonCell {
     int n, ld, active, pad;
     float* Ut;           // [2n][utld] transposed U rows of the current outer LU block (tensor-core operand)
     int utld, pad2;
+    float* Dinv;         // [ceil(2n/64)][2][64][64] inverses of the 64 x 64 diagonal blocks' unit-lower and
+                         //      upper factors (identity-padded), row-major
+    float* zt;           // [2n] FP32 solve workspace (the forward solve's result)
 };
 
 // TMA descriptors of one cell's dense LU: J (fp32, 2n x 2n, row stride ld) and Ut

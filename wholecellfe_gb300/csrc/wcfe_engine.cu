@@ -47,6 +47,9 @@ void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int
 const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots, int max_m, const LuMaps* maps,
                              int* d_prefix, int nb, int kind, cudaStream_t st);
 void lu_tc_attributes(int* regs, int* max_threads);
+void launch_newton_clear(NewtonCell* nc, int nslots, int max_n, cudaStream_t st);
+void launch_norms_clear(double* norms, int nslots, int first, int count, cudaStream_t st);
+void launch_dense_clear(NewtonCell* nc, int nslots, int max_n, cudaStream_t st);
 std::string lu_attr_note() {
     int regs = 0, mt = 0;
     lu_tc_attributes(&regs, &mt);
@@ -1477,6 +1480,7 @@ struct NewtonPlan {
     double* norms = nullptr;         // [nslots][8]
     LuMaps* d_maps = nullptr;        // [nslots] TMA descriptors of J and Ut
     int* d_prefix = nullptr;         // per-launch tile prefix sums of the LU's trailing updates
+    cudaEvent_t sev[2] = {nullptr, nullptr};   // around each triangular solve (statistics)
     double *res = nullptr, *rea = nullptr, *mm = nullptr, *f4 = nullptr, *fext = nullptr;
     int max_n = 0;
 };
@@ -1496,7 +1500,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
     const size_t o_norm = put(sizeof(double) * 8 * ns), o_nc = put(sizeof(NewtonCell) * ns);
     const size_t o_id = put(sizeof(int) * ns), o_tk = put(sizeof(unsigned int) * ns);
     const size_t o_maps = put(sizeof(LuMaps) * ns);
-    struct Off { size_t J, Ut, Ke, diag, G, dx, d, r, z; int n, ld; };
+    struct Off { size_t J, Ut, Dinv, Ke, diag, G, dx, d, r, z, zt; int n, ld; };
     std::vector<Off> off(ns);
     P.max_n = 0;
     for (int sl = 0; sl < ns; ++sl) {
@@ -1507,6 +1511,8 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         f.ld = ld;
         f.J = put(sizeof(float) * (size_t)m * ld);
         f.Ut = put(sizeof(float) * (size_t)m * kLuUtld);
+        f.Dinv = put(sizeof(float) * 2 * 64 * 64 * (size_t)((m + 63) / 64));
+        f.zt = put(sizeof(float) * m);
         f.Ke = put(sizeof(float) * 36 * (size_t)c->topo.nt);
         f.diag = put(sizeof(double) * n);
         f.G = put(sizeof(double) * m);
@@ -1544,6 +1550,8 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         N.Ut = (float*)(b + f.Ut);
         N.utld = kLuUtld;
         N.pad2 = 0;
+        N.Dinv = (float*)(b + f.Dinv);
+        N.zt = (float*)(b + f.zt);
         N.Ke = (float*)(b + f.Ke);
         N.diag = (double*)(b + f.diag);
         N.G = (double*)(b + f.G);
@@ -1567,10 +1575,13 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
     CK(cudaMemcpyAsync(P.d_ident, ident.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, e->stream));
     CK(cudaMemcpyAsync(P.d_cells, P.cells.data(), sizeof(NewtonCell) * ns, cudaMemcpyHostToDevice, e->stream));
     CK(cudaStreamSynchronize(e->stream));
+    for (auto& ev : P.sev) CK(cudaEventCreate(&ev));
     return WCFE_OK;
 }
 
 void newton_free(wcfe_engine* e, NewtonPlan& P) {
+    for (auto& ev : P.sev)
+        if (ev) cudaEventDestroy(ev);
     if (P.block) {
         cudaStreamSynchronize(e->stream);
         dev_free(e, P.block, P.bytes);
@@ -1625,7 +1636,7 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
     for (int it = 0;; ++it) {
         newton_membrane(e, P, dt);
         // |G| and the force scale (entries 0, 1) are rebuilt; entries 4, 5 hold the last update
-        for (int sl = 0; sl < ns; ++sl) CK(cudaMemsetAsync(P.norms + 8 * (size_t)sl, 0, sizeof(double) * 4, e->stream));
+        launch_norms_clear(P.norms, ns, 0, 4, e->stream);
         launch_newton_residual(e->d_table, P.d_cells, P.d_ident, ns, P.max_n, dt, e->stream);
         e->launches += 2;
         if ((r = newton_read_norms(e, P, hn))) return r;
@@ -1666,9 +1677,7 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
         // reuse).  Later iterations keep the factors: the FP64 refinement against the current
         // sparse tangent still gives the Newton correction to 1e-10, in a pass or two more.
         const bool factor = it == 0 || !e->lu_reuse;
-        if (factor)
-            for (const auto& N : P.cells)
-                if (N.active) CK(cudaMemsetAsync(N.J, 0, sizeof(float) * 2 * (size_t)N.n * N.ld, e->stream));
+        if (factor) launch_dense_clear(P.d_cells, ns, P.max_n, e->stream);
         launch_newton_tangent(e->d_table, P.d_cells, P.d_ident, e->d_k2, n2, e->patch_emax, dt, factor ? 1 : 0,
                               e->stream);
         if (factor) {
@@ -1683,23 +1692,25 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
         }
         }
         // J dx = -G, refined in FP64
-        for (const auto& N : P.cells)
-            if (N.active) {
-                CK(cudaMemsetAsync(N.dx, 0, sizeof(double) * 2 * (size_t)N.n, e->stream));
-                CK(cudaMemsetAsync(N.z, 0, sizeof(float) * 2 * (size_t)N.n, e->stream));
-            }
+        launch_newton_clear(P.d_cells, ns, P.max_n, e->stream);
         launch_newton_refine(e->d_table, P.d_cells, P.d_ident, e->d_k2, n2, 0, e->stream);
         int q = 0;
         double final_ratio = 0.0;
         for (; q < 16; ++q) {
+            if (st) CK(cudaEventRecord(P.sev[0], e->stream));
             launch_newton_solve(P.d_cells, ns, P.max_n, e->stream);
-            for (int sl = 0; sl < ns; ++sl)   // |r| only (G's norm is kept on the host)
-                CK(cudaMemsetAsync(P.norms + 8 * (size_t)sl + 2, 0, sizeof(double), e->stream));
+            if (st) CK(cudaEventRecord(P.sev[1], e->stream));
+            launch_norms_clear(P.norms, ns, 2, 1, e->stream);   // |r| only (G's norm is kept on the host)
             launch_newton_refine(e->d_table, P.d_cells, P.d_ident, e->d_k2, n2, 1, e->stream);
             launch_newton_accumulate(P.d_cells, ns, P.max_n, e->stream);
             e->launches += 3;
             std::vector<double> hr;
             if ((r = newton_read_norms(e, P, hr))) return r;
+            if (st) {
+                float sv = 0.0f;
+                CK(cudaEventElapsedTime(&sv, P.sev[0], P.sev[1]));   // the stream was synchronised
+                st->solve_ms += sv;
+            }
             bool done = true;
             final_ratio = 0.0;
             for (int sl = 0; sl < ns; ++sl) {
@@ -1717,7 +1728,7 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
             st->max_refine_iters = std::max(st->max_refine_iters, q + 1);
             st->max_refine_rel_residual = std::max(st->max_refine_rel_residual, final_ratio);
         }
-        for (int sl = 0; sl < ns; ++sl) CK(cudaMemsetAsync(P.norms + 8 * (size_t)sl + 4, 0, sizeof(double) * 2, e->stream));
+        launch_norms_clear(P.norms, ns, 4, 2, e->stream);
         launch_newton_apply(e->d_table, P.d_cells, P.d_ident, ns, P.max_n, 0, e->stream);
         e->launches += 4 + 3 * ((2 * P.max_n + 63) / 64);
         CK(cudaGetLastError());
@@ -1810,9 +1821,10 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     CK(configure_newton((size_t)max_optin, sms));
     const int ld = (m + 3) & ~3;
     const size_t npref = lu_prefix_capacity(1, m);
+    const size_t ndinv = 2 * 64 * 64 * (size_t)((m + 63) / 64);
     const size_t bytes = sizeof(float) * (size_t)m * ld + sizeof(float) * (size_t)m * kLuUtld + sizeof(double) * m +
-                         sizeof(float) * m + sizeof(double) * 8 + sizeof(NewtonCell) + sizeof(LuMaps) +
-                         sizeof(int) * npref + 8 * 256;
+                         2 * sizeof(float) * m + sizeof(float) * ndinv + sizeof(double) * 8 + sizeof(NewtonCell) +
+                         sizeof(LuMaps) + sizeof(int) * npref + 10 * 256;
     char* blk = nullptr;
     CK(cudaMalloc(&blk, bytes));
     size_t o = 0;
@@ -1823,6 +1835,8 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     N.utld = kLuUtld;
     N.r = (double*)take(sizeof(double) * m);
     N.z = (float*)take(sizeof(float) * m);
+    N.zt = (float*)take(sizeof(float) * m);
+    N.Dinv = (float*)take(sizeof(float) * ndinv);
     N.norms = (double*)take(sizeof(double) * 8);
     N.n = m / 2;
     N.ld = ld;

@@ -384,13 +384,42 @@ __global__ void __launch_bounds__(256) k_lu_diag(NewtonCell* nc, int nslots, int
     }
     for (int i = ty; i < kb; i += 16)
         for (int j = tx; j < kb; j += 16) N.J[(size_t)(k0 + i) * N.ld + k0 + j] = A[i][j];
+    // explicit inverses of the (identity-padded) unit-lower and upper factors, one column per
+    // thread held in registers: L X = I forward, U Y = I backward
+    float* Li = N.Dinv + (size_t)(k0 / kNb) * 2 * kNb * kNb;
+    float* Ui = Li + kNb * kNb;
+    float x[kNb];
+    if (threadIdx.x < kNb) {
+        const int j = threadIdx.x;
+#pragma unroll
+        for (int i = 0; i < kNb; ++i) {
+            float s = i == j ? 1.0f : 0.0f;
+#pragma unroll
+            for (int k = 0; k < i; ++k) s -= A[i][k] * x[k];
+            x[i] = s;
+        }
+#pragma unroll
+        for (int i = 0; i < kNb; ++i) Li[i * kNb + j] = x[i];
+    } else if (threadIdx.x < 2 * kNb) {
+        const int j = threadIdx.x - kNb;
+#pragma unroll
+        for (int i = kNb - 1; i >= 0; --i) {
+            float s = i == j ? 1.0f : 0.0f;
+#pragma unroll
+            for (int k = i + 1; k < kNb; ++k) s -= A[i][k] * x[k];
+            x[i] = s / A[i][i];
+        }
+#pragma unroll
+        for (int i = 0; i < kNb; ++i) Ui[i * kNb + j] = x[i];
+    }
 }
 
 // U12 = L11^-1 A12 (block x: column chunks) and L21 = A21 U11^-1 (block x: row chunks
-// after the column chunks); one column or one row per thread, held in registers (the
-// padded 64-step substitutions are fully unrolled), in place.  The U rows also go,
-// transposed, to Ut[col][kbase + i] (the tensor-core update's K-major operand).
-__global__ void __launch_bounds__(256) k_lu_panels(NewtonCell* nc, int nslots, int k0, int nchunks, int kbase) {
+// after the column chunks), in place, with the explicit inverses of the diagonal block's
+// factors: one column or one row per thread, held in registers, and 64 independent dot
+// products (no serial substitution chain).  The U rows also go, transposed, to
+// Ut[col][kbase + i] (the tensor-core update's K-major operand).
+__global__ void __launch_bounds__(256, 1) k_lu_panels(NewtonCell* nc, int nslots, int k0, int nchunks, int kbase) {
     const int slot = blockIdx.y;
     if (slot >= nslots) return;
     NewtonCell& N = nc[slot];
@@ -399,46 +428,66 @@ __global__ void __launch_bounds__(256) k_lu_panels(NewtonCell* nc, int nslots, i
     const int kb = min(kNb, m - k0);
     const int r0 = k0 + kb;
     if (r0 >= m) return;
-    __shared__ float D[kNb][kNb + 1];
-    load_block_padded(N, k0, kb, D);
-    __syncthreads();
     const int half = nchunks / 2;
-    float x[kNb];
-    if ((int)blockIdx.x < half) {   // columns: forward substitution with the unit lower L11
+    const bool cols = (int)blockIdx.x < half;
+    __shared__ __align__(16) float D[kNb][kNb];   // Linv for the columns, Uinv for the rows
+    {
+        const float4* src = reinterpret_cast<const float4*>(N.Dinv + (size_t)(k0 / kNb) * 2 * kNb * kNb +
+                                                            (cols ? 0 : kNb * kNb));
+        float4* dst = reinterpret_cast<float4*>(&D[0][0]);
+        for (int i = threadIdx.x; i < kNb * kNb / 4; i += blockDim.x) dst[i] = src[i];
+    }
+    __syncthreads();
+    // kb == 64 here: a partial diagonal block is the last one and has no panels
+    float a[kNb];
+    if (cols) {   // u = Linv a (Linv unit lower): u_i = a_i + sum_{j < i} Linv[i][j] a_j
         for (int col = r0 + blockIdx.x * blockDim.x + threadIdx.x; col < m; col += half * blockDim.x) {
 #pragma unroll
-            for (int i = 0; i < kNb; ++i) x[i] = i < kb ? N.J[(size_t)(k0 + i) * N.ld + col] : 0.0f;
+            for (int i = 0; i < kNb; ++i) a[i] = N.J[(size_t)(k0 + i) * N.ld + col];
+            float4* ut = N.Ut ? reinterpret_cast<float4*>(N.Ut + (size_t)col * N.utld + kbase) : nullptr;
 #pragma unroll
-            for (int i = 1; i < kNb; ++i) {
-                float a = x[i];
+            for (int ig = 0; ig < kNb / 4; ++ig) {
+                float u[4];
 #pragma unroll
-                for (int j = 0; j < i; ++j) a -= D[i][j] * x[j];
-                x[i] = a;
-            }
+                for (int q = 0; q < 4; ++q) {
+                    const int i = 4 * ig + q;
+                    const float4* d4 = reinterpret_cast<const float4*>(&D[i][0]);
+                    float s = a[i];
 #pragma unroll
-            for (int i = 0; i < kNb; ++i)
-                if (i < kb) N.J[(size_t)(k0 + i) * N.ld + col] = x[i];
-            if (N.Ut) {
-                float4* u = reinterpret_cast<float4*>(N.Ut + (size_t)col * N.utld + kbase);
-#pragma unroll
-                for (int i = 0; i < kNb / 4; ++i) u[i] = make_float4(x[4 * i], x[4 * i + 1], x[4 * i + 2], x[4 * i + 3]);
+                    for (int jg = 0; jg < (i + 3) / 4; ++jg) {   // Linv[i][j] = 0 for j >= i
+                        const float4 d = d4[jg];
+                        s += d.x * a[4 * jg] + (4 * jg + 1 < i ? d.y * a[4 * jg + 1] : 0.0f) +
+                             (4 * jg + 2 < i ? d.z * a[4 * jg + 2] : 0.0f) + (4 * jg + 3 < i ? d.w * a[4 * jg + 3] : 0.0f);
+                    }
+                    u[q] = s;
+                    N.J[(size_t)(k0 + i) * N.ld + col] = s;
+                }
+                if (ut) ut[ig] = make_float4(u[0], u[1], u[2], u[3]);
+                asm volatile("" ::: "memory");   // keep the next group's loads from being hoisted (registers)
             }
         }
-    } else {                         // rows: x U11 = a
+    } else {      // l = a Uinv (Uinv upper): l_j = sum_{i <= j} a_i Uinv[i][j]
         for (int row = r0 + (blockIdx.x - half) * blockDim.x + threadIdx.x; row < m; row += half * blockDim.x) {
-            float* ar = N.J + (size_t)row * N.ld + k0;
+            float4* ar = reinterpret_cast<float4*>(N.J + (size_t)row * N.ld + k0);
 #pragma unroll
-            for (int j = 0; j < kNb; ++j) x[j] = j < kb ? ar[j] : 0.0f;
-#pragma unroll
-            for (int j = 0; j < kNb; ++j) {
-                float s = x[j];
-#pragma unroll
-                for (int i = 0; i < j; ++i) s -= x[i] * D[i][j];
-                x[j] = s / D[j][j];
+            for (int ig = 0; ig < kNb / 4; ++ig) {
+                const float4 v = ar[ig];
+                a[4 * ig] = v.x; a[4 * ig + 1] = v.y; a[4 * ig + 2] = v.z; a[4 * ig + 3] = v.w;
             }
 #pragma unroll
-            for (int j = 0; j < kNb; ++j)
-                if (j < kb) ar[j] = x[j];
+            for (int jg = 0; jg < kNb / 4; ++jg) {
+                float l[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+                for (int i = 0; i < 4 * jg + 4; ++i) {   // Uinv[i][j] = 0 for i > j
+                    const float4 d = *reinterpret_cast<const float4*>(&D[i][4 * jg]);
+                    l[0] += i <= 4 * jg ? a[i] * d.x : 0.0f;
+                    l[1] += i <= 4 * jg + 1 ? a[i] * d.y : 0.0f;
+                    l[2] += i <= 4 * jg + 2 ? a[i] * d.z : 0.0f;
+                    l[3] += a[i] * d.w;
+                }
+                ar[jg] = make_float4(l[0], l[1], l[2], l[3]);
+                asm volatile("" ::: "memory");
+            }
         }
     }
 }
@@ -555,61 +604,83 @@ __global__ void k_trsv_init(NewtonCell* nc, int nslots) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * N.n; i += gridDim.x * blockDim.x) N.z[i] = (float)N.r[i];
 }
 
-// diagonal block b0: lower (unit) forward or upper backward substitution; the block is
-// staged in shared memory by the CTA, the substitution runs on warp 0
-__global__ void __launch_bounds__(256) k_trsv_diag(NewtonCell* nc, int nslots, int b0, int upper) {
-    NewtonCell& N = nc[blockIdx.x];
-    const int m = 2 * N.n;
-    if (blockIdx.x >= nslots || !N.active || b0 >= m) return;
-    const int kb = min(kNb, m - b0), lane = threadIdx.x & 31;
-    __shared__ float T[kNb][kNb + 1];
-    __shared__ float y[kNb];
-    load_block_padded(N, b0, kb, T);
-    if (threadIdx.x < kNb) y[threadIdx.x] = threadIdx.x < kb ? N.z[b0 + threadIdx.x] : 0.0f;
-    __syncthreads();
-    if (threadIdx.x >= 32) return;
-    if (!upper) {
-        for (int i = 1; i < kb; ++i) {
-            float s = (lane < i ? T[i][lane] * y[lane] : 0.0f) + (lane + 32 < i ? T[i][lane + 32] * y[lane + 32] : 0.0f);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) y[i] -= s;
-            __syncwarp();
-        }
-    } else {
-        for (int i = kb - 1; i >= 0; --i) {
-            float s = (lane > i && lane < kb ? T[i][lane] * y[lane] : 0.0f) +
-                      (lane + 32 > i && lane + 32 < kb ? T[i][lane + 32] * y[lane + 32] : 0.0f);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-            if (lane == 0) y[i] = (y[i] - s) / T[i][i];
-            __syncwarp();
-        }
-    }
-    for (int i = lane; i < kb; i += 32) N.z[b0 + i] = y[i];
-}
-
-// rows outside block b0 (below it for L, above it for U) -= their 64 entries of the block times y_block
-constexpr int kTrsvRows = 64;
-__global__ void __launch_bounds__(256) k_trsv_update(NewtonCell* nc, int nslots, int b0, int upper) {
+// One block step of the triangular solves with the diagonal blocks' explicit inverses.
+// Forward (L): x_b = Linv_b z_b into zt, then z_i -= L[i, b] x_b for the rows below.
+// Backward (U): x_b = Uinv_b zt_b into z, then zt_i -= U[i, b] x_b for the rows above.
+// Every CTA forms x_b itself (a 64 x 64 matvec) from the block's final input; CTA 0
+// stores it.  The rows a CTA updates never include the block's own rows.
+constexpr int kTrsvRows = 128;
+__global__ void __launch_bounds__(256) k_trsv_step(NewtonCell* nc, int nslots, int b0, int upper) {
     NewtonCell& N = nc[blockIdx.y];
     const int m = 2 * N.n;
     if (blockIdx.y >= nslots || !N.active || b0 >= m) return;
     const int kb = min(kNb, m - b0);
     const int lo = upper ? 0 : b0 + kb, hi = upper ? b0 : m;
     const int r0 = lo + blockIdx.x * kTrsvRows;
-    if (r0 >= hi) return;
-    __shared__ float yb[kNb];
-    if (threadIdx.x < kNb) yb[threadIdx.x] = threadIdx.x < kb ? N.z[b0 + threadIdx.x] : 0.0f;
+    if (blockIdx.x > 0 && r0 >= hi) return;
+    const float* in = upper ? N.zt : N.z;
+    float* out = upper ? N.z : N.zt;
+    float* upd = upper ? N.zt : N.z;
+    __shared__ float T[kNb][kNb + 1];
+    __shared__ float rb[kNb], xb[kNb];
+    const float* inv = N.Dinv + (size_t)(b0 / kNb) * 2 * kNb * kNb + (upper ? kNb * kNb : 0);
+    for (int i = threadIdx.x; i < kNb * kNb; i += blockDim.x) T[i >> 6][i & (kNb - 1)] = inv[i];
+    if (threadIdx.x < kNb) rb[threadIdx.x] = threadIdx.x < kb ? in[b0 + threadIdx.x] : 0.0f;
     __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int i = r0 + warp; i < min(r0 + kTrsvRows, hi); i += 8) {
-        const float* Ai = N.J + (size_t)i * N.ld + b0;
-        float s = (lane < kb ? Ai[lane] * yb[lane] : 0.0f) + (lane + 32 < kb ? Ai[lane + 32] * yb[lane + 32] : 0.0f);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) N.z[i] -= s;
+    if (threadIdx.x < kNb) {
+        float s = 0.0f;
+#pragma unroll 16
+        for (int k = 0; k < kNb; ++k) s += T[threadIdx.x][k] * rb[k];
+        xb[threadIdx.x] = s;
+        if (blockIdx.x == 0 && threadIdx.x < kb) out[b0 + threadIdx.x] = s;
     }
+    __syncthreads();
+    // a warp per row, four rows in flight: rows i, i + 8, i + 16, i + 24
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rend = min(r0 + kTrsvRows, hi);
+    const float x0 = xb[lane], x1 = xb[lane + 32];
+    for (int i = r0 + warp; i < rend; i += 32) {
+        float s[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int r = i + 8 * u;
+            const float* Ai = N.J + (size_t)r * N.ld + b0;
+            s[u] = r < rend ? (lane < kb ? Ai[lane] * x0 : 0.0f) + (lane + 32 < kb ? Ai[lane + 32] * x1 : 0.0f) : 0.0f;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) s[u] += __shfl_xor_sync(0xffffffffu, s[u], o);
+        if (lane < 4) {
+            const int r = i + 8 * lane;
+            const float v = lane == 0 ? s[0] : lane == 1 ? s[1] : lane == 2 ? s[2] : s[3];
+            if (r < rend) upd[r] -= v;
+        }
+    }
+}
+
+// per-iteration clears, one launch each over all cells: the correction and the FP32
+// workspace of active cells; entries [first, first + count) of every cell's norms;
+// the dense tangent of active cells before its assembly
+__global__ void k_newton_clear(NewtonCell* nc, int nslots) {
+    NewtonCell& N = nc[blockIdx.y];
+    if (blockIdx.y >= nslots || !N.active) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * N.n; i += gridDim.x * blockDim.x) {
+        N.dx[i] = 0.0;
+        N.z[i] = 0.0f;
+    }
+}
+__global__ void k_norms_clear(double* norms, int nslots, int first, int count) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nslots * count; i += gridDim.x * blockDim.x)
+        norms[8 * (size_t)(i / count) + first + i % count] = 0.0;
+}
+__global__ void k_dense_clear(NewtonCell* nc, int nslots) {
+    NewtonCell& N = nc[blockIdx.y];
+    if (blockIdx.y >= nslots || !N.active) return;
+    float4* J = reinterpret_cast<float4*>(N.J);   // 2n rows of ld floats, ld a multiple of 4
+    const size_t n4 = (size_t)2 * N.n * N.ld / 4;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x)
+        J[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 }
 
 // dx += z; r = -G - J dx in FP64 with J element by element (diagonal + the FP32 element
@@ -872,22 +943,32 @@ const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots,
     }
     return failed;
 }
+void launch_newton_clear(NewtonCell* nc, int nslots, int max_n, cudaStream_t st) {
+    k_newton_clear<<<dim3((unsigned)std::max(1, std::min((2 * max_n + 255) / 256, 32)), (unsigned)nslots), 256, 0, st>>>(
+        nc, nslots);
+}
+void launch_norms_clear(double* norms, int nslots, int first, int count, cudaStream_t st) {
+    const int n = nslots * count;
+    k_norms_clear<<<std::max(1, std::min((n + 255) / 256, 64)), 256, 0, st>>>(norms, nslots, first, count);
+}
+void launch_dense_clear(NewtonCell* nc, int nslots, int max_n, cudaStream_t st) {
+    const size_t n4 = (size_t)2 * max_n * (2 * max_n + 4) / 4;
+    const unsigned gx = (unsigned)std::max<size_t>(1, std::min<size_t>((n4 + 255) / 256, 1024));
+    k_dense_clear<<<dim3(gx, (unsigned)nslots), 256, 0, st>>>(nc, nslots);
+}
+
 void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, cudaStream_t st) {
     const int m = 2 * max_n, nblk = (m + kNb - 1) / kNb;
     k_trsv_init<<<dim3((unsigned)std::max(1, std::min((m + 255) / 256, 32)), (unsigned)nslots), 256, 0, st>>>(nc, nslots);
     for (int b = 0; b < nblk; ++b) {   // forward, L
-        k_trsv_diag<<<nslots, 256, 0, st>>>(nc, nslots, b * kNb, 0);
         const int rows = m - (b + 1) * kNb;
-        if (rows > 0)
-            k_trsv_update<<<dim3((unsigned)((rows + kTrsvRows - 1) / kTrsvRows), (unsigned)nslots), 256, 0, st>>>(
-                nc, nslots, b * kNb, 0);
+        const unsigned g = (unsigned)std::max(1, (rows + kTrsvRows - 1) / kTrsvRows);
+        k_trsv_step<<<dim3(g, (unsigned)nslots), 256, 0, st>>>(nc, nslots, b * kNb, 0);
     }
     for (int b = nblk - 1; b >= 0; --b) {   // backward, U
-        k_trsv_diag<<<nslots, 256, 0, st>>>(nc, nslots, b * kNb, 1);
         const int rows = b * kNb;
-        if (rows > 0)
-            k_trsv_update<<<dim3((unsigned)((rows + kTrsvRows - 1) / kTrsvRows), (unsigned)nslots), 256, 0, st>>>(
-                nc, nslots, b * kNb, 1);
+        const unsigned g = (unsigned)std::max(1, (rows + kTrsvRows - 1) / kTrsvRows);
+        k_trsv_step<<<dim3(g, (unsigned)nslots), 256, 0, st>>>(nc, nslots, b * kNb, 1);
     }
 }
 void launch_newton_refine(const CellDev* cells, NewtonCell* nc, const int* cell_slot, const WorkItem* work, int nwork,
