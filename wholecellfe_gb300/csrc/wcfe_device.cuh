@@ -153,13 +153,15 @@ struct NewtonCell {
     float* Dinv;         // [ceil(2n/64)][2][64][64] inverses of the 64 x 64 diagonal blocks' unit-lower and
                          //      upper factors (identity-padded), row-major
     float* zt;           // [2n] FP32 solve workspace (the forward solve's result)
+    float* At;           // [2n][64] the current row panel A12, transposed (tensor-core operand)
 };
 
-// TMA descriptors of one cell's dense LU: J (fp32, 2n x 2n, row stride ld) and Ut
-// (2n rows x utld), both read as boxes of 32 columns x 128 rows, 128-byte swizzled
+// TMA descriptors of one cell's dense LU (fp32, 128-byte swizzled boxes)
 struct LuMaps {
-    CUtensorMap jmap;
-    CUtensorMap umap;
+    CUtensorMap jmap;    // J: 32 columns x 128 rows
+    CUtensorMap umap;    // Ut: 32 columns x 128 rows
+    CUtensorMap amap;    // At: 32 columns x 128 rows
+    CUtensorMap dmap;    // the diagonal blocks' Linv / Uinv^T (Dinv as [nblk * 128][64]): 32 columns x 64 rows
 };
 
 // One trailing-update launch of the blocked LU: per cell, C[rows, cols] -= J[rows, ka:ka+K]

@@ -1500,7 +1500,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
     const size_t o_norm = put(sizeof(double) * 8 * ns), o_nc = put(sizeof(NewtonCell) * ns);
     const size_t o_id = put(sizeof(int) * ns), o_tk = put(sizeof(unsigned int) * ns);
     const size_t o_maps = put(sizeof(LuMaps) * ns);
-    struct Off { size_t J, Ut, Dinv, Ke, diag, G, dx, d, r, z, zt; int n, ld; };
+    struct Off { size_t J, Ut, Dinv, At, Ke, diag, G, dx, d, r, z, zt; int n, ld; };
     std::vector<Off> off(ns);
     P.max_n = 0;
     for (int sl = 0; sl < ns; ++sl) {
@@ -1513,6 +1513,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         f.Ut = put(sizeof(float) * (size_t)m * kLuUtld);
         f.Dinv = put(sizeof(float) * 2 * 64 * 64 * (size_t)((m + 63) / 64));
         f.zt = put(sizeof(float) * m);
+        f.At = put(sizeof(float) * 64 * (size_t)m);
         f.Ke = put(sizeof(float) * 36 * (size_t)c->topo.nt);
         f.diag = put(sizeof(double) * n);
         f.G = put(sizeof(double) * m);
@@ -1552,6 +1553,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         N.pad2 = 0;
         N.Dinv = (float*)(b + f.Dinv);
         N.zt = (float*)(b + f.zt);
+        N.At = (float*)(b + f.At);
         N.Ke = (float*)(b + f.Ke);
         N.diag = (double*)(b + f.diag);
         N.G = (double*)(b + f.G);
@@ -1823,8 +1825,8 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     const size_t npref = lu_prefix_capacity(1, m);
     const size_t ndinv = 2 * 64 * 64 * (size_t)((m + 63) / 64);
     const size_t bytes = sizeof(float) * (size_t)m * ld + sizeof(float) * (size_t)m * kLuUtld + sizeof(double) * m +
-                         2 * sizeof(float) * m + sizeof(float) * ndinv + sizeof(double) * 8 + sizeof(NewtonCell) +
-                         sizeof(LuMaps) + sizeof(int) * npref + 10 * 256;
+                         2 * sizeof(float) * m + sizeof(float) * ndinv + sizeof(float) * 64 * (size_t)m +
+                         sizeof(double) * 8 + sizeof(NewtonCell) + sizeof(LuMaps) + sizeof(int) * npref + 11 * 256;
     char* blk = nullptr;
     CK(cudaMalloc(&blk, bytes));
     size_t o = 0;
@@ -1837,6 +1839,7 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     N.z = (float*)take(sizeof(float) * m);
     N.zt = (float*)take(sizeof(float) * m);
     N.Dinv = (float*)take(sizeof(float) * ndinv);
+    N.At = (float*)take(sizeof(float) * 64 * (size_t)m);
     N.norms = (double*)take(sizeof(double) * 8);
     N.n = m / 2;
     N.ld = ld;

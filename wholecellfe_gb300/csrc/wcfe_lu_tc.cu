@@ -44,7 +44,7 @@ constexpr long long kWait = 2000000000ll;          // SM clocks (about 1 s) befo
 constexpr size_t kSmemBytes = 1024 + (size_t)kStages * kStageBytes + 256;
 
 struct Tile {
-    int slot, tm, tn, rhi, chi;
+    int slot, reg, tm, tn, rhi, chi;
 };
 
 __device__ __forceinline__ void region_of(const LuUpdateArgs& a, int r, int m, int& rlo, int& rhi, int& clo,
@@ -67,6 +67,7 @@ __device__ __forceinline__ Tile decode_tile(const NewtonCell* nc, const int* __r
     Tile t;
     t.slot = lo / a.nreg;
     const int reg = lo - t.slot * a.nreg;
+    t.reg = reg;
     const int m = 2 * nc[t.slot].n;
     int rlo, rhi, clo, chi;
     region_of(a, reg, m, rlo, rhi, clo, chi);
@@ -237,14 +238,195 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
     }
 }
 
+// ---------------------------------------------------------------------------- panels
+// The two panels of a 64-wide LU step as tcgen05 GEMMs with N = 64, K = 64, from the
+// diagonal block's explicit inverses (Dinv block b: Linv rows, then Uinv^T rows):
+//   region 0, 128-row tiles of L21:  L21 = A21 Uinv     (A: J rows, B: Uinv^T)
+//        D[i][j] in TMEM lane i: the thread of row i writes J[i][k0 + j], 64 B per slice;
+//   region 1, 128-column tiles of U12:  U12^T = A12^T Linv^T   (A: At rows, B: Linv)
+//        D[c][i] in TMEM lane c: Ut[c][kbase + i] (64 B per slice) and J[k0 + i][c]
+//        (coalesced across the warp's columns).
+// Same pipeline as the update kernel; 16 epilogue warps, each 16 TMEM columns of a quadrant.
+constexpr int kPN = 64;                                  // panel width (N)
+constexpr uint32_t kPBoxA = 128u * 128u, kPBoxB = 64u * 128u;
+constexpr uint32_t kPStageBytes = kPBoxA + kPBoxB;       // 24 KB, a multiple of 1024
+constexpr uint32_t kPTmemCols = 128;                     // two 64-column accumulators
+constexpr size_t kPSmemBytes = 1024 + (size_t)kStages * kPStageBytes + 256;
+
+__global__ void __launch_bounds__(kThreads, 1) k_lu_panels_tc(NewtonCell* nc, const LuMaps* __restrict__ maps,
+                                                             const int* __restrict__ prefix, int ngroups,
+                                                             LuUpdateArgs a) {
+    extern __shared__ uint8_t tc_smem_raw[];
+    uint8_t* sm = tc_smem_raw + ((1024u - (smem_addr(tc_smem_raw) & 1023u)) & 1023u);
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm + kStages * kPStageBytes);
+    uint64_t* empty = full + kStages;
+    uint64_t* tfull = empty + kStages;
+    uint64_t* tempty = tfull + 2;
+    uint64_t* drain = tempty + 2;
+    uint32_t* tbase_s = reinterpret_cast<uint32_t*>(drain + 1);
+    volatile int* abort_s = reinterpret_cast<volatile int*>(tbase_s + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int total = __ldg(prefix + ngroups);
+    const int k0 = a.ka, kbase = a.kb;
+    const int dblk = (k0 / kPN) * 2 * kPN;   // the block's first row in the Dinv map
+    constexpr int nch = kPN / kBK;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(full + s, 1);
+            mbar_init(empty + s, 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(tfull + b, 1);
+            mbar_init(tempty + b, kEpiWarps);
+        }
+        mbar_init(drain, 1);
+        *abort_s = 0;
+        mbar_init_fence();
+    }
+    if (warp == 1) {
+        tc_alloc(tbase_s, kPTmemCols);
+        tc_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tbase = *tbase_s;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            int g = 0;
+            for (int f = blockIdx.x; f < total && !*abort_s; f += gridDim.x) {
+                const Tile t = decode_tile(nc, prefix, ngroups, a, f);
+                const LuMaps* mp = maps + t.slot;
+                const bool lpanel = t.reg == 0;
+                const CUtensorMap* amap = lpanel ? &mp->jmap : &mp->amap;
+                tmap_acquire(amap);
+                tmap_acquire(&mp->dmap);
+                for (int c = 0; c < nch; ++c, ++g) {
+                    const int s = g % kStages;
+                    const uint32_t u = (uint32_t)(g / kStages);
+                    if (!mbar_wait_bounded(empty + s, (u & 1u) ^ 1u, kWait)) {
+                        *abort_s = 1;
+                        nc[t.slot].norms[3] = 2.0;
+                        break;
+                    }
+                    uint8_t* st = sm + s * kPStageBytes;
+                    mbar_arrive_expect_tx(full + s, kPStageBytes);
+                    if (lpanel) tma_load_2d(st, amap, k0 + c * kBK, t.tm, full + s);   // A21 rows
+                    else tma_load_2d(st, amap, c * kBK, t.tn, full + s);                // At rows
+                    tma_load_2d(st + kPBoxA, &mp->dmap, c * kBK, dblk + (lpanel ? kPN : 0), full + s);
+                }
+            }
+            for (int s = 0; s < kStages && s < g; ++s) {
+                const uint32_t ulast = (uint32_t)((g - 1 - s) / kStages);
+                mbar_wait_bounded(full + s, ulast & 1u, kWait);
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = tc_idesc_tf32(kTile, kPN);
+            int g = 0, it = 0;
+            for (int f = blockIdx.x; f < total && !*abort_s; f += gridDim.x, ++it) {
+                const int b = it & 1;
+                const uint32_t v = (uint32_t)(it >> 1);
+                if (!mbar_wait_bounded(tempty + b, (v & 1u) ^ 1u, kWait)) {
+                    *abort_s = 1;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t d = tbase + (uint32_t)(b * kPN);
+                bool ok = true;
+                for (int c = 0; c < nch; ++c, ++g) {
+                    const int s = g % kStages;
+                    const uint32_t u = (uint32_t)(g / kStages);
+                    if (!mbar_wait_bounded(full + s, u & 1u, kWait)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = smem_addr(sm + s * kPStageBytes);
+                    const uint64_t da = tc_desc_k_sw128(sa), db = tc_desc_k_sw128(sa + kPBoxA);
+#pragma unroll
+                    for (int k = 0; k < kBK / 8; ++k)
+                        tc_mma_tf32(d, da + 2u * (uint32_t)k, db + 2u * (uint32_t)k, idesc, (uint32_t)(c | k));
+                    tc_commit(empty + s);
+                }
+                if (!ok) {
+                    *abort_s = 1;
+                    break;
+                }
+                tc_commit(tfull + b);
+            }
+            tc_commit(drain);
+            mbar_wait_bounded(drain, 0u, kWait);
+        }
+        __syncwarp();
+    } else {
+        const int q = warp & 3;
+        const int j0 = 16 * ((warp - 2) >> 2);   // the 16 TMEM columns (panel entries) of this warp
+        const uint32_t lane_field = (uint32_t)(32 * q) << 16;
+        int it = 0;
+        for (int f = blockIdx.x; f < total; f += gridDim.x, ++it) {
+            const int b = it & 1;
+            const uint32_t v = (uint32_t)(it >> 1);
+            const Tile t = decode_tile(nc, prefix, ngroups, a, f);
+            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(tfull + b, v & 1u, kWait));
+            if (!ok) {
+                if (lane == 0) nc[t.slot].norms[3] = 2.0;
+                *abort_s = 1;
+                break;
+            }
+            tc_fence_after();
+            float p[16];
+            tc_ld_32x32b_x16(tbase + (uint32_t)(b * kPN + j0) + lane_field, p);
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty + b);
+            NewtonCell& N = nc[t.slot];
+            const int m = 2 * N.n;
+            if (t.reg == 0) {   // L21 row
+                const int row = t.tm + 32 * q + lane;
+                if (row < m) {
+                    float4* dst = reinterpret_cast<float4*>(N.J + (size_t)row * N.ld + k0 + j0);
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) dst[r] = make_float4(p[4 * r], p[4 * r + 1], p[4 * r + 2], p[4 * r + 3]);
+                }
+            } else {            // U12 column
+                const int col = t.tn + 32 * q + lane;
+                if (col < m) {
+                    if (N.Ut) {
+                        float4* ut = reinterpret_cast<float4*>(N.Ut + (size_t)col * N.utld + kbase + j0);
+#pragma unroll
+                        for (int r = 0; r < 4; ++r)
+                            ut[r] = make_float4(p[4 * r], p[4 * r + 1], p[4 * r + 2], p[4 * r + 3]);
+                    }
+                    float* dst = N.J + (size_t)(k0 + j0) * N.ld + col;
+#pragma unroll
+                    for (int r = 0; r < 16; ++r) dst[(size_t)r * N.ld] = p[r];
+                }
+            }
+            if (*abort_s) break;
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tc_dealloc(tbase, kPTmemCols);
+    }
+}
+
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 int g_sms = 0;
 int g_lu_tc_regs = 0, g_lu_tc_max_threads = 0;
 
-int encode_f32_2d(CUtensorMap* map, const float* base, uint64_t cols, uint64_t rows, uint64_t row_bytes) {
+int encode_f32_2d(CUtensorMap* map, const float* base, uint64_t cols, uint64_t rows, uint64_t row_bytes,
+                  uint32_t box_rows = 128) {
     const cuuint64_t dims[2] = {cols, rows};
     const cuuint64_t strides[1] = {row_bytes};
-    const cuuint32_t box[2] = {32, 128};
+    const cuuint32_t box[2] = {32, box_rows};
     const cuuint32_t estr[2] = {1, 1};
     const CUresult r = g_encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box,
                                 estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -267,6 +449,9 @@ cudaError_t configure_lu_tc(int num_sms) {
     }
     cudaError_t e = cudaFuncSetAttribute((const void*)k_lu_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)kSmemBytes);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute((const void*)k_lu_panels_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kPSmemBytes);
     if (e != cudaSuccess) return e;
     cudaFuncAttributes at;
     if ((e = cudaFuncGetAttributes(&at, (const void*)k_lu_update_tc)) != cudaSuccess) return e;
@@ -293,6 +478,10 @@ int encode_lu_maps(const NewtonCell* h, int nslots, LuMaps* out) {
         if (encode_f32_2d(&out[s].jmap, h[s].J, m, m, sizeof(float) * (uint64_t)h[s].ld)) return -1;
         if (encode_f32_2d(&out[s].umap, h[s].Ut, (uint64_t)h[s].utld, m, sizeof(float) * (uint64_t)h[s].utld))
             return -1;
+        if (!h[s].At || !h[s].Dinv) return -1;
+        if (encode_f32_2d(&out[s].amap, h[s].At, 64, m, sizeof(float) * 64)) return -1;
+        const uint64_t nblk = (m + 63) / 64;
+        if (encode_f32_2d(&out[s].dmap, h[s].Dinv, 64, nblk * 128, sizeof(float) * 64, 64)) return -1;
     }
     return 0;
 }
@@ -321,6 +510,29 @@ bool launch_lu_update_tc(NewtonCell* nc, const LuMaps* maps, const int* d_prefix
     const int grid = std::max(1, std::min(total, g_sms > 0 ? g_sms : 1));
     k_lu_update_tc<<<grid, kThreads, kSmemBytes, st>>>(nc, maps, d_prefix, nslots * a.nreg, a);
     return cudaGetLastError() == cudaSuccess;
+}
+
+// the panels of the 64-wide step at a.ka = k0 (a.kb = its offset in Ut); regions as
+// lu_panel_args builds them
+bool launch_lu_panels_tc(NewtonCell* nc, const LuMaps* maps, const int* d_prefix, int nslots, int total,
+                         const LuUpdateArgs& a, cudaStream_t st) {
+    if (g_lu_tc_max_threads < kThreads) return false;
+    if (total <= 0) return true;
+    const int grid = std::max(1, std::min(total, g_sms > 0 ? g_sms : 1));
+    k_lu_panels_tc<<<grid, kThreads, kPSmemBytes, st>>>(nc, maps, d_prefix, nslots * a.nreg, a);
+    return cudaGetLastError() == cudaSuccess;
+}
+
+// region 0: 128-row tiles of L21 (rows k0 + 64 .. 2n); region 1: 128-column tiles of U12
+LuUpdateArgs lu_panel_args(int k0, int kbase) {
+    LuUpdateArgs a{};
+    a.nreg = 2;
+    a.rlo[0] = k0 + 64; a.rhi[0] = -1; a.clo[0] = 0; a.chi[0] = 1;
+    a.rlo[1] = 0; a.rhi[1] = 1; a.clo[1] = k0 + 64; a.chi[1] = -1;
+    a.ka = k0;
+    a.kb = kbase;
+    a.K = 64;
+    return a;
 }
 
 }  // namespace wcfe

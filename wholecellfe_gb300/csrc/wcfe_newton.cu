@@ -385,7 +385,8 @@ __global__ void __launch_bounds__(256) k_lu_diag(NewtonCell* nc, int nslots, int
     for (int i = ty; i < kb; i += 16)
         for (int j = tx; j < kb; j += 16) N.J[(size_t)(k0 + i) * N.ld + k0 + j] = A[i][j];
     // explicit inverses of the (identity-padded) unit-lower and upper factors, one column per
-    // thread held in registers: L X = I forward, U Y = I backward
+    // thread held in registers: L X = I forward, U Y = I backward.  Stored as Linv and Uinv^T
+    // (row-major), the K-major operands of the tensor-core panels.
     float* Li = N.Dinv + (size_t)(k0 / kNb) * 2 * kNb * kNb;
     float* Ui = Li + kNb * kNb;
     float x[kNb];
@@ -410,7 +411,7 @@ __global__ void __launch_bounds__(256) k_lu_diag(NewtonCell* nc, int nslots, int
             x[i] = s / A[i][i];
         }
 #pragma unroll
-        for (int i = 0; i < kNb; ++i) Ui[i * kNb + j] = x[i];
+        for (int i = 0; i < kNb; ++i) Ui[j * kNb + i] = x[i];   // stored transposed: row j = column j of Uinv
     }
 }
 
@@ -432,10 +433,14 @@ __global__ void __launch_bounds__(256, 1) k_lu_panels(NewtonCell* nc, int nslots
     const bool cols = (int)blockIdx.x < half;
     __shared__ __align__(16) float D[kNb][kNb];   // Linv for the columns, Uinv for the rows
     {
-        const float4* src = reinterpret_cast<const float4*>(N.Dinv + (size_t)(k0 / kNb) * 2 * kNb * kNb +
-                                                            (cols ? 0 : kNb * kNb));
-        float4* dst = reinterpret_cast<float4*>(&D[0][0]);
-        for (int i = threadIdx.x; i < kNb * kNb / 4; i += blockDim.x) dst[i] = src[i];
+        const float* src = N.Dinv + (size_t)(k0 / kNb) * 2 * kNb * kNb;
+        if (cols) {
+            const float4* s4 = reinterpret_cast<const float4*>(src);
+            float4* dst = reinterpret_cast<float4*>(&D[0][0]);
+            for (int i = threadIdx.x; i < kNb * kNb / 4; i += blockDim.x) dst[i] = s4[i];
+        } else {   // Uinv from its stored transpose
+            for (int i = threadIdx.x; i < kNb * kNb; i += blockDim.x) D[i & (kNb - 1)][i >> 6] = src[kNb * kNb + i];
+        }
     }
     __syncthreads();
     // kb == 64 here: a partial diagonal block is the last one and has no panels
@@ -489,6 +494,27 @@ __global__ void __launch_bounds__(256, 1) k_lu_panels(NewtonCell* nc, int nslots
                 asm volatile("" ::: "memory");
             }
         }
+    }
+}
+
+// At[c][k] = J[k0 + k][c] for the columns c >= k0 + 64 (the row panel A12, transposed
+// through shared memory: coalesced reads and writes)
+__global__ void __launch_bounds__(256) k_lu_transpose_a12(NewtonCell* nc, int nslots, int k0) {
+    NewtonCell& N = nc[blockIdx.y];
+    const int m = 2 * N.n;
+    if (blockIdx.y >= nslots || !N.active || k0 + kNb >= m) return;
+    const int c0 = k0 + kNb + blockIdx.x * kNb;
+    if (c0 >= m) return;
+    __shared__ float T[kNb][kNb + 1];
+    const int tx = threadIdx.x & 63, ty = threadIdx.x >> 6;   // 64 x 4
+    for (int k = ty; k < kNb; k += 4) {
+        const int c = c0 + tx;
+        T[k][tx] = c < m ? N.J[(size_t)(k0 + k) * N.ld + c] : 0.0f;
+    }
+    __syncthreads();
+    for (int cc = ty; cc < kNb; cc += 4) {
+        const int c = c0 + cc;
+        if (c < m) N.At[(size_t)c * kNb + tx] = T[tx][cc];
     }
 }
 
@@ -624,7 +650,10 @@ __global__ void __launch_bounds__(256) k_trsv_step(NewtonCell* nc, int nslots, i
     __shared__ float T[kNb][kNb + 1];
     __shared__ float rb[kNb], xb[kNb];
     const float* inv = N.Dinv + (size_t)(b0 / kNb) * 2 * kNb * kNb + (upper ? kNb * kNb : 0);
-    for (int i = threadIdx.x; i < kNb * kNb; i += blockDim.x) T[i >> 6][i & (kNb - 1)] = inv[i];
+    if (!upper)
+        for (int i = threadIdx.x; i < kNb * kNb; i += blockDim.x) T[i >> 6][i & (kNb - 1)] = inv[i];
+    else   // Uinv from its stored transpose
+        for (int i = threadIdx.x; i < kNb * kNb; i += blockDim.x) T[i & (kNb - 1)][i >> 6] = inv[i];
     if (threadIdx.x < kNb) rb[threadIdx.x] = threadIdx.x < kb ? in[b0 + threadIdx.x] : 0.0f;
     __syncthreads();
     if (threadIdx.x < kNb) {
@@ -825,6 +854,9 @@ cudaError_t configure_lu_tc(int num_sms);
 int lu_update_prefix(const NewtonCell* h, int nslots, const LuUpdateArgs& a, int* pref);
 bool launch_lu_update_tc(NewtonCell* nc, const LuMaps* maps, const int* d_prefix, int nslots, int total,
                          const LuUpdateArgs& a, cudaStream_t st);
+bool launch_lu_panels_tc(NewtonCell* nc, const LuMaps* maps, const int* d_prefix, int nslots, int total,
+                         const LuUpdateArgs& a, cudaStream_t st);
+LuUpdateArgs lu_panel_args(int k0, int kbase);
 
 cudaError_t configure_newton(size_t max_smem, int num_sms) {
     g_num_sms = num_sms;
@@ -860,8 +892,10 @@ void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int
 // row strips; the trailing matrix then takes one update with K = nb on the tcgen05
 // tensor cores.  The per-launch tile counts go to the device in one copy (d_prefix,
 // lu_prefix_capacity ints).
+// per 64-wide step at most a panel launch and an update launch of two regions each, plus
+// per outer block one update of one region
 size_t lu_prefix_capacity(int nslots, int max_m) {
-    return (size_t)2 * ((size_t)(max_m + kNb - 1) / kNb + 1) * (2 * (size_t)nslots + 1);
+    return (size_t)3 * ((size_t)(max_m + kNb - 1) / kNb + 1) * (2 * (size_t)nslots + 1);
 }
 
 const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots, int max_m, const LuMaps* maps,
@@ -889,12 +923,12 @@ const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots,
         return failed;
     }
     struct Op {
-        int type, k0, kbase, pref, total;   // type 0 diag, 1 panels, 2 update
+        int type, k0, kbase, pref, total;   // type 0 diag, 1 panels (A12 transpose + tcgen05 panels), 2 update
         LuUpdateArgs a;
     };
     std::vector<Op> ops;
     std::vector<int> pref;
-    auto update = [&](const LuUpdateArgs& a) {
+    auto tiles = [&](int type, int k0, const LuUpdateArgs& a) {
         const size_t at = pref.size();
         pref.resize(at + (size_t)nslots * a.nreg + 1);
         const int total = lu_update_prefix(h_nc, nslots, a, pref.data() + at);
@@ -902,14 +936,15 @@ const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots,
             pref.resize(at);
             return;
         }
-        ops.push_back({2, 0, 0, (int)at, total, a});
+        ops.push_back({type, k0, a.kb, (int)at, total, a});
     };
+    auto update = [&](const LuUpdateArgs& a) { tiles(2, 0, a); };
     for (int K0 = 0; K0 < max_m; K0 += nb) {
         for (int ib = 0; ib < nb / kNb && K0 + ib * kNb < max_m; ++ib) {
             const int k0 = K0 + ib * kNb;
             ops.push_back({0, k0, 0, 0, 0, {}});
             if (max_m - k0 - kNb <= 0) break;
-            ops.push_back({1, k0, ib * kNb, 0, 0, {}});
+            tiles(1, k0, lu_panel_args(k0, ib * kNb));
             LuUpdateArgs a{};   // the rest of the outer block's column strip, then of its row strip
             a.nreg = 2;
             a.rlo[0] = k0 + kNb; a.rhi[0] = -1; a.clo[0] = k0 + kNb; a.chi[0] = K0 + nb;
@@ -928,14 +963,19 @@ const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots,
         a.rlo[1] = a.rhi[1] = a.clo[1] = a.chi[1] = 0;
         update(a);
     }
+    if (pref.size() > lu_prefix_capacity(nslots, max_m)) return "tile lists (capacity)";
     if (!pref.empty()) cudaMemcpyAsync(d_prefix, pref.data(), sizeof(int) * pref.size(), cudaMemcpyHostToDevice, st);
     for (const Op& o : ops) {
         if (o.type == 0) {
             k_lu_diag<<<nslots, 256, 0, st>>>(nc, nslots, o.k0);
             checked("k_lu_diag");
         } else if (o.type == 1) {
-            panels(o.k0, o.kbase);
-            checked("k_lu_panels");
+            const int rest = max_m - o.k0 - kNb;
+            k_lu_transpose_a12<<<dim3((unsigned)((rest + kNb - 1) / kNb), (unsigned)nslots), 256, 0, st>>>(nc, nslots,
+                                                                                                          o.k0);
+            checked("k_lu_transpose_a12");
+            if (!launch_lu_panels_tc(nc, maps, d_prefix + o.pref, nslots, o.total, o.a, st) && !failed)
+                failed = "k_lu_panels_tc";
         } else {
             if (!launch_lu_update_tc(nc, maps, d_prefix + o.pref, nslots, o.total, o.a, st) && !failed)
                 failed = "k_lu_update_tc";
