@@ -638,7 +638,7 @@ def main():
     ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain", "newton", "config2"],
                     help="profiling aid: run only one timed loop (default shape, no autotune) and print its timing")
     ap.add_argument("--lu", default="256,0", help="--phase newton: LU outer block and kind (0 tcgen05, 1 mma.sync)")
-    ap.add_argument("--newton-cells", type=int, default=64,
+    ap.add_argument("--newton-cells", type=int, default=512,
                     help="cells of the bounded implicit-step (Newton, dense LU) measurement (0: skip)")
     ap.add_argument("--shape", default="", help="with --phase: patch threads,elements (default: the engine's)")
     ap.add_argument("--patch-kernel", type=int, default=1, choices=[0, 1],

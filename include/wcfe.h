@@ -361,6 +361,31 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
  * with the cell's state as step start, and the mass/damping diagonal [n]. */
 int wcfe_cell_newton_tangent(wcfe_engine* e, int32_t id, double dt, const double* x, float* J_out, double* diag_out);
 
+/* ---- VTK frames (cellBP/iomesh.cpp:690-1047), byte for byte ------------------
+ * Replaces the reference's write_vtk calls (cellBP/main.cpp:447-454, :721-723) without
+ * stalling the stepping stream: a write packs the cell's current state on the engine's
+ * stream (one gather kernel, either precision), copies it to pinned host memory on the
+ * frame writer's own stream, and a host writer thread formats and writes the file.
+ * slots: staging buffers in flight (a write waits for a free one); threads: writer
+ * threads.  format 0: positions and triangles (iomesh.cpp:690); 1: strain measure
+ * sqrt(det((I - 2 ea)^-1)) and bond vectors, fixed notation (:730, the substrate's
+ * frames); 2: c_A, the strain measure, c_C, the integrin force and the bond vectors
+ * (:844, the cell's frames; the force follows the cell's law: for WCFE_LAW_MD_TABLE
+ * (kMD) the MD table, or kint |u| when kint >= 0; else |k_lin u| in the plane (k1,
+ * k31)).  time: the header's time; NaN takes the cell's clock. */
+typedef struct wcfe_frames wcfe_frames;
+int wcfe_frames_create(wcfe_engine* e, int32_t slots, int32_t threads, wcfe_frames** out);
+int wcfe_frames_write(wcfe_frames* f, int32_t cell, int32_t format, double time, double kint, const char* path);
+/* wait until every queued frame is written; the first write error since the last flush */
+int wcfe_frames_flush(wcfe_frames* f);
+int wcfe_frames_destroy(wcfe_frames* f);
+/* Host only: the text of a frame from host arrays (x, fau [n][3], cA, cC [n], ea [n][6]);
+ * law and k_fa give the force column of format 2 as above.  Copies at most cap bytes
+ * to out; *len is the full length. */
+int wcfe_vtk_format(int32_t format, int32_t n, int32_t nt, const int32_t* tri, const double* x, const double* cA,
+                    const double* cC, const double* fau, const double* ea, double time, double kint, int32_t law,
+                    double k_fa, char* out, int64_t cap, int64_t* len);
+
 /* ---- host-only inspection of the connectivity preprocessing (no device) --- */
 /* Boundary ranks and neighbour candidates (the scan of UL:1500-1531), patches and
  * one-ring slot codes, exactly as the engine builds them.  Capacities in int32 units. */

@@ -3,6 +3,7 @@
 # oracle/_ref/libwcfe_ref_<variant>.so (test infrastructure: pins the C
 # restatement and generates tests/golden/).  Compiles, per variant, exactly
 #   cellBP/UL_growth_explicit.cpp + eltopo3d/nondestructivetrimesh.cpp
+#   + cellBP/iomesh.cpp and common/bfstream.cpp (the VTK frame writers)
 # with the reference's own release flags (-O3 -funroll-loops, cellBP/Makefile.local_defs:9)
 # plus -fPIC, and links the harness (ref_harness.cpp) and the rand()/srand()
 # stand-ins (ref_rng.c) with -Bsymbolic.  Does not run the reference's build system.
@@ -24,10 +25,14 @@ for V in kMD k1 k31; do
     FLAGS="-O3 -funroll-loops -fPIC -w -D__LITTLE_ENDIAN__ -DNO_GUI"
     g++ $FLAGS $INC -c "$D/cellBP/UL_growth_explicit.cpp" -o "$OUT/ul_$V.o" &
     g++ $FLAGS $INC -c "$D/eltopo3d/nondestructivetrimesh.cpp" -o "$OUT/ndtm_$V.o" &
-    g++ $FLAGS $INC -c "$HERE/ref_harness.cpp" -o "$OUT/harness_$V.o" &
+    g++ $FLAGS $INC -c "$D/cellBP/iomesh.cpp" -o "$OUT/iomesh_$V.o" &
+    g++ $FLAGS $INC -c "$D/common/bfstream.cpp" -o "$OUT/bfs_$V.o" &
+    HFLAGS=""
+    if [ "$V" = "kMD" ]; then HFLAGS="-DWCFE_REF_WRITER_KINT"; fi
+    g++ $FLAGS $HFLAGS $INC -c "$HERE/ref_harness.cpp" -o "$OUT/harness_$V.o" &
     wait
-    g++ -shared -Wl,-Bsymbolic -o "$OUT/libwcfe_ref_$V.so" "$OUT/ul_$V.o" "$OUT/ndtm_$V.o" "$OUT/harness_$V.o" \
-        "$OUT/ref_rng.o" -lm
+    g++ -shared -Wl,-Bsymbolic -o "$OUT/libwcfe_ref_$V.so" "$OUT/ul_$V.o" "$OUT/ndtm_$V.o" "$OUT/iomesh_$V.o" \
+        "$OUT/bfs_$V.o" "$OUT/harness_$V.o" "$OUT/ref_rng.o" -lm
 done
 rm -f "$OUT"/*.o
 echo "built $(ls "$OUT"/*.so | wc -l) reference libraries in $OUT"

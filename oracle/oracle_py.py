@@ -243,6 +243,15 @@ class Ref:
                      "ref_force_fa_subs", "ref_steps", "ref_predict"):
             getattr(self.lib, name).restype = None
 
+    def write_vtk(self, h, fmt, x, cA, cC, fau, ea, time, kint, path):
+        """The reference's VTK frame writer `fmt` (cellBP/iomesh.cpp:690-1047) into `path`."""
+        f = self.lib.ref_write_vtk
+        f.restype = None
+        f.argtypes = [C.c_void_p, C.c_int32, C.c_int32] + [C.POINTER(C.c_double)] * 5 + [C.c_double, C.c_double,
+                                                                                        C.c_char_p]
+        f(h, fmt, len(x), dp(f64(x)), dp(f64(cA)), dp(f64(cC)), dp(f64(fau)), dp(f64(ea)), time, kint,
+          str(path).encode())
+
     def mesh(self, tri, n_vert):
         tri = np.ascontiguousarray(tri, dtype=np.int32)
         h = self.lib.ref_mesh_new(n_vert, len(tri), ip(tri))

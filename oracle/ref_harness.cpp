@@ -15,6 +15,7 @@
 #include <iostream>
 #include <vector>
 
+#include "iomesh.h"
 #include "nondestructivetrimesh.h"
 #include "vec.h"
 
@@ -278,6 +279,33 @@ void ref_steps(void* mcell, int32_t n, double* x, double* V, double* A, double* 
     out3(f, fau);
     std::memcpy(cA, a.data(), sizeof(double) * n);
     std::memcpy(cC, c.data(), sizeof(double) * n);
+}
+
+// The reference's VTK frame writers (cellBP/iomesh.cpp:690-1047): format 0 positions and
+// triangles (:690), 1 strain measure and bond vectors (:730, the substrate's frames), 2
+// concentrations, strain measure and integrin force (:844, the cell's frames; the kMD
+// variant takes kint, k1 and k31 do not).
+void ref_write_vtk(void* mp, int32_t format, int32_t n, const double* x, const double* cA, const double* cC,
+                   const double* fau, const double* ea, double time, double kint, const char* path) {
+    const NonDestructiveTriMesh& m = *static_cast<NonDestructiveTriMesh*>(mp);
+    const std::vector<Vec3d> xv = v3(x, n);
+    if (format == 0) {
+        write_vtk(m, xv, time, path);
+        return;
+    }
+    const std::vector<Vec3d> fv = v3(fau, n);
+    std::vector<Eigen::VectorXd> ev = v6(ea, n);
+    if (format == 1) {
+        write_vtk(m, xv, ev, fv, time, path);
+        return;
+    }
+    const std::vector<double> a = vd(cA, n), b(n, 0.0), c = vd(cC, n);
+#ifdef WCFE_REF_WRITER_KINT
+    write_vtk(m, xv, a, b, c, fv, ev, time, path, kint);
+#else
+    (void)kint;
+    write_vtk(m, xv, a, b, c, fv, ev, time, path);
+#endif
 }
 
 }  // extern "C"

@@ -84,6 +84,28 @@ def make(variant: str) -> dict:
     return g
 
 
+# VTK frames: the reference's writers on one seeded state, bond vectors spanning every
+# segment of the MD table (cellBP/iomesh.cpp:927-949)
+VTK_FRAMES = [("kMD", 0, -1.0), ("kMD", 1, -1.0), ("kMD", 2, -1.0), ("kMD", 2, 1000.0), ("k1", 2, -1.0),
+              ("k31", 2, -1.0)]
+VTK_TIME = 0.35
+
+
+def vtk_state():
+    x0, tri = synth.disk_mesh(60, seed=3)
+    x, V, A, ea, cA, cC, fau = synth.initial_state(x0, perturb=1.0, seed=9)
+    x = x + np.array([0.0, 0.0, 1e-3]) * np.sin(np.arange(len(x)))[:, None]
+    ext = np.array([0.0, 0.001, 0.003, 0.005, 0.008, 0.013, 0.02, 0.03])
+    for i, d in enumerate(ext):   # bond vectors of these lengths, one per MD segment and beyond
+        fau[i] = d * np.array([0.6, 0.8, 0.0])
+    ea[:, 2] = 0.002 * np.cos(np.arange(len(x)))
+    return dict(x=x, tri=tri, cA=cA, cC=cC, fau=fau, ea=ea, time=VTK_TIME)
+
+
+def vtk_name(variant, fmt, kint):
+    return f"{variant}_f{fmt}" + ("_kint%g" % kint if kint >= 0 else "") + ".vtk"
+
+
 def main():
     for variant in ("kMD", "k1", "k31"):
         if not O.ref_available(variant):
@@ -91,6 +113,15 @@ def main():
         g = make(variant)
         path = os.path.join(HERE, f"golden_{variant}.npz")
         np.savez_compressed(path, **g)
+        print("wrote", path, os.path.getsize(path), "bytes")
+    st = vtk_state()
+    os.makedirs(os.path.join(HERE, "vtk"), exist_ok=True)
+    np.savez_compressed(os.path.join(HERE, "vtk", "state.npz"), **st)
+    for variant, fmt, kint in VTK_FRAMES:
+        R = O.Ref(variant)
+        h = R.mesh(st["tri"], len(st["x"]))
+        path = os.path.join(HERE, "vtk", vtk_name(variant, fmt, kint))
+        R.write_vtk(h, fmt, st["x"], st["cA"], st["cC"], st["fau"], st["ea"], VTK_TIME, kint, path)
         print("wrote", path, os.path.getsize(path), "bytes")
 
 

@@ -18,7 +18,8 @@ LIB = os.path.join(HERE, "libwcfe.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["wcfe_kernels.cu", "wcfe_mixed.cu", "wcfe_engine.cu", "wcfe_server.cu", "wcfe_topology.cpp",
-           "wcfe_noalloc.cu", "wcfe_newton.cu", "wcfe_lu_tc.cu"]
+           "wcfe_noalloc.cu", "wcfe_newton.cu", "wcfe_lu_tc.cu",
+           "wcfe_vtk.cu"]
 
 
 def nvcc() -> str:
@@ -36,7 +37,7 @@ def _compile(src: str, extra: list[str]) -> str:
     deps.append(os.path.join(HERE, "..", "include", "wcfe.h"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
-    cmd = [nvcc(), "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2", "--expt-relaxed-constexpr", *ARCH,
+    cmd = [nvcc(), "-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-O2,-ffp-contract=off", "--expt-relaxed-constexpr", *ARCH,
            "-c", path, "-o", obj, *extra]
     if src.endswith(".cpp"):
         cmd.insert(1, "-x=cu")

@@ -94,6 +94,12 @@ SIGNATURES = {
                                            C.c_int32]),
     "wcfe_engine_set_lu": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "wcfe_engine_set_lu_reuse": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_frames_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "wcfe_frames_write": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_char_p]),
+    "wcfe_frames_flush": (C.c_int, [C.c_void_p]),
+    "wcfe_frames_destroy": (C.c_int, [C.c_void_p]),
+    "wcfe_vtk_format": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _i, _d, _d, _d, _d, _d, C.c_double, C.c_double,
+                                  C.c_int32, C.c_double, C.c_char_p, C.c_int64, C.POINTER(C.c_int64)]),
     "wcfe_area_tot_noalloc": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p]),
     "wcfe_debug_topology": (C.c_int, [C.c_int32, C.c_int32, _i, _i, _i, _u8, C.c_int32, _i, _i, _i, _i, C.c_int32, _i,
                                       _i, C.c_int32, _i, C.c_int32, C.POINTER(C.c_uint16)]),
@@ -161,6 +167,22 @@ def debug_lu_solve(A, b, block: int | None = None, kind: int = 0):
         check(load().wcfe_debug_lu_solve_with(len(b), A.ctypes.data_as(fp), dp(b), x.ctypes.data_as(fp), block, kind),
               "wcfe_debug_lu_solve_with")
     return x
+
+
+def vtk_format(fmt: int, x, tri, cA=None, cC=None, fau=None, ea=None, time: float = 0.0, kint: float = -1.0,
+               law: int = 0, k_fa: float = 0.0) -> bytes:
+    """The text of a VTK frame (cellBP/iomesh.cpp:690-1047 formats) from host arrays."""
+    x = f64(x)
+    tri = i32(tri)
+    n = len(x)
+    args = [dp(None if a is None else f64(a)) for a in (cA, cC, fau, ea)]
+    ln = C.c_int64()
+    check(load().wcfe_vtk_format(fmt, n, len(tri), ip(tri), dp(x), *args, time, kint, law, k_fa, None, 0,
+                                 C.byref(ln)), "wcfe_vtk_format")
+    buf = C.create_string_buffer(ln.value)
+    check(load().wcfe_vtk_format(fmt, n, len(tri), ip(tri), dp(x), *args, time, kint, law, k_fa, buf, ln.value,
+                                 C.byref(ln)), "wcfe_vtk_format")
+    return buf.raw[:ln.value]
 
 
 class WcfeError(RuntimeError):
@@ -322,6 +344,25 @@ class Engine:
 
     def free_bytes(self) -> int:
         return int(load().wcfe_engine_free_bytes(self.h))
+
+
+class Frames:
+    """Asynchronous VTK frame writer of an engine (wcfe_frames_*)."""
+
+    def __init__(self, eng: Engine, slots: int = 4, threads: int = 1):
+        self.h = C.c_void_p()
+        check(load().wcfe_frames_create(eng.h, slots, threads, C.byref(self.h)), "wcfe_frames_create")
+
+    def write(self, cell: "Cell", fmt: int, path: str, time: float = float("nan"), kint: float = -1.0):
+        check(load().wcfe_frames_write(self.h, cell.id, fmt, time, kint, str(path).encode()), "wcfe_frames_write")
+
+    def flush(self):
+        check(load().wcfe_frames_flush(self.h), "wcfe_frames_flush")
+
+    def close(self):
+        if self.h:
+            load().wcfe_frames_destroy(self.h)
+            self.h = C.c_void_p()
 
 
 class Cell:

@@ -17,6 +17,7 @@
 
 #include "../../include/wcfe.h"
 #include "wcfe_device.cuh"
+#include "wcfe_frames.h"
 #include "wcfe_topology.h"
 
 namespace wcfe {
@@ -2073,3 +2074,27 @@ int wcfe_engine_autotune(wcfe_engine* e, double dt, int32_t reps) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------- frame output (wcfe_vtk.cu)
+namespace wcfe {
+int set_error(const char* msg, int code) {
+    g_last_error = msg;
+    return code;
+}
+
+int engine_device(wcfe_engine* e) { return e->device; }
+
+int engine_frame_source(wcfe_engine* e, int32_t id, FrameSource* out) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c || !out) return fail("unknown cell", WCFE_ERR_ARG);
+    out->dev = c->dev;
+    out->mixed = e->prec == WCFE_PREC_MIXED ? 1 : 0;
+    out->nv = c->topo.nv;
+    out->nt = c->topo.nt;
+    out->tri = c->topo.tri;
+    out->prm = c->prm;
+    out->stream = e->stream;
+    out->device = e->device;
+    return WCFE_OK;
+}
+}  // namespace wcfe
