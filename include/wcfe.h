@@ -361,6 +361,22 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
  * with the cell's state as step start, and the mass/damping diagonal [n]. */
 int wcfe_cell_newton_tangent(wcfe_engine* e, int32_t id, double dt, const double* x, float* J_out, double* diag_out);
 
+/* ---- El Topo co-residency ---------------------------------------------------
+ * After the host's remeshing (improve_mesh, defrag_mesh; cellBP/main.cpp:191-192),
+ * rebuild cell `id` with its state carried on the device, as El Topo carries it:
+ * split k (El Topo's VERTEX_ADD events, in order; eltopo3d/edgesplitter.cpp:564-577)
+ * appends vertex n_old + k with every state field 0.5 (s[a] + s[b]), split_ab[2k] = a,
+ * split_ab[2k + 1] = b in the same numbering (old vertices or earlier splits);
+ * collapses and flips leave the survivors' states as they are; keep [nv_new] is the
+ * defrag map (eltopo3d/surftrack.cpp:487-593): new vertex j is vertex keep[j] of that
+ * numbering, ascending.  tri, vt_ptr, vt_idx, is_bnd: the new connectivity as for
+ * wcfe_cell_set_topology; x_new [nv_new][3]: the remeshed positions.  The clock, the AP
+ * counter and the integrin densities (copied and averaged like the state) carry over;
+ * per-element moduli return to params.mu.  Not for coupled cells or substrates. */
+int wcfe_cell_remesh(wcfe_engine* e, int32_t id, int32_t n_split, const int32_t* split_ab, int32_t nv_new,
+                     const int32_t* keep, int32_t nt_new, const int32_t* tri, const int32_t* vt_ptr,
+                     const int32_t* vt_idx, const uint8_t* is_bnd, const double* x_new);
+
 /* ---- VTK frames (cellBP/iomesh.cpp:690-1047), byte for byte ------------------
  * Replaces the reference's write_vtk calls (cellBP/main.cpp:447-454, :721-723) without
  * stalling the stepping stream: a write packs the cell's current state on the engine's

@@ -94,6 +94,8 @@ SIGNATURES = {
                                            C.c_int32]),
     "wcfe_engine_set_lu": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
     "wcfe_engine_set_lu_reuse": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_cell_remesh": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _i, C.c_int32, _i, C.c_int32, _i, _i, _i, _u8,
+                                   _d]),
     "wcfe_frames_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
     "wcfe_frames_write": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double, C.c_double, C.c_char_p]),
     "wcfe_frames_flush": (C.c_int, [C.c_void_p]),
@@ -391,6 +393,20 @@ class Cell:
         """Couple this cell to a deformable substrate cell of the same engine (None: uncouple)."""
         check(load().wcfe_cell_couple_substrate(self.eng.h, self.id, -1 if sub is None else sub.id, margin),
               "wcfe_cell_couple_substrate")
+
+    def remesh(self, split_ab, keep, tri, x_new, vt_ptr=None, vt_idx=None, bnd=None):
+        """Rebuild after El Topo's remeshing with the state carried on the device: split_ab
+        [n_split][2] (VERTEX_ADD events in order), keep [nv_new] (the defrag map)."""
+        sab = i32(np.zeros((0, 2)) if split_ab is None else split_ab).reshape(-1)
+        keep = i32(keep)
+        tri = i32(tri)
+        x_new = f64(x_new)
+        check(load().wcfe_cell_remesh(self.eng.h, self.id, len(sab) // 2, ip(sab) if len(sab) else None, len(keep),
+                                      ip(keep), len(tri), ip(tri), ip(None if vt_ptr is None else i32(vt_ptr)),
+                                      ip(None if vt_idx is None else i32(vt_idx)),
+                                      None if bnd is None else np.ascontiguousarray(bnd, np.uint8).ctypes.data_as(_u8),
+                                      dp(x_new)), "wcfe_cell_remesh")
+        self.n, self.nt = len(keep), len(tri)
 
     def set_element_mu(self, mu):
         """Per-element shear modulus [n_tri] (None: the cell's params.mu everywhere)."""

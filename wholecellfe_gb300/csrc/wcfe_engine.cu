@@ -69,6 +69,11 @@ void launch_newton_finish(const CellDev* cells, NewtonCell* nc, const int* cell_
                           const double* res_ea, double dt, unsigned int* tickets, cudaStream_t st);
 void launch_sum4(const double* a, const double* b, const double* c, const double* d, double* o, size_t n,
                  cudaStream_t st);
+void launch_remesh_pack(const CellDev& c, int mixed, const void* rho, double* ext, unsigned long long* hdr,
+                        cudaStream_t st);
+void launch_remesh_split(double* ext, int n_old, const int* ks, int cnt, const int2* ab, cudaStream_t st);
+void launch_remesh_unpack(const CellDev& c, int mixed, const double* ext, const int* keep, const double* x, void* rho,
+                          const unsigned long long* hdr, cudaStream_t st);
 }  // namespace wcfe
 
 using namespace wcfe;
@@ -710,6 +715,22 @@ int get_ff(wcfe_engine* e, double* h, const void* d, int n, int kind) {
 }
 enum { FF_VEC = 0, FF_ACC = 1, FF_EA = 2, FF_SCALAR = 3 };
 
+// the mixed form assumes a planar membrane with counter-clockwise triangles (its element
+// inputs drop z and its area comes from the boundary loop)
+int check_planar_ccw(const double* x, int n, const std::vector<int32_t>& T) {
+    for (int v = 0; v < n; ++v)
+        if (x[3 * v + 2] != 0.0) return fail("the mixed form needs a planar membrane (z = 0)", WCFE_ERR_ARG);
+    for (size_t t = 0; 3 * t < T.size(); ++t) {
+        const double* a = x + 3 * T[3 * t];
+        const double* b = x + 3 * T[3 * t + 1];
+        const double* q = x + 3 * T[3 * t + 2];
+        if ((b[0] - a[0]) * (q[1] - a[1]) - (b[1] - a[1]) * (q[0] - a[0]) <= 0)
+            return fail("the mixed form needs counter-clockwise, non-degenerate triangles", WCFE_ERR_ARG);
+    }
+    return WCFE_OK;
+}
+
+
 }  // namespace
 
 // =============================================================================
@@ -884,6 +905,107 @@ int wcfe_cell_set_topology(wcfe_engine* e, int32_t id, int32_t nv, int32_t nt, c
     return r;
 }
 
+int wcfe_cell_remesh(wcfe_engine* e, int32_t id, int32_t n_split, const int32_t* split_ab, int32_t nv_new,
+                     const int32_t* keep, int32_t nt_new, const int32_t* tri, const int32_t* vt_ptr,
+                     const int32_t* vt_idx, const uint8_t* is_bnd, const double* x_new) {
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    if (n_split < 0 || (n_split > 0 && !split_ab) || nv_new <= 0 || !keep || nt_new <= 0 || !tri || !x_new)
+        return fail("bad argument", WCFE_ERR_ARG);
+    if (c->couple_sub >= 0 || c->is_sub) return fail("remeshing a coupled cell or substrate is not supported", WCFE_ERR_STATE);
+    const int32_t n_old = c->topo.nv;
+    const int64_t M = (int64_t)n_old + n_split;
+    if (M > INT32_MAX) return fail("too many vertices", WCFE_ERR_ARG);
+    // El Topo's change list: split k appends vertex n_old + k from two earlier vertices; its
+    // level is one more than theirs (old vertices: level 0)
+    std::vector<int32_t> level((size_t)M, 0);
+    int32_t max_level = 0;
+    for (int32_t k = 0; k < n_split; ++k) {
+        const int32_t a = split_ab[2 * k], b = split_ab[2 * k + 1];
+        if (a < 0 || b < 0 || a >= n_old + k || b >= n_old + k) return fail("split endpoint out of range", WCFE_ERR_ARG);
+        level[(size_t)n_old + k] = 1 + std::max(level[a], level[b]);
+        max_level = std::max(max_level, level[(size_t)n_old + k]);
+    }
+    for (int32_t j = 0; j < nv_new; ++j)   // defrag_mesh keeps the survivors in order
+        if (keep[j] < 0 || keep[j] >= M || (j && keep[j] <= keep[j - 1])) return fail("bad vertex map", WCFE_ERR_ARG);
+    Topology T;
+    std::string err = build_topology(T, nv_new, nt_new, tri, vt_ptr, vt_idx, is_bnd);
+    if (!err.empty()) return fail(err, WCFE_ERR_TOPOLOGY);
+    const int mixed = e->prec == WCFE_PREC_MIXED ? 1 : 0;
+    int r;
+    if (mixed && (r = check_planar_ccw(x_new, nv_new, T.tri))) return r;
+    CK(cudaSetDevice(e->device));
+    // scratch: records [M][18], header, splits grouped by level, the map, the positions
+    std::vector<int32_t> ks;
+    std::vector<int32_t> lstart(max_level + 2, 0);
+    for (int32_t k = 0; k < n_split; ++k) lstart[level[(size_t)n_old + k] + 1]++;
+    for (int32_t l = 1; l <= max_level + 1; ++l) lstart[l] += lstart[l - 1];
+    ks.resize(n_split);
+    {
+        std::vector<int32_t> fill(lstart.begin(), lstart.end() - 1);
+        for (int32_t k = 0; k < n_split; ++k) ks[fill[level[(size_t)n_old + k]]++] = k;
+    }
+    size_t o = 0;
+    auto put = [&](size_t bytes) { const size_t at = o; o = align_up(o + bytes); return at; };
+    const size_t o_ext = put(sizeof(double) * 18 * (size_t)M), o_hdr = put(sizeof(unsigned long long) * 4);
+    const size_t o_ab = put(sizeof(int2) * (size_t)std::max(n_split, 1)), o_ks = put(sizeof(int32_t) * std::max(n_split, 1));
+    const size_t o_keep = put(sizeof(int32_t) * nv_new), o_x = put(sizeof(double) * 3 * (size_t)nv_new);
+    void* scratch = nullptr;
+    if ((r = dev_alloc(e, &scratch, o))) return r;
+    size_t scratch_bytes = o;
+    char* sb = (char*)scratch;
+    double* ext = (double*)(sb + o_ext);
+    unsigned long long* hdr = (unsigned long long*)(sb + o_hdr);
+    if (n_split) {
+        CK(cudaMemcpyAsync(sb + o_ab, split_ab, sizeof(int2) * n_split, cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemcpyAsync(sb + o_ks, ks.data(), sizeof(int32_t) * n_split, cudaMemcpyHostToDevice, e->stream));
+    }
+    CK(cudaMemcpyAsync(sb + o_keep, keep, sizeof(int32_t) * nv_new, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaMemcpyAsync(sb + o_x, x_new, sizeof(double) * 3 * nv_new, cudaMemcpyHostToDevice, e->stream));
+    // old state -> records, then the splits level by level (stream order keeps the old block
+    // alive until these have run: its release below is stream-ordered)
+    launch_remesh_pack(c->dev, mixed, c->rho_dev, ext, hdr, e->stream);
+    for (int32_t l = 1; l <= max_level; ++l)
+        launch_remesh_split(ext, n_old, (const int*)(sb + o_ks) + lstart[l], lstart[l + 1] - lstart[l],
+                            (const int2*)(sb + o_ab), e->stream);
+    CK(cudaGetLastError());
+    const bool had_rho = c->rho_dev != nullptr;
+    if (had_rho) {
+        void* p = c->rho_dev;
+        size_t b = c->rho_size;
+        dev_free(e, p, b);
+        c->rho_dev = nullptr;
+    }
+    if (c->mu_dev) {   // per-element moduli do not survive a change of elements: back to params.mu
+        void* p = c->mu_dev;
+        size_t b = c->mu_size;
+        dev_free(e, p, b);
+        c->mu_dev = nullptr;
+    }
+    c->topo = std::move(T);
+    if ((r = upload_cell_topology(e, c)) || (r = upload_cell_patches(e, c))) {
+        dev_free(e, scratch, scratch_bytes);
+        return r;
+    }
+    if (had_rho) {
+        void* p = nullptr;
+        if ((r = dev_alloc(e, &p, rho_bytes(nv_new)))) {
+            dev_free(e, scratch, scratch_bytes);
+            return r;
+        }
+        c->rho_dev = (double*)p;
+        c->rho_size = rho_bytes(nv_new);
+    }
+    launch_remesh_unpack(c->dev, mixed, ext, (const int*)(sb + o_keep), (const double*)(sb + o_x), c->rho_dev, hdr,
+                         e->stream);
+    CK(cudaGetLastError());
+    dev_free(e, scratch, scratch_bytes);
+    CK(cudaStreamSynchronize(e->stream));
+    e->version++;
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
 int wcfe_cell_set_substrate(wcfe_engine* e, int32_t id, int32_t nv, int32_t nt, const int32_t* tri, const double* Xs,
                             const double* xs) {
     Cell* c = e ? find(e, id) : nullptr;
@@ -919,20 +1041,7 @@ int wcfe_cell_set_state(wcfe_engine* e, int32_t id, const double* x, const doubl
     if (r) return r;
     const int n = c->topo.nv;
     CellDev& d = c->dev;
-    if (x && e->prec == WCFE_PREC_MIXED) {
-        // the mixed form assumes a planar membrane with counter-clockwise triangles (its
-        // element inputs drop z and its area comes from the boundary loop)
-        for (int v = 0; v < n; ++v)
-            if (x[3 * v + 2] != 0.0) return fail("the mixed form needs a planar membrane (z = 0)", WCFE_ERR_ARG);
-        const std::vector<int32_t>& T = c->topo.tri;
-        for (int t = 0; t < c->topo.nt; ++t) {
-            const double* a = x + 3 * T[3 * t];
-            const double* b = x + 3 * T[3 * t + 1];
-            const double* q = x + 3 * T[3 * t + 2];
-            if ((b[0] - a[0]) * (q[1] - a[1]) - (b[1] - a[1]) * (q[0] - a[0]) <= 0)
-                return fail("the mixed form needs counter-clockwise, non-degenerate triangles", WCFE_ERR_ARG);
-        }
-    }
+    if (x && e->prec == WCFE_PREC_MIXED && (r = check_planar_ccw(x, n, c->topo.tri))) return r;
     if (e->prec == WCFE_PREC_MIXED) {
         if (x && (r = put_ff(e, d.pos[par], x, n, FF_VEC))) return r;
         if (V && (r = put_ff(e, d.vel, V, n, FF_VEC))) return r;
