@@ -80,6 +80,7 @@ struct CellDev {
     const int4* patch_x;        // per patch (h0, nh, c0, nc): halo list and one-ring code range (mixed form staging)
     const int32_t* patch_halo;  // halo vertices of each patch, ascending
     const uint16_t* patch_loc;  // [4 per element slot] corners as patch-local vertex indices
+    const int4* patch_tri;      // [per element slot] (vertex a, b, c, element id)
     const int32_t* bnd_rank;
     const int32_t* bnd_cptr;
     const int2* bnd_cand;

@@ -243,7 +243,7 @@ size_t state_layout(int32_t nv, int32_t nt, int32_t nb, int32_t ncand, int32_t n
 }
 
 // patch arrays; every array ends with 64 B of slack so that 16-B-rounded bulk copies stay in the block
-size_t patch_layout(int32_t np, size_t nelems, size_t ncodes, size_t nhalo, size_t* off /* 6 */) {
+size_t patch_layout(int32_t np, size_t nelems, size_t ncodes, size_t nhalo, size_t* off /* 7 */) {
     size_t o = 0;
     int i = 0;
     auto put = [&](size_t bytes) { off[i++] = o; o = align_up(o + bytes + 64); };
@@ -253,6 +253,7 @@ size_t patch_layout(int32_t np, size_t nelems, size_t ncodes, size_t nhalo, size
     put(sizeof(int4) * np);                               // 3 staging info (h0, nh, c0, nc)
     put(sizeof(int32_t) * std::max<size_t>(nhalo, 1));    // 4 halo vertices
     put(sizeof(uint16_t) * 4 * std::max<size_t>(nelems, 1));  // 5 element corners, patch-local
+    put(sizeof(int4) * std::max<size_t>(nelems, 1));      // 6 element vertices and id per slot
     return o;
 }
 
@@ -383,7 +384,7 @@ int upload_cell_patches(wcfe_engine* e, Cell* c) {
     std::string err = build_patches(c->patches, c->topo, e->patch_emax);
     if (!err.empty()) return fail(err, WCFE_ERR_TOPOLOGY);
     const Patches& P = c->patches;
-    size_t off[6];
+    size_t off[7];
     size_t bytes = patch_layout(P.np, P.elems.size(), P.vc_code.size(), P.halo.size(), off);
     if (c->patch_block && c->patch_bytes != bytes) dev_free(e, c->patch_block, c->patch_bytes);
     if (!c->patch_block) {
@@ -400,6 +401,19 @@ int upload_cell_patches(wcfe_engine* e, Cell* c) {
     c->dev.patch_x = (const int4*)(b + off[3]);
     c->dev.patch_halo = (const int32_t*)(b + off[4]);
     c->dev.patch_loc = (const uint16_t*)(b + off[5]);
+    c->dev.patch_tri = (const int4*)(b + off[6]);
+    {   // each element slot with its triangle's vertices (one load instead of two dependent ones)
+        std::vector<int4> pt(P.elems.size());
+        const std::vector<int32_t>& T = c->topo.tri;
+        for (size_t k = 0; k < P.elems.size(); ++k) {
+            const int32_t el = P.elems[k];
+            pt[k] = make_int4(T[3 * el], T[3 * el + 1], T[3 * el + 2], el);
+        }
+        if (!pt.empty())
+            CK(cudaMemcpyAsync((void*)c->dev.patch_tri, pt.data(), sizeof(int4) * pt.size(), cudaMemcpyHostToDevice,
+                               e->stream));
+        CK(cudaStreamSynchronize(e->stream));   // pt is a local buffer
+    }
     CK(cudaMemcpyAsync((void*)c->dev.patch, P.patch.data(), sizeof(int32_t) * P.patch.size(), cudaMemcpyHostToDevice, e->stream));
     CK(cudaMemcpyAsync((void*)c->dev.patch_elems, P.elems.data(), sizeof(int32_t) * P.elems.size(), cudaMemcpyHostToDevice, e->stream));
     CK(cudaMemcpyAsync((void*)c->dev.vc_code, P.vc_code.data(), sizeof(uint16_t) * P.vc_code.size(), cudaMemcpyHostToDevice, e->stream));
@@ -820,8 +834,8 @@ uint64_t wcfe_cell_bytes(int32_t nv, int32_t nt) {
     size_t off[32];
     int32_t nb = (int32_t)(4 * std::sqrt((double)std::max(nv, 1)) + 16);
     size_t s = state_layout(nv, nt, nb, 3 * nb, nk1_of(nv, nt, 64), true, off);
-    size_t p6[6];
-    size_t p = patch_layout(nv / 64 + 2, (size_t)(1.6 * nt) + 64, 3 * (size_t)nt, (size_t)(0.6 * nv) + 64, p6);
+    size_t p7[7];
+    size_t p = patch_layout(nv / 64 + 2, (size_t)(1.6 * nt) + 64, 3 * (size_t)nt, (size_t)(0.6 * nv) + 64, p7);
     return (uint64_t)(s + p + rho_bytes(nv));
 }
 int wcfe_engine_sync(wcfe_engine* e) {

@@ -498,8 +498,8 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
         const ElemParams q = s_q;
         // ---- elements of the patch -> shared memory ----
         for (int j = threadIdx.x; j < pt.w; j += blockDim.x) {
-            const int e = c.patch_elems[pt.z + j];
-            const int4 t4 = __ldg(c.tri + e);
+            const int4 t4 = __ldg(c.patch_tri + pt.z + j);   // (a, b, c, element id)
+            const int e = t4.w;
             const int id[3] = {t4.x, t4.y, t4.z};
             float4 r[3][kRec];
 #pragma unroll
@@ -529,9 +529,19 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
         const float rho_max = pf.rho_i_max;
         for (int i = threadIdx.x; i < pt.y; i += blockDim.x) {
             const int v = pt.x + i;
+            // the vertex's own state first: these loads do not depend on the one-ring sums below
+            const int kb = c.vt_ptr[v], ke = c.vt_ptr[v + 1];
+            const ff4 f4 = ldg_ff4(c.fau, c.nv, v);
+            const float cCh = ld_ff(c.cC, c.nv, v).hi;
+            const float rho = c.rho_w ? ld_rho(c.rho_w, v) : rho_max;
+            const int rank = c.bnd_rank[v];
+            const float4* eo = reinterpret_cast<const float4*>(c.ea[par]);
+            const ff4 Vv = ldg_ff4(c.vel, c.nv, v);
+            const float4 Av = a.vh_from_buf ? make_float4(0.f, 0.f, 0.f, 0.f) : ld_acc(c.acc, v);
+            const float4 eh = __ldg(eo + v), el = __ldg(eo + c.nv + v);
             float Q0 = 0, Q1 = 0, Q2 = 0, Q3 = 0, MMf = 0, Asf = 0;
             ff R0 = {0.0f, 0.0f}, R1 = {0.0f, 0.0f};   // compensated: the corner forces largely cancel
-            for (int k = c.vt_ptr[v]; k < c.vt_ptr[v + 1]; ++k) {
+            for (int k = kb; k < ke; ++k) {
                 const int code = c.vc_code[k];
                 const int sl = code >> 2, cn = code & 3;
                 R0 = ff_add_f(R0, smf[(2 * cn) * emax + sl]);
@@ -545,14 +555,11 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             }
             const float Asum = Asf * (1.0f / 3.0f);
             // integrin force (UL:1241-1269) in FP32
-            const ff4 f4 = ldg_ff4(c.fau, c.nv, v);
             float fs[3], bell;
             spring_force32(pf, f4.hx, f4.hy, f4.hz, fs, &bell);
-            const float rho = c.rho_w ? ld_rho(c.rho_w, v) : rho_max;
-            const float kfa = -ld_ff(c.cC, c.nv, v).hi * Asum * rho;
+            const float kfa = -cCh * Asum * rho;
             // F = kfa fs - R with the product exact (TwoProduct) and one rounding at the end
             float F0 = net_force(kfa, fs[0], R0), F1 = net_force(kfa, fs[1], R1);
-            const int rank = c.bnd_rank[v];
             if (rank >= 0) {
                 const int slot = atomicAdd(&s_nbnd, 1);
                 if (slot < kBndSlots) {
@@ -563,7 +570,7 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
                 }
                 boundary_force(c, s_bc, pt, X, xp, v, rank, F0, F1);   // queue full: finish in place
             }
-            finish_vertex(c, a, par, v, F0, F1, Q0, Q1, Q2, Q3, MMf);
+            finish_vertex_core(c, a, par, v, F0, F1, Q0, Q1, Q2, Q3, MMf, Vv, Av, eh, el);
         }
         __syncthreads();
         const int nq = min(s_nbnd, kBndSlots);
