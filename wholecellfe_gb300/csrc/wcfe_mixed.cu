@@ -683,6 +683,12 @@ __global__ void __launch_bounds__(kK1Threads, 3) k_vertex_phase_mixed(const Cell
     if (v < c.nv) {
         const double4* __restrict__ X = c.pos[par];
         const ff4 Xv = ldg_ff4(X, c.nv, v);
+        // every load of this vertex's state up front: none depends on the prediction's stores
+        const bool do_fa = (flags & VM_UPDATE_FA) != 0;
+        const ff4 f = do_fa ? ldg_ff4(c.fau, c.nv, v) : ff4{};
+        const ff cold = do_fa ? ld_ff(c.cC, c.nv, v) : ff{0.0f, 0.0f};
+        const ff cAv = do_fa ? ld_ff(c.cA, c.nv, v) : ff{0.0f, 0.0f};
+        const float4 eh = __ldg(reinterpret_cast<const float4*>(c.ea[par]) + v);   // (xx, yy, zz, xy) hi
         ff xn0, xn1, xn2 = ffz(Xv);
         if (flags & VM_IMPORT) {
             const double* qq = va.stage_in + 3 * (size_t)(c.hoff + v);
@@ -705,10 +711,8 @@ __global__ void __launch_bounds__(kK1Threads, 3) k_vertex_phase_mixed(const Cell
             xn0 = ffx(t); xn1 = ffy(t); xn2 = ffz(t);
         }
         const ff cu0 = ff_sub(xn0, ffx(Xv)), cu1 = ff_sub(xn1, ffy(Xv));   // step displacement
-        if (flags & VM_UPDATE_FA) {
+        if (do_fa) {
             const ParamF& pf = c.pf;
-            const ff4 f = ldg_ff4(c.fau, c.nv, v);
-            const ff cold = ld_ff(c.cC, c.nv, v), cAv = ld_ff(c.cA, c.nv, v);
             ff u0 = ff_add(ffx(f), cu0), u1 = ff_add(ffy(f), cu1), u2 = ffz(f);
             if (c.has_sub && c.sub.moving) {
                 double wgt[3], Xd[3], fd[3];
@@ -748,7 +752,6 @@ __global__ void __launch_bounds__(kK1Threads, 3) k_vertex_phase_mixed(const Cell
             st_ff4(c.fau, c.nv, v, make_ff4(n0, n1, n2));
         }
         if (!(flags & VM_EXPORT)) {
-            const float4 eh = __ldg(reinterpret_cast<const float4*>(c.ea[par]) + v);  // (xx, yy, zz, xy) hi
             float4* r = c.rec + kRec * (size_t)v;
             r[0] = make_float4(Xv.hx, Xv.hy, Xv.lx, Xv.ly);
             r[1] = make_float4(cu0.hi, cu1.hi, eh.x, eh.y);
