@@ -541,6 +541,7 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             const float4 eh = __ldg(eo + v), el = __ldg(eo + c.nv + v);
             float Q0 = 0, Q1 = 0, Q2 = 0, Q3 = 0, MMf = 0, Asf = 0;
             ff R0 = {0.0f, 0.0f}, R1 = {0.0f, 0.0f};   // compensated: the corner forces largely cancel
+#pragma unroll 4
             for (int k = kb; k < ke; ++k) {
                 const int code = c.vc_code[k];
                 const int sl = code >> 2, cn = code & 3;
