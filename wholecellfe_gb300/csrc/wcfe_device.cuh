@@ -81,6 +81,7 @@ struct CellDev {
     const int32_t* patch_halo;  // halo vertices of each patch, ascending
     const uint16_t* patch_loc;  // [4 per element slot] corners as patch-local vertex indices
     const int4* patch_tri;      // [per element slot] (vertex a, b, c, element id)
+    float4* stepc;              // [8] the mixed form's per-step cell constants (element and boundary terms)
     const int32_t* bnd_rank;
     const int32_t* bnd_cptr;
     const int2* bnd_cand;

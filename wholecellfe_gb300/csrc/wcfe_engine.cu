@@ -238,7 +238,8 @@ size_t state_layout(int32_t nv, int32_t nt, int32_t nb, int32_t ncand, int32_t n
     put(sizeof(int32_t) * std::max(2 * nb, 1));  // 22 bnd_out (at most a few edges per boundary vertex)
     put(sizeof(double) * 4);     // 23 area4
     put(sizeof(int32_t) * std::max(nb, 1));  // 24 bnd_vert: boundary vertices in rank order
-    put(64);                     // 25 slack: 16-B-rounded bulk copies of the last arrays stay in the block
+    put(128);                    // 25 step constants of the mixed form (written by its vertex phase)
+    put(64);                     // 26 slack: 16-B-rounded bulk copies of the last arrays stay in the block
     return o;
 }
 
@@ -352,6 +353,7 @@ int upload_cell_topology(wcfe_engine* e, Cell* c) {
     d.rec = e->prec == WCFE_PREC_MIXED ? (float4*)(b + off[20]) : nullptr;
     d.area4 = (double*)(b + off[23]);
     d.bnd_vert = (const int32_t*)(b + off[24]);
+    d.stepc = (float4*)(b + off[25]);
     d.bnd_optr = (const int32_t*)(b + off[21]);
     d.bnd_out = (const int32_t*)(b + off[22]);
     if ((int64_t)T.bnd_out.size() > std::max<int64_t>(2 * (int64_t)T.nb, 1)) return fail("non-manifold boundary", WCFE_ERR_TOPOLOGY);

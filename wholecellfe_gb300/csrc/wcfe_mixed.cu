@@ -329,6 +329,42 @@ __device__ __forceinline__ BndConst make_bnd_const(const CellDev& c, const Mixed
     return b;
 }
 
+// The cell constants of one mixed-form step, formed once per cell by the vertex phase's
+// finishing block (it has the cell's area and centroid) and read by every patch CTA.
+struct StepConst {
+    ElemParams q;
+    BndConst b;
+};
+static_assert(sizeof(StepConst) <= 128, "step constants exceed their slot");
+
+__device__ __forceinline__ StepConst make_step_const(const CellDev& c, double dt_real, double area, double cx,
+                                                     double cy) {
+    const wcfe_params& p = c.prm;
+    const double t = c.clk[0];
+    const double t_act = t < p.tact_t1 ? t * p.tact_rate : p.tact_max;
+    StepConst s;
+    s.q.mu = (float)p.mu;
+    s.q.thick = (float)p.thick;
+    s.q.grow = (float)(p.thetag_dot * dt_real);
+    s.q.s_iso = (float)(p.kappa * t_act);
+    s.q.t_an = (float)((1.0 - 2.0 * p.kappa) * t_act);
+    s.q.cx = (float)cx;
+    s.q.cy = (float)cy;
+    const double s_iso = p.kappa * t_act;
+    s.b.w = (float)(0.5 * s_iso * p.thick);
+    s.b.area_term = (float)(-p.k_area * (area - p.area0) / 2);
+    s.b.k_bend = (float)p.k_bend;
+    s.b.ap_force = (float)p.ap_force;
+    s.b.half_density = ff_from_d(p.ap_density / 2);
+    const double thr = ceil(c.ap_thresh * 2147483648.0);
+    s.b.ap_thr = thr <= 0.0 ? 0u : (thr >= 4294967295.0 ? 4294967295u : (uint32_t)thr);
+    s.b.ap_enable = p.ap_enable;
+    s.b.seed = p.seed;
+    s.b.stream = p.stream;
+    s.b.ap_call = c.ap[0];
+    return s;
+}
+
 // The neighbour frame of a boundary vertex (UL:1500-1531): the candidate scan of
 // boundary_frame, with the orientation test on float-float differences.
 __device__ __forceinline__ bool boundary_frame_ff(const CellDev& c, const double4* __restrict__ xp, int rank,
@@ -467,10 +503,10 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
     extern __shared__ float smf[];
     const int emax = a.emax;
     // structure of arrays: field k of slot j at smf[k * emax + j]
-    __shared__ ElemParams s_q;
-    __shared__ BndConst s_bc;
     __shared__ int s_nbnd;
     __shared__ float s_bnd[8 * kBndSlots];
+    if (threadIdx.x == 0) s_nbnd = 0;
+    __syncthreads();
     for (int w = blockIdx.x; w < a.nwork; w += gridDim.x) {
         const WorkItem it = a.work[w];
         const CellDev& c = a.cells[it.cell];
@@ -480,22 +516,10 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
         const double4* __restrict__ xp = c.pos[par ^ 1];
         const float4* __restrict__ rec = c.rec;
         const unsigned long long ap_call = c.ap[0];
-        if (threadIdx.x == 0) {   // the element constants of this cell and step, once per CTA
-            s_nbnd = 0;
-            const wcfe_params& p = c.prm;
-            const double t = isnan(a.t_override) ? c.clk[0] : a.t_override;
-            const double t_act = t < p.tact_t1 ? t * p.tact_rate : p.tact_max;
-            s_q.mu = (float)p.mu;
-            s_q.thick = (float)p.thick;
-            s_q.grow = (float)(p.thetag_dot * a.dt_real);
-            s_q.s_iso = (float)(p.kappa * t_act);
-            s_q.t_an = (float)((1.0 - 2.0 * p.kappa) * t_act);
-            s_q.cx = (float)c.area4[1];
-            s_q.cy = (float)c.area4[2];
-            s_bc = make_bnd_const(c, a, ap_call);
-        }
-        __syncthreads();
-        const ElemParams q = s_q;
+        // the cell's constants of this step, formed by the vertex phase
+        const StepConst& sc = *reinterpret_cast<const StepConst*>(c.stepc);
+        const BndConst& s_bc = sc.b;
+        const ElemParams q = sc.q;
         // ---- elements of the patch -> shared memory ----
         for (int j = threadIdx.x; j < pt.w; j += blockDim.x) {
             const int4 t4 = __ldg(c.patch_tri + pt.z + j);   // (a, b, c, element id)
@@ -584,6 +608,7 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
         }
         __syncthreads();
         if (threadIdx.x == 0) {
+            s_nbnd = 0;   // for the next patch: every thread passes this CTA's next element barrier first
             __threadfence();
             const unsigned int done = atomicAdd(reinterpret_cast<unsigned int*>(c.ctl + 1), 1u);
             if ((int)done == c.np - 1) {
@@ -611,7 +636,7 @@ enum { VM_PREDICT = 1, VM_UPDATE_FA = 2, VM_EXPORT = 8, VM_IMPORT = 16, VM_NOARE
 // wrote (through L2) and sums the terms in a fixed order: boundary ranks strided
 // over the threads, then lanes, then warps.  Only that block runs the FP64
 // shoelace, with all of its lanes busy.
-__device__ __forceinline__ void finish_area_boundary(const CellDev& c, const double4* xo) {
+__device__ __forceinline__ void finish_area_boundary(const CellDev& c, const double4* xo, double dt_real) {
     __shared__ int s_last;
     __shared__ double s_w[kK1Threads / 32][3];
     __syncthreads();
@@ -657,11 +682,13 @@ __device__ __forceinline__ void finish_area_boundary(const CellDev& c, const dou
         c.area4[2] = Ay / A;
         c.area4[3] = 0.0;
         c.ctl[2] = 0;
+        *reinterpret_cast<StepConst*>(c.stepc) = make_step_const(c, dt_real, A, Ax / A, Ay / A);
     }
 }
 
 struct VertexArgs {
     ff dt, hdt;
+    double dtd;
     float dtf;
     int flags;
     const double* stage_in;
@@ -761,7 +788,7 @@ __global__ void __launch_bounds__(kK1Threads, 3) k_vertex_phase_mixed(const Cell
         // boundary positions are read by the block that finishes the area
         if (!(flags & VM_NOAREA) && c.bnd_rank[v] >= 0) __threadfence();
     }
-    if (!(flags & VM_NOAREA)) finish_area_boundary(c, xo);
+    if (!(flags & VM_NOAREA)) finish_area_boundary(c, xo, va.dtd);
 }
 
 void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
@@ -771,6 +798,7 @@ void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, 
     VertexArgs va;
     va.dt = ff_from_d(dt);
     va.hdt = ff_from_d(dt / 2.0);
+    va.dtd = dt;
     va.dtf = (float)dt;
     va.flags = flags;
     va.stage_in = stage_in;
