@@ -699,7 +699,7 @@ struct VertexArgs {
 // one cell): predict, bond kinetics with FP32 rates and float-float accumulation,
 // and the FP32 element records.  No FP64 arithmetic outside the exchange
 // conversions and the area of the finishing block.
-__global__ void __launch_bounds__(kK1Threads, 4) k_vertex_phase_mixed(const CellDev* __restrict__ cells,
+__global__ void __launch_bounds__(kK1Threads, 5) k_vertex_phase_mixed(const CellDev* __restrict__ cells,
                                                                     const WorkItem* __restrict__ work,
                                                                     const VertexArgs va) {
     const WorkItem it = work[blockIdx.x];
