@@ -630,25 +630,21 @@ __global__ void k_trsv_init(NewtonCell* nc, int nslots) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * N.n; i += gridDim.x * blockDim.x) N.z[i] = (float)N.r[i];
 }
 
-// One block step of the triangular solves with the diagonal blocks' explicit inverses.
-// Forward (L): x_b = Linv_b z_b into zt, then z_i -= L[i, b] x_b for the rows below.
-// Backward (U): x_b = Uinv_b zt_b into z, then zt_i -= U[i, b] x_b for the rows above.
-// Every CTA forms x_b itself (a 64 x 64 matvec) from the block's final input; CTA 0
-// stores it.  The rows a CTA updates never include the block's own rows.
+// One block step of the triangular solves with the diagonal blocks' explicit inverses, as
+// two launches.  Forward (L): x_b = Linv_b z_b into zt (k_trsv_block, one CTA per cell),
+// then z_i -= L[i, b] x_b for the rows below (k_trsv_rows).  Backward (U): x_b = Uinv_b
+// zt_b into z, then zt_i -= U[i, b] x_b for the rows above.  The row kernel reads x_b
+// from where the block kernel stored it; the rows it updates never include the block's.
 constexpr int kTrsvRows = 128;
-__global__ void __launch_bounds__(256) k_trsv_step(NewtonCell* nc, int nslots, int b0, int upper) {
-    NewtonCell& N = nc[blockIdx.y];
+__global__ void __launch_bounds__(256) k_trsv_block(NewtonCell* nc, int nslots, int b0, int upper) {
+    NewtonCell& N = nc[blockIdx.x];
     const int m = 2 * N.n;
-    if (blockIdx.y >= nslots || !N.active || b0 >= m) return;
+    if (blockIdx.x >= nslots || !N.active || b0 >= m) return;
     const int kb = min(kNb, m - b0);
-    const int lo = upper ? 0 : b0 + kb, hi = upper ? b0 : m;
-    const int r0 = lo + blockIdx.x * kTrsvRows;
-    if (blockIdx.x > 0 && r0 >= hi) return;
     const float* in = upper ? N.zt : N.z;
     float* out = upper ? N.z : N.zt;
-    float* upd = upper ? N.zt : N.z;
     __shared__ float T[kNb][kNb + 1];
-    __shared__ float rb[kNb], xb[kNb];
+    __shared__ float rb[kNb];
     const float* inv = N.Dinv + (size_t)(b0 / kNb) * 2 * kNb * kNb + (upper ? kNb * kNb : 0);
     if (!upper)
         for (int i = threadIdx.x; i < kNb * kNb; i += blockDim.x) T[i >> 6][i & (kNb - 1)] = inv[i];
@@ -656,18 +652,28 @@ __global__ void __launch_bounds__(256) k_trsv_step(NewtonCell* nc, int nslots, i
         for (int i = threadIdx.x; i < kNb * kNb; i += blockDim.x) T[i & (kNb - 1)][i >> 6] = inv[i];
     if (threadIdx.x < kNb) rb[threadIdx.x] = threadIdx.x < kb ? in[b0 + threadIdx.x] : 0.0f;
     __syncthreads();
-    if (threadIdx.x < kNb) {
+    if (threadIdx.x < kb) {
         float s = 0.0f;
 #pragma unroll 16
         for (int k = 0; k < kNb; ++k) s += T[threadIdx.x][k] * rb[k];
-        xb[threadIdx.x] = s;
-        if (blockIdx.x == 0 && threadIdx.x < kb) out[b0 + threadIdx.x] = s;
+        out[b0 + threadIdx.x] = s;
     }
-    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_trsv_rows(NewtonCell* nc, int nslots, int b0, int upper) {
+    NewtonCell& N = nc[blockIdx.y];
+    const int m = 2 * N.n;
+    if (blockIdx.y >= nslots || !N.active || b0 >= m) return;
+    const int kb = min(kNb, m - b0);
+    const int lo = upper ? 0 : b0 + kb, hi = upper ? b0 : m;
+    const int r0 = lo + blockIdx.x * kTrsvRows;
+    if (r0 >= hi) return;
+    const float* xsrc = (upper ? N.z : N.zt) + b0;
+    float* upd = upper ? N.zt : N.z;
     // a warp per row, four rows in flight: rows i, i + 8, i + 16, i + 24
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int rend = min(r0 + kTrsvRows, hi);
-    const float x0 = xb[lane], x1 = xb[lane + 32];
+    const float x0 = lane < kb ? xsrc[lane] : 0.0f, x1 = lane + 32 < kb ? xsrc[lane + 32] : 0.0f;
     for (int i = r0 + warp; i < rend; i += 32) {
         float s[4];
 #pragma unroll
@@ -1002,13 +1008,17 @@ void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, cudaStream_t st)
     k_trsv_init<<<dim3((unsigned)std::max(1, std::min((m + 255) / 256, 32)), (unsigned)nslots), 256, 0, st>>>(nc, nslots);
     for (int b = 0; b < nblk; ++b) {   // forward, L
         const int rows = m - (b + 1) * kNb;
-        const unsigned g = (unsigned)std::max(1, (rows + kTrsvRows - 1) / kTrsvRows);
-        k_trsv_step<<<dim3(g, (unsigned)nslots), 256, 0, st>>>(nc, nslots, b * kNb, 0);
+        k_trsv_block<<<nslots, 256, 0, st>>>(nc, nslots, b * kNb, 0);
+        if (rows > 0)
+            k_trsv_rows<<<dim3((unsigned)((rows + kTrsvRows - 1) / kTrsvRows), (unsigned)nslots), 256, 0, st>>>(
+                nc, nslots, b * kNb, 0);
     }
     for (int b = nblk - 1; b >= 0; --b) {   // backward, U
         const int rows = b * kNb;
-        const unsigned g = (unsigned)std::max(1, (rows + kTrsvRows - 1) / kTrsvRows);
-        k_trsv_step<<<dim3(g, (unsigned)nslots), 256, 0, st>>>(nc, nslots, b * kNb, 1);
+        k_trsv_block<<<nslots, 256, 0, st>>>(nc, nslots, b * kNb, 1);
+        if (rows > 0)
+            k_trsv_rows<<<dim3((unsigned)((rows + kTrsvRows - 1) / kTrsvRows), (unsigned)nslots), 256, 0, st>>>(
+                nc, nslots, b * kNb, 1);
     }
 }
 void launch_newton_refine(const CellDev* cells, NewtonCell* nc, const int* cell_slot, const WorkItem* work, int nwork,
