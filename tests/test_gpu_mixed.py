@@ -80,13 +80,15 @@ def test_mixed_batched_equals_alone():
         ea.close()
 
 
+@pytest.mark.parametrize("pinned", [False, True])
 @pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
-def test_exchange_path_equals_internal_steps(prec):
+def test_exchange_path_equals_internal_steps(prec, pinned):
     """wcfe_engine_predict / wcfe_engine_update with the host returning the predicted
     positions unchanged is the same computation as wcfe_engine_step: bit-identical for
     the FP64 form.  The mixed form keeps positions as float-float pairs (about 48
     bits) and the exchange carries them as binary64, which can round a pair's low
-    part; its results agree to 1e-9 of each array's magnitude."""
+    part; its results agree to 1e-9 of each array's magnitude.  Both a pageable and
+    a page-locked host buffer."""
     cells = [synth.disk_mesh(n, seed=300 + n) for n in (400, 1300)]
     res = []
     for mode in ("internal", "exchange"):
@@ -99,7 +101,12 @@ def test_exchange_path_equals_internal_steps(prec):
         if mode == "internal":
             e.step(15, 5e-5)
         else:
-            buf = np.zeros((e.total_vertices(), 3))
+            if pinned:
+                import torch
+                pin = torch.zeros((e.total_vertices(), 3), dtype=torch.float64, pin_memory=True)
+                buf = pin.numpy()
+            else:
+                buf = np.zeros((e.total_vertices(), 3))
             for _ in range(15):
                 e.predict_all(5e-5, buf)
                 e.update_all(5e-5, 5e-5, buf)
