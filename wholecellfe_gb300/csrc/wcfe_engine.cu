@@ -146,6 +146,12 @@ struct wcfe_engine {
     uint64_t budget = 0;
     uint64_t used = 0;
     cudaStream_t stream = nullptr;
+    // the exchange path's copies run on their own stream, chunk by chunk, overlapped with
+    // the phases of the other chunks (events: [0, kXChunks) computed, [kXChunks, 2 kXChunks)
+    // copied, 2 kXChunks the stream's previous work)
+    static constexpr int kXChunks = 2;
+    cudaStream_t xstream = nullptr;
+    cudaEvent_t xev[2 * kXChunks + 1] = {};
     int num_sms = 0;
     std::map<int32_t, std::unique_ptr<Cell>> cells;
     int32_t next_id = 0;
@@ -798,6 +804,8 @@ int wcfe_engine_create(int32_t device, int32_t precision, uint64_t hbm_budget_by
     CK(configure_kernels((size_t)max_optin));
     CK(configure_newton((size_t)max_optin, e->num_sms > 0 ? e->num_sms : 1));
     for (auto& ev : e->ev) CK(cudaEventCreate(&ev));
+    CK(cudaStreamCreateWithFlags(&e->xstream, cudaStreamNonBlocking));
+    for (auto& ev : e->xev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     if (precision == WCFE_PREC_MIXED) { e->patch_threads = 128; e->patch_emax = 512; e->vblock = 256; }
     else { e->patch_threads = 64; e->patch_emax = 96; e->vblock = 64; }  // FP64: more, smaller blocks
     *out = e.release();
@@ -822,6 +830,12 @@ int wcfe_engine_destroy(wcfe_engine* e) {
     for (auto& ev : e->ev)
         if (ev) cudaEventDestroy(ev);
     for (auto& ev : e->tev) cudaEventDestroy(ev);
+    for (auto& ev : e->xev)
+        if (ev) cudaEventDestroy(ev);
+    if (e->xstream) {
+        cudaStreamSynchronize(e->xstream);
+        cudaStreamDestroy(e->xstream);
+    }
     cudaStreamDestroy(e->stream);
     delete e;
     return WCFE_OK;
@@ -1555,6 +1569,38 @@ int64_t wcfe_engine_total_vertices(wcfe_engine* e) {
     return e->total_nv;
 }
 
+namespace {
+// The exchange split into up to kXChunks groups of consecutive cells (table order, which
+// is also the order of the work lists and of the packed exchange array), balanced by
+// vertex count.
+struct XChunk {
+    int k1_lo, k1_hi, k2_lo, k2_hi;
+    size_t v_lo, v_hi;
+};
+std::vector<XChunk> exchange_chunks(const wcfe_engine* e) {
+    std::vector<XChunk> out;
+    const int ncell = (int)e->table.size();
+    const int nch = std::max(1, std::min(wcfe_engine::kXChunks, ncell));
+    size_t k1 = 0, k2 = 0, v = 0;
+    int cell = 0;
+    for (int c = 0; c < nch && cell < ncell; ++c) {
+        XChunk x{(int)k1, (int)k1, (int)k2, (int)k2, v, v};
+        const size_t target = (size_t)e->total_nv * (c + 1) / nch;
+        while (cell < ncell && (x.v_hi < target || x.v_hi == x.v_lo || c == nch - 1)) {
+            x.v_hi += (size_t)e->table[cell].nv;
+            while (k1 < e->k1.size() && e->k1[k1].cell == cell) ++k1;
+            while (k2 < e->k2.size() && e->k2[k2].cell == cell) ++k2;
+            ++cell;
+        }
+        x.k1_hi = (int)k1;
+        x.k2_hi = (int)k2;
+        v = x.v_hi;
+        out.push_back(x);
+    }
+    return out;
+}
+}  // namespace
+
 int wcfe_engine_predict(wcfe_engine* e, double dt, double* x_pred) {
     if (e && std::any_of(e->cells.begin(), e->cells.end(), [](const auto& kv) { return kv.second->is_sub; }))
         return fail("coupled substrates step only through wcfe_engine_step", WCFE_ERR_STATE);
@@ -1564,13 +1610,23 @@ int wcfe_engine_predict(wcfe_engine* e, double dt, double* x_pred) {
     int r = sync_tables(e, dt);
     if (r) return r;
     if ((r = ensure_dev(&e->d_xchg, &e->d_xchg_cap, 3 * (size_t)e->total_nv))) return r;
-    const int n1 = (int)e->k1.size();
-    vphase(e, e->d_table, e->d_k1, n1, dt, VP_PREDICT | VP_EXPORT | VP_NOAREA, grid_for(e, n1, vertex_occupancy(e->vblock)),
-           e->stream, nullptr, e->d_xchg);
-    e->launches++;
+    // chunk by chunk: the predicted positions of a chunk copy back while the next one predicts
+    const std::vector<XChunk> ch = exchange_chunks(e);
+    for (size_t c = 0; c < ch.size(); ++c) {
+        const XChunk& x = ch[c];
+        const int n1 = x.k1_hi - x.k1_lo;
+        if (n1 > 0)
+            vphase(e, e->d_table, e->d_k1 + x.k1_lo, n1, dt, VP_PREDICT | VP_EXPORT | VP_NOAREA,
+                   grid_for(e, n1, vertex_occupancy(e->vblock)), e->stream, nullptr, e->d_xchg);
+        e->launches++;
+        CK(cudaEventRecord(e->xev[c], e->stream));
+        CK(cudaStreamWaitEvent(e->xstream, e->xev[c], 0));
+        if (x.v_hi > x.v_lo)
+            CK(cudaMemcpyAsync(x_pred + 3 * x.v_lo, e->d_xchg + 3 * x.v_lo, sizeof(double) * 3 * (x.v_hi - x.v_lo),
+                               cudaMemcpyDeviceToHost, e->xstream));
+    }
     CK(cudaGetLastError());
-    CK(cudaMemcpyAsync(x_pred, e->d_xchg, sizeof(double) * 3 * e->total_nv, cudaMemcpyDeviceToHost, e->stream));
-    CK(cudaStreamSynchronize(e->stream));
+    CK(cudaStreamSynchronize(e->xstream));
     return WCFE_OK;
 }
 
@@ -1583,13 +1639,31 @@ int wcfe_engine_update(wcfe_engine* e, double dt, double dt_real, const double* 
     int r = sync_tables(e, dt_real);
     if (r) return r;
     if ((r = ensure_dev(&e->d_xchg, &e->d_xchg_cap, 3 * (size_t)e->total_nv))) return r;
-    CK(cudaMemcpyAsync(e->d_xchg, x_new, sizeof(double) * 3 * e->total_nv, cudaMemcpyHostToDevice, e->stream));
-    const int n1 = (int)e->k1.size(), n2 = (int)e->k2.size();
-    vphase(e, e->d_table, e->d_k1, n1, dt_real, VP_IMPORT | VP_UPDATE_FA | rec_flag(e), grid_for(e, n1, vertex_occupancy(e->vblock)),
-           e->stream, e->d_xchg, nullptr);
-    patch_step(e, e->d_k2, n2, dt, dt_real, std::numeric_limits<double>::quiet_NaN(),
-               std::numeric_limits<double>::quiet_NaN(), 1);
-    e->launches += 2;
+    // all chunks' copies in on the copy stream (after anything the engine stream still does
+    // with the staging array); each chunk's phases start as soon as its positions are in
+    const std::vector<XChunk> ch = exchange_chunks(e);
+    const int K = wcfe_engine::kXChunks;
+    CK(cudaEventRecord(e->xev[2 * K], e->stream));
+    CK(cudaStreamWaitEvent(e->xstream, e->xev[2 * K], 0));
+    for (size_t c = 0; c < ch.size(); ++c) {
+        const XChunk& x = ch[c];
+        if (x.v_hi > x.v_lo)
+            CK(cudaMemcpyAsync(e->d_xchg + 3 * x.v_lo, x_new + 3 * x.v_lo, sizeof(double) * 3 * (x.v_hi - x.v_lo),
+                               cudaMemcpyHostToDevice, e->xstream));
+        CK(cudaEventRecord(e->xev[K + c], e->xstream));
+    }
+    for (size_t c = 0; c < ch.size(); ++c) {
+        const XChunk& x = ch[c];
+        CK(cudaStreamWaitEvent(e->stream, e->xev[K + c], 0));
+        const int n1 = x.k1_hi - x.k1_lo, n2 = x.k2_hi - x.k2_lo;
+        if (n1 > 0)
+            vphase(e, e->d_table, e->d_k1 + x.k1_lo, n1, dt_real, VP_IMPORT | VP_UPDATE_FA | rec_flag(e),
+                   grid_for(e, n1, vertex_occupancy(e->vblock)), e->stream, e->d_xchg, nullptr);
+        if (n2 > 0)
+            patch_step(e, e->d_k2 + x.k2_lo, n2, dt, dt_real, std::numeric_limits<double>::quiet_NaN(),
+                       std::numeric_limits<double>::quiet_NaN(), 1);
+        e->launches += 2;
+    }
     CK(cudaGetLastError());
     return WCFE_OK;
 }
