@@ -347,6 +347,9 @@ class Engine:
     def free_bytes(self) -> int:
         return int(load().wcfe_engine_free_bytes(self.h))
 
+    def engine_precision(self) -> int:
+        return int(load().wcfe_engine_precision(self.h))
+
 
 class Frames:
     """Asynchronous VTK frame writer of an engine (wcfe_frames_*)."""
@@ -393,6 +396,17 @@ class Cell:
         """Couple this cell to a deformable substrate cell of the same engine (None: uncouple)."""
         check(load().wcfe_cell_couple_substrate(self.eng.h, self.id, -1 if sub is None else sub.id, margin),
               "wcfe_cell_couple_substrate")
+
+    def set_topology(self, tri, n_vert=None, vt_ptr=None, vt_idx=None, bnd=None):
+        """Replace the connectivity (the state, clock and integrins must be set again)."""
+        tri = i32(tri)
+        n = self.n if n_vert is None else int(n_vert)
+        check(load().wcfe_cell_set_topology(self.eng.h, self.id, n, len(tri), ip(tri),
+                                            ip(None if vt_ptr is None else i32(vt_ptr)),
+                                            ip(None if vt_idx is None else i32(vt_idx)),
+                                            None if bnd is None else np.ascontiguousarray(bnd, np.uint8).ctypes.data_as(_u8)),
+              "wcfe_cell_set_topology")
+        self.n, self.nt = n, len(tri)
 
     def remesh(self, split_ab, keep, tri, x_new, vt_ptr=None, vt_idx=None, bnd=None):
         """Rebuild after El Topo's remeshing with the state carried on the device: split_ab
