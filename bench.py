@@ -502,6 +502,25 @@ def run_config2(steps: int = 500, seed: int = 2):
             "status": [out["fp64"][2], out["mixed"][2]]}
 
 
+def lu_roofline(tflops):
+    """The LU's rate against the dense TF32 tensor rate, taken as half the measured bf16
+    GEMM rate (a derived figure: the measured peaks hold bf16 only); sustained, since a
+    factorisation runs for hundreds of milliseconds."""
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        peaks = {}
+    bf16 = peaks.get("bf16_tflops_sustained")
+    src = "MEASURED_PEAKS.json bf16_tflops_sustained / 2"
+    if bf16 is None:
+        bf16, src = 1700.0, "fallback 1700 TFLOP/s bf16 sustained / 2"
+    peak = bf16 / 2.0
+    return {"bound": "tensor", "achieved": tflops, "peak": round(peak, 1), "unit": "TFLOP/s",
+            "frac": round(tflops / peak, 4) if tflops else None, "peak_source": src,
+            "note": "TF32 flops 2/3 (2N)^3 per factorisation over the LU's device time; "
+                    "the trailing updates are HBM-bound at K/4 flop/B (K = 256)"}
+
+
 def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(256, 0)):
     """Config 4, bounded: implicit (Newton) steps of `ncells` cells with 1000-4000 vertices
     (uniform), dense 2N x 2N tangents, LU with TF32 tensor-core trailing updates, FP64
@@ -541,6 +560,7 @@ def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(256, 0)):
             "lu_ms_per_step": round(st["lu_ms"] / steps, 2),
             "lu_tflop_per_s": round(st["lu_gflop"] / st["lu_ms"], 2) if st["lu_ms"] > 0 else None,
             "lu_share_of_step": round(st["lu_ms"] / (wall * 1e3), 3),
+            "lu_roofline": lu_roofline(st["lu_gflop"] / st["lu_ms"] if st["lu_ms"] > 0 else None),
             "solve_ms_per_step": round(st["solve_ms"] / steps, 2),
             "timing": "host wall clock around wcfe_engine_step_implicit (it synchronises per Newton iteration); "
                       "LU: CUDA events around each factorisation, TF32 flops 2/3 (2N)^3 per factored cell"}
