@@ -502,7 +502,7 @@ def run_config2(steps: int = 500, seed: int = 2):
             "status": [out["fp64"][2], out["mixed"][2]]}
 
 
-def lu_roofline(tflops):
+def lu_roofline(tflops, outer_block=512):
     """The LU's rate against the dense TF32 tensor rate, taken as half the measured bf16
     GEMM rate (a derived figure: the measured peaks hold bf16 only); sustained, since a
     factorisation runs for hundreds of milliseconds."""
@@ -518,10 +518,10 @@ def lu_roofline(tflops):
     return {"bound": "tensor", "achieved": tflops, "peak": round(peak, 1), "unit": "TFLOP/s",
             "frac": round(tflops / peak, 4) if tflops else None, "peak_source": src,
             "note": "TF32 flops 2/3 (2N)^3 per factorisation over the LU's device time; "
-                    "the trailing updates are HBM-bound at K/4 flop/B (K = 256)"}
+                    f"a trailing update moves 8 B of the matrix per 2 K flops (K = {outer_block})"}
 
 
-def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(256, 0)):
+def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(512, 0)):
     """Config 4, bounded: implicit (Newton) steps of `ncells` cells with 1000-4000 vertices
     (uniform), dense 2N x 2N tangents, LU with TF32 tensor-core trailing updates, FP64
     residual and refinement to 1e-10.  Reports cell-steps/s, Newton iterations, the
@@ -560,7 +560,7 @@ def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(256, 0)):
             "lu_ms_per_step": round(st["lu_ms"] / steps, 2),
             "lu_tflop_per_s": round(st["lu_gflop"] / st["lu_ms"], 2) if st["lu_ms"] > 0 else None,
             "lu_share_of_step": round(st["lu_ms"] / (wall * 1e3), 3),
-            "lu_roofline": lu_roofline(st["lu_gflop"] / st["lu_ms"] if st["lu_ms"] > 0 else None),
+            "lu_roofline": lu_roofline(st["lu_gflop"] / st["lu_ms"] if st["lu_ms"] > 0 else None, lu[0]),
             "solve_ms_per_step": round(st["solve_ms"] / steps, 2),
             "timing": "host wall clock around wcfe_engine_step_implicit (it synchronises per Newton iteration); "
                       "LU: CUDA events around each factorisation, TF32 flops 2/3 (2N)^3 per factored cell"}
@@ -657,7 +657,7 @@ def main():
                     help="length of the Poisson arrival window of the serving measurement (0: skip)")
     ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain", "newton", "config2"],
                     help="profiling aid: run only one timed loop (default shape, no autotune) and print its timing")
-    ap.add_argument("--lu", default="256,0", help="--phase newton: LU outer block and kind (0 tcgen05, 1 mma.sync)")
+    ap.add_argument("--lu", default="512,0", help="--phase newton: LU outer block and kind (0 tcgen05, 1 mma.sync)")
     ap.add_argument("--newton-cells", type=int, default=512,
                     help="cells of the bounded implicit-step (Newton, dense LU) measurement (0: skip)")
     ap.add_argument("--shape", default="", help="with --phase: patch threads,elements (default: the engine's)")

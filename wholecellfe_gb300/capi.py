@@ -156,8 +156,8 @@ def debug_patch_staging(tri, n_vert, emax=320):
 
 def debug_lu_solve(A, b, block: int | None = None, kind: int = 0):
     """The implicit step's dense LU (TF32 trailing updates) and one unrefined solve.
-    block None: the default LU; else the outer block width (64, 256) and kind (0 tcgen05,
-    1 mma.sync) of wcfe_engine_set_lu."""
+    block None: the default LU; else the outer block width (a multiple of 64 up to 512) and
+    kind (0 tcgen05, 1 mma.sync with block 64) of wcfe_engine_set_lu."""
     A = np.ascontiguousarray(A, np.float32)
     b = np.ascontiguousarray(b, np.float64)
     x = np.zeros(len(b), np.float32)
@@ -312,8 +312,9 @@ class Engine:
     def set_shape(self, threads: int, emax: int):
         check(load().wcfe_engine_set_shape(self.h, threads, emax), "wcfe_engine_set_shape")
 
-    def set_lu(self, block: int = 256, kind: int = 0):
-        """The implicit step's LU: outer block width 64 or 256; kind 0 tcgen05, 1 mma.sync (block 64)."""
+    def set_lu(self, block: int = 512, kind: int = 0):
+        """The implicit step's LU: outer block width (64 to 512 in steps of 64); kind 0 tcgen05,
+        1 mma.sync (block 64)."""
         check(load().wcfe_engine_set_lu(self.h, block, kind), "wcfe_engine_set_lu")
 
     def set_lu_reuse(self, reuse: bool):

@@ -184,7 +184,7 @@ struct wcfe_engine {
     int patch_emax = 320;
     int vblock = 256;             // vertices (threads) per vertex-phase block
     int patch_kernel = 1;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
-    int lu_nb = 256, lu_kind = 0; // implicit step's LU: outer block width, 0 tcgen05 / 1 mma.sync updates
+    int lu_nb = 512, lu_kind = 0; // implicit step's LU: outer block width, 0 tcgen05 / 1 mma.sync updates
     int lu_reuse = 1;             // 1: factor once per implicit step, 0: every Newton iteration
     int cap_ne = 0, cap_nvp = 0, cap_nh = 0, cap_nc = 0;   // largest patch over the cells (staging plan)
     int n2_sub = 0;               // patch work items of substrate cells, at the end of k2 (second launch)
@@ -207,6 +207,12 @@ namespace {
 int fail(const std::string& msg, int code) {
     g_last_error = msg;
     return code;
+}
+
+// kind 0 (tcgen05 updates): outer blocks of 64 to 512 columns in steps of 64; kind 1: 64
+bool lu_block_ok(int block, int kind) {
+    if (kind == 1) return block == 64;
+    return kind == 0 && block >= 64 && block <= 512 && block % 64 == 0;
 }
 
 Cell* find(wcfe_engine* e, int32_t id) {
@@ -1466,8 +1472,7 @@ int wcfe_engine_set_shape(wcfe_engine* e, int32_t threads, int32_t emax) {
 }
 
 int wcfe_engine_set_lu(wcfe_engine* e, int32_t block, int32_t kind) {
-    if (!e || (block != 64 && block != 256) || kind < 0 || kind > 1 || (kind == 1 && block != 64))
-        return fail("bad argument", WCFE_ERR_ARG);
+    if (!e || !lu_block_ok(block, kind)) return fail("bad argument", WCFE_ERR_ARG);
     e->lu_nb = block;
     e->lu_kind = kind;
     return WCFE_OK;
@@ -1686,7 +1691,6 @@ struct NewtonPlan {
 };
 
 size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
-constexpr int kLuUtld = 256;   // Ut row length: the widest outer LU block
 
 // one device block for every cell of the table: packed residual and force arrays, per cell
 // J, element tangents and vectors
@@ -1710,7 +1714,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         f.n = n;
         f.ld = ld;
         f.J = put(sizeof(float) * (size_t)m * ld);
-        f.Ut = put(sizeof(float) * (size_t)m * kLuUtld);
+        f.Ut = put(sizeof(float) * (size_t)m * e->lu_nb);   // Ut row length: the outer block width
         f.Dinv = put(sizeof(float) * 2 * 64 * 64 * (size_t)((m + 63) / 64));
         f.zt = put(sizeof(float) * m);
         f.At = put(sizeof(float) * 64 * (size_t)m);
@@ -1749,7 +1753,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         NewtonCell& N = P.cells[sl];
         N.J = (float*)(b + f.J);
         N.Ut = (float*)(b + f.Ut);
-        N.utld = kLuUtld;
+        N.utld = e->lu_nb;
         N.pad2 = 0;
         N.Dinv = (float*)(b + f.Dinv);
         N.zt = (float*)(b + f.zt);
@@ -2005,13 +2009,12 @@ int wcfe_cell_newton_tangent(wcfe_engine* e, int32_t id, double dt, const double
 }
 
 int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x) {
-    return wcfe_debug_lu_solve_with(m, A, b, x, 256, 0);
+    return wcfe_debug_lu_solve_with(m, A, b, x, 512, 0);
 }
 
 int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* x, int32_t block, int32_t kind) {
     if (m <= 0 || (m & 1) || !A || !b || !x) return fail("bad argument", WCFE_ERR_ARG);
-    if ((block != 64 && block != 256) || kind < 0 || kind > 1 || (kind == 1 && block != 64))
-        return fail("bad argument", WCFE_ERR_ARG);
+    if (!lu_block_ok(block, kind)) return fail("bad argument", WCFE_ERR_ARG);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
         cudaGetLastError();
@@ -2024,7 +2027,7 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     const int ld = (m + 3) & ~3;
     const size_t npref = lu_prefix_capacity(1, m);
     const size_t ndinv = 2 * 64 * 64 * (size_t)((m + 63) / 64);
-    const size_t bytes = sizeof(float) * (size_t)m * ld + sizeof(float) * (size_t)m * kLuUtld + sizeof(double) * m +
+    const size_t bytes = sizeof(float) * (size_t)m * ld + sizeof(float) * (size_t)m * block + sizeof(double) * m +
                          2 * sizeof(float) * m + sizeof(float) * ndinv + sizeof(float) * 64 * (size_t)m +
                          sizeof(double) * 8 + sizeof(NewtonCell) + sizeof(LuMaps) + sizeof(int) * npref + 11 * 256;
     char* blk = nullptr;
@@ -2033,8 +2036,8 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     auto take = [&](size_t n) { char* p = blk + o; o = (o + n + 255) & ~(size_t)255; return p; };
     NewtonCell N{};
     N.J = (float*)take(sizeof(float) * (size_t)m * ld);
-    N.Ut = (float*)take(sizeof(float) * (size_t)m * kLuUtld);
-    N.utld = kLuUtld;
+    N.Ut = (float*)take(sizeof(float) * (size_t)m * block);
+    N.utld = block;
     N.r = (double*)take(sizeof(double) * m);
     N.z = (float*)take(sizeof(float) * m);
     N.zt = (float*)take(sizeof(float) * m);

@@ -893,13 +893,15 @@ void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int
 }
 // The blocked LU of every active cell, in lockstep over the largest matrix.  kind 1: the
 // 64-wide right-looking algorithm with mma.sync updates (nb must be 64).  kind 0:
-// outer blocks of nb (64 or 256) columns; inside one, 64-wide steps factor the diagonal
-// block and the two panels and update only the rest of the outer block's column and
-// row strips; the trailing matrix then takes one update with K = nb on the tcgen05
-// tensor cores.  The per-launch tile counts go to the device in one copy (d_prefix,
-// lu_prefix_capacity ints).
-// per 64-wide step at most a panel launch and an update launch of two regions each, plus
-// per outer block one update of one region
+// outer blocks of nb columns (a multiple of 64 up to 512), each factored recursively by
+// halves: 64-wide leaves factor the diagonal block and the two panels, and each split
+// updates its right half's column strip and row strip with K = the left half's width;
+// the trailing matrix then takes one update with K = nb.  All updates and panels run on
+// the tcgen05 tensor cores.  The per-launch tile counts go to the device in one copy
+// (d_prefix, lu_prefix_capacity ints).
+// A non-empty split update implies a 64-wide leaf inside the matrix (the leftmost of its
+// right half), so there are at most two launches of two regions each per 64 columns, plus
+// per outer block one update of one region.
 size_t lu_prefix_capacity(int nslots, int max_m) {
     return (size_t)3 * ((size_t)(max_m + kNb - 1) / kNb + 1) * (2 * (size_t)nslots + 1);
 }
@@ -945,21 +947,31 @@ const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots,
         ops.push_back({type, k0, a.kb, (int)at, total, a});
     };
     auto update = [&](const LuUpdateArgs& a) { tiles(2, 0, a); };
-    for (int K0 = 0; K0 < max_m; K0 += nb) {
-        for (int ib = 0; ib < nb / kNb && K0 + ib * kNb < max_m; ++ib) {
-            const int k0 = K0 + ib * kNb;
-            ops.push_back({0, k0, 0, 0, 0, {}});
-            if (max_m - k0 - kNb <= 0) break;
-            tiles(1, k0, lu_panel_args(k0, ib * kNb));
-            LuUpdateArgs a{};   // the rest of the outer block's column strip, then of its row strip
-            a.nreg = 2;
-            a.rlo[0] = k0 + kNb; a.rhi[0] = -1; a.clo[0] = k0 + kNb; a.chi[0] = K0 + nb;
-            a.rlo[1] = k0 + kNb; a.rhi[1] = K0 + nb; a.clo[1] = K0 + nb; a.chi[1] = -1;
-            a.ka = k0;
-            a.kb = ib * kNb;
-            a.K = kNb;
-            update(a);
+    // Columns [s, s + w) of the outer block starting at K0, recursively: factor the left
+    // half, update the right half's columns below it and the right half's rows to the
+    // right of the block with K = the left half's width, then factor the right half.  The
+    // strips inside an outer block thus run with K = 64, 128, ... instead of all with 64.
+    auto block = [&](auto&& self, int K0, int s, int w) -> void {
+        if (s >= max_m) return;
+        if (w == kNb) {
+            ops.push_back({0, s, 0, 0, 0, {}});
+            if (max_m - s - kNb > 0) tiles(1, s, lu_panel_args(s, s - K0));
+            return;
         }
+        const int h = kNb * ((w / kNb + 1) / 2);
+        self(self, K0, s, h);
+        LuUpdateArgs a{};
+        a.nreg = 2;
+        a.rlo[0] = s + h; a.rhi[0] = -1; a.clo[0] = s + h; a.chi[0] = s + w;
+        a.rlo[1] = s + h; a.rhi[1] = s + w; a.clo[1] = s + w; a.chi[1] = -1;
+        a.ka = s;
+        a.kb = s - K0;
+        a.K = h;
+        update(a);
+        self(self, K0, s + h, w - h);
+    };
+    for (int K0 = 0; K0 < max_m; K0 += nb) {
+        block(block, K0, K0, nb);
         LuUpdateArgs a{};   // the trailing matrix, K = nb
         a.nreg = 1;
         a.rlo[0] = K0 + nb; a.rhi[0] = -1; a.clo[0] = K0 + nb; a.chi[0] = -1;
