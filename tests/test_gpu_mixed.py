@@ -121,6 +121,57 @@ def test_exchange_path_equals_internal_steps(prec, pinned):
                 assert np.max(np.abs(u - w)) <= 1e-9 * max(np.max(np.abs(w)), 1e-12)
 
 
+@pytest.mark.parametrize("groups", [1, 3, 8])
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
+def test_exchange_groups_equal_internal_steps(prec, groups):
+    """The exchange path with the cells split into groups on their own streams, with calls
+    on the main stream in between (state reads, a regrouping, a status read), is the same
+    computation as wcfe_engine_step: bit-identical for the FP64 form, 1e-9 of each array's
+    magnitude for the mixed form (the binary64 exchange of float-float positions)."""
+    sizes = (300, 900, 500, 1200, 400, 700)
+    cells = [synth.disk_mesh(n, seed=500 + n) for n in sizes]
+    res = []
+    for mode in ("internal", "exchange"):
+        e = capi.Engine(prec)
+        hs = []
+        for i, (x0, tri) in enumerate(cells):
+            p = default_params(["k1", "k31"][i % 2])
+            p.stream = i
+            hs.append(e.add_cell(x0, tri, p, state=synth.initial_state(x0, perturb=1.0, seed=i)))
+        if mode == "internal":
+            e.step(12, 5e-5)
+        else:
+            e.set_exchange_groups(groups)
+            buf = np.zeros((e.total_vertices(), 3))
+            for k in range(12):
+                e.predict_all(5e-5, buf)
+                if k == 4:
+                    hs[2].get_state()            # a main-stream read between predict and update
+                e.update_all(5e-5, 5e-5, buf)
+                if k == 6:
+                    e.set_exchange_groups(1 + groups % 4)
+                if k == 8:
+                    assert hs[5].status() == 0   # and between update and predict
+            e.sync()
+        res.append([h.get_state() for h in hs])
+        e.close()
+    for a, b in zip(*res):
+        for u, w in zip(a, b):
+            if prec == capi.PREC_FP64:
+                assert np.array_equal(u, w)
+            else:
+                assert np.max(np.abs(u - w)) <= 1e-9 * max(np.max(np.abs(w)), 1e-12)
+
+
+def test_exchange_groups_argument():
+    e = capi.Engine(capi.PREC_MIXED)
+    for g in (0, 9, -1):
+        with pytest.raises(capi.WcfeError):
+            e.set_exchange_groups(g)
+    e.set_exchange_groups(8)
+    e.close()
+
+
 def test_mixed_engine_refuses_per_function_entry_points():
     """The reference-function mirrors run on FP64 engines; a mixed engine says so."""
     x0, tri = synth.disk_mesh(300, seed=8)

@@ -77,6 +77,7 @@ SIGNATURES = {
     "wcfe_engine_total_vertices": (C.c_int64, [C.c_void_p]),
     "wcfe_engine_predict": (C.c_int, [C.c_void_p, C.c_double, _d]),
     "wcfe_engine_update": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _d]),
+    "wcfe_engine_set_exchange_groups": (C.c_int, [C.c_void_p, C.c_int32]),
     "wcfe_cell_set_integrins": (C.c_int, [C.c_void_p, C.c_int32, _d]),
     "wcfe_server_create": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_void_p)]),
     "wcfe_server_destroy": (C.c_int, [C.c_void_p]),
@@ -344,6 +345,10 @@ class Engine:
 
     def update_all(self, dt: float, dt_real: float, x_new: np.ndarray):
         check(load().wcfe_engine_update(self.h, dt, dt_real, dp(x_new)), "wcfe_engine_update")
+
+    def set_exchange_groups(self, groups: int):
+        """Exchange path: cells stepped in `groups` (1-8) overlapped groups."""
+        check(load().wcfe_engine_set_exchange_groups(self.h, groups), "wcfe_engine_set_exchange_groups")
 
     def free_bytes(self) -> int:
         return int(load().wcfe_engine_free_bytes(self.h))

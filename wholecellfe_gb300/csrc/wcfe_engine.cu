@@ -146,12 +146,19 @@ struct wcfe_engine {
     uint64_t budget = 0;
     uint64_t used = 0;
     cudaStream_t stream = nullptr;
-    // the exchange path's copies run on their own stream, chunk by chunk, overlapped with
-    // the phases of the other chunks (events: [0, kXChunks) computed, [kXChunks, 2 kXChunks)
-    // copied, 2 kXChunks the stream's previous work)
-    static constexpr int kXChunks = 2;
+    // The exchange path (wcfe_engine_predict / _update) splits the cells into xchunks
+    // groups.  Each group's phases run on its own stream (cstream), its copies on xstream,
+    // so one group's predict and copy-out overlap another's update.  A group depends only
+    // on its own earlier work (cells are independent), so the main stream joins the group
+    // streams lazily: xpending marks group work the main stream has not waited for, and
+    // every other entry point waits for it first (xjoin).  Events: xin copy-in of a group
+    // done, xout a group predicted, cdone a group's work done, xprev the main stream's work.
+    static constexpr int kXMax = 8;
+    int xchunks = 8;
+    bool xpending = false;
     cudaStream_t xstream = nullptr;
-    cudaEvent_t xev[2 * kXChunks + 1] = {};
+    cudaStream_t cstream[kXMax] = {};
+    cudaEvent_t xin[kXMax] = {}, xout[kXMax] = {}, cdone[kXMax] = {}, xprev = nullptr;
     int num_sms = 0;
     std::map<int32_t, std::unique_ptr<Cell>> cells;
     int32_t next_id = 0;
@@ -618,17 +625,25 @@ void invalidate_graph(wcfe_engine* e) {
     e->graph.exec = nullptr;
 }
 
+// the main stream waits for the exchange path's group work (see wcfe_engine::xpending)
+void xjoin(wcfe_engine* e) {
+    if (!e || !e->xpending) return;
+    for (int c = 0; c < wcfe_engine::kXMax; ++c) cudaStreamWaitEvent(e->stream, e->cdone[c], 0);
+    e->xpending = false;
+}
+
 // the patch phase of a step (STEP mode): the staged mixed kernel where it applies
 void patch_step(wcfe_engine* e, const WorkItem* k2, int n2, double dt, double dt_real, double apt, double t_override,
-                int vh_from_buf) {
+                int vh_from_buf, cudaStream_t st = nullptr) {
+    if (!st) st = e->stream;
     if (e->prec == WCFE_PREC_MIXED && e->patch_kernel == 0 &&
         launch_patch_staged(e->d_table, k2, n2, e->cap_ne, e->cap_nvp, e->cap_nh, e->cap_nc, dt, dt_real, apt,
-                            t_override, vh_from_buf, e->num_sms, e->stream))
+                            t_override, vh_from_buf, e->num_sms, st))
         return;
     size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
     launch_patch(e->prec, PP_STEP, e->d_table, k2, n2, e->patch_emax, dt, dt_real, apt, t_override, vh_from_buf,
                  nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, e->patch_threads,
-                 grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem)), e->stream);
+                 grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem)), st);
 }
 
 // one explicit step of the cells listed in (k1, k2) device lists
@@ -811,7 +826,13 @@ int wcfe_engine_create(int32_t device, int32_t precision, uint64_t hbm_budget_by
     CK(configure_newton((size_t)max_optin, e->num_sms > 0 ? e->num_sms : 1));
     for (auto& ev : e->ev) CK(cudaEventCreate(&ev));
     CK(cudaStreamCreateWithFlags(&e->xstream, cudaStreamNonBlocking));
-    for (auto& ev : e->xev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    for (int c = 0; c < wcfe_engine::kXMax; ++c) {
+        CK(cudaStreamCreateWithFlags(&e->cstream[c], cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&e->xin[c], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&e->xout[c], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&e->cdone[c], cudaEventDisableTiming));
+    }
+    CK(cudaEventCreateWithFlags(&e->xprev, cudaEventDisableTiming));
     if (precision == WCFE_PREC_MIXED) { e->patch_threads = 128; e->patch_emax = 512; e->vblock = 256; }
     else { e->patch_threads = 64; e->patch_emax = 96; e->vblock = 64; }  // FP64: more, smaller blocks
     *out = e.release();
@@ -821,6 +842,7 @@ int wcfe_engine_create(int32_t device, int32_t precision, uint64_t hbm_budget_by
 int wcfe_engine_destroy(wcfe_engine* e) {
     if (!e) return WCFE_ERR_ARG;
     cudaSetDevice(e->device);
+    xjoin(e);
     cudaStreamSynchronize(e->stream);
     for (auto& kv : e->cells) free_cell(e, kv.second.get());
     e->cells.clear();
@@ -836,8 +858,15 @@ int wcfe_engine_destroy(wcfe_engine* e) {
     for (auto& ev : e->ev)
         if (ev) cudaEventDestroy(ev);
     for (auto& ev : e->tev) cudaEventDestroy(ev);
-    for (auto& ev : e->xev)
-        if (ev) cudaEventDestroy(ev);
+    for (int c = 0; c < wcfe_engine::kXMax; ++c) {
+        if (e->cstream[c]) {
+            cudaStreamSynchronize(e->cstream[c]);
+            cudaStreamDestroy(e->cstream[c]);
+        }
+        for (cudaEvent_t ev : {e->xin[c], e->xout[c], e->cdone[c]})
+            if (ev) cudaEventDestroy(ev);
+    }
+    if (e->xprev) cudaEventDestroy(e->xprev);
     if (e->xstream) {
         cudaStreamSynchronize(e->xstream);
         cudaStreamDestroy(e->xstream);
@@ -861,6 +890,7 @@ uint64_t wcfe_cell_bytes(int32_t nv, int32_t nt) {
     return (uint64_t)(s + p + rho_bytes(nv));
 }
 int wcfe_engine_sync(wcfe_engine* e) {
+    xjoin(e);
     if (!e) return WCFE_ERR_ARG;
     CK(cudaStreamSynchronize(e->stream));
     return WCFE_OK;
@@ -868,6 +898,7 @@ int wcfe_engine_sync(wcfe_engine* e) {
 
 int wcfe_cell_create(wcfe_engine* e, int32_t nv, int32_t nt, const int32_t* tri, const int32_t* vt_ptr,
                      const int32_t* vt_idx, const uint8_t* is_bnd, const wcfe_params* params, int32_t* cell_out) {
+    xjoin(e);
     if (!e || !tri || !params || !cell_out || nv <= 0 || nt <= 0) return fail("bad argument", WCFE_ERR_ARG);
     CK(cudaSetDevice(e->device));
     std::unique_ptr<Cell> c(new Cell());
@@ -889,6 +920,7 @@ int wcfe_cell_create(wcfe_engine* e, int32_t nv, int32_t nt, const int32_t* tri,
 }
 
 int wcfe_cell_destroy(wcfe_engine* e, int32_t id) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     // drop substrate couplings that involve this cell
@@ -905,6 +937,7 @@ int wcfe_cell_destroy(wcfe_engine* e, int32_t id) {
 }
 
 int wcfe_cell_set_params(wcfe_engine* e, int32_t id, const wcfe_params* p) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c || !p) return fail("bad argument", WCFE_ERR_ARG);
     c->prm = *p;
@@ -915,6 +948,7 @@ int wcfe_cell_set_params(wcfe_engine* e, int32_t id, const wcfe_params* p) {
 
 int wcfe_cell_set_topology(wcfe_engine* e, int32_t id, int32_t nv, int32_t nt, const int32_t* tri,
                            const int32_t* vt_ptr, const int32_t* vt_idx, const uint8_t* is_bnd) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c || !tri) return fail("bad argument", WCFE_ERR_ARG);
     CK(cudaSetDevice(e->device));
@@ -944,6 +978,7 @@ int wcfe_cell_set_topology(wcfe_engine* e, int32_t id, int32_t nv, int32_t nt, c
 int wcfe_cell_remesh(wcfe_engine* e, int32_t id, int32_t n_split, const int32_t* split_ab, int32_t nv_new,
                      const int32_t* keep, int32_t nt_new, const int32_t* tri, const int32_t* vt_ptr,
                      const int32_t* vt_idx, const uint8_t* is_bnd, const double* x_new) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     if (n_split < 0 || (n_split > 0 && !split_ab) || nv_new <= 0 || !keep || nt_new <= 0 || !tri || !x_new)
@@ -1044,6 +1079,7 @@ int wcfe_cell_remesh(wcfe_engine* e, int32_t id, int32_t n_split, const int32_t*
 
 int wcfe_cell_set_substrate(wcfe_engine* e, int32_t id, int32_t nv, int32_t nt, const int32_t* tri, const double* Xs,
                             const double* xs) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     CK(cudaSetDevice(e->device));
@@ -1069,6 +1105,7 @@ int wcfe_cell_set_substrate(wcfe_engine* e, int32_t id, int32_t nv, int32_t nt, 
 
 int wcfe_cell_set_state(wcfe_engine* e, int32_t id, const double* x, const double* V, const double* A, const double* ea,
                         const double* cA, const double* cC, const double* fau) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     CK(cudaSetDevice(e->device));
@@ -1102,6 +1139,7 @@ int wcfe_cell_set_state(wcfe_engine* e, int32_t id, const double* x, const doubl
 
 int wcfe_cell_get_state(wcfe_engine* e, int32_t id, double* x, double* V, double* A, double* ea, double* cA,
                         double* cC, double* fau) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     CK(cudaSetDevice(e->device));
@@ -1132,6 +1170,7 @@ int wcfe_cell_get_state(wcfe_engine* e, int32_t id, double* x, double* V, double
 }
 
 int wcfe_cell_set_clock(wcfe_engine* e, int32_t id, double t, uint64_t calls) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     unsigned long long ap = calls;
@@ -1142,6 +1181,7 @@ int wcfe_cell_set_clock(wcfe_engine* e, int32_t id, double t, uint64_t calls) {
 }
 
 int wcfe_cell_get_clock(wcfe_engine* e, int32_t id, double* t, uint64_t* calls) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     double tt;
@@ -1155,6 +1195,7 @@ int wcfe_cell_get_clock(wcfe_engine* e, int32_t id, double* t, uint64_t* calls) 
 }
 
 int wcfe_cell_status(wcfe_engine* e, int32_t id, uint32_t* status) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c || !status) return fail("bad argument", WCFE_ERR_ARG);
     CK(cudaMemcpyAsync(status, c->dev.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->stream));
@@ -1163,6 +1204,7 @@ int wcfe_cell_status(wcfe_engine* e, int32_t id, uint32_t* status) {
 }
 
 int wcfe_cell_sizes(wcfe_engine* e, int32_t id, int32_t* nv, int32_t* nt, int32_t* nb, int32_t* np) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     if (nv) *nv = c->topo.nv;
@@ -1174,6 +1216,7 @@ int wcfe_cell_sizes(wcfe_engine* e, int32_t id, int32_t* nv, int32_t* nt, int32_
 
 // ---- drop-in pieces -------------------------------------------------------
 int wcfe_cell_predict(wcfe_engine* e, int32_t id, double dt, double* x_pred, double* V_hlf) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     if (e->prec == WCFE_PREC_MIXED)
@@ -1196,6 +1239,7 @@ int wcfe_cell_predict(wcfe_engine* e, int32_t id, double dt, double* x_pred, dou
 
 int wcfe_cell_update_fa(wcfe_engine* e, int32_t id, double dt_real, const double* X, const double* x_new,
                         const double* X_s, const double* x_s) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c || !x_new) return fail("bad argument", WCFE_ERR_ARG);
     if (e->prec == WCFE_PREC_MIXED)
@@ -1239,6 +1283,7 @@ int wcfe_cell_update_fa(wcfe_engine* e, int32_t id, double dt_real, const double
 }
 
 int wcfe_cell_update_forces(wcfe_engine* e, int32_t id, double dt, double dt_real, double t_tot) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     if (e->prec == WCFE_PREC_MIXED)
@@ -1263,6 +1308,7 @@ int wcfe_cell_update_forces(wcfe_engine* e, int32_t id, double dt, double dt_rea
 int wcfe_cell_eval_residual(wcfe_engine* e, int32_t id, const double* X, const double* x_new, double dt_real,
                             const double centroid[3], double t_tot, double* Res, double* Res_ea, double* MM,
                             double* Res_Adif, double* Res_Cdif) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c || !X || !x_new || !centroid) return fail("bad argument", WCFE_ERR_ARG);
     if (e->prec == WCFE_PREC_MIXED)
@@ -1306,6 +1352,7 @@ int wcfe_cell_eval_residual(wcfe_engine* e, int32_t id, const double* X, const d
 
 int wcfe_cell_eval_forces(wcfe_engine* e, int32_t id, const double* x, double dt_real, double* F_FA, double* F_AP,
                           double* F_bend, double* F_area, double area4[4]) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c || !x) return fail("bad argument", WCFE_ERR_ARG);
     if (e->prec == WCFE_PREC_MIXED)
@@ -1352,6 +1399,7 @@ int wcfe_cell_eval_forces(wcfe_engine* e, int32_t id, const double* x, double dt
 
 // ---- batched stepping -------------------------------------------------------
 int wcfe_engine_step(wcfe_engine* e, int32_t nsteps, double dt) {
+    xjoin(e);
     if (!e || nsteps < 0 || !(dt > 0)) return fail("bad argument", WCFE_ERR_ARG);
     if (e->cells.empty() || nsteps == 0) return WCFE_OK;
     CK(cudaSetDevice(e->device));
@@ -1419,6 +1467,7 @@ int wcfe_engine_step(wcfe_engine* e, int32_t nsteps, double dt) {
 }
 
 int wcfe_engine_step_cells(wcfe_engine* e, const int32_t* ids, int32_t ncells, int32_t nsteps, double dt) {
+    xjoin(e);
     if (!e || !ids || ncells <= 0 || nsteps < 0 || !(dt > 0)) return fail("bad argument", WCFE_ERR_ARG);
     if (e && std::any_of(e->cells.begin(), e->cells.end(), [](const auto& kv) { return kv.second->is_sub; }))
         return fail("coupled substrates step only through wcfe_engine_step", WCFE_ERR_STATE);
@@ -1443,6 +1492,7 @@ int wcfe_engine_step_cells(wcfe_engine* e, const int32_t* ids, int32_t ncells, i
 }
 
 int wcfe_engine_set_graphs(wcfe_engine* e, int32_t enable) {
+    xjoin(e);
     if (!e) return WCFE_ERR_ARG;
     e->use_graphs = enable != 0;
     if (!e->use_graphs) invalidate_graph(e);
@@ -1450,6 +1500,7 @@ int wcfe_engine_set_graphs(wcfe_engine* e, int32_t enable) {
 }
 
 int wcfe_engine_set_shape(wcfe_engine* e, int32_t threads, int32_t emax) {
+    xjoin(e);
     if (!e) return WCFE_ERR_ARG;
     if (threads == 0) threads = e->patch_threads;
     if (emax == 0) emax = e->patch_emax;
@@ -1472,6 +1523,7 @@ int wcfe_engine_set_shape(wcfe_engine* e, int32_t threads, int32_t emax) {
 }
 
 int wcfe_engine_set_lu(wcfe_engine* e, int32_t block, int32_t kind) {
+    xjoin(e);
     if (!e || !lu_block_ok(block, kind)) return fail("bad argument", WCFE_ERR_ARG);
     e->lu_nb = block;
     e->lu_kind = kind;
@@ -1479,12 +1531,14 @@ int wcfe_engine_set_lu(wcfe_engine* e, int32_t block, int32_t kind) {
 }
 
 int wcfe_engine_set_lu_reuse(wcfe_engine* e, int32_t reuse) {
+    xjoin(e);
     if (!e || reuse < 0 || reuse > 1) return fail("bad argument", WCFE_ERR_ARG);
     e->lu_reuse = reuse;
     return WCFE_OK;
 }
 
 int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind) {
+    xjoin(e);
     if (!e || kind < 0 || kind > 1) return fail("bad argument", WCFE_ERR_ARG);
     e->patch_kernel = kind;
     invalidate_graph(e);
@@ -1499,6 +1553,7 @@ int wcfe_engine_get_shape(const wcfe_engine* e, int32_t* threads, int32_t* emax)
 }
 
 int wcfe_engine_set_timing(wcfe_engine* e, int32_t enable) {
+    xjoin(e);
     if (!e) return WCFE_ERR_ARG;
     e->timing = enable != 0;
     return WCFE_OK;
@@ -1512,6 +1567,7 @@ int64_t wcfe_engine_step_times(wcfe_engine* e, float* out, int64_t cap, float* s
 }
 
 int wcfe_engine_last_timing(wcfe_engine* e, float* ms_v, float* ms_p) {
+    xjoin(e);
     if (!e) return WCFE_ERR_ARG;
     if (ms_v) *ms_v = e->ms_v;
     if (ms_p) *ms_p = e->ms_p;
@@ -1575,7 +1631,7 @@ int64_t wcfe_engine_total_vertices(wcfe_engine* e) {
 }
 
 namespace {
-// The exchange split into up to kXChunks groups of consecutive cells (table order, which
+// The exchange split into up to xchunks groups of consecutive cells (table order, which
 // is also the order of the work lists and of the packed exchange array), balanced by
 // vertex count.
 struct XChunk {
@@ -1585,7 +1641,7 @@ struct XChunk {
 std::vector<XChunk> exchange_chunks(const wcfe_engine* e) {
     std::vector<XChunk> out;
     const int ncell = (int)e->table.size();
-    const int nch = std::max(1, std::min(wcfe_engine::kXChunks, ncell));
+    const int nch = std::max(1, std::min(e->xchunks, ncell));
     size_t k1 = 0, k2 = 0, v = 0;
     int cell = 0;
     for (int c = 0; c < nch && cell < ncell; ++c) {
@@ -1604,6 +1660,26 @@ std::vector<XChunk> exchange_chunks(const wcfe_engine* e) {
     }
     return out;
 }
+
+// Start of an exchange call: the tables (re-uploaded on the main stream once every group
+// stream has finished with them, if they changed) and whether the group streams are
+// already ordered after everything the main stream holds.  They are when the last work
+// on this engine was an exchange call; otherwise each group stream, and the copy stream,
+// waits for the main stream.
+int exchange_begin(wcfe_engine* e, double dt, bool* ordered) {
+    const bool stale = (dt > 0 && dt != e->table_dt) || e->table_version != e->version;
+    if (stale) xjoin(e);
+    int r = sync_tables(e, dt);
+    if (r) return r;
+    if ((r = ensure_dev(&e->d_xchg, &e->d_xchg_cap, 3 * (size_t)e->total_nv))) return r;
+    *ordered = e->xpending;
+    if (!e->xpending) {
+        CK(cudaEventRecord(e->xprev, e->stream));
+        CK(cudaStreamWaitEvent(e->xstream, e->xprev, 0));
+        for (int c = 0; c < wcfe_engine::kXMax; ++c) CK(cudaStreamWaitEvent(e->cstream[c], e->xprev, 0));
+    }
+    return WCFE_OK;
+}
 }  // namespace
 
 int wcfe_engine_predict(wcfe_engine* e, double dt, double* x_pred) {
@@ -1612,24 +1688,27 @@ int wcfe_engine_predict(wcfe_engine* e, double dt, double* x_pred) {
     if (!e || !x_pred || !(dt > 0)) return fail("bad argument", WCFE_ERR_ARG);
     if (e->cells.empty()) return WCFE_OK;
     CK(cudaSetDevice(e->device));
-    int r = sync_tables(e, dt);
+    bool ordered = false;
+    int r = exchange_begin(e, dt, &ordered);
     if (r) return r;
-    if ((r = ensure_dev(&e->d_xchg, &e->d_xchg_cap, 3 * (size_t)e->total_nv))) return r;
-    // chunk by chunk: the predicted positions of a chunk copy back while the next one predicts
+    // group by group on the group's own stream (after that group's update): the predicted
+    // positions of a group copy back while the other groups still update or predict
     const std::vector<XChunk> ch = exchange_chunks(e);
     for (size_t c = 0; c < ch.size(); ++c) {
         const XChunk& x = ch[c];
         const int n1 = x.k1_hi - x.k1_lo;
         if (n1 > 0)
             vphase(e, e->d_table, e->d_k1 + x.k1_lo, n1, dt, VP_PREDICT | VP_EXPORT | VP_NOAREA,
-                   grid_for(e, n1, vertex_occupancy(e->vblock)), e->stream, nullptr, e->d_xchg);
+                   grid_for(e, n1, vertex_occupancy(e->vblock)), e->cstream[c], nullptr, e->d_xchg);
         e->launches++;
-        CK(cudaEventRecord(e->xev[c], e->stream));
-        CK(cudaStreamWaitEvent(e->xstream, e->xev[c], 0));
+        CK(cudaEventRecord(e->xout[c], e->cstream[c]));
+        CK(cudaEventRecord(e->cdone[c], e->cstream[c]));
+        CK(cudaStreamWaitEvent(e->xstream, e->xout[c], 0));
         if (x.v_hi > x.v_lo)
             CK(cudaMemcpyAsync(x_pred + 3 * x.v_lo, e->d_xchg + 3 * x.v_lo, sizeof(double) * 3 * (x.v_hi - x.v_lo),
                                cudaMemcpyDeviceToHost, e->xstream));
     }
+    e->xpending = true;
     CK(cudaGetLastError());
     CK(cudaStreamSynchronize(e->xstream));
     return WCFE_OK;
@@ -1641,35 +1720,45 @@ int wcfe_engine_update(wcfe_engine* e, double dt, double dt_real, const double* 
     if (!e || !x_new || !(dt > 0) || !(dt_real > 0)) return fail("bad argument", WCFE_ERR_ARG);
     if (e->cells.empty()) return WCFE_OK;
     CK(cudaSetDevice(e->device));
-    int r = sync_tables(e, dt_real);
+    bool ordered = false;
+    int r = exchange_begin(e, dt_real, &ordered);
     if (r) return r;
-    if ((r = ensure_dev(&e->d_xchg, &e->d_xchg_cap, 3 * (size_t)e->total_nv))) return r;
-    // all chunks' copies in on the copy stream (after anything the engine stream still does
-    // with the staging array); each chunk's phases start as soon as its positions are in
     const std::vector<XChunk> ch = exchange_chunks(e);
-    const int K = wcfe_engine::kXChunks;
-    CK(cudaEventRecord(e->xev[2 * K], e->stream));
-    CK(cudaStreamWaitEvent(e->xstream, e->xev[2 * K], 0));
+    // a group's copy overwrites its part of the staging array only after that group's
+    // earlier work has read it
+    if (ordered)
+        for (size_t c = 0; c < ch.size(); ++c) CK(cudaStreamWaitEvent(e->xstream, e->cdone[c], 0));
     for (size_t c = 0; c < ch.size(); ++c) {
         const XChunk& x = ch[c];
         if (x.v_hi > x.v_lo)
             CK(cudaMemcpyAsync(e->d_xchg + 3 * x.v_lo, x_new + 3 * x.v_lo, sizeof(double) * 3 * (x.v_hi - x.v_lo),
                                cudaMemcpyHostToDevice, e->xstream));
-        CK(cudaEventRecord(e->xev[K + c], e->xstream));
+        CK(cudaEventRecord(e->xin[c], e->xstream));
     }
+    // each group's phases start on its own stream as soon as its positions are in
     for (size_t c = 0; c < ch.size(); ++c) {
         const XChunk& x = ch[c];
-        CK(cudaStreamWaitEvent(e->stream, e->xev[K + c], 0));
+        cudaStream_t st = e->cstream[c];
+        CK(cudaStreamWaitEvent(st, e->xin[c], 0));
         const int n1 = x.k1_hi - x.k1_lo, n2 = x.k2_hi - x.k2_lo;
         if (n1 > 0)
             vphase(e, e->d_table, e->d_k1 + x.k1_lo, n1, dt_real, VP_IMPORT | VP_UPDATE_FA | rec_flag(e),
-                   grid_for(e, n1, vertex_occupancy(e->vblock)), e->stream, e->d_xchg, nullptr);
+                   grid_for(e, n1, vertex_occupancy(e->vblock)), st, e->d_xchg, nullptr);
         if (n2 > 0)
             patch_step(e, e->d_k2 + x.k2_lo, n2, dt, dt_real, std::numeric_limits<double>::quiet_NaN(),
-                       std::numeric_limits<double>::quiet_NaN(), 1);
+                       std::numeric_limits<double>::quiet_NaN(), 1, st);
+        CK(cudaEventRecord(e->cdone[c], st));
         e->launches += 2;
     }
+    e->xpending = true;
     CK(cudaGetLastError());
+    return WCFE_OK;
+}
+
+int wcfe_engine_set_exchange_groups(wcfe_engine* e, int32_t groups) {
+    if (!e || groups < 1 || groups > wcfe_engine::kXMax) return fail("bad argument", WCFE_ERR_ARG);
+    xjoin(e);
+    e->xchunks = groups;
     return WCFE_OK;
 }
 
@@ -1950,6 +2039,7 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
 
 int wcfe_engine_step_implicit(wcfe_engine* e, int32_t nsteps, double dt, double newton_rtol, int32_t max_newton,
                               wcfe_newton_stats* stats) {
+    xjoin(e);
     if (!e || nsteps < 0 || !(dt > 0) || !(newton_rtol > 0) || max_newton < 1) return fail("bad argument", WCFE_ERR_ARG);
     if (e->prec != WCFE_PREC_FP64)
         return fail("the implicit step runs on an FP64 engine (WCFE_PREC_FP64)", WCFE_ERR_STATE);
@@ -1972,6 +2062,7 @@ int wcfe_engine_step_implicit(wcfe_engine* e, int32_t nsteps, double dt, double 
 }
 
 int wcfe_cell_newton_tangent(wcfe_engine* e, int32_t id, double dt, const double* x, float* J_out, double* diag_out) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c || !x || !J_out || !(dt > 0)) return fail("bad argument", WCFE_ERR_ARG);
     if (e->prec != WCFE_PREC_FP64)
@@ -2080,6 +2171,7 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
 }
 
 int wcfe_cell_set_element_mu(wcfe_engine* e, int32_t id, const double* mu) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     CK(cudaSetDevice(e->device));
@@ -2116,6 +2208,7 @@ int wcfe_cell_set_element_mu(wcfe_engine* e, int32_t id, const double* mu) {
 }
 
 int wcfe_cell_couple_substrate(wcfe_engine* e, int32_t id, int32_t sub_id, double grid_margin) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     if (e->prec != WCFE_PREC_FP64) return fail("substrate coupling runs on an FP64 engine", WCFE_ERR_STATE);
@@ -2186,6 +2279,7 @@ int wcfe_cell_couple_substrate(wcfe_engine* e, int32_t id, int32_t sub_id, doubl
 }
 
 int wcfe_cell_set_integrins(wcfe_engine* e, int32_t id, const double* rho) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c) return fail("unknown cell", WCFE_ERR_ARG);
     CK(cudaSetDevice(e->device));
@@ -2222,6 +2316,7 @@ int wcfe_cell_set_integrins(wcfe_engine* e, int32_t id, const double* rho) {
 // Autotuner: time every candidate (threads, emax) on the live cells.  The state
 // is saved and restored around the trials so tuning does not advance the cells.
 int wcfe_engine_autotune(wcfe_engine* e, double dt, int32_t reps) {
+    xjoin(e);
     if (!e || !(dt > 0) || reps < 1) return fail("bad argument", WCFE_ERR_ARG);
     if (e->cells.empty()) return WCFE_OK;
     CK(cudaSetDevice(e->device));
@@ -2287,6 +2382,7 @@ int set_error(const char* msg, int code) {
 int engine_device(wcfe_engine* e) { return e->device; }
 
 int engine_frame_source(wcfe_engine* e, int32_t id, FrameSource* out) {
+    xjoin(e);
     Cell* c = e ? find(e, id) : nullptr;
     if (!c || !out) return fail("unknown cell", WCFE_ERR_ARG);
     out->dev = c->dev;

@@ -193,22 +193,33 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
         const int q = warp & 3;                   // the TMEM lane quadrant this warp may access
         const int i0 = 32 * ((warp - 2) >> 2);    // rows of the tile (TMEM columns) of this warp
         const uint32_t lane_field = (uint32_t)(32 * q) << 16;
-        int it = 0;
-        for (int f = blockIdx.x; f < total; f += gridDim.x, ++it) {
-            const int b = it & 1;
-            const uint32_t v = (uint32_t)(it >> 1);
-            const Tile t = decode_tile(nc, prefix, ngroups, a, f);
+        // Software-pipelined over this CTA's tiles: once a tile's product is subtracted, the
+        // next tile's C values are requested before this tile's results are stored, so their
+        // latency overlaps the stores and the next product.  The tiles of one launch are
+        // disjoint, so a load of the next tile never reads what this tile writes.
+        // This warp's 32 rows of a tile: rows t.tm + i0 + r, r < nrows valid.
+        int f = blockIdx.x, slot = 0, ld = 0, nrows = 0;
+        float* __restrict__ Cb = nullptr;
+        auto locate = [&](int ff) {
+            const Tile t = decode_tile(nc, prefix, ngroups, a, ff);
             const int col = t.tn + 32 * q + lane;
-            const int ld = nc[t.slot].ld;
-            // this warp's 32 rows of the tile: rows t.tm + i0 + r, r < nrows valid
-            const int nrows = col < t.chi ? min(32, t.rhi - (t.tm + i0)) : 0;
-            float* __restrict__ Cb = nc[t.slot].J + (size_t)(t.tm + i0) * ld + col;
-            float c[32];
+            slot = t.slot;
+            ld = nc[t.slot].ld;
+            nrows = col < t.chi ? min(32, t.rhi - (t.tm + i0)) : 0;
+            Cb = nc[t.slot].J + (size_t)(t.tm + i0) * ld + col;
+        };
+        float c[32];
+        if (f < total) {
+            locate(f);
 #pragma unroll
             for (int r = 0; r < 32; ++r) c[r] = r < nrows ? Cb[r * ld] : 0.0f;
+        }
+        for (int it = 0; f < total; f += gridDim.x, ++it) {
+            const int b = it & 1;
+            const uint32_t v = (uint32_t)(it >> 1);
             const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(tfull + b, v & 1u, kWait));
             if (!ok) {
-                if (lane == 0) nc[t.slot].norms[3] = 2.0;
+                if (lane == 0) nc[slot].norms[3] = 2.0;
                 *abort_s = 1;
                 break;
             }
@@ -218,14 +229,19 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(tempty + b);   // the accumulator may be overwritten
-            // the row stride through a shuffle: the store addresses are recomputed here rather
-            // than kept live (in registers) from the loads across the wait
-            const int lds = __shfl_sync(0xffffffffu, ld, 0);
+#pragma unroll
+            for (int r = 0; r < 32; ++r) p[r] = c[r] - p[r];
+            // row r of this tile is stored, then row r of the next tile requested: about 32
+            // values stay live instead of 64
             float* __restrict__ Cs = Cb;
+            const int lds = ld, ns = nrows;
+            if (f + (int)gridDim.x < total) locate(f + (int)gridDim.x);
+            else nrows = 0;
 #pragma unroll
             for (int r = 0; r < 32; ++r) {
-                if (r < nrows) *Cs = c[r] - p[r];
+                if (r < ns) *Cs = p[r];
                 Cs += lds;
+                c[r] = r < nrows ? Cb[r * ld] : 0.0f;
             }
             if (*abort_s) break;
         }
