@@ -521,6 +521,34 @@ def lu_roofline(tflops, outer_block=512):
                     f"a trailing update moves 8 B of the matrix per 2 K flops (K = {outer_block})"}
 
 
+def cpu_lu_baseline(sizes, budget_s: float = 12.0):
+    """FP64 LU (LAPACK dgetrf through scipy.linalg.lu_factor, all host threads) of the
+    workload's 2N x 2N matrices, cell by cell until the time budget is spent: the CPU
+    counterpart of the implicit step's factorisation.  Diagonally dominant random matrices
+    of the cells' sizes (dgetrf's time does not depend on the values)."""
+    try:
+        import scipy.linalg as sla
+    except ImportError as ex:
+        return {"unavailable": f"scipy: {ex}"}
+    rng = np.random.default_rng(5)
+    done, secs, flops = 0, 0.0, 0.0
+    for n in sizes:
+        m = 2 * int(n)
+        A = rng.standard_normal((m, m)) + m * np.eye(m)
+        A = np.asfortranarray(A)
+        t0 = time.perf_counter()
+        sla.lu_factor(A, overwrite_a=True, check_finite=False)
+        secs += time.perf_counter() - t0
+        flops += 2.0 / 3.0 * m ** 3
+        done += 1
+        if secs > budget_s:
+            break
+    return {"kind": "scipy.linalg.lu_factor (LAPACK dgetrf, FP64, partial pivoting)", "cores": os.cpu_count(),
+            "sample": f"the first {done} of the workload's {len(sizes)} matrices (2N = {2 * min(sizes[:done])}"
+                      f"-{2 * max(sizes[:done])})",
+            "lu_per_s": round(done / secs, 3), "tflop_per_s": round(flops / secs / 1e12, 4)}
+
+
 def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(512, 0)):
     """Config 4, bounded: implicit (Newton) steps of `ncells` cells with 1000-4000 vertices
     (uniform), dense 2N x 2N tangents, LU with TF32 tensor-core trailing updates, FP64
@@ -562,6 +590,7 @@ def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(512, 0)):
             "lu_share_of_step": round(st["lu_ms"] / (wall * 1e3), 3),
             "lu_roofline": lu_roofline(st["lu_gflop"] / st["lu_ms"] if st["lu_ms"] > 0 else None, lu[0]),
             "solve_ms_per_step": round(st["solve_ms"] / steps, 2),
+            "cpu_lu_baseline": cpu_lu_baseline(sizes),
             "timing": "host wall clock around wcfe_engine_step_implicit (it synchronises per Newton iteration); "
                       "LU: CUDA events around each factorisation, TF32 flops 2/3 (2N)^3 per factored cell"}
 
