@@ -5,16 +5,19 @@
 // L = J[rows, ka:ka+K] (the L21 panel, K-major as stored) and Ut the transposed U rows
 // of the current outer block (Ut[c][k] = U[K0 + k][c], written by the panel kernel).
 // The MMA computes the transposed product D = Ut L^T with M = 128 columns of C and
-// N = 128 rows of C, so a TMEM lane is a column of C and a TMEM column is a row of C:
+// N = TM rows of C, so a TMEM lane is a column of C and a TMEM column is a row of C:
 // each epilogue thread owns one column of the tile and reads and writes C one row at a
 // time, a warp covering 32 consecutive floats (coalesced, no staging buffer).
 //
-// Persistent CTAs, one per SM, walk a flat list of 128 x 128 tiles over all cells (the
-// host gives the per-cell tile counts as a prefix sum).  Warp 0 streams the operand
+// Persistent CTAs, one per SM, walk a flat list of TM x 128 tiles over all cells (the
+// host gives the per-cell tile counts as a prefix sum); TM = 256 rows for the updates
+// with K >= 512, whose operand reads from L2 bound them (a 256-row tile reads a quarter
+// fewer operand bytes per flop), 128 for the narrower strips.  Warp 0 streams the operand
 // boxes with TMA into a 4-stage ring (K = 32 per stage, 128-byte swizzled); one thread of
 // warp 1 issues the MMAs into two TMEM accumulators, so tile t + 1 multiplies while tile t
-// is written back; 16 epilogue warps, four per TMEM lane quadrant (32 rows of C each),
-// prefetch the tile's C values before its product is ready, then subtract and store.
+// is written back; 16 epilogue warps, four per TMEM lane quadrant (TM / 4 rows of C each,
+// in slices of 32), prefetch each slice's C values before its product is needed, then
+// subtract and store.
 //
 // Every wait is bounded: on a timeout the CTA flags the cell it was working on (norms[3],
 // the LU's failure flag), stops issuing work, waits (bounded) for its copies and MMAs in
@@ -32,16 +35,20 @@
 namespace wcfe {
 namespace {
 
-constexpr int kTile = 128;                         // tile rows and columns of C
+constexpr int kTile = 128;                         // tile columns of C (and rows, but for wide updates)
 constexpr int kBK = 32;                            // K per pipeline stage (one 128-B swizzle atom of fp32)
 constexpr int kStages = 4;
 constexpr int kEpiWarps = 16;                     // four per TMEM lane quadrant, 32 rows of C each
 constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr uint32_t kBoxBytes = 128u * 128u;        // 128 rows x 128 B
-constexpr uint32_t kStageBytes = 2 * kBoxBytes;    // Ut box, then L box
-constexpr uint32_t kTmemCols = 256;                // two 128-column fp32 accumulators
+// update tiles of TM rows x 128 columns of C: TM = 256 for the K >= 512 updates (a quarter
+// fewer operand bytes per flop), 128 for the narrower strip updates
+template <int TM>
+__host__ __device__ constexpr uint32_t stage_bytes() { return (1 + TM / 128) * kBoxBytes; }   // Ut box, then TM / 128 L boxes
+template <int TM>
+__host__ __device__ constexpr size_t update_smem() { return 1024 + (size_t)kStages * stage_bytes<TM>() + 256; }
+constexpr uint32_t kStageBytes = stage_bytes<128>();
 constexpr long long kWait = 2000000000ll;          // SM clocks (about 1 s) before a wait gives up
-constexpr size_t kSmemBytes = 1024 + (size_t)kStages * kStageBytes + 256;
 
 struct Tile {
     int slot, reg, tm, tn, rhi, chi;
@@ -55,7 +62,9 @@ __device__ __forceinline__ void region_of(const LuUpdateArgs& a, int r, int m, i
     chi = a.chi[r] < 0 ? m : min(a.chi[r], m);
 }
 
-// flat tile f -> cell, tile origin; groups are (cell, region) pairs in cell-major order
+// flat tile f -> cell, tile origin; groups are (cell, region) pairs in cell-major order;
+// tiles of TM rows x 128 columns
+template <int TM = kTile>
 __device__ __forceinline__ Tile decode_tile(const NewtonCell* nc, const int* __restrict__ prefix, int ngroups, const LuUpdateArgs& a,
                             int f) {
     int lo = 0, hi = ngroups;   // prefix[lo] <= f < prefix[hi]; empty groups are skipped
@@ -73,19 +82,23 @@ __device__ __forceinline__ Tile decode_tile(const NewtonCell* nc, const int* __r
     region_of(a, reg, m, rlo, rhi, clo, chi);
     const int tiles_n = (chi - clo + kTile - 1) / kTile;
     const int local = f - __ldg(prefix + lo);
-    t.tm = rlo + (local / tiles_n) * kTile;
+    t.tm = rlo + (local / tiles_n) * TM;
     t.tn = clo + (local % tiles_n) * kTile;
     t.rhi = rhi;
     t.chi = chi;
     return t;
 }
 
+template <int TM>
 __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, const LuMaps* __restrict__ maps,
                                                              const int* __restrict__ prefix, int ngroups,
                                                              LuUpdateArgs a) {
+    constexpr int NH = TM / 128;                        // 32-row slices of C per epilogue warp
+    constexpr uint32_t kSB = stage_bytes<TM>();
+    constexpr uint32_t kCols = 2 * TM;                  // two TM-column fp32 accumulators
     extern __shared__ uint8_t tc_smem_raw[];
     uint8_t* sm = tc_smem_raw + ((1024u - (smem_addr(tc_smem_raw) & 1023u)) & 1023u);
-    uint64_t* full = reinterpret_cast<uint64_t*>(sm + kStages * kStageBytes);
+    uint64_t* full = reinterpret_cast<uint64_t*>(sm + kStages * kSB);
     uint64_t* empty = full + kStages;
     uint64_t* tfull = empty + kStages;
     uint64_t* tempty = tfull + 2;
@@ -110,7 +123,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
         mbar_init_fence();
     }
     if (warp == 1) {
-        tc_alloc(tbase_s, kTmemCols);
+        tc_alloc(tbase_s, kCols);
         tc_relinquish();
     }
     tc_fence_before();
@@ -123,7 +136,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
         if (lane == 0) {
             int g = 0;   // chunks issued so far
             for (int f = blockIdx.x; f < total && !*abort_s; f += gridDim.x) {
-                const Tile t = decode_tile(nc, prefix, ngroups, a, f);
+                const Tile t = decode_tile<TM>(nc, prefix, ngroups, a, f);
                 const LuMaps* mp = maps + t.slot;
                 tmap_acquire(&mp->umap);
                 tmap_acquire(&mp->jmap);
@@ -135,10 +148,12 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
                         nc[t.slot].norms[3] = 2.0;
                         break;
                     }
-                    uint8_t* st = sm + s * kStageBytes;
-                    mbar_arrive_expect_tx(full + s, kStageBytes);
+                    uint8_t* st = sm + s * kSB;
+                    mbar_arrive_expect_tx(full + s, kSB);
                     tma_load_2d(st, &mp->umap, a.kb + c * kBK, t.tn, full + s);
-                    tma_load_2d(st + kBoxBytes, &mp->jmap, a.ka + c * kBK, t.tm, full + s);
+#pragma unroll
+                    for (int j = 0; j < NH; ++j)   // rows past the matrix read as zeros
+                        tma_load_2d(st + (1 + j) * kBoxBytes, &mp->jmap, a.ka + c * kBK, t.tm + 128 * j, full + s);
                 }
             }
             // every stage's last fill has landed before the CTA may exit
@@ -151,7 +166,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
     } else if (warp == 1) {
         // ---------------------------------------------------------------- MMA issuer
         if (lane == 0) {
-            const uint32_t idesc = tc_idesc_tf32(kTile, kTile);
+            const uint32_t idesc = tc_idesc_tf32(kTile, TM);
             int g = 0, it = 0;
             for (int f = blockIdx.x; f < total && !*abort_s; f += gridDim.x, ++it) {
                 const int b = it & 1;
@@ -161,7 +176,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
                     break;
                 }
                 tc_fence_after();
-                const uint32_t d = tbase + (uint32_t)(b * kTile);
+                const uint32_t d = tbase + (uint32_t)(b * TM);
                 bool ok = true;
                 for (int c = 0; c < nch; ++c, ++g) {
                     const int s = g % kStages;
@@ -171,7 +186,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t sa = smem_addr(sm + s * kStageBytes);
+                    const uint32_t sa = smem_addr(sm + s * kSB);
                     const uint64_t da = tc_desc_k_sw128(sa), db = tc_desc_k_sw128(sa + kBoxBytes);
 #pragma unroll
                     for (int k = 0; k < kBK / 8; ++k)
@@ -191,23 +206,28 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
     } else {
         // ---------------------------------------------------------------- epilogue: C -= D^T
         const int q = warp & 3;                   // the TMEM lane quadrant this warp may access
-        const int i0 = 32 * ((warp - 2) >> 2);    // rows of the tile (TMEM columns) of this warp
+        const int g = (warp - 2) >> 2;            // this warp's NH slices of 32 rows: rows 32 (NH g + h)
         const uint32_t lane_field = (uint32_t)(32 * q) << 16;
-        // Software-pipelined over this CTA's tiles: once a tile's product is subtracted, the
-        // next tile's C values are requested before this tile's results are stored, so their
-        // latency overlaps the stores and the next product.  The tiles of one launch are
-        // disjoint, so a load of the next tile never reads what this tile writes.
-        // This warp's 32 rows of a tile: rows t.tm + i0 + r, r < nrows valid.
-        int f = blockIdx.x, slot = 0, ld = 0, nrows = 0;
+        // Software-pipelined: once a slice's product is subtracted, the following slice's C
+        // values (the same tile's next slice, or the next tile's first) are requested between
+        // this slice's stores, so their latency overlaps the stores and the next product.  The
+        // tiles of one launch are disjoint, so a load never reads what a store of this launch
+        // writes.  A slice: rows r0 + r of column col, r < nrows valid.
+        Tile t{};
+        int ld = 0, nrows = 0;
         float* __restrict__ Cb = nullptr;
-        auto locate = [&](int ff) {
-            const Tile t = decode_tile(nc, prefix, ngroups, a, ff);
+        auto slice = [&](int h) {
             const int col = t.tn + 32 * q + lane;
-            slot = t.slot;
-            ld = nc[t.slot].ld;
-            nrows = col < t.chi ? min(32, t.rhi - (t.tm + i0)) : 0;
-            Cb = nc[t.slot].J + (size_t)(t.tm + i0) * ld + col;
+            const int r0 = t.tm + 32 * (NH * g + h);
+            nrows = col < t.chi ? min(32, t.rhi - r0) : 0;
+            Cb = nc[t.slot].J + (size_t)r0 * ld + col;
         };
+        auto locate = [&](int ff) {
+            t = decode_tile<TM>(nc, prefix, ngroups, a, ff);
+            ld = nc[t.slot].ld;
+            slice(0);
+        };
+        int f = blockIdx.x;
         float c[32];
         if (f < total) {
             locate(f);
@@ -219,29 +239,35 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
             const uint32_t v = (uint32_t)(it >> 1);
             const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(tfull + b, v & 1u, kWait));
             if (!ok) {
-                if (lane == 0) nc[slot].norms[3] = 2.0;
+                if (lane == 0) nc[t.slot].norms[3] = 2.0;
                 *abort_s = 1;
                 break;
             }
             tc_fence_after();
-            float p[32];
-            tc_ld_32x32b_x32(tbase + (uint32_t)(b * kTile + i0) + lane_field, p);
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(tempty + b);   // the accumulator may be overwritten
+#pragma unroll 1
+            for (int h = 0; h < NH; ++h) {
+                float p[32];
+                tc_ld_32x32b_x32(tbase + (uint32_t)(b * TM + 32 * (NH * g + h)) + lane_field, p);
+                if (h == NH - 1) {
+                    tc_fence_before();
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(tempty + b);   // the accumulator may be overwritten
+                }
 #pragma unroll
-            for (int r = 0; r < 32; ++r) p[r] = c[r] - p[r];
-            // row r of this tile is stored, then row r of the next tile requested: about 32
-            // values stay live instead of 64
-            float* __restrict__ Cs = Cb;
-            const int lds = ld, ns = nrows;
-            if (f + (int)gridDim.x < total) locate(f + (int)gridDim.x);
-            else nrows = 0;
+                for (int r = 0; r < 32; ++r) p[r] = c[r] - p[r];
+                // row r of this slice is stored, then row r of the following slice requested:
+                // about 32 values stay live instead of 64
+                float* __restrict__ Cs = Cb;
+                const int lds = ld, ns = nrows;
+                if (h + 1 < NH) slice(h + 1);
+                else if (f + (int)gridDim.x < total) locate(f + (int)gridDim.x);
+                else nrows = 0;
 #pragma unroll
-            for (int r = 0; r < 32; ++r) {
-                if (r < ns) *Cs = p[r];
-                Cs += lds;
-                c[r] = r < nrows ? Cb[r * ld] : 0.0f;
+                for (int r = 0; r < 32; ++r) {
+                    if (r < ns) *Cs = p[r];
+                    Cs += lds;
+                    c[r] = r < nrows ? Cb[r * ld] : 0.0f;
+                }
             }
             if (*abort_s) break;
         }
@@ -250,7 +276,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
     __syncthreads();
     if (warp == 1) {
         tc_fence_after();
-        tc_dealloc(tbase, kTmemCols);
+        tc_dealloc(tbase, kCols);
     }
 }
 
@@ -463,16 +489,22 @@ cudaError_t configure_lu_tc(int num_sms) {
         if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorSymbolNotFound;
         g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
-    cudaError_t e = cudaFuncSetAttribute((const void*)k_lu_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kSmemBytes);
+    cudaError_t e = cudaFuncSetAttribute((const void*)k_lu_update_tc<128>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)update_smem<128>());
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute((const void*)k_lu_update_tc<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)update_smem<256>());
     if (e != cudaSuccess) return e;
     e = cudaFuncSetAttribute((const void*)k_lu_panels_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kPSmemBytes);
     if (e != cudaSuccess) return e;
     cudaFuncAttributes at;
-    if ((e = cudaFuncGetAttributes(&at, (const void*)k_lu_update_tc)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&at, (const void*)k_lu_update_tc<128>)) != cudaSuccess) return e;
     g_lu_tc_regs = at.numRegs;
     g_lu_tc_max_threads = at.maxThreadsPerBlock;
+    if ((e = cudaFuncGetAttributes(&at, (const void*)k_lu_update_tc<256>)) != cudaSuccess) return e;
+    g_lu_tc_regs = std::max(g_lu_tc_regs, at.numRegs);
+    g_lu_tc_max_threads = std::min(g_lu_tc_max_threads, at.maxThreadsPerBlock);
     return cudaSuccess;
 }
 
@@ -504,7 +536,12 @@ int encode_lu_maps(const NewtonCell* h, int nslots, LuMaps* out) {
 
 // tiles of one update launch per (cell, region) group, as a prefix sum (ngroups + 1 entries);
 // returns the total
+// rows of an update tile: 256 for the updates with K >= 512, else 128 (the kernel
+// instantiation and the host's tile counts both follow this)
+int lu_tile_rows(const LuUpdateArgs& a) { return a.K >= 512 ? 256 : kTile; }
+
 int lu_update_prefix(const NewtonCell* h, int nslots, const LuUpdateArgs& a, int* pref) {
+    const int tm = lu_tile_rows(a);
     int acc = 0;
     for (int s = 0; s < nslots; ++s)
         for (int r = 0; r < a.nreg; ++r) {
@@ -513,7 +550,7 @@ int lu_update_prefix(const NewtonCell* h, int nslots, const LuUpdateArgs& a, int
             const int m = 2 * h[s].n;
             const int rlo = std::min(a.rlo[r], m), rhi = a.rhi[r] < 0 ? m : std::min(a.rhi[r], m);
             const int clo = std::min(a.clo[r], m), chi = a.chi[r] < 0 ? m : std::min(a.chi[r], m);
-            if (rhi > rlo && chi > clo) acc += ((rhi - rlo + kTile - 1) / kTile) * ((chi - clo + kTile - 1) / kTile);
+            if (rhi > rlo && chi > clo) acc += ((rhi - rlo + tm - 1) / tm) * ((chi - clo + kTile - 1) / kTile);
         }
     pref[nslots * a.nreg] = acc;
     return acc;
@@ -524,7 +561,10 @@ bool launch_lu_update_tc(NewtonCell* nc, const LuMaps* maps, const int* d_prefix
     if (g_lu_tc_max_threads < kThreads) return false;
     if (total <= 0) return true;
     const int grid = std::max(1, std::min(total, g_sms > 0 ? g_sms : 1));
-    k_lu_update_tc<<<grid, kThreads, kSmemBytes, st>>>(nc, maps, d_prefix, nslots * a.nreg, a);
+    if (lu_tile_rows(a) == 256)
+        k_lu_update_tc<256><<<grid, kThreads, update_smem<256>(), st>>>(nc, maps, d_prefix, nslots * a.nreg, a);
+    else
+        k_lu_update_tc<128><<<grid, kThreads, update_smem<128>(), st>>>(nc, maps, d_prefix, nslots * a.nreg, a);
     return cudaGetLastError() == cudaSuccess;
 }
 

@@ -385,33 +385,39 @@ __global__ void __launch_bounds__(256) k_lu_diag(NewtonCell* nc, int nslots, int
     for (int i = ty; i < kb; i += 16)
         for (int j = tx; j < kb; j += 16) N.J[(size_t)(k0 + i) * N.ld + k0 + j] = A[i][j];
     // explicit inverses of the (identity-padded) unit-lower and upper factors, one column per
-    // thread held in registers: L X = I forward, U Y = I backward.  Stored as Linv and Uinv^T
-    // (row-major), the K-major operands of the tensor-core panels.
+    // thread: L X = I forward, U Y = I backward.  Rolled loops: fully unrolled, the two
+    // substitutions were about 8k instructions that each launch's four warps ran once, from
+    // a cold instruction cache.  Both inverses share one array Z: column j of Linv below
+    // the diagonal (its diagonal is 1, the rest 0) and column j of Uinv on and above it, so
+    // each thread reads only entries of its own column that it wrote.  The zero terms the
+    // substitutions skip contribute exact zeros.  Stored as Linv and Uinv^T (row-major), the
+    // K-major operands of the tensor-core panels.
+    __shared__ float Z[kNb][kNb + 1];
     float* Li = N.Dinv + (size_t)(k0 / kNb) * 2 * kNb * kNb;
     float* Ui = Li + kNb * kNb;
-    float x[kNb];
     if (threadIdx.x < kNb) {
         const int j = threadIdx.x;
-#pragma unroll
-        for (int i = 0; i < kNb; ++i) {
-            float s = i == j ? 1.0f : 0.0f;
-#pragma unroll
-            for (int k = 0; k < i; ++k) s -= A[i][k] * x[k];
-            x[i] = s;
+        for (int i = j + 1; i < kNb; ++i) {
+            float s = -A[i][j];
+#pragma unroll 4
+            for (int k = j + 1; k < i; ++k) s -= A[i][k] * Z[k][j];
+            Z[i][j] = s;
         }
-#pragma unroll
-        for (int i = 0; i < kNb; ++i) Li[i * kNb + j] = x[i];
     } else if (threadIdx.x < 2 * kNb) {
         const int j = threadIdx.x - kNb;
-#pragma unroll
-        for (int i = kNb - 1; i >= 0; --i) {
+        for (int i = j; i >= 0; --i) {
             float s = i == j ? 1.0f : 0.0f;
-#pragma unroll
-            for (int k = i + 1; k < kNb; ++k) s -= A[i][k] * x[k];
-            x[i] = s / A[i][i];
+#pragma unroll 4
+            for (int k = i + 1; k <= j; ++k) s -= A[i][k] * Z[k][j];
+            Z[i][j] = s / A[i][i];
         }
-#pragma unroll
-        for (int i = 0; i < kNb; ++i) Ui[j * kNb + i] = x[i];   // stored transposed: row j = column j of Uinv
+    }
+    __syncthreads();
+    // coalesced stores: Li[r][c] = Linv[r][c]; Ui[r][c] = Uinv[c][r]
+    for (int e = threadIdx.x; e < kNb * kNb; e += blockDim.x) {
+        const int r = e / kNb, cc = e % kNb;
+        Li[e] = r > cc ? Z[r][cc] : (r == cc ? 1.0f : 0.0f);
+        Ui[e] = cc <= r ? Z[cc][r] : 0.0f;
     }
 }
 
