@@ -359,6 +359,12 @@ int wcfe_engine_set_lu_reuse(wcfe_engine* e, int32_t reuse);
  * LU (no pivoting; TF32 tensor-core trailing updates) and solve A x = b once
  * (unrefined).  Device 0; for tests of the factorisation itself. */
 int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x);
+/* The tensor-core LU's schedule for a matrix of order m and outer block `block` (host
+ * logic, no device): *nops steps, each 14 int32 in ops (when ops is not NULL and cap, in
+ * int32, holds them): type (0 diagonal 64 x 64 factor and its inverses at k0, 1 that
+ * step's panels, 2 region update), k0, nreg, ka, kb, K, then (rlo, rhi, clo, chi) of two
+ * regions (-1 = m): C[rlo:rhi, clo:chi] -= J[rlo:rhi, ka:ka+K] U[ka:ka+K, clo:chi]. */
+int wcfe_debug_lu_schedule(int32_t m, int32_t block, int32_t* ops, int32_t cap, int32_t* nops);
 /* The same with the LU variant of wcfe_engine_set_lu. */
 int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* x, int32_t block, int32_t kind);
 

@@ -78,6 +78,7 @@ SIGNATURES = {
     "wcfe_engine_predict": (C.c_int, [C.c_void_p, C.c_double, _d]),
     "wcfe_engine_update": (C.c_int, [C.c_void_p, C.c_double, C.c_double, _d]),
     "wcfe_engine_set_exchange_groups": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_debug_lu_schedule": (C.c_int, [C.c_int32, C.c_int32, _i, C.c_int32, _i]),
     "wcfe_cell_set_integrins": (C.c_int, [C.c_void_p, C.c_int32, _d]),
     "wcfe_server_create": (C.c_int, [C.c_void_p, C.c_double, C.POINTER(C.c_void_p)]),
     "wcfe_server_destroy": (C.c_int, [C.c_void_p]),
@@ -153,6 +154,16 @@ def debug_patch_staging(tri, n_vert, emax=320):
     xinfo = xinfo[:4 * npv].reshape(npv, 4)
     return dict(np=npv, xinfo=xinfo, halo=halo, loc=loc.reshape(-1, 4),
                 max_ne=int(mx[0]), max_nvp=int(mx[1]), max_nh=int(mx[2]), max_nc=int(mx[3]))
+
+
+def debug_lu_schedule(m: int, block: int = 512):
+    """The tensor-core LU's schedule (host logic): an int32 array [nops][14] of
+    (type, k0, nreg, ka, kb, K, rlo0, rhi0, clo0, chi0, rlo1, rhi1, clo1, chi1)."""
+    n = C.c_int32()
+    check(load().wcfe_debug_lu_schedule(m, block, None, 0, C.byref(n)), "wcfe_debug_lu_schedule")
+    ops = np.zeros((n.value, 14), np.int32)
+    check(load().wcfe_debug_lu_schedule(m, block, ip(ops), ops.size, C.byref(n)), "wcfe_debug_lu_schedule")
+    return ops
 
 
 def debug_lu_solve(A, b, block: int | None = None, kind: int = 0):

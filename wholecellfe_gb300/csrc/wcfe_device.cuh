@@ -174,6 +174,16 @@ struct LuUpdateArgs {
     int nreg, ka, kb, K;
 };
 
+// One step of the tensor-core LU's schedule (host side): type 0 factors the 64 x 64
+// diagonal block at k0 and forms its inverses; type 1 computes that step's panels (L21 for
+// the rows below, U12 for the columns to the right; a = lu_panel_args); type 2 updates up
+// to two regions, C[rlo:rhi, clo:chi] -= J[rows, ka:ka+K] U[K0+kb : K0+kb+K, cols] (a bound
+// of -1 is the matrix's order).
+struct LuOp {
+    int type, k0;
+    LuUpdateArgs a;
+};
+
 struct WorkItem {               // one block of a phase: (cell index into the table, block/patch index)
     int32_t cell, idx;
 };

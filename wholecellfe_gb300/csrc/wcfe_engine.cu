@@ -58,6 +58,7 @@ std::string lu_attr_note() {
            " threads per block)";
 }
 size_t lu_prefix_capacity(int nslots, int max_m);
+std::vector<LuOp> lu_schedule(int max_m, int nb);
 int encode_lu_maps(const NewtonCell* h, int nslots, LuMaps* out);
 void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, cudaStream_t st);
 void launch_newton_refine(const CellDev* cells, NewtonCell* nc, const int* cell_slot, const WorkItem* work, int nwork,
@@ -2097,6 +2098,23 @@ int wcfe_cell_newton_tangent(wcfe_engine* e, int32_t id, double dt, const double
     }
     newton_free(e, P);
     return r;
+}
+
+int wcfe_debug_lu_schedule(int32_t m, int32_t block, int32_t* ops, int32_t cap, int32_t* nops) {
+    if (m <= 0 || !nops || !lu_block_ok(block, 0) || cap < 0 || (cap > 0 && !ops))
+        return fail("bad argument", WCFE_ERR_ARG);
+    const std::vector<LuOp> sched = lu_schedule(m, block);
+    *nops = (int32_t)sched.size();
+    if (!ops) return WCFE_OK;
+    if ((int64_t)sched.size() * 14 > (int64_t)cap) return fail("ops buffer too small", WCFE_ERR_LIMIT);
+    for (const LuOp& o : sched) {
+        const LuUpdateArgs& a = o.a;
+        const int32_t rec[14] = {o.type,    o.k0,      a.nreg,    a.ka,      a.kb,      a.K,       a.rlo[0],
+                                 a.rhi[0],  a.clo[0],  a.chi[0],  a.rlo[1],  a.rhi[1],  a.clo[1],  a.chi[1]};
+        std::memcpy(ops, rec, sizeof rec);
+        ops += 14;
+    }
+    return WCFE_OK;
 }
 
 int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x) {

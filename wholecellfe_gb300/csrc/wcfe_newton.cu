@@ -912,6 +912,46 @@ size_t lu_prefix_capacity(int nslots, int max_m) {
     return (size_t)3 * ((size_t)(max_m + kNb - 1) / kNb + 1) * (2 * (size_t)nslots + 1);
 }
 
+// The kind-0 schedule for matrices of order up to max_m with outer blocks of nb columns.
+// Columns [s, s + w) of the outer block starting at K0, recursively: factor the left half,
+// update the right half's columns below it and the right half's rows to the right of the
+// block with K = the left half's width, then factor the right half.  The strips inside an
+// outer block thus run with K = 64, 128, ... instead of all with 64; the trailing matrix
+// then takes one update with K = nb.  A 64-wide step at the matrix's end has no panels.
+std::vector<LuOp> lu_schedule(int max_m, int nb) {
+    std::vector<LuOp> ops;
+    auto block = [&](auto&& self, int K0, int s, int w) -> void {
+        if (s >= max_m) return;
+        if (w == kNb) {
+            ops.push_back({0, s, {}});
+            if (max_m - s - kNb > 0) ops.push_back({1, s, lu_panel_args(s, s - K0)});
+            return;
+        }
+        const int h = kNb * ((w / kNb + 1) / 2);
+        self(self, K0, s, h);
+        LuUpdateArgs a{};
+        a.nreg = 2;
+        a.rlo[0] = s + h; a.rhi[0] = -1; a.clo[0] = s + h; a.chi[0] = s + w;
+        a.rlo[1] = s + h; a.rhi[1] = s + w; a.clo[1] = s + w; a.chi[1] = -1;
+        a.ka = s;
+        a.kb = s - K0;
+        a.K = h;
+        ops.push_back({2, s, a});
+        self(self, K0, s + h, w - h);
+    };
+    for (int K0 = 0; K0 < max_m; K0 += nb) {
+        block(block, K0, K0, nb);
+        LuUpdateArgs a{};   // the trailing matrix, K = nb
+        a.nreg = 1;
+        a.rlo[0] = K0 + nb; a.rhi[0] = -1; a.clo[0] = K0 + nb; a.chi[0] = -1;
+        a.ka = K0;
+        a.kb = 0;
+        a.K = nb;
+        ops.push_back({2, K0, a});
+    }
+    return ops;
+}
+
 const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots, int max_m, const LuMaps* maps,
                              int* d_prefix, int nb, int kind, cudaStream_t st) {
     const char* failed = nullptr;
@@ -942,50 +982,19 @@ const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots,
     };
     std::vector<Op> ops;
     std::vector<int> pref;
-    auto tiles = [&](int type, int k0, const LuUpdateArgs& a) {
+    for (const LuOp& o : lu_schedule(max_m, nb)) {
+        if (o.type == 0) {
+            ops.push_back({0, o.k0, 0, 0, 0, {}});
+            continue;
+        }
         const size_t at = pref.size();
-        pref.resize(at + (size_t)nslots * a.nreg + 1);
-        const int total = lu_update_prefix(h_nc, nslots, a, pref.data() + at);
+        pref.resize(at + (size_t)nslots * o.a.nreg + 1);
+        const int total = lu_update_prefix(h_nc, nslots, o.a, pref.data() + at);
         if (!total) {
             pref.resize(at);
-            return;
+            continue;
         }
-        ops.push_back({type, k0, a.kb, (int)at, total, a});
-    };
-    auto update = [&](const LuUpdateArgs& a) { tiles(2, 0, a); };
-    // Columns [s, s + w) of the outer block starting at K0, recursively: factor the left
-    // half, update the right half's columns below it and the right half's rows to the
-    // right of the block with K = the left half's width, then factor the right half.  The
-    // strips inside an outer block thus run with K = 64, 128, ... instead of all with 64.
-    auto block = [&](auto&& self, int K0, int s, int w) -> void {
-        if (s >= max_m) return;
-        if (w == kNb) {
-            ops.push_back({0, s, 0, 0, 0, {}});
-            if (max_m - s - kNb > 0) tiles(1, s, lu_panel_args(s, s - K0));
-            return;
-        }
-        const int h = kNb * ((w / kNb + 1) / 2);
-        self(self, K0, s, h);
-        LuUpdateArgs a{};
-        a.nreg = 2;
-        a.rlo[0] = s + h; a.rhi[0] = -1; a.clo[0] = s + h; a.chi[0] = s + w;
-        a.rlo[1] = s + h; a.rhi[1] = s + w; a.clo[1] = s + w; a.chi[1] = -1;
-        a.ka = s;
-        a.kb = s - K0;
-        a.K = h;
-        update(a);
-        self(self, K0, s + h, w - h);
-    };
-    for (int K0 = 0; K0 < max_m; K0 += nb) {
-        block(block, K0, K0, nb);
-        LuUpdateArgs a{};   // the trailing matrix, K = nb
-        a.nreg = 1;
-        a.rlo[0] = K0 + nb; a.rhi[0] = -1; a.clo[0] = K0 + nb; a.chi[0] = -1;
-        a.ka = K0;
-        a.kb = 0;
-        a.K = nb;
-        a.rlo[1] = a.rhi[1] = a.clo[1] = a.chi[1] = 0;
-        update(a);
+        ops.push_back({o.type, o.k0, o.a.kb, (int)at, total, o.a});
     }
     if (pref.size() > lu_prefix_capacity(nslots, max_m)) return "tile lists (capacity)";
     if (!pref.empty()) cudaMemcpyAsync(d_prefix, pref.data(), sizeof(int) * pref.size(), cudaMemcpyHostToDevice, st);
