@@ -431,6 +431,8 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_panels_tc(NewtonCell* nc, co
         const int q = warp & 3;
         const int j0 = 16 * ((warp - 2) >> 2);   // the 16 TMEM columns (panel entries) of this warp
         const uint32_t lane_field = (uint32_t)(32 * q) << 16;
+        __shared__ float stage_rows[kEpiWarps][32][17];   // per warp: 32 rows of 16 entries (padded)
+        float (*S)[17] = stage_rows[warp - 2];
         int it = 0;
         for (int f = blockIdx.x; f < total; f += gridDim.x, ++it) {
             const int b = it & 1;
@@ -450,25 +452,39 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_panels_tc(NewtonCell* nc, co
             if (lane == 0) mbar_arrive(tempty + b);
             NewtonCell& N = nc[t.slot];
             const int m = 2 * N.n;
-            if (t.reg == 0) {   // L21 row
-                const int row = t.tm + 32 * q + lane;
-                if (row < m) {
-                    float4* dst = reinterpret_cast<float4*>(N.J + (size_t)row * N.ld + k0 + j0);
+            // Rows of 16 entries (this warp's TMEM columns) go out two rows per store
+            // instruction, each a whole 64-byte segment, through the warp's staging tile:
+            // lane l writes row (l >> 4) + 2 r2, entry l & 15.
+            const int rl0 = lane >> 4, cl = lane & 15;
+            if (t.reg == 0) {   // L21 rows t.tm + 32 q + i, entries k0 + j0 + 0..15 of each
 #pragma unroll
-                    for (int r = 0; r < 4; ++r) dst[r] = make_float4(p[4 * r], p[4 * r + 1], p[4 * r + 2], p[4 * r + 3]);
+                for (int r = 0; r < 16; ++r) S[lane][r] = p[r];
+                __syncwarp();
+                const int rbase = t.tm + 32 * q;
+#pragma unroll 4
+                for (int r2 = 0; r2 < 16; ++r2) {
+                    const int rl = rl0 + 2 * r2, row = rbase + rl;
+                    if (row < m) N.J[(size_t)row * N.ld + k0 + j0 + cl] = S[rl][cl];
                 }
-            } else {            // U12 column
+                __syncwarp();
+            } else {            // U12 columns t.tn + 32 q + i: rows k0 + j0 + 0..15 of J, and Ut rows
                 const int col = t.tn + 32 * q + lane;
                 if (col < m) {
-                    if (N.Ut) {
-                        float4* ut = reinterpret_cast<float4*>(N.Ut + (size_t)col * N.utld + kbase + j0);
-#pragma unroll
-                        for (int r = 0; r < 4; ++r)
-                            ut[r] = make_float4(p[4 * r], p[4 * r + 1], p[4 * r + 2], p[4 * r + 3]);
-                    }
                     float* dst = N.J + (size_t)(k0 + j0) * N.ld + col;
 #pragma unroll
                     for (int r = 0; r < 16; ++r) dst[(size_t)r * N.ld] = p[r];
+                }
+                if (N.Ut) {
+#pragma unroll
+                    for (int r = 0; r < 16; ++r) S[lane][r] = p[r];
+                    __syncwarp();
+                    const int cbase = t.tn + 32 * q;
+#pragma unroll 4
+                    for (int r2 = 0; r2 < 16; ++r2) {
+                        const int rl = rl0 + 2 * r2, c = cbase + rl;
+                        if (c < m) N.Ut[(size_t)c * N.utld + kbase + j0 + cl] = S[rl][cl];
+                    }
+                    __syncwarp();
                 }
             }
             if (*abort_s) break;
