@@ -13,8 +13,10 @@
  *   vertex -> triangle map (CSR, in the mesh's own order)    : int32[n+1], int32[3t]
  *
  * Every entry point returns an int status (WCFE_OK == 0).  No C++ exception
- * crosses the ABI.  An engine owns one CUDA stream on one device; calls on one
- * engine are not re-entrant (the reference is single threaded too).
+ * crosses the ABI.  An engine works on one device with its own CUDA streams (one
+ * main stream; the exchange path adds a copy stream and group streams that every
+ * other call waits for); calls on one engine are not re-entrant (the reference is
+ * single threaded too).
  *
  * Reference interfaces replaced (file:line inside dredremontes/wholeCellFE,
  * variant directory wholeCellFE_kMD unless stated):
