@@ -94,6 +94,54 @@ def test_boundary_candidates_reproduce_reference_scan(n):
         assert t["cptr"][t["rank"][v] + 1] - t["cptr"][t["rank"][v]] == cto[v]
 
 
+def _annulus(n, r_hole, seed):
+    """A disk mesh with the triangles near the centre removed: two boundary loops."""
+    x, tri = synth.disk_mesh(n, seed=seed)
+    c = x[tri].mean(axis=1)
+    r = np.hypot(c[:, 0] - x[:, 0].mean(), c[:, 1] - x[:, 1].mean())
+    tri = tri[r > r_hole * np.hypot(x[:, 0] - x[:, 0].mean(), x[:, 1] - x[:, 1].mean()).max()]
+    used = np.unique(tri)
+    remap = -np.ones(len(x), np.int64)
+    remap[used] = np.arange(len(used))
+    return np.ascontiguousarray(x[used]), np.ascontiguousarray(remap[tri].astype(np.int32))
+
+
+@pytest.mark.parametrize("n", [400, 3000])
+def test_boundary_candidates_on_an_annulus(n):
+    """Two boundary loops (an inner hole): the candidates reproduce the reference's
+    neighbour scan (UL:1500-1531) on both loops."""
+    x, tri = _annulus(n, 0.35, seed=n + 1)
+    t = capi.debug_topology(tri, len(x))
+    m = O.OMesh(tri, len(x))
+    j1o, j2o, cto = O.bnd_table(m, x)
+    bnd = m.bnd
+    r = np.hypot(x[:, 0] - x[:, 0].mean(), x[:, 1] - x[:, 1].mean())
+    assert bnd[r < 0.5 * r.max()].any() and bnd[r > 0.9 * r.max()].any()   # both loops
+    assert t["nb"] == int(bnd.sum())
+    assert np.array_equal(t["rank"] >= 0, bnd.astype(bool))
+    for v in np.nonzero(bnd)[0]:
+        j1, j2 = _j1j2_from_candidates(x, t["rank"], t["cptr"], t["cand"], v)
+        assert (j1, j2) == (j1o[v], j2o[v])
+        assert t["cptr"][t["rank"][v] + 1] - t["cptr"][t["rank"][v]] == cto[v]
+
+
+def test_one_ring_limit_and_tiny_meshes():
+    """A vertex whose one-ring fills a patch exactly is accepted, one element more is
+    refused with a message; one- and two-triangle meshes are one patch."""
+    def fan(d):
+        return np.array([[0, 1 + i, 1 + (i + 1) % d] for i in range(d)], np.int32), d + 1
+    tri, n = fan(512)
+    t = capi.debug_topology(tri, n, emax=512)
+    assert t["np"] >= 1 and int(t["patch"][:, 3].max()) <= 512
+    tri, n = fan(513)
+    with pytest.raises(capi.WcfeError, match="one-ring"):
+        capi.debug_topology(tri, n, emax=512)
+    for tri, n in ((np.array([[0, 1, 2]], np.int32), 3), (np.array([[0, 1, 2], [0, 2, 3]], np.int32), 4)):
+        t = capi.debug_topology(tri, n, emax=512)
+        assert t["np"] == 1 and t["patch"][0].tolist() == [0, n, 0, len(tri)]
+        assert t["nb"] == n and sorted(t["rank"].tolist()) == list(range(n))
+
+
 def test_topology_matches_reference_mesh_structures(golden):
     g = golden
     n = len(g["x0"])
