@@ -94,23 +94,11 @@ def test_boundary_candidates_reproduce_reference_scan(n):
         assert t["cptr"][t["rank"][v] + 1] - t["cptr"][t["rank"][v]] == cto[v]
 
 
-def _annulus(n, r_hole, seed):
-    """A disk mesh with the triangles near the centre removed: two boundary loops."""
-    x, tri = synth.disk_mesh(n, seed=seed)
-    c = x[tri].mean(axis=1)
-    r = np.hypot(c[:, 0] - x[:, 0].mean(), c[:, 1] - x[:, 1].mean())
-    tri = tri[r > r_hole * np.hypot(x[:, 0] - x[:, 0].mean(), x[:, 1] - x[:, 1].mean()).max()]
-    used = np.unique(tri)
-    remap = -np.ones(len(x), np.int64)
-    remap[used] = np.arange(len(used))
-    return np.ascontiguousarray(x[used]), np.ascontiguousarray(remap[tri].astype(np.int32))
-
-
 @pytest.mark.parametrize("n", [400, 3000])
 def test_boundary_candidates_on_an_annulus(n):
     """Two boundary loops (an inner hole): the candidates reproduce the reference's
     neighbour scan (UL:1500-1531) on both loops."""
-    x, tri = _annulus(n, 0.35, seed=n + 1)
+    x, tri = synth.annulus_mesh(n, 0.35, seed=n + 1)
     t = capi.debug_topology(tri, len(x))
     m = O.OMesh(tri, len(x))
     j1o, j2o, cto = O.bnd_table(m, x)

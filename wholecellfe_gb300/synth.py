@@ -101,6 +101,19 @@ def disk_mesh(n_target: int, radius: float = 10.0, jitter: float = 0.02, seed: i
     return x, tri.astype(np.int32)
 
 
+def annulus_mesh(n_target: int, hole: float = 0.35, radius: float = 10.0, seed: int = 1):
+    """A disk mesh with the triangles whose centroid lies within hole * radius of the
+    centre removed, unused vertices dropped (vertex order kept): a mesh with two
+    boundary loops.  Returns (x[n,3] float64, tri[t,3] int32)."""
+    x, tri = disk_mesh(n_target, radius=radius, seed=seed)
+    c = x[tri].mean(axis=1)
+    tri = tri[np.hypot(c[:, 0], c[:, 1]) > hole * radius]
+    used = np.unique(tri)
+    remap = -np.ones(len(x), np.int64)
+    remap[used] = np.arange(len(used))
+    return np.ascontiguousarray(x[used]), np.ascontiguousarray(remap[tri].astype(np.int32))
+
+
 def square_substrate(half: float = 50.0, cells: int = 24):
     """Structured square mesh [-half, half]^2 with alternating diagonals (CCW)."""
     m = cells + 1
