@@ -30,6 +30,23 @@ def test_library_exports_every_declared_symbol():
     assert set(names) <= set(capi.SIGNATURES), set(names) - set(capi.SIGNATURES)
 
 
+@pytest.mark.parametrize("lang,std", [("c", "c99"), ("c++", "c++11")])
+def test_header_is_plain_c(tmp_path, lang, std):
+    """include/wcfe.h compiles on its own as strict C99 and C++11 (the ABI a cgo, JNI or
+    ctypes binding includes), warnings as errors."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / "use_header.c"
+    src.write_text('#include "wcfe.h"\nint main(void) { wcfe_params p; (void)p; return WCFE_OK; }\n')
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include")
+    r = subprocess.run([cc, "-x", lang, f"-std={std}", "-Wall", "-Wextra", "-Werror", "-pedantic", "-I", inc, "-c",
+                        str(src), "-o", str(tmp_path / "use_header.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
 def test_engine_without_device_fails_cleanly():
     import torch
     if torch.cuda.is_available():
