@@ -367,10 +367,7 @@ def run_ours(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_s * 1e3 / args.steps, 4),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (assembly, forces) + float-float (state, accumulation)",
             "data": "synthetic: seeded disk meshes, random-init state from rest",
-            "config": {"workload": f"{len(cells)} uneven cells per GPU, vertices log-uniform [500, 20000], "
-                                   "integrins 0.4 x vertices, stiffness {linear 1, linear 31, poly 31 pN/nm x0 5 nm}, "
-                                   "flat rigid substrate, dt 5e-5 s, explicit step A1-A9",
-                       "cells": len(cells), "vertices": nv_total, "triangles": nt_total,
+            "config": {**workload_config(cells),
                        "l2": f"state {nv_total * 600 / 1e9:.2f} GB resident > 129 MB L2 (inputs larger than L2)",
                        "patch_threads": thr, "patch_elems": emax, "autotuned": True,
                        "parallelism": f"cell shards x{world} (population {len(specs)} cells, LPT by vertex count, "
@@ -635,6 +632,15 @@ def run_phase(args):
     eng.close()
 
 
+def workload_config(cells):
+    """The workload keys of `config`, shared by both arms (the same seeded population)."""
+    return {"workload": f"{len(cells)} uneven cells per GPU, vertices log-uniform [500, 20000], "
+                        "integrins 0.4 x vertices, stiffness {linear 1, linear 31, poly 31 pN/nm x0 5 nm}, "
+                        "flat rigid substrate, dt 5e-5 s, explicit step A1-A9",
+            "cells": len(cells), "vertices": int(sum(len(c["x0"]) for c in cells)),
+            "triangles": int(sum(len(c["tri"]) for c in cells))}
+
+
 def run_reference(args):
     """The reference's CPU implementation of the step (the oracle port; the reference's own
     sources are not on this machine) on all host cores, bounded sample of the workload."""
@@ -666,7 +672,7 @@ def run_reference(args):
     out = {"metric": METRIC, "value": round(value, 1), "unit": "cell-steps/s", "n_gpus": 0, "steps": steps,
            "warmup": args.warmup, "ms_per_step": round(tot / steps * 1e3, 3), "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
-           "config": {"workload": "same 256-cell workload, CPU sample", "cells_sampled": len(sample)},
+           "config": {**workload_config(cells), "cells_sampled": len(sample)},
            "impl": "reference", "cpu_baseline": cpu,
            "e2e": {"value": round(value, 1), "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "p50_ms_per_step": round(percentile(times, 0.5) * 1e3, 3),
