@@ -74,6 +74,12 @@ def test_philox_and_ap_stream_match_oracle():
     o = (C.c_uint32 * 4)()
     L.wcfe_philox4x32_10(c, k, o)
     assert tuple(o) == (0x6627e8d5, 0xe169c58d, 0xbc57ac4c, 0x9b00dbd8)
+    # the other published Philox4x32-10 known-answer vectors (Salmon et al., SC'11; Random123)
+    for ctr, key, want in [((0xffffffff,) * 4, (0xffffffff,) * 2, (0x408f276d, 0x41c83b0e, 0xa20bc7c6, 0x6d5451fd)),
+                           ((0x243f6a88, 0x85a308d3, 0x13198a2e, 0x03707344), (0xa4093822, 0x299f31d0),
+                            (0xd16cfe09, 0x94fdcceb, 0x5001e420, 0x24126ea1))]:
+        L.wcfe_philox4x32_10((C.c_uint32 * 4)(*ctr), (C.c_uint32 * 2)(*key), o)
+        assert tuple(o) == want
     rng = np.random.default_rng(3)
     for _ in range(200):
         s, st, call, kk = (int(rng.integers(0, 2**32)), int(rng.integers(0, 2**32)), int(rng.integers(0, 2**40)),
