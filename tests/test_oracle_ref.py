@@ -59,3 +59,31 @@ def test_oracle_matches_reference_build_on_an_annulus(variant):
     for a, b, s0 in zip(c.state(), s_ref, st):
         assert relerr(a - s0, b - s0) <= 1e-12
     assert c.t == t_ref and c.ap_call == c_ref
+
+
+@pytest.mark.parametrize("variant", ["kMD", "k1", "k31"])
+@pytest.mark.parametrize("t0,dt", [(1.99940, 5e-5), (1.996, 2e-4)])
+def test_oracle_matches_reference_across_the_active_stress_switch(variant, t0, dt):
+    """Runs that cross t = 2 s, where the active stress stops ramping and holds
+    (UL:744-757), at two time steps."""
+    if not O.ref_available(variant):
+        pytest.skip("reference not built here (oracle/build_ref.sh)")
+    R = O.Ref(variant)
+    p = default_params(variant)
+    x0, tri = synth.disk_mesh(400, seed=29)
+    n = len(x0)
+    hc = R.mesh(tri, n)
+    ptr, idx, bnd = R.mesh_map(hc, n, len(tri))
+    m = O.OMesh(tri, n, ptr, idx, bnd)
+    Xs, tri_s = synth.square_substrate(40.0, 16)
+    hs = R.mesh(tri_s, len(Xs))
+    ms = O.OMesh(tri_s, len(Xs))
+    st = synth.initial_state(x0, perturb=1.0, seed=7)
+    nsteps = 25
+    assert t0 < 2.0 < t0 + nsteps * dt
+    s_ref, t_ref, c_ref = R.steps(hc, st, hs, Xs, kint_for(variant), dt, nsteps, t0, p.seed, p.stream, 0)
+    c = O.OCell(m, st, p, t=t0, ap_call=0, sub=ms, Xs=Xs)
+    c.steps(nsteps, dt)
+    for a, b, s0 in zip(c.state(), s_ref, st):
+        assert relerr(a - s0, b - s0) <= 1e-12
+    assert c.t == t_ref and c.ap_call == c_ref
