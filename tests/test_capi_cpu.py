@@ -30,6 +30,47 @@ def test_library_exports_every_declared_symbol():
     assert set(names) <= set(capi.SIGNATURES), set(names) - set(capi.SIGNATURES)
 
 
+_C_KIND = {"int32_t": "i32", "int": "i32", "uint32_t": "u32", "int64_t": "i64", "uint64_t": "u64", "double": "f64",
+           "float": "f32", "uint16_t": "u16", "size_t": "u64", "uint8_t": "u8", "void": "void"}
+_PY_KIND = {C.c_int32: "i32", C.c_int: "i32", C.c_uint32: "u32", C.c_int64: "i64", C.c_uint64: "u64",
+            C.c_longlong: "i64", C.c_ulonglong: "u64", C.c_double: "f64", C.c_float: "f32", C.c_uint16: "u16",
+            C.c_size_t: "u64", C.c_uint8: "u8", None: "void"}
+
+
+def _c_kind(decl):
+    decl = re.sub(r"\bconst\b", "", decl).strip()
+    if "*" in decl or "[" in decl:
+        return "ptr"
+    words = decl.split()
+    return _C_KIND.get(words[0] if len(words) else "", "?" + decl)
+
+
+def _py_kind(ct):
+    if ct in (C.c_void_p, C.c_char_p) or (isinstance(ct, type) and issubclass(ct, C._Pointer)):
+        return "ptr"
+    return _PY_KIND.get(ct, "?" + str(ct))
+
+
+def test_bindings_match_the_header_prototypes():
+    """Each ctypes signature in capi.py has the prototype's parameter count, and per
+    parameter and for the result the same kind (pointer, or the scalar's width and type)."""
+    src = open(os.path.join(ROOT, "include", "wcfe.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    src = re.sub(r"#[^\n]*", "", src)
+    protos = re.findall(r"([A-Za-z_][A-Za-z0-9_ \t\*]*?)\s*\b(wcfe_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", src)
+    assert len(protos) >= 60
+    bad = []
+    for ret, name, args in protos:
+        args = args.strip()
+        want = [] if args in ("", "void") else [_c_kind(a) for a in args.split(",")]
+        rt, at = capi.SIGNATURES[name]
+        got = [_py_kind(a) for a in at]
+        ret_c = "ptr" if "*" in ret else _C_KIND.get(ret.split()[-1], "?" + ret)
+        if want != got or ret_c != _py_kind(rt):
+            bad.append((name, ret_c, want, _py_kind(rt), got))
+    assert not bad, bad
+
+
 @pytest.mark.parametrize("lang,std", [("c", "c99"), ("c++", "c++11")])
 def test_header_is_plain_c(tmp_path, lang, std):
     """include/wcfe.h compiles on its own as strict C99 and C++11 (the ABI a cgo, JNI or
