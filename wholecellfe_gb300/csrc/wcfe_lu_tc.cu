@@ -294,7 +294,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
     }
     tc_fence_before();
     __syncthreads();
-    // neither CTA leaves while its peer may still multicast into it or arrive on its barriers
+    // neither CTA leaves while its peer may still multicast into it or arrive on its barriers:
+    // each producer's drain above has seen the last fill of every stage land in its own
+    // shared memory, peer bytes included.  After a timed-out wait (the cell already flagged
+    // as failed) one CTA may have stopped issuing while the other did not, and the drain
+    // then covers only the fills this CTA waited for.
     if (CL > 1) cluster_sync();
     if (warp == 1) {
         tc_fence_after();
