@@ -666,8 +666,8 @@ WO_API void wo_force_fa_subs(const wo_mesh* ms, const double* Xs, const double* 
                              const double* xcell, const double* fau, const wo_mesh* mc, const wcfe_params* p,
                              const double* rho_w, double* F) {
     /* Xs mirrors the reference's X_t argument: its containment test on X_t is commented out
-       (UL:1332-1337) and the anchors are located with the current positions x_t; the one
-       use of X_t, subs_u (UL:1353), does not reach the force */
+       (UL:1333-1334, 1339) and the anchors are located with the current positions x_t; the one
+       use of X_t, subs_u (UL:1354), does not reach the force */
     (void)Xs;
     memset(F, 0, sizeof(double) * 3 * ms->nv);
     for (int v = 0; v < mc->nv; ++v) {
