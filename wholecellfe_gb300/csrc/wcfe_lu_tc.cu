@@ -12,8 +12,9 @@
 // Persistent CTAs, one per SM, walk a flat list of TM x 128 tiles over all cells (the
 // host gives the per-cell tile counts as a prefix sum); TM = 256 rows for the updates
 // with K >= 512, whose operand reads from L2 bound them (a 256-row tile reads a quarter
-// fewer operand bytes per flop), 128 for the narrower strips.  Warp 0 streams the operand
-// boxes with TMA into a 4-stage ring (K = 32 per stage, 128-byte swizzled); one thread of
+// fewer operand bytes per flop), 128 for the narrower strips.  Every CTA loads all of its
+// own operands (no cluster sharing), so no CTA waits on another.  Warp 0 streams the
+// operand boxes with TMA into a 4-stage ring (K = 32 per stage, 128-byte swizzled); one thread of
 // warp 1 issues the MMAs into two TMEM accumulators, so tile t + 1 multiplies while tile t
 // is written back; 16 epilogue warps, four per TMEM lane quadrant (TM / 4 rows of C each,
 // in slices of 32), prefetch each slice's C values before its product is needed, then
@@ -62,9 +63,9 @@ __device__ __forceinline__ void region_of(const LuUpdateArgs& a, int r, int m, i
     chi = a.chi[r] < 0 ? m : min(a.chi[r], m);
 }
 
-// flat unit f -> cell, unit origin; groups are (cell, region) pairs in cell-major order;
-// units of TM rows x TW columns (TW = 128, or 256 for a cluster pair's two tiles)
-template <int TM = kTile, int TW = kTile>
+// flat tile f -> cell, tile origin; groups are (cell, region) pairs in cell-major order;
+// tiles of TM rows x 128 columns
+template <int TM = kTile>
 __device__ __forceinline__ Tile decode_tile(const NewtonCell* nc, const int* __restrict__ prefix, int ngroups, const LuUpdateArgs& a,
                             int f) {
     int lo = 0, hi = ngroups;   // prefix[lo] <= f < prefix[hi]; empty groups are skipped
@@ -80,27 +81,19 @@ __device__ __forceinline__ Tile decode_tile(const NewtonCell* nc, const int* __r
     const int m = 2 * nc[t.slot].n;
     int rlo, rhi, clo, chi;
     region_of(a, reg, m, rlo, rhi, clo, chi);
-    const int tiles_n = (chi - clo + TW - 1) / TW;
+    const int tiles_n = (chi - clo + kTile - 1) / kTile;
     const int local = f - __ldg(prefix + lo);
     t.tm = rlo + (local / tiles_n) * TM;
-    t.tn = clo + (local % tiles_n) * TW;
+    t.tn = clo + (local % tiles_n) * kTile;
     t.rhi = rhi;
     t.chi = chi;
     return t;
 }
 
-// CL = 2: clusters of two CTAs on the two 128-column halves of a 256 x 256 unit.  Both
-// need the unit's 256 L rows: each CTA loads one 128-row L box per stage and multicasts
-// it to both, so a CTA reads 32 KB of operands per stage instead of 48.  A stage is
-// refilled only when both CTAs' MMAs have read it (each commit arrives on both CTAs'
-// `empty`); the CTAs of a cluster walk the same units in the same order.
-template <int TM, int CL>
+template <int TM>
 __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, const LuMaps* __restrict__ maps,
                                                              const int* __restrict__ prefix, int ngroups,
                                                              LuUpdateArgs a) {
-    static_assert(CL == 1 || (CL == 2 && TM == 256), "cluster pairs share 256-row units");
-    constexpr int TW = 128 * CL;                        // columns of a unit
-    constexpr uint16_t kPair = 0x3;
     constexpr int NH = TM / 128;                        // 32-row slices of C per epilogue warp
     constexpr uint32_t kSB = stage_bytes<TM>();
     constexpr uint32_t kCols = 2 * TM;                  // two TM-column fp32 accumulators
@@ -117,12 +110,11 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int total = __ldg(prefix + ngroups);   // units
     const int nch = a.K / kBK;
-    const int crank = CL > 1 ? (int)cluster_ctarank() : 0;
-    const int unit0 = blockIdx.x / CL, nunits = gridDim.x / CL;
+    const int unit0 = blockIdx.x, nunits = gridDim.x;
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
             mbar_init(full + s, 1);
-            mbar_init(empty + s, CL);
+            mbar_init(empty + s, 1);
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(tfull + b, 1);
@@ -138,7 +130,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
     }
     tc_fence_before();
     __syncthreads();
-    if (CL > 1) cluster_sync();   // the peer's barriers exist before any multicast reaches them
     tc_fence_after();
     const uint32_t tbase = *tbase_s;
 
@@ -147,8 +138,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
         if (lane == 0) {
             int g = 0;   // chunks issued so far
             for (int f = unit0; f < total && !*abort_s; f += nunits) {
-                Tile t = decode_tile<TM, TW>(nc, prefix, ngroups, a, f);
-                t.tn += 128 * crank;
+                const Tile t = decode_tile<TM>(nc, prefix, ngroups, a, f);
                 const LuMaps* mp = maps + t.slot;
                 tmap_acquire(&mp->umap);
                 tmap_acquire(&mp->jmap);
@@ -163,14 +153,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
                     uint8_t* st = sm + s * kSB;
                     mbar_arrive_expect_tx(full + s, kSB);
                     tma_load_2d(st, &mp->umap, a.kb + c * kBK, t.tn, full + s);
-                    if (CL == 1) {
 #pragma unroll
-                        for (int j = 0; j < NH; ++j)   // rows past the matrix read as zeros
-                            tma_load_2d(st + (1 + j) * kBoxBytes, &mp->jmap, a.ka + c * kBK, t.tm + 128 * j, full + s);
-                    } else {
-                        tma_load_2d_mc(st + (1 + crank) * kBoxBytes, &mp->jmap, a.ka + c * kBK, t.tm + 128 * crank,
-                                       full + s, kPair);
-                    }
+                    for (int j = 0; j < NH; ++j)   // rows past the matrix read as zeros
+                        tma_load_2d(st + (1 + j) * kBoxBytes, &mp->jmap, a.ka + c * kBK, t.tm + 128 * j, full + s);
                 }
             }
             // every stage's last fill has landed before the CTA may exit
@@ -208,9 +193,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
 #pragma unroll
                     for (int k = 0; k < kBK / 8; ++k)
                         tc_mma_tf32(d, da + 2u * (uint32_t)k, db + 2u * (uint32_t)k, idesc, (uint32_t)(c | k));
-                    // the stage is free once these MMAs (and the peer's) have read it
-                    if (CL == 1) tc_commit(empty + s);
-                    else tc_commit_mc(empty + s, kPair);
+                    tc_commit(empty + s);   // the stage is free once these MMAs have read it
                 }
                 if (!ok) {
                     *abort_s = 1;
@@ -242,8 +225,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
             Cb = nc[t.slot].J + (size_t)r0 * ld + col;
         };
         auto locate = [&](int ff) {
-            t = decode_tile<TM, TW>(nc, prefix, ngroups, a, ff);
-            t.tn += 128 * crank;
+            t = decode_tile<TM>(nc, prefix, ngroups, a, ff);
             ld = nc[t.slot].ld;
             slice(0);
         };
@@ -294,12 +276,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_update_tc(NewtonCell* nc, co
     }
     tc_fence_before();
     __syncthreads();
-    // neither CTA leaves while its peer may still multicast into it or arrive on its barriers:
-    // each producer's drain above has seen the last fill of every stage land in its own
-    // shared memory, peer bytes included.  After a timed-out wait (the cell already flagged
-    // as failed) one CTA may have stopped issuing while the other did not, and the drain
-    // then covers only the fills this CTA waited for.
-    if (CL > 1) cluster_sync();
     if (warp == 1) {
         tc_fence_after();
         tc_dealloc(tbase, kCols);
@@ -504,7 +480,6 @@ __global__ void __launch_bounds__(kThreads, 1) k_lu_panels_tc(NewtonCell* nc, co
 
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 int g_sms = 0;
-int g_lu_pairs = 0;   // resident clusters of the paired 256-row update kernel (0: pairs unused)
 int g_lu_tc_regs = 0, g_lu_tc_max_threads = 0;
 
 int encode_f32_2d(CUtensorMap* map, const float* base, uint64_t cols, uint64_t rows, uint64_t row_bytes,
@@ -532,43 +507,20 @@ cudaError_t configure_lu_tc(int num_sms) {
         if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorSymbolNotFound;
         g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
     }
-    cudaError_t e = cudaFuncSetAttribute((const void*)k_lu_update_tc<128, 1>,
+    cudaError_t e = cudaFuncSetAttribute((const void*)k_lu_update_tc<128>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)update_smem<128>());
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute((const void*)k_lu_update_tc<256, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    e = cudaFuncSetAttribute((const void*)k_lu_update_tc<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)update_smem<256>());
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute((const void*)k_lu_update_tc<256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)update_smem<256>());
-    if (e != cudaSuccess) return e;
-    // how many CTA pairs can be resident at once (the persistent grid); 0 disables pairs
-    {
-        cudaLaunchConfig_t cfg{};
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = 2;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.gridDim = dim3(2 * (unsigned)std::max(1, num_sms / 2));
-        cfg.blockDim = dim3(kThreads);
-        cfg.dynamicSmemBytes = update_smem<256>();
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        int n = 0;
-        if (cudaOccupancyMaxActiveClusters(&n, (const void*)k_lu_update_tc<256, 2>, &cfg) != cudaSuccess) {
-            cudaGetLastError();
-            n = 0;
-        }
-        g_lu_pairs = n;
-    }
     e = cudaFuncSetAttribute((const void*)k_lu_panels_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)kPSmemBytes);
     if (e != cudaSuccess) return e;
     cudaFuncAttributes at;
-    if ((e = cudaFuncGetAttributes(&at, (const void*)k_lu_update_tc<128, 1>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&at, (const void*)k_lu_update_tc<128>)) != cudaSuccess) return e;
     g_lu_tc_regs = at.numRegs;
     g_lu_tc_max_threads = at.maxThreadsPerBlock;
-    if ((e = cudaFuncGetAttributes(&at, (const void*)k_lu_update_tc<256, 2>)) != cudaSuccess) return e;
+    if ((e = cudaFuncGetAttributes(&at, (const void*)k_lu_update_tc<256>)) != cudaSuccess) return e;
     g_lu_tc_regs = std::max(g_lu_tc_regs, at.numRegs);
     g_lu_tc_max_threads = std::min(g_lu_tc_max_threads, at.maxThreadsPerBlock);
     return cudaSuccess;
@@ -605,11 +557,9 @@ int encode_lu_maps(const NewtonCell* h, int nslots, LuMaps* out) {
 // rows of an update tile: 256 for the updates with K >= 512, else 128 (the kernel
 // instantiation and the host's tile counts both follow this)
 int lu_tile_rows(const LuUpdateArgs& a) { return a.K >= 512 ? 256 : kTile; }
-// columns of a work unit: two 128-column tiles when 256-row tiles run as cluster pairs
-int lu_unit_cols(const LuUpdateArgs& a) { return (lu_tile_rows(a) == 256 && g_lu_pairs > 0) ? 256 : kTile; }
 
 int lu_update_prefix(const NewtonCell* h, int nslots, const LuUpdateArgs& a, int* pref) {
-    const int tm = lu_tile_rows(a), tw = lu_unit_cols(a);
+    const int tm = lu_tile_rows(a), tw = kTile;
     int acc = 0;
     for (int s = 0; s < nslots; ++s)
         for (int r = 0; r < a.nreg; ++r) {
@@ -628,29 +578,11 @@ bool launch_lu_update_tc(NewtonCell* nc, const LuMaps* maps, const int* d_prefix
                          const LuUpdateArgs& a, cudaStream_t st) {
     if (g_lu_tc_max_threads < kThreads) return false;
     if (total <= 0) return true;
-    if (lu_unit_cols(a) == 256) {   // cluster pairs: total counts 256 x 256 units
-        const int clusters = std::max(1, std::min(total, g_lu_pairs));
-        cudaLaunchConfig_t cfg{};
-        cudaLaunchAttribute at[1];
-        at[0].id = cudaLaunchAttributeClusterDimension;
-        at[0].val.clusterDim.x = 2;
-        at[0].val.clusterDim.y = 1;
-        at[0].val.clusterDim.z = 1;
-        cfg.gridDim = dim3(2 * (unsigned)clusters);
-        cfg.blockDim = dim3(kThreads);
-        cfg.dynamicSmemBytes = update_smem<256>();
-        cfg.stream = st;
-        cfg.attrs = at;
-        cfg.numAttrs = 1;
-        if (cudaLaunchKernelEx(&cfg, k_lu_update_tc<256, 2>, nc, maps, d_prefix, nslots * a.nreg, a) != cudaSuccess)
-            return false;
-        return cudaGetLastError() == cudaSuccess;
-    }
     const int grid = std::max(1, std::min(total, g_sms > 0 ? g_sms : 1));
     if (lu_tile_rows(a) == 256)
-        k_lu_update_tc<256, 1><<<grid, kThreads, update_smem<256>(), st>>>(nc, maps, d_prefix, nslots * a.nreg, a);
+        k_lu_update_tc<256><<<grid, kThreads, update_smem<256>(), st>>>(nc, maps, d_prefix, nslots * a.nreg, a);
     else
-        k_lu_update_tc<128, 1><<<grid, kThreads, update_smem<128>(), st>>>(nc, maps, d_prefix, nslots * a.nreg, a);
+        k_lu_update_tc<128><<<grid, kThreads, update_smem<128>(), st>>>(nc, maps, d_prefix, nslots * a.nreg, a);
     return cudaGetLastError() == cudaSuccess;
 }
 

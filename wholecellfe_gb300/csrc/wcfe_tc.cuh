@@ -105,34 +105,6 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, int x, 
         "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(bar))
         : "memory");
 }
-// the same box written to the same shared-memory offset of every CTA in `mask` (this
-// cluster's ranks), each CTA's mbarrier at `bar`'s offset receiving the bytes it got
-__device__ __forceinline__ void tma_load_2d_mc(void* dst, const void* tmap, int x, int y, uint64_t* bar,
-                                               uint16_t mask) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster "
-        "[%0], [%1, {%2, %3}], [%4], %5;" ::"r"(smem_addr(dst)),
-        "l"(tmap), "r"(x), "r"(y), "r"(smem_addr(bar)), "h"(mask)
-        : "memory");
-}
-// one arrival on the mbarrier at `bar`'s offset in every CTA of `mask`, once every tcgen05
-// operation this thread issued before has completed
-__device__ __forceinline__ void tc_commit_mc(uint64_t* bar, uint16_t mask) {
-    asm volatile(
-        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-            smem_addr(bar)),
-        "h"(mask)
-        : "memory");
-}
-__device__ __forceinline__ uint32_t cluster_ctarank() {
-    uint32_t r;
-    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-    return r;
-}
-// every thread of every CTA of the cluster
-__device__ __forceinline__ void cluster_sync() {
-    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
 // make tensor-map contents written through the generic proxy (host copies) visible to TMA
 __device__ __forceinline__ void tmap_acquire(const void* tmap) {
     asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tmap) : "memory");
