@@ -31,3 +31,30 @@ def golden(request):
     d = {k: g[k] for k in g.files}
     d["variant"] = request.param
     return d
+
+
+SHIPPED_MESHES = ("disk_20um_diam_edited", "disk_20um_diam_N1025", "disk_20um_diam_N2944")
+SHIPPED_STATE = ("x", "V", "A", "ea", "cA", "cC", "fau")
+SHIPPED_FINAL = ("x", "V", "ea", "cC", "fau")
+
+
+@pytest.fixture(scope="session", params=VARIANTS)
+def shipped(request):
+    """Trajectories of the reference's own step loop on its shipped meshes
+    (tests/golden/make_golden.py, make_shipped)."""
+    g = np.load(os.path.join(GOLDEN, f"shipped_{request.param}.npz"))
+    d = {k: g[k] for k in g.files}
+    d["variant"] = request.param
+    return d
+
+
+def shipped_runs(g):
+    """(mesh index, run kind, start state, start time, start AP call, steps) of a shipped fixture."""
+    from wholecellfe_gb300 import synth
+    runs = []
+    for m in range(len(SHIPPED_MESHES)):
+        st = tuple(g[f"m{m}_mov0_{k}"] for k in SHIPPED_STATE)
+        runs.append((m, "mov", st, 0.7, 7, 20))
+        if f"m{m}_rest_x" in g:
+            runs.append((m, "rest", synth.initial_state(g[f"m{m}_x0"]), 0.0, 0, 200))
+    return runs

@@ -1,8 +1,9 @@
 """Generate the golden fixtures from the reference itself.
 
 Runs the reference's own functions, compiled from its sources by
-oracle/build_ref.sh into oracle/_ref/, on seeded synthetic inputs.  It stores
-their inputs and outputs as tests/golden/golden_<variant>.npz.  The reference
+oracle/build_ref.sh into oracle/_ref/, on seeded synthetic inputs and on the
+reference's own shipped meshes.  It stores their inputs and outputs as
+tests/golden/golden_<variant>.npz and tests/golden/shipped_<variant>.npz.  The reference
 ships no tests, expected outputs or golden vectors, so these fixtures are the
 parity anchor.  The oracle must reproduce them (tests/test_oracle_golden.py)
 on any machine, including ones without the reference sources.
@@ -106,7 +107,78 @@ def vtk_name(variant, fmt, kint):
     return f"{variant}_f{fmt}" + ("_kint%g" % kint if kint >= 0 else "") + ".vtk"
 
 
+# The reference's own meshes (cellBP/scripts, read as read_ecomsol reads them,
+# cellBP/iomesh.cpp:491-565): three COMSOL-edited disks of 20 um diameter and the 100 um
+# square substrate, used as the rigid substrate of every run below.
+SHIPPED = ("disk_20um_diam_edited", "disk_20um_diam_N1025", "disk_20um_diam_N2944")
+SHIPPED_SUBSTRATE = "sq_subs_100um"
+SHIPPED_MOVING_STEPS = 20     # from a seeded moving, pre-strained state (all variants)
+SHIPPED_REST_STEPS = 200      # from the reference start state (k1, k31; kMD from rest is noise-driven)
+SHIPPED_SEED = 21
+FINAL = ("x", "V", "ea", "cC", "fau")   # the end-state arrays stored
+
+
+def read_comsol(path):
+    """Vertices and triangles of a COMSOL text mesh as read_ecomsol reads it: the count on
+    the line after the line holding "Nodes", that many coordinate lines (x y, z forced to 0);
+    the count after "Elements", that many lines of three 0-based vertex indices."""
+    lines = open(path).read().splitlines()
+    x, tri = None, None
+    for i, line in enumerate(lines):
+        if "Nodes" in line:
+            n = int(lines[i + 1].split()[0])
+            x = np.zeros((n, 3))
+            for k in range(n):
+                f = lines[i + 2 + k].split()
+                x[k, 0], x[k, 1] = float(f[0]), float(f[1])
+        elif "Elements" in line:
+            n = int(lines[i + 1].split()[0])
+            tri = np.array([[int(v) for v in lines[i + 2 + k].split()[:3]] for k in range(n)], dtype=np.int32)
+    return x, tri
+
+
+def make_shipped(variant: str, ref_root: str) -> dict:
+    """Trajectories of the reference's own step loop on its shipped meshes: for each mesh,
+    SHIPPED_MOVING_STEPS steps from a seeded moving state and (k1, k31) SHIPPED_REST_STEPS
+    steps from rest, over the shipped substrate held rigid."""
+    R = O.Ref(variant)
+    p = default_params(variant)
+    d = os.path.join(ref_root, "wholeCellFE_kMD", "cellBP", "scripts")
+    Xs, tri_s = read_comsol(os.path.join(d, SHIPPED_SUBSTRATE + ".txt"))
+    hs = R.mesh(tri_s, len(Xs))
+    g: dict = dict(Xs=Xs, tri_s=tri_s, dt=DT, seed=p.seed, stream=p.stream)
+    keep = ("x", "V", "A", "ea", "cA", "cC", "fau")
+    for m, name in enumerate(SHIPPED):
+        x0, tri = read_comsol(os.path.join(d, name + ".txt"))
+        hc = R.mesh(tri, len(x0))
+        g[f"m{m}_x0"], g[f"m{m}_tri"] = x0, tri
+        st = synth.initial_state(x0, perturb=1.0, seed=SHIPPED_SEED + m)
+        for k, a in zip(keep, st):
+            g[f"m{m}_mov0_{k}"] = a
+        s, t, c = R.steps(hc, st, hs, Xs, kint_for(variant), DT, SHIPPED_MOVING_STEPS, T_TOT, p.seed, p.stream, AP_CALL)
+        for k, a in zip(keep, s):
+            if k in FINAL:
+                g[f"m{m}_mov_{k}"] = a
+        g[f"m{m}_mov_t"], g[f"m{m}_mov_call"] = t, c
+        if variant != "kMD":
+            s, t, c = R.steps(hc, synth.initial_state(x0), hs, Xs, kint_for(variant), DT, SHIPPED_REST_STEPS, 0.0,
+                              p.seed, p.stream, 0)
+            for k, a in zip(keep, s):
+                if k in FINAL:
+                    g[f"m{m}_rest_{k}"] = a
+            g[f"m{m}_rest_t"], g[f"m{m}_rest_call"] = t, c
+    return g
+
+
 def main():
+    ref_root = os.environ.get("WCFE_REF", "/root/reference")
+    for variant in ("kMD", "k1", "k31"):
+        if not O.ref_available(variant):
+            sys.exit("oracle/_ref not built: run oracle/build_ref.sh first")
+        g = make_shipped(variant, ref_root)
+        path = os.path.join(HERE, f"shipped_{variant}.npz")
+        np.savez_compressed(path, **g)
+        print("wrote", path, os.path.getsize(path), "bytes")
     for variant in ("kMD", "k1", "k31"):
         if not O.ref_available(variant):
             sys.exit("oracle/_ref not built: run oracle/build_ref.sh first")

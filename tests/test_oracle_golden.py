@@ -139,3 +139,21 @@ def test_oracle_per_element_mu_uniform_equals_params_mu():
     b.steps(5, 5e-5)
     for u, w in zip(a.state(), b.state()):
         assert np.array_equal(u, w)
+
+
+def test_shipped_meshes(shipped):
+    """The oracle's step on the reference's own meshes and substrate (cellBP/scripts),
+    against the reference's step loop: 20 steps from a moving state, 200 from rest."""
+    from conftest import SHIPPED_FINAL, SHIPPED_STATE, shipped_runs
+    g = shipped
+    p = default_params(g["variant"])
+    ms = O.OMesh(g["tri_s"], len(g["Xs"]))
+    for m, kind, st, t0, c0, n in shipped_runs(g):
+        mesh = O.OMesh(g[f"m{m}_tri"], len(g[f"m{m}_x0"]))
+        c = O.OCell(mesh, st, p, t=t0, ap_call=c0, sub=ms, Xs=g["Xs"])
+        c.steps(n, float(g["dt"]))
+        out = dict(zip(SHIPPED_STATE, c.state()))
+        s0 = dict(zip(SHIPPED_STATE, st))
+        for k in SHIPPED_FINAL:
+            assert relerr(out[k] - s0[k], g[f"m{m}_{kind}_{k}"] - s0[k]) <= 1e-12, (m, kind, k)
+        assert c.t == float(g[f"m{m}_{kind}_t"]) and c.ap_call == int(g[f"m{m}_{kind}_call"])
