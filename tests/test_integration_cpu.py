@@ -1,5 +1,5 @@
-"""The C++ shim of INTEGRATION.md compiles against the reference's headers and links with
-the reference's own declarations of the mechanics functions and libwcfe.so
+"""The cellBP drop-in (wholecellfe_gb300/shim) compiles against the reference's headers and
+links with the reference's own declarations of the mechanics functions and libwcfe.so
 (oracle/check_integration.sh).  Runs where the reference sources are available (the
 container that builds oracle/_ref); skipped elsewhere.  No GPU."""
 import os
