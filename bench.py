@@ -37,6 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "cell-steps/s batched+mixed vs plain FP64 on 1 GB300 at <=1e-6 rel err; p50/p99"
+ELEMENT_FLOPS = 2360   # FP64 flops of the reference's cell element (oracle/flop_count.cpp)
 DT = 5e-5
 N_CELLS = 256
 
@@ -96,7 +97,7 @@ def load_cells(eng, cells):
 
 # ----------------------------------------------------------------------------- clocks
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 100 ms while running."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms while running."""
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
@@ -109,7 +110,7 @@ class ClockSampler:
     def start(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                                          "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                                          "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
             return
@@ -174,6 +175,56 @@ def cpu_baseline(cells, steps: int, budget_s: float = 15.0):
                       f"vertices) x {nsteps} steps, oracle/wcfe_oracle.c on {nthreads} host threads, {dt:.1f} s"}
 
 
+def _ref_worker(job):
+    """One process of the reference-build baseline: the reference's own step loop
+    (oracle/_ref, cellBP/UL_growth_explicit.cpp compiled from its sources) on its cells."""
+    from oracle import oracle_py as O
+    from wholecellfe_gb300 import synth
+    from wholecellfe_gb300.params import kint_for
+    cells, nsteps = job
+    Xs = np.array([[-60.0, -60.0, 0.0], [60.0, -60.0, 0.0], [60.0, 60.0, 0.0], [-60.0, 60.0, 0.0]])
+    tri_s = np.array([[0, 1, 2], [0, 2, 3]], dtype=np.int32)   # a rigid plane under the cells
+    t0 = time.perf_counter()
+    done = 0
+    for c in cells:
+        variant = "k1" if c["model"] == 0 else "k31"
+        R = O.Ref(variant)
+        hc, hs = R.mesh(c["tri"], len(c["x0"])), R.mesh(tri_s, len(Xs))
+        R.steps(hc, synth.initial_state(c["x0"]), hs, Xs, kint_for(variant), DT, nsteps, 0.0, c["p"].seed,
+                c["p"].stream, 0)
+        done += nsteps
+    return done, time.perf_counter() - t0
+
+
+def ref_build_baseline(cells, steps: int, budget_s: float = 15.0, procs: int | None = None):
+    """The reference's own CPU path (oracle/_ref, built from the reference's sources) on a
+    bounded sample of the workload's linear-law cells (the reference has no polynomial
+    law), one process per core (its rand() stand-in is process-global).  None where
+    oracle/_ref is absent (it is built only where the reference sources are)."""
+    import multiprocessing as mp
+    from oracle import oracle_py as O
+    if not (O.ref_available("k1") and O.ref_available("k31")):
+        return None
+    procs = procs or (os.cpu_count() or 1)
+    lin = [c for c in cells if c["model"] in (0, 1)]
+    probe = min(lin, key=lambda c: abs(len(c["x0"]) - 5000))
+    done, sec = _ref_worker(([probe], 1))
+    per_vertex_step = sec / len(probe["x0"])
+    sample = lin[:max(procs, min(len(lin), 32))]
+    mean_nv = float(np.mean([len(c["x0"]) for c in sample]))
+    nsteps = max(1, min(steps, int(budget_s * procs / (per_vertex_step * mean_nv * len(sample)))))
+    jobs = [(sample[i::procs], nsteps) for i in range(procs) if sample[i::procs]]
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(len(jobs)) as pool:
+        res = pool.map(_ref_worker, jobs)
+    wall = time.perf_counter() - t0
+    return {"value": round(sum(r[0] for r in res) / wall, 1), "unit": "cell-steps/s", "cores": len(jobs),
+            "kind": "reference",
+            "sample": f"{len(sample)} linear-law cells of the workload (mean {mean_nv:.0f} vertices) x {nsteps} steps, "
+                      f"the reference's UL_growth_explicit.cpp built from its sources (oracle/_ref), {len(jobs)} "
+                      f"processes, {wall:.1f} s wall"}
+
+
 # ----------------------------------------------------------------------------- measurements
 def kernel_bytes_patch_mixed(nv_total: int, nt_total: int) -> float:
     """Algorithmic DRAM bytes of one mixed patch-phase launch (float-float state).
@@ -218,6 +269,26 @@ def timed_steps(eng, steps, dt, ranks_barrier=None):
     return dict(total_ms=span, wall_s=wall, per_step=per_step, ms_v=ms_v, ms_p=ms_p)
 
 
+def timed_graph_steps(eng, steps, dt, ranks_barrier=None):
+    """The same loop replayed from captured CUDA graphs (eight steps per graph), timed by
+    CUDA events recorded on the engine's own stream."""
+    import torch
+    eng.set_graphs(True)
+    eng.step(8, dt)   # capture and first replay
+    eng.sync()
+    st = torch.cuda.ExternalStream(eng.stream_ptr())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    if ranks_barrier:
+        ranks_barrier()
+    e0.record(st)
+    eng.step(steps, dt)
+    e1.record(st)
+    e1.synchronize()
+    eng.set_graphs(False)
+    return {"total_ms": e0.elapsed_time(e1)}
+
+
 def run_ours(args):
     import torch
     from wholecellfe_gb300 import capi
@@ -253,15 +324,20 @@ def run_ours(args):
     load_cells(eng, cells)
     eng.autotune(DT, 3)
     thr, emax = eng.shape()
+    kinds = eng.kernels()
+    # clocks over the whole measurement window (warm-up, the eager and graph-captured timed
+    # steps and the e2e steps): a timed region of a few ms is shorter than nvidia-smi's period
+    clocks = ClockSampler()
+    clocks.start()
     for _ in range(args.warmup):
         eng.step(1, DT)
     eng.sync()
     launches0 = eng.launches()
-    clocks = ClockSampler()
-    clocks.start()
     res = timed_steps(eng, args.steps, DT, barrier)
-    clocks_info = clocks.stop()
     launches = eng.launches() - launches0
+    graph = timed_graph_steps(eng, args.steps, DT, barrier)
+    graph_s = max_over_ranks(graph["total_ms"] / 1e3, dist, f"cuda:{local}")
+    graph_value = len(specs) * args.steps / graph_s
     t_s = max_over_ranks(res["total_ms"] / 1e3, dist, f"cuda:{local}")
     value = len(specs) * args.steps / t_s
     p50 = percentile(res["per_step"], 0.5)
@@ -294,32 +370,28 @@ def run_ours(args):
            "api": "wcfe_engine_predict + wcfe_engine_update (include/wcfe.h), pinned host buffers",
            "gpu_launches": int(e2e_launches)}
     log(f"[bench] e2e: {e2e['value']:.3e} cell-steps/s")
+    clocks_info = clocks.stop()
     eng.close()
 
     out = None
     if rank == 0:
-        # ---- error of the mixed form against the FP64 form (same workload, same steps) ----
-        err_steps = min(args.steps, 300)
-        finals = {}
-        for prec in (capi.PREC_MIXED, capi.PREC_FP64):
-            e = capi.Engine(prec, device=device)
-            hs = load_cells(e, cells)
-            e.step(err_steps, DT)
-            e.sync()
-            finals[prec] = [h.get_state()[0] for h in hs]
-            e.close()
-        errs = []
-        for c, xm, xd in zip(cells, finals[capi.PREC_MIXED], finals[capi.PREC_FP64]):
-            u = xd - c["x0"]
-            errs.append(float(np.max(np.abs(xm - xd)) / max(float(np.max(np.abs(u))), 1e-300)))
-        max_err = max(errs)
-        log(f"[bench] mixed vs FP64 relative displacement error after {err_steps} steps: max {max_err:.2e}")
+        # ---- error of the mixed form against the FP64 form (same workload), at the
+        # workload's own 300-step horizon and at 20 steps beside the FP64 form's own noise ----
+        accuracy = mixed_error(cells, device)
+        max_err = accuracy["gate"]["max_rel_displacement_error"]
+        err_steps = accuracy["gate"]["steps"]
+        log(f"[bench] mixed vs FP64: {json.dumps(accuracy)}")
 
-        # ---- plain one-cell FP64 form (config 1 size) ----
-        x0, tri = synth.disk_mesh(2000, seed=1)
-        p = default_params("k1")
+        # ---- the pipe rates of this GPU (roofline denominators the peak file does not hold) ----
+        rates = capi.pipe_rates()
+        log(f"[bench] pipe rates: {rates}")
+
+        # ---- plain one-cell FP64 form: the single-cell workload with a protruding edge (2,044
+        # vertices, E 1 kPa / nu 0.45, 0.1 um thick, 600 integrins 1 pN/nm rest 20 nm, 10 nm/step) ----
+        x0, tri, p, rho = synth.protruding_cell(dt=DT)
         ep = capi.Engine(capi.PREC_FP64, device=device)
         hp = ep.add_cell(x0, tri, p, state=synth.initial_state(x0))
+        hp.set_integrins(rho)
         ep.autotune(DT, 5)
         plain_shape = ep.shape()
         for _ in range(args.warmup):
@@ -328,6 +400,15 @@ def run_ours(args):
         pr = timed_steps(ep, plain_steps, DT)
         ep.close()
         plain_value = plain_steps / (pr["total_ms"] / 1e3)
+        # its FP64 work: the reference's element, 2,360 flops (oracle/flop_count.cpp), per triangle and step
+        plain_flops = ELEMENT_FLOPS * len(tri)
+        plain_achieved = plain_flops / (pr["total_ms"] / plain_steps * 1e-3) / 1e12
+        plain_roofline = {"bound": "fp64", "achieved": round(plain_achieved, 5), "peak": round(rates["fp64_tflops"], 4),
+                          "unit": "TFLOP/s", "frac": round(plain_achieved / rates["fp64_tflops"], 4),
+                          "peak_source": "measured FP64 FMA rate of this GPU (wcfe_debug_pipe_rates)",
+                          "note": "2,360 FP64 flops per element x 3,929 elements per step over the step's device "
+                                  "time; one 2,044-vertex cell is a few dozen CTAs per phase, less than one wave of the "
+                                  "152 SMs, so the form is latency-bound"}
         plain_wall = plain_steps / pr["wall_s"]
         log(f"[bench] plain FP64 one cell: {pr['total_ms'] / plain_steps * 1e3:.1f} us/step device, "
             f"{plain_value:.3e} cell-steps/s device, {plain_wall:.3e} wall")
@@ -355,13 +436,25 @@ def run_ours(args):
 
         config2 = run_config2()
         log(f"[bench] config 2: {config2}")
-        newton = run_newton(args.newton_cells) if args.newton_cells > 0 else None
+        newton = run_newton(args.newton_cells, tf32_peak=rates["tf32_tflops"]) if args.newton_cells > 0 else None
         if newton:
             log(f"[bench] newton: {newton}")
-        serving = run_serving(args.serve_seconds) if args.serve_seconds > 0 else None
-        if serving:
+        serving = None
+        if args.serve_seconds > 0:
+            serving = {"poisson": run_serving(args.serve_seconds),
+                       "saturated": run_serving(saturate=args.serve_saturate, budget_gb=4.0, seed=8)}
+            serving["capacity_vs_plain_fp64"] = round(serving["saturated"]["cell_steps_per_s"] / plain_value, 2)
             log(f"[bench] serving: {serving}")
-        cpu = cpu_baseline(cells, args.steps) if not args.no_cpu else None
+        cpu = None
+        if not args.no_cpu:
+            port = cpu_baseline(cells, args.steps)
+            ref = ref_build_baseline(cells, args.steps)
+            cpu = ref if ref else port
+            if ref:
+                cpu["port"] = port
+            else:
+                cpu["reference_build"] = ("unavailable here: the reference's sources are not on this machine and "
+                                          "oracle/_ref holds no build for it; the oracle port is timed instead")
         out = {
             "metric": METRIC, "value": round(value, 1), "unit": "cell-steps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(t_s * 1e3 / args.steps, 4),
@@ -369,21 +462,30 @@ def run_ours(args):
             "data": "synthetic: seeded disk meshes, random-init state from rest",
             "config": {**workload_config(cells),
                        "l2": f"state {nv_total * 600 / 1e9:.2f} GB resident > 129 MB L2 (inputs larger than L2)",
-                       "patch_threads": thr, "patch_elems": emax, "autotuned": True,
+                       "patch_threads": thr, "patch_elems": emax, "patch_kernel": kinds[0],
+                       "vertex_kernel": kinds[1], "autotuned": True,
                        "parallelism": f"cell shards x{world} (population {len(specs)} cells, LPT by vertex count, "
                                       "no data-path collective)"},
             "p50_ms_per_step": round(p50, 4), "p99_ms_per_step": round(p99, 4),
+            "graph": {"value": round(graph_value, 1), "unit": "cell-steps/s",
+                      "ms_per_step": round(graph_s * 1e3 / args.steps, 4),
+                      "how": "the same steps replayed from captured CUDA graphs (8 steps each), CUDA events on the "
+                             "engine stream; the headline value launches eagerly with per-step events"},
             "plain_fp64": {"value": round(plain_value, 1), "unit": "cell-steps/s", "cell_vertices": len(x0),
+                           "workload": "one cell of 2,044 vertices / 3,929 triangles, E 1 kPa, nu 0.45, 0.1 um, 600 "
+                                       "integrins (1 pN/nm, rest 20 nm), boundary protruding 10 nm/step, 200 steps",
                            "shape": list(plain_shape),
+                           "roofline": plain_roofline,
                            "p50_ms_per_step": round(percentile(pr["per_step"], 0.5), 4),
                            "p99_ms_per_step": round(percentile(pr["per_step"], 0.99), 4),
                            "wall_cell_steps_per_s": round(plain_wall, 1)},
             "ratio_vs_plain_fp64": round(value / world / plain_value, 2),
             "mixed_vs_fp64_rel_displacement_error": max_err, "error_steps": err_steps,
+            "accuracy": accuracy,
             "element_assemblies_per_s": round(value / len(cells) * nt_total / world, 1),
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "serving": serving,
             "newton": newton, "config2": config2,
-            "clocks": clocks_info,
+            "clocks": clocks_info, "pipe_rates": rates,
         }
     if dist:
         dist.barrier()
@@ -392,11 +494,73 @@ def run_ours(args):
         print(json.dumps(out), flush=True)
 
 
-def run_serving(seconds: float, rate: float = 200.0, budget_gb: float = 16.0, seed: int = 7):
+SHIFT = (0.5, -0.25, 0.0)   # a rigid in-plane translation: the physics is unchanged, the rounding is not
+
+
+def mixed_error(cells, device=0, horizons=(20, 300), gate_steps=300, tol=1e-6):
+    """Relative displacement error of the mixed form against the FP64 form on the same
+    cells: per cell max|x_mixed - x_fp64| / max|x_fp64 - x0|, the max over cells.
+
+    The gate (<= tol) is taken at the workload's own horizon (gate_steps, 300 steps for
+    the 256-cell workload), whatever --steps is.  At shorter horizons from rest the
+    slowest cells have moved only ~1e-9 um while binary64 positions near 10 um round at
+    ~1e-15 um per step, so the FP64 form's own rounding noise is itself ~1e-6 of the
+    displacement there.  That noise is measured by stepping the FP64 form once more on
+    the rigidly translated cells (x0 + SHIFT: the same physics, other roundings):
+    fp64_noise = max|(x_fp64' - SHIFT) - x_fp64| / max|x_fp64 - x0|.  A cell is within
+    the FP64 form's noise when its mixed error <= max(tol, 2 fp64_noise)."""
+    from wholecellfe_gb300 import capi, synth
+    shift = np.asarray(SHIFT)
+    hz = sorted(set(horizons) | {gate_steps})
+    runs = {}
+    for name, prec, sh in (("mixed", capi.PREC_MIXED, 0.0), ("fp64", capi.PREC_FP64, 0.0),
+                           ("fp64_shift", capi.PREC_FP64, 1.0)):
+        e = capi.Engine(prec, device=device)
+        hs = []
+        for c in cells:
+            x0 = c["x0"] + sh * shift
+            h = e.add_cell(x0, c["tri"], c["p"], state=synth.initial_state(x0))
+            h.set_integrins(c["rho"])
+            hs.append(h)
+        done, out = 0, {}
+        for n in hz:
+            e.step(n - done, DT)
+            e.sync()
+            done = n
+            out[n] = [h.get_state()[0] - sh * shift for h in hs]
+        runs[name] = out
+        e.close()
+    res = {}
+    for n in hz:
+        em, en, um, within = [], [], [], 0
+        for i, c in enumerate(cells):
+            xd = runs["fp64"][n][i]
+            u = float(np.max(np.abs(xd - c["x0"])))
+            a = float(np.max(np.abs(runs["mixed"][n][i] - xd)))
+            b = float(np.max(np.abs(runs["fp64_shift"][n][i] - xd)))
+            um.append(u)
+            em.append(a / u if u > 0 else (0.0 if a == 0 else math.inf))
+            en.append(b / u if u > 0 else (0.0 if b == 0 else math.inf))
+            within += em[-1] <= max(tol, 2.0 * en[-1])
+        res[n] = {"steps": n, "max_rel_displacement_error": max(em), "median_rel_displacement_error": float(np.median(em)),
+                  "fp64_noise_max": max(en), "fp64_noise_median": float(np.median(en)),
+                  "min_displacement_um": min(um), "cells_within_fp64_noise": f"{within}/{len(cells)}"}
+    gate = dict(res[gate_steps])
+    gate["tol"] = tol
+    gate["pass"] = gate["max_rel_displacement_error"] <= tol
+    return {"gate": gate, "horizons": [res[n] for n in hz if n != gate_steps],
+            "definition": "per cell max|x_mixed - x_fp64| / max|x_fp64 - x0|, max over cells; fp64_noise: the FP64 "
+                          f"form on the cells translated by {list(SHIFT)} um against the untranslated run"}
+
+
+def run_serving(seconds: float = 10.0, rate: float = 200.0, budget_gb: float = 16.0, seed: int = 7,
+                saturate: int = 0):
     """Config 5, bounded: Poisson arrivals (rate per second) of cell simulations with 1k-50k
     vertices (log-uniform), 50-2000 steps (uniform) and a random stiffness model, admitted by
     an HBM budget into one mixed-precision engine (wcfe_server_*).  Arrivals stop after
-    `seconds`; the loop then drains.  Meshes come from a pool of 24 seeded disks."""
+    `seconds`; the loop then drains.  saturate > 0 instead submits that many requests at
+    once (the offered load far above capacity, the budget binding), so that the measured
+    rate is the serving form's capacity.  Meshes come from a pool of 24 seeded disks."""
     import ctypes as C
     from wholecellfe_gb300 import capi, synth
     from wholecellfe_gb300.params import default_params
@@ -416,31 +580,39 @@ def run_serving(seconds: float, rate: float = 200.0, budget_gb: float = 16.0, se
     eng = capi.Engine(capi.PREC_MIXED, budget_bytes=int(budget_gb * 2**30))
     srv = C.c_void_p()
     capi.check(L.wcfe_server_create(eng.h, DT, C.byref(srv)), "wcfe_server_create")
-    keep, ids, steps_of, nv_of = [], [], [], []
+    ids, steps_of, nv_of = [], [], []
+
+    def submit():
+        x0, tri = pool[int(rng.integers(0, len(pool)))]
+        p = params[int(rng.integers(0, 3))]
+        steps = int(rng.integers(50, 2001))
+        rq = capi.Request(len(x0), len(tri), capi.ip(tri), capi.dp(x0), C.pointer(p), steps, None, None, 0, 0)
+        rid = C.c_int64()
+        capi.check(L.wcfe_server_submit(srv, C.byref(rq), C.byref(rid)), "wcfe_server_submit")
+        ids.append(rid.value)
+        steps_of.append(steps)
+        nv_of.append(len(x0))
+
     t0 = time.perf_counter()
+    if saturate:
+        for _ in range(saturate):
+            submit()
     next_arrival = rng.exponential(1.0 / rate)
     na, nq = C.c_int32(), C.c_int32()
-    cell_steps = 0
     active_hist = []
     while True:
         now = time.perf_counter() - t0
-        while next_arrival <= now and next_arrival < seconds:
-            x0, tri = pool[int(rng.integers(0, len(pool)))]
-            p = params[int(rng.integers(0, 3))]
-            steps = int(rng.integers(50, 2001))
-            rq = capi.Request(len(x0), len(tri), capi.ip(tri), capi.dp(x0), C.pointer(p), steps, None, None, 0, 0)
-            rid = C.c_int64()
-            capi.check(L.wcfe_server_submit(srv, C.byref(rq), C.byref(rid)), "wcfe_server_submit")
-            ids.append(rid.value)
-            steps_of.append(steps)
-            nv_of.append(len(x0))
+        while not saturate and next_arrival <= now and next_arrival < seconds:
+            submit()
             next_arrival += rng.exponential(1.0 / rate)
         capi.check(L.wcfe_server_iterate(srv, C.byref(na), C.byref(nq)), "wcfe_server_iterate")
         active_hist.append(na.value)
-        if now >= seconds and na.value == 0 and nq.value == 0:
+        if (saturate or now >= seconds) and na.value == 0 and nq.value == 0:
             break
-        if now > seconds + 120:   # drain bound
+        if now > (0 if saturate else seconds) + 300:   # drain bound
             break
+        if na.value == 0 and not saturate:
+            time.sleep(0.0005)
     wall = time.perf_counter() - t0
     n = L.wcfe_server_step_times(srv, None, 0)
     buf = (C.c_double * max(n, 1))()
@@ -454,16 +626,23 @@ def run_serving(seconds: float, rate: float = 200.0, budget_gb: float = 16.0, se
             lat.append(t.value)
             done_steps += st
     L.wcfe_server_destroy(srv)
+    used_peak = max(active_hist) if active_hist else 0
     eng.close()
-    return {"arrival_rate_per_s": rate, "arrival_seconds": seconds, "requests": len(ids), "completed": len(lat),
-            "vertices_per_request": "log-uniform [1000, 50000] (pool of 24 meshes)", "steps_per_request": "uniform [50, 2000]",
-            "hbm_budget_gb": budget_gb, "wall_s": round(wall, 2),
-            "cell_steps_per_s": round(done_steps / wall, 1),
-            "p50_step_ms": round(percentile(it_ms, 0.5), 4) if it_ms else None,
-            "p99_step_ms": round(percentile(it_ms, 0.99), 4) if it_ms else None,
-            "p50_request_s": round(percentile(lat, 0.5), 3) if lat else None,
-            "p99_request_s": round(percentile(lat, 0.99), 3) if lat else None,
-            "max_resident_cells": max(active_hist) if active_hist else 0}
+    out = {"requests": len(ids), "completed": len(lat),
+           "vertices_per_request": "log-uniform [1000, 50000] (pool of 24 meshes)", "steps_per_request": "uniform [50, 2000]",
+           "hbm_budget_gb": budget_gb, "wall_s": round(wall, 2),
+           "cell_steps_per_s": round(done_steps / wall, 1),
+           "p50_step_ms": round(percentile(it_ms, 0.5), 4) if it_ms else None,
+           "p99_step_ms": round(percentile(it_ms, 0.99), 4) if it_ms else None,
+           "p50_request_s": round(percentile(lat, 0.5), 3) if lat else None,
+           "p99_request_s": round(percentile(lat, 0.99), 3) if lat else None,
+           "max_resident_cells": used_peak}
+    if saturate:
+        out["arrivals"] = f"{saturate} requests submitted at once (offered load above capacity)"
+    else:
+        out.update({"arrival_rate_per_s": rate, "arrival_seconds": seconds,
+                    "offered_cell_steps_per_s": round(sum(steps_of) / max(seconds, 1e-9), 1)})
+    return out
 
 
 def run_config2(steps: int = 500, seed: int = 2):
@@ -499,19 +678,22 @@ def run_config2(steps: int = 500, seed: int = 2):
             "status": [out["fp64"][2], out["mixed"][2]]}
 
 
-def lu_roofline(tflops, outer_block=512):
-    """The LU's rate against the dense TF32 tensor rate, taken as half the measured bf16
-    GEMM rate (a derived figure: the measured peaks hold bf16 only); sustained, since a
-    factorisation runs for hundreds of milliseconds."""
-    try:
-        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
-    except (OSError, ValueError):
-        peaks = {}
-    bf16 = peaks.get("bf16_tflops_sustained")
-    src = "MEASURED_PEAKS.json bf16_tflops_sustained / 2"
-    if bf16 is None:
-        bf16, src = 1700.0, "fallback 1700 TFLOP/s bf16 sustained / 2"
-    peak = bf16 / 2.0
+def lu_roofline(tflops, outer_block=512, tf32_peak=None):
+    """The LU's rate against the TF32 tensor rate measured on this GPU by
+    wcfe_debug_pipe_rates (tcgen05 MMAs of the LU's shape from resident operands); without
+    it, half the measured bf16 GEMM rate."""
+    if tf32_peak and tf32_peak > 0:
+        peak, src = tf32_peak, "measured TF32 tcgen05 rate of this GPU (wcfe_debug_pipe_rates, M 128 N 256)"
+    else:
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except (OSError, ValueError):
+            peaks = {}
+        bf16 = peaks.get("bf16_tflops_sustained")
+        src = "MEASURED_PEAKS.json bf16_tflops_sustained / 2"
+        if bf16 is None:
+            bf16, src = 1700.0, "fallback 1700 TFLOP/s bf16 sustained / 2"
+        peak = bf16 / 2.0
     return {"bound": "tensor", "achieved": tflops, "peak": round(peak, 1), "unit": "TFLOP/s",
             "frac": round(tflops / peak, 4) if tflops else None, "peak_source": src,
             "note": "TF32 flops 2/3 (2N)^3 per factorisation over the LU's device time; "
@@ -546,7 +728,7 @@ def cpu_lu_baseline(sizes, budget_s: float = 12.0):
             "lu_per_s": round(done / secs, 3), "tflop_per_s": round(flops / secs / 1e12, 4)}
 
 
-def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(512, 0)):
+def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(512, 0), tf32_peak=None):
     """Config 4, bounded: implicit (Newton) steps of `ncells` cells with 1000-4000 vertices
     (uniform), dense 2N x 2N tangents, LU with TF32 tensor-core trailing updates, FP64
     residual and refinement to 1e-10.  Reports cell-steps/s, Newton iterations, the
@@ -585,7 +767,7 @@ def run_newton(ncells: int = 64, steps: int = 2, seed: int = 4, lu=(512, 0)):
             "lu_ms_per_step": round(st["lu_ms"] / steps, 2),
             "lu_tflop_per_s": round(st["lu_gflop"] / st["lu_ms"], 2) if st["lu_ms"] > 0 else None,
             "lu_share_of_step": round(st["lu_ms"] / (wall * 1e3), 3),
-            "lu_roofline": lu_roofline(st["lu_gflop"] / st["lu_ms"] if st["lu_ms"] > 0 else None, lu[0]),
+            "lu_roofline": lu_roofline(st["lu_gflop"] / st["lu_ms"] if st["lu_ms"] > 0 else None, lu[0], tf32_peak),
             "solve_ms_per_step": round(st["solve_ms"] / steps, 2),
             "cpu_lu_baseline": cpu_lu_baseline(sizes),
             "timing": "host wall clock around wcfe_engine_step_implicit (it synchronises per Newton iteration); "
@@ -602,14 +784,19 @@ def run_phase(args):
     if args.phase == "config2":
         print(json.dumps(run_config2(max(1, min(args.steps, 500)))))
         return
+    if args.phase == "serve":
+        pois = run_serving(args.serve_seconds) if args.serve_seconds > 0 else None
+        sat = run_serving(saturate=args.serve_saturate, budget_gb=4.0, seed=8) if args.serve_saturate > 0 else None
+        print(json.dumps({"poisson": pois, "saturated": sat}))
+        return
     if args.phase == "newton":
         lu = tuple(int(v) for v in args.lu.split(","))
         print(json.dumps(run_newton(args.cells if args.cells != N_CELLS else 64, max(1, min(args.steps, 5)), lu=lu)))
         return
     if args.phase == "plain":
-        x0, tri = synth.disk_mesh(2000, seed=1)
+        x0, tri, p, rho = synth.protruding_cell(dt=DT)
         eng = capi.Engine(capi.PREC_FP64)
-        eng.add_cell(x0, tri, default_params("k1"), state=synth.initial_state(x0))
+        eng.add_cell(x0, tri, p, state=synth.initial_state(x0)).set_integrins(rho)
         ncells = 1
     else:
         cells = make_workload(seed=1000, ncells=args.cells)
@@ -651,6 +838,8 @@ def run_reference(args):
     from wholecellfe_gb300 import synth
     cells = make_workload(seed=1000, ncells=args.cells)
     nthreads = os.cpu_count() or 1
+    if O.ref_available("k1") and O.ref_available("k31"):
+        return run_reference_build(args, cells, nthreads)
     # one timed "step" = every sampled cell advanced by a few explicit steps, sized to finish in minutes
     sample = cells[:max(nthreads, 32)]
     ocs = [O.OCell(O.OMesh(c["tri"], len(c["x0"])), synth.initial_state(c["x0"]), c["p"], rho_w=c["rho"])
@@ -680,6 +869,40 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def run_reference_build(args, cells, nprocs):
+    """--impl reference where the reference was built from its sources (oracle/_ref): its own
+    step loop, one process per host core, on the workload's linear-law cells."""
+    import multiprocessing as mp
+    lin = [c for c in cells if c["model"] in (0, 1)]
+    sample = lin[:max(nprocs, 32)]
+    per = 2
+    jobs = [(sample[i::nprocs], per) for i in range(nprocs) if sample[i::nprocs]]
+    times = []
+    steps = min(args.steps, 10)
+    with mp.get_context("spawn").Pool(len(jobs)) as pool:
+        for _ in range(min(args.warmup, 1)):
+            pool.map(_ref_worker, jobs)
+        for _ in range(steps):
+            t0 = time.perf_counter()
+            pool.map(_ref_worker, jobs)
+            times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = len(sample) * per * steps / tot
+    cpu = {"value": round(value, 1), "unit": "cell-steps/s", "cores": len(jobs), "kind": "reference",
+           "sample": f"{len(sample)} linear-law cells of the {len(cells)} workload cells x {per} explicit steps per "
+                     f"timed step, {steps} timed steps, the reference's UL_growth_explicit.cpp built from its sources "
+                     f"(oracle/_ref), {len(jobs)} processes"}
+    out = {"metric": METRIC, "value": round(value, 1), "unit": "cell-steps/s", "n_gpus": 0, "steps": steps,
+           "warmup": args.warmup, "ms_per_step": round(tot / steps * 1e3, 3), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "fp64", "data": "synthetic",
+           "config": {**workload_config(cells), "cells_sampled": len(sample)},
+           "impl": "reference", "cpu_baseline": cpu,
+           "e2e": {"value": round(value, 1), "unit": "cell-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "p50_ms_per_step": round(percentile(times, 0.5) * 1e3, 3),
+           "p99_ms_per_step": round(percentile(times, 0.99) * 1e3, 3)}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -690,14 +913,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="length of the Poisson arrival window of the serving measurement (0: skip)")
-    ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain", "newton", "config2"],
+    ap.add_argument("--serve-saturate", type=int, default=1000,
+                    help="requests submitted at once for the serving capacity measurement")
+    ap.add_argument("--phase", default="all", choices=["all", "mixed", "fp64", "plain", "newton", "config2", "serve"],
                     help="profiling aid: run only one timed loop (default shape, no autotune) and print its timing")
     ap.add_argument("--lu", default="512,0", help="--phase newton: LU outer block and kind (0 tcgen05, 1 mma.sync)")
     ap.add_argument("--newton-cells", type=int, default=512,
                     help="cells of the bounded implicit-step (Newton, dense LU) measurement (0: skip)")
     ap.add_argument("--shape", default="", help="with --phase: patch threads,elements (default: the engine's)")
-    ap.add_argument("--patch-kernel", type=int, default=1, choices=[0, 1],
-                    help="with --phase mixed: 0 staged patch kernel, 1 plain (default)")
+    ap.add_argument("--patch-kernel", type=int, default=1, choices=[0, 1, 2, 3, 4],
+                    help="with --phase mixed: 0 staged patch kernel, 1 plain (default), 2-4 plain with registers "
+                         "capped for 6-8 CTAs per SM")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3

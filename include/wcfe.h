@@ -60,15 +60,20 @@ enum {
 
 /* ---- integrin force laws ------------------------------------------------ */
 enum {
-    WCFE_LAW_LINEAR = 0,     /* f = k (D - L0); wholeCellFE_k1 / wholeCellFE_k31 */
+    WCFE_LAW_LINEAR = 0,     /* f = k D (L0 = 0: wholeCellFE_k1 / wholeCellFE_k31); with a rest length
+                                L0 > 0 the bond is slack below it: f = k max(D - L0, 0) */
     WCFE_LAW_MD_TABLE = 1,   /* piecewise-linear MD fit; wholeCellFE_kMD UL:1203-1214 */
-    WCFE_LAW_POLY = 2        /* tangent stiffness k0 (1 + (e/x0)^2): f = k0 (e + e^3/(3 x0^2)), e = D - L0 */
+    WCFE_LAW_POLY = 2        /* tangent stiffness k0 (1 + (e/x0)^2): f = k0 (e + e^3/(3 x0^2)) for
+                                e = D - L0 > 0, slack (0) below */
 };
 
 /* ---- arithmetic forms --------------------------------------------------- */
 enum {
     WCFE_PREC_FP64 = 0,      /* element assembly and update in FP64 (the plain form) */
-    WCFE_PREC_MIXED = 1      /* element assembly in FP32 (increment form), state/update in FP64 */
+    WCFE_PREC_MIXED = 1      /* element assembly and forces in FP32 (increment form); the state and
+                                the update in extended FP32 formats: positions triple-float (about
+                                72 bits, exact for binary64 input), velocity, strain, bond state
+                                float-float (about 48 bits); planar cells (z = 0) only */
 };
 
 /* Reference variants for wcfe_params_default. */
@@ -93,7 +98,9 @@ typedef struct wcfe_params {
     int32_t force_law;    /* WCFE_LAW_* */
     int32_t linear_norm2d;/* 1: Bell force of the linear law uses the in-plane norm (k1 UL:2077) */
     double k_lin;         /* linear stiffness, pN/um (1000 = 1 pN/nm) */
-    double rest_len;      /* spring rest length, um (0 in the reference) */
+    double rest_len;      /* spring rest length, um (0 in the reference); a bond shorter than it
+                             carries no force (tension only), so that a fresh bond of zero length,
+                             whose direction is rounding noise, pushes nothing */
     double poly_k0;       /* WCFE_LAW_POLY stiffness at zero extension, pN/um */
     double poly_x0;       /* WCFE_LAW_POLY stiffening length, um */
     double rho_i_max;     /* integrin density 100 /um^2 (UL:1218) */
@@ -112,6 +119,13 @@ typedef struct wcfe_params {
     double drag;          /* 0.001 */
     double damp;          /* 0.001 */
     double rho;           /* 1 */
+    /* radial protrusion driver (no counterpart in the reference's default driver; the
+     * reference's velocity drivers, e.g. driverVelocities_Uniaxial UL:125-168, prescribe the
+     * half-step velocity of selected nodes the same way): when protrude_v != 0, every
+     * boundary vertex gets V_hlf = protrude_v (X - c) / |X - c| in the plane, c =
+     * (protrude_cx, protrude_cy), instead of V + dt/2 A; 0 in the reference variants */
+    double protrude_v;    /* um/s (10 nm per step at dt = 5e-5 s: 200) */
+    double protrude_cx, protrude_cy;
 } wcfe_params;
 
 void wcfe_params_default(wcfe_params* p, int32_t variant);
@@ -174,6 +188,12 @@ int wcfe_cell_get_state(wcfe_engine* eng, int32_t cell, double* x, double* V, do
                         double* c_A, double* c_C, double* fa_u);
 /* Simulation time used for the active-stress ramp and the AP call counter. */
 int wcfe_cell_set_clock(wcfe_engine* eng, int32_t cell, double t_cur, uint64_t ap_calls);
+/* Step budget of a cell (no counterpart in the reference; the serving loop's stop rule):
+ * 0 = unlimited (the default), n > 0 = the cell runs n more steps and then stays put,
+ * skipped by every later step, whatever the number of steps queued; the device counts it
+ * down, and get returns -1 once it ran out. */
+int wcfe_cell_set_step_budget(wcfe_engine* eng, int32_t cell, int32_t steps);
+int wcfe_cell_get_step_budget(wcfe_engine* eng, int32_t cell, int32_t* steps);
 int wcfe_cell_get_clock(wcfe_engine* eng, int32_t cell, double* t_cur, uint64_t* ap_calls);
 /* Bit 0: NaN/Inf in the state after the last step. */
 int wcfe_cell_status(wcfe_engine* eng, int32_t cell, uint32_t* status);
@@ -205,9 +225,16 @@ int wcfe_cell_eval_forces(wcfe_engine* eng, int32_t cell, const double* x, doubl
 /* Mixed engines: which patch-phase kernel a step uses.  0: the staged kernel (a
  * producer warp copies each patch's records and owned-vertex state into shared
  * memory one patch ahead with bulk asynchronous copies) wherever its shared-memory
- * plan fits, else the plain kernel; 1 (default): the plain kernel.  Results are
- * identical; wcfe_engine_autotune times both.  No counterpart in the reference. */
+ * plan fits, else the plain kernel; 1 (default): the plain kernel; 2, 3, 4: the plain
+ * kernel compiled for at least 6, 7, 8 resident CTAs of 128 threads per SM (registers
+ * capped; 128 patch threads only).  Results are identical; wcfe_engine_autotune times
+ * them all.  No counterpart in the reference. */
 int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind);
+/* Mixed engines: the vertex-phase kernel compiled for 5 (kind 0, default) or 4 (kind 1)
+ * resident blocks of 256 threads per SM (48 or 64 registers); results are identical. */
+int wcfe_engine_set_vertex_kernel(wcfe_engine* e, int32_t kind);
+/* The patch and vertex kernel kinds in use (after wcfe_engine_autotune: its choice). */
+int wcfe_engine_get_kernels(const wcfe_engine* e, int32_t* patch_kind, int32_t* vertex_kind);
 
 /* Couple cell `cell` to a deformable substrate simulated by the same FP64 engine:
  * `substrate` is another cell of the engine holding the substrate mesh and state
@@ -272,6 +299,9 @@ int64_t wcfe_engine_step_times(wcfe_engine* eng, float* out, int64_t cap, float*
 int wcfe_engine_set_timing(wcfe_engine* eng, int32_t enable);
 /* Number of kernels this engine launched since creation. */
 uint64_t wcfe_engine_launches(const wcfe_engine* eng);
+/* The engine's main CUDA stream (a cudaStream_t), so that a caller can order its own work
+ * or record timing events against the engine's steps. */
+void* wcfe_engine_stream(const wcfe_engine* eng);
 
 /* ---- serving: continuous batching of whole cell simulations -------------- */
 typedef struct wcfe_server wcfe_server;
@@ -291,15 +321,30 @@ int wcfe_server_create(wcfe_engine* eng, double dt, wcfe_server** out);
 int wcfe_server_destroy(wcfe_server* srv);
 /* Queue a request; *req_id receives its id (monotonic from 0). */
 int wcfe_server_submit(wcfe_server* srv, const wcfe_request* req, int64_t* req_id);
-/* One serving iteration: admit queued requests that fit the free budget, advance
- * every resident cell by one step in one batched launch per phase, retire the
- * finished ones.  *n_active / *n_queued report the counts after the iteration. */
+/* One serving iteration: admit queued requests (prepared on the server's host worker
+ * threads, in arrival order) while the engine's HBM budget has room, enqueue K steps of
+ * every resident cell (K chosen so that an iteration takes about the target GPU time,
+ * wcfe_server_set_iteration_ms; each cell stops on the device after exactly its
+ * n_steps), and queue the results of the cells that finish.  At most two iterations are
+ * in flight: the call waits for the one before the last.  *n_active reports the resident
+ * cells, *n_queued the requests not yet admitted plus the iterations still in flight. */
 int wcfe_server_iterate(wcfe_server* srv, int32_t* n_active, int32_t* n_queued);
+/* Target GPU time of one serving iteration (default 8 ms). */
+int wcfe_server_set_iteration_ms(wcfe_server* srv, double ms);
+/* Cell-steps enqueued by the server so far. */
+uint64_t wcfe_server_cell_steps(const wcfe_server* srv);
 /* Fetch a finished request's final positions (double[n][3]) and latency stats.
  * Returns WCFE_ERR_ARG while it is still running. */
 int wcfe_server_result(wcfe_server* srv, int64_t req_id, double* x_out, double* seconds_in_system);
-/* Per-iteration wall time samples (seconds) collected so far; returns count. */
+/* Per-step latency samples (seconds) collected so far, one per step: the device time
+ * of each completed iteration divided by its steps; returns the count. */
 int64_t wcfe_server_step_times(wcfe_server* srv, double* out, int64_t cap);
+
+/* Rates of the pipes on the current device, for roofline denominators (no counterpart in
+ * the reference): TF32 tcgen05 MMAs (M 128, N 256, operands resident in shared memory,
+ * one CTA per SM), and FP64 and FP32 FMA chains, in TFLOP/s.  A negative TF32 rate means
+ * its bounded wait gave up.  Takes a few hundred milliseconds. */
+int wcfe_debug_pipe_rates(double* tf32_tflops, double* fp64_tflops, double* fp32_tflops);
 
 /* ---- allocation-free area reduction ------------------------------------- */
 /* No counterpart in the reference: the same total area and area-weighted
@@ -311,8 +356,12 @@ int64_t wcfe_server_step_times(wcfe_server* srv, double* out, int64_t cap);
  * scratch is a 128 KiB file-scope device array that every GPU loading the
  * library keeps until exit; t <= 4,194,304 (else WCFE_ERR_LIMIT).  The first
  * call on a device resolves the array's address (do it before any stream
- * capture).  Calls overlapping on the GPU race on the shared array.  An index
- * outside [0, n) yields NaN.  stream: a cudaStream_t, or NULL. */
+ * capture) and keeps it for the life of the process, so the entry point must
+ * not be called on a device again after a cudaDeviceReset of it.  Calls
+ * overlapping on the GPU race on the shared array.  An index outside [0, n)
+ * yields NaN.  A CUDA error already pending on the calling thread is left in
+ * place and the call returns WCFE_ERR_CUDA without launching.  stream: a
+ * cudaStream_t, or NULL. */
 int wcfe_area_tot_noalloc(const double* x_dev, int32_t n_vert, const int32_t* tri_dev, int32_t n_tri,
                           double* area4_dev, void* stream);
 

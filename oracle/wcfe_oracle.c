@@ -179,15 +179,16 @@ static void spring_force(const wcfe_params* p, const double* u, double* fs, doub
             else if (D >= MD_PX[5]) mag = MD_PY[5] + MD_K[5] * (D - MD_PX[5]);
         }
     } else if (p->force_law == WCFE_LAW_LINEAR) {
-        mag = p->k_lin * (D - p->rest_len);
+        /* a bond with a rest length is slack below it (tension only) */
+        mag = D > p->rest_len ? p->k_lin * (D - p->rest_len) : 0.0;
     } else {
         double e = D - p->rest_len;
-        mag = p->poly_k0 * (e + e * e * e / (3.0 * p->poly_x0 * p->poly_x0));
+        mag = e > 0.0 ? p->poly_k0 * (e + e * e * e / (3.0 * p->poly_x0 * p->poly_x0)) : 0.0;
     }
     fs[0] = mag * uD[0]; fs[1] = mag * uD[1]; fs[2] = mag * uD[2];
     if (p->force_law == WCFE_LAW_LINEAR && p->linear_norm2d) {
         double D2 = sqrt(u[0] * u[0] + u[1] * u[1]);
-        *bell_force = fabs(p->k_lin * (D2 - p->rest_len));
+        *bell_force = D2 > p->rest_len ? p->k_lin * (D2 - p->rest_len) : 0.0;
     } else {
         *bell_force = sqrt((fs[0] * fs[0] + fs[1] * fs[1]) + fs[2] * fs[2]);
     }
@@ -749,12 +750,36 @@ typedef struct wo_cell {
     const double* Xs;
 } wo_cell;
 
+/*
+ * The radial protrusion driver (wcfe_params.protrude_v), an extension: the reference's
+ * default driver (driverVelocities_Explicit UL:103-124) prescribes nothing, and its other
+ * drivers (driverVelocities_Uniaxial UL:125-168) prescribe the half-step velocity of the
+ * driven nodes, after which x = X + dt V_hlf as usual.  Here every boundary vertex is
+ * driven radially from c = (protrude_cx, protrude_cy): V_hlf = protrude_v (X - c) / |X - c|
+ * in the plane (a vertex at c keeps its default V_hlf).
+ */
+WO_API void wo_drive_protrusion(const wo_mesh* m, const double* X, const wcfe_params* p, double dt, double* Vh,
+                                double* xn) {
+    if (p->protrude_v == 0.0) return;
+    for (int i = 0; i < m->nv; ++i) {
+        if (!m->bnd[i]) continue;
+        const double dx = X[3 * i] - p->protrude_cx, dy = X[3 * i + 1] - p->protrude_cy;
+        const double r = sqrt(dx * dx + dy * dy);
+        if (r == 0.0) continue;
+        Vh[3 * i] = p->protrude_v * (dx / r);
+        Vh[3 * i + 1] = p->protrude_v * (dy / r);
+        Vh[3 * i + 2] = 0.0;
+        for (int c = 0; c < 3; ++c) xn[3 * i + c] = X[3 * i + c] + dt * Vh[3 * i + c];
+    }
+}
+
 WO_API void wo_cell_steps(wo_cell* c, int32_t nsteps, double dt) {
     int nv = c->mesh.nv;
     double* Vh = (double*)malloc(sizeof(double) * 3 * nv);
     double* xn = (double*)malloc(sizeof(double) * 3 * nv);
     for (int s = 0; s < nsteps; ++s) {
         wo_predict(nv, c->x, c->V, c->A, dt, Vh, xn);
+        wo_drive_protrusion(&c->mesh, c->x, &c->p, dt, Vh, xn);
         wo_update_fa(nv, c->cA, c->cC, c->fau, dt, c->x, xn, c->sub, c->Xs, c->Xs, &c->p, NULL);
         wo_update_forces(&c->mesh, c->x, xn, c->V, Vh, c->A, c->ea, c->cA, c->cC, c->fau, dt, dt, c->t, &c->p,
                          c->rho_w, c->ap_call, NULL);

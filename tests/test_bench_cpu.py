@@ -34,3 +34,5 @@ def test_lu_roofline_arithmetic():
     assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
     assert abs(r["frac"] - 200.0 / r["peak"]) < 1e-3 and "K = 512" in r["note"]
     assert bench.lu_roofline(None)["frac"] is None
+    m = bench.lu_roofline(250.0, 512, tf32_peak=1000.0)
+    assert m["peak"] == 1000.0 and m["frac"] == 0.25 and "measured TF32" in m["peak_source"]

@@ -185,16 +185,93 @@ def test_mixed_engine_refuses_per_function_entry_points():
 
 
 def test_mixed_state_round_trip():
-    """set_state / get_state of a mixed engine: float-float storage keeps 48 bits."""
+    """set_state / get_state of a mixed engine: positions (triple-float) come back bit for
+    bit, float-float storage keeps 48 bits, the acceleration is FP32."""
     x0, tri = synth.disk_mesh(500, seed=9)
     st = synth.initial_state(x0, perturb=1.0, seed=3)
     e = capi.Engine(capi.PREC_MIXED)
     h = e.add_cell(x0, tri, default_params("k31"), state=st)
     got = h.get_state()
+    assert np.array_equal(got[0], st[0])
     for k, (a, b) in enumerate(zip(got, st)):
         tol = 2.0 ** -23 if k == 2 else 2.0 ** -47   # the acceleration is stored in FP32
         assert np.all(np.abs(a - b) <= tol * np.abs(b) + 1e-300), k
     e.close()
+
+
+def _horizon_errors(cells, horizons, shift=(0.5, -0.25, 0.0)):
+    """Per cell and horizon: (mixed error, FP64 noise, displacement), the errors as
+    max|x_mixed - x_fp64| and max|(x_fp64' - shift) - x_fp64| with x_fp64' the FP64 form on
+    the rigidly translated cell (the same physics, other roundings)."""
+    shift = np.asarray(shift)
+    runs = {}
+    for name, prec, sh in (("m", capi.PREC_MIXED, 0.0), ("d", capi.PREC_FP64, 0.0), ("s", capi.PREC_FP64, 1.0)):
+        e = capi.Engine(prec)
+        hs = []
+        for x0, tri, p, st, rho in cells:
+            s0 = (st[0] + sh * shift,) + tuple(st[1:])
+            h = e.add_cell(x0 + sh * shift, tri, p, state=s0)
+            if rho is not None:
+                h.set_integrins(rho)
+            hs.append(h)
+        done, runs[name] = 0, {}
+        for n in horizons:
+            e.step(n - done, 5e-5)
+            done = n
+            runs[name][n] = [h.get_state()[0] - sh * shift for h in hs]
+            assert all(h.status() == 0 for h in hs)
+        e.close()
+    out = {}
+    for n in horizons:
+        out[n] = []
+        for i, (x0, tri, p, st, rho) in enumerate(cells):
+            xd = runs["d"][n][i]
+            out[n].append((float(np.max(np.abs(runs["m"][n][i] - xd))), float(np.max(np.abs(runs["s"][n][i] - xd))),
+                           float(np.max(np.abs(xd - st[0])))))
+    return out
+
+
+def test_mixed_error_every_horizon_bench_subset():
+    """The 256-cell benchmark workload's smallest and largest cells and one cell of each
+    stiffness model, from rest, after 1, 5, 20 and 300 steps.  After one step from rest
+    nothing has moved and the mixed positions equal the FP64 ones exactly; at every
+    horizon each cell's mixed error is <= 1e-6 of its displacement or within twice the
+    FP64 form's own rounding noise (a 20-step-old cell of the workload has moved ~1e-9 um,
+    where binary64 positions near 10 um carry ~1e-15 um of rounding per step); at the
+    workload's 300-step horizon every cell is <= 1e-6."""
+    import bench
+    specs = bench.workload_specs(1000, 256)
+    ns = [s["n"] for s in specs]
+    pick = {int(np.argmin(ns)), int(np.argmax(ns))}
+    for m in range(3):
+        pick.add(next(s["index"] for s in specs if s["model"] == m))
+    cells = []
+    for i in sorted(pick):
+        c = bench.build_cell(1000, specs[i])
+        cells.append((c["x0"], c["tri"], c["p"], synth.initial_state(c["x0"]), c["rho"]))
+    res = _horizon_errors(cells, (1, 5, 20, 300))
+    for a, b, u in res[1]:
+        assert u == 0.0 and a == 0.0
+    for n in (5, 20):
+        for a, b, u in res[n]:
+            assert u > 0 and a <= max(MIXED_TOL * u, 2.0 * b), (n, a, b, u)
+    for a, b, u in res[300]:
+        assert a <= MIXED_TOL * u, (a, u)
+
+
+@pytest.mark.parametrize("variant,law", [("kMD", 1), ("k1", 0), ("k31", 2)])
+def test_mixed_error_every_horizon_moving_state(variant, law):
+    """From a moving, pre-strained state (every law, the MD table included) the mixed
+    displacement error stays <= 1e-6 at 1, 5, 20 and 300 steps."""
+    x0, tri = synth.disk_mesh(2500, seed=33)
+    p = default_params(variant)
+    if law == 2:
+        _law(p, 2)
+    st = synth.initial_state(x0, perturb=1.0, seed=6)
+    res = _horizon_errors([(x0, tri, p, st, None)], (1, 5, 20, 300))
+    for n, rows in res.items():
+        for a, b, u in rows:
+            assert u > 0 and a <= MIXED_TOL * u, (n, a, b, u)
 
 
 def test_integrin_density_mask():
@@ -251,3 +328,21 @@ def test_staged_patch_kernel_equals_plain():
         for a, b in zip(*res):
             for u, w in zip(a, b):
                 assert np.array_equal(u, w)
+
+
+def test_mixed_protruding_cell():
+    """The protruding single-cell workload (boundary driven 10 nm per step, 600 integrins
+    with a 20 nm rest length, thin soft membrane) over 200 steps: mixed within 1e-6 of FP64."""
+    x0, tri, p, rho = synth.protruding_cell()
+    out = {}
+    for prec in (capi.PREC_FP64, capi.PREC_MIXED):
+        e = capi.Engine(prec)
+        h = e.add_cell(x0, tri, p, state=synth.initial_state(x0))
+        h.set_integrins(rho)
+        e.step(200, 5e-5)
+        out[prec] = h.get_state()[0]
+        assert h.status() == 0
+        e.close()
+    u = out[capi.PREC_FP64] - x0
+    err = np.max(np.abs(out[capi.PREC_MIXED] - out[capi.PREC_FP64])) / np.max(np.abs(u))
+    assert err <= MIXED_TOL, err

@@ -38,7 +38,11 @@ def _alone(x0, tri, p, steps, prec):
 
 
 @pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
-def test_server_results_equal_alone(prec):
+@pytest.mark.parametrize("iter_ms", [1e-6, 8.0])
+def test_server_results_equal_alone(prec, iter_ms):
+    """iter_ms 1e-6: one step per iteration, so cells stay resident across iterations and
+    the overlap shows in n_active; 8.0 (the default): many steps per iteration, cells
+    finishing inside an iteration stopped by their device-side step budget."""
     reqs = _requests()
     L = capi.load()
     # a budget that holds only a few cells at once, so admissions wait for retirements
@@ -46,6 +50,7 @@ def test_server_results_equal_alone(prec):
     eng = capi.Engine(prec, budget_bytes=budget)
     srv = C.c_void_p()
     capi.check(L.wcfe_server_create(eng.h, DT, C.byref(srv)), "wcfe_server_create")
+    capi.check(L.wcfe_server_set_iteration_ms(srv, iter_ms), "wcfe_server_set_iteration_ms")
     keep = []
     ids = []
     for k, (x0, tri, p, steps) in enumerate(reqs):
@@ -68,7 +73,9 @@ def test_server_results_equal_alone(prec):
         if na.value == 0 and nq.value == 0:
             break
     assert na.value == 0 and nq.value == 0
-    assert max_active >= 2          # requests overlapped on the device
+    if iter_ms < 1e-3:
+        assert max_active >= 2      # requests overlapped on the device
+    assert L.wcfe_server_cell_steps(srv) == sum(r[3] for r in reqs)
     for rid, (x0, tri, p, steps) in zip(ids, reqs):
         out = np.zeros((len(x0), 3))
         lat = C.c_double()
@@ -88,3 +95,24 @@ def test_budget_rejects_oversized_cell():
     with pytest.raises(capi.WcfeError):
         eng.add_cell(x0, tri, default_params("k1"))
     eng.close()
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
+def test_step_budget_stops_cell_exactly(prec):
+    """A cell with a step budget of n runs exactly n steps and then stays put while later
+    steps run the other cells (the serving loop's stop rule); the budget reads -1 after."""
+    x0, tri = synth.disk_mesh(900, seed=71)
+    x1, tri1 = synth.disk_mesh(1500, seed=72)
+    p = default_params("k31")
+    e = capi.Engine(prec)
+    a = e.add_cell(x0, tri, p, state=synth.initial_state(x0))
+    b = e.add_cell(x1, tri1, p, state=synth.initial_state(x1))
+    a.set_step_budget(5)
+    assert a.step_budget() == 5 and b.step_budget() == 0
+    e.step(12, DT)
+    got_a, got_b = a.get_state()[0], b.get_state()[0]
+    assert a.step_budget() == -1 and b.step_budget() == 0
+    assert a.clock()[0] == pytest.approx(5 * DT, rel=1e-12)
+    e.close()
+    assert np.array_equal(got_a, _alone(x0, tri, p, 5, prec))
+    assert np.array_equal(got_b, _alone(x1, tri1, p, 12, prec))

@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["wcfe_kernels.cu", "wcfe_mixed.cu", "wcfe_engine.cu", "wcfe_server.cu", "wcfe_topology.cpp",
            "wcfe_noalloc.cu", "wcfe_newton.cu", "wcfe_lu_tc.cu",
-           "wcfe_vtk.cu", "wcfe_remesh.cu"]
+           "wcfe_vtk.cu", "wcfe_remesh.cu", "wcfe_peaks.cu"]
 
 
 def nvcc() -> str:

@@ -55,6 +55,8 @@ SIGNATURES = {
     "wcfe_cell_set_state": (C.c_int, [C.c_void_p, C.c_int32, _d, _d, _d, _d, _d, _d, _d]),
     "wcfe_cell_get_state": (C.c_int, [C.c_void_p, C.c_int32, _d, _d, _d, _d, _d, _d, _d]),
     "wcfe_cell_set_clock": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_uint64]),
+    "wcfe_cell_set_step_budget": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
+    "wcfe_cell_get_step_budget": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32)]),
     "wcfe_cell_get_clock": (C.c_int, [C.c_void_p, C.c_int32, _d, C.POINTER(C.c_uint64)]),
     "wcfe_cell_status": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_uint32)]),
     "wcfe_cell_sizes": (C.c_int, [C.c_void_p, C.c_int32, _i, _i, _i, _i]),
@@ -73,6 +75,8 @@ SIGNATURES = {
     "wcfe_engine_last_timing": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "wcfe_engine_set_timing": (C.c_int, [C.c_void_p, C.c_int32]),
     "wcfe_engine_launches": (C.c_uint64, [C.c_void_p]),
+    "wcfe_engine_stream": (C.c_void_p, [C.c_void_p]),
+    "wcfe_debug_pipe_rates": (C.c_int, [_d, _d, _d]),
     "wcfe_engine_step_times": (C.c_int64, [C.c_void_p, C.POINTER(C.c_float), C.c_int64, C.POINTER(C.c_float)]),
     "wcfe_engine_total_vertices": (C.c_int64, [C.c_void_p]),
     "wcfe_engine_predict": (C.c_int, [C.c_void_p, C.c_double, _d]),
@@ -86,7 +90,11 @@ SIGNATURES = {
     "wcfe_server_iterate": (C.c_int, [C.c_void_p, _i, _i]),
     "wcfe_server_result": (C.c_int, [C.c_void_p, C.c_int64, _d, _d]),
     "wcfe_server_step_times": (C.c_int64, [C.c_void_p, _d, C.c_int64]),
+    "wcfe_server_set_iteration_ms": (C.c_int, [C.c_void_p, C.c_double]),
+    "wcfe_server_cell_steps": (C.c_uint64, [C.c_void_p]),
     "wcfe_engine_set_patch_kernel": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_engine_set_vertex_kernel": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_engine_get_kernels": (C.c_int, [C.c_void_p, _i, _i]),
     "wcfe_cell_set_element_mu": (C.c_int, [C.c_void_p, C.c_int32, _d]),
     "wcfe_cell_couple_substrate": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
     "wcfe_engine_step_implicit": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_void_p]),
@@ -154,6 +162,13 @@ def debug_patch_staging(tri, n_vert, emax=320):
     xinfo = xinfo[:4 * npv].reshape(npv, 4)
     return dict(np=npv, xinfo=xinfo, halo=halo, loc=loc.reshape(-1, 4),
                 max_ne=int(mx[0]), max_nvp=int(mx[1]), max_nh=int(mx[2]), max_nc=int(mx[3]))
+
+
+def pipe_rates():
+    """Measured TF32 tensor, FP64 and FP32 FMA rates of the current device (TFLOP/s)."""
+    a, b, c = C.c_double(), C.c_double(), C.c_double()
+    check(load().wcfe_debug_pipe_rates(C.byref(a), C.byref(b), C.byref(c)), "wcfe_debug_pipe_rates")
+    return {"tf32_tflops": a.value, "fp64_tflops": b.value, "fp32_tflops": c.value}
 
 
 def debug_lu_schedule(m: int, block: int = 512):
@@ -337,6 +352,15 @@ class Engine:
         """Mixed engines: 0 staged patch kernel where it fits, 1 plain (default)."""
         check(load().wcfe_engine_set_patch_kernel(self.h, kind), "wcfe_engine_set_patch_kernel")
 
+    def set_vertex_kernel(self, kind: int):
+        check(load().wcfe_engine_set_vertex_kernel(self.h, kind), "wcfe_engine_set_vertex_kernel")
+
+    def kernels(self):
+        """(patch kernel kind, vertex kernel kind) in use."""
+        a, b = C.c_int32(), C.c_int32()
+        check(load().wcfe_engine_get_kernels(self.h, C.byref(a), C.byref(b)), "wcfe_engine_get_kernels")
+        return a.value, b.value
+
     def shape(self):
         a, b = C.c_int32(), C.c_int32()
         check(load().wcfe_engine_get_shape(self.h, C.byref(a), C.byref(b)), "wcfe_engine_get_shape")
@@ -347,6 +371,10 @@ class Engine:
 
     def launches(self) -> int:
         return int(load().wcfe_engine_launches(self.h))
+
+    def stream_ptr(self) -> int:
+        """The engine's main cudaStream_t as an integer (torch.cuda.ExternalStream)."""
+        return int(load().wcfe_engine_stream(self.h) or 0)
 
     def total_vertices(self) -> int:
         return int(load().wcfe_engine_total_vertices(self.h))
@@ -450,6 +478,14 @@ class Cell:
 
     def set_clock(self, t: float, ap_calls: int):
         check(load().wcfe_cell_set_clock(self.eng.h, self.id, t, ap_calls), "wcfe_cell_set_clock")
+
+    def set_step_budget(self, steps: int):
+        check(load().wcfe_cell_set_step_budget(self.eng.h, self.id, steps), "wcfe_cell_set_step_budget")
+
+    def step_budget(self) -> int:
+        b = C.c_int32()
+        check(load().wcfe_cell_get_step_budget(self.eng.h, self.id, C.byref(b)), "wcfe_cell_get_step_budget")
+        return b.value
 
     def clock(self):
         t = C.c_double()

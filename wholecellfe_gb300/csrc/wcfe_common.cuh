@@ -48,6 +48,30 @@ __device__ __forceinline__ void predict_vertex(const double4& x, const double4& 
     xn[2] = xa(x.z, xm(dt, vh[2]));
 }
 
+// The radial protrusion driver (wcfe_params.protrude_v, the oracle's wo_drive_protrusion;
+// the reference's velocity drivers prescribe the half-step velocity of driven nodes the
+// same way, driverVelocities_Uniaxial UL:125-168): a boundary vertex moves radially from
+// (protrude_cx, protrude_cy) at protrude_v, V_hlf = v (X - c) / |X - c| in the plane.
+__device__ __forceinline__ void drive_protrusion(const wcfe_params& p, bool boundary, const double4& x, double dt,
+                                                 double vh[3], double xn[3]) {
+    if (p.protrude_v == 0.0 || !boundary) return;
+    const double dx = xs(x.x, p.protrude_cx), dy = xs(x.y, p.protrude_cy);
+    const double r = __dsqrt_rn(xa(xm(dx, dx), xm(dy, dy)));
+    if (r == 0.0) return;
+    vh[0] = xm(p.protrude_v, __ddiv_rn(dx, r));
+    vh[1] = xm(p.protrude_v, __ddiv_rn(dy, r));
+    vh[2] = 0.0;
+    xn[0] = xa(x.x, xm(dt, vh[0]));
+    xn[1] = xa(x.y, xm(dt, vh[1]));
+    xn[2] = xa(x.z, xm(dt, vh[2]));
+}
+// predict_vertex with the cell's driver applied to vertex v
+__device__ __forceinline__ void predict_vertex_c(const CellDev& c, int v, const double4& x, const double4& V,
+                                                 const double4& A, double dt, double hdt, double vh[3], double xn[3]) {
+    predict_vertex(x, V, A, dt, hdt, vh, xn);
+    drive_protrusion(c.prm, c.bnd_rank[v] >= 0, x, dt, vh, xn);
+}
+
 // MD force-extension fit, UL:1203-1214
 static __constant__ double c_md_px[6] = {0., 2.51250583e-03, 4.40265201e-03, 5.91408228e-03, 11.76817302e-03, 17.001e-03};
 static __constant__ double c_md_py[6] = {-7.15514497, 71.80501308, 356.62420075, 356.96656556, 126.21811585, 528.40481124};
@@ -78,15 +102,15 @@ __device__ __forceinline__ void spring_force(const wcfe_params& p, double ux, do
         }
         if (j >= 0) mag = c_md_py[j] + c_md_k[j] * xs(D, c_md_px[j]);
     } else if (p.force_law == WCFE_LAW_LINEAR) {
-        mag = p.k_lin * (D - p.rest_len);
+        mag = D > p.rest_len ? p.k_lin * (D - p.rest_len) : 0.0;   // slack below the rest length
     } else {
         double e = D - p.rest_len;
-        mag = p.poly_k0 * (e + e * e * e / (3.0 * p.poly_x0 * p.poly_x0));
+        mag = e > 0.0 ? p.poly_k0 * (e + e * e * e / (3.0 * p.poly_x0 * p.poly_x0)) : 0.0;
     }
     fs[0] = mag * dx; fs[1] = mag * dy; fs[2] = mag * dz;
     if (p.force_law == WCFE_LAW_LINEAR && p.linear_norm2d) {
         double D2 = __dsqrt_rn(xa(xm(ux, ux), xm(uy, uy)));
-        *bell = fabs(p.k_lin * (D2 - p.rest_len));
+        *bell = D2 > p.rest_len ? p.k_lin * (D2 - p.rest_len) : 0.0;
     } else {
         *bell = sqrt(fs[0] * fs[0] + fs[1] * fs[1] + fs[2] * fs[2]);
     }

@@ -53,6 +53,8 @@ struct ParamF {
     int32_t norm2d;
     // low parts (x - RN(x)) of the constants the Bell force and rate use in float-float
     float k_lin_lo, rest_len_lo, poly_k0_lo, poly_c3_lo, iFa_lo, iFb_lo;
+    // the radial protrusion driver (wcfe_params.protrude_v, _cx, _cy) as float-float pairs
+    float pv, pv_lo, pcx, pcx_lo, pcy, pcy_lo;
 };
 
 struct CellDev {
@@ -93,7 +95,8 @@ struct CellDev {
     const int32_t* bnd_vert;    // [nb] boundary vertices in rank order (the inverse of bnd_rank)
     // control words, advanced by the last patch-phase CTA of the cell to finish a step:
     int32_t* ctl;               // [0] parity (which pos/ea buffer holds the step-start state), [1] patch-phase
-                                //     CTA ticket, [2] vertex-phase block ticket
+                                //     CTA ticket, [2] vertex-phase block ticket, [3] step budget (serving):
+                                //     0 unlimited, n > 0 steps left, -1 done (every kernel skips the cell)
     double* clk;                // [0] simulation time at the start of the next step
     unsigned long long* ap;     // [0] calculateForce_AP calls made (the AP counter of the next step)
     uint32_t* status;
@@ -103,6 +106,18 @@ struct CellDev {
     wcfe_params prm;
     ParamF pf;
 };
+
+#ifdef __CUDACC__
+// The step budget ctl[3] of a cell.  A kernel reads it before any work on the cell; the
+// last patch-phase CTA of the cell's step (after every other CTA of that cell finished the
+// step) counts it down, so all work of one launch sees the same value and a cell with n
+// steps left runs exactly n more steps, however many are queued.
+__device__ __forceinline__ bool cell_done(const CellDev& c) { return c.ctl[3] < 0; }
+__device__ __forceinline__ void count_step(const CellDev& c) {
+    const int32_t b = c.ctl[3];
+    if (b > 0) c.ctl[3] = b > 1 ? b - 1 : -1;
+}
+#endif
 
 inline ParamF make_paramf(const wcfe_params& p) {
     ParamF f{};
@@ -124,6 +139,12 @@ inline ParamF make_paramf(const wcfe_params& p) {
           : PF_POLY;
     f.norm2d = p.linear_norm2d ? 1 : 0;
     auto lo = [](double x) { return (float)(x - (double)(float)x); };
+    f.pv = (float)p.protrude_v;
+    f.pv_lo = lo(p.protrude_v);
+    f.pcx = (float)p.protrude_cx;
+    f.pcx_lo = lo(p.protrude_cx);
+    f.pcy = (float)p.protrude_cy;
+    f.pcy_lo = lo(p.protrude_cy);
     f.k_lin_lo = lo(p.k_lin);
     f.rest_len_lo = lo(p.rest_len);
     f.poly_k0_lo = lo(p.poly_k0);

@@ -13,11 +13,13 @@
 #include <map>
 #include <memory>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/wcfe.h"
 #include "wcfe_device.cuh"
 #include "wcfe_frames.h"
+#include "wcfe_serving.h"
 #include "wcfe_topology.h"
 
 namespace wcfe {
@@ -30,11 +32,16 @@ bool launch_patch_staged(const CellDev* cells, const WorkItem* work, int nwork, 
                          int cap_nc, double dt, double dt_real, double ap_thresh, double t_override, int vh_from_buf,
                          int num_sms, cudaStream_t st);
 size_t patch_smem_bytes(int prec, int mode, int emax);
+size_t mixed_smem_bytes(int emax);
+int mixed_occupancy(int threads, size_t smem, int kind);
+void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt, double dt_real,
+                        double ap_thresh, double t_override, int vh_from_buf, int threads, int grid, cudaStream_t st,
+                        int kind);
 int patch_occupancy(int prec, int threads, size_t smem);
 int vertex_occupancy(int threads);
 bool mixed_available();
 void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
-                         int threads, cudaStream_t st, const double* stage_in, double* stage_out);
+                         int threads, cudaStream_t st, const double* stage_in, double* stage_out, int kind = 0);
 void launch_patch(int prec, int mode, const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt,
                   double dt_real, double ap_thresh, double t_override, int vh_from_buf, const double* centroid_dev,
                   double* o0, double* o1, double* o2, double* o3, double* o4, int threads, int grid, cudaStream_t st,
@@ -191,6 +198,7 @@ struct wcfe_engine {
     int patch_threads = 128;
     int patch_emax = 320;
     int vblock = 256;             // vertices (threads) per vertex-phase block
+    int vertex_kind = 0;          // mixed form: vertex-phase kernel for 5 (0) or 4 (1) blocks per SM
     int patch_kernel = 1;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
     int lu_nb = 512, lu_kind = 0; // implicit step's LU: outer block width, 0 tcgen05 / 1 mma.sync updates
     int lu_reuse = 1;             // 1: factor once per implicit step, 0: every Newton iteration
@@ -208,6 +216,11 @@ struct wcfe_engine {
     float ms_v = 0, ms_p = 0, ms_span = 0;
     std::vector<float> step_ms;
     uint64_t launches = 0;
+    // serving: tables uploaded without a host synchronisation, from two pinned buffers
+    void* h_tab[2] = {nullptr, nullptr};
+    size_t h_tab_cap[2] = {0, 0};
+    cudaEvent_t tab_ev[2] = {nullptr, nullptr};
+    int tab_buf = 0;
 };
 
 namespace {
@@ -329,27 +342,15 @@ double* dev_stage(wcfe_engine* e, size_t bytes) {
     return e->d_stage;
 }
 
-// upload the whole static part of a cell (topology) and zero the state
-int upload_cell_topology(wcfe_engine* e, Cell* c) {
+// the device pointers of a cell's state block (layout state_layout)
+void bind_state(Cell* c, char* b, const size_t* off, int32_t nk1, int32_t vblock, bool mixed) {
     const Topology& T = c->topo;
-    int32_t ncand = (int32_t)(T.bnd_cand.size() / 2);
-    int32_t nk1 = nk1_of(T.nv, T.nt, e->vblock);
-    size_t off[32];
-    size_t bytes = state_layout(T.nv, T.nt, T.nb, ncand, nk1, e->prec == WCFE_PREC_MIXED, off);
-    if (c->state_block && c->state_bytes != bytes) dev_free(e, c->state_block, c->state_bytes);
-    if (!c->state_block) {
-        int r = dev_alloc(e, &c->state_block, bytes);
-        if (r) return r;
-        c->state_bytes = bytes;
-    }
-    char* b = (char*)c->state_block;
-    CK(cudaMemsetAsync(b, 0, bytes, e->stream));
     CellDev& d = c->dev;
     d.nv = T.nv;
     d.nt = T.nt;
     d.nb = T.nb;
     d.nk1 = nk1;
-    d.vb = e->vblock;
+    d.vb = vblock;
     d.pos[0] = (double4*)(b + off[0]);
     d.pos[1] = (double4*)(b + off[1]);
     d.vel = (double4*)(b + off[2]);
@@ -370,35 +371,116 @@ int upload_cell_topology(wcfe_engine* e, Cell* c) {
     d.clk = (double*)(b + off[17]);
     d.ap = (unsigned long long*)(b + off[18]);
     d.status = (uint32_t*)(b + off[19]);
-    d.rec = e->prec == WCFE_PREC_MIXED ? (float4*)(b + off[20]) : nullptr;
+    d.rec = mixed ? (float4*)(b + off[20]) : nullptr;
     d.area4 = (double*)(b + off[23]);
     d.bnd_vert = (const int32_t*)(b + off[24]);
     d.stepc = (float4*)(b + off[25]);
     d.bnd_optr = (const int32_t*)(b + off[21]);
     d.bnd_out = (const int32_t*)(b + off[22]);
-    if ((int64_t)T.bnd_out.size() > std::max<int64_t>(2 * (int64_t)T.nb, 1)) return fail("non-manifold boundary", WCFE_ERR_TOPOLOGY);
-    CK(cudaMemcpyAsync((void*)d.bnd_optr, T.bnd_optr.data(), sizeof(int32_t) * (T.nb + 1), cudaMemcpyHostToDevice, e->stream));
-    if (!T.bnd_out.empty())
-        CK(cudaMemcpyAsync((void*)d.bnd_out, T.bnd_out.data(), sizeof(int32_t) * T.bnd_out.size(), cudaMemcpyHostToDevice, e->stream));
-    if (T.nb > 0) {
-        std::vector<int32_t> bv(T.nb);
-        for (int v = 0; v < T.nv; ++v)
-            if (T.bnd_rank[v] >= 0) bv[T.bnd_rank[v]] = v;
-        CK(cudaMemcpyAsync((void*)d.bnd_vert, bv.data(), sizeof(int32_t) * T.nb, cudaMemcpyHostToDevice, e->stream));
-    }
-    // topology arrays
-    std::vector<int4> t4(T.nt);
+}
+
+// host images of a cell's derived static arrays
+void tri4_of(const Topology& T, std::vector<int4>& t4) {
+    t4.resize(T.nt);
     for (int t = 0; t < T.nt; ++t) t4[t] = make_int4(T.tri[3 * t], T.tri[3 * t + 1], T.tri[3 * t + 2], 0);
-    CK(cudaMemcpyAsync((void*)d.tri, t4.data(), sizeof(int4) * T.nt, cudaMemcpyHostToDevice, e->stream));
-    CK(cudaMemcpyAsync((void*)d.vt_ptr, T.vt_ptr.data(), sizeof(int32_t) * (T.nv + 1), cudaMemcpyHostToDevice, e->stream));
-    CK(cudaMemcpyAsync((void*)d.bnd_rank, T.bnd_rank.data(), sizeof(int32_t) * T.nv, cudaMemcpyHostToDevice, e->stream));
-    CK(cudaMemcpyAsync((void*)d.bnd_cptr, T.bnd_cptr.data(), sizeof(int32_t) * (T.nb + 1), cudaMemcpyHostToDevice, e->stream));
-    if (ncand)
-        CK(cudaMemcpyAsync((void*)d.bnd_cand, T.bnd_cand.data(), sizeof(int2) * ncand, cudaMemcpyHostToDevice, e->stream));
-    // reference start state: c_A = 100 (cellBP/main.cpp:674-677)
-    std::vector<double> ca(T.nv, 100.0);
-    CK(cudaMemcpyAsync(d.cA, ca.data(), sizeof(double) * T.nv, cudaMemcpyHostToDevice, e->stream));
+}
+void bnd_vert_of(const Topology& T, std::vector<int32_t>& bv) {
+    bv.assign(T.nb, 0);
+    for (int v = 0; v < T.nv; ++v)
+        if (T.bnd_rank[v] >= 0) bv[T.bnd_rank[v]] = v;
+}
+// c_A = 100 at the start (cellBP/main.cpp:674-677), in the engine's layout: binary64, or a
+// float-float hi plane then lo plane
+void ca_init_of(int32_t nv, bool mixed, std::vector<double>& buf) {
+    if (!mixed) {
+        buf.assign(nv, 100.0);
+        return;
+    }
+    buf.assign(nv, 0.0);   // 2 nv floats in the same bytes
+    float* f = reinterpret_cast<float*>(buf.data());
+    for (int v = 0; v < nv; ++v) f[v] = 100.0f;
+}
+
+// topology arrays of the bound state block, copied on stream st; the host sources must
+// stay unchanged until the copies have run
+int upload_state_arrays(Cell* c, cudaStream_t st, const std::vector<int4>& t4, const std::vector<int32_t>& bv,
+                        const std::vector<double>& ca) {
+    const Topology& T = c->topo;
+    CellDev& d = c->dev;
+    const int32_t ncand = (int32_t)(T.bnd_cand.size() / 2);
+    CK(cudaMemcpyAsync((void*)d.bnd_optr, T.bnd_optr.data(), sizeof(int32_t) * (T.nb + 1), cudaMemcpyHostToDevice, st));
+    if (!T.bnd_out.empty())
+        CK(cudaMemcpyAsync((void*)d.bnd_out, T.bnd_out.data(), sizeof(int32_t) * T.bnd_out.size(), cudaMemcpyHostToDevice, st));
+    if (T.nb > 0) CK(cudaMemcpyAsync((void*)d.bnd_vert, bv.data(), sizeof(int32_t) * T.nb, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void*)d.tri, t4.data(), sizeof(int4) * T.nt, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void*)d.vt_ptr, T.vt_ptr.data(), sizeof(int32_t) * (T.nv + 1), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void*)d.bnd_rank, T.bnd_rank.data(), sizeof(int32_t) * T.nv, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void*)d.bnd_cptr, T.bnd_cptr.data(), sizeof(int32_t) * (T.nb + 1), cudaMemcpyHostToDevice, st));
+    if (ncand) CK(cudaMemcpyAsync((void*)d.bnd_cand, T.bnd_cand.data(), sizeof(int2) * ncand, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(d.cA, ca.data(), sizeof(double) * T.nv, cudaMemcpyHostToDevice, st));
+    return WCFE_OK;
+}
+
+// upload the whole static part of a cell (topology) and zero the state
+int upload_cell_topology(wcfe_engine* e, Cell* c) {
+    const Topology& T = c->topo;
+    int32_t ncand = (int32_t)(T.bnd_cand.size() / 2);
+    int32_t nk1 = nk1_of(T.nv, T.nt, e->vblock);
+    size_t off[32];
+    const bool mixed = e->prec == WCFE_PREC_MIXED;
+    size_t bytes = state_layout(T.nv, T.nt, T.nb, ncand, nk1, mixed, off);
+    if (c->state_block && c->state_bytes != bytes) dev_free(e, c->state_block, c->state_bytes);
+    if (!c->state_block) {
+        int r = dev_alloc(e, &c->state_block, bytes);
+        if (r) return r;
+        c->state_bytes = bytes;
+    }
+    char* b = (char*)c->state_block;
+    CK(cudaMemsetAsync(b, 0, bytes, e->stream));
+    bind_state(c, b, off, nk1, e->vblock, mixed);
+    if ((int64_t)T.bnd_out.size() > std::max<int64_t>(2 * (int64_t)T.nb, 1)) return fail("non-manifold boundary", WCFE_ERR_TOPOLOGY);
+    std::vector<int4> t4;
+    std::vector<int32_t> bv;
+    std::vector<double> ca;
+    tri4_of(T, t4);
+    bnd_vert_of(T, bv);
+    ca_init_of(T.nv, mixed, ca);
+    int r = upload_state_arrays(c, e->stream, t4, bv, ca);
+    if (r) return r;
     CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+// the device pointers of a cell's patch block (layout patch_layout)
+void bind_patches(Cell* c, char* b, const size_t* off) {
+    c->dev.np = c->patches.np;
+    c->dev.patch = (const int4*)(b + off[0]);
+    c->dev.patch_elems = (const int32_t*)(b + off[1]);
+    c->dev.vc_code = (const uint16_t*)(b + off[2]);
+    c->dev.patch_x = (const int4*)(b + off[3]);
+    c->dev.patch_halo = (const int32_t*)(b + off[4]);
+    c->dev.patch_loc = (const uint16_t*)(b + off[5]);
+    c->dev.patch_tri = (const int4*)(b + off[6]);
+}
+// each element slot with its triangle's vertices (one load instead of two dependent ones)
+void patch_tri_of(const Patches& P, const Topology& T, std::vector<int4>& pt) {
+    pt.resize(P.elems.size());
+    for (size_t k = 0; k < P.elems.size(); ++k) {
+        const int32_t el = P.elems[k];
+        pt[k] = make_int4(T.tri[3 * el], T.tri[3 * el + 1], T.tri[3 * el + 2], el);
+    }
+}
+int upload_patch_arrays(Cell* c, cudaStream_t st, const std::vector<int4>& pt) {
+    const Patches& P = c->patches;
+    if (!pt.empty())
+        CK(cudaMemcpyAsync((void*)c->dev.patch_tri, pt.data(), sizeof(int4) * pt.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void*)c->dev.patch, P.patch.data(), sizeof(int32_t) * P.patch.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void*)c->dev.patch_elems, P.elems.data(), sizeof(int32_t) * P.elems.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void*)c->dev.vc_code, P.vc_code.data(), sizeof(uint16_t) * P.vc_code.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void*)c->dev.patch_x, P.xinfo.data(), sizeof(int32_t) * P.xinfo.size(), cudaMemcpyHostToDevice, st));
+    if (!P.halo.empty())
+        CK(cudaMemcpyAsync((void*)c->dev.patch_halo, P.halo.data(), sizeof(int32_t) * P.halo.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync((void*)c->dev.patch_loc, P.loc.data(), sizeof(uint16_t) * P.loc.size(), cudaMemcpyHostToDevice, st));
     return WCFE_OK;
 }
 
@@ -416,33 +498,11 @@ int upload_cell_patches(wcfe_engine* e, Cell* c) {
     }
     char* b = (char*)c->patch_block;
     CK(cudaMemsetAsync(b, 0, bytes, e->stream));
-    c->dev.np = P.np;
-    c->dev.patch = (const int4*)(b + off[0]);
-    c->dev.patch_elems = (const int32_t*)(b + off[1]);
-    c->dev.vc_code = (const uint16_t*)(b + off[2]);
-    c->dev.patch_x = (const int4*)(b + off[3]);
-    c->dev.patch_halo = (const int32_t*)(b + off[4]);
-    c->dev.patch_loc = (const uint16_t*)(b + off[5]);
-    c->dev.patch_tri = (const int4*)(b + off[6]);
-    {   // each element slot with its triangle's vertices (one load instead of two dependent ones)
-        std::vector<int4> pt(P.elems.size());
-        const std::vector<int32_t>& T = c->topo.tri;
-        for (size_t k = 0; k < P.elems.size(); ++k) {
-            const int32_t el = P.elems[k];
-            pt[k] = make_int4(T[3 * el], T[3 * el + 1], T[3 * el + 2], el);
-        }
-        if (!pt.empty())
-            CK(cudaMemcpyAsync((void*)c->dev.patch_tri, pt.data(), sizeof(int4) * pt.size(), cudaMemcpyHostToDevice,
-                               e->stream));
-        CK(cudaStreamSynchronize(e->stream));   // pt is a local buffer
-    }
-    CK(cudaMemcpyAsync((void*)c->dev.patch, P.patch.data(), sizeof(int32_t) * P.patch.size(), cudaMemcpyHostToDevice, e->stream));
-    CK(cudaMemcpyAsync((void*)c->dev.patch_elems, P.elems.data(), sizeof(int32_t) * P.elems.size(), cudaMemcpyHostToDevice, e->stream));
-    CK(cudaMemcpyAsync((void*)c->dev.vc_code, P.vc_code.data(), sizeof(uint16_t) * P.vc_code.size(), cudaMemcpyHostToDevice, e->stream));
-    CK(cudaMemcpyAsync((void*)c->dev.patch_x, P.xinfo.data(), sizeof(int32_t) * P.xinfo.size(), cudaMemcpyHostToDevice, e->stream));
-    if (!P.halo.empty())
-        CK(cudaMemcpyAsync((void*)c->dev.patch_halo, P.halo.data(), sizeof(int32_t) * P.halo.size(), cudaMemcpyHostToDevice, e->stream));
-    CK(cudaMemcpyAsync((void*)c->dev.patch_loc, P.loc.data(), sizeof(uint16_t) * P.loc.size(), cudaMemcpyHostToDevice, e->stream));
+    bind_patches(c, b, off);
+    std::vector<int4> pt;
+    patch_tri_of(P, c->topo, pt);
+    int r = upload_patch_arrays(c, e->stream, pt);
+    if (r) return r;
     CK(cudaStreamSynchronize(e->stream));
     return WCFE_OK;
 }
@@ -534,6 +594,8 @@ int ensure_dev(T** p, size_t* cap, size_t n) {
 
 int table_index(wcfe_engine* e, int32_t id);
 
+int build_tables(wcfe_engine* e);
+
 int sync_tables(wcfe_engine* e, double dt = -1.0) {
     if (dt > 0 && dt != e->table_dt) {
         e->table_dt = dt;
@@ -541,6 +603,35 @@ int sync_tables(wcfe_engine* e, double dt = -1.0) {
         invalidate_graph(e);
     }
     if (e->table_version == e->version) return WCFE_OK;
+    int r = build_tables(e);
+    if (r) return r;
+    if ((r = ensure_dev(&e->d_table, &e->d_table_cap, std::max<size_t>(e->table.size(), 1)))) return r;
+    if ((r = ensure_dev(&e->d_k1, &e->d_k1_cap, std::max<size_t>(e->k1.size(), 1)))) return r;
+    if ((r = ensure_dev(&e->d_k2, &e->d_k2_cap, std::max<size_t>(e->k2.size(), 1)))) return r;
+    // coupled cells point at their substrate's table entry (device address, known now)
+    for (size_t ti = 0; ti < e->table.size(); ++ti) {
+        const Cell* c = e->cells.at(e->order[ti]).get();
+        if (c->couple_sub < 0) continue;
+        auto it = e->cells.find(c->couple_sub);
+        if (it == e->cells.end()) return fail("coupled substrate cell no longer exists", WCFE_ERR_STATE);
+        const int ts = table_index(e, c->couple_sub);
+        SubDev& sd = e->table[ti].sub;
+        sd.scell = e->d_table + ts;
+        sd.fext = (unsigned long long*)it->second->fext_block;
+    }
+    if (!e->table.empty())
+        CK(cudaMemcpyAsync(e->d_table, e->table.data(), sizeof(CellDev) * e->table.size(), cudaMemcpyHostToDevice, e->stream));
+    if (!e->k1.empty())
+        CK(cudaMemcpyAsync(e->d_k1, e->k1.data(), sizeof(WorkItem) * e->k1.size(), cudaMemcpyHostToDevice, e->stream));
+    if (!e->k2.empty())
+        CK(cudaMemcpyAsync(e->d_k2, e->k2.data(), sizeof(WorkItem) * e->k2.size(), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    e->table_version = e->version;
+    return WCFE_OK;
+}
+
+// the host tables of the live cells: the table entries, the work lists, the staging caps
+int build_tables(wcfe_engine* e) {
     e->order.clear();
     e->table.clear();
     e->total_nv = 0;
@@ -575,29 +666,6 @@ int sync_tables(wcfe_engine* e, double dt = -1.0) {
     }
     e->n2_sub = (int)k2_sub.size();
     e->k2.insert(e->k2.end(), k2_sub.begin(), k2_sub.end());
-    int r;
-    if ((r = ensure_dev(&e->d_table, &e->d_table_cap, std::max<size_t>(e->table.size(), 1)))) return r;
-    // coupled cells point at their substrate's table entry (device address, known now)
-    for (size_t ti = 0; ti < e->table.size(); ++ti) {
-        const Cell* c = e->cells.at(e->order[ti]).get();
-        if (c->couple_sub < 0) continue;
-        auto it = e->cells.find(c->couple_sub);
-        if (it == e->cells.end()) return fail("coupled substrate cell no longer exists", WCFE_ERR_STATE);
-        const int ts = table_index(e, c->couple_sub);
-        SubDev& sd = e->table[ti].sub;
-        sd.scell = e->d_table + ts;
-        sd.fext = (unsigned long long*)it->second->fext_block;
-    }
-    if ((r = ensure_dev(&e->d_k1, &e->d_k1_cap, std::max<size_t>(e->k1.size(), 1)))) return r;
-    if ((r = ensure_dev(&e->d_k2, &e->d_k2_cap, std::max<size_t>(e->k2.size(), 1)))) return r;
-    if (!e->table.empty())
-        CK(cudaMemcpyAsync(e->d_table, e->table.data(), sizeof(CellDev) * e->table.size(), cudaMemcpyHostToDevice, e->stream));
-    if (!e->k1.empty())
-        CK(cudaMemcpyAsync(e->d_k1, e->k1.data(), sizeof(WorkItem) * e->k1.size(), cudaMemcpyHostToDevice, e->stream));
-    if (!e->k2.empty())
-        CK(cudaMemcpyAsync(e->d_k2, e->k2.data(), sizeof(WorkItem) * e->k2.size(), cudaMemcpyHostToDevice, e->stream));
-    CK(cudaStreamSynchronize(e->stream));
-    e->table_version = e->version;
     return WCFE_OK;
 }
 
@@ -612,7 +680,8 @@ int rec_flag(const wcfe_engine* e) { return e->prec == WCFE_PREC_MIXED ? VP_RECO
 // vertex phase of the engine's arithmetic form (the mixed form has its own kernel)
 void vphase(const wcfe_engine* e, const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
             cudaStream_t st, const double* stage_in = nullptr, double* stage_out = nullptr) {
-    if (e->prec == WCFE_PREC_MIXED) launch_vertex_mixed(cells, work, nwork, dt, flags, grid, e->vblock, st, stage_in, stage_out);
+    if (e->prec == WCFE_PREC_MIXED)
+        launch_vertex_mixed(cells, work, nwork, dt, flags, grid, e->vblock, st, stage_in, stage_out, e->vertex_kind);
     else launch_vertex_phase(cells, work, nwork, dt, flags, grid, e->vblock, st, stage_in, stage_out);
 }
 
@@ -637,10 +706,17 @@ void xjoin(wcfe_engine* e) {
 void patch_step(wcfe_engine* e, const WorkItem* k2, int n2, double dt, double dt_real, double apt, double t_override,
                 int vh_from_buf, cudaStream_t st = nullptr) {
     if (!st) st = e->stream;
-    if (e->prec == WCFE_PREC_MIXED && e->patch_kernel == 0 &&
-        launch_patch_staged(e->d_table, k2, n2, e->cap_ne, e->cap_nvp, e->cap_nh, e->cap_nc, dt, dt_real, apt,
-                            t_override, vh_from_buf, e->num_sms, st))
+    if (e->prec == WCFE_PREC_MIXED) {
+        if (e->patch_kernel == 0 &&
+            launch_patch_staged(e->d_table, k2, n2, e->cap_ne, e->cap_nvp, e->cap_nh, e->cap_nc, dt, dt_real, apt,
+                                t_override, vh_from_buf, e->num_sms, st))
+            return;
+        const int kind = e->patch_kernel == 0 ? 1 : e->patch_kernel;
+        const size_t smem = mixed_smem_bytes(e->patch_emax);
+        launch_patch_mixed(e->d_table, k2, n2, e->patch_emax, dt, dt_real, apt, t_override, vh_from_buf,
+                           e->patch_threads, grid_for(e, n2, mixed_occupancy(e->patch_threads, smem, kind)), st, kind);
         return;
+    }
     size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
     launch_patch(e->prec, PP_STEP, e->d_table, k2, n2, e->patch_emax, dt, dt_real, apt, t_override, vh_from_buf,
                  nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, e->patch_threads,
@@ -706,16 +782,32 @@ int get3(wcfe_engine* e, double* h, const double4* d, int n) {
 // (wcfe_mixed.cu): pos, vel, fau, vhl as hi float4[n] then lo float4[n]; acc as the
 // FP32 acceleration float4[n]; ea as hi float4[n] (xx yy zz xy), lo float4[n],
 // then float4[n] (xz hi, yz hi, xz lo, yz lo); cA, cC as hi float[n] then lo float[n].
+// Positions are triple-float (wcfe_ff.cuh): hi float4 (x.h, y.h, z.h, x.l) and lo float4
+// (x.m, y.m, z.m, y.l), exact for any binary64 input (z is 0 in the planar mixed form).
 // These convert on the host.
 inline void split_ff(double x, float* hi, float* lo) {
     const float h = (float)x;
     *hi = h;
     *lo = (float)(x - (double)h);
 }
+inline void split_tf(double x, float* h, float* m, float* l) {
+    *h = (float)x;
+    const double r = x - (double)*h;
+    *m = (float)r;
+    *l = (float)(r - (double)*m);
+}
 int put_ff(wcfe_engine* e, void* d, const double* h, int n, int kind) {
     const size_t N = (size_t)n;
     std::vector<float> b;
-    if (kind == 0 || kind == 1) {          // [n][3] vectors
+    if (kind == 4) {                       // [n][3] positions (triple-float x, y; float-float z)
+        b.assign(8 * N, 0.0f);
+        for (size_t v = 0; v < N; ++v) {
+            const double* q = h + 3 * v;
+            split_tf(q[0], &b[4 * v + 0], &b[4 * (N + v) + 0], &b[4 * v + 3]);
+            split_tf(q[1], &b[4 * v + 1], &b[4 * (N + v) + 1], &b[4 * (N + v) + 3]);
+            split_ff(q[2], &b[4 * v + 2], &b[4 * (N + v) + 2]);
+        }
+    } else if (kind == 0 || kind == 1) {   // [n][3] vectors
         b.assign((kind == 1 ? 4 : 8) * N, 0.0f);
         for (size_t v = 0; v < N; ++v)
             for (int k = 0; k < 3; ++k) {
@@ -740,13 +832,17 @@ int put_ff(wcfe_engine* e, void* d, const double* h, int n, int kind) {
 }
 int get_ff(wcfe_engine* e, double* h, const void* d, int n, int kind) {
     const size_t N = (size_t)n;
-    const size_t per = kind == 0 ? 8 : kind == 1 ? 4 : kind == 2 ? 12 : 2;
+    const size_t per = (kind == 0 || kind == 4) ? 8 : kind == 1 ? 4 : kind == 2 ? 12 : 2;
     std::vector<float> b(per * N);
     CK(cudaMemcpyAsync(b.data(), d, sizeof(float) * b.size(), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     auto ffd = [](float hi, float lo) { return (double)hi + (double)lo; };
     for (size_t v = 0; v < N; ++v) {
-        if (kind == 0) for (int k = 0; k < 3; ++k) h[3 * v + k] = ffd(b[4 * v + k], b[4 * (N + v) + k]);
+        if (kind == 4) {   // (h + m) is exact in binary64; one rounding for + l
+            h[3 * v] = ffd(b[4 * v], b[4 * (N + v)]) + (double)b[4 * v + 3];
+            h[3 * v + 1] = ffd(b[4 * v + 1], b[4 * (N + v) + 1]) + (double)b[4 * (N + v) + 3];
+            h[3 * v + 2] = ffd(b[4 * v + 2], b[4 * (N + v) + 2]);
+        } else if (kind == 0) for (int k = 0; k < 3; ++k) h[3 * v + k] = ffd(b[4 * v + k], b[4 * (N + v) + k]);
         else if (kind == 1) for (int k = 0; k < 3; ++k) h[3 * v + k] = (double)b[4 * v + k];
         else if (kind == 2) {
             double* q = h + 6 * v;
@@ -757,7 +853,7 @@ int get_ff(wcfe_engine* e, double* h, const void* d, int n, int kind) {
     }
     return WCFE_OK;
 }
-enum { FF_VEC = 0, FF_ACC = 1, FF_EA = 2, FF_SCALAR = 3 };
+enum { FF_VEC = 0, FF_ACC = 1, FF_EA = 2, FF_SCALAR = 3, FF_POS = 4 };
 
 // the mixed form assumes a planar membrane with counter-clockwise triangles (its element
 // inputs drop z and its area comes from the boundary loop)
@@ -856,6 +952,10 @@ int wcfe_engine_destroy(wcfe_engine* e) {
     if (e->d_xchg) cudaFree(e->d_xchg);
     if (e->d_stage) cudaFree(e->d_stage);
     if (e->h_stage) cudaFreeHost(e->h_stage);
+    for (int k = 0; k < 2; ++k) {
+        if (e->h_tab[k]) cudaFreeHost(e->h_tab[k]);
+        if (e->tab_ev[k]) cudaEventDestroy(e->tab_ev[k]);
+    }
     for (auto& ev : e->ev)
         if (ev) cudaEventDestroy(ev);
     for (auto& ev : e->tev) cudaEventDestroy(ev);
@@ -1117,7 +1217,7 @@ int wcfe_cell_set_state(wcfe_engine* e, int32_t id, const double* x, const doubl
     CellDev& d = c->dev;
     if (x && e->prec == WCFE_PREC_MIXED && (r = check_planar_ccw(x, n, c->topo.tri))) return r;
     if (e->prec == WCFE_PREC_MIXED) {
-        if (x && (r = put_ff(e, d.pos[par], x, n, FF_VEC))) return r;
+        if (x && (r = put_ff(e, d.pos[par], x, n, FF_POS))) return r;
         if (V && (r = put_ff(e, d.vel, V, n, FF_VEC))) return r;
         if (A && (r = put_ff(e, d.acc, A, n, FF_ACC))) return r;
         if (fau && (r = put_ff(e, d.fau, fau, n, FF_VEC))) return r;
@@ -1150,7 +1250,7 @@ int wcfe_cell_get_state(wcfe_engine* e, int32_t id, double* x, double* V, double
     const int n = c->topo.nv;
     CellDev& d = c->dev;
     if (e->prec == WCFE_PREC_MIXED) {
-        if (x && (r = get_ff(e, x, d.pos[par], n, FF_VEC))) return r;
+        if (x && (r = get_ff(e, x, d.pos[par], n, FF_POS))) return r;
         if (V && (r = get_ff(e, V, d.vel, n, FF_VEC))) return r;
         if (A && (r = get_ff(e, A, d.acc, n, FF_ACC))) return r;
         if (fau && (r = get_ff(e, fau, d.fau, n, FF_VEC))) return r;
@@ -1166,6 +1266,26 @@ int wcfe_cell_get_state(wcfe_engine* e, int32_t id, double* x, double* V, double
     if (ea) CK(cudaMemcpyAsync(ea, d.ea[par], sizeof(double) * 6 * n, cudaMemcpyDeviceToHost, e->stream));
     if (cA) CK(cudaMemcpyAsync(cA, d.cA, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
     if (cC) CK(cudaMemcpyAsync(cC, d.cC, sizeof(double) * n, cudaMemcpyDeviceToHost, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_cell_set_step_budget(wcfe_engine* e, int32_t id, int32_t steps) {
+    xjoin(e);
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c || steps < 0) return fail("bad argument", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    CK(cudaMemcpyAsync(c->dev.ctl + 3, &steps, sizeof(int32_t), cudaMemcpyHostToDevice, e->stream));
+    CK(cudaStreamSynchronize(e->stream));
+    return WCFE_OK;
+}
+
+int wcfe_cell_get_step_budget(wcfe_engine* e, int32_t id, int32_t* steps) {
+    xjoin(e);
+    Cell* c = e ? find(e, id) : nullptr;
+    if (!c || !steps) return fail("bad argument", WCFE_ERR_ARG);
+    CK(cudaSetDevice(e->device));
+    CK(cudaMemcpyAsync(steps, c->dev.ctl + 3, sizeof(int32_t), cudaMemcpyDeviceToHost, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     return WCFE_OK;
 }
@@ -1540,9 +1660,25 @@ int wcfe_engine_set_lu_reuse(wcfe_engine* e, int32_t reuse) {
 
 int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind) {
     xjoin(e);
-    if (!e || kind < 0 || kind > 1) return fail("bad argument", WCFE_ERR_ARG);
+    if (!e || kind < 0 || kind > 4) return fail("bad argument", WCFE_ERR_ARG);
+    if (kind >= 2 && e->patch_threads != 128) return fail("register-capped patch kernels run 128 threads", WCFE_ERR_ARG);
     e->patch_kernel = kind;
     invalidate_graph(e);
+    return WCFE_OK;
+}
+
+int wcfe_engine_set_vertex_kernel(wcfe_engine* e, int32_t kind) {
+    xjoin(e);
+    if (!e || kind < 0 || kind > 1) return fail("bad argument", WCFE_ERR_ARG);
+    e->vertex_kind = kind;
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
+int wcfe_engine_get_kernels(const wcfe_engine* e, int32_t* patch_kind, int32_t* vertex_kind) {
+    if (!e) return WCFE_ERR_ARG;
+    if (patch_kind) *patch_kind = e->patch_kernel;
+    if (vertex_kind) *vertex_kind = e->vertex_kind;
     return WCFE_OK;
 }
 
@@ -1576,6 +1712,7 @@ int wcfe_engine_last_timing(wcfe_engine* e, float* ms_v, float* ms_p) {
 }
 
 uint64_t wcfe_engine_launches(const wcfe_engine* e) { return e ? e->launches : 0; }
+void* wcfe_engine_stream(const wcfe_engine* e) { return e ? (void*)e->stream : nullptr; }
 
 int wcfe_debug_topology(int32_t nv, int32_t nt, const int32_t* tri, const int32_t* vt_ptr, const int32_t* vt_idx,
                         const uint8_t* is_bnd, int32_t emax, int32_t* nb_out, int32_t* bnd_rank, int32_t* bnd_cptr,
@@ -2046,6 +2183,8 @@ int wcfe_engine_step_implicit(wcfe_engine* e, int32_t nsteps, double dt, double 
         return fail("the implicit step runs on an FP64 engine (WCFE_PREC_FP64)", WCFE_ERR_STATE);
     if (e && std::any_of(e->cells.begin(), e->cells.end(), [](const auto& kv) { return kv.second->is_sub; }))
         return fail("coupled substrates step only through wcfe_engine_step", WCFE_ERR_STATE);
+    if (std::any_of(e->cells.begin(), e->cells.end(), [](const auto& kv) { return kv.second->prm.protrude_v != 0.0; }))
+        return fail("the implicit step has no protrusion driver (params.protrude_v must be 0)", WCFE_ERR_ARG);
     if (stats) std::memset(stats, 0, sizeof *stats);
     if (e->cells.empty() || nsteps == 0) return WCFE_OK;
     CK(cudaSetDevice(e->device));
@@ -2356,13 +2495,16 @@ int wcfe_engine_autotune(wcfe_engine* e, double dt, int32_t reps) {
     bool was_timing = e->timing;
     e->timing = true;
     // mixed engines also try the staged patch kernel (its block shape is fixed; it uses emax)
-    const int nkinds = e->prec == WCFE_PREC_MIXED ? 2 : 1;
-    for (int kind = 1; kind >= 2 - nkinds; --kind) {
+    // and the plain kernel with register caps for 6, 7 and 8 CTAs of 128 threads per SM
+    std::vector<int> kinds = {1};
+    if (e->prec == WCFE_PREC_MIXED) kinds = {1, 2, 3, 4, 0};
+    for (int kind : kinds) {
         e->patch_kernel = kind;
         for (int em : emax_c) {
             if (patch_smem_bytes(e->prec, PP_RESIDUAL, em) + 1024 > (size_t)max_optin) continue;
             for (int th : threads_c) {
                 if (kind == 0 && th != threads_c[0]) continue;
+                if (kind >= 2 && th != 128) continue;
                 int r = wcfe_engine_set_shape(e, kind == 0 ? e->patch_threads : th, em);
                 if (r) continue;
                 wcfe_engine_step(e, 1, dt);  // warm
@@ -2376,9 +2518,23 @@ int wcfe_engine_autotune(wcfe_engine* e, double dt, int32_t reps) {
             }
         }
     }
-    e->timing = was_timing;
     e->patch_kernel = bk;
     int r = wcfe_engine_set_shape(e, bt, be);
+    if (!r && e->prec == WCFE_PREC_MIXED) {   // the vertex phase's register cap, at the chosen patch shape
+        float bestv = 1e30f;
+        int bv = 0;
+        for (int vk = 0; vk < 2; ++vk) {
+            e->vertex_kind = vk;
+            wcfe_engine_step(e, 1, dt);
+            if (wcfe_engine_step(e, reps, dt)) continue;
+            if (e->ms_v < bestv) { bestv = e->ms_v; bv = vk; }
+            for (auto& s : saved)
+                CK(cudaMemcpyAsync(s.first->state_block, s.second, s.first->state_bytes, cudaMemcpyDeviceToDevice,
+                                   e->stream));
+        }
+        e->vertex_kind = bv;
+    }
+    e->timing = was_timing;
     for (auto& s : saved) {
         cudaMemcpyAsync(s.first->state_block, s.second, s.first->state_bytes, cudaMemcpyDeviceToDevice, e->stream);
     }
@@ -2413,4 +2569,206 @@ int engine_frame_source(wcfe_engine* e, int32_t id, FrameSource* out) {
     out->device = e->device;
     return WCFE_OK;
 }
+}  // namespace wcfe
+
+// ---------------------------------------------------------------------------- serving (wcfe_server.cu)
+namespace wcfe {
+namespace {
+std::string planar_ccw_error(const double* x, int n, const std::vector<int32_t>& T) {
+    for (int v = 0; v < n; ++v)
+        if (x[3 * v + 2] != 0.0) return "the mixed form needs a planar membrane (z = 0)";
+    for (size_t t = 0; 3 * t < T.size(); ++t) {
+        const double* a = x + 3 * T[3 * t];
+        const double* b = x + 3 * T[3 * t + 1];
+        const double* q = x + 3 * T[3 * t + 2];
+        if ((b[0] - a[0]) * (q[1] - a[1]) - (b[1] - a[1]) * (q[0] - a[0]) <= 0)
+            return "the mixed form needs counter-clockwise, non-degenerate triangles";
+    }
+    return "";
+}
+
+// the tables into the device buffers without a host synchronisation: device buffers grow in
+// stream order, the host images go through one of two pinned buffers (reused once the copy
+// made from it two refreshes ago has run)
+int sync_tables_async(wcfe_engine* e, double dt) {
+    if (dt > 0 && dt != e->table_dt) {
+        e->table_dt = dt;
+        e->version++;
+        invalidate_graph(e);
+    }
+    if (e->table_version == e->version) return WCFE_OK;
+    for (auto& kv : e->cells)
+        if (kv.second->couple_sub >= 0 || kv.second->is_sub)
+            return fail("a serving engine holds no coupled substrates", WCFE_ERR_STATE);
+    int r = build_tables(e);
+    if (r) return r;
+    auto grow = [&](auto** p, size_t* cap, size_t n, size_t elem) -> int {
+        if (n <= *cap) return WCFE_OK;
+        const size_t c = std::max<size_t>(n, 2 * *cap);
+        void* q = nullptr;
+        if (cudaMallocAsync(&q, elem * c, e->stream) != cudaSuccess) {
+            cudaGetLastError();
+            return fail("cudaMallocAsync of a work list failed", WCFE_ERR_NOMEM);
+        }
+        if (*p) cudaFreeAsync(*p, e->stream);
+        *p = static_cast<std::remove_reference_t<decltype(**p)>*>(q);
+        *cap = c;
+        return WCFE_OK;
+    };
+    if ((r = grow(&e->d_table, &e->d_table_cap, std::max<size_t>(e->table.size(), 1), sizeof(CellDev)))) return r;
+    if ((r = grow(&e->d_k1, &e->d_k1_cap, std::max<size_t>(e->k1.size(), 1), sizeof(WorkItem)))) return r;
+    if ((r = grow(&e->d_k2, &e->d_k2_cap, std::max<size_t>(e->k2.size(), 1), sizeof(WorkItem)))) return r;
+    const size_t b0 = sizeof(CellDev) * e->table.size(), b1 = sizeof(WorkItem) * e->k1.size(),
+                 b2 = sizeof(WorkItem) * e->k2.size();
+    const int k = e->tab_buf;
+    e->tab_buf ^= 1;
+    if (!e->tab_ev[k]) CK(cudaEventCreateWithFlags(&e->tab_ev[k], cudaEventDisableTiming));
+    else CK(cudaEventSynchronize(e->tab_ev[k]));
+    if (b0 + b1 + b2 > e->h_tab_cap[k]) {
+        if (e->h_tab[k]) cudaFreeHost(e->h_tab[k]);
+        e->h_tab[k] = nullptr;
+        e->h_tab_cap[k] = 0;
+        const size_t cap = 2 * (b0 + b1 + b2) + 4096;
+        CK(cudaMallocHost(&e->h_tab[k], cap));
+        e->h_tab_cap[k] = cap;
+    }
+    char* h = static_cast<char*>(e->h_tab[k]);
+    std::memcpy(h, e->table.data(), b0);
+    std::memcpy(h + b0, e->k1.data(), b1);
+    std::memcpy(h + b0 + b1, e->k2.data(), b2);
+    if (b0) CK(cudaMemcpyAsync(e->d_table, h, b0, cudaMemcpyHostToDevice, e->stream));
+    if (b1) CK(cudaMemcpyAsync(e->d_k1, h + b0, b1, cudaMemcpyHostToDevice, e->stream));
+    if (b2) CK(cudaMemcpyAsync(e->d_k2, h + b0 + b1, b2, cudaMemcpyHostToDevice, e->stream));
+    CK(cudaEventRecord(e->tab_ev[k], e->stream));
+    e->table_version = e->version;
+    return WCFE_OK;
+}
+}  // namespace
+
+std::string serving_prepare(const wcfe_engine* e, PreparedCell& pc, int32_t nv, int32_t nt, const int32_t* tri,
+                            const double* x, const wcfe_params& prm, int32_t steps) {
+    pc.mixed = e->prec == WCFE_PREC_MIXED;
+    pc.prm = prm;
+    pc.steps = steps;
+    std::string err = build_topology(pc.topo, nv, nt, tri, nullptr, nullptr, nullptr);
+    if (!err.empty()) return err;
+    if (pc.mixed && !(err = planar_ccw_error(x, nv, pc.topo.tri)).empty()) return err;
+    const Topology& T = pc.topo;
+    if ((int64_t)T.bnd_out.size() > std::max<int64_t>(2 * (int64_t)T.nb, 1)) return "non-manifold boundary";
+    err = build_patches(pc.patches, T, e->patch_emax);
+    if (!err.empty()) return err;
+    const Patches& P = pc.patches;
+    pc.nk1 = nk1_of(T.nv, T.nt, e->vblock);
+    pc.state_bytes = state_layout(T.nv, T.nt, T.nb, (int32_t)(T.bnd_cand.size() / 2), pc.nk1, pc.mixed, pc.soff);
+    pc.patch_bytes = patch_layout(P.np, P.elems.size(), P.vc_code.size(), P.halo.size(), pc.poff);
+    tri4_of(T, pc.tri4);
+    bnd_vert_of(T, pc.bnd_vert);
+    patch_tri_of(P, T, pc.patch_tri);
+    ca_init_of(T.nv, pc.mixed, pc.ca);
+    // positions: binary64 double4, or the mixed form's triple-float planes (hi float4 then lo float4)
+    pc.pos.assign(4 * (size_t)nv, 0.0);
+    if (!pc.mixed) {
+        for (int v = 0; v < nv; ++v)
+            for (int k = 0; k < 3; ++k) pc.pos[4 * (size_t)v + k] = x[3 * (size_t)v + k];
+    } else {
+        float* f = reinterpret_cast<float*>(pc.pos.data());
+        const size_t N = (size_t)nv;
+        for (size_t v = 0; v < N; ++v) {
+            split_tf(x[3 * v], &f[4 * v + 0], &f[4 * (N + v) + 0], &f[4 * v + 3]);
+            split_tf(x[3 * v + 1], &f[4 * v + 1], &f[4 * (N + v) + 1], &f[4 * (N + v) + 3]);
+            split_ff(x[3 * v + 2], &f[4 * v + 2], &f[4 * (N + v) + 2]);
+        }
+    }
+    return "";
+}
+
+int serving_admit(wcfe_engine* e, PreparedCell& pc, cudaStream_t st, cudaMemPool_t pool, int32_t* id) {
+    CK(cudaSetDevice(e->device));
+    std::unique_ptr<Cell> c(new Cell());
+    c->topo = std::move(pc.topo);
+    c->patches = std::move(pc.patches);
+    c->prm = pc.prm;
+    void* sb = nullptr;
+    void* pb = nullptr;
+    if (cudaMallocFromPoolAsync(&sb, pc.state_bytes, pool, st) != cudaSuccess ||
+        cudaMallocFromPoolAsync(&pb, pc.patch_bytes, pool, st) != cudaSuccess) {
+        cudaGetLastError();
+        if (sb) cudaFreeAsync(sb, st);
+        return fail("cudaMallocFromPoolAsync failed", WCFE_ERR_NOMEM);
+    }
+    c->state_block = sb;
+    c->state_bytes = pc.state_bytes;
+    c->patch_block = pb;
+    c->patch_bytes = pc.patch_bytes;
+    CK(cudaMemsetAsync(sb, 0, pc.state_bytes, st));
+    CK(cudaMemsetAsync(pb, 0, pc.patch_bytes, st));
+    bind_state(c.get(), (char*)sb, pc.soff, pc.nk1, e->vblock, pc.mixed);
+    bind_patches(c.get(), (char*)pb, pc.poff);
+    int r = upload_state_arrays(c.get(), st, pc.tri4, pc.bnd_vert, pc.ca);
+    if (!r) r = upload_patch_arrays(c.get(), st, pc.patch_tri);
+    if (!r && cudaMemcpyAsync(c->dev.pos[0], pc.pos.data(), sizeof(double) * pc.pos.size(), cudaMemcpyHostToDevice,
+                              st) != cudaSuccess)
+        r = fail("cudaMemcpyAsync of the start positions failed", WCFE_ERR_CUDA);
+    if (!r && cudaMemcpyAsync(c->dev.ctl + 3, &pc.steps, sizeof(int32_t), cudaMemcpyHostToDevice, st) != cudaSuccess)
+        r = fail("cudaMemcpyAsync of the step budget failed", WCFE_ERR_CUDA);
+    if (r) {
+        cudaFreeAsync(sb, st);
+        cudaFreeAsync(pb, st);
+        return r;
+    }
+    e->used += pc.state_bytes + pc.patch_bytes;
+    c->id = e->next_id++;
+    *id = c->id;
+    e->cells[c->id] = std::move(c);
+    e->version++;
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
+int serving_step(wcfe_engine* e, int32_t nsteps, double dt) {
+    if (e->cells.empty() || nsteps <= 0) return WCFE_OK;
+    CK(cudaSetDevice(e->device));
+    int r = sync_tables_async(e, dt);
+    if (r) return r;
+    const int n1 = (int)e->k1.size(), n2 = (int)e->k2.size();
+    for (int s = 0; s < nsteps; ++s)
+        if ((r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt))) return r;
+    return WCFE_OK;
+}
+
+size_t serving_raw_bytes(int32_t nv) { return sizeof(double4) * (size_t)nv; }
+
+int serving_retire(wcfe_engine* e, int32_t id, int parity, void* pinned_dst, size_t cap, size_t* bytes) {
+    Cell* c = find(e, id);
+    if (!c) return fail("unknown cell", WCFE_ERR_ARG);
+    const size_t nb = serving_raw_bytes(c->topo.nv);
+    if (nb > cap) return fail("result buffer too small", WCFE_ERR_ARG);
+    CK(cudaMemcpyAsync(pinned_dst, c->dev.pos[parity & 1], nb, cudaMemcpyDeviceToHost, e->stream));
+    *bytes = nb;
+    free_cell(e, c);   // cudaFreeAsync on the engine stream: after the copy
+    e->cells.erase(id);
+    e->version++;
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
+void serving_decode_positions(const wcfe_engine* e, const void* raw, int32_t nv, double* x) {
+    const size_t N = (size_t)nv;
+    if (e->prec != WCFE_PREC_MIXED) {
+        const double* d = static_cast<const double*>(raw);
+        for (size_t v = 0; v < N; ++v)
+            for (int k = 0; k < 3; ++k) x[3 * v + k] = d[4 * v + k];
+        return;
+    }
+    const float* b = static_cast<const float*>(raw);   // hi float4 plane, then lo float4 plane
+    for (size_t v = 0; v < N; ++v) {
+        x[3 * v] = ((double)b[4 * v] + (double)b[4 * (N + v)]) + (double)b[4 * v + 3];
+        x[3 * v + 1] = ((double)b[4 * v + 1] + (double)b[4 * (N + v) + 1]) + (double)b[4 * (N + v) + 3];
+        x[3 * v + 2] = (double)b[4 * v + 2] + (double)b[4 * (N + v) + 2];
+    }
+}
+
+cudaStream_t engine_stream(const wcfe_engine* e) { return e->stream; }
+uint64_t engine_budget(const wcfe_engine* e) { return e->budget; }
+uint64_t engine_used(const wcfe_engine* e) { return e->used; }
 }  // namespace wcfe

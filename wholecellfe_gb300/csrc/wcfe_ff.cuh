@@ -76,6 +76,13 @@ WCFE_HD ff ff_mul(ff a, ff b) {
 WCFE_HD ff ff_fma_f(ff a, ff b, float c) { return ff_add(a, ff_mul_f(b, c)); }
 // a + b * c, both products' factors float-float
 WCFE_HD ff ff_fma(ff a, ff b, ff c) { return ff_add(a, ff_mul(b, c)); }
+// a / b, both float-float: the quotient of the high parts corrected by one step on the
+// remainder a - q b (Dekker's long division)
+WCFE_HD ff ff_div(ff a, ff b) {
+    const float q1 = a.hi / b.hi;
+    const ff r = ff_sub(a, ff_mul_f(b, q1));
+    return fast_two_sum(q1, r.hi / b.hi);
+}
 // square root: s = sqrt(hi) corrected by one Newton step on the exact residual
 WCFE_HD ff ff_sqrt(ff a) {
     if (!(a.hi > 0.0f)) return {0.0f, 0.0f};
@@ -104,6 +111,47 @@ WCFE_HD ff ffx(const ff4& v) { return {v.hx, v.lx}; }
 WCFE_HD ff ffy(const ff4& v) { return {v.hy, v.ly}; }
 WCFE_HD ff ffz(const ff4& v) { return {v.hz, v.lz}; }
 WCFE_HD ff4 make_ff4(ff x, ff y, ff z) { return {x.hi, y.hi, z.hi, 0.0f, x.lo, y.lo, z.lo, 0.0f}; }
+
+// ---- positions: triple-float --------------------------------------------------
+// A position coordinate is h + (m + l): a float h and a normalised float-float
+// remainder (m, l) with |m + l| <= ulp(h) / 2 or so, about 72 significant bits.  Any
+// binary64 value splits into it exactly, so a state set from doubles is held
+// exactly, and adding a step displacement d rounds only inside the remainder
+// (an absolute error near 2^-47 |m + d|, about 1e-20 um at cell scale, against
+// 2^-53 |x| = 1e-15 um for a binary64 position update).  The planar mixed form
+// keeps z = 0, so the third float of x and y lives in the w slots of the ff4
+// layout: hi float4 (x.h, y.h, 0, x.l), lo float4 (x.m, y.m, 0, y.l); ffx / ffy
+// then read the float-float (h, m) part unchanged.
+struct tf {
+    float h, m, l;
+};
+// x + d exactly but for the rounding of the remainder sum (m, l) + d
+WCFE_HD tf tf_add_ff(tf x, ff d) {
+    const ff r = ff_add({x.m, x.l}, d);
+    const ff s = two_sum(x.h, r.hi);
+    const ff n = two_sum(s.lo, r.lo);
+    return {s.hi, n.hi, n.lo};
+}
+// a - b as float-float (the displacement between two positions)
+WCFE_HD ff tf_sub(tf a, tf b) {
+    const ff s = two_sum(a.h, -b.h);
+    return ff_add(s, ff_sub({a.m, a.l}, {b.m, b.l}));
+}
+// the float-float part (h, m); the omitted l is below 2^-48 |x|
+WCFE_HD ff tf_ff(tf a) { return {a.h, a.m}; }
+// exact split of a binary64 value: h = RN(x), m = RN(x - h), l = x - h - m
+WCFE_HD tf tf_from_d(double x) {
+    const float h = f64_to_f32_rn(x);
+    const double r = x - f32_to_f64(h);
+    const float m = f64_to_f32_rn(r);
+    return {h, m, f64_to_f32_rn(r - f32_to_f64(m))};
+}
+// RN(h + m + l): h + m is exact in binary64, the one rounding is the last addition
+WCFE_HD double tf_to_d(tf a) { return (f32_to_f64(a.h) + f32_to_f64(a.m)) + f32_to_f64(a.l); }
+WCFE_HD tf tfx(const ff4& v) { return {v.hx, v.lx, v.hw}; }
+WCFE_HD tf tfy(const ff4& v) { return {v.hy, v.ly, v.lw}; }
+// the position layout above (z = 0 in the planar mixed form, kept as its float-float)
+WCFE_HD ff4 make_pos4(tf x, tf y, ff z) { return {x.h, y.h, z.hi, x.l, x.m, y.m, z.lo, y.l}; }
 
 // per-vertex strain: Voigt (xx, yy, zz, xy) hi and lo, then (xz, yz) hi and lo, 48 bytes
 struct alignas(16) ffea {

@@ -64,6 +64,7 @@ __global__ void __launch_bounds__(kK1Threads) k_vertex_phase(const CellDev* __re
     for (int w = blockIdx.x; w < nwork; w += gridDim.x) {
         const WorkItem it = work[w];
         const CellDev& c = cells[it.cell];
+        if (cell_done(c)) continue;   // block-uniform: a serving cell that ran its steps
         const int b = it.idx;
         const int nv = c.nv, nt = c.nt;
         const int par = c.ctl[0];
@@ -82,7 +83,7 @@ __global__ void __launch_bounds__(kK1Threads) k_vertex_phase(const CellDev* __re
                 st4(xo + v, xn[0], xn[1], xn[2]);
             } else if (flags & VP_PREDICT) {
                 double vh[3];
-                predict_vertex(Xv, ld4(c.vel + v), ld4(c.acc + v), dt, hdt, vh, xn);
+                predict_vertex_c(c, v, Xv, ld4(c.vel + v), ld4(c.acc + v), dt, hdt, vh, xn);
                 st4(xo + v, xn[0], xn[1], xn[2]);
                 if (flags & VP_EXPORT) {
                     st4(c.vhl + v, vh[0], vh[1], vh[2]);
@@ -166,7 +167,8 @@ __global__ void __launch_bounds__(kK1Threads) k_vertex_phase(const CellDev* __re
                     p[k][0] = q[0]; p[k][1] = q[1]; p[k][2] = q[2];
                 } else if (flags & VP_PREDICT) {
                     double vh[3];
-                    predict_vertex(ld4(X + id[k]), ld4(c.vel + id[k]), ld4(c.acc + id[k]), dt, hdt, vh, p[k]);
+                    predict_vertex_c(c, id[k], ld4(X + id[k]), ld4(c.vel + id[k]), ld4(c.acc + id[k]), dt, hdt, vh,
+                                     p[k]);
                 } else {
                     double4 q = ld4v(xo + id[k]);
                     p[k][0] = q.x; p[k][1] = q.y; p[k][2] = q.z;
@@ -388,6 +390,7 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
     for (int w = blockIdx.x; w < a.nwork; w += gridDim.x) {
         const WorkItem it = a.work[w];
         const CellDev& c = a.cells[it.cell];
+        if (MODE == PP_STEP && cell_done(c)) continue;   // block-uniform
         const wcfe_params& p = c.prm;
         const int4 pt = c.patch[it.idx];
         const int par = c.ctl[0];
@@ -563,7 +566,7 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
                 vh[0] = h.x; vh[1] = h.y; vh[2] = h.z;
             } else {
                 double xn_unused[3];
-                predict_vertex(X[v], V4, A4, a.dt, a.hdt, vh, xn_unused);
+                predict_vertex_c(c, v, X[v], V4, A4, a.dt, a.hdt, vh, xn_unused);
             }
             const double Vo[3] = {V4.x, V4.y, V4.z};
             double An[3], Vn[3];
@@ -610,6 +613,7 @@ __global__ void __launch_bounds__(128) k_patch_phase_fp64(PatchArgs a) {
                 c.ctl[0] = par ^ 1;
                 c.clk[0] = c.clk[0] + a.dt_real;
                 c.ap[0] = ap_call + 1ull;
+                count_step(c);
             }
         }
     }
@@ -622,7 +626,7 @@ __global__ void k_predict(const CellDev* __restrict__ cells, int cell, double dt
     const int par = c.ctl[0];
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < c.nv; v += gridDim.x * blockDim.x) {
         double vh[3], xn[3];
-        predict_vertex(ld4(c.pos[par] + v), ld4(c.vel + v), ld4(c.acc + v), dt, hdt, vh, xn);
+        predict_vertex_c(c, v, ld4(c.pos[par] + v), ld4(c.vel + v), ld4(c.acc + v), dt, hdt, vh, xn);
         st4(c.vhl + v, vh[0], vh[1], vh[2]);
         st4(c.pos[par ^ 1] + v, xn[0], xn[1], xn[2]);
         if (xout) { xout[3 * (size_t)v] = xn[0]; xout[3 * (size_t)v + 1] = xn[1]; xout[3 * (size_t)v + 2] = xn[2]; }

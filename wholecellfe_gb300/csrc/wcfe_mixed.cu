@@ -18,7 +18,7 @@
 // FP32 quantity is thus a small number at full relative precision, not a
 // difference of two O(1) numbers.  The isotropic active stress kappa t_act I
 // contributes w b_i per element corner; on a closed one-ring these sum to
-// exactly zero, so it stays out of the FP32 element and is added in FP64 for
+// exactly zero, so it stays out of the FP32 element and is added in float-float for
 // boundary vertices: (1/2) kappa t_act thick e3 x sum (X_k - X_j).  The strain
 // update uses K = F^-1 - I = -H F^-1:
 //     ea_s - E = theta_g^2 D + (theta_g^2 - 1)(E - I/2),
@@ -27,8 +27,11 @@
 // The vertex phase packs each vertex's element inputs into an FP32 record:
 // the position as float-float (hi, lo), the step displacement u = x - X and
 // the strain.  The element loop therefore does no FP64 arithmetic.  The state
-// and every accumulation (x, V, the strain, c_C, the bond vector) stay FP64; the
-// per-step force and acceleration are FP32.
+// and every accumulation are extended-precision FP32 formats (wcfe_ff.cuh), not
+// binary64, because GB300 retires FP64 at about 1/64 of its FP32 rate: positions
+// triple-float (about 72 bits, exact for any binary64 input), velocity, strain,
+// c_C and the bond vector float-float (about 48 bits).  The per-step force and
+// acceleration are FP32.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -86,57 +89,17 @@ __device__ __forceinline__ float4 ld_acc(const double4* base, int v) {
 }
 __device__ __forceinline__ void st_acc(double4* base, int v, float4 a) { reinterpret_cast<float4*>(base)[v] = a; }
 __device__ __forceinline__ float ld_rho(const double* base, int v) { return __ldg(reinterpret_cast<const float*>(base) + v); }
-// positions as doubles (boundary terms, area, exchange)
+// a position (triple-float x, y; float-float z) as doubles (area, substrate location)
 __device__ __forceinline__ void pos_d(const ff4& a, double x[3]) {
-    x[0] = ff_to_d(ffx(a)); x[1] = ff_to_d(ffy(a)); x[2] = ff_to_d(ffz(a));
+    x[0] = tf_to_d(tfx(a)); x[1] = tf_to_d(tfy(a)); x[2] = ff_to_d(ffz(a));
 }
-// predicted velocity and position of one in-plane component:
-// vh = V + (dt/2) A, x = X + dt vh (the z component does not move, UL:119)
-__device__ __forceinline__ void predict_ff(ff X, ff V, float A, ff hdt, ff dt, ff& vh, ff& x) {
-    vh = ff_add(V, ff_mul_f(hdt, A));
-    x = ff_add(X, ff_mul(dt, vh));
+// a float-float vector as doubles
+__device__ __forceinline__ void vec_d(const ff4& a, double x[3]) {
+    x[0] = ff_to_d(ffx(a)); x[1] = ff_to_d(ffy(a)); x[2] = ff_to_d(ffz(a));
 }
 
 constexpr int kRec = 3;      // float4 per vertex record
 constexpr int kSlot32 = 20;  // floats per element slot in shared memory
-
-// MD force-extension fit (UL:1203-1214) in FP32
-static __constant__ float c_md_px32[6] = {0.f, 2.51250583e-03f, 4.40265201e-03f, 5.91408228e-03f, 11.76817302e-03f, 17.001e-03f};
-static __constant__ float c_md_py32[6] = {-7.15514497f, 71.80501308f, 356.62420075f, 356.96656556f, 126.21811585f, 528.40481124f};
-static __constant__ float c_md_k32[6] = {31426.8556f, 99485.86235f, 67080.67086f, -7908.39043f, 21978.66923f, 76858.39733f};
-
-// Spring force of bond u in FP32 (UL:1245-1264; k1 UL:1259-1261; the polynomial extension)
-// and the Bell force magnitude of updateFA (UL:2137; k1 UL:2077).
-__device__ __forceinline__ void spring_force32(const ParamF& p, float ux, float uy, float uz, float fs[3],
-                                               float* bell) {
-    const float D = sqrtf(ux * ux + uy * uy + uz * uz);
-    const float k = p.k_lin, L0 = p.rest_len;
-    if (p.law == PF_LINEAR0) {
-        fs[0] = k * ux; fs[1] = k * uy; fs[2] = k * uz;
-        *bell = p.norm2d ? k * sqrtf(ux * ux + uy * uy) : k * D;
-        return;
-    }
-    const float iD = D != 0.0f ? 1.0f / D : 0.0f;
-    float mag = 0.0f;
-    if (p.law == PF_MD) {
-        int j = -1;
-        if (D >= c_md_px32[5]) j = 5;
-        else {
-#pragma unroll
-            for (int q = 0; q < 5; ++q)
-                if (D < c_md_px32[q + 1] && D >= c_md_px32[q]) j = q;
-        }
-        if (j >= 0) mag = c_md_py32[j] + c_md_k32[j] * (D - c_md_px32[j]);
-    } else if (p.law == PF_LINEAR) {
-        mag = k * (D - L0);
-    } else {
-        const float e = D - L0;
-        mag = p.poly_k0 * (e + e * e * e * p.poly_c3);
-    }
-    fs[0] = mag * ux * iD; fs[1] = mag * uy * iD; fs[2] = mag * uz * iD;
-    if (p.law == PF_LINEAR && p.norm2d) *bell = fabsf(k * (sqrtf(ux * ux + uy * uy) - L0));
-    else *bell = fabsf(mag) * (D != 0.0f ? 1.0f : 0.0f);
-}
 
 // kfa * f - R, with kfa * f exact (FMA TwoProduct) and R float-float: one final rounding
 __device__ __forceinline__ float net_force(float kfa, float f, ff R) {
@@ -161,6 +124,45 @@ __device__ __forceinline__ ff md_px(int j) { return {c_md_pxh[j], c_md_pxl[j]}; 
 __device__ __forceinline__ ff md_py(int j) { return {c_md_pyh[j], c_md_pyl[j]}; }
 __device__ __forceinline__ ff md_k(int j) { return {c_md_kh[j], c_md_kl[j]}; }
 
+// MD force-extension fit (UL:1203-1214) in FP32
+static __constant__ float c_md_px32[6] = {0.f, 2.51250583e-03f, 4.40265201e-03f, 5.91408228e-03f, 11.76817302e-03f, 17.001e-03f};
+static __constant__ float c_md_py32[6] = {-7.15514497f, 71.80501308f, 356.62420075f, 356.96656556f, 126.21811585f, 528.40481124f};
+static __constant__ float c_md_k32[6] = {31426.8556f, 99485.86235f, 67080.67086f, -7908.39043f, 21978.66923f, 76858.39733f};
+
+// Spring force of bond u = (ux, uy, uz) + (lx, ly, lz) (float-float) in FP32 (UL:1245-1264;
+// k1 UL:1259-1261; the polynomial extension).  The MD table is discontinuous at its
+// breakpoints (a jump of 285 pN at 4.4 nm), so its branch is chosen on the float-float
+// extension, as the binary64 form would choose it; the force within the branch is FP32.
+__device__ __forceinline__ void spring_force32(const ParamF& p, float ux, float uy, float uz, float lx, float ly,
+                                               float lz, float fs[3]) {
+    const float D = sqrtf(ux * ux + uy * uy + uz * uz);
+    const float k = p.k_lin, L0 = p.rest_len;
+    if (p.law == PF_LINEAR0) {
+        fs[0] = k * ux; fs[1] = k * uy; fs[2] = k * uz;
+        return;
+    }
+    const float iD = D != 0.0f ? 1.0f / D : 0.0f;
+    float mag = 0.0f;
+    if (p.law == PF_MD) {
+        const ff X = {ux, lx}, Y = {uy, ly}, Z = {uz, lz};
+        const ff Dff = ff_sqrt(ff_add(ff_add(ff_mul(X, X), ff_mul(Y, Y)), ff_mul(Z, Z)));
+        int j = -1;
+        if (!ff_lt(Dff, md_px(5))) j = 5;
+        else {
+#pragma unroll
+            for (int q = 0; q < 5; ++q)
+                if (ff_lt(Dff, md_px(q + 1)) && !ff_lt(Dff, md_px(q))) j = q;
+        }
+        if (j >= 0) mag = c_md_py32[j] + c_md_k32[j] * (D - c_md_px32[j]);
+    } else if (p.law == PF_LINEAR) {
+        mag = D > L0 ? k * (D - L0) : 0.0f;   // slack below the rest length
+    } else {
+        const float e = D - L0;
+        mag = e > 0.0f ? p.poly_k0 * (e + e * e * e * p.poly_c3) : 0.0f;
+    }
+    fs[0] = mag * ux * iD; fs[1] = mag * uy * iD; fs[2] = mag * uz * iD;
+}
+
 // Bell force magnitude of updateFA (UL:2137; k1 UL:2077) in float-float.  The off-rate
 // k_a exp(F / F_a) turns a relative error e of F into (F / F_a) e, so F is carried
 // to about 48 bits.
@@ -169,7 +171,10 @@ __device__ __forceinline__ ff bell_ff(const ParamF& p, ff ux, ff uy, ff uz) {
     const ff d2xy = ff_add(ff_mul(ux, ux), ff_mul(uy, uy));
     const ff d2 = ff_add(d2xy, ff_mul(uz, uz));
     if (p.law == PF_LINEAR0) return ff_mul(k, ff_sqrt(p.norm2d ? d2xy : d2));
-    if (p.law == PF_LINEAR) return ff_abs(ff_mul(k, ff_sub(ff_sqrt(p.norm2d ? d2xy : d2), L0)));
+    if (p.law == PF_LINEAR) {   // slack below the rest length
+        const ff e = ff_sub(ff_sqrt(p.norm2d ? d2xy : d2), L0);
+        return (e.hi > 0.0f || (e.hi == 0.0f && e.lo > 0.0f)) ? ff_mul(k, e) : ff{0.0f, 0.0f};
+    }
     const ff D = ff_sqrt(d2);
     if (p.law == PF_MD) {
         int j = -1;
@@ -181,8 +186,9 @@ __device__ __forceinline__ ff bell_ff(const ParamF& p, ff ux, ff uy, ff uz) {
         return ff_abs(ff_add(md_py(j), ff_mul(md_k(j), ff_sub(D, md_px(j)))));
     }
     const ff e = ff_sub(D, L0);
+    if (!(e.hi > 0.0f || (e.hi == 0.0f && e.lo > 0.0f))) return {0.0f, 0.0f};   // slack
     const ff c3 = {p.poly_c3, p.poly_c3_lo}, k0 = {p.poly_k0, p.poly_k0_lo};
-    return ff_abs(ff_mul(k0, ff_add(e, ff_mul(ff_mul(ff_mul(e, e), e), c3))));
+    return ff_mul(k0, ff_add(e, ff_mul(ff_mul(ff_mul(e, e), e), c3)));
 }
 
 struct ElemParams {   // per-cell constants of the element, hoisted out of the element loop
@@ -295,12 +301,12 @@ __device__ __forceinline__ void element2d(const float4 r[3][kRec], const ElemPar
     o.acur = 0.5f * fabsf(gc);
 }
 
-constexpr int kBndSlots = 128;   // boundary vertices a patch CTA queues for its second loop
+constexpr int kBndSlots = 96;    // boundary vertices a patch CTA queues for its second loop (more finish in place)
 
 // Per-cell, per-step constants of the boundary terms (computed once per patch CTA).
 struct BndConst {
-    float w;              // (1/2) kappa t_act thick: isotropic active stress on the open one-ring
-    float area_term;      // -k_area (A - A_0) / 2 (calculateAreaConstraintForce)
+    ff w;                 // (1/2) kappa t_act thick: isotropic active stress on the open one-ring
+    ff area_term;         // -k_area (A - A_0) / 2 (calculateAreaConstraintForce)
     float k_bend, ap_force;
     ff half_density;      // ap_density / 2
     uint32_t ap_thr;      // r31 < ap_thr  <=>  r31 / 2^31 < ap_rate dt exp(-ap_rate dt)
@@ -315,8 +321,8 @@ __device__ __forceinline__ BndConst make_bnd_const(const CellDev& c, const Mixed
     const double s_iso = p.kappa * (t < p.tact_t1 ? t * p.tact_rate : p.tact_max);
     const double apt = isnan(a.ap_thresh) ? c.ap_thresh : a.ap_thresh;
     BndConst b;
-    b.w = (float)(0.5 * s_iso * p.thick);
-    b.area_term = (float)(-p.k_area * (c.area4[0] - p.area0) / 2);
+    b.w = ff_from_d(0.5 * s_iso * p.thick);
+    b.area_term = ff_from_d(-p.k_area * (c.area4[0] - p.area0) / 2);
     b.k_bend = (float)p.k_bend;
     b.ap_force = (float)p.ap_force;
     b.half_density = ff_from_d(p.ap_density / 2);
@@ -351,8 +357,8 @@ __device__ __forceinline__ StepConst make_step_const(const CellDev& c, double dt
     s.q.cx = (float)cx;
     s.q.cy = (float)cy;
     const double s_iso = p.kappa * t_act;
-    s.b.w = (float)(0.5 * s_iso * p.thick);
-    s.b.area_term = (float)(-p.k_area * (area - p.area0) / 2);
+    s.b.w = ff_from_d(0.5 * s_iso * p.thick);
+    s.b.area_term = ff_from_d(-p.k_area * (area - p.area0) / 2);
     s.b.k_bend = (float)p.k_bend;
     s.b.ap_force = (float)p.ap_force;
     s.b.half_density = ff_from_d(p.ap_density / 2);
@@ -385,16 +391,20 @@ __device__ __forceinline__ bool boundary_frame_ff(const CellDev& c, const double
     return true;
 }
 
-// Boundary terms of vertex v (rank `rank`) added to (F0, F1), in FP32 on float-float
-// positions: the isotropic active stress of the open one-ring, AP push
+// Boundary terms of vertex v (rank `rank`) added to (F0, F1) in float-float, on the
+// triple-float positions: the isotropic active stress of the open one-ring, AP push
 // (calculateForce_AP UL:1477-1569), bending (calculateBendingForce2D UL:1571-1689) and
 // area constraint (calculateAreaConstraintForce UL:1691-1784), on the neighbour frame of
-// UL:1500-1531.  The turning-angle term cos(theta) - 1 is evaluated as -|e1 - e2|^2 / 2,
-// free of the cancellation that FP32 would suffer on a nearly straight boundary, and
-// the AP bond count ceil(density L / 2) is taken on a float-float L.
+// UL:1500-1531 (in the plane: the mixed form keeps z = 0).  On a boundary these forces
+// nearly balance one another (a cell whose edge is at rest moves by the small remainder),
+// so each is formed and summed in float-float: FP32 terms would leave their own 6e-8
+// relative rounding on a net force a hundred times smaller.  The turning-angle term
+// 1 - cos(theta) is |e1 - e2|^2 / 2 with e1 - e2 = (d1 l2 - d2 l1) / (l1 l2); the unit
+// normal is (d1 + d2) x e3 / L, the reference's length-weighted mean of the two edge
+// normals.  The AP bond count ceil(density L / 2) is taken on the float-float L.
 __device__ __forceinline__ void boundary_force(const CellDev& c, const BndConst& bc, const int4& pt,
                                                const double4* __restrict__ X, const double4* __restrict__ xp, int v,
-                                               int rank, float& F0, float& F1) {
+                                               int rank, ff& F0, ff& F1) {
     const ff4 xi = ldg_ff4(xp, c.nv, v);
     // isotropic active stress on the open one-ring: (1/2) s_iso thick e3 x sum (X_k - X_j)
     ff sx = {0.0f, 0.0f}, sy = {0.0f, 0.0f};
@@ -405,23 +415,21 @@ __device__ __forceinline__ void boundary_force(const CellDev& c, const BndConst&
         const int4 t4 = c.tri[e];
         const int ids[3] = {t4.x, t4.y, t4.z};
         const ff4 Xj = ldg_ff4(X, c.nv, ids[(cn + 1) % 3]), Xk = ldg_ff4(X, c.nv, ids[(cn + 2) % 3]);
-        sx = ff_add(sx, ff_sub(ffx(Xk), ffx(Xj)));
-        sy = ff_add(sy, ff_sub(ffy(Xk), ffy(Xj)));
+        sx = ff_add(sx, tf_sub(tfx(Xk), tfx(Xj)));
+        sy = ff_add(sy, tf_sub(tfy(Xk), tfy(Xj)));
     }
-    float Fb0 = bc.w * sy.hi, Fb1 = -bc.w * sx.hi;  // minus the residual term w e3 x s
+    ff Fb0 = ff_mul(bc.w, sy), Fb1 = ff_mul(bc.w, sx);   // minus the residual term w e3 x s
+    Fb1 = {-Fb1.hi, -Fb1.lo};
     ff4 x1, x2;
     if (boundary_frame_ff(c, xp, rank, xi, x1, x2)) {
-        const float d1x = ff_sub(ffx(xi), ffx(x1)).hi, d1y = ff_sub(ffy(xi), ffy(x1)).hi;
-        const float d1z = ff_sub(ffz(xi), ffz(x1)).hi;
-        const float d2x = ff_sub(ffx(x2), ffx(xi)).hi, d2y = ff_sub(ffy(x2), ffy(xi)).hi;
-        const float d2z = ff_sub(ffz(x2), ffz(xi)).hi;
-        const float nn1 = sqrtf(d1y * d1y + d1x * d1x), nn2 = sqrtf(d2y * d2y + d2x * d2x);
-        const float l1 = sqrtf(d1x * d1x + d1y * d1y + d1z * d1z), l2 = sqrtf(d2x * d2x + d2y * d2y + d2z * d2z);
-        const ff Lf = two_sum(l1, l2);
-        const float L = Lf.hi;
-        const float nx = l1 / L * (d1y / nn1) + l2 / L * (d2y / nn2);
-        const float ny = l1 / L * (-d1x / nn1) + l2 / L * (-d2x / nn2);
-        float fb = 0.0f;
+        const ff D1x = tf_sub(tfx(xi), tfx(x1)), D1y = tf_sub(tfy(xi), tfy(x1));
+        const ff D2x = tf_sub(tfx(x2), tfx(xi)), D2y = tf_sub(tfy(x2), tfy(xi));
+        const ff L1 = ff_sqrt(ff_add(ff_mul(D1x, D1x), ff_mul(D1y, D1y)));
+        const ff L2 = ff_sqrt(ff_add(ff_mul(D2x, D2x), ff_mul(D2y, D2y)));
+        const ff Lf = ff_add(L1, L2);
+        const ff nx = ff_div(ff_add(D1y, D2y), Lf);
+        const ff nyn = ff_div(ff_add(D1x, D2x), Lf);   // -ny
+        ff fb = {0.0f, 0.0f};
         if (bc.ap_enable) {
             const uint32_t r31 = ap_draw(bc.seed, bc.stream, bc.ap_call, (uint32_t)rank);
             const ff lim = ff_mul(Lf, bc.half_density);
@@ -430,29 +438,46 @@ __device__ __forceinline__ void boundary_force(const CellDev& c, const BndConst&
                 cnt = ceilf(lim.hi);
                 if (cnt == lim.hi && lim.lo > 0.0f) cnt += 1.0f;
             }
-            fb += (r31 < bc.ap_thr) ? bc.ap_force * cnt : 0.0f;
+            if (r31 < bc.ap_thr) fb = ff_mul_f({bc.ap_force, 0.0f}, cnt);
         }
-        const float i1 = 1.0f / l1, i2 = 1.0f / l2;
-        const float e1x = d1x * i1, e1y = d1y * i1, e1z = d1z * i1, e2x = d2x * i2, e2y = d2y * i2, e2z = d2z * i2;
-        const float gx = e1x - e2x, gy = e1y - e2y, gz = e1z - e2z;
-        const float q = 0.5f * (gx * gx + gy * gy + gz * gz);   // 1 - cos(theta)
-        const float ez = e1x * e2y - e1y * e2x;
-        const float turna = ez > 0.0f ? -q : q;
-        fb += bc.k_bend * (turna * 2.0f / L);
-        fb += bc.area_term * L;
-        Fb0 += fb * nx;
-        Fb1 += fb * ny;
+        const ff l12 = ff_mul(L1, L2);
+        const ff gx = ff_div(ff_sub(ff_mul(D1x, L2), ff_mul(D2x, L1)), l12);
+        const ff gy = ff_div(ff_sub(ff_mul(D1y, L2), ff_mul(D2y, L1)), l12);
+        ff q = ff_add(ff_mul(gx, gx), ff_mul(gy, gy));   // 2 (1 - cos(theta))
+        const float ez = D1x.hi * D2y.hi - D1y.hi * D2x.hi;   // the sign of (e1 x e2).z
+        if (ez > 0.0f) q = {-q.hi, -q.lo};                     // turna = -(1 - cos) for a left turn
+        fb = ff_add(fb, ff_div(ff_mul_f(q, bc.k_bend), Lf));   // k_bend turna 2 / L
+        fb = ff_add(fb, ff_mul(bc.area_term, Lf));
+        Fb0 = ff_add(Fb0, ff_mul(fb, nx));
+        Fb1 = ff_sub(Fb1, ff_mul(fb, nyn));
     }
-    F0 += Fb0;
-    F1 += Fb1;
+    F0 = ff_add(F0, Fb0);
+    F1 = ff_add(F1, Fb1);
 }
 
-// Explicit update of vertex v (UL:592-628): the acceleration in FP32 from the FP32
-// force; the velocity and the strain accumulate in float-float.  V, A and the strain
-// (xx yy zz xy, hi and lo) come in from the caller (global memory or a staged copy).
-__device__ __forceinline__ void finish_vertex_core(const CellDev& c, const MixedArgs& a, int par, int v, float F0,
-                                                   float F1, float Q0, float Q1, float Q2, float Q3, float MMf,
-                                                   const ff4& V, const float4& A, const float4& eh, const float4& el) {
+// The radial protrusion driver (wcfe_params.protrude_v; the FP64 form's drive_protrusion):
+// a boundary vertex's half-step velocity is v (X - c) / |X - c| in the plane, the speed in
+// float-float and the unit direction in FP32 (a 1e-7 error of the direction moves the
+// vertex by 1e-7 of one step's travel).
+__device__ __forceinline__ void protrude_ff(const CellDev& c, int v, const ff4& X, ff& vh0, ff& vh1) {
+    const ParamF& pf = c.pf;
+    if ((pf.pv == 0.0f && pf.pv_lo == 0.0f) || c.bnd_rank[v] < 0) return;
+    const float dx = ff_sub(ffx(X), {pf.pcx, pf.pcx_lo}).hi, dy = ff_sub(ffy(X), {pf.pcy, pf.pcy_lo}).hi;
+    const float r = sqrtf(dx * dx + dy * dy);
+    if (r == 0.0f) return;
+    vh0 = ff_mul_f({pf.pv, pf.pv_lo}, dx / r);
+    vh1 = ff_mul_f({pf.pv, pf.pv_lo}, dy / r);
+}
+
+// Explicit update of vertex v (UL:592-628): the acceleration in FP32 from the force; the
+// velocity and the strain accumulate in float-float.  A boundary vertex (exact = true)
+// brings a float-float force and forms F - drag vh - damp m V in float-float (its terms
+// nearly cancel); an interior vertex brings its FP32 force (F0.lo = 0).  V, A and the
+// strain (xx yy zz xy, hi and lo) come in from the caller (global memory or a staged copy).
+__device__ __forceinline__ void finish_vertex_core(const CellDev& c, const MixedArgs& a, int par, int v, ff F0,
+                                                   ff F1, bool exact, float Q0, float Q1, float Q2, float Q3,
+                                                   float MMf, const ff4& V, const float4& A, const float4& eh,
+                                                   const float4& el) {
     const ParamF& pf = c.pf;
     ff vh0, vh1;
     if (a.vh_from_buf) {
@@ -461,12 +486,19 @@ __device__ __forceinline__ void finish_vertex_core(const CellDev& c, const Mixed
     } else {
         vh0 = ff_add(ffx(V), ff_mul_f(a.hdt, A.x));
         vh1 = ff_add(ffy(V), ff_mul_f(a.hdt, A.y));
+        if (c.pf.pv != 0.0f && c.bnd_rank[v] >= 0) protrude_ff(c, v, ldg_ff4(c.pos[par], c.nv, v), vh0, vh1);
     }
     const float rhom = pf.rho;
     const float iM = 1.0f / (MMf * rhom);
     const float damp_m = pf.damp * MMf * rhom;
-    const float An0 = (F0 - pf.drag * vh0.hi - damp_m * V.hx) * iM;
-    const float An1 = (F1 - pf.drag * vh1.hi - damp_m * V.hy) * iM;
+    float An0, An1;
+    if (exact) {
+        An0 = ff_mul_f(ff_sub(F0, ff_add(ff_mul_f(vh0, pf.drag), ff_mul_f(ffx(V), damp_m))), iM).hi;
+        An1 = ff_mul_f(ff_sub(F1, ff_add(ff_mul_f(vh1, pf.drag), ff_mul_f(ffy(V), damp_m))), iM).hi;
+    } else {
+        An0 = (F0.hi - pf.drag * vh0.hi - damp_m * V.hx) * iM;
+        An1 = (F1.hi - pf.drag * vh1.hi - damp_m * V.hy) * iM;
+    }
     const float An2 = V.hz == 0.0f ? 0.0f : (-damp_m * V.hz) * iM;  // no force normal to the plane
     ff Vn0, Vn1, Vn2;
     if (a.half) {
@@ -491,25 +523,37 @@ __device__ __forceinline__ void finish_vertex_core(const CellDev& c, const Mixed
     if (!isfinite(chk)) atomicOr(c.status, 1u);
 }
 
-__device__ __forceinline__ void finish_vertex(const CellDev& c, const MixedArgs& a, int par, int v, float F0, float F1,
+__device__ __forceinline__ void finish_vertex(const CellDev& c, const MixedArgs& a, int par, int v, ff F0, ff F1,
                                               float Q0, float Q1, float Q2, float Q3, float MMf) {
     const float4* eo = reinterpret_cast<const float4*>(c.ea[par]);
     const float4 A = a.vh_from_buf ? make_float4(0.f, 0.f, 0.f, 0.f) : ld_acc(c.acc, v);
-    finish_vertex_core(c, a, par, v, F0, F1, Q0, Q1, Q2, Q3, MMf, ldg_ff4(c.vel, c.nv, v), A, __ldg(eo + v),
+    finish_vertex_core(c, a, par, v, F0, F1, true, Q0, Q1, Q2, Q3, MMf, ldg_ff4(c.vel, c.nv, v), A, __ldg(eo + v),
                        __ldg(eo + c.nv + v));
 }
 
-__global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
+// kfa f - R as float-float (the boundary vertices' force before their boundary terms)
+__device__ __forceinline__ ff net_force_ff(float kfa, float f, ff R) {
+    const float p = kfa * f;
+    return ff_sub({p, __fmaf_rn(kfa, f, -p)}, R);
+}
+constexpr int kBndRec = 10;   // floats per queued boundary vertex: index, F0 and F1 (hi, lo), Q0-Q3, MM
+
+// MINB: the least CTAs of 128 threads per SM the register allocation must allow (5: 96
+// registers; 6, 7, 8: 80, 72, 64 registers, with shared memory then limiting emax); the
+// autotuner picks among them.
+template <int MINB>
+__global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a) {
     extern __shared__ float smf[];
     const int emax = a.emax;
     // structure of arrays: field k of slot j at smf[k * emax + j]
     __shared__ int s_nbnd;
-    __shared__ float s_bnd[8 * kBndSlots];
+    __shared__ float s_bnd[kBndRec * kBndSlots];
     if (threadIdx.x == 0) s_nbnd = 0;
     __syncthreads();
     for (int w = blockIdx.x; w < a.nwork; w += gridDim.x) {
         const WorkItem it = a.work[w];
         const CellDev& c = a.cells[it.cell];
+        if (cell_done(c)) continue;   // block-uniform: a serving cell that ran its steps
         const int4 pt = c.patch[it.idx];
         const int par = c.ctl[0];
         const double4* __restrict__ X = c.pos[par];
@@ -545,9 +589,9 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             smf[19 * emax + j] = o.acur;
         }
         __syncthreads();
-        // ---- owned vertices: forces and the acceleration in FP32, accumulations in FP64 ----
+        // ---- owned vertices: forces and the acceleration in FP32, accumulations in float-float ----
         // Interior vertices finish here.  Boundary vertices queue their FP32 sums in shared
-        // memory and finish in a second loop over consecutive threads, so that the FP64
+        // memory and finish in a second loop over consecutive threads, so that the float-float
         // boundary terms run on full warps instead of one or two lanes of many warps.
         const ParamF& pf = c.pf;
         const float rho_max = pf.rho_i_max;
@@ -580,31 +624,34 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
             }
             const float Asum = Asf * (1.0f / 3.0f);
             // integrin force (UL:1241-1269) in FP32
-            float fs[3], bell;
-            spring_force32(pf, f4.hx, f4.hy, f4.hz, fs, &bell);
+            float fs[3];
+            spring_force32(pf, f4.hx, f4.hy, f4.hz, f4.lx, f4.ly, f4.lz, fs);
             const float kfa = -cCh * Asum * rho;
-            // F = kfa fs - R with the product exact (TwoProduct) and one rounding at the end
-            float F0 = net_force(kfa, fs[0], R0), F1 = net_force(kfa, fs[1], R1);
-            if (rank >= 0) {
+            if (rank >= 0) {   // F = kfa fs - R in float-float, then the boundary terms
+                ff G0 = net_force_ff(kfa, fs[0], R0), G1 = net_force_ff(kfa, fs[1], R1);
                 const int slot = atomicAdd(&s_nbnd, 1);
                 if (slot < kBndSlots) {
-                    float* b = s_bnd + 8 * slot;
-                    b[0] = __int_as_float(i); b[1] = F0; b[2] = F1; b[3] = Q0;
-                    b[4] = Q1; b[5] = Q2; b[6] = Q3; b[7] = MMf;
+                    float* b = s_bnd + kBndRec * slot;
+                    b[0] = __int_as_float(i); b[1] = G0.hi; b[2] = G0.lo; b[3] = G1.hi; b[4] = G1.lo;
+                    b[5] = Q0; b[6] = Q1; b[7] = Q2; b[8] = Q3; b[9] = MMf;
                     continue;
                 }
-                boundary_force(c, s_bc, pt, X, xp, v, rank, F0, F1);   // queue full: finish in place
+                boundary_force(c, s_bc, pt, X, xp, v, rank, G0, G1);   // queue full: finish in place
+                finish_vertex_core(c, a, par, v, G0, G1, true, Q0, Q1, Q2, Q3, MMf, Vv, Av, eh, el);
+                continue;
             }
-            finish_vertex_core(c, a, par, v, F0, F1, Q0, Q1, Q2, Q3, MMf, Vv, Av, eh, el);
+            // F = kfa fs - R with the product exact (TwoProduct) and one rounding at the end
+            const float F0 = net_force(kfa, fs[0], R0), F1 = net_force(kfa, fs[1], R1);
+            finish_vertex_core(c, a, par, v, {F0, 0.0f}, {F1, 0.0f}, false, Q0, Q1, Q2, Q3, MMf, Vv, Av, eh, el);
         }
         __syncthreads();
         const int nq = min(s_nbnd, kBndSlots);
         for (int j = threadIdx.x; j < nq; j += blockDim.x) {
-            const float* b = s_bnd + 8 * j;
+            const float* b = s_bnd + kBndRec * j;
             const int v = pt.x + __float_as_int(b[0]);
-            float F0 = b[1], F1 = b[2];
+            ff F0 = {b[1], b[2]}, F1 = {b[3], b[4]};
             boundary_force(c, s_bc, pt, X, xp, v, c.bnd_rank[v], F0, F1);
-            finish_vertex(c, a, par, v, F0, F1, b[3], b[4], b[5], b[6], b[7]);
+            finish_vertex(c, a, par, v, F0, F1, b[5], b[6], b[7], b[8], b[9]);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -616,14 +663,15 @@ __global__ void __launch_bounds__(128) k_patch_phase_mixed(MixedArgs a) {
                 c.ctl[0] = par ^ 1;
                 c.clk[0] = c.clk[0] + a.dt_real;
                 c.ap[0] = ap_call + 1ull;
+                count_step(c);
             }
         }
     }
 }
 
 // ===========================================================================
-// mixed-form vertex phase: predict (FP64), bond kinetics with FP32 rates and
-// FP64 accumulation, the FP32 element records, and the cell area and
+// mixed-form vertex phase: predict (triple-float positions), bond kinetics with FP32
+// rates and float-float accumulation, the FP32 element records, and the cell area and
 // area-weighted centroid from the boundary loop (shoelace over the directed
 // boundary edges).  For a planar mesh without inverted elements that equals
 // calculateAreaTot's sum of element areas.
@@ -699,11 +747,15 @@ struct VertexArgs {
 // one cell): predict, bond kinetics with FP32 rates and float-float accumulation,
 // and the FP32 element records.  No FP64 arithmetic outside the exchange
 // conversions and the area of the finishing block.
-__global__ void __launch_bounds__(kK1Threads, 5) k_vertex_phase_mixed(const CellDev* __restrict__ cells,
+// MINB: the least blocks of 256 threads per SM the register allocation must allow (5:
+// 48 registers with some spilling; 4: 64 registers); the autotuner picks.
+template <int MINB>
+__global__ void __launch_bounds__(kK1Threads, MINB) k_vertex_phase_mixed(const CellDev* __restrict__ cells,
                                                                     const WorkItem* __restrict__ work,
                                                                     const VertexArgs va) {
     const WorkItem it = work[blockIdx.x];
     const CellDev& c = cells[it.cell];
+    if (cell_done(c)) return;   // block-uniform: a serving cell that ran its steps
     const int v = it.idx * c.vb + threadIdx.x;
     const int flags = va.flags;
     const int par = c.ctl[0];
@@ -717,35 +769,46 @@ __global__ void __launch_bounds__(kK1Threads, 5) k_vertex_phase_mixed(const Cell
         const ff cold = do_fa ? ld_ff(c.cC, c.nv, v) : ff{0.0f, 0.0f};
         const ff cAv = do_fa ? ld_ff(c.cA, c.nv, v) : ff{0.0f, 0.0f};
         const float4 eh = __ldg(reinterpret_cast<const float4*>(c.ea[par]) + v);   // (xx, yy, zz, xy) hi
-        ff xn0, xn1, xn2 = ffz(Xv);
+        // positions are triple-float (wcfe_ff.cuh); the step displacement cu is float-float
+        tf xn0, xn1;
+        ff xn2 = ffz(Xv);
         if (flags & VM_IMPORT) {
+            // a coordinate the caller returned as the binary64 rounding of the predicted one keeps
+            // the predicted triple-float (so the exchange path steps exactly as the internal one);
+            // any other value is taken as given
             const double* qq = va.stage_in + 3 * (size_t)(c.hoff + v);
-            xn0 = ff_from_d(qq[0]); xn1 = ff_from_d(qq[1]); xn2 = ff_from_d(qq[2]);
-            st_ff4(xo, c.nv, v, make_ff4(xn0, xn1, xn2));
+            const ff4 pr = ld_ff4(xo, c.nv, v);
+            const tf p0 = tfx(pr), p1 = tfy(pr);
+            xn0 = tf_to_d(p0) == qq[0] ? p0 : tf_from_d(qq[0]);
+            xn1 = tf_to_d(p1) == qq[1] ? p1 : tf_from_d(qq[1]);
+            xn2 = ff_from_d(qq[2]);
+            st_ff4(xo, c.nv, v, make_pos4(xn0, xn1, xn2));
         } else if (flags & VM_PREDICT) {
+            // vh = V + (dt/2) A; x = X + dt vh
             const ff4 V = ldg_ff4(c.vel, c.nv, v);
             const float4 A = ld_acc(c.acc, v);
-            ff vh0, vh1;
-            predict_ff(ffx(Xv), ffx(V), A.x, va.hdt, va.dt, vh0, xn0);
-            predict_ff(ffy(Xv), ffy(V), A.y, va.hdt, va.dt, vh1, xn1);
-            st_ff4(xo, c.nv, v, make_ff4(xn0, xn1, xn2));
+            ff vh0 = ff_add(ffx(V), ff_mul_f(va.hdt, A.x)), vh1 = ff_add(ffy(V), ff_mul_f(va.hdt, A.y));
+            protrude_ff(c, v, Xv, vh0, vh1);
+            xn0 = tf_add_ff(tfx(Xv), ff_mul(va.dt, vh0));
+            xn1 = tf_add_ff(tfy(Xv), ff_mul(va.dt, vh1));
+            st_ff4(xo, c.nv, v, make_pos4(xn0, xn1, xn2));
             if (flags & VM_EXPORT) {
                 st_ff4(c.vhl, c.nv, v, make_ff4(vh0, vh1, {0.0f, 0.0f}));
                 double* qq = va.stage_out + 3 * (size_t)(c.hoff + v);
-                qq[0] = ff_to_d(xn0); qq[1] = ff_to_d(xn1); qq[2] = ff_to_d(xn2);
+                qq[0] = tf_to_d(xn0); qq[1] = tf_to_d(xn1); qq[2] = ff_to_d(xn2);
             }
         } else {
             const ff4 t = ld_ff4(xo, c.nv, v);
-            xn0 = ffx(t); xn1 = ffy(t); xn2 = ffz(t);
+            xn0 = tfx(t); xn1 = tfy(t); xn2 = ffz(t);
         }
-        const ff cu0 = ff_sub(xn0, ffx(Xv)), cu1 = ff_sub(xn1, ffy(Xv));   // step displacement
+        const ff cu0 = tf_sub(xn0, tfx(Xv)), cu1 = tf_sub(xn1, tfy(Xv));   // step displacement
         if (do_fa) {
             const ParamF& pf = c.pf;
             ff u0 = ff_add(ffx(f), cu0), u1 = ff_add(ffy(f), cu1), u2 = ffz(f);
             if (c.has_sub && c.sub.moving) {
                 double wgt[3], Xd[3], fd[3];
                 pos_d(Xv, Xd);
-                pos_d(f, fd);
+                vec_d(f, fd);
                 const int e = locate(c.sub, xs(Xd[0], fd[0]), xs(Xd[1], fd[1]), xs(Xd[2], fd[2]), wgt);
                 if (e >= 0) {
                     const int4 t = c.sub.tri[e];
@@ -792,7 +855,7 @@ __global__ void __launch_bounds__(kK1Threads, 5) k_vertex_phase_mixed(const Cell
 }
 
 void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
-                         int threads, cudaStream_t st, const double* stage_in, double* stage_out) {
+                         int threads, cudaStream_t st, const double* stage_in, double* stage_out, int kind) {
     if (nwork <= 0) return;
     (void)grid;   // one block per work item
     VertexArgs va;
@@ -803,7 +866,8 @@ void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, 
     va.flags = flags;
     va.stage_in = stage_in;
     va.stage_out = stage_out;
-    k_vertex_phase_mixed<<<nwork, threads, 0, st>>>(cells, work, va);
+    if (kind == 1) k_vertex_phase_mixed<4><<<nwork, threads, 0, st>>>(cells, work, va);
+    else k_vertex_phase_mixed<5><<<nwork, threads, 0, st>>>(cells, work, va);
 }
 
 // ===========================================================================
@@ -868,9 +932,10 @@ __device__ __forceinline__ void stage_issue(const MixedArgs& a, const StageLayou
             h->bc = make_bnd_const(c, a, h->ap_call);
         }
         const bool bad = pt.w > L.cap_ne || pt.y > L.cap_nvp || px.y > L.cap_nh || px.w > L.cap_nc;
-        h->bad = bad;
-        if (bad) {
-            atomicOr(c.status, 4u);
+        const bool skip = cell_done(c);   // a serving cell that ran its steps: no copies, no work
+        h->bad = skip ? 2 : (bad ? 1 : 0);
+        if (bad || skip) {
+            if (!skip) atomicOr(c.status, 4u);
             mbar_arrive_expect_tx(bar + s, 0);
         } else {
             const int v0 = pt.x, nvp = pt.y;
@@ -939,7 +1004,7 @@ __global__ void __launch_bounds__(kConsumers + 32) k_patch_mixed_staged(MixedArg
     extern __shared__ __align__(128) unsigned char sm[];
     __shared__ uint64_t full[2], empty[2];
     __shared__ int s_nbnd, s_ok;
-    __shared__ float s_bnd[8 * kBndSlots];
+    __shared__ float s_bnd[kBndRec * kBndSlots];
     float* smf = reinterpret_cast<float*>(sm + L.smf_off);
     const int emax = L.cap_ne;   // field stride of the element outputs
     if (threadIdx.x == 0) {
@@ -984,7 +1049,7 @@ __global__ void __launch_bounds__(kConsumers + 32) k_patch_mixed_staged(MixedArg
         }
         const unsigned char* st = sm + (size_t)s * L.stage_bytes;
         const StageHdr* h = reinterpret_cast<const StageHdr*>(st + L.o_hdr);
-        if (h->bad) {   // capacity exceeded: status already flagged
+        if (h->bad) {   // capacity exceeded (status already flagged), or a serving cell that is done
             consumer_sync();
             if (threadIdx.x == 0) mbar_arrive(empty + s);
             continue;
@@ -1053,38 +1118,44 @@ __global__ void __launch_bounds__(kConsumers + 32) k_patch_mixed_staged(MixedArg
                 Asf += smf[19 * emax + sl];
             }
             const float Asum = Asf * (1.0f / 3.0f);
-            const float4 f4 = fau_s[i];
-            float fs[3], bell;
-            spring_force32(pf, f4.x, f4.y, f4.z, fs, &bell);
+            const float4 f4 = fau_s[i];   // the high words; the MD branch also reads the low words
+            const float4 f4l = pf.law == PF_MD ? __ldg(reinterpret_cast<const float4*>(c.fau) + c.nv + pt.x + i)
+                                               : make_float4(0.f, 0.f, 0.f, 0.f);
+            float fs[3];
+            spring_force32(pf, f4.x, f4.y, f4.z, f4l.x, f4l.y, f4l.z, fs);
             const float rho = has_rho ? rho_s[i] : rho_max;
             const float kfa = -cc_s[i] * Asum * rho;
-            // F = kfa fs - R with the product exact (TwoProduct) and one rounding at the end
-            float F0 = net_force(kfa, fs[0], R0), F1 = net_force(kfa, fs[1], R1);
             const int rank = rank_s[i];
-            if (rank >= 0) {
+            const float4 vh = vhi_s[i], vl = vlo_s[i];
+            if (rank >= 0) {   // F = kfa fs - R in float-float, then the boundary terms
+                ff G0 = net_force_ff(kfa, fs[0], R0), G1 = net_force_ff(kfa, fs[1], R1);
                 const int slot = atomicAdd(&s_nbnd, 1);
                 if (slot < kBndSlots) {
-                    float* b = s_bnd + 8 * slot;
-                    b[0] = __int_as_float(i); b[1] = F0; b[2] = F1; b[3] = Q0;
-                    b[4] = Q1; b[5] = Q2; b[6] = Q3; b[7] = MMf;
+                    float* b = s_bnd + kBndRec * slot;
+                    b[0] = __int_as_float(i); b[1] = G0.hi; b[2] = G0.lo; b[3] = G1.hi; b[4] = G1.lo;
+                    b[5] = Q0; b[6] = Q1; b[7] = Q2; b[8] = Q3; b[9] = MMf;
                     continue;
                 }
-                boundary_force(c, h->bc, pt, X, xp, v, rank, F0, F1);   // queue full: finish in place
+                boundary_force(c, h->bc, pt, X, xp, v, rank, G0, G1);   // queue full: finish in place
+                finish_vertex_core(c, a, par, v, G0, G1, true, Q0, Q1, Q2, Q3, MMf,
+                                   {vh.x, vh.y, vh.z, vh.w, vl.x, vl.y, vl.z, vl.w}, acc_s[i], eahi_s[i], ealo_s[i]);
+                continue;
             }
-            const float4 vh = vhi_s[i], vl = vlo_s[i];
-            finish_vertex_core(c, a, par, v, F0, F1, Q0, Q1, Q2, Q3, MMf,
+            // F = kfa fs - R with the product exact (TwoProduct) and one rounding at the end
+            const float F0 = net_force(kfa, fs[0], R0), F1 = net_force(kfa, fs[1], R1);
+            finish_vertex_core(c, a, par, v, {F0, 0.0f}, {F1, 0.0f}, false, Q0, Q1, Q2, Q3, MMf,
                                {vh.x, vh.y, vh.z, vh.w, vl.x, vl.y, vl.z, vl.w}, acc_s[i], eahi_s[i], ealo_s[i]);
         }
         consumer_sync();
         const int nq = min(s_nbnd, kBndSlots);
         for (int j = threadIdx.x; j < nq; j += kConsumers) {
-            const float* b = s_bnd + 8 * j;
+            const float* b = s_bnd + kBndRec * j;
             const int i = __float_as_int(b[0]);
             const int v = pt.x + i;
-            float F0 = b[1], F1 = b[2];
+            ff F0 = {b[1], b[2]}, F1 = {b[3], b[4]};
             boundary_force(c, h->bc, pt, X, xp, v, rank_s[i], F0, F1);
             const float4 vh = vhi_s[i], vl = vlo_s[i];
-            finish_vertex_core(c, a, par, v, F0, F1, b[3], b[4], b[5], b[6], b[7],
+            finish_vertex_core(c, a, par, v, F0, F1, true, b[5], b[6], b[7], b[8], b[9],
                                {vh.x, vh.y, vh.z, vh.w, vl.x, vl.y, vl.z, vl.w}, acc_s[i], eahi_s[i], ealo_s[i]);
         }
         consumer_sync();
@@ -1098,6 +1169,7 @@ __global__ void __launch_bounds__(kConsumers + 32) k_patch_mixed_staged(MixedArg
                 c.ctl[0] = par ^ 1;
                 c.clk[0] = c.clk[0] + a.dt_real;
                 c.ap[0] = ap_call + 1ull;
+                count_step(c);
             }
         }
     }
@@ -1185,27 +1257,43 @@ bool launch_patch_staged(const CellDev* cells, const WorkItem* work, int nwork, 
 
 size_t mixed_smem_bytes(int emax) { return sizeof(float) * (size_t)emax * kSlot32; }
 
+namespace {
+const void* mixed_kernel(int kind) {
+    switch (kind) {
+        case 2: return (const void*)k_patch_phase_mixed<6>;
+        case 3: return (const void*)k_patch_phase_mixed<7>;
+        case 4: return (const void*)k_patch_phase_mixed<8>;
+        default: return (const void*)k_patch_phase_mixed<5>;
+    }
+}
+}  // namespace
+
 cudaError_t configure_mixed(size_t max_smem) {
-    cudaFuncAttributes at;
-    cudaError_t e = cudaFuncGetAttributes(&at, (const void*)k_patch_phase_mixed);
-    if (e != cudaSuccess) return e;
-    size_t dyn = max_smem > at.sharedSizeBytes ? max_smem - at.sharedSizeBytes : 0;
-    e = cudaFuncSetAttribute((const void*)k_patch_phase_mixed, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
-    if (e != cudaSuccess) return e;
+    for (int kind = 1; kind <= 4; ++kind) {
+        cudaFuncAttributes at;
+        cudaError_t e = cudaFuncGetAttributes(&at, mixed_kernel(kind));
+        if (e != cudaSuccess) return e;
+        size_t dyn = max_smem > at.sharedSizeBytes ? max_smem - at.sharedSizeBytes : 0;
+        e = cudaFuncSetAttribute(mixed_kernel(kind), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn);
+        if (e != cudaSuccess) return e;
+    }
     return configure_staged(max_smem);
 }
 
-int mixed_occupancy(int threads, size_t smem) {
+// resident CTAs per SM of the plain kernel variant `kind` (1-4, see k_patch_phase_mixed)
+int mixed_occupancy(int threads, size_t smem, int kind) {
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)k_patch_phase_mixed, threads, smem) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mixed_kernel(kind), threads, smem) != cudaSuccess) {
         cudaGetLastError();
         return 1;
     }
     return n > 0 ? n : 1;
 }
+int mixed_occupancy(int threads, size_t smem) { return mixed_occupancy(threads, smem, 1); }
 
 void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt, double dt_real,
-                        double ap_thresh, double t_override, int vh_from_buf, int threads, int grid, cudaStream_t st) {
+                        double ap_thresh, double t_override, int vh_from_buf, int threads, int grid, cudaStream_t st,
+                        int kind) {
     if (nwork <= 0) return;
     MixedArgs a;
     a.cells = cells;
@@ -1220,7 +1308,17 @@ void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, i
     a.ap_thresh = ap_thresh;
     a.t_override = t_override;
     a.vh_from_buf = vh_from_buf;
-    k_patch_phase_mixed<<<grid, threads, mixed_smem_bytes(emax), st>>>(a);
+    const size_t smem = mixed_smem_bytes(emax);
+    switch (kind) {
+        case 2: k_patch_phase_mixed<6><<<grid, threads, smem, st>>>(a); break;
+        case 3: k_patch_phase_mixed<7><<<grid, threads, smem, st>>>(a); break;
+        case 4: k_patch_phase_mixed<8><<<grid, threads, smem, st>>>(a); break;
+        default: k_patch_phase_mixed<5><<<grid, threads, smem, st>>>(a); break;
+    }
+}
+void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt, double dt_real,
+                        double ap_thresh, double t_override, int vh_from_buf, int threads, int grid, cudaStream_t st) {
+    launch_patch_mixed(cells, work, nwork, emax, dt, dt_real, ap_thresh, t_override, vh_from_buf, threads, grid, st, 1);
 }
 
 }  // namespace wcfe

@@ -22,12 +22,22 @@
 //  - all calls share the one array, and each call overwrites the slots it uses
 //    before reading them.  Calls that overlap on the GPU (two streams, or two
 //    host threads) race on it: serialise them.
-//  - a triangle index outside [0, n) makes the result NaN.
+//  - a triangle index outside [0, n) makes the result NaN;
+//  - a CUDA error already pending on the calling thread when the call starts is
+//    left in place (not cleared) and the call returns WCFE_ERR_CUDA without
+//    launching, so the status this call returns is always about its own launches;
+//  - the device address is kept for the life of the process: after a
+//    cudaDeviceReset of a device this entry point must not be called on it again.
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <string>
 
 #include "../../include/wcfe.h"
+
+namespace wcfe {
+int set_error(const char* msg, int code);   // wcfe_engine.cu: the thread's wcfe_last_error message
+}
 
 namespace {
 
@@ -109,6 +119,13 @@ extern "C" int wcfe_area_tot_noalloc(const double* x_dev, int32_t n_vert, const 
     if (!x_dev || !tri_dev || !area4_dev || n_vert <= 0 || n_tri <= 0) return WCFE_ERR_ARG;
     const int nb = (n_tri + kNaElems - 1) / kNaElems;
     if (nb > kNaMaxBlocks) return WCFE_ERR_LIMIT;
+    // an error left pending by earlier work is not ours to clear, and would be taken
+    // for this call's launch status below
+    const cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+        return wcfe::set_error((std::string("wcfe_area_tot_noalloc: CUDA error pending before the call: ") +
+                                cudaGetErrorString(pending)).c_str(),
+                               WCFE_ERR_CUDA);
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNaMaxDevices) return WCFE_ERR_NODEVICE;
     double* part = nullptr;
@@ -120,8 +137,8 @@ extern "C" int wcfe_area_tot_noalloc(const double* x_dev, int32_t n_vert, const 
             void* p = nullptr;
             cudaError_t rc = cudaGetSymbolAddress(&p, g_na_part);
             if (rc != cudaSuccess || !p) {
-                cudaGetLastError();
-                return WCFE_ERR_CUDA;
+                cudaGetLastError();   // the failed lookup's own error
+                return wcfe::set_error("wcfe_area_tot_noalloc: cudaGetSymbolAddress failed", WCFE_ERR_CUDA);
             }
             g_na_addr[dev] = static_cast<double*>(p);
         }
@@ -129,6 +146,13 @@ extern "C" int wcfe_area_tot_noalloc(const double* x_dev, int32_t n_vert, const 
     }
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     k_na_partials<<<nb, kNaThreads, 0, st>>>(x_dev, n_vert, tri_dev, n_tri, part);
-    k_na_final<<<1, 32, 0, st>>>(part, nb, area4_dev);
-    return cudaGetLastError() == cudaSuccess ? WCFE_OK : WCFE_ERR_CUDA;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) {
+        k_na_final<<<1, 32, 0, st>>>(part, nb, area4_dev);
+        e = cudaGetLastError();
+    }
+    if (e != cudaSuccess)
+        return wcfe::set_error((std::string("wcfe_area_tot_noalloc launch: ") + cudaGetErrorString(e)).c_str(),
+                               WCFE_ERR_CUDA);
+    return WCFE_OK;
 }

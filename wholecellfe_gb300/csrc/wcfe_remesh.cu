@@ -27,6 +27,13 @@ __device__ __forceinline__ void ff_split(double x, float& hi, float& lo) {
     hi = __double2float_rn(x);
     lo = __double2float_rn(x - (double)hi);
 }
+// exact split of a binary64 position coordinate into h + m + l
+__device__ __forceinline__ void tf_split(double x, float& h, float& m, float& l) {
+    h = __double2float_rn(x);
+    const double r = x - (double)h;
+    m = __double2float_rn(r);
+    l = __double2float_rn(r - (double)m);
+}
 
 __global__ void k_remesh_pack(CellDev c, int mixed, const void* rho, double* __restrict__ ext,
                               unsigned long long* __restrict__ hdr) {
@@ -108,8 +115,10 @@ __global__ void k_remesh_unpack(CellDev c, int mixed, const double* __restrict__
             float4* uh = reinterpret_cast<float4*>(c.fau);
             float4* ah = reinterpret_cast<float4*>(c.acc);
             float4 h, l;
-            ff_split(p[0], h.x, l.x); ff_split(p[1], h.y, l.y); ff_split(p[2], h.z, l.z);
-            h.w = l.w = 0.0f;
+            // positions: triple-float x and y (the third floats in the w slots), float-float z
+            tf_split(p[0], h.x, l.x, h.w);
+            tf_split(p[1], h.y, l.y, l.w);
+            ff_split(p[2], h.z, l.z);
             ph[j] = h; ph[N + j] = l;
             ff_split(r[0], h.x, l.x); ff_split(r[1], h.y, l.y); ff_split(r[2], h.z, l.z);
             vh[j] = h; vh[N + j] = l;

@@ -58,8 +58,9 @@ __global__ void k_frame_gather(CellDev c, int mixed, double* __restrict__ out) {
             const float4* ph = reinterpret_cast<const float4*>(c.pos[par]);
             const float4* fh = reinterpret_cast<const float4*>(c.fau);
             const float4 xh = ph[v], xl = ph[N + v], uh = fh[v], ul = fh[N + v];
-            X[3 * v] = (double)xh.x + (double)xl.x;
-            X[3 * v + 1] = (double)xh.y + (double)xl.y;
+            // triple-float x, y (third floats in the w slots): (h + m) exact, one rounding for + l
+            X[3 * v] = ((double)xh.x + (double)xl.x) + (double)xh.w;
+            X[3 * v + 1] = ((double)xh.y + (double)xl.y) + (double)xl.w;
             X[3 * v + 2] = (double)xh.z + (double)xl.z;
             F[3 * v] = (double)uh.x + (double)ul.x;
             F[3 * v + 1] = (double)uh.y + (double)ul.y;

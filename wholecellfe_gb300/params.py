@@ -26,6 +26,7 @@ class Params(C.Structure):
         ("ap_rate", C.c_double), ("ap_force", C.c_double), ("ap_density", C.c_double),
         ("ap_enable", C.c_int32), ("seed", C.c_uint32), ("stream", C.c_uint32),
         ("drag", C.c_double), ("damp", C.c_double), ("rho", C.c_double),
+        ("protrude_v", C.c_double), ("protrude_cx", C.c_double), ("protrude_cy", C.c_double),
     ]
 
     def copy(self) -> "Params":

@@ -180,3 +180,37 @@ def initial_state(x: np.ndarray, perturb: float = 0.0, seed: int = 0):
         cC[:] = rng.uniform(0.0, 0.5, size=n)
         fau[:, :2] = rng.normal(0, 0.004 * perturb, size=(n, 2))
     return x, V, A, ea, cA, cC, fau
+
+
+def protruding_cell(n_target: int = 2100, integrins: int = 600, dt: float = 5e-5, seed: int = 1,
+                    E: float = 1000.0, nu: float = 0.45, thickness: float = 0.1):
+    """The single-cell workload with a protruding edge: a disk of radius 10 um with about
+    n_target vertices (seeded +-2 % jitter; 2,044 vertices and 3,929 triangles by default), membrane modulus E (Pa) and Poisson ratio nu
+    mapped to the shear modulus mu = E / (2 (1 + nu)) (the small-strain map of the
+    reference's incompressible neo-Hookean membrane, UL:861-865), thickness in um, linear
+    integrin springs of 1 pN/nm with a 20 nm rest length on `integrins` vertices (the ones
+    nearest to as many seeded anchor points uniform over the disk, distinct), and every
+    boundary vertex driven radially outward by 10 nm per step of dt.  Returns
+    (x0, tri, params, rho) with rho the per-vertex integrin density."""
+    from .params import LAW_LINEAR, default_params
+    x0, tri = disk_mesh(n_target, seed=seed)
+    p = default_params("k1")
+    p.mu = E / (2.0 * (1.0 + nu))
+    p.thick = thickness
+    p.force_law, p.k_lin, p.rest_len = LAW_LINEAR, 1000.0, 0.02
+    p.protrude_v = 0.010 / dt
+    p.protrude_cx = p.protrude_cy = 0.0
+    rng = np.random.default_rng([seed, 600])
+    r = 10.0 * np.sqrt(rng.uniform(0.0, 1.0, 4 * integrins))
+    a = rng.uniform(0.0, 2.0 * np.pi, 4 * integrins)
+    anchors = np.c_[r * np.cos(a), r * np.sin(a)]
+    rho = np.zeros(len(x0))
+    taken = 0
+    for q in anchors:   # nearest free vertex of each anchor, until `integrins` vertices carry one
+        d = np.sum((x0[:, :2] - q) ** 2, axis=1)
+        d[rho > 0] = np.inf
+        rho[int(np.argmin(d))] = p.rho_i_max
+        taken += 1
+        if taken == integrins:
+            break
+    return x0, tri, p, rho
