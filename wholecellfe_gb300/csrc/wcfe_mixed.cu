@@ -684,6 +684,24 @@ enum { VM_PREDICT = 1, VM_UPDATE_FA = 2, VM_EXPORT = 8, VM_IMPORT = 16, VM_NOARE
 // wrote (through L2) and sums the terms in a fixed order: boundary ranks strided
 // over the threads, then lanes, then warps.  Only that block runs the FP64
 // shoelace, with all of its lanes busy.
+// The substrate's displacement under a bond's anchor (a rigid substrate mesh moved by the
+// caller), subtracted from the bond vector (UL:2053-2099).  Out of line: few cells have
+// one, and its FP64 point location would otherwise set the register budget of every block.
+__device__ __noinline__ void substrate_move(const CellDev& c, const ff4& Xv, const ff4& f, ff& u0, ff& u1, ff& u2) {
+    double wgt[3], Xd[3], fd[3];
+    pos_d(Xv, Xd);
+    vec_d(f, fd);
+    const int e = locate(c.sub, xs(Xd[0], fd[0]), xs(Xd[1], fd[1]), xs(Xd[2], fd[2]), wgt);
+    if (e >= 0) {
+        const int4 t = c.sub.tri[e];
+        const double4 a0 = ld4(c.sub.x + t.x), a1 = ld4(c.sub.x + t.y), a2 = ld4(c.sub.x + t.z);
+        const double4 b0 = ld4(c.sub.X + t.x), b1 = ld4(c.sub.X + t.y), b2 = ld4(c.sub.X + t.z);
+        u0 = ff_sub(u0, ff_from_d(wgt[0] * (a0.x - b0.x) + wgt[1] * (a1.x - b1.x) + wgt[2] * (a2.x - b2.x)));
+        u1 = ff_sub(u1, ff_from_d(wgt[0] * (a0.y - b0.y) + wgt[1] * (a1.y - b1.y) + wgt[2] * (a2.y - b2.y)));
+        u2 = ff_sub(u2, ff_from_d(wgt[0] * (a0.z - b0.z) + wgt[1] * (a1.z - b1.z) + wgt[2] * (a2.z - b2.z)));
+    }
+}
+
 __device__ __forceinline__ void finish_area_boundary(const CellDev& c, const double4* xo, double dt_real) {
     __shared__ int s_last;
     __shared__ double s_w[kK1Threads / 32][3];
@@ -805,20 +823,7 @@ __global__ void __launch_bounds__(kK1Threads, MINB) k_vertex_phase_mixed(const C
         if (do_fa) {
             const ParamF& pf = c.pf;
             ff u0 = ff_add(ffx(f), cu0), u1 = ff_add(ffy(f), cu1), u2 = ffz(f);
-            if (c.has_sub && c.sub.moving) {
-                double wgt[3], Xd[3], fd[3];
-                pos_d(Xv, Xd);
-                vec_d(f, fd);
-                const int e = locate(c.sub, xs(Xd[0], fd[0]), xs(Xd[1], fd[1]), xs(Xd[2], fd[2]), wgt);
-                if (e >= 0) {
-                    const int4 t = c.sub.tri[e];
-                    const double4 a0 = ld4(c.sub.x + t.x), a1 = ld4(c.sub.x + t.y), a2 = ld4(c.sub.x + t.z);
-                    const double4 b0 = ld4(c.sub.X + t.x), b1 = ld4(c.sub.X + t.y), b2 = ld4(c.sub.X + t.z);
-                    u0 = ff_sub(u0, ff_from_d(wgt[0] * (a0.x - b0.x) + wgt[1] * (a1.x - b1.x) + wgt[2] * (a2.x - b2.x)));
-                    u1 = ff_sub(u1, ff_from_d(wgt[0] * (a0.y - b0.y) + wgt[1] * (a1.y - b1.y) + wgt[2] * (a2.y - b2.y)));
-                    u2 = ff_sub(u2, ff_from_d(wgt[0] * (a0.z - b0.z) + wgt[1] * (a1.z - b1.z) + wgt[2] * (a2.z - b2.z)));
-                }
-            }
+            if (c.has_sub && c.sub.moving) substrate_move(c, Xv, f, u0, u1, u2);
             // Bell kinetics (UL:2137-2171): k_off from the float-float force, the c_C update in float-float
             const ff F = bell_ff(pf, u0, u1, u2);
             const ff xa = ff_mul(F, {pf.iFa, pf.iFa_lo}), xb = ff_mul(F, {pf.iFb, pf.iFb_lo});
