@@ -346,3 +346,94 @@ def test_mixed_protruding_cell():
     u = out[capi.PREC_FP64] - x0
     err = np.max(np.abs(out[capi.PREC_MIXED] - out[capi.PREC_FP64])) / np.max(np.abs(u))
     assert err <= MIXED_TOL, err
+
+
+def _fused_cells():
+    """Cells that reach every branch of the fused step: small and large meshes, the
+    three laws and the MD table, an integrin mask, a protruding edge, a moving state."""
+    cells = []
+    for i, (n, var, law) in enumerate([(180, "k1", 0), (900, "kMD", 0), (2600, "k31", 2), (5200, "k31", 0)]):
+        x0, tri = synth.disk_mesh(n, seed=500 + i)
+        p = _law(default_params(var), law)
+        p.stream = i
+        st = synth.initial_state(x0, perturb=1.0 if i % 2 else 0.0, seed=i)
+        rho = np.where(np.random.default_rng(i).random(len(x0)) < 0.5, p.rho_i_max, 0.0) if i == 2 else None
+        cells.append((x0, tri, p, st, rho, 0.2 * i))
+    x0, tri, p, rho = synth.protruding_cell(n_target=1200)
+    cells.append((x0, tri, p, synth.initial_state(x0), rho, 0.0))
+    return cells
+
+
+def _run_mixed(cells, calls, fused, graphs=False, shape=None, kind=1):
+    e = capi.Engine(capi.PREC_MIXED)
+    if shape:
+        e.set_shape(*shape)
+    e.set_patch_kernel(kind)
+    e.set_fused(fused)
+    e.set_graphs(graphs)
+    hs = []
+    for x0, tri, p, st, rho, t in cells:
+        h = e.add_cell(x0, tri, p, state=st, t=t)
+        if rho is not None:
+            h.set_integrins(rho)
+        hs.append(h)
+    assert e.fused() == (fused and kind != 0)
+    snaps = []
+    for n in calls:
+        e.step(n, 5e-5)
+        snaps.append([h.get_state() for h in hs] + [[h.clock() for h in hs]])
+    assert all(h.status() == 0 for h in hs)
+    e.close()
+    return snaps
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+def test_fused_steps_equal_unfused(graphs):
+    """A fused run of steps (each next vertex phase inside the patch phase) is the unfused
+    computation bit for bit, in the state left after every call: calls of 1, 2, 3, 17 and 9
+    steps, eager and from captured graphs (whose middle steps replay as one graph)."""
+    cells = _fused_cells()
+    calls = [1, 2, 3, 17, 9]
+    ref = _run_mixed(cells, calls, fused=False)
+    got = _run_mixed(cells, calls, fused=True, graphs=graphs)
+    for a, b in zip(ref, got):
+        for u, w in zip(a, b):
+            for x, y in zip(u, w):
+                assert np.array_equal(np.asarray(x), np.asarray(y))
+
+
+@pytest.mark.parametrize("shape,kind", [((32, 128), 1), ((64, 256), 1), ((128, 768), 1), ((128, 512), 2),
+                                        ((128, 192), 4)])
+def test_fused_steps_equal_unfused_shapes(shape, kind):
+    """The fused area sum has one order whatever the patch block size (32, 64 or 128
+    threads) and register cap: bit-identical to the unfused steps."""
+    cells = _fused_cells()[1:4]
+    ref = _run_mixed(cells, [12], fused=False, shape=shape, kind=kind)
+    got = _run_mixed(cells, [12], fused=True, shape=shape, kind=kind)
+    for u, w in zip(ref[0], got[0]):
+        for x, y in zip(u, w):
+            assert np.array_equal(np.asarray(x), np.asarray(y))
+
+
+def test_fused_flag():
+    """Fused runs are off by default, apply to the plain patch kernels of a mixed engine,
+    and never to the staged patch kernel or the FP64 form."""
+    x0, tri = synth.disk_mesh(300, seed=1)
+    e = capi.Engine(capi.PREC_MIXED)
+    e.add_cell(x0, tri, default_params("k1"))
+    assert not e.fused()
+    e.set_fused(True)
+    assert e.fused()
+    e.set_patch_kernel(0)
+    assert not e.fused()
+    e.set_patch_kernel(1)
+    e.set_fused(False)
+    assert not e.fused()
+    with pytest.raises(capi.WcfeError):
+        e.set_shape(256, 512)   # the mixed patch kernels run at most 128 threads
+    e.close()
+    f = capi.Engine(capi.PREC_FP64)
+    f.add_cell(x0, tri, default_params("k1"))
+    f.set_fused(True)
+    assert not f.fused()
+    f.close()

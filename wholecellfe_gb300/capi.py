@@ -95,6 +95,8 @@ SIGNATURES = {
     "wcfe_engine_set_patch_kernel": (C.c_int, [C.c_void_p, C.c_int32]),
     "wcfe_engine_set_vertex_kernel": (C.c_int, [C.c_void_p, C.c_int32]),
     "wcfe_engine_get_kernels": (C.c_int, [C.c_void_p, _i, _i]),
+    "wcfe_engine_set_fused": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_engine_get_fused": (C.c_int, [C.c_void_p]),
     "wcfe_cell_set_element_mu": (C.c_int, [C.c_void_p, C.c_int32, _d]),
     "wcfe_cell_couple_substrate": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
     "wcfe_engine_step_implicit": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_void_p]),
@@ -354,6 +356,14 @@ class Engine:
 
     def set_vertex_kernel(self, kind: int):
         check(load().wcfe_engine_set_vertex_kernel(self.h, kind), "wcfe_engine_set_vertex_kernel")
+
+    def set_fused(self, enable: bool):
+        """Mixed engines: fold each next vertex phase into the patch phase in runs of steps."""
+        check(load().wcfe_engine_set_fused(self.h, 1 if enable else 0), "wcfe_engine_set_fused")
+
+    def fused(self) -> bool:
+        """True where a run of steps of this engine is fused."""
+        return load().wcfe_engine_get_fused(self.h) == 1
 
     def kernels(self):
         """(patch kernel kind, vertex kernel kind) in use."""

@@ -13,7 +13,7 @@
 //   bnd_optr [nb+1], bnd_out: directed boundary edges; bnd_vert [nb] boundary vertices by rank
 //   k1_part [nk1][4] double: per-block partial sums of area and area-weighted centroid
 //   area4 [4] double: cell area and centroid of the predicted positions (written by the vertex phase)
-//   rec [nv][3] float4: mixed form only, the FP32 element inputs of each vertex
+//   rec[2][nv][3] float4: mixed form only, the FP32 element inputs of each vertex, by step parity
 #pragma once
 #include <cstdint>
 
@@ -91,7 +91,7 @@ struct CellDev {
     const int32_t* bnd_out;     //        and their end vertices (the boundary loop, mixed-form area)
     double* k1_part;
     double* area4;              // {A, cx, cy, cz} of the positions after predict, reduced by the vertex phase
-    float4* rec;                // mixed form: per-vertex FP32 element inputs [nv][4] (see wcfe_mixed.cu)
+    float4* rec[2];             // mixed form: per-vertex FP32 element inputs [nv][3] by step parity (wcfe_mixed.cu)
     const int32_t* bnd_vert;    // [nb] boundary vertices in rank order (the inverse of bnd_rank)
     // control words, advanced by the last patch-phase CTA of the cell to finish a step:
     int32_t* ctl;               // [0] parity (which pos/ea buffer holds the step-start state), [1] patch-phase

@@ -36,7 +36,7 @@ size_t mixed_smem_bytes(int emax);
 int mixed_occupancy(int threads, size_t smem, int kind);
 void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt, double dt_real,
                         double ap_thresh, double t_override, int vh_from_buf, int threads, int grid, cudaStream_t st,
-                        int kind);
+                        int kind, int fused);
 int patch_occupancy(int prec, int threads, size_t smem);
 int vertex_occupancy(int threads);
 bool mixed_available();
@@ -143,6 +143,7 @@ struct Graph {
     cudaGraphExec_t exec = nullptr;
     double dt = 0;
     int steps = 0;
+    int kind = 0;                 // the step kind captured (STEP_FULL or STEP_MID)
     uint64_t version = 0;
 };
 
@@ -200,6 +201,7 @@ struct wcfe_engine {
     int vblock = 256;             // vertices (threads) per vertex-phase block
     int vertex_kind = 0;          // mixed form: vertex-phase kernel for 5 (0) or 4 (1) blocks per SM
     int patch_kernel = 1;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
+    bool fused = false;           // mixed form: runs of steps fold each next vertex phase into the patch phase
     int lu_nb = 512, lu_kind = 0; // implicit step's LU: outer block width, 0 tcgen05 / 1 mma.sync updates
     int lu_reuse = 1;             // 1: factor once per implicit step, 0: every Newton iteration
     int cap_ne = 0, cap_nvp = 0, cap_nh = 0, cap_nc = 0;   // largest patch over the cells (staging plan)
@@ -242,7 +244,7 @@ Cell* find(wcfe_engine* e, int32_t id) {
 }
 
 // ---- device memory of a cell -------------------------------------------------
-size_t state_layout(int32_t nv, int32_t nt, int32_t nb, int32_t ncand, int32_t nk1, bool rec, size_t* off /* 24 */) {
+size_t state_layout(int32_t nv, int32_t nt, int32_t nb, int32_t ncand, int32_t nk1, bool rec, size_t* off /* 28 */) {
     size_t o = 0;
     int i = 0;
     auto put = [&](size_t bytes) { off[i++] = o; o = align_up(o + bytes); };
@@ -272,7 +274,8 @@ size_t state_layout(int32_t nv, int32_t nt, int32_t nb, int32_t ncand, int32_t n
     put(sizeof(double) * 4);     // 23 area4
     put(sizeof(int32_t) * std::max(nb, 1));  // 24 bnd_vert: boundary vertices in rank order
     put(128);                    // 25 step constants of the mixed form (written by its vertex phase)
-    put(64);                     // 26 slack: 16-B-rounded bulk copies of the last arrays stay in the block
+    put(rec ? sizeof(float4) * 3 * (size_t)nv : 0);  // 26 the second buffer of element records (by step parity)
+    put(64);                     // 27 slack: 16-B-rounded bulk copies of the last arrays stay in the block
     return o;
 }
 
@@ -371,7 +374,8 @@ void bind_state(Cell* c, char* b, const size_t* off, int32_t nk1, int32_t vblock
     d.clk = (double*)(b + off[17]);
     d.ap = (unsigned long long*)(b + off[18]);
     d.status = (uint32_t*)(b + off[19]);
-    d.rec = mixed ? (float4*)(b + off[20]) : nullptr;
+    d.rec[0] = mixed ? (float4*)(b + off[20]) : nullptr;
+    d.rec[1] = mixed ? (float4*)(b + off[26]) : nullptr;
     d.area4 = (double*)(b + off[23]);
     d.bnd_vert = (const int32_t*)(b + off[24]);
     d.stepc = (float4*)(b + off[25]);
@@ -702,9 +706,27 @@ void xjoin(wcfe_engine* e) {
     e->xpending = false;
 }
 
+// The kinds of step in a run of explicit steps.  A mixed engine folds the vertex phase of
+// step s + 1 into the patch phase of step s (each patch predicts its owned vertices once
+// their update is done, and the cell's last patch forms the next area): the first step of
+// a run launches the vertex phase and a fused patch phase, the middle steps one fused
+// patch phase each, and the last step a plain patch phase, so that between runs the state
+// is exactly that of the unfused steps.  The arithmetic is the same either way.
+enum { STEP_FULL = 0, STEP_FIRST = 1, STEP_MID = 2, STEP_LAST = 3 };
+
+// fused runs: the mixed form's plain patch kernels, no coupled substrate (whose patch phase
+// must follow its cells' before their next prediction)
+bool fused_ok(const wcfe_engine* e) {
+    return e->prec == WCFE_PREC_MIXED && e->fused && e->patch_kernel != 0 && e->n2_sub == 0;
+}
+int step_kind(const wcfe_engine* e, int s, int n) {
+    if (n < 2 || !fused_ok(e)) return STEP_FULL;
+    return s == 0 ? STEP_FIRST : (s == n - 1 ? STEP_LAST : STEP_MID);
+}
+
 // the patch phase of a step (STEP mode): the staged mixed kernel where it applies
 void patch_step(wcfe_engine* e, const WorkItem* k2, int n2, double dt, double dt_real, double apt, double t_override,
-                int vh_from_buf, cudaStream_t st = nullptr) {
+                int vh_from_buf, cudaStream_t st = nullptr, int fused = 0) {
     if (!st) st = e->stream;
     if (e->prec == WCFE_PREC_MIXED) {
         if (e->patch_kernel == 0 &&
@@ -714,7 +736,8 @@ void patch_step(wcfe_engine* e, const WorkItem* k2, int n2, double dt, double dt
         const int kind = e->patch_kernel == 0 ? 1 : e->patch_kernel;
         const size_t smem = mixed_smem_bytes(e->patch_emax);
         launch_patch_mixed(e->d_table, k2, n2, e->patch_emax, dt, dt_real, apt, t_override, vh_from_buf,
-                           e->patch_threads, grid_for(e, n2, mixed_occupancy(e->patch_threads, smem, kind)), st, kind);
+                           e->patch_threads, grid_for(e, n2, mixed_occupancy(e->patch_threads, smem, kind)), st, kind,
+                           fused);
         return;
     }
     size_t smem = patch_smem_bytes(e->prec, PP_STEP, e->patch_emax);
@@ -723,16 +746,19 @@ void patch_step(wcfe_engine* e, const WorkItem* k2, int n2, double dt, double dt
                  grid_for(e, n2, patch_occupancy(e->prec, e->patch_threads, smem)), st);
 }
 
-// one explicit step of the cells listed in (k1, k2) device lists
-int enqueue_step(wcfe_engine* e, const WorkItem* k1, int n1, const WorkItem* k2, int n2, double dt) {
+// one explicit step of the cells listed in (k1, k2) device lists; kind: STEP_* above
+int enqueue_step(wcfe_engine* e, const WorkItem* k1, int n1, const WorkItem* k2, int n2, double dt,
+                 int kind = STEP_FULL) {
     const double apt = std::numeric_limits<double>::quiet_NaN();  // per-cell thresholds from the table
     int g1 = grid_for(e, n1, vertex_occupancy(e->vblock));
     cudaEvent_t* tv = (e->timing && e->tev.size() >= 3) ? &e->tev[3 * (size_t)e->timed_steps] : nullptr;
+    const bool vertex = kind == STEP_FULL || kind == STEP_FIRST;
     if (tv) cudaEventRecord(tv[0], e->stream);
-    vphase(e, e->d_table, k1, n1, dt, VP_PREDICT | VP_UPDATE_FA | rec_flag(e), g1, e->stream);
+    if (vertex) vphase(e, e->d_table, k1, n1, dt, VP_PREDICT | VP_UPDATE_FA | rec_flag(e), g1, e->stream);
     if (tv) cudaEventRecord(tv[1], e->stream);
     const int nsub = (k2 == e->d_k2 && n2 == (int)e->k2.size()) ? e->n2_sub : 0;
-    patch_step(e, k2, n2 - nsub, dt, dt, apt, std::numeric_limits<double>::quiet_NaN(), 0);
+    patch_step(e, k2, n2 - nsub, dt, dt, apt, std::numeric_limits<double>::quiet_NaN(), 0, nullptr,
+               (kind == STEP_FIRST || kind == STEP_MID) ? 1 : 0);
     if (nsub > 0) {   // substrate cells, after the reactions of their coupled cells
         patch_step(e, k2 + (n2 - nsub), nsub, dt, dt, apt, std::numeric_limits<double>::quiet_NaN(), 0);
         e->launches += 1;
@@ -741,7 +767,7 @@ int enqueue_step(wcfe_engine* e, const WorkItem* k1, int n1, const WorkItem* k2,
         cudaEventRecord(tv[2], e->stream);
         e->timed_steps++;
     }
-    e->launches += 2;
+    e->launches += vertex ? 2 : 1;
     CK(cudaGetLastError());
     return WCFE_OK;
 }
@@ -1528,34 +1554,43 @@ int wcfe_engine_step(wcfe_engine* e, int32_t nsteps, double dt) {
     if (r) return r;
     const int n1 = (int)e->k1.size(), n2 = (int)e->k2.size();
     if (e->use_graphs && !e->timing) {
-        const int chunk = std::min(nsteps, 8);
-        if (!e->graph.exec || e->graph.dt != dt || e->graph.version != e->version || e->graph.steps != chunk) {
+        // a fused run replays its middle steps from the graph; the first and last launch directly
+        const bool fz = step_kind(e, 0, nsteps) != STEP_FULL;
+        const int gkind = fz ? STEP_MID : STEP_FULL;
+        const int ngraph = fz ? nsteps - 2 : nsteps;
+        if (fz && (r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt, STEP_FIRST))) return r;
+        const int chunk = std::min(ngraph, 8);
+        const int per_step = gkind == STEP_MID ? 1 : 2;
+        if (chunk > 0 && (!e->graph.exec || e->graph.dt != dt || e->graph.version != e->version ||
+                          e->graph.steps != chunk || e->graph.kind != gkind)) {
             invalidate_graph(e);
             cudaGraph_t g;
             CK(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
             for (int s = 0; s < chunk; ++s) {
-                r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt);
+                r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt, gkind);
                 if (r) {
                     cudaStreamEndCapture(e->stream, &g);
                     return r;
                 }
             }
-            e->launches -= 2 * chunk;  // counted at replay
+            e->launches -= (uint64_t)per_step * chunk;  // counted at replay
             CK(cudaStreamEndCapture(e->stream, &g));
             CK(cudaGraphInstantiate(&e->graph.exec, g, 0));
             cudaGraphDestroy(g);
             e->graph.dt = dt;
             e->graph.version = e->version;
             e->graph.steps = chunk;
+            e->graph.kind = gkind;
         }
         int done = 0;
-        while (done + chunk <= nsteps) {
+        while (chunk > 0 && done + chunk <= ngraph) {
             CK(cudaGraphLaunch(e->graph.exec, e->stream));
-            e->launches += 2 * chunk;
+            e->launches += (uint64_t)per_step * chunk;
             done += chunk;
         }
-        for (; done < nsteps; ++done)
-            if ((r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt))) return r;
+        for (; done < ngraph; ++done)
+            if ((r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt, gkind))) return r;
+        if (fz && (r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt, STEP_LAST))) return r;
         return WCFE_OK;
     }
     if (e->timing) {
@@ -1569,7 +1604,7 @@ int wcfe_engine_step(wcfe_engine* e, int32_t nsteps, double dt) {
         e->timed_steps = 0;
     }
     for (int s = 0; s < nsteps; ++s)
-        if ((r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt))) return r;
+        if ((r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt, step_kind(e, s, nsteps)))) return r;
     if (e->timing) {
         CK(cudaEventSynchronize(e->tev[3 * (size_t)e->timed_steps - 1]));
         e->ms_v = e->ms_p = 0;
@@ -1626,6 +1661,7 @@ int wcfe_engine_set_shape(wcfe_engine* e, int32_t threads, int32_t emax) {
     if (threads == 0) threads = e->patch_threads;
     if (emax == 0) emax = e->patch_emax;
     if (threads % 32 || threads < 32 || threads > 512 || emax < 32 || emax > 4096) return fail("bad shape", WCFE_ERR_ARG);
+    if (e->prec == WCFE_PREC_MIXED && threads > 128) return fail("mixed patch kernels run at most 128 threads", WCFE_ERR_ARG);
     int max_optin = 0;
     cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->device);
     if (patch_smem_bytes(e->prec, PP_RESIDUAL, emax) + 1024 > (size_t)max_optin) return fail("shape exceeds shared memory", WCFE_ERR_LIMIT);
@@ -1666,6 +1702,16 @@ int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind) {
     invalidate_graph(e);
     return WCFE_OK;
 }
+
+int wcfe_engine_set_fused(wcfe_engine* e, int32_t enable) {
+    xjoin(e);
+    if (!e || enable < 0 || enable > 1) return fail("bad argument", WCFE_ERR_ARG);
+    e->fused = enable != 0;
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
+int wcfe_engine_get_fused(const wcfe_engine* e) { return e ? (fused_ok(e) ? 1 : 0) : -1; }
 
 int wcfe_engine_set_vertex_kernel(wcfe_engine* e, int32_t kind) {
     xjoin(e);
@@ -2732,7 +2778,7 @@ int serving_step(wcfe_engine* e, int32_t nsteps, double dt) {
     if (r) return r;
     const int n1 = (int)e->k1.size(), n2 = (int)e->k2.size();
     for (int s = 0; s < nsteps; ++s)
-        if ((r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt))) return r;
+        if ((r = enqueue_step(e, e->d_k1, n1, e->d_k2, n2, dt, step_kind(e, s, nsteps)))) return r;
     return WCFE_OK;
 }
 

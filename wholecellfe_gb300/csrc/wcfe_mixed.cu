@@ -45,6 +45,16 @@
 
 namespace wcfe {
 
+// the vertex phase's step arguments (predict, bond kinetics, element records)
+struct VertexArgs {
+    ff dt, hdt;
+    double dtd;
+    float dtf;
+    int flags;
+    const double* stage_in;
+    double* stage_out;
+};
+
 struct MixedArgs {
     const CellDev* cells;
     const WorkItem* work;
@@ -52,6 +62,10 @@ struct MixedArgs {
     double dt_real, ap_thresh, t_override;
     ff hdt, cdt, dtr;        // dt/2, dt_real - dt/2, dt_real as float-float
     int vh_from_buf, half;   // half = dt_real > dt/2
+    // fused != 0: after its owned vertices' update, each patch also runs the next step's vertex
+    // phase on them (arguments va), and the cell's last patch forms the next step's area
+    int fused;
+    VertexArgs va;
 };
 
 // The mixed engine's state arrays hold float-float values (wcfe_ff.cuh) in the
@@ -391,6 +405,14 @@ __device__ __forceinline__ bool boundary_frame_ff(const CellDev& c, const double
     return true;
 }
 
+// The step-start position of vertex j as its element record holds it: triple-float x, y
+// (the record's float-float (h, m) pair and the third floats in its last two slots).
+__device__ __forceinline__ void rec_pos(const float4* __restrict__ rp, int j, tf& x, tf& y) {
+    const float4 r0 = __ldg(rp + kRec * (size_t)j), r2 = __ldg(rp + kRec * (size_t)j + 2);
+    x = {r0.x, r0.z, r2.z};
+    y = {r0.y, r0.w, r2.w};
+}
+
 // Boundary terms of vertex v (rank `rank`) added to (F0, F1) in float-float, on the
 // triple-float positions: the isotropic active stress of the open one-ring, AP push
 // (calculateForce_AP UL:1477-1569), bending (calculateBendingForce2D UL:1571-1689) and
@@ -402,8 +424,11 @@ __device__ __forceinline__ bool boundary_frame_ff(const CellDev& c, const double
 // 1 - cos(theta) is |e1 - e2|^2 / 2 with e1 - e2 = (d1 l2 - d2 l1) / (l1 l2); the unit
 // normal is (d1 + d2) x e3 / L, the reference's length-weighted mean of the two edge
 // normals.  The AP bond count ceil(density L / 2) is taken on the float-float L.
+// The step-start positions X come from the step's element records rp (the step-start
+// position buffer may be overwritten by a fused next-step prediction while this runs);
+// xp holds the predicted positions.
 __device__ __forceinline__ void boundary_force(const CellDev& c, const BndConst& bc, const int4& pt,
-                                               const double4* __restrict__ X, const double4* __restrict__ xp, int v,
+                                               const float4* __restrict__ rp, const double4* __restrict__ xp, int v,
                                                int rank, ff& F0, ff& F1) {
     const ff4 xi = ldg_ff4(xp, c.nv, v);
     // isotropic active stress on the open one-ring: (1/2) s_iso thick e3 x sum (X_k - X_j)
@@ -414,9 +439,11 @@ __device__ __forceinline__ void boundary_force(const CellDev& c, const BndConst&
         const int e = c.patch_elems[pt.z + (code >> 2)];
         const int4 t4 = c.tri[e];
         const int ids[3] = {t4.x, t4.y, t4.z};
-        const ff4 Xj = ldg_ff4(X, c.nv, ids[(cn + 1) % 3]), Xk = ldg_ff4(X, c.nv, ids[(cn + 2) % 3]);
-        sx = ff_add(sx, tf_sub(tfx(Xk), tfx(Xj)));
-        sy = ff_add(sy, tf_sub(tfy(Xk), tfy(Xj)));
+        tf Xjx, Xjy, Xkx, Xky;
+        rec_pos(rp, ids[(cn + 1) % 3], Xjx, Xjy);
+        rec_pos(rp, ids[(cn + 2) % 3], Xkx, Xky);
+        sx = ff_add(sx, tf_sub(Xkx, Xjx));
+        sy = ff_add(sy, tf_sub(Xky, Xjy));
     }
     ff Fb0 = ff_mul(bc.w, sy), Fb1 = ff_mul(bc.w, sx);   // minus the residual term w e3 x s
     Fb1 = {-Fb1.hi, -Fb1.lo};
@@ -469,15 +496,217 @@ __device__ __forceinline__ void protrude_ff(const CellDev& c, int v, const ff4& 
     vh1 = ff_mul_f({pf.pv, pf.pv_lo}, dy / r);
 }
 
+// ===========================================================================
+// mixed-form vertex phase: predict (triple-float positions), bond kinetics with FP32
+// rates and float-float accumulation, the FP32 element records, and the cell area and
+// area-weighted centroid from the boundary loop (shoelace over the directed
+// boundary edges).  For a planar mesh without inverted elements that equals
+// calculateAreaTot's sum of element areas.
+// ===========================================================================
+enum { VM_PREDICT = 1, VM_UPDATE_FA = 2, VM_EXPORT = 8, VM_IMPORT = 16, VM_NOAREA = 32 };
+
+// The substrate's displacement under a bond's anchor (a rigid substrate mesh moved by the
+// caller), subtracted from the bond vector (UL:2053-2099).  Out of line: few cells have
+// one, and its FP64 point location would otherwise set the register budget of every block.
+__device__ __noinline__ void substrate_move(const CellDev& c, const ff4& Xv, const ff4& f, ff& u0, ff& u1, ff& u2) {
+    double wgt[3], Xd[3], fd[3];
+    pos_d(Xv, Xd);
+    vec_d(f, fd);
+    const int e = locate(c.sub, xs(Xd[0], fd[0]), xs(Xd[1], fd[1]), xs(Xd[2], fd[2]), wgt);
+    if (e >= 0) {
+        const int4 t = c.sub.tri[e];
+        const double4 a0 = ld4(c.sub.x + t.x), a1 = ld4(c.sub.x + t.y), a2 = ld4(c.sub.x + t.z);
+        const double4 b0 = ld4(c.sub.X + t.x), b1 = ld4(c.sub.X + t.y), b2 = ld4(c.sub.X + t.z);
+        u0 = ff_sub(u0, ff_from_d(wgt[0] * (a0.x - b0.x) + wgt[1] * (a1.x - b1.x) + wgt[2] * (a2.x - b2.x)));
+        u1 = ff_sub(u1, ff_from_d(wgt[0] * (a0.y - b0.y) + wgt[1] * (a1.y - b1.y) + wgt[2] * (a2.y - b2.y)));
+        u2 = ff_sub(u2, ff_from_d(wgt[0] * (a0.z - b0.z) + wgt[1] * (a1.z - b1.z) + wgt[2] * (a2.z - b2.z)));
+    }
+}
+
+// The cell area and centroid of the predicted positions xo (shoelace over the directed
+// boundary edges), then the step constants of the patch phase that follows.  Called by all
+// threads of one block of any size that is a multiple of 32 dividing 256, after every
+// prediction of the cell is visible to it; the sum has one fixed order whatever the block
+// size: boundary ranks strided over 256 virtual threads, the 32 lanes of each virtual warp
+// by a butterfly, then the 8 virtual warps in order.  s_w: 24 doubles of shared scratch.
+__device__ void area_shoelace(const CellDev& c, const double4* xo, double dt_real, double* s_w) {
+    constexpr int kVW = kK1Threads / 32;
+    const int lane = threadIdx.x & 31;
+    for (int vw = threadIdx.x >> 5; vw < kVW; vw += blockDim.x >> 5) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        for (int r = vw * 32 + lane; r < c.nb; r += kK1Threads) {
+            double xi[3];
+            pos_d(ld_ff4(xo, c.nv, c.bnd_vert[r]), xi);
+            for (int k = c.bnd_optr[r]; k < c.bnd_optr[r + 1]; ++k) {
+                double xj[3];
+                pos_d(ld_ff4(xo, c.nv, c.bnd_out[k]), xj);
+                const double cr = xi[0] * xj[1] - xj[0] * xi[1];
+                s0 += 0.5 * cr;
+                s1 += (1.0 / 6.0) * (xi[0] + xj[0]) * cr;
+                s2 += (1.0 / 6.0) * (xi[1] + xj[1]) * cr;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        }
+        if (lane == 0) {
+            s_w[3 * vw] = s0; s_w[3 * vw + 1] = s1; s_w[3 * vw + 2] = s2;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double A = 0, Ax = 0, Ay = 0;
+        for (int w = 0; w < kVW; ++w) {
+            A += s_w[3 * w]; Ax += s_w[3 * w + 1]; Ay += s_w[3 * w + 2];
+        }
+        c.area4[0] = A;
+        c.area4[1] = Ax / A;
+        c.area4[2] = Ay / A;
+        c.area4[3] = 0.0;
+        *reinterpret_cast<StepConst*>(c.stepc) = make_step_const(c, dt_real, A, Ax / A, Ay / A);
+    }
+    __syncthreads();   // the scratch may be reused by the caller
+}
+
+// The vertex phase's cell area: the last block of the cell to finish (ticket ctl[2]) reads
+// the positions the other blocks wrote (through L2) and runs area_shoelace.
+__device__ __forceinline__ void finish_area_boundary(const CellDev& c, const double4* xo, double dt_real) {
+    __shared__ int s_last;
+    __shared__ double s_w[3 * kK1Threads / 32];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned int t = atomicAdd(reinterpret_cast<unsigned int*>(c.ctl + 2), 1u);
+        s_last = ((int)t == c.nk1 - 1);
+        if (s_last) c.ctl[2] = 0;
+    }
+    __syncthreads();
+    if (!s_last) return;   // block-uniform
+    __threadfence();
+    area_shoelace(c, xo, dt_real, s_w);
+}
+
+// The prediction of vertex v at step parity par from its step-start position Xv, velocity V
+// and acceleration A: vh = V + (dt/2) A (or the protrusion driver), x = X + dt vh, stored
+// in pos[par ^ 1] (and, for the exchange path, vh and x as binary64 for the host).
+__device__ __forceinline__ void vertex_predict(const CellDev& c, int v, int par, const VertexArgs& va, const ff4& Xv,
+                                               const ff4& V, const float4& A, tf& xn0, tf& xn1, ff& xn2) {
+    ff vh0 = ff_add(ffx(V), ff_mul_f(va.hdt, A.x)), vh1 = ff_add(ffy(V), ff_mul_f(va.hdt, A.y));
+    protrude_ff(c, v, Xv, vh0, vh1);
+    xn0 = tf_add_ff(tfx(Xv), ff_mul(va.dt, vh0));
+    xn1 = tf_add_ff(tfy(Xv), ff_mul(va.dt, vh1));
+    xn2 = ffz(Xv);
+    st_ff4(c.pos[par ^ 1], c.nv, v, make_pos4(xn0, xn1, xn2));
+    if (va.flags & VM_EXPORT) {
+        st_ff4(c.vhl, c.nv, v, make_ff4(vh0, vh1, {0.0f, 0.0f}));
+        double* qq = va.stage_out + 3 * (size_t)(c.hoff + v);
+        qq[0] = tf_to_d(xn0); qq[1] = tf_to_d(xn1); qq[2] = ff_to_d(xn2);
+    }
+}
+
+// Bond kinetics of vertex v at step parity par on the step displacement x - X (bond vector
+// f, bond density c_C = cold, c_A = cAv as loaded before), and its FP32 element record
+// rec[par] (strain hi eh).
+__device__ __forceinline__ void vertex_kinetics(const CellDev& c, int v, int par, const VertexArgs& va, const ff4& Xv,
+                                                const ff4& f, ff cold, ff cAv, const float4& eh, const tf& xn0,
+                                                const tf& xn1) {
+    const int flags = va.flags;
+    const ff cu0 = tf_sub(xn0, tfx(Xv)), cu1 = tf_sub(xn1, tfy(Xv));   // step displacement
+    if (flags & VM_UPDATE_FA) {
+        const ParamF& pf = c.pf;
+        ff u0 = ff_add(ffx(f), cu0), u1 = ff_add(ffy(f), cu1), u2 = ffz(f);
+        if (c.has_sub && c.sub.moving) substrate_move(c, Xv, f, u0, u1, u2);
+        // Bell kinetics (UL:2137-2171): k_off from the float-float force, the c_C update in float-float
+        const ff F = bell_ff(pf, u0, u1, u2);
+        const ff xa = ff_mul(F, {pf.iFa, pf.iFa_lo}), xb = ff_mul(F, {pf.iFb, pf.iFb_lo});
+        // the exponent is capped below FP32 overflow (e^88 ~ 1.7e38): any force that large already
+        // gives dt k_off >> 1, i.e. the same decisions as the unbounded FP64 rate
+        const float koff = pf.ka * expf(fminf(xa.hi, 88.0f)) * (1.0f + xa.lo) + pf.kb * expf(-xb.hi) * (1.0f - xb.lo);
+        const float coldf = cold.hi, kon = pf.k_on, dtf = va.dtf;
+        const ff rate = ff_sub(ff_mul_f(ff_sub({1.0f, 0.0f}, cold), kon), ff_mul_f(cold, koff));
+        ff cn = ff_add(cold, ff_mul(va.dt, rate));
+        if (cn.hi < 0.0f) cn = {0.0f, 0.0f};
+        if (cAv.hi < 0.0f) st_ff(c.cA, c.nv, v, {0.0f, 0.0f});
+        ff n0, n1, n2;
+        const bool keep_pos = coldf > 0.0f && (1.0f - dtf * koff) > 0.0f;
+        if (keep_pos && cn.hi > 0.0f) {
+            // keep / c_new = 1 + ds with ds = -dt k_on (1 - c_old) / c_new exactly
+            const float ds = -dtf * kon * (1.0f - coldf) / cn.hi;
+            n0 = ff_add(u0, ff_mul_f(u0, ds)); n1 = ff_add(u1, ff_mul_f(u1, ds)); n2 = ff_add(u2, ff_mul_f(u2, ds));
+        } else {
+            n0 = {0.0f * u0.hi, 0.0f}; n1 = {0.0f * u1.hi, 0.0f}; n2 = {0.0f * u2.hi, 0.0f};
+        }
+        st_ff(c.cC, c.nv, v, cn);
+        st_ff4(c.fau, c.nv, v, make_ff4(n0, n1, n2));
+    }
+    if (!(flags & VM_EXPORT)) {
+        // r0 = (X.x h, X.y h, X.x m, X.y m), r1 = (u.x, u.y, exx, eyy), r2 = (exy, ezz, X.x l, X.y l)
+        float4* r = c.rec[par] + kRec * (size_t)v;
+        r[0] = make_float4(Xv.hx, Xv.hy, Xv.lx, Xv.ly);
+        r[1] = make_float4(cu0.hi, cu1.hi, eh.x, eh.y);
+        r[2] = make_float4(eh.w, eh.z, Xv.hw, Xv.lw);
+    }
+    // boundary positions are read by the block that finishes the area
+    if (!(flags & VM_NOAREA) && c.bnd_rank[v] >= 0) __threadfence();
+}
+
+// One vertex of the vertex phase at step parity par: predict into pos[par ^ 1] (or take
+// the caller's positions), bond kinetics with FP32 rates and float-float accumulation,
+// and the FP32 element record rec[par].
+__device__ __forceinline__ void vertex_mixed_body(const CellDev& c, int v, int par, const VertexArgs& va) {
+    const int flags = va.flags;
+    double4* __restrict__ xo = c.pos[par ^ 1];
+    const ff4 Xv = ldg_ff4(c.pos[par], c.nv, v);
+    // every load of this vertex's state up front: none depends on the prediction's stores
+    const bool do_fa = (flags & VM_UPDATE_FA) != 0;
+    const ff4 f = do_fa ? ldg_ff4(c.fau, c.nv, v) : ff4{};
+    const ff cold = do_fa ? ld_ff(c.cC, c.nv, v) : ff{0.0f, 0.0f};
+    const ff cAv = do_fa ? ld_ff(c.cA, c.nv, v) : ff{0.0f, 0.0f};
+    const float4 eh = __ldg(reinterpret_cast<const float4*>(c.ea[par]) + v);   // (xx, yy, zz, xy) hi
+    // positions are triple-float (wcfe_ff.cuh); the step displacement cu is float-float
+    tf xn0, xn1;
+    ff xn2 = ffz(Xv);
+    if (flags & VM_IMPORT) {
+        // a coordinate the caller returned as the binary64 rounding of the predicted one keeps
+        // the predicted triple-float (so the exchange path steps exactly as the internal one);
+        // any other value is taken as given
+        const double* qq = va.stage_in + 3 * (size_t)(c.hoff + v);
+        const ff4 pr = ld_ff4(xo, c.nv, v);
+        const tf p0 = tfx(pr), p1 = tfy(pr);
+        xn0 = tf_to_d(p0) == qq[0] ? p0 : tf_from_d(qq[0]);
+        xn1 = tf_to_d(p1) == qq[1] ? p1 : tf_from_d(qq[1]);
+        xn2 = ff_from_d(qq[2]);
+        st_ff4(xo, c.nv, v, make_pos4(xn0, xn1, xn2));
+    } else if (flags & VM_PREDICT) {
+        vertex_predict(c, v, par, va, Xv, ldg_ff4(c.vel, c.nv, v), ld_acc(c.acc, v), xn0, xn1, xn2);
+    } else {
+        const ff4 t = ld_ff4(xo, c.nv, v);
+        xn0 = tfx(t); xn1 = tfy(t); xn2 = ffz(t);
+    }
+    vertex_kinetics(c, v, par, va, Xv, f, cold, cAv, eh, xn0, xn1);
+}
+
+// The next step's vertex-phase inputs of an owned vertex in a fused patch phase: its
+// predicted position (the next step-start position), bond vector, c_C and c_A.
+struct FusedIn {
+    ff4 X, f;
+    ff cold, cA;
+};
+
 // Explicit update of vertex v (UL:592-628): the acceleration in FP32 from the force; the
 // velocity and the strain accumulate in float-float.  A boundary vertex (exact = true)
 // brings a float-float force and forms F - drag vh - damp m V in float-float (its terms
 // nearly cancel); an interior vertex brings its FP32 force (F0.lo = 0).  V, A and the
 // strain (xx yy zz xy, hi and lo) come in from the caller (global memory or a staged copy).
+// nx (fused patch phase): the vertex's next-step inputs; the next step's vertex phase then
+// runs on it here, from the new velocity, acceleration and strain still in registers.
 __device__ __forceinline__ void finish_vertex_core(const CellDev& c, const MixedArgs& a, int par, int v, ff F0,
                                                    ff F1, bool exact, float Q0, float Q1, float Q2, float Q3,
                                                    float MMf, const ff4& V, const float4& A, const float4& eh,
-                                                   const float4& el) {
+                                                   const float4& el, const FusedIn* nx = nullptr) {
     const ParamF& pf = c.pf;
     ff vh0, vh1;
     if (a.vh_from_buf) {
@@ -521,14 +750,29 @@ __device__ __forceinline__ void finish_vertex_core(const CellDev& c, const Mixed
     // NaN/Inf in the state shows up in the FP32 quantities derived from it
     const float chk = An0 + An1 + Q0 + Q1 + Q2 + vh0.hi + vh1.hi;
     if (!isfinite(chk)) atomicOr(c.status, 1u);
+    if (nx) {   // the next step's vertex phase of v, on the values just stored
+        tf xn0, xn1;
+        ff xn2;
+        vertex_predict(c, v, par ^ 1, a.va, nx->X, make_ff4(Vn0, Vn1, Vn2), make_float4(An0, An1, An2, 0.0f), xn0,
+                       xn1, xn2);
+        vertex_kinetics(c, v, par ^ 1, a.va, nx->X, nx->f, nx->cold, nx->cA,
+                        make_float4(exx.hi, eyy.hi, ezz.hi, exy.hi), xn0, xn1);
+    }
+}
+
+// the next-step inputs of vertex v of a fused patch phase at parity par
+__device__ __forceinline__ FusedIn fused_in(const CellDev& c, int par, int v) {
+    return {ldg_ff4(c.pos[par ^ 1], c.nv, v), ldg_ff4(c.fau, c.nv, v), ld_ff(c.cC, c.nv, v), ld_ff(c.cA, c.nv, v)};
 }
 
 __device__ __forceinline__ void finish_vertex(const CellDev& c, const MixedArgs& a, int par, int v, ff F0, ff F1,
-                                              float Q0, float Q1, float Q2, float Q3, float MMf) {
+                                              float Q0, float Q1, float Q2, float Q3, float MMf, bool fuse) {
     const float4* eo = reinterpret_cast<const float4*>(c.ea[par]);
     const float4 A = a.vh_from_buf ? make_float4(0.f, 0.f, 0.f, 0.f) : ld_acc(c.acc, v);
+    FusedIn nx;
+    if (fuse) nx = fused_in(c, par, v);
     finish_vertex_core(c, a, par, v, F0, F1, true, Q0, Q1, Q2, Q3, MMf, ldg_ff4(c.vel, c.nv, v), A, __ldg(eo + v),
-                       __ldg(eo + c.nv + v));
+                       __ldg(eo + c.nv + v), fuse ? &nx : nullptr);
 }
 
 // kfa f - R as float-float (the boundary vertices' force before their boundary terms)
@@ -546,7 +790,7 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a) {
     extern __shared__ float smf[];
     const int emax = a.emax;
     // structure of arrays: field k of slot j at smf[k * emax + j]
-    __shared__ int s_nbnd;
+    __shared__ int s_nbnd, s_last;
     __shared__ float s_bnd[kBndRec * kBndSlots];
     if (threadIdx.x == 0) s_nbnd = 0;
     __syncthreads();
@@ -554,11 +798,13 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a) {
         const WorkItem it = a.work[w];
         const CellDev& c = a.cells[it.cell];
         if (cell_done(c)) continue;   // block-uniform: a serving cell that ran its steps
+        // fused: predict the cell's next step here unless this step is the last of its budget
+        // (ctl[3] is counted down only after every patch of the cell took its ticket)
+        const bool fuse = a.fused && c.ctl[3] != 1;
         const int4 pt = c.patch[it.idx];
         const int par = c.ctl[0];
-        const double4* __restrict__ X = c.pos[par];
         const double4* __restrict__ xp = c.pos[par ^ 1];
-        const float4* __restrict__ rec = c.rec;
+        const float4* __restrict__ rec = c.rec[par];
         const unsigned long long ap_call = c.ap[0];
         // the cell's constants of this step, formed by the vertex phase
         const StepConst& sc = *reinterpret_cast<const StepConst*>(c.stepc);
@@ -600,7 +846,8 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a) {
             // the vertex's own state first: these loads do not depend on the one-ring sums below
             const int kb = c.vt_ptr[v], ke = c.vt_ptr[v + 1];
             const ff4 f4 = ldg_ff4(c.fau, c.nv, v);
-            const float cCh = ld_ff(c.cC, c.nv, v).hi;
+            const ff cCv = ld_ff(c.cC, c.nv, v);
+            const float cCh = cCv.hi;
             const float rho = c.rho_w ? ld_rho(c.rho_w, v) : rho_max;
             const int rank = c.bnd_rank[v];
             const float4* eo = reinterpret_cast<const float4*>(c.ea[par]);
@@ -636,13 +883,19 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a) {
                     b[5] = Q0; b[6] = Q1; b[7] = Q2; b[8] = Q3; b[9] = MMf;
                     continue;
                 }
-                boundary_force(c, s_bc, pt, X, xp, v, rank, G0, G1);   // queue full: finish in place
-                finish_vertex_core(c, a, par, v, G0, G1, true, Q0, Q1, Q2, Q3, MMf, Vv, Av, eh, el);
+                boundary_force(c, s_bc, pt, rec, xp, v, rank, G0, G1);   // queue full: finish in place
+                FusedIn nx;
+                if (fuse) nx = {ldg_ff4(xp, c.nv, v), f4, cCv, ld_ff(c.cA, c.nv, v)};
+                finish_vertex_core(c, a, par, v, G0, G1, true, Q0, Q1, Q2, Q3, MMf, Vv, Av, eh, el,
+                                   fuse ? &nx : nullptr);
                 continue;
             }
             // F = kfa fs - R with the product exact (TwoProduct) and one rounding at the end
             const float F0 = net_force(kfa, fs[0], R0), F1 = net_force(kfa, fs[1], R1);
-            finish_vertex_core(c, a, par, v, {F0, 0.0f}, {F1, 0.0f}, false, Q0, Q1, Q2, Q3, MMf, Vv, Av, eh, el);
+            FusedIn nx;
+            if (fuse) nx = {ldg_ff4(xp, c.nv, v), f4, cCv, ld_ff(c.cA, c.nv, v)};
+            finish_vertex_core(c, a, par, v, {F0, 0.0f}, {F1, 0.0f}, false, Q0, Q1, Q2, Q3, MMf, Vv, Av, eh, el,
+                               fuse ? &nx : nullptr);
         }
         __syncthreads();
         const int nq = min(s_nbnd, kBndSlots);
@@ -650,116 +903,35 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a) {
             const float* b = s_bnd + kBndRec * j;
             const int v = pt.x + __float_as_int(b[0]);
             ff F0 = {b[1], b[2]}, F1 = {b[3], b[4]};
-            boundary_force(c, s_bc, pt, X, xp, v, c.bnd_rank[v], F0, F1);
-            finish_vertex(c, a, par, v, F0, F1, b[5], b[6], b[7], b[8], b[9]);
+            boundary_force(c, s_bc, pt, rec, xp, v, c.bnd_rank[v], F0, F1);
+            finish_vertex(c, a, par, v, F0, F1, b[5], b[6], b[7], b[8], b[9], fuse);
         }
         __syncthreads();
         if (threadIdx.x == 0) {
             s_nbnd = 0;   // for the next patch: every thread passes this CTA's next element barrier first
             __threadfence();
             const unsigned int done = atomicAdd(reinterpret_cast<unsigned int*>(c.ctl + 1), 1u);
-            if ((int)done == c.np - 1) {
+            const bool last = (int)done == c.np - 1;
+            if (last) {
                 c.ctl[1] = 0;
                 c.ctl[0] = par ^ 1;
                 c.clk[0] = c.clk[0] + a.dt_real;
                 c.ap[0] = ap_call + 1ull;
                 count_step(c);
             }
+            s_last = last;
+        }
+        if (fuse) {
+            // the cell's last patch: area and step constants of the next step from every patch's
+            // predictions (the shared element slots are free until the next patch)
+            __syncthreads();
+            if (s_last) {
+                __threadfence();
+                area_shoelace(c, c.pos[par], a.va.dtd, reinterpret_cast<double*>(smf));
+            }
         }
     }
 }
-
-// ===========================================================================
-// mixed-form vertex phase: predict (triple-float positions), bond kinetics with FP32
-// rates and float-float accumulation, the FP32 element records, and the cell area and
-// area-weighted centroid from the boundary loop (shoelace over the directed
-// boundary edges).  For a planar mesh without inverted elements that equals
-// calculateAreaTot's sum of element areas.
-// ===========================================================================
-enum { VM_PREDICT = 1, VM_UPDATE_FA = 2, VM_EXPORT = 8, VM_IMPORT = 16, VM_NOAREA = 32 };
-
-// The cell area and centroid of the mixed form, from the predicted positions of
-// the boundary loop (shoelace over the directed boundary edges).  The last block
-// of the cell to finish (ticket ctl[2]) reads the positions the other blocks
-// wrote (through L2) and sums the terms in a fixed order: boundary ranks strided
-// over the threads, then lanes, then warps.  Only that block runs the FP64
-// shoelace, with all of its lanes busy.
-// The substrate's displacement under a bond's anchor (a rigid substrate mesh moved by the
-// caller), subtracted from the bond vector (UL:2053-2099).  Out of line: few cells have
-// one, and its FP64 point location would otherwise set the register budget of every block.
-__device__ __noinline__ void substrate_move(const CellDev& c, const ff4& Xv, const ff4& f, ff& u0, ff& u1, ff& u2) {
-    double wgt[3], Xd[3], fd[3];
-    pos_d(Xv, Xd);
-    vec_d(f, fd);
-    const int e = locate(c.sub, xs(Xd[0], fd[0]), xs(Xd[1], fd[1]), xs(Xd[2], fd[2]), wgt);
-    if (e >= 0) {
-        const int4 t = c.sub.tri[e];
-        const double4 a0 = ld4(c.sub.x + t.x), a1 = ld4(c.sub.x + t.y), a2 = ld4(c.sub.x + t.z);
-        const double4 b0 = ld4(c.sub.X + t.x), b1 = ld4(c.sub.X + t.y), b2 = ld4(c.sub.X + t.z);
-        u0 = ff_sub(u0, ff_from_d(wgt[0] * (a0.x - b0.x) + wgt[1] * (a1.x - b1.x) + wgt[2] * (a2.x - b2.x)));
-        u1 = ff_sub(u1, ff_from_d(wgt[0] * (a0.y - b0.y) + wgt[1] * (a1.y - b1.y) + wgt[2] * (a2.y - b2.y)));
-        u2 = ff_sub(u2, ff_from_d(wgt[0] * (a0.z - b0.z) + wgt[1] * (a1.z - b1.z) + wgt[2] * (a2.z - b2.z)));
-    }
-}
-
-__device__ __forceinline__ void finish_area_boundary(const CellDev& c, const double4* xo, double dt_real) {
-    __shared__ int s_last;
-    __shared__ double s_w[kK1Threads / 32][3];
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        __threadfence();
-        const unsigned int t = atomicAdd(reinterpret_cast<unsigned int*>(c.ctl + 2), 1u);
-        s_last = ((int)t == c.nk1 - 1);
-    }
-    __syncthreads();
-    if (!s_last) return;   // block-uniform
-    __threadfence();
-    double s0 = 0, s1 = 0, s2 = 0;
-    for (int r = threadIdx.x; r < c.nb; r += blockDim.x) {
-        double xi[3];
-        pos_d(ld_ff4(xo, c.nv, c.bnd_vert[r]), xi);
-        for (int k = c.bnd_optr[r]; k < c.bnd_optr[r + 1]; ++k) {
-            double xj[3];
-            pos_d(ld_ff4(xo, c.nv, c.bnd_out[k]), xj);
-            const double cr = xi[0] * xj[1] - xj[0] * xi[1];
-            s0 += 0.5 * cr;
-            s1 += (1.0 / 6.0) * (xi[0] + xj[0]) * cr;
-            s2 += (1.0 / 6.0) * (xi[1] + xj[1]) * cr;
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-    }
-    const int wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        s_w[wid][0] = s0; s_w[wid][1] = s1; s_w[wid][2] = s2;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double A = 0, Ax = 0, Ay = 0;
-        for (int w = 0; w < nw; ++w) {
-            A += s_w[w][0]; Ax += s_w[w][1]; Ay += s_w[w][2];
-        }
-        c.area4[0] = A;
-        c.area4[1] = Ax / A;
-        c.area4[2] = Ay / A;
-        c.area4[3] = 0.0;
-        c.ctl[2] = 0;
-        *reinterpret_cast<StepConst*>(c.stepc) = make_step_const(c, dt_real, A, Ax / A, Ay / A);
-    }
-}
-
-struct VertexArgs {
-    ff dt, hdt;
-    double dtd;
-    float dtf;
-    int flags;
-    const double* stage_in;
-    double* stage_out;
-};
 
 // Mixed-form vertex phase, one block per work item (c.vb consecutive vertices of
 // one cell): predict, bond kinetics with FP32 rates and float-float accumulation,
@@ -775,88 +947,9 @@ __global__ void __launch_bounds__(kK1Threads, MINB) k_vertex_phase_mixed(const C
     const CellDev& c = cells[it.cell];
     if (cell_done(c)) return;   // block-uniform: a serving cell that ran its steps
     const int v = it.idx * c.vb + threadIdx.x;
-    const int flags = va.flags;
     const int par = c.ctl[0];
-    double4* __restrict__ xo = c.pos[par ^ 1];
-    if (v < c.nv) {
-        const double4* __restrict__ X = c.pos[par];
-        const ff4 Xv = ldg_ff4(X, c.nv, v);
-        // every load of this vertex's state up front: none depends on the prediction's stores
-        const bool do_fa = (flags & VM_UPDATE_FA) != 0;
-        const ff4 f = do_fa ? ldg_ff4(c.fau, c.nv, v) : ff4{};
-        const ff cold = do_fa ? ld_ff(c.cC, c.nv, v) : ff{0.0f, 0.0f};
-        const ff cAv = do_fa ? ld_ff(c.cA, c.nv, v) : ff{0.0f, 0.0f};
-        const float4 eh = __ldg(reinterpret_cast<const float4*>(c.ea[par]) + v);   // (xx, yy, zz, xy) hi
-        // positions are triple-float (wcfe_ff.cuh); the step displacement cu is float-float
-        tf xn0, xn1;
-        ff xn2 = ffz(Xv);
-        if (flags & VM_IMPORT) {
-            // a coordinate the caller returned as the binary64 rounding of the predicted one keeps
-            // the predicted triple-float (so the exchange path steps exactly as the internal one);
-            // any other value is taken as given
-            const double* qq = va.stage_in + 3 * (size_t)(c.hoff + v);
-            const ff4 pr = ld_ff4(xo, c.nv, v);
-            const tf p0 = tfx(pr), p1 = tfy(pr);
-            xn0 = tf_to_d(p0) == qq[0] ? p0 : tf_from_d(qq[0]);
-            xn1 = tf_to_d(p1) == qq[1] ? p1 : tf_from_d(qq[1]);
-            xn2 = ff_from_d(qq[2]);
-            st_ff4(xo, c.nv, v, make_pos4(xn0, xn1, xn2));
-        } else if (flags & VM_PREDICT) {
-            // vh = V + (dt/2) A; x = X + dt vh
-            const ff4 V = ldg_ff4(c.vel, c.nv, v);
-            const float4 A = ld_acc(c.acc, v);
-            ff vh0 = ff_add(ffx(V), ff_mul_f(va.hdt, A.x)), vh1 = ff_add(ffy(V), ff_mul_f(va.hdt, A.y));
-            protrude_ff(c, v, Xv, vh0, vh1);
-            xn0 = tf_add_ff(tfx(Xv), ff_mul(va.dt, vh0));
-            xn1 = tf_add_ff(tfy(Xv), ff_mul(va.dt, vh1));
-            st_ff4(xo, c.nv, v, make_pos4(xn0, xn1, xn2));
-            if (flags & VM_EXPORT) {
-                st_ff4(c.vhl, c.nv, v, make_ff4(vh0, vh1, {0.0f, 0.0f}));
-                double* qq = va.stage_out + 3 * (size_t)(c.hoff + v);
-                qq[0] = tf_to_d(xn0); qq[1] = tf_to_d(xn1); qq[2] = ff_to_d(xn2);
-            }
-        } else {
-            const ff4 t = ld_ff4(xo, c.nv, v);
-            xn0 = tfx(t); xn1 = tfy(t); xn2 = ffz(t);
-        }
-        const ff cu0 = tf_sub(xn0, tfx(Xv)), cu1 = tf_sub(xn1, tfy(Xv));   // step displacement
-        if (do_fa) {
-            const ParamF& pf = c.pf;
-            ff u0 = ff_add(ffx(f), cu0), u1 = ff_add(ffy(f), cu1), u2 = ffz(f);
-            if (c.has_sub && c.sub.moving) substrate_move(c, Xv, f, u0, u1, u2);
-            // Bell kinetics (UL:2137-2171): k_off from the float-float force, the c_C update in float-float
-            const ff F = bell_ff(pf, u0, u1, u2);
-            const ff xa = ff_mul(F, {pf.iFa, pf.iFa_lo}), xb = ff_mul(F, {pf.iFb, pf.iFb_lo});
-            // the exponent is capped below FP32 overflow (e^88 ~ 1.7e38): any force that large already
-            // gives dt k_off >> 1, i.e. the same decisions as the unbounded FP64 rate
-            const float koff = pf.ka * expf(fminf(xa.hi, 88.0f)) * (1.0f + xa.lo) + pf.kb * expf(-xb.hi) * (1.0f - xb.lo);
-            const float coldf = cold.hi, kon = pf.k_on, dtf = va.dtf;
-            const ff rate = ff_sub(ff_mul_f(ff_sub({1.0f, 0.0f}, cold), kon), ff_mul_f(cold, koff));
-            ff cn = ff_add(cold, ff_mul(va.dt, rate));
-            if (cn.hi < 0.0f) cn = {0.0f, 0.0f};
-            if (cAv.hi < 0.0f) st_ff(c.cA, c.nv, v, {0.0f, 0.0f});
-            ff n0, n1, n2;
-            const bool keep_pos = coldf > 0.0f && (1.0f - dtf * koff) > 0.0f;
-            if (keep_pos && cn.hi > 0.0f) {
-                // keep / c_new = 1 + ds with ds = -dt k_on (1 - c_old) / c_new exactly
-                const float ds = -dtf * kon * (1.0f - coldf) / cn.hi;
-                n0 = ff_add(u0, ff_mul_f(u0, ds)); n1 = ff_add(u1, ff_mul_f(u1, ds)); n2 = ff_add(u2, ff_mul_f(u2, ds));
-            } else {
-                n0 = {0.0f * u0.hi, 0.0f}; n1 = {0.0f * u1.hi, 0.0f}; n2 = {0.0f * u2.hi, 0.0f};
-            }
-            st_ff(c.cC, c.nv, v, cn);
-            st_ff4(c.fau, c.nv, v, make_ff4(n0, n1, n2));
-        }
-        if (!(flags & VM_EXPORT)) {
-            float4* r = c.rec + kRec * (size_t)v;
-            r[0] = make_float4(Xv.hx, Xv.hy, Xv.lx, Xv.ly);
-            r[1] = make_float4(cu0.hi, cu1.hi, eh.x, eh.y);
-            r[2] = make_float4(eh.w, eh.z, 0.0f, 0.0f);
-        }
-        // boundary positions are read by the block that finishes the area
-        if (!(flags & VM_NOAREA) && c.bnd_rank[v] >= 0) __threadfence();
-    }
-    if (!(flags & VM_NOAREA)) finish_area_boundary(c, xo, va.dtd);
+    if (v < c.nv) vertex_mixed_body(c, v, par, va);
+    if (!(va.flags & VM_NOAREA)) finish_area_boundary(c, c.pos[par ^ 1], va.dtd);
 }
 
 void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,
@@ -961,7 +1054,7 @@ __device__ __forceinline__ void stage_issue(const MixedArgs& a, const StageLayou
             const float4* vel = reinterpret_cast<const float4*>(c.vel);
             const float4* ea = reinterpret_cast<const float4*>(c.ea[par]);
             bulk_g2s(st + L.o_loc, c.patch_loc + 4 * (size_t)pt.z, b_loc, bar + s);
-            if (b_rec) bulk_g2s(st + L.o_rec, c.rec + 3 * (size_t)v0, b_rec, bar + s);
+            if (b_rec) bulk_g2s(st + L.o_rec, c.rec[par] + 3 * (size_t)v0, b_rec, bar + s);
             bulk_g2s(st + L.o_vt, c.vt_ptr + a4, b_vt, bar + s);
             if (b_code) bulk_g2s(st + L.o_code, c.vc_code + cb, b_code, bar + s);
             if (b_v16) {
@@ -987,7 +1080,7 @@ __device__ __forceinline__ void stage_issue(const MixedArgs& a, const StageLayou
         const int nvp = h->pt.y, h0 = h->px.x, nh = h->px.y;
         float4* rec_s = reinterpret_cast<float4*>(st + L.o_rec) + kRec * (size_t)nvp;
         for (int k = lane; k < nh; k += 32) {
-            const float4* src = c.rec + kRec * (size_t)c.patch_halo[h0 + k];
+            const float4* src = c.rec[h->par] + kRec * (size_t)c.patch_halo[h0 + k];
 #pragma unroll
             for (int m = 0; m < kRec; ++m) cp_async16(rec_s + kRec * (size_t)k + m, src + m);
         }
@@ -1104,7 +1197,6 @@ __global__ void __launch_bounds__(kConsumers + 32) k_patch_mixed_staged(MixedArg
         const ParamF& pf = c.pf;
         const float rho_max = pf.rho_i_max;
         const bool has_rho = h->has_rho;
-        const double4* __restrict__ X = c.pos[par];
         const double4* __restrict__ xp = c.pos[par ^ 1];
         for (int i = threadIdx.x; i < pt.y; i += kConsumers) {
             const int v = pt.x + i;
@@ -1141,7 +1233,7 @@ __global__ void __launch_bounds__(kConsumers + 32) k_patch_mixed_staged(MixedArg
                     b[5] = Q0; b[6] = Q1; b[7] = Q2; b[8] = Q3; b[9] = MMf;
                     continue;
                 }
-                boundary_force(c, h->bc, pt, X, xp, v, rank, G0, G1);   // queue full: finish in place
+                boundary_force(c, h->bc, pt, c.rec[par], xp, v, rank, G0, G1);   // queue full: finish in place
                 finish_vertex_core(c, a, par, v, G0, G1, true, Q0, Q1, Q2, Q3, MMf,
                                    {vh.x, vh.y, vh.z, vh.w, vl.x, vl.y, vl.z, vl.w}, acc_s[i], eahi_s[i], ealo_s[i]);
                 continue;
@@ -1158,7 +1250,7 @@ __global__ void __launch_bounds__(kConsumers + 32) k_patch_mixed_staged(MixedArg
             const int i = __float_as_int(b[0]);
             const int v = pt.x + i;
             ff F0 = {b[1], b[2]}, F1 = {b[3], b[4]};
-            boundary_force(c, h->bc, pt, X, xp, v, rank_s[i], F0, F1);
+            boundary_force(c, h->bc, pt, c.rec[par], xp, v, rank_s[i], F0, F1);
             const float4 vh = vhi_s[i], vl = vlo_s[i];
             finish_vertex_core(c, a, par, v, F0, F1, true, b[5], b[6], b[7], b[8], b[9],
                                {vh.x, vh.y, vh.z, vh.w, vl.x, vl.y, vl.z, vl.w}, acc_s[i], eahi_s[i], ealo_s[i]);
@@ -1255,6 +1347,7 @@ bool launch_patch_staged(const CellDev* cells, const WorkItem* work, int nwork, 
     a.ap_thresh = ap_thresh;
     a.t_override = t_override;
     a.vh_from_buf = vh_from_buf;
+    a.fused = 0;
     const int grid = std::min(nwork, per_sm * num_sms);
     k_patch_mixed_staged<<<grid, kConsumers + 32, smem, st>>>(a, L);
     return true;
@@ -1298,9 +1391,17 @@ int mixed_occupancy(int threads, size_t smem) { return mixed_occupancy(threads, 
 
 void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt, double dt_real,
                         double ap_thresh, double t_override, int vh_from_buf, int threads, int grid, cudaStream_t st,
-                        int kind) {
+                        int kind, int fused) {
     if (nwork <= 0) return;
     MixedArgs a;
+    a.fused = fused;
+    a.va.dt = ff_from_d(dt);
+    a.va.hdt = ff_from_d(dt / 2.0);
+    a.va.dtd = dt;
+    a.va.dtf = (float)dt;
+    a.va.flags = VM_PREDICT | VM_UPDATE_FA;
+    a.va.stage_in = nullptr;
+    a.va.stage_out = nullptr;
     a.cells = cells;
     a.work = work;
     a.nwork = nwork;
@@ -1323,7 +1424,7 @@ void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, i
 }
 void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt, double dt_real,
                         double ap_thresh, double t_override, int vh_from_buf, int threads, int grid, cudaStream_t st) {
-    launch_patch_mixed(cells, work, nwork, emax, dt, dt_real, ap_thresh, t_override, vh_from_buf, threads, grid, st, 1);
+    launch_patch_mixed(cells, work, nwork, emax, dt, dt_real, ap_thresh, t_override, vh_from_buf, threads, grid, st, 1, 0);
 }
 
 }  // namespace wcfe
