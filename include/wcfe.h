@@ -244,9 +244,10 @@ int wcfe_engine_get_kernels(const wcfe_engine* e, int32_t* patch_kind, int32_t* 
  * bit-identical to enable 0.  On GB300 it is slower (0.50 against 0.35 ms per step on
  * the 256-cell workload): the vertex work then runs at the patch kernel's 20 resident
  * warps per SM instead of the vertex kernel's 40, and both phases are latency-bound, not
- * bandwidth-bound.  It applies to the plain patch kernels (kinds 1-4) of engines without
- * a coupled substrate; wcfe_engine_get_fused returns 1 where a run of steps is fused, else
- * 0 (-1: no engine).  No counterpart in the reference (a batching schedule). */
+ * bandwidth-bound.  It applies where a plain patch kernel (kinds 1-4) is selected, in
+ * engines without a coupled substrate (the fused form is one kernel, for 5 CTAs of 128
+ * threads per SM); wcfe_engine_get_fused returns 1 where a run of steps is fused, else 0
+ * (-1: no engine).  No counterpart in the reference (a batching schedule). */
 int wcfe_engine_set_fused(wcfe_engine* e, int32_t enable);
 int wcfe_engine_get_fused(const wcfe_engine* e);
 

@@ -735,8 +735,9 @@ void patch_step(wcfe_engine* e, const WorkItem* k2, int n2, double dt, double dt
             return;
         const int kind = e->patch_kernel == 0 ? 1 : e->patch_kernel;
         const size_t smem = mixed_smem_bytes(e->patch_emax);
+        const int okind = fused ? 5 : kind;   // the fused form is its own instantiation
         launch_patch_mixed(e->d_table, k2, n2, e->patch_emax, dt, dt_real, apt, t_override, vh_from_buf,
-                           e->patch_threads, grid_for(e, n2, mixed_occupancy(e->patch_threads, smem, kind)), st, kind,
+                           e->patch_threads, grid_for(e, n2, mixed_occupancy(e->patch_threads, smem, okind)), st, kind,
                            fused);
         return;
     }

@@ -62,9 +62,8 @@ struct MixedArgs {
     double dt_real, ap_thresh, t_override;
     ff hdt, cdt, dtr;        // dt/2, dt_real - dt/2, dt_real as float-float
     int vh_from_buf, half;   // half = dt_real > dt/2
-    // fused != 0: after its owned vertices' update, each patch also runs the next step's vertex
-    // phase on them (arguments va), and the cell's last patch forms the next step's area
-    int fused;
+    // the fused form (k_patch_phase_mixed<5, true>): after its owned vertices' update, each
+    // patch also runs the next step's vertex phase on them with these arguments
     VertexArgs va;
 };
 
@@ -785,8 +784,11 @@ constexpr int kBndRec = 10;   // floats per queued boundary vertex: index, F0 an
 // MINB: the least CTAs of 128 threads per SM the register allocation must allow (5: 96
 // registers; 6, 7, 8: 80, 72, 64 registers, with shared memory then limiting emax); the
 // autotuner picks among them.
-template <int MINB>
-__global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a) {
+// FUSED: the fused form (MixedArgs::fused), a separate instantiation so that its code does
+// not weigh on the register allocation of the plain one.
+template <int MINB, bool FUSED>
+__global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a, const CellDev* __restrict__ cells,
+                                                                 const WorkItem* __restrict__ work) {
     extern __shared__ float smf[];
     const int emax = a.emax;
     // structure of arrays: field k of slot j at smf[k * emax + j]
@@ -795,12 +797,12 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a) {
     if (threadIdx.x == 0) s_nbnd = 0;
     __syncthreads();
     for (int w = blockIdx.x; w < a.nwork; w += gridDim.x) {
-        const WorkItem it = a.work[w];
-        const CellDev& c = a.cells[it.cell];
+        const WorkItem it = work[w];
+        const CellDev& c = cells[it.cell];   // the table is read-only here: its fields stay in registers
         if (cell_done(c)) continue;   // block-uniform: a serving cell that ran its steps
         // fused: predict the cell's next step here unless this step is the last of its budget
         // (ctl[3] is counted down only after every patch of the cell took its ticket)
-        const bool fuse = a.fused && c.ctl[3] != 1;
+        const bool fuse = FUSED && c.ctl[3] != 1;
         const int4 pt = c.patch[it.idx];
         const int par = c.ctl[0];
         const double4* __restrict__ xp = c.pos[par ^ 1];
@@ -1347,7 +1349,6 @@ bool launch_patch_staged(const CellDev* cells, const WorkItem* work, int nwork, 
     a.ap_thresh = ap_thresh;
     a.t_override = t_override;
     a.vh_from_buf = vh_from_buf;
-    a.fused = 0;
     const int grid = std::min(nwork, per_sm * num_sms);
     k_patch_mixed_staged<<<grid, kConsumers + 32, smem, st>>>(a, L);
     return true;
@@ -1356,18 +1357,20 @@ bool launch_patch_staged(const CellDev* cells, const WorkItem* work, int nwork, 
 size_t mixed_smem_bytes(int emax) { return sizeof(float) * (size_t)emax * kSlot32; }
 
 namespace {
+// kinds 1-4: the plain kernel for 5-8 CTAs per SM; 5: the fused form (5 CTAs per SM)
 const void* mixed_kernel(int kind) {
     switch (kind) {
-        case 2: return (const void*)k_patch_phase_mixed<6>;
-        case 3: return (const void*)k_patch_phase_mixed<7>;
-        case 4: return (const void*)k_patch_phase_mixed<8>;
-        default: return (const void*)k_patch_phase_mixed<5>;
+        case 2: return (const void*)k_patch_phase_mixed<6, false>;
+        case 3: return (const void*)k_patch_phase_mixed<7, false>;
+        case 4: return (const void*)k_patch_phase_mixed<8, false>;
+        case 5: return (const void*)k_patch_phase_mixed<5, true>;
+        default: return (const void*)k_patch_phase_mixed<5, false>;
     }
 }
 }  // namespace
 
 cudaError_t configure_mixed(size_t max_smem) {
-    for (int kind = 1; kind <= 4; ++kind) {
+    for (int kind = 1; kind <= 5; ++kind) {
         cudaFuncAttributes at;
         cudaError_t e = cudaFuncGetAttributes(&at, mixed_kernel(kind));
         if (e != cudaSuccess) return e;
@@ -1378,7 +1381,7 @@ cudaError_t configure_mixed(size_t max_smem) {
     return configure_staged(max_smem);
 }
 
-// resident CTAs per SM of the plain kernel variant `kind` (1-4, see k_patch_phase_mixed)
+// resident CTAs per SM of the plain kernel variant `kind` (1-4, see k_patch_phase_mixed; 5 fused)
 int mixed_occupancy(int threads, size_t smem, int kind) {
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mixed_kernel(kind), threads, smem) != cudaSuccess) {
@@ -1394,7 +1397,6 @@ void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, i
                         int kind, int fused) {
     if (nwork <= 0) return;
     MixedArgs a;
-    a.fused = fused;
     a.va.dt = ff_from_d(dt);
     a.va.hdt = ff_from_d(dt / 2.0);
     a.va.dtd = dt;
@@ -1415,11 +1417,15 @@ void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, i
     a.t_override = t_override;
     a.vh_from_buf = vh_from_buf;
     const size_t smem = mixed_smem_bytes(emax);
+    if (fused) {   // one fused instantiation (5 CTAs per SM) serves every plain kind
+        k_patch_phase_mixed<5, true><<<grid, threads, smem, st>>>(a, cells, work);
+        return;
+    }
     switch (kind) {
-        case 2: k_patch_phase_mixed<6><<<grid, threads, smem, st>>>(a); break;
-        case 3: k_patch_phase_mixed<7><<<grid, threads, smem, st>>>(a); break;
-        case 4: k_patch_phase_mixed<8><<<grid, threads, smem, st>>>(a); break;
-        default: k_patch_phase_mixed<5><<<grid, threads, smem, st>>>(a); break;
+        case 2: k_patch_phase_mixed<6, false><<<grid, threads, smem, st>>>(a, cells, work); break;
+        case 3: k_patch_phase_mixed<7, false><<<grid, threads, smem, st>>>(a, cells, work); break;
+        case 4: k_patch_phase_mixed<8, false><<<grid, threads, smem, st>>>(a, cells, work); break;
+        default: k_patch_phase_mixed<5, false><<<grid, threads, smem, st>>>(a, cells, work); break;
     }
 }
 void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt, double dt_real,
