@@ -411,7 +411,7 @@ int wcfe_engine_step_implicit(wcfe_engine* e, int32_t nsteps, double dt, double 
                               wcfe_newton_stats* stats);
 
 /* The implicit step's dense LU.  block: the outer block width, a multiple of 64 from 64
- * to 512 (default 512): the trailing matrix takes one update per outer block with
+ * to 1024 (default 1024): the trailing matrix takes one update per outer block with
  * K = block, which reads and writes it once per block.  kind 0 (default):
  * trailing updates on the tcgen05 tensor cores (TMA-fed, TF32, accumulators in TMEM);
  * kind 1: the mma.sync TF32 updates (block must be 64).  FP64 engines; results agree

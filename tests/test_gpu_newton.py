@@ -155,7 +155,7 @@ def test_implicit_refuses_mixed_engine():
 
 
 # (outer block, kind): tcgen05 two-level, tcgen05, mma.sync, then wider two-level blocks
-LU_VARIANTS = [(256, 0), (64, 0), (64, 1), (384, 0), (512, 0)]
+LU_VARIANTS = [(256, 0), (64, 0), (64, 1), (384, 0), (512, 0), (1024, 0)]
 
 
 @pytest.mark.parametrize("block,kind", LU_VARIANTS)
@@ -210,16 +210,16 @@ def test_implicit_step_lu_variants_agree():
 
 
 def test_set_lu_rejects_bad_blocks():
-    """Outer blocks are multiples of 64 up to 512; the mma.sync updates take 64 only."""
+    """Outer blocks are multiples of 64 up to 1024; the mma.sync updates take 64 only."""
     e = capi.Engine(capi.PREC_FP64)
-    for block, kind in [(0, 0), (32, 0), (96, 0), (576, 0), (256, 1), (64, 2), (64, -1)]:
+    for block, kind in [(0, 0), (32, 0), (96, 0), (1088, 0), (256, 1), (64, 2), (64, -1)]:
         with pytest.raises(capi.WcfeError):
             e.set_lu(block, kind)
     e.set_lu(448, 0)
     e.close()
     A = np.eye(4, dtype=np.float32)
     with pytest.raises(capi.WcfeError):
-        capi.debug_lu_solve(A, np.ones(4), 1024, 0)
+        capi.debug_lu_solve(A, np.ones(4), 1088, 0)
 
 
 def test_implicit_step_factor_reuse_agrees():

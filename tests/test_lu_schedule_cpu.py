@@ -42,7 +42,7 @@ def replay(A, ops):
 
 
 @pytest.mark.parametrize("m", [2, 64, 130, 520, 1000, 2050])
-@pytest.mark.parametrize("block", [64, 128, 192, 256, 384, 448, 512])
+@pytest.mark.parametrize("block", [64, 128, 192, 256, 384, 448, 512, 768, 1024])
 def test_schedule_factors(m, block):
     rng = np.random.default_rng(m + block)
     A = rng.uniform(-1.0, 1.0, (m, m)) + m * np.eye(m)
@@ -80,6 +80,6 @@ def test_strips_run_at_growing_k():
 
 
 def test_schedule_arguments():
-    for m, block in [(0, 512), (100, 96), (100, 576), (100, 0)]:
+    for m, block in [(0, 512), (100, 96), (100, 1088), (100, 0)]:
         with pytest.raises(capi.WcfeError):
             capi.debug_lu_schedule(m, block)

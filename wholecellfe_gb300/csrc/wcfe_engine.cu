@@ -53,7 +53,8 @@ void launch_newton_residual(const CellDev* cells, const NewtonCell* nc, const in
 void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int* cell_slot, const WorkItem* work,
                            int nwork, int emax, double dt, int dense, cudaStream_t st);
 const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots, int max_m, const LuMaps* maps,
-                             int* d_prefix, int nb, int kind, cudaStream_t st);
+                             int* d_prefix, int nb, int kind, cudaStream_t st, cudaStream_t side = nullptr,
+                             const cudaEvent_t* ev = nullptr);
 void lu_tc_attributes(int* regs, int* max_threads);
 void launch_newton_clear(NewtonCell* nc, int nslots, int max_n, cudaStream_t st);
 void launch_norms_clear(double* norms, int nslots, int first, int count, cudaStream_t st);
@@ -202,7 +203,7 @@ struct wcfe_engine {
     int vertex_kind = 0;          // mixed form: vertex-phase kernel for 5 (0) or 4 (1) blocks per SM
     int patch_kernel = 1;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
     bool fused = false;           // mixed form: runs of steps fold each next vertex phase into the patch phase
-    int lu_nb = 512, lu_kind = 0; // implicit step's LU: outer block width, 0 tcgen05 / 1 mma.sync updates
+    int lu_nb = 1024, lu_kind = 0; // implicit step's LU: outer block width, 0 tcgen05 / 1 mma.sync updates
     int lu_reuse = 1;             // 1: factor once per implicit step, 0: every Newton iteration
     int cap_ne = 0, cap_nvp = 0, cap_nh = 0, cap_nc = 0;   // largest patch over the cells (staging plan)
     int n2_sub = 0;               // patch work items of substrate cells, at the end of k2 (second launch)
@@ -232,10 +233,10 @@ int fail(const std::string& msg, int code) {
     return code;
 }
 
-// kind 0 (tcgen05 updates): outer blocks of 64 to 512 columns in steps of 64; kind 1: 64
+// kind 0 (tcgen05 updates): outer blocks of 64 to 1024 columns in steps of 64; kind 1: 64
 bool lu_block_ok(int block, int kind) {
     if (kind == 1) return block == 64;
-    return kind == 0 && block >= 64 && block <= 512 && block % 64 == 0;
+    return kind == 0 && block >= 64 && block <= 1024 && block % 64 == 0;
 }
 
 Cell* find(wcfe_engine* e, int32_t id) {
@@ -1960,6 +1961,8 @@ struct NewtonPlan {
     LuMaps* d_maps = nullptr;        // [nslots] TMA descriptors of J and Ut
     int* d_prefix = nullptr;         // per-launch tile prefix sums of the LU's trailing updates
     cudaEvent_t sev[2] = {nullptr, nullptr};   // around each triangular solve (statistics)
+    cudaStream_t side = nullptr;                // the LU's second stream (row-panel transposes)
+    cudaEvent_t lev[2] = {nullptr, nullptr};    // ordering between the two LU streams
     double *res = nullptr, *rea = nullptr, *mm = nullptr, *f4 = nullptr, *fext = nullptr;
     int max_n = 0;
 };
@@ -2056,12 +2059,20 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
     CK(cudaMemcpyAsync(P.d_cells, P.cells.data(), sizeof(NewtonCell) * ns, cudaMemcpyHostToDevice, e->stream));
     CK(cudaStreamSynchronize(e->stream));
     for (auto& ev : P.sev) CK(cudaEventCreate(&ev));
+    for (auto& ev : P.lev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CK(cudaStreamCreateWithFlags(&P.side, cudaStreamNonBlocking));
     return WCFE_OK;
 }
 
 void newton_free(wcfe_engine* e, NewtonPlan& P) {
     for (auto& ev : P.sev)
         if (ev) cudaEventDestroy(ev);
+    for (auto& ev : P.lev)
+        if (ev) cudaEventDestroy(ev);
+    if (P.side) {
+        cudaStreamSynchronize(P.side);
+        cudaStreamDestroy(P.side);
+    }
     if (P.block) {
         cudaStreamSynchronize(e->stream);
         dev_free(e, P.block, P.bytes);
@@ -2163,7 +2174,7 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
         if (factor) {
         if (st) CK(cudaEventRecord(e->ev[0], e->stream));
         if (const char* k = launch_newton_lu(P.d_cells, P.cells.data(), ns, 2 * P.max_n, P.d_maps, P.d_prefix,
-                                             e->lu_nb, e->lu_kind, e->stream))
+                                             e->lu_nb, e->lu_kind, e->stream, P.side, P.lev))
             return fail(std::string("launch failed: ") + k + lu_attr_note(), WCFE_ERR_CUDA);
         if (st) {
             CK(cudaEventRecord(e->ev[1], e->stream));

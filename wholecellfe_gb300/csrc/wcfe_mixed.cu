@@ -784,13 +784,15 @@ constexpr int kBndRec = 10;   // floats per queued boundary vertex: index, F0 an
 // MINB: the least CTAs of 128 threads per SM the register allocation must allow (5: 96
 // registers; 6, 7, 8: 80, 72, 64 registers, with shared memory then limiting emax); the
 // autotuner picks among them.
-// FUSED: the fused form (MixedArgs::fused), a separate instantiation so that its code does
-// not weigh on the register allocation of the plain one.
-template <int MINB, bool FUSED>
+// FUSED: the fused form (MixedArgs::va), a separate instantiation so that its code does
+// not weigh on the register allocation of the plain one.  EMAX > 0: the element-slot
+// stride of the shared arrays as a constant (a.emax == EMAX), so that the field offsets
+// are immediates; 0: a.emax at run time.
+template <int MINB, bool FUSED, int EMAX = 0>
 __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a, const CellDev* __restrict__ cells,
                                                                  const WorkItem* __restrict__ work) {
     extern __shared__ float smf[];
-    const int emax = a.emax;
+    const int emax = EMAX > 0 ? EMAX : a.emax;
     // structure of arrays: field k of slot j at smf[k * emax + j]
     __shared__ int s_nbnd, s_last;
     __shared__ float s_bnd[kBndRec * kBndSlots];
@@ -1370,6 +1372,15 @@ const void* mixed_kernel(int kind) {
 }  // namespace
 
 cudaError_t configure_mixed(size_t max_smem) {
+    {   // the constant-stride instantiation of kind 1 (emax 512)
+        const void* f = (const void*)k_patch_phase_mixed<5, false, 512>;
+        cudaFuncAttributes at;
+        cudaError_t e = cudaFuncGetAttributes(&at, f);
+        if (e != cudaSuccess) return e;
+        e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(max_smem > at.sharedSizeBytes ? max_smem - at.sharedSizeBytes : 0));
+        if (e != cudaSuccess) return e;
+    }
     for (int kind = 1; kind <= 5; ++kind) {
         cudaFuncAttributes at;
         cudaError_t e = cudaFuncGetAttributes(&at, mixed_kernel(kind));
@@ -1425,7 +1436,10 @@ void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, i
         case 2: k_patch_phase_mixed<6, false><<<grid, threads, smem, st>>>(a, cells, work); break;
         case 3: k_patch_phase_mixed<7, false><<<grid, threads, smem, st>>>(a, cells, work); break;
         case 4: k_patch_phase_mixed<8, false><<<grid, threads, smem, st>>>(a, cells, work); break;
-        default: k_patch_phase_mixed<5, false><<<grid, threads, smem, st>>>(a, cells, work); break;
+        default:
+            if (emax == 512) k_patch_phase_mixed<5, false, 512><<<grid, threads, smem, st>>>(a, cells, work);
+            else k_patch_phase_mixed<5, false><<<grid, threads, smem, st>>>(a, cells, work);
+            break;
     }
 }
 void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt, double dt_real,

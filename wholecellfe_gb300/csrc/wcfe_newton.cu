@@ -899,7 +899,7 @@ void launch_newton_tangent(const CellDev* cells, const NewtonCell* nc, const int
 }
 // The blocked LU of every active cell, in lockstep over the largest matrix.  kind 1: the
 // 64-wide right-looking algorithm with mma.sync updates (nb must be 64).  kind 0:
-// outer blocks of nb columns (a multiple of 64 up to 512), each factored recursively by
+// outer blocks of nb columns (a multiple of 64 up to 1024), each factored recursively by
 // halves: 64-wide leaves factor the diagonal block and the two panels, and each split
 // updates its right half's column strip and row strip with K = the left half's width;
 // the trailing matrix then takes one update with K = nb.  All updates and panels run on
@@ -952,8 +952,15 @@ std::vector<LuOp> lu_schedule(int max_m, int nb) {
     return ops;
 }
 
+// side, ev[2] (optional): a second stream and two events of the caller.  The transpose of a
+// leaf's row panel then runs on the side stream beside the leaf's diagonal factor (which
+// reads and writes only the diagonal block and its inverses): the factor is latency-bound
+// with one CTA per cell, the transpose bandwidth-bound, and both only follow the update
+// before them.  The next leaf's transpose follows this leaf's panels in stream order (the
+// side stream waits for an event recorded after them), so At is never overwritten early.
 const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots, int max_m, const LuMaps* maps,
-                             int* d_prefix, int nb, int kind, cudaStream_t st) {
+                             int* d_prefix, int nb, int kind, cudaStream_t st, cudaStream_t side,
+                             const cudaEvent_t* ev) {
     const char* failed = nullptr;
     auto checked = [&](const char* name) {
         if (!failed && cudaGetLastError() != cudaSuccess) failed = name;
@@ -998,15 +1005,35 @@ const char* launch_newton_lu(NewtonCell* nc, const NewtonCell* h_nc, int nslots,
     }
     if (pref.size() > lu_prefix_capacity(nslots, max_m)) return "tile lists (capacity)";
     if (!pref.empty()) cudaMemcpyAsync(d_prefix, pref.data(), sizeof(int) * pref.size(), cudaMemcpyHostToDevice, st);
-    for (const Op& o : ops) {
+    const bool overlap = side && ev;
+    auto transpose = [&](int k0, cudaStream_t s) {
+        const int rest = max_m - k0 - kNb;
+        k_lu_transpose_a12<<<dim3((unsigned)((rest + kNb - 1) / kNb), (unsigned)nslots), 256, 0, s>>>(nc, nslots, k0);
+        checked("k_lu_transpose_a12");
+    };
+    for (size_t i = 0; i < ops.size(); ++i) {
+        const Op& o = ops[i];
         if (o.type == 0) {
+            // a leaf with panels: its transpose on the side stream beside the diagonal factor
+            const bool pair = overlap && i + 1 < ops.size() && ops[i + 1].type == 1 && ops[i + 1].k0 == o.k0;
+            if (pair) {
+                cudaEventRecord(ev[0], st);
+                cudaStreamWaitEvent(side, ev[0], 0);
+                transpose(o.k0, side);
+                cudaEventRecord(ev[1], side);
+            }
             k_lu_diag<<<nslots, 256, 0, st>>>(nc, nslots, o.k0);
             checked("k_lu_diag");
+            if (pair) {
+                cudaStreamWaitEvent(st, ev[1], 0);
+                if (!launch_lu_panels_tc(nc, maps, d_prefix + ops[i + 1].pref, nslots, ops[i + 1].total, ops[i + 1].a,
+                                         st) &&
+                    !failed)
+                    failed = "k_lu_panels_tc";
+                ++i;
+            }
         } else if (o.type == 1) {
-            const int rest = max_m - o.k0 - kNb;
-            k_lu_transpose_a12<<<dim3((unsigned)((rest + kNb - 1) / kNb), (unsigned)nslots), 256, 0, st>>>(nc, nslots,
-                                                                                                          o.k0);
-            checked("k_lu_transpose_a12");
+            transpose(o.k0, st);
             if (!launch_lu_panels_tc(nc, maps, d_prefix + o.pref, nslots, o.total, o.a, st) && !failed)
                 failed = "k_lu_panels_tc";
         } else {
