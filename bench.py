@@ -351,6 +351,25 @@ def run_ours(args):
     ntot = eng.total_vertices()
     host = torch.empty((ntot, 3), dtype=torch.float64, pin_memory=True)
     xbuf = host.numpy()
+    # the exchange groups (streams whose predict and copies overlap the others' updates):
+    # fewer, larger groups keep the kernels' waves full, more hide more of the copies;
+    # the count is chosen by timing a few exchange steps of each (public API:
+    # wcfe_engine_set_exchange_groups), then the timed loop runs with it
+    group_ms = {}
+    for groups in (1, 2, 4, 8):
+        eng.set_exchange_groups(groups)
+        for _ in range(2):
+            eng.predict_all(DT, xbuf)
+            eng.update_all(DT, DT, xbuf)
+        eng.sync()
+        t0 = time.perf_counter()
+        for _ in range(4):
+            eng.predict_all(DT, xbuf)
+            eng.update_all(DT, DT, xbuf)
+        eng.sync()
+        group_ms[groups] = (time.perf_counter() - t0) / 4 * 1e3
+    best_groups = min(group_ms, key=group_ms.get)
+    eng.set_exchange_groups(best_groups)
     for _ in range(2):
         eng.predict_all(DT, xbuf)
         eng.update_all(DT, DT, xbuf)
@@ -368,6 +387,8 @@ def run_ours(args):
     e2e = {"value": len(specs) * args.steps / e2e_s, "unit": "cell-steps/s",
            "h2d_bytes_per_step": int(ntot * 24), "d2h_bytes_per_step": int(ntot * 24),
            "api": "wcfe_engine_predict + wcfe_engine_update (include/wcfe.h), pinned host buffers",
+           "exchange_groups": best_groups,
+           "ms_per_step_by_groups": {str(k): round(v, 4) for k, v in group_ms.items()},
            "gpu_launches": int(e2e_launches)}
     log(f"[bench] e2e: {e2e['value']:.3e} cell-steps/s")
     # the timed regions last a few ms, shorter than nvidia-smi's 50 ms period: the same steps
@@ -682,7 +703,7 @@ def run_config2(steps: int = 500, seed: int = 2):
     err = float(np.max(np.abs(out["mixed"][0] - out["fp64"][0])) / np.max(np.abs(u)))
     return {"vertices": len(x0), "triangles": len(tri), "integrins": 8000, "steps": steps,
             "fp64_ms_per_step": round(out["fp64"][1], 4), "mixed_ms_per_step": round(out["mixed"][1], 4),
-            "mixed_vs_fp64_rel_displacement_error": err,
+            "mixed_vs_fp64_rel_displacement_error": err, "within_1e-6": bool(err <= 1e-6),
             "status": [out["fp64"][2], out["mixed"][2]]}
 
 
