@@ -177,6 +177,7 @@ struct NewtonCell {
                          //      upper factors (identity-padded), row-major
     float* zt;           // [2n] FP32 solve workspace (the forward solve's result)
     float* At;           // [2n][64] the current row panel A12, transposed (tensor-core operand)
+    int* flags;          // [ceil(2n/64)] the triangular sweeps' published blocks (the sweep's epoch)
 };
 
 // TMA descriptors of one cell's dense LU (fp32, 128-byte swizzled boxes)

@@ -68,7 +68,7 @@ std::string lu_attr_note() {
 size_t lu_prefix_capacity(int nslots, int max_m);
 std::vector<LuOp> lu_schedule(int max_m, int nb);
 int encode_lu_maps(const NewtonCell* h, int nslots, LuMaps* out);
-void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, cudaStream_t st);
+void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, int* sweep, int* epoch, cudaStream_t st);
 void launch_newton_refine(const CellDev* cells, NewtonCell* nc, const int* cell_slot, const WorkItem* work, int nwork,
                           int add_z, cudaStream_t st);
 void launch_newton_accumulate(NewtonCell* nc, int nslots, int max_n, cudaStream_t st);
@@ -1960,6 +1960,8 @@ struct NewtonPlan {
     double* norms = nullptr;         // [nslots][8]
     LuMaps* d_maps = nullptr;        // [nslots] TMA descriptors of J and Ut
     int* d_prefix = nullptr;         // per-launch tile prefix sums of the LU's trailing updates
+    int* d_sweep = nullptr;          // the triangular sweeps' block counter and abort word
+    int sweep_epoch = 0;             // the last epoch the cells' sweep flags were given
     cudaEvent_t sev[2] = {nullptr, nullptr};   // around each triangular solve (statistics)
     cudaStream_t side = nullptr;                // the LU's second stream (row-panel transposes)
     cudaEvent_t lev[2] = {nullptr, nullptr};    // ordering between the two LU streams
@@ -1981,7 +1983,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
     const size_t o_norm = put(sizeof(double) * 8 * ns), o_nc = put(sizeof(NewtonCell) * ns);
     const size_t o_id = put(sizeof(int) * ns), o_tk = put(sizeof(unsigned int) * ns);
     const size_t o_maps = put(sizeof(LuMaps) * ns);
-    struct Off { size_t J, Ut, Dinv, At, Ke, diag, G, dx, d, r, z, zt; int n, ld; };
+    struct Off { size_t J, Ut, Dinv, At, Ke, diag, G, dx, d, r, z, zt, flags; int n, ld; };
     std::vector<Off> off(ns);
     P.max_n = 0;
     for (int sl = 0; sl < ns; ++sl) {
@@ -2002,9 +2004,11 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         f.d = put(sizeof(double) * m);
         f.r = put(sizeof(double) * m);
         f.z = put(sizeof(float) * m);
+        f.flags = put(sizeof(int) * (size_t)((m + 63) / 64));
         P.max_n = std::max(P.max_n, n);
     }
     const size_t o_pref = put(sizeof(int) * lu_prefix_capacity(ns, 2 * P.max_n));
+    const size_t o_sweep = put(sizeof(int) * 2);
     int r = dev_alloc(e, &P.block, o);
     if (r) return r;
     P.bytes = o;
@@ -2021,6 +2025,8 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
     P.d_tickets = (unsigned int*)(b + o_tk);
     P.d_maps = (LuMaps*)(b + o_maps);
     P.d_prefix = (int*)(b + o_pref);
+    P.d_sweep = (int*)(b + o_sweep);
+    P.sweep_epoch = 0;   // the block is zeroed: every flag is below the first epoch
     P.cells.resize(ns);
     std::vector<int> ident(ns);
     for (int sl = 0; sl < ns; ++sl) {
@@ -2042,6 +2048,7 @@ int newton_plan(wcfe_engine* e, NewtonPlan& P) {
         N.d = (double*)(b + f.d);
         N.r = (double*)(b + f.r);
         N.z = (float*)(b + f.z);
+        N.flags = (int*)(b + f.flags);
         N.Fext = P.fext + 3 * h;
         N.Res = P.res + 3 * h;
         N.MM = P.mm + h;
@@ -2189,7 +2196,7 @@ int newton_step(wcfe_engine* e, NewtonPlan& P, double dt, double rtol, int max_n
         double final_ratio = 0.0;
         for (; q < 16; ++q) {
             if (st) CK(cudaEventRecord(P.sev[0], e->stream));
-            launch_newton_solve(P.d_cells, ns, P.max_n, e->stream);
+            launch_newton_solve(P.d_cells, ns, P.max_n, P.d_sweep, &P.sweep_epoch, e->stream);
             if (st) CK(cudaEventRecord(P.sev[1], e->stream));
             launch_norms_clear(P.norms, ns, 2, 1, e->stream);   // |r| only (G's norm is kept on the host)
             launch_newton_refine(e->d_table, P.d_cells, P.d_ident, e->d_k2, n2, 1, e->stream);
@@ -2335,7 +2342,8 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     const size_t ndinv = 2 * 64 * 64 * (size_t)((m + 63) / 64);
     const size_t bytes = sizeof(float) * (size_t)m * ld + sizeof(float) * (size_t)m * block + sizeof(double) * m +
                          2 * sizeof(float) * m + sizeof(float) * ndinv + sizeof(float) * 64 * (size_t)m +
-                         sizeof(double) * 8 + sizeof(NewtonCell) + sizeof(LuMaps) + sizeof(int) * npref + 11 * 256;
+                         sizeof(double) * 8 + sizeof(NewtonCell) + sizeof(LuMaps) + sizeof(int) * npref +
+                         sizeof(int) * ((size_t)(m + 63) / 64 + 2) + 13 * 256;
     char* blk = nullptr;
     CK(cudaMalloc(&blk, bytes));
     size_t o = 0;
@@ -2350,6 +2358,9 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     N.Dinv = (float*)take(sizeof(float) * ndinv);
     N.At = (float*)take(sizeof(float) * 64 * (size_t)m);
     N.norms = (double*)take(sizeof(double) * 8);
+    N.flags = (int*)take(sizeof(int) * (size_t)((m + 63) / 64));
+    int* d_sweep = (int*)take(sizeof(int) * 2);
+    int epoch = 0;
     N.n = m / 2;
     N.ld = ld;
     N.active = 1;
@@ -2367,7 +2378,7 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     const char* failed = nullptr;
     if (ce == cudaSuccess) {
         failed = launch_newton_lu(d_nc, &N, 1, m, d_maps, d_pref, block, kind, 0);
-        launch_newton_solve(d_nc, 1, m / 2, 0);
+        launch_newton_solve(d_nc, 1, m / 2, d_sweep, &epoch, 0);
         if (!failed && cudaGetLastError() != cudaSuccess) failed = "triangular solves";
         ce = cudaDeviceSynchronize();
     }
@@ -2381,6 +2392,7 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     cudaFree(blk);
     if (ce != cudaSuccess) return fail(std::string("CUDA: ") + cudaGetErrorString(ce), WCFE_ERR_CUDA);
     if (flag == 2.0) return fail("tensor-core update timed out", WCFE_ERR_CUDA);
+    if (flag == 3.0) return fail("triangular sweep timed out", WCFE_ERR_CUDA);
     if (flag != 0.0) return fail("zero or non-finite pivot", WCFE_ERR_STATE);
     return WCFE_OK;
 }

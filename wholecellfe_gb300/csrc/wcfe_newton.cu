@@ -625,10 +625,7 @@ __global__ void __launch_bounds__(256) k_lu_update(NewtonCell* nc, int nslots, i
 }
 
 // ===========================================================================
-// Triangular solves with the LU factors, z = U^-1 L^-1 r (FP32), blocked by 64 rows:
-// per block one CTA per cell solves the diagonal block, then a grid of CTAs
-// subtracts the block's contribution from the remaining rows (one warp per row,
-// the row's 64 entries read coalesced).
+// Triangular solves with the LU factors, z = U^-1 L^-1 r (FP32), blocked by 64 rows.
 // ===========================================================================
 __global__ void k_trsv_init(NewtonCell* nc, int nslots) {
     NewtonCell& N = nc[blockIdx.y];
@@ -636,67 +633,128 @@ __global__ void k_trsv_init(NewtonCell* nc, int nslots) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 2 * N.n; i += gridDim.x * blockDim.x) N.z[i] = (float)N.r[i];
 }
 
-// One block step of the triangular solves with the diagonal blocks' explicit inverses, as
-// two launches.  Forward (L): x_b = Linv_b z_b into zt (k_trsv_block, one CTA per cell),
-// then z_i -= L[i, b] x_b for the rows below (k_trsv_rows).  Backward (U): x_b = Uinv_b
-// zt_b into z, then zt_i -= U[i, b] x_b for the rows above.  The row kernel reads x_b
-// from where the block kernel stored it; the rows it updates never include the block's.
-constexpr int kTrsvRows = 128;
-__global__ void __launch_bounds__(256) k_trsv_block(NewtonCell* nc, int nslots, int b0, int upper) {
-    NewtonCell& N = nc[blockIdx.x];
-    const int m = 2 * N.n;
-    if (blockIdx.x >= nslots || !N.active || b0 >= m) return;
-    const int kb = min(kNb, m - b0);
-    const float* in = upper ? N.zt : N.z;
-    float* out = upper ? N.z : N.zt;
+// The triangular solves in one launch per direction (a sweep): persistent CTAs take the
+// 64-row blocks of every cell from a shared counter, in an order in which each cell's
+// blocks come in dependency order (forward: first to last; backward: last to first), so a
+// block only ever waits for blocks that running CTAs took before it.  For its block a CTA
+// subtracts the contributions of the solved blocks as their solutions are published (a
+// warp per eight rows, each row's 64 entries read coalesced: the factor is read once),
+// solves the diagonal block with its explicit inverse and publishes the solution with the
+// sweep's epoch in the cell's flag of that block.  Row r's right-hand side takes the solved
+// blocks' contributions one block at a time in solve order, each a 64-entry dot product
+// reduced across the warp.  Every wait is bounded: on a timeout the CTA flags the cell
+// (norms[3] = 3) and raises the sweep's abort word, which ends every other wait (and flags
+// the waiting cells too).
+// sweep[0]: the block counter (zero before the launch); sweep[1]: the abort word.
+constexpr long long kSweepWait = 2000000000ll;   // SM clocks (about 1 s) before a wait gives up
+
+// 8 warps of 8 rows each; 32 registers, so that 8 CTAs (8 blocks in flight) fit on an SM:
+// measured on the 512-cell implicit step, the sweeps take 84, 75 and 64 ms per step at 5, 6
+// and 8 CTAs per SM, and 75 ms with CTAs of 4 warps at 12 per SM.
+constexpr int kSweepThreads = 256;
+
+__global__ void __launch_bounds__(kSweepThreads, 8) k_trsv_sweep(NewtonCell* nc, int nslots, int maxblk, int upper,
+                                                                 int epoch, int* sweep) {
+    constexpr int kW = kSweepThreads / 32;   // warps
+    constexpr int kR = kNb / kW;             // rows per warp
+    __shared__ int s_t;
     __shared__ float T[kNb][kNb + 1];
     __shared__ float rb[kNb];
-    const float* inv = N.Dinv + (size_t)(b0 / kNb) * 2 * kNb * kNb + (upper ? kNb * kNb : 0);
-    if (!upper)
-        for (int i = threadIdx.x; i < kNb * kNb; i += blockDim.x) T[i >> 6][i & (kNb - 1)] = inv[i];
-    else   // Uinv from its stored transpose
-        for (int i = threadIdx.x; i < kNb * kNb; i += blockDim.x) T[i & (kNb - 1)][i >> 6] = inv[i];
-    if (threadIdx.x < kNb) rb[threadIdx.x] = threadIdx.x < kb ? in[b0 + threadIdx.x] : 0.0f;
-    __syncthreads();
-    if (threadIdx.x < kb) {
-        float s = 0.0f;
-#pragma unroll 16
-        for (int k = 0; k < kNb; ++k) s += T[threadIdx.x][k] * rb[k];
-        out[b0 + threadIdx.x] = s;
-    }
-}
-
-__global__ void __launch_bounds__(256) k_trsv_rows(NewtonCell* nc, int nslots, int b0, int upper) {
-    NewtonCell& N = nc[blockIdx.y];
-    const int m = 2 * N.n;
-    if (blockIdx.y >= nslots || !N.active || b0 >= m) return;
-    const int kb = min(kNb, m - b0);
-    const int lo = upper ? 0 : b0 + kb, hi = upper ? b0 : m;
-    const int r0 = lo + blockIdx.x * kTrsvRows;
-    if (r0 >= hi) return;
-    const float* xsrc = (upper ? N.z : N.zt) + b0;
-    float* upd = upper ? N.zt : N.z;
-    // a warp per row, four rows in flight: rows i, i + 8, i + 16, i + 24
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int rend = min(r0 + kTrsvRows, hi);
-    const float x0 = lane < kb ? xsrc[lane] : 0.0f, x1 = lane + 32 < kb ? xsrc[lane + 32] : 0.0f;
-    for (int i = r0 + warp; i < rend; i += 32) {
-        float s[4];
+    const int total = maxblk * nslots;
+    volatile int* abort_w = sweep + 1;
+    for (;;) {
+        __syncthreads();   // the previous block's shared arrays are free
+        if (threadIdx.x == 0) s_t = atomicAdd(sweep, 1);
+        __syncthreads();
+        const int t = s_t;
+        if (t >= total) break;
+        const int slot = t % nslots, rt = t / nslots;   // by block rank, then cell
+        NewtonCell& N = nc[slot];
+        const int m = 2 * N.n, nblk = (m + kNb - 1) / kNb;
+        if (!N.active || rt >= nblk) continue;
+        const int b = upper ? nblk - 1 - rt : rt;
+        const int b0 = b * kNb, kb = min(kNb, m - b0);
+        const float* in = upper ? N.zt : N.z;   // this pass's right-hand side
+        float* out = upper ? N.z : N.zt;        // this pass's solution
+        volatile int* flag = N.flags;
+        const float* inv = N.Dinv + (size_t)b * 2 * kNb * kNb + (upper ? kNb * kNb : 0);
+        if (!upper)
+            for (int i = threadIdx.x; i < kNb * kNb; i += blockDim.x) T[i >> 6][i & (kNb - 1)] = inv[i];
+        else   // Uinv from its stored transpose
+            for (int i = threadIdx.x; i < kNb * kNb; i += blockDim.x) T[i & (kNb - 1)][i >> 6] = inv[i];
+        // this warp's rows: b0 + warp + kW u, u < kR
+        float acc[kR];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int r = i + 8 * u;
-            const float* Ai = N.J + (size_t)r * N.ld + b0;
-            s[u] = r < rend ? (lane < kb ? Ai[lane] * x0 : 0.0f) + (lane + 32 < kb ? Ai[lane + 32] * x1 : 0.0f) : 0.0f;
+        for (int u = 0; u < kR; ++u) {
+            const int r = warp + kW * u;
+            acc[u] = r < kb ? in[b0 + r] : 0.0f;
         }
+        // the solved blocks j, in solve order
+        const int jstep = upper ? -1 : 1;
+        int j = upper ? nblk - 1 : 0;
+        while (j != b) {
+            // lane 0 finds how far the consecutive published blocks reach (waiting, bounded,
+            // for the first one), then the warp applies them
+            int ready = j;
+            if (lane == 0) {
+                const long long t0 = clock64();
+                bool stop = false;
+                while (flag[ready] != epoch) {
+                    if (*abort_w) stop = true;
+                    else if (clock64() - t0 > kSweepWait) {
+                        *abort_w = 1;
+                        stop = true;
+                    }
+                    if (stop) break;
+                    __nanosleep(64);
+                }
+                if (stop) {
+                    N.norms[3] = 3.0;   // this cell's solution is not valid
+                    ready = b;          // apply nothing more
+                } else {
+                    while (ready != b && flag[ready] == epoch) ready += jstep;
+                }
+                __threadfence();        // the solutions published before the flags
+            }
+            ready = __shfl_sync(0xffffffffu, ready, 0);
+            for (; j != ready; j += jstep) {
+                const int j0 = j * kNb, kj = min(kNb, m - j0);
+                const float x0 = lane < kj ? __ldcg(out + j0 + lane) : 0.0f;
+                const float x1 = lane + 32 < kj ? __ldcg(out + j0 + lane + 32) : 0.0f;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
+                for (int h = 0; h < kR / 8; ++h) {   // eight rows at a time
+                    float sp[8];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) s[u] += __shfl_xor_sync(0xffffffffu, s[u], o);
-        if (lane < 4) {
-            const int r = i + 8 * lane;
-            const float v = lane == 0 ? s[0] : lane == 1 ? s[1] : lane == 2 ? s[2] : s[3];
-            if (r < rend) upd[r] -= v;
+                    for (int u = 0; u < 8; ++u) {
+                        const int r = warp + kW * (8 * h + u);
+                        const float* Ai = N.J + (size_t)(b0 + r) * N.ld + j0;
+                        sp[u] = r < kb ? (lane < kj ? Ai[lane] * x0 : 0.0f) +
+                                             (lane + 32 < kj ? Ai[lane + 32] * x1 : 0.0f)
+                                       : 0.0f;
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+                        for (int u = 0; u < 8; ++u) sp[u] += __shfl_xor_sync(0xffffffffu, sp[u], o);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) acc[8 * h + u] -= sp[u];
+                }
+            }
         }
+        if (lane == 0)
+#pragma unroll
+            for (int u = 0; u < kR; ++u) rb[warp + kW * u] = warp + kW * u < kb ? acc[u] : 0.0f;
+        __syncthreads();
+        if (threadIdx.x < kb) {
+            float s = 0.0f;
+#pragma unroll 16
+            for (int k = 0; k < kNb; ++k) s += T[threadIdx.x][k] * rb[k];
+            out[b0 + threadIdx.x] = s;
+            __threadfence();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) flag[b] = epoch;
     }
 }
 
@@ -1057,22 +1115,23 @@ void launch_dense_clear(NewtonCell* nc, int nslots, int max_n, cudaStream_t st) 
     k_dense_clear<<<dim3(gx, (unsigned)nslots), 256, 0, st>>>(nc, nslots);
 }
 
-void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, cudaStream_t st) {
+// z = U^-1 L^-1 r for every active cell.  sweep: 2 ints of device scratch; *epoch: the last
+// epoch used by this cell set's flags (advanced by two).
+void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, int* sweep, int* epoch, cudaStream_t st) {
     const int m = 2 * max_n, nblk = (m + kNb - 1) / kNb;
     k_trsv_init<<<dim3((unsigned)std::max(1, std::min((m + 255) / 256, 32)), (unsigned)nslots), 256, 0, st>>>(nc, nslots);
-    for (int b = 0; b < nblk; ++b) {   // forward, L
-        const int rows = m - (b + 1) * kNb;
-        k_trsv_block<<<nslots, 256, 0, st>>>(nc, nslots, b * kNb, 0);
-        if (rows > 0)
-            k_trsv_rows<<<dim3((unsigned)((rows + kTrsvRows - 1) / kTrsvRows), (unsigned)nslots), 256, 0, st>>>(
-                nc, nslots, b * kNb, 0);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)k_trsv_sweep, kSweepThreads, 0) !=
+            cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        per_sm = 1;
     }
-    for (int b = nblk - 1; b >= 0; --b) {   // backward, U
-        const int rows = b * kNb;
-        k_trsv_block<<<nslots, 256, 0, st>>>(nc, nslots, b * kNb, 1);
-        if (rows > 0)
-            k_trsv_rows<<<dim3((unsigned)((rows + kTrsvRows - 1) / kTrsvRows), (unsigned)nslots), 256, 0, st>>>(
-                nc, nslots, b * kNb, 1);
+    const int grid = std::max(1, std::min(nblk * nslots, std::max(1, g_num_sms) * per_sm));
+    for (int upper = 0; upper < 2; ++upper) {   // forward with L, then backward with U
+        *epoch += 1;
+        cudaMemsetAsync(sweep, 0, 2 * sizeof(int), st);
+        k_trsv_sweep<<<grid, kSweepThreads, 0, st>>>(nc, nslots, nblk, upper, *epoch, sweep);
     }
 }
 void launch_newton_refine(const CellDev* cells, NewtonCell* nc, const int* cell_slot, const WorkItem* work, int nwork,
