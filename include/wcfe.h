@@ -394,7 +394,9 @@ int wcfe_area_tot_noalloc(const double* x_dev, int32_t n_vert, const int32_t* tr
  * positions: the last correction below 1e-13 of the displacement, or no further
  * reduction of |G| (more than 1/4 of the previous) once below 1e-6 of the scale.
  * After the step V = (x - X)/dt, A = (V - V_old)/dt, ea += Res_ea/MM.  FP64 engines
- * only.  Dense factors take 4 (2N)^2 bytes per cell on the device. */
+ * only.  Dense factors take 4 (2N)^2 bytes per cell on the device; this workspace is kept
+ * (and counted against the HBM budget) from one call to the next until the cells or the
+ * LU's outer block change, or the engine is destroyed. */
 typedef struct wcfe_newton_stats {
     int32_t newton_iters;              /* Newton updates summed over steps (all cells together) */
     int32_t max_refine_iters;          /* largest number of refinement passes of one linear solve */

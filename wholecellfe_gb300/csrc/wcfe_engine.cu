@@ -203,6 +203,11 @@ struct wcfe_engine {
     int vertex_kind = 0;          // mixed form: vertex-phase kernel for 5 (0) or 4 (1) blocks per SM
     int patch_kernel = 1;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
     bool fused = false;           // mixed form: runs of steps fold each next vertex phase into the patch phase
+    // the implicit step's workspace (dense tangents, factors, solve vectors), kept between
+    // calls while the cell set and the LU's outer block stay the same
+    void* newton_plan = nullptr;
+    uint64_t newton_version = 0;
+    int newton_nb = 0;
     int lu_nb = 1024, lu_kind = 0; // implicit step's LU: outer block width, 0 tcgen05 / 1 mma.sync updates
     int lu_reuse = 1;             // 1: factor once per implicit step, 0: every Newton iteration
     int cap_ne = 0, cap_nvp = 0, cap_nh = 0, cap_nc = 0;   // largest patch over the cells (staging plan)
@@ -905,6 +910,10 @@ int check_planar_ccw(const double* x, int n, const std::vector<int32_t>& T) {
 // C ABI
 // =============================================================================
 extern "C" {
+namespace {
+void release_newton_plan(wcfe_engine* e);   // the implicit step's kept workspace (below)
+}  // namespace
+
 
 void wcfe_params_default(wcfe_params* p, int32_t variant) {
     std::memset(p, 0, sizeof *p);
@@ -969,6 +978,7 @@ int wcfe_engine_destroy(wcfe_engine* e) {
     cudaSetDevice(e->device);
     xjoin(e);
     cudaStreamSynchronize(e->stream);
+    release_newton_plan(e);
     for (auto& kv : e->cells) free_cell(e, kv.second.get());
     e->cells.clear();
     invalidate_graph(e);
@@ -2086,6 +2096,35 @@ void newton_free(wcfe_engine* e, NewtonPlan& P) {
     }
 }
 
+void release_newton_plan(wcfe_engine* e) {
+    if (!e->newton_plan) return;
+    NewtonPlan* P = static_cast<NewtonPlan*>(e->newton_plan);
+    newton_free(e, *P);
+    delete P;
+    e->newton_plan = nullptr;
+}
+
+// the engine's implicit-step workspace: kept between calls, rebuilt when the cells or the
+// LU's outer block changed (a workspace for 512 cells of up to 4,000 vertices is tens of
+// GB: allocating and clearing it per call took longer than a factorisation)
+int kept_newton_plan(wcfe_engine* e, NewtonPlan** out) {
+    if (e->newton_plan && (e->newton_version != e->version || e->newton_nb != e->lu_nb)) release_newton_plan(e);
+    if (!e->newton_plan) {
+        NewtonPlan* P = new NewtonPlan;
+        int r = newton_plan(e, *P);
+        if (r) {
+            newton_free(e, *P);
+            delete P;
+            return r;
+        }
+        e->newton_plan = P;
+        e->newton_version = e->version;
+        e->newton_nb = e->lu_nb;
+    }
+    *out = static_cast<NewtonPlan*>(e->newton_plan);
+    return WCFE_OK;
+}
+
 int newton_upload_active(wcfe_engine* e, NewtonPlan& P) {
     CK(cudaMemcpyAsync(P.d_cells, P.cells.data(), sizeof(NewtonCell) * P.cells.size(), cudaMemcpyHostToDevice,
                        e->stream));
@@ -2255,14 +2294,14 @@ int wcfe_engine_step_implicit(wcfe_engine* e, int32_t nsteps, double dt, double 
     CK(cudaSetDevice(e->device));
     int r = sync_tables(e, dt);
     if (r) return r;
-    NewtonPlan P;
-    if ((r = newton_plan(e, P))) return r;
-    for (int s = 0; s < nsteps && !r; ++s) r = newton_step(e, P, dt, newton_rtol, max_newton, stats);
+    NewtonPlan* P = nullptr;
+    if ((r = kept_newton_plan(e, &P))) return r;
+    for (int s = 0; s < nsteps && !r; ++s) r = newton_step(e, *P, dt, newton_rtol, max_newton, stats);
     if (!r) {
         cudaError_t ce = cudaStreamSynchronize(e->stream);
         if (ce != cudaSuccess) r = fail(std::string("CUDA: ") + cudaGetErrorString(ce), WCFE_ERR_CUDA);
     }
-    newton_free(e, P);
+    if (r) release_newton_plan(e);   // rebuilt on the next call
     return r;
 }
 
