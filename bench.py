@@ -832,6 +832,7 @@ def run_phase(args):
         eng = capi.Engine(capi.PREC_MIXED if args.phase == "mixed" else capi.PREC_FP64)
         if args.phase == "mixed":
             eng.set_patch_kernel(args.patch_kernel)
+            eng.set_vertex_kernel(args.vertex_kernel)
             eng.set_fused(bool(args.fused))
         if args.shape:
             t, e_ = (int(x) for x in args.shape.split(","))
@@ -845,7 +846,8 @@ def run_phase(args):
     print(json.dumps({"phase": args.phase, "cells": ncells, "ms_per_step": r["total_ms"] / args.steps,
                       "vertex_ms": r["ms_v"] / args.steps, "patch_ms": r["ms_p"] / args.steps,
                       "cell_steps_per_s": ncells * args.steps / (r["total_ms"] / 1e3), "shape": [thr, emax],
-                      "patch_kernel": args.patch_kernel, "fused": eng.fused()}))
+                      "patch_kernel": args.patch_kernel, "vertex_kernel": args.vertex_kernel,
+                      "fused": eng.fused()}))
     eng.close()
 
 
@@ -954,6 +956,8 @@ def main():
     ap.add_argument("--patch-kernel", type=int, default=1, choices=[0, 1, 2, 3, 4],
                     help="with --phase mixed: 0 staged patch kernel, 1 plain (default), 2-4 plain with registers "
                          "capped for 6-8 CTAs per SM")
+    ap.add_argument("--vertex-kernel", type=int, default=0, choices=[0, 1, 2, 3],
+                    help="with --phase mixed: vertex kernel for 5, 4, 6 or 8 blocks per SM")
     ap.add_argument("--fused", type=int, default=0, choices=[0, 1],
                     help="with --phase mixed: fold each next vertex phase into the patch phase (default 0)")
     args = ap.parse_args()

@@ -230,8 +230,9 @@ int wcfe_cell_eval_forces(wcfe_engine* eng, int32_t cell, const double* x, doubl
  * capped; 128 patch threads only).  Results are identical; wcfe_engine_autotune times
  * them all.  No counterpart in the reference. */
 int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind);
-/* Mixed engines: the vertex-phase kernel compiled for 5 (kind 0, default) or 4 (kind 1)
- * resident blocks of 256 threads per SM (48 or 64 registers); results are identical. */
+/* Mixed engines: the vertex-phase kernel compiled for 5 (kind 0, default), 4 (kind 1), 6
+ * (kind 2) or 8 (kind 3) resident blocks of 256 threads per SM (48, 64, 40 or 32
+ * registers); results are identical; wcfe_engine_autotune times them all. */
 int wcfe_engine_set_vertex_kernel(wcfe_engine* e, int32_t kind);
 /* The patch and vertex kernel kinds in use (after wcfe_engine_autotune: its choice). */
 int wcfe_engine_get_kernels(const wcfe_engine* e, int32_t* patch_kind, int32_t* vertex_kind);

@@ -437,3 +437,26 @@ def test_fused_flag():
     f.set_fused(True)
     assert not f.fused()
     f.close()
+
+
+def test_vertex_kernel_kinds_equal():
+    """The vertex phase compiled for 5, 4, 6 and 8 blocks per SM computes the same bits."""
+    cells = _fused_cells()[:3]
+    ref = None
+    for kind in range(4):
+        e = capi.Engine(capi.PREC_MIXED)
+        e.set_vertex_kernel(kind)
+        hs = []
+        for x0, tri, p, st, rho, t in cells:
+            h = e.add_cell(x0, tri, p, state=st, t=t)
+            if rho is not None:
+                h.set_integrins(rho)
+            hs.append(h)
+        e.step(15, 5e-5)
+        got = [h.get_state() for h in hs]
+        e.close()
+        if ref is None:
+            ref = got
+        for a, b in zip(ref, got):
+            for u, w in zip(a, b):
+                assert np.array_equal(u, w)

@@ -200,7 +200,7 @@ struct wcfe_engine {
     int patch_threads = 128;
     int patch_emax = 320;
     int vblock = 256;             // vertices (threads) per vertex-phase block
-    int vertex_kind = 0;          // mixed form: vertex-phase kernel for 5 (0) or 4 (1) blocks per SM
+    int vertex_kind = 0;          // mixed form: vertex-phase kernel for 5 (0), 4 (1), 6 (2) or 8 (3) blocks per SM
     int patch_kernel = 1;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
     bool fused = false;           // mixed form: runs of steps fold each next vertex phase into the patch phase
     // the implicit step's workspace (dense tangents, factors, solve vectors), kept between
@@ -1727,7 +1727,7 @@ int wcfe_engine_get_fused(const wcfe_engine* e) { return e ? (fused_ok(e) ? 1 : 
 
 int wcfe_engine_set_vertex_kernel(wcfe_engine* e, int32_t kind) {
     xjoin(e);
-    if (!e || kind < 0 || kind > 1) return fail("bad argument", WCFE_ERR_ARG);
+    if (!e || kind < 0 || kind > 3) return fail("bad argument", WCFE_ERR_ARG);
     e->vertex_kind = kind;
     invalidate_graph(e);
     return WCFE_OK;
@@ -2632,7 +2632,7 @@ int wcfe_engine_autotune(wcfe_engine* e, double dt, int32_t reps) {
     if (!r && e->prec == WCFE_PREC_MIXED) {   // the vertex phase's register cap, at the chosen patch shape
         float bestv = 1e30f;
         int bv = 0;
-        for (int vk = 0; vk < 2; ++vk) {
+        for (int vk = 0; vk < 4; ++vk) {
             e->vertex_kind = vk;
             wcfe_engine_step(e, 1, dt);
             if (wcfe_engine_step(e, reps, dt)) continue;

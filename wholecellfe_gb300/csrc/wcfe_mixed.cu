@@ -941,8 +941,8 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a, co
 // one cell): predict, bond kinetics with FP32 rates and float-float accumulation,
 // and the FP32 element records.  No FP64 arithmetic outside the exchange
 // conversions and the area of the finishing block.
-// MINB: the least blocks of 256 threads per SM the register allocation must allow (5:
-// 48 registers with some spilling; 4: 64 registers); the autotuner picks.
+// MINB: the least blocks of 256 threads per SM the register allocation must allow (4, 5,
+// 6, 8: 64, 48, 40, 32 registers, spilling more as the cap falls); the autotuner picks.
 template <int MINB>
 __global__ void __launch_bounds__(kK1Threads, MINB) k_vertex_phase_mixed(const CellDev* __restrict__ cells,
                                                                     const WorkItem* __restrict__ work,
@@ -968,8 +968,12 @@ void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, 
     va.flags = flags;
     va.stage_in = stage_in;
     va.stage_out = stage_out;
-    if (kind == 1) k_vertex_phase_mixed<4><<<nwork, threads, 0, st>>>(cells, work, va);
-    else k_vertex_phase_mixed<5><<<nwork, threads, 0, st>>>(cells, work, va);
+    switch (kind) {
+        case 1: k_vertex_phase_mixed<4><<<nwork, threads, 0, st>>>(cells, work, va); break;
+        case 2: k_vertex_phase_mixed<6><<<nwork, threads, 0, st>>>(cells, work, va); break;
+        case 3: k_vertex_phase_mixed<8><<<nwork, threads, 0, st>>>(cells, work, va); break;
+        default: k_vertex_phase_mixed<5><<<nwork, threads, 0, st>>>(cells, work, va); break;
+    }
 }
 
 // ===========================================================================
