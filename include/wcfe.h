@@ -437,6 +437,12 @@ int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x);
 int wcfe_debug_lu_schedule(int32_t m, int32_t block, int32_t* ops, int32_t cap, int32_t* nops);
 /* The same with the LU variant of wcfe_engine_set_lu. */
 int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* x, int32_t block, int32_t kind);
+/* The failure path of the triangular solves, for tests: as wcfe_debug_lu_solve, but the
+ * solution of 64-row block `withhold` is never published to the blocks that wait for it,
+ * whose waits give up after wait_clocks SM clocks.  Returns WCFE_ERR_CUDA ("triangular
+ * sweep timed out") when a wait ran out; the context stays usable. */
+int wcfe_debug_trsv_withheld(int32_t m, const float* A, const double* b, float* x, int32_t withhold,
+                             int64_t wait_clocks);
 
 /* The dense tangent J (2N x 2N, row-major, FP32) of cell `id` at positions x [n][3]
  * with the cell's state as step start, and the mass/damping diagonal [n]. */

@@ -238,3 +238,23 @@ def test_implicit_step_factor_reuse_agrees():
         e.close()
     u = out[1] - st[0]
     assert np.max(np.abs(out[0] - out[1])) / np.max(np.abs(u)) < 1e-9
+
+
+def test_trsv_sweep_wait_times_out_cleanly():
+    """The triangular sweep's failure path, with no GPU fault: block 0's solution is never
+    published, so the next block's wait runs out (after 2e6 SM clocks, about 1 ms) and
+    raises the sweep's abort word, which ends every other wait.  The call reports the
+    timeout and returns promptly, and the context stays usable: a normal factorisation and
+    solve right after it are correct."""
+    import time
+    m = 640
+    rng = np.random.default_rng(5)
+    A = (rng.uniform(-1.0, 1.0, (m, m)) + m * np.eye(m)).astype(np.float32)
+    b = rng.uniform(-1.0, 1.0, m)
+    t0 = time.perf_counter()
+    rc, msg = capi.debug_trsv_withheld(A, b, 0, 2_000_000)
+    assert rc != 0 and "timed out" in msg, (rc, msg)
+    assert time.perf_counter() - t0 < 10.0
+    x = capi.debug_lu_solve(A, b, 1024, 0).astype(np.float64)
+    ref = np.linalg.solve(A.astype(np.float64), b)
+    assert np.max(np.abs(x - ref)) / np.max(np.abs(ref)) < 3e-3

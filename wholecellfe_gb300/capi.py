@@ -102,6 +102,8 @@ SIGNATURES = {
     "wcfe_engine_step_implicit": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_void_p]),
     "wcfe_cell_newton_tangent": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, _d, C.POINTER(C.c_float), _d]),
     "wcfe_debug_lu_solve": (C.c_int, [C.c_int32, C.POINTER(C.c_float), _d, C.POINTER(C.c_float)]),
+    "wcfe_debug_trsv_withheld": (C.c_int, [C.c_int32, C.POINTER(C.c_float), _d, C.POINTER(C.c_float), C.c_int32,
+                                           C.c_int64]),
     "wcfe_debug_lu_solve_with": (C.c_int, [C.c_int32, C.POINTER(C.c_float), _d, C.POINTER(C.c_float), C.c_int32,
                                            C.c_int32]),
     "wcfe_engine_set_lu": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
@@ -198,6 +200,18 @@ def debug_lu_solve(A, b, block: int | None = None, kind: int = 0):
         check(load().wcfe_debug_lu_solve_with(len(b), A.ctypes.data_as(fp), dp(b), x.ctypes.data_as(fp), block, kind),
               "wcfe_debug_lu_solve_with")
     return x
+
+
+def debug_trsv_withheld(A, b, withhold: int, wait_clocks: int):
+    """The triangular sweep with block `withhold`'s solution never published (its
+    dependents' waits run out after wait_clocks SM clocks); returns (status, message)."""
+    A = np.ascontiguousarray(A, np.float32)
+    b = np.ascontiguousarray(b, np.float64)
+    x = np.zeros(len(b), np.float32)
+    fp = C.POINTER(C.c_float)
+    rc = load().wcfe_debug_trsv_withheld(len(b), A.ctypes.data_as(fp), dp(b), x.ctypes.data_as(fp), withhold,
+                                         wait_clocks)
+    return rc, (load().wcfe_last_error().decode() if rc else "")
 
 
 def vtk_format(fmt: int, x, tri, cA=None, cC=None, fau=None, ea=None, time: float = 0.0, kint: float = -1.0,

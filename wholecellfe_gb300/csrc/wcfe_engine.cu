@@ -68,7 +68,8 @@ std::string lu_attr_note() {
 size_t lu_prefix_capacity(int nslots, int max_m);
 std::vector<LuOp> lu_schedule(int max_m, int nb);
 int encode_lu_maps(const NewtonCell* h, int nslots, LuMaps* out);
-void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, int* sweep, int* epoch, cudaStream_t st);
+void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, int* sweep, int* epoch, cudaStream_t st,
+                         int withhold = -1, long long wait_limit = 0);
 void launch_newton_refine(const CellDev* cells, NewtonCell* nc, const int* cell_slot, const WorkItem* work, int nwork,
                           int add_z, cudaStream_t st);
 void launch_newton_accumulate(NewtonCell* nc, int nslots, int max_n, cudaStream_t st);
@@ -2364,7 +2365,24 @@ int wcfe_debug_lu_solve(int32_t m, const float* A, const double* b, float* x) {
     return wcfe_debug_lu_solve_with(m, A, b, x, 512, 0);
 }
 
+namespace {
+int debug_lu_solve_impl(int32_t m, const float* A, const double* b, float* x, int32_t block, int32_t kind,
+                        int withhold, long long wait_limit);
+}  // namespace
+
 int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* x, int32_t block, int32_t kind) {
+    return debug_lu_solve_impl(m, A, b, x, block, kind, -1, 0);
+}
+
+int wcfe_debug_trsv_withheld(int32_t m, const float* A, const double* b, float* x, int32_t withhold,
+                             int64_t wait_clocks) {
+    if (withhold < 0 || wait_clocks <= 0) return fail("bad argument", WCFE_ERR_ARG);
+    return debug_lu_solve_impl(m, A, b, x, 1024, 0, withhold, wait_clocks);
+}
+
+namespace {
+int debug_lu_solve_impl(int32_t m, const float* A, const double* b, float* x, int32_t block, int32_t kind,
+                        int withhold, long long wait_limit) {
     if (m <= 0 || (m & 1) || !A || !b || !x) return fail("bad argument", WCFE_ERR_ARG);
     if (!lu_block_ok(block, kind)) return fail("bad argument", WCFE_ERR_ARG);
     int ndev = 0;
@@ -2417,7 +2435,7 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     const char* failed = nullptr;
     if (ce == cudaSuccess) {
         failed = launch_newton_lu(d_nc, &N, 1, m, d_maps, d_pref, block, kind, 0);
-        launch_newton_solve(d_nc, 1, m / 2, d_sweep, &epoch, 0);
+        launch_newton_solve(d_nc, 1, m / 2, d_sweep, &epoch, 0, withhold, wait_limit);
         if (!failed && cudaGetLastError() != cudaSuccess) failed = "triangular solves";
         ce = cudaDeviceSynchronize();
     }
@@ -2435,6 +2453,7 @@ int wcfe_debug_lu_solve_with(int32_t m, const float* A, const double* b, float* 
     if (flag != 0.0) return fail("zero or non-finite pivot", WCFE_ERR_STATE);
     return WCFE_OK;
 }
+}  // namespace
 
 int wcfe_cell_set_element_mu(wcfe_engine* e, int32_t id, const double* mu) {
     xjoin(e);

@@ -653,8 +653,11 @@ constexpr long long kSweepWait = 2000000000ll;   // SM clocks (about 1 s) before
 // and 8 CTAs per SM, and 75 ms with CTAs of 4 warps at 12 per SM.
 constexpr int kSweepThreads = 256;
 
+// withhold >= 0 (tests of the timeout path only): that block of every cell is solved but its
+// flag is never published, so every block after it waits until wait_limit clocks run out.
 __global__ void __launch_bounds__(kSweepThreads, 8) k_trsv_sweep(NewtonCell* nc, int nslots, int maxblk, int upper,
-                                                                 int epoch, int* sweep) {
+                                                                 int epoch, int* sweep, int withhold,
+                                                                 long long wait_limit) {
     constexpr int kW = kSweepThreads / 32;   // warps
     constexpr int kR = kNb / kW;             // rows per warp
     __shared__ int s_t;
@@ -702,7 +705,7 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_trsv_sweep(NewtonCell* nc,
                 bool stop = false;
                 while (flag[ready] != epoch) {
                     if (*abort_w) stop = true;
-                    else if (clock64() - t0 > kSweepWait) {
+                    else if (clock64() - t0 > wait_limit) {
                         *abort_w = 1;
                         stop = true;
                     }
@@ -754,7 +757,7 @@ __global__ void __launch_bounds__(kSweepThreads, 8) k_trsv_sweep(NewtonCell* nc,
             __threadfence();
         }
         __syncthreads();
-        if (threadIdx.x == 0) flag[b] = epoch;
+        if (threadIdx.x == 0 && b != withhold) flag[b] = epoch;
     }
 }
 
@@ -1116,8 +1119,11 @@ void launch_dense_clear(NewtonCell* nc, int nslots, int max_n, cudaStream_t st) 
 }
 
 // z = U^-1 L^-1 r for every active cell.  sweep: 2 ints of device scratch; *epoch: the last
-// epoch used by this cell set's flags (advanced by two).
-void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, int* sweep, int* epoch, cudaStream_t st) {
+// epoch used by this cell set's flags (advanced by two); withhold, wait_limit: see
+// k_trsv_sweep (-1 and 0: the normal solve with waits of about 1 s).
+void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, int* sweep, int* epoch, cudaStream_t st,
+                         int withhold, long long wait_limit) {
+    if (wait_limit <= 0) wait_limit = kSweepWait;
     const int m = 2 * max_n, nblk = (m + kNb - 1) / kNb;
     k_trsv_init<<<dim3((unsigned)std::max(1, std::min((m + 255) / 256, 32)), (unsigned)nslots), 256, 0, st>>>(nc, nslots);
     int per_sm = 0;
@@ -1131,7 +1137,7 @@ void launch_newton_solve(NewtonCell* nc, int nslots, int max_n, int* sweep, int*
     for (int upper = 0; upper < 2; ++upper) {   // forward with L, then backward with U
         *epoch += 1;
         cudaMemsetAsync(sweep, 0, 2 * sizeof(int), st);
-        k_trsv_sweep<<<grid, kSweepThreads, 0, st>>>(nc, nslots, nblk, upper, *epoch, sweep);
+        k_trsv_sweep<<<grid, kSweepThreads, 0, st>>>(nc, nslots, nblk, upper, *epoch, sweep, withhold, wait_limit);
     }
 }
 void launch_newton_refine(const CellDev* cells, NewtonCell* nc, const int* cell_slot, const WorkItem* work, int nwork,
