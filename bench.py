@@ -9,7 +9,8 @@ one explicit step (A1-A9), so a step is 256 cell-steps.
 
 Reported on one JSON line: the headline value (batched mixed form: FP32 element
 assembly and forces, float-float state and accumulation; device-timed, inputs
-resident), e2e (the same loop through the batched drop-in exchange with
+resident, the steps replayed from captured CUDA graphs; the same steps launched
+eagerly with per-step events give the p50/p99 step latency), e2e (the same loop through the batched drop-in exchange with
 pinned host buffers: per step the predicted positions go to the host and the
 integrated positions come back), the plain FP64 one-cell form (about 2000 vertices),
 the relative displacement error of the mixed form against the FP64 form, per-step
@@ -281,12 +282,14 @@ def timed_graph_steps(eng, steps, dt, ranks_barrier=None):
     torch.cuda.synchronize()
     if ranks_barrier:
         ranks_barrier()
+    l0 = eng.launches()
     e0.record(st)
     eng.step(steps, dt)
     e1.record(st)
     e1.synchronize()
+    launches = eng.launches() - l0
     eng.set_graphs(False)
-    return {"total_ms": e0.elapsed_time(e1)}
+    return {"total_ms": e0.elapsed_time(e1), "launches": launches}
 
 
 def run_ours(args):
@@ -337,15 +340,18 @@ def run_ours(args):
     launches = eng.launches() - launches0
     graph = timed_graph_steps(eng, args.steps, DT, barrier)
     graph_s = max_over_ranks(graph["total_ms"] / 1e3, dist, f"cuda:{local}")
-    graph_value = len(specs) * args.steps / graph_s
-    t_s = max_over_ranks(res["total_ms"] / 1e3, dist, f"cuda:{local}")
+    eager_s = max_over_ranks(res["total_ms"] / 1e3, dist, f"cuda:{local}")
+    eager_value = len(specs) * args.steps / eager_s
+    # the headline: the batched form as it runs in production, its steps replayed from captured
+    # CUDA graphs (the same K steps, CUDA events on the engine stream around them)
+    t_s = graph_s
     value = len(specs) * args.steps / t_s
     p50 = percentile(res["per_step"], 0.5)
     p99 = percentile(res["per_step"], 0.99)
     avg_v = res["ms_v"] / args.steps
     avg_p = res["ms_p"] / args.steps
-    log(f"[bench] mixed: {t_s * 1e3 / args.steps:.3f} ms/step (vertex {avg_v:.3f}, patch {avg_p:.3f}), "
-        f"{value:.3e} cell-steps/s, wall {res['wall_s']:.2f}s")
+    log(f"[bench] mixed: {t_s * 1e3 / args.steps:.3f} ms/step from graphs, {value:.3e} cell-steps/s; eager "
+        f"{eager_s * 1e3 / args.steps:.3f} ms/step (vertex {avg_v:.3f}, patch {avg_p:.3f})")
 
     # ---- e2e through the batched drop-in exchange, pinned host buffers ----
     ntot = eng.total_vertices()
@@ -496,10 +502,13 @@ def run_ours(args):
                        "parallelism": f"cell shards x{world} (population {len(specs)} cells, LPT by vertex count, "
                                       "no data-path collective)"},
             "p50_ms_per_step": round(p50, 4), "p99_ms_per_step": round(p99, 4),
-            "graph": {"value": round(graph_value, 1), "unit": "cell-steps/s",
-                      "ms_per_step": round(graph_s * 1e3 / args.steps, 4),
-                      "how": "the same steps replayed from captured CUDA graphs (8 steps each), CUDA events on the "
-                             "engine stream; the headline value launches eagerly with per-step events"},
+            "timing": "value: the K steps replayed from captured CUDA graphs (8 steps each), CUDA events on the "
+                      "engine stream around them; p50/p99: the same K steps launched eagerly with events around "
+                      "every step (`eager`)",
+            "eager": {"value": round(eager_value, 1), "unit": "cell-steps/s",
+                      "ms_per_step": round(eager_s * 1e3 / args.steps, 4),
+                      "vertex_phase_ms": round(avg_v, 4), "patch_phase_ms": round(avg_p, 4),
+                      "gpu_launches": int(launches)},
             "plain_fp64": {"value": round(plain_value, 1), "unit": "cell-steps/s", "cell_vertices": len(x0),
                            "workload": "one cell of 2,044 vertices / 3,929 triangles, E 1 kPa, nu 0.45, 0.1 um, 600 "
                                        "integrins (1 pN/nm, rest 20 nm), boundary protruding 10 nm/step, 200 steps",
@@ -512,7 +521,7 @@ def run_ours(args):
             "mixed_vs_fp64_rel_displacement_error": max_err, "error_steps": err_steps,
             "accuracy": accuracy,
             "element_assemblies_per_s": round(value / len(cells) * nt_total / world, 1),
-            "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "serving": serving,
+            "e2e": e2e, "gpu_launches": int(graph["launches"]), "roofline": roofline, "cpu_baseline": cpu, "serving": serving,
             "newton": newton, "config2": config2,
             "clocks": clocks_info, "pipe_rates": rates,
         }
