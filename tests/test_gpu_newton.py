@@ -258,3 +258,33 @@ def test_trsv_sweep_wait_times_out_cleanly():
     x = capi.debug_lu_solve(A, b, 1024, 0).astype(np.float64)
     ref = np.linalg.solve(A.astype(np.float64), b)
     assert np.max(np.abs(x - ref)) / np.max(np.abs(ref)) < 3e-3
+
+
+def test_implicit_workspace_kept_between_calls():
+    """The implicit step keeps its workspace from one call to the next: three calls of one
+    step give exactly the state of one call of three steps; after a cell is added the
+    workspace is rebuilt, and the new cell steps as it does alone (to the Newton
+    tolerance: in a batch a cell may take one more refinement pass than alone)."""
+    x0, tri, st, p, t = _cell(220, 41)
+    out = []
+    for calls in ([1, 1, 1], [3]):
+        e = capi.Engine(capi.PREC_FP64)
+        h = e.add_cell(x0, tri, p, state=st, t=t)
+        for n in calls:
+            stats = e.step_implicit(n, DT, rtol=1e-11, max_newton=8)
+            assert stats["unconverged"] == 0 and h.status() == 0, stats
+        out.append(h.get_state())
+        if len(calls) == 3:   # grow the cell set: the kept workspace must be rebuilt
+            x1, tri1, st1, p1, t1 = _cell(160, 42)
+            h1 = e.add_cell(x1, tri1, p1, state=st1, t=t1)
+            e.step_implicit(1, DT, rtol=1e-11, max_newton=8)
+            grown = h1.get_state()[0]
+            a = capi.Engine(capi.PREC_FP64)
+            ha = a.add_cell(x1, tri1, p1, state=st1, t=t1)
+            a.step_implicit(1, DT, rtol=1e-11, max_newton=8)
+            alone = ha.get_state()[0]
+            a.close()
+            assert np.max(np.abs(grown - alone)) <= 1e-9 * np.max(np.abs(alone - st1[0]))
+        e.close()
+    for u, w in zip(out[0], out[1]):
+        assert np.array_equal(u, w)
