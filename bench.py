@@ -240,6 +240,15 @@ def kernel_bytes_patch_mixed(nv_total: int, nt_total: int) -> float:
     return per_v * nv_total + per_t * nt_total
 
 
+def kernel_bytes_vertex_mixed(nv_total: int) -> float:
+    """Algorithmic DRAM bytes of one mixed vertex-phase launch: per vertex it reads the
+    triple-float position (32 B), V (32), the FP32 acceleration (16), the bond vector
+    (32), c_C and c_A (8 each), the strain's high words (16) and the boundary rank (4);
+    it writes the predicted position (32), the bond vector (32), c_C (8) and the FP32
+    element record (48)."""
+    return (32 + 32 + 16 + 32 + 8 + 8 + 16 + 4 + 32 + 32 + 8 + 48) * nv_total
+
+
 def percentile(xs, q):
     xs = sorted(xs)
     if not xs:
@@ -463,11 +472,20 @@ def run_ours(args):
             for line in open(prof):
                 if line.startswith("dram_bytes_per_vertex:"):
                     traffic = float(line.split(":")[1]) * nv_total
+        vbytes = kernel_bytes_vertex_mixed(nv_total)
+        step_ms = t_s * 1e3 / args.steps
         roofline = {"bound": "hbm", "kernel": "k_patch_phase_mixed", "achieved": round(achieved, 1),
                     "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
                     "traffic": traffic, "algorithmic_bytes_per_launch": int(kbytes),
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in peaks else "fallback 6800 GB/s",
-                    "avg_launch_ms": round(avg_p, 4), "vertex_phase_avg_launch_ms": round(avg_v, 4)}
+                    "avg_launch_ms": round(avg_p, 4), "vertex_phase_avg_launch_ms": round(avg_v, 4),
+                    "vertex_phase": {"algorithmic_bytes_per_launch": int(vbytes),
+                                     "achieved": round(vbytes / (avg_v * 1e-3) / 1e9, 1),
+                                     "frac": round(vbytes / (avg_v * 1e-3) / 1e9 / hbm, 4)},
+                    "step": {"algorithmic_bytes": int(kbytes + vbytes), "ms": round(step_ms, 4),
+                             "achieved": round((kbytes + vbytes) / (step_ms * 1e-3) / 1e9, 1),
+                             "frac": round((kbytes + vbytes) / (step_ms * 1e-3) / 1e9 / hbm, 4),
+                             "note": "both phases' algorithmic bytes over the graph-replayed step time"}}
 
         config2 = run_config2()
         log(f"[bench] config 2: {config2}")
