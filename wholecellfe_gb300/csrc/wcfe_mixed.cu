@@ -522,23 +522,35 @@ __device__ __noinline__ void substrate_move(const CellDev& c, const ff4& Xv, con
     }
 }
 
-// The cell area and centroid of the predicted positions xo (shoelace over the directed
+// The predicted in-plane position of vertex v from its step-start position Xv, velocity V
+// and acceleration A: vh = V + (dt/2) A (or the protrusion driver), x = X + dt vh.
+__device__ __forceinline__ void predict_xy(const CellDev& c, int v, const VertexArgs& va, const ff4& Xv, const ff4& V,
+                                           const float4& A, tf& xn0, tf& xn1, ff& vh0, ff& vh1) {
+    vh0 = ff_add(ffx(V), ff_mul_f(va.hdt, A.x));
+    vh1 = ff_add(ffy(V), ff_mul_f(va.hdt, A.y));
+    protrude_ff(c, v, Xv, vh0, vh1);
+    xn0 = tf_add_ff(tfx(Xv), ff_mul(va.dt, vh0));
+    xn1 = tf_add_ff(tfy(Xv), ff_mul(va.dt, vh1));
+}
+
+// The cell area and centroid of the positions pos(u, x) gives (shoelace over the directed
 // boundary edges), then the step constants of the patch phase that follows.  Called by all
-// threads of one block of any size that is a multiple of 32 dividing 256, after every
-// prediction of the cell is visible to it; the sum has one fixed order whatever the block
-// size: boundary ranks strided over 256 virtual threads, the 32 lanes of each virtual warp
-// by a butterfly, then the 8 virtual warps in order.  s_w: 24 doubles of shared scratch.
-__device__ void area_shoelace(const CellDev& c, const double4* xo, double dt_real, double* s_w) {
+// threads of one block of any size that is a multiple of 32 dividing 256; the sum has one
+// fixed order whatever the block size: boundary ranks strided over 256 virtual threads, the
+// 32 lanes of each virtual warp by a butterfly, then the 8 virtual warps in order.  s_w: 24
+// doubles of shared scratch.
+template <class Pos>
+__device__ void shoelace_step_const(const CellDev& c, Pos pos, double dt_real, double* s_w) {
     constexpr int kVW = kK1Threads / 32;
     const int lane = threadIdx.x & 31;
     for (int vw = threadIdx.x >> 5; vw < kVW; vw += blockDim.x >> 5) {
         double s0 = 0, s1 = 0, s2 = 0;
         for (int r = vw * 32 + lane; r < c.nb; r += kK1Threads) {
             double xi[3];
-            pos_d(ld_ff4(xo, c.nv, c.bnd_vert[r]), xi);
+            pos(c.bnd_vert[r], xi);
             for (int k = c.bnd_optr[r]; k < c.bnd_optr[r + 1]; ++k) {
                 double xj[3];
-                pos_d(ld_ff4(xo, c.nv, c.bnd_out[k]), xj);
+                pos(c.bnd_out[k], xj);
                 const double cr = xi[0] * xj[1] - xj[0] * xi[1];
                 s0 += 0.5 * cr;
                 s1 += (1.0 / 6.0) * (xi[0] + xj[0]) * cr;
@@ -570,8 +582,31 @@ __device__ void area_shoelace(const CellDev& c, const double4* xo, double dt_rea
     __syncthreads();   // the scratch may be reused by the caller
 }
 
-// The vertex phase's cell area: the last block of the cell to finish (ticket ctl[2]) reads
-// the positions the other blocks wrote (through L2) and runs area_shoelace.
+// shoelace_step_const on positions stored in xo, after every store of them is visible (out of
+// line, as is area_predicted: its FP64 registers stay off the vertices' path)
+__device__ __noinline__ void area_shoelace(const CellDev& c, const double4* xo, double dt_real, double* s_w) {
+    shoelace_step_const(c, [&](int u, double* x) { pos_d(ld_ff4(xo, c.nv, u), x); }, dt_real, s_w);
+}
+
+// shoelace_step_const on the predictions of the step at parity par, formed here from the
+// step-start state with the arithmetic of vertex_predict (the same values its blocks store),
+// so that it needs no store of this step's vertex phase
+__device__ __noinline__ void area_predicted(const CellDev& c, int par, const VertexArgs& va, double* s_w) {
+    shoelace_step_const(
+        c,
+        [&](int u, double* x) {
+            const ff4 Xu = ldg_ff4(c.pos[par], c.nv, u);
+            tf x0, x1;
+            ff h0, h1;
+            predict_xy(c, u, va, Xu, ldg_ff4(c.vel, c.nv, u), ld_acc(c.acc, u), x0, x1, h0, h1);
+            pos_d(make_pos4(x0, x1, ffz(Xu)), x);
+        },
+        va.dtd, s_w);
+}
+
+// The vertex phase's cell area where this launch stores the positions it sums (imported
+// ones): the last block of the cell to finish (ticket ctl[2]) reads the positions the other
+// blocks wrote (through L2) and runs area_shoelace.
 __device__ __forceinline__ void finish_area_boundary(const CellDev& c, const double4* xo, double dt_real) {
     __shared__ int s_last;
     __shared__ double s_w[3 * kK1Threads / 32];
@@ -588,15 +623,12 @@ __device__ __forceinline__ void finish_area_boundary(const CellDev& c, const dou
     area_shoelace(c, xo, dt_real, s_w);
 }
 
-// The prediction of vertex v at step parity par from its step-start position Xv, velocity V
-// and acceleration A: vh = V + (dt/2) A (or the protrusion driver), x = X + dt vh, stored
-// in pos[par ^ 1] (and, for the exchange path, vh and x as binary64 for the host).
+// The prediction of vertex v at step parity par (predict_xy), stored in pos[par ^ 1] (and,
+// for the exchange path, vh and x as binary64 for the host).
 __device__ __forceinline__ void vertex_predict(const CellDev& c, int v, int par, const VertexArgs& va, const ff4& Xv,
                                                const ff4& V, const float4& A, tf& xn0, tf& xn1, ff& xn2) {
-    ff vh0 = ff_add(ffx(V), ff_mul_f(va.hdt, A.x)), vh1 = ff_add(ffy(V), ff_mul_f(va.hdt, A.y));
-    protrude_ff(c, v, Xv, vh0, vh1);
-    xn0 = tf_add_ff(tfx(Xv), ff_mul(va.dt, vh0));
-    xn1 = tf_add_ff(tfy(Xv), ff_mul(va.dt, vh1));
+    ff vh0, vh1;
+    predict_xy(c, v, va, Xv, V, A, xn0, xn1, vh0, vh1);
     xn2 = ffz(Xv);
     st_ff4(c.pos[par ^ 1], c.nv, v, make_pos4(xn0, xn1, xn2));
     if (va.flags & VM_EXPORT) {
@@ -814,6 +846,16 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a, co
         const StepConst& sc = *reinterpret_cast<const StepConst*>(c.stepc);
         const BndConst& s_bc = sc.b;
         const ElemParams q = sc.q;
+        // this CTA's next patch: its owned element records and its element slots into L2
+        // while this one computes (the records are gathered with dependent loads; the owned
+        // state is read coalesced and gains nothing from a prefetch)
+        if (threadIdx.x == blockDim.x - 32 && w + (int)gridDim.x < a.nwork) {
+            const WorkItem nt = work[w + gridDim.x];
+            const CellDev& cn = cells[nt.cell];
+            const int4 pn = cn.patch[nt.idx];
+            l2_prefetch(cn.rec[cn.ctl[0] & 1] + kRec * (size_t)pn.x, 16u * kRec * (size_t)pn.y);
+            l2_prefetch(cn.patch_tri + pn.z, 16u * (size_t)pn.w);
+        }
         // ---- elements of the patch -> shared memory ----
         for (int j = threadIdx.x; j < pt.w; j += blockDim.x) {
             const int4 t4 = __ldg(c.patch_tri + pt.z + j);   // (a, b, c, element id)
@@ -940,7 +982,10 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a, co
 // Mixed-form vertex phase, one block per work item (c.vb consecutive vertices of
 // one cell): predict, bond kinetics with FP32 rates and float-float accumulation,
 // and the FP32 element records.  No FP64 arithmetic outside the exchange
-// conversions and the area of the finishing block.
+// conversions and the cell area.  The area and the step constants come from the
+// cell's block 0, before its vertices, on predictions it forms itself (area_predicted)
+// or on positions already in place, so no block waits for another; only positions this
+// launch imports are summed after every block stored them (ticket, finish_area_boundary).
 // MINB: the least blocks of 256 threads per SM the register allocation must allow (4, 5,
 // 6, 8: 64, 48, 40, 32 registers, spilling more as the cap falls); the autotuner picks.
 template <int MINB>
@@ -952,8 +997,16 @@ __global__ void __launch_bounds__(kK1Threads, MINB) k_vertex_phase_mixed(const C
     if (cell_done(c)) return;   // block-uniform: a serving cell that ran its steps
     const int v = it.idx * c.vb + threadIdx.x;
     const int par = c.ctl[0];
-    if (v < c.nv) vertex_mixed_body(c, v, par, va);
-    if (!(va.flags & VM_NOAREA)) finish_area_boundary(c, c.pos[par ^ 1], va.dtd);
+    const bool area = !(va.flags & VM_NOAREA), ticket = area && (va.flags & VM_IMPORT);
+    if (area && !ticket && it.idx == 0) {   // block-uniform
+        __shared__ double s_w[3 * kK1Threads / 32];
+        if (va.flags & VM_PREDICT) area_predicted(c, par, va, s_w);
+        else area_shoelace(c, c.pos[par ^ 1], va.dtd, s_w);
+    }
+    VertexArgs vb = va;
+    if (!ticket) vb.flags |= VM_NOAREA;   // no block reads this launch's stored positions
+    if (v < c.nv) vertex_mixed_body(c, v, par, vb);
+    if (ticket) finish_area_boundary(c, c.pos[par ^ 1], va.dtd);
 }
 
 void launch_vertex_mixed(const CellDev* cells, const WorkItem* work, int nwork, double dt, int flags, int grid,

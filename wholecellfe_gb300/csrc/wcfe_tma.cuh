@@ -66,4 +66,16 @@ __device__ __forceinline__ void cp_async_mbar_arrive(uint64_t* bar) {
 
 __device__ __forceinline__ uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
 
+// Bulk prefetch into L2 of the 16-byte-aligned part of [p, p + bytes): the start rounded
+// up and the end rounded down, so the range never leaves the one given.  A hint with no
+// completion to wait for.
+__device__ __forceinline__ void l2_prefetch(const void* p, size_t bytes) {
+    const uintptr_t s = ((uintptr_t)p + 15) & ~(uintptr_t)15;
+    const uintptr_t e = ((uintptr_t)p + bytes) & ~(uintptr_t)15;
+    if (e > s)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(__cvta_generic_to_global((const void*)s)),
+                     "r"((uint32_t)(e - s))
+                     : "memory");
+}
+
 }  // namespace wcfe
