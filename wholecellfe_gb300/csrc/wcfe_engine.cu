@@ -180,6 +180,9 @@ struct wcfe_engine {
     std::vector<int32_t> order;   // table index -> cell id
     std::vector<CellDev> table;
     std::vector<WorkItem> k1, k2;
+    // k1 with every cell's block 0 first (the mixed vertex phase's area blocks start in
+    // the first wave), stored on the device right after k1 in d_k1
+    std::vector<WorkItem> k1a;
     int64_t total_nv = 0;         // vertices of all live cells (packed exchange arrays)
     double* d_xchg = nullptr;     // packed [total_nv][3] exchange buffer on the device
     size_t d_xchg_cap = 0;
@@ -617,7 +620,7 @@ int sync_tables(wcfe_engine* e, double dt = -1.0) {
     int r = build_tables(e);
     if (r) return r;
     if ((r = ensure_dev(&e->d_table, &e->d_table_cap, std::max<size_t>(e->table.size(), 1)))) return r;
-    if ((r = ensure_dev(&e->d_k1, &e->d_k1_cap, std::max<size_t>(e->k1.size(), 1)))) return r;
+    if ((r = ensure_dev(&e->d_k1, &e->d_k1_cap, std::max<size_t>(2 * e->k1.size(), 1)))) return r;
     if ((r = ensure_dev(&e->d_k2, &e->d_k2_cap, std::max<size_t>(e->k2.size(), 1)))) return r;
     // coupled cells point at their substrate's table entry (device address, known now)
     for (size_t ti = 0; ti < e->table.size(); ++ti) {
@@ -632,8 +635,11 @@ int sync_tables(wcfe_engine* e, double dt = -1.0) {
     }
     if (!e->table.empty())
         CK(cudaMemcpyAsync(e->d_table, e->table.data(), sizeof(CellDev) * e->table.size(), cudaMemcpyHostToDevice, e->stream));
-    if (!e->k1.empty())
+    if (!e->k1.empty()) {
         CK(cudaMemcpyAsync(e->d_k1, e->k1.data(), sizeof(WorkItem) * e->k1.size(), cudaMemcpyHostToDevice, e->stream));
+        CK(cudaMemcpyAsync(e->d_k1 + e->k1.size(), e->k1a.data(), sizeof(WorkItem) * e->k1a.size(),
+                           cudaMemcpyHostToDevice, e->stream));
+    }
     if (!e->k2.empty())
         CK(cudaMemcpyAsync(e->d_k2, e->k2.data(), sizeof(WorkItem) * e->k2.size(), cudaMemcpyHostToDevice, e->stream));
     CK(cudaStreamSynchronize(e->stream));
@@ -677,6 +683,11 @@ int build_tables(wcfe_engine* e) {
     }
     e->n2_sub = (int)k2_sub.size();
     e->k2.insert(e->k2.end(), k2_sub.begin(), k2_sub.end());
+    e->k1a.clear();
+    for (const WorkItem& w : e->k1)
+        if (w.idx == 0) e->k1a.push_back(w);
+    for (const WorkItem& w : e->k1)
+        if (w.idx != 0) e->k1a.push_back(w);
     return WCFE_OK;
 }
 
@@ -761,8 +772,10 @@ int enqueue_step(wcfe_engine* e, const WorkItem* k1, int n1, const WorkItem* k2,
     int g1 = grid_for(e, n1, vertex_occupancy(e->vblock));
     cudaEvent_t* tv = (e->timing && e->tev.size() >= 3) ? &e->tev[3 * (size_t)e->timed_steps] : nullptr;
     const bool vertex = kind == STEP_FULL || kind == STEP_FIRST;
+    // the whole engine's list: the same items with every cell's block 0 first
+    const WorkItem* k1v = (k1 == e->d_k1 && n1 == (int)e->k1.size() && e->k1a.size() == e->k1.size()) ? k1 + n1 : k1;
     if (tv) cudaEventRecord(tv[0], e->stream);
-    if (vertex) vphase(e, e->d_table, k1, n1, dt, VP_PREDICT | VP_UPDATE_FA | rec_flag(e), g1, e->stream);
+    if (vertex) vphase(e, e->d_table, k1v, n1, dt, VP_PREDICT | VP_UPDATE_FA | rec_flag(e), g1, e->stream);
     if (tv) cudaEventRecord(tv[1], e->stream);
     const int nsub = (k2 == e->d_k2 && n2 == (int)e->k2.size()) ? e->n2_sub : 0;
     patch_step(e, k2, n2 - nsub, dt, dt, apt, std::numeric_limits<double>::quiet_NaN(), 0, nullptr,
@@ -2744,9 +2757,9 @@ int sync_tables_async(wcfe_engine* e, double dt) {
         return WCFE_OK;
     };
     if ((r = grow(&e->d_table, &e->d_table_cap, std::max<size_t>(e->table.size(), 1), sizeof(CellDev)))) return r;
-    if ((r = grow(&e->d_k1, &e->d_k1_cap, std::max<size_t>(e->k1.size(), 1), sizeof(WorkItem)))) return r;
+    if ((r = grow(&e->d_k1, &e->d_k1_cap, std::max<size_t>(2 * e->k1.size(), 1), sizeof(WorkItem)))) return r;
     if ((r = grow(&e->d_k2, &e->d_k2_cap, std::max<size_t>(e->k2.size(), 1), sizeof(WorkItem)))) return r;
-    const size_t b0 = sizeof(CellDev) * e->table.size(), b1 = sizeof(WorkItem) * e->k1.size(),
+    const size_t b0 = sizeof(CellDev) * e->table.size(), b1 = 2 * sizeof(WorkItem) * e->k1.size(),
                  b2 = sizeof(WorkItem) * e->k2.size();
     const int k = e->tab_buf;
     e->tab_buf ^= 1;
@@ -2762,7 +2775,8 @@ int sync_tables_async(wcfe_engine* e, double dt) {
     }
     char* h = static_cast<char*>(e->h_tab[k]);
     std::memcpy(h, e->table.data(), b0);
-    std::memcpy(h + b0, e->k1.data(), b1);
+    std::memcpy(h + b0, e->k1.data(), b1 / 2);
+    std::memcpy(h + b0 + b1 / 2, e->k1a.data(), b1 / 2);
     std::memcpy(h + b0 + b1, e->k2.data(), b2);
     if (b0) CK(cudaMemcpyAsync(e->d_table, h, b0, cudaMemcpyHostToDevice, e->stream));
     if (b1) CK(cudaMemcpyAsync(e->d_k1, h + b0, b1, cudaMemcpyHostToDevice, e->stream));
