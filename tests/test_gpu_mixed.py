@@ -121,13 +121,16 @@ def test_exchange_path_equals_internal_steps(prec, pinned):
                 assert np.max(np.abs(u - w)) <= 1e-9 * max(np.max(np.abs(w)), 1e-12)
 
 
+@pytest.mark.parametrize("host", ["pageable", "pinned", "alternating"])
 @pytest.mark.parametrize("groups", [1, 3, 8])
 @pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
-def test_exchange_groups_equal_internal_steps(prec, groups):
+def test_exchange_groups_equal_internal_steps(prec, groups, host):
     """The exchange path with the cells split into groups on their own streams, with calls
     on the main stream in between (state reads, a regrouping, a status read), is the same
     computation as wcfe_engine_step: bit-identical for the FP64 form, 1e-9 of each array's
-    magnitude for the mixed form (the binary64 exchange of float-float positions)."""
+    magnitude for the mixed form (the binary64 exchange of float-float positions).  The
+    host array is pageable, page-locked (copied asynchronously), or page-locked on odd
+    steps only."""
     sizes = (300, 900, 500, 1200, 400, 700)
     cells = [synth.disk_mesh(n, seed=500 + n) for n in sizes]
     res = []
@@ -142,8 +145,13 @@ def test_exchange_groups_equal_internal_steps(prec, groups):
             e.step(12, 5e-5)
         else:
             e.set_exchange_groups(groups)
-            buf = np.zeros((e.total_vertices(), 3))
+            pageable = np.zeros((e.total_vertices(), 3))
+            pinned = None
+            if host != "pageable":
+                import torch
+                pinned = torch.zeros((e.total_vertices(), 3), dtype=torch.float64, pin_memory=True).numpy()
             for k in range(12):
+                buf = pinned if host == "pinned" or (host == "alternating" and k % 2) else pageable
                 e.predict_all(5e-5, buf)
                 if k == 4:
                     hs[2].get_state()            # a main-stream read between predict and update
@@ -161,6 +169,42 @@ def test_exchange_groups_equal_internal_steps(prec, groups):
                 assert np.array_equal(u, w)
             else:
                 assert np.max(np.abs(u - w)) <= 1e-9 * max(np.max(np.abs(w)), 1e-12)
+
+
+@pytest.mark.parametrize("prec", [capi.PREC_FP64, capi.PREC_MIXED])
+def test_exchange_pinned_equals_pageable_with_host_moves(prec):
+    """A host integrator that moves the predicted positions (as El Topo's collision
+    handling does) before the update: a page-locked array (asynchronous copies) gives the
+    same states bit for bit as a pageable one, for any grouping."""
+    sizes = (500, 1100, 700)
+    cells = [synth.disk_mesh(n, seed=700 + n) for n in sizes]
+    res = []
+    for host, groups in (("pageable", 1), ("pinned", 1), ("pinned", 3)):
+        e = capi.Engine(prec)
+        hs = []
+        for i, (x0, tri) in enumerate(cells):
+            p = default_params("k31")
+            p.stream = i
+            hs.append(e.add_cell(x0, tri, p, state=synth.initial_state(x0, perturb=1.0, seed=i)))
+        e.set_exchange_groups(groups)
+        n = e.total_vertices()
+        if host == "pinned":
+            import torch
+            buf = torch.zeros((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+        else:
+            buf = np.zeros((n, 3))
+        shift = 1e-7 * np.sin(np.arange(n, dtype=np.float64))[:, None] * np.array([1.0, -0.5, 0.0])
+        for k in range(10):
+            e.predict_all(5e-5, buf)
+            buf += shift * (k % 3)
+            e.update_all(5e-5, 5e-5, buf)
+            e.sync()
+        res.append([h.get_state() for h in hs])
+        e.close()
+    for other in res[1:]:
+        for a, b in zip(res[0], other):
+            for u, w in zip(a, b):
+                assert np.array_equal(u, w)
 
 
 def test_exchange_groups_argument():

@@ -624,17 +624,17 @@ __device__ __forceinline__ void finish_area_boundary(const CellDev& c, const dou
 }
 
 // The prediction of vertex v at step parity par (predict_xy), stored in pos[par ^ 1] (and,
-// for the exchange path, vh and x as binary64 for the host).
+// for the exchange path, vh, and x as binary64 into xq[0..2]).
 __device__ __forceinline__ void vertex_predict(const CellDev& c, int v, int par, const VertexArgs& va, const ff4& Xv,
-                                               const ff4& V, const float4& A, tf& xn0, tf& xn1, ff& xn2) {
+                                               const ff4& V, const float4& A, tf& xn0, tf& xn1, ff& xn2,
+                                               double* xq = nullptr) {
     ff vh0, vh1;
     predict_xy(c, v, va, Xv, V, A, xn0, xn1, vh0, vh1);
     xn2 = ffz(Xv);
     st_ff4(c.pos[par ^ 1], c.nv, v, make_pos4(xn0, xn1, xn2));
     if (va.flags & VM_EXPORT) {
         st_ff4(c.vhl, c.nv, v, make_ff4(vh0, vh1, {0.0f, 0.0f}));
-        double* qq = va.stage_out + 3 * (size_t)(c.hoff + v);
-        qq[0] = tf_to_d(xn0); qq[1] = tf_to_d(xn1); qq[2] = ff_to_d(xn2);
+        xq[0] = tf_to_d(xn0); xq[1] = tf_to_d(xn1); xq[2] = ff_to_d(xn2);
     }
 }
 
@@ -686,8 +686,10 @@ __device__ __forceinline__ void vertex_kinetics(const CellDev& c, int v, int par
 
 // One vertex of the vertex phase at step parity par: predict into pos[par ^ 1] (or take
 // the caller's positions), bond kinetics with FP32 rates and float-float accumulation,
-// and the FP32 element record rec[par].
-__device__ __forceinline__ void vertex_mixed_body(const CellDev& c, int v, int par, const VertexArgs& va) {
+// and the FP32 element record rec[par].  xq: the vertex's three binary64 coordinates of
+// the exchange (read with VM_IMPORT, written with VM_EXPORT).
+__device__ __forceinline__ void vertex_mixed_body(const CellDev& c, int v, int par, const VertexArgs& va,
+                                                  double* xq) {
     const int flags = va.flags;
     double4* __restrict__ xo = c.pos[par ^ 1];
     const ff4 Xv = ldg_ff4(c.pos[par], c.nv, v);
@@ -704,7 +706,7 @@ __device__ __forceinline__ void vertex_mixed_body(const CellDev& c, int v, int p
         // a coordinate the caller returned as the binary64 rounding of the predicted one keeps
         // the predicted triple-float (so the exchange path steps exactly as the internal one);
         // any other value is taken as given
-        const double* qq = va.stage_in + 3 * (size_t)(c.hoff + v);
+        const double* qq = xq;
         const ff4 pr = ld_ff4(xo, c.nv, v);
         const tf p0 = tfx(pr), p1 = tfy(pr);
         xn0 = tf_to_d(p0) == qq[0] ? p0 : tf_from_d(qq[0]);
@@ -712,7 +714,7 @@ __device__ __forceinline__ void vertex_mixed_body(const CellDev& c, int v, int p
         xn2 = ff_from_d(qq[2]);
         st_ff4(xo, c.nv, v, make_pos4(xn0, xn1, xn2));
     } else if (flags & VM_PREDICT) {
-        vertex_predict(c, v, par, va, Xv, ldg_ff4(c.vel, c.nv, v), ld_acc(c.acc, v), xn0, xn1, xn2);
+        vertex_predict(c, v, par, va, Xv, ldg_ff4(c.vel, c.nv, v), ld_acc(c.acc, v), xn0, xn1, xn2, xq);
     } else {
         const ff4 t = ld_ff4(xo, c.nv, v);
         xn0 = tfx(t); xn1 = tfy(t); xn2 = ffz(t);
@@ -826,14 +828,19 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a, co
     extern __shared__ float smf[];
     const int emax = EMAX > 0 ? EMAX : a.emax;
     // structure of arrays: field k of slot j at smf[k * emax + j]
-    __shared__ int s_nbnd, s_last;
+    // boundary-queue counts of alternate patches: a patch's count is cleared after the element
+    // barrier of the patch before it, when every thread has read it, so no barrier ends a patch
+    __shared__ int s_nb2[2], s_last;
     __shared__ float s_bnd[kBndRec * kBndSlots];
-    if (threadIdx.x == 0) s_nbnd = 0;
+    if (threadIdx.x == 0) s_nb2[0] = s_nb2[1] = 0;
     __syncthreads();
+    int kp = -1;   // patches this CTA has processed, less one
     for (int w = blockIdx.x; w < a.nwork; w += gridDim.x) {
         const WorkItem it = work[w];
         const CellDev& c = cells[it.cell];   // the table is read-only here: its fields stay in registers
         if (cell_done(c)) continue;   // block-uniform: a serving cell that ran its steps
+        ++kp;
+        int& s_nbnd = s_nb2[kp & 1];
         // fused: predict the cell's next step here unless this step is the last of its budget
         // (ctl[3] is counted down only after every patch of the cell took its ticket)
         const bool fuse = FUSED && c.ctl[3] != 1;
@@ -881,6 +888,7 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a, co
             smf[19 * emax + j] = o.acur;
         }
         __syncthreads();
+        if (threadIdx.x == 0) s_nb2[(kp + 1) & 1] = 0;   // the next patch's count
         // ---- owned vertices: forces and the acceleration in FP32, accumulations in float-float ----
         // Interior vertices finish here.  Boundary vertices queue their FP32 sums in shared
         // memory and finish in a second loop over consecutive threads, so that the float-float
@@ -952,10 +960,15 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a, co
             boundary_force(c, s_bc, pt, rec, xp, v, c.bnd_rank[v], F0, F1);
             finish_vertex(c, a, par, v, F0, F1, b[5], b[6], b[7], b[8], b[9], fuse);
         }
-        __syncthreads();
+        // The next patch's element loop may start while boundary vertices finish: it writes
+        // only the element slots, which nothing after the vertex loop's barrier reads.
+        if (fuse) __syncthreads();
         if (threadIdx.x == 0) {
-            s_nbnd = 0;   // for the next patch: every thread passes this CTA's next element barrier first
-            __threadfence();
+            // The ticket only counts the cell's patches, so that the last one advances the
+            // parity, clock and AP counter, which the next launch reads; only the fused form's
+            // last patch reads what the others stored (their predictions) and needs the
+            // release fence before its ticket.
+            if (fuse) __threadfence();
             const unsigned int done = atomicAdd(reinterpret_cast<unsigned int*>(c.ctl + 1), 1u);
             const bool last = (int)done == c.np - 1;
             if (last) {
@@ -1005,7 +1018,22 @@ __global__ void __launch_bounds__(kK1Threads, MINB) k_vertex_phase_mixed(const C
     }
     VertexArgs vb = va;
     if (!ticket) vb.flags |= VM_NOAREA;   // no block reads this launch's stored positions
-    if (v < c.nv) vertex_mixed_body(c, v, par, vb);
+    // The exchange coordinates of the block's vertices, 3 binary64 each, pass through shared
+    // memory so that the exchange staging array is read and written in consecutive runs
+    // (a warp's access covers 256 contiguous bytes instead of 32 doubles 24 bytes apart).
+    __shared__ double s_x[3 * kK1Threads];
+    const int v0 = it.idx * c.vb, nd = 3 * max(0, min(c.vb, c.nv - v0));
+    if (va.flags & VM_IMPORT) {   // block-uniform
+        const double* src = va.stage_in + 3 * ((size_t)c.hoff + v0);
+        for (int k = threadIdx.x; k < nd; k += blockDim.x) s_x[k] = src[k];
+        __syncthreads();
+    }
+    if (v < c.nv) vertex_mixed_body(c, v, par, vb, s_x + 3 * threadIdx.x);
+    if (va.flags & VM_EXPORT) {
+        __syncthreads();
+        double* dst = va.stage_out + 3 * ((size_t)c.hoff + v0);
+        for (int k = threadIdx.x; k < nd; k += blockDim.x) dst[k] = s_x[k];
+    }
     if (ticket) finish_area_boundary(c, c.pos[par ^ 1], va.dtd);
 }
 
