@@ -974,8 +974,14 @@ int wcfe_engine_create(int32_t device, int32_t precision, uint64_t hbm_budget_by
     CK(configure_newton((size_t)max_optin, e->num_sms > 0 ? e->num_sms : 1));
     for (auto& ev : e->ev) CK(cudaEventCreate(&ev));
     CK(cudaStreamCreateWithFlags(&e->xstream, cudaStreamNonBlocking));
+    // exchange group c's stream at a higher priority than group c + 1's (as far as the
+    // device's levels go): the block scheduler then finishes the groups in order, so each
+    // group's copy to the host runs while later groups still compute
+    int prio_least = 0, prio_greatest = 0;
+    CK(cudaDeviceGetStreamPriorityRange(&prio_least, &prio_greatest));
     for (int c = 0; c < wcfe_engine::kXMax; ++c) {
-        CK(cudaStreamCreateWithFlags(&e->cstream[c], cudaStreamNonBlocking));
+        const int prio = std::min(prio_least, prio_greatest + c);
+        CK(cudaStreamCreateWithPriority(&e->cstream[c], cudaStreamNonBlocking, prio));
         CK(cudaEventCreateWithFlags(&e->xin[c], cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&e->xout[c], cudaEventDisableTiming));
         CK(cudaEventCreateWithFlags(&e->cdone[c], cudaEventDisableTiming));
