@@ -1944,16 +1944,15 @@ int wcfe_engine_update(wcfe_engine* e, double dt, double dt_real, const double* 
     // earlier work has read it
     if (ordered)
         for (size_t c = 0; c < ch.size(); ++c) CK(cudaStreamWaitEvent(e->xstream, e->cdone[c], 0));
+    // each group's phases start on its own stream as soon as its positions are in; the copy
+    // and the phases of a group are issued together, so the first group's work is queued
+    // before the host issues the later groups' copies
     for (size_t c = 0; c < ch.size(); ++c) {
         const XChunk& x = ch[c];
         if (x.v_hi > x.v_lo)
             CK(cudaMemcpyAsync(e->d_xchg + 3 * x.v_lo, x_new + 3 * x.v_lo, sizeof(double) * 3 * (x.v_hi - x.v_lo),
                                cudaMemcpyHostToDevice, e->xstream));
         CK(cudaEventRecord(e->xin[c], e->xstream));
-    }
-    // each group's phases start on its own stream as soon as its positions are in
-    for (size_t c = 0; c < ch.size(); ++c) {
-        const XChunk& x = ch[c];
         cudaStream_t st = e->cstream[c];
         CK(cudaStreamWaitEvent(st, e->xin[c], 0));
         const int n1 = x.k1_hi - x.k1_lo, n2 = x.k2_hi - x.k2_lo;
