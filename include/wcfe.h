@@ -291,8 +291,9 @@ int64_t wcfe_engine_total_vertices(wcfe_engine* eng);
 int wcfe_engine_predict(wcfe_engine* eng, double dt, double* x_pred);
 int wcfe_engine_update(wcfe_engine* eng, double dt, double dt_real, const double* x_new);
 /* The exchange path splits the cells into `groups` (1 to 8, default 8) of about equal
- * vertex count, each stepped on its own stream: one group's predict and copy to the host
- * overlap another group's update.  Results do not depend on the grouping. */
+ * vertex count, each stepped on its own stream, the streams at descending priorities so
+ * that the groups finish in order: one group's predict and copy to the host overlap the
+ * later groups' update.  Results do not depend on the grouping. */
 int wcfe_engine_set_exchange_groups(wcfe_engine* eng, int32_t groups);
 /* Per-vertex integrin density (#/um^2) replacing rho_i_max (UL:1218); NULL restores the
  * uniform density.  A zero entry is a vertex without integrins. */

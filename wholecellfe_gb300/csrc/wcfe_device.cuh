@@ -95,7 +95,8 @@ struct CellDev {
     const int32_t* bnd_vert;    // [nb] boundary vertices in rank order (the inverse of bnd_rank)
     // control words, advanced by the last patch-phase CTA of the cell to finish a step:
     int32_t* ctl;               // [0] parity (which pos/ea buffer holds the step-start state), [1] patch-phase
-                                //     CTA ticket, [2] vertex-phase block ticket, [3] step budget (serving):
+                                //     CTA ticket, [2] vertex-phase block ticket (FP64 form; the mixed form
+                                //     only for imported positions), [3] step budget (serving):
                                 //     0 unlimited, n > 0 steps left, -1 done (every kernel skips the cell)
     double* clk;                // [0] simulation time at the start of the next step
     unsigned long long* ap;     // [0] calculateForce_AP calls made (the AP counter of the next step)
