@@ -213,4 +213,9 @@ __device__ __forceinline__ void finish_area(const CellDev& c) {
     }
 }
 
+// Blocks per SM of `kernel` at a launch shape (at least 1), cached per device, kernel,
+// block size and dynamic shared memory (wcfe_kernels.cu): the occupancy query is a driver
+// call of a few microseconds, and the host issues the same shapes every step.
+int occupancy_cached(const void* kernel, int threads, size_t smem);
+
 }  // namespace wcfe

@@ -149,6 +149,13 @@ struct Graph {
     uint64_t version = 0;
 };
 
+// One group of the exchange path: consecutive cells of the table (also consecutive in the
+// work lists and in the packed exchange array), their work-list ranges and vertex range.
+struct XChunk {
+    int k1_lo, k1_hi, k2_lo, k2_hi;
+    size_t v_lo, v_hi;
+};
+
 }  // namespace
 
 struct wcfe_engine {
@@ -166,6 +173,9 @@ struct wcfe_engine {
     // done, xout a group predicted, cdone a group's work done, xprev the main stream's work.
     static constexpr int kXMax = 8;
     int xchunks = 8;
+    std::vector<XChunk> xch;                 // the groups, kept for (xch_version, xch_count)
+    uint64_t xch_version = ~0ull;
+    int xch_count = 0;
     bool xpending = false;
     cudaStream_t xstream = nullptr;
     cudaStream_t cstream[kXMax] = {};
@@ -1849,13 +1859,11 @@ int64_t wcfe_engine_total_vertices(wcfe_engine* e) {
 namespace {
 // The exchange split into up to xchunks groups of consecutive cells (table order, which
 // is also the order of the work lists and of the packed exchange array), balanced by
-// vertex count.
-struct XChunk {
-    int k1_lo, k1_hi, k2_lo, k2_hi;
-    size_t v_lo, v_hi;
-};
-std::vector<XChunk> exchange_chunks(const wcfe_engine* e) {
-    std::vector<XChunk> out;
+// vertex count; rebuilt only when the tables or the group count change.
+const std::vector<XChunk>& exchange_chunks(wcfe_engine* e) {
+    if (e->xch_version == e->table_version && e->xch_count == e->xchunks) return e->xch;
+    std::vector<XChunk>& out = e->xch;
+    out.clear();
     const int ncell = (int)e->table.size();
     const int nch = std::max(1, std::min(e->xchunks, ncell));
     size_t k1 = 0, k2 = 0, v = 0;
@@ -1874,6 +1882,8 @@ std::vector<XChunk> exchange_chunks(const wcfe_engine* e) {
         v = x.v_hi;
         out.push_back(x);
     }
+    e->xch_version = e->table_version;
+    e->xch_count = e->xchunks;
     return out;
 }
 
@@ -1909,7 +1919,7 @@ int wcfe_engine_predict(wcfe_engine* e, double dt, double* x_pred) {
     if (r) return r;
     // group by group on the group's own stream (after that group's update): the predicted
     // positions of a group copy back while the other groups still update or predict
-    const std::vector<XChunk> ch = exchange_chunks(e);
+    const std::vector<XChunk>& ch = exchange_chunks(e);
     for (size_t c = 0; c < ch.size(); ++c) {
         const XChunk& x = ch[c];
         const int n1 = x.k1_hi - x.k1_lo;
@@ -1939,7 +1949,7 @@ int wcfe_engine_update(wcfe_engine* e, double dt, double dt_real, const double* 
     bool ordered = false;
     int r = exchange_begin(e, dt_real, &ordered);
     if (r) return r;
-    const std::vector<XChunk> ch = exchange_chunks(e);
+    const std::vector<XChunk>& ch = exchange_chunks(e);
     // a group's copy overwrites its part of the staging array only after that group's
     // earlier work has read it
     if (ordered)

@@ -22,6 +22,8 @@
 
 #include <cmath>
 #include <cstdint>
+#include <mutex>
+#include <vector>
 
 #include "wcfe_common.cuh"
 
@@ -664,26 +666,45 @@ static const void* patch_kernel(int mode) {
     return (const void*)k_patch_phase_fp64<PP_FORCES>;
 }
 
-int patch_occupancy(int prec, int threads, size_t smem) {
-    if (prec == WCFE_PREC_MIXED) return mixed_occupancy(threads, smem);
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, patch_kernel(PP_STEP), threads, smem) != cudaSuccess) {
+int occupancy_cached(const void* kernel, int threads, size_t smem) {
+    struct Entry {
+        int dev;
+        const void* kernel;
+        int threads;
+        size_t smem;
+        int blocks;
+    };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
         cudaGetLastError();
         return 1;
     }
-    return n > 0 ? n : 1;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (const Entry& x : cache)
+            if (x.dev == dev && x.kernel == kernel && x.threads == threads && x.smem == smem) return x.blocks;
+    }
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    n = n > 0 ? n : 1;
+    std::lock_guard<std::mutex> lk(mu);
+    cache.push_back({dev, kernel, threads, smem, n});
+    return n;
+}
+
+int patch_occupancy(int prec, int threads, size_t smem) {
+    if (prec == WCFE_PREC_MIXED) return mixed_occupancy(threads, smem);
+    return occupancy_cached(patch_kernel(PP_STEP), threads, smem);
 }
 
 bool mixed_available() { return true; }
 
-int vertex_occupancy(int threads) {
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, (const void*)k_vertex_phase, threads, 0) != cudaSuccess) {
-        cudaGetLastError();
-        return 1;
-    }
-    return n > 0 ? n : 1;
-}
+int vertex_occupancy(int threads) { return occupancy_cached((const void*)k_vertex_phase, threads, 0); }
 
 void launch_patch(int prec, int mode, const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt,
                   double dt_real, double ap_thresh, double t_override, int vh_from_buf, const double* centroid_dev,

@@ -1478,14 +1478,7 @@ cudaError_t configure_mixed(size_t max_smem) {
 }
 
 // resident CTAs per SM of the plain kernel variant `kind` (1-4, see k_patch_phase_mixed; 5 fused)
-int mixed_occupancy(int threads, size_t smem, int kind) {
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, mixed_kernel(kind), threads, smem) != cudaSuccess) {
-        cudaGetLastError();
-        return 1;
-    }
-    return n > 0 ? n : 1;
-}
+int mixed_occupancy(int threads, size_t smem, int kind) { return occupancy_cached(mixed_kernel(kind), threads, smem); }
 int mixed_occupancy(int threads, size_t smem) { return mixed_occupancy(threads, smem, 1); }
 
 void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, int emax, double dt, double dt_real,
