@@ -704,8 +704,9 @@ def run_serving(seconds: float = 10.0, rate: float = 200.0, budget_gb: float = 1
 def run_config2(steps: int = 500, seed: int = 2):
     """Config 2: one 20,000-vertex cell, 8,000 integrins with k(x) = k0 (1 + (x/x0)^2), k0 = 31 pN/nm,
     x0 = 5 nm, shear modulus log-normal per element (median mu, sigma 0.3), 500 steps, in the FP64
-    form and in the mixed form (FP32 assembly); device time per step of each and the mixed
-    form's relative displacement error against the FP64 form."""
+    form and in the mixed form with the FP32 element and with the float-float element; device
+    time per step of each and each mixed run's relative displacement error against the FP64
+    form."""
     import torch
     from wholecellfe_gb300 import capi, synth
     from wholecellfe_gb300.params import default_params
@@ -717,8 +718,11 @@ def run_config2(steps: int = 500, seed: int = 2):
     rho[rng.choice(len(x0), size=8000, replace=False)] = p.rho_i_max
     mu = p.mu * np.exp(0.3 * rng.standard_normal(len(tri)))
     out = {}
-    for name, prec in (("fp64", capi.PREC_FP64), ("mixed", capi.PREC_MIXED)):
+    for name, prec, ff in (("fp64", capi.PREC_FP64, 0), ("mixed", capi.PREC_MIXED, 0),
+                           ("mixed_ff", capi.PREC_MIXED, 1)):
         eng = capi.Engine(prec)
+        if ff:
+            eng.set_element_precision(1)
         h = eng.add_cell(x0, tri, p, state=synth.initial_state(x0))
         h.set_integrins(rho)
         h.set_element_mu(mu)
@@ -728,10 +732,15 @@ def run_config2(steps: int = 500, seed: int = 2):
         eng.close()
     u = out["fp64"][0] - x0
     err = float(np.max(np.abs(out["mixed"][0] - out["fp64"][0])) / np.max(np.abs(u)))
+    err_ff = float(np.max(np.abs(out["mixed_ff"][0] - out["fp64"][0])) / np.max(np.abs(u)))
     return {"vertices": len(x0), "triangles": len(tri), "integrins": 8000, "steps": steps,
             "fp64_ms_per_step": round(out["fp64"][1], 4), "mixed_ms_per_step": round(out["mixed"][1], 4),
             "mixed_vs_fp64_rel_displacement_error": err, "within_1e-6": bool(err <= 1e-6),
-            "status": [out["fp64"][2], out["mixed"][2]]}
+            "mixed_ff_element": {"ms_per_step": round(out["mixed_ff"][1], 4),
+                                 "rel_displacement_error": err_ff, "within_1e-6": bool(err_ff <= 1e-6),
+                                 "note": "the mixed form with the float-float element "
+                                         "(wcfe_engine_set_element_precision 1)"},
+            "status": [out["fp64"][2], out["mixed"][2], out["mixed_ff"][2]]}
 
 
 def lu_roofline(tflops, outer_block=512, tf32_peak=None):

@@ -251,6 +251,16 @@ int wcfe_engine_get_kernels(const wcfe_engine* e, int32_t* patch_kind, int32_t* 
  * (-1: no engine).  No counterpart in the reference (a batching schedule). */
 int wcfe_engine_set_fused(wcfe_engine* e, int32_t enable);
 int wcfe_engine_get_fused(const wcfe_engine* e);
+/* Mixed engines: the arithmetic of the element assembly.  0 (default): FP32 (the
+ * increment form of the mixed form); 1: every intermediate of the element in
+ * float-float (about 48 bits) from the same FP32 vertex records, the per-corner outputs
+ * rounded to FP32 once.  Mode 1 removes the FP32 element's own rounding floor (on a
+ * 20,000-vertex cell over 500 steps the displacement error against the FP64 form falls
+ * from about 1.1e-6 to about 1e-7) and runs the patch phase at 2 CTAs per SM; it is not
+ * fused (wcfe_engine_set_fused) and not staged (patch kernel kind 0).  FP64 engines
+ * accept 0 only.  get: *mode receives the current value. */
+int wcfe_engine_set_element_precision(wcfe_engine* e, int32_t mode);
+int wcfe_engine_get_element_precision(const wcfe_engine* e, int32_t* mode);
 
 /* Couple cell `cell` to a deformable substrate simulated by the same FP64 engine:
  * `substrate` is another cell of the engine holding the substrate mesh and state

@@ -504,3 +504,71 @@ def test_vertex_kernel_kinds_equal():
         for a, b in zip(ref, got):
             for u, w in zip(a, b):
                 assert np.array_equal(u, w)
+
+
+def _config2_cell(seed=2):
+    """Config 2: one 20,000-vertex disk, 8,000 integrins on the polynomial law, a log-normal
+    shear modulus per element (sigma 0.3)."""
+    rng = np.random.default_rng(seed)
+    x0, tri = synth.disk_mesh(20000, seed=seed)
+    p = default_params("k31")
+    p.force_law, p.poly_k0, p.poly_x0, p.linear_norm2d = 2, 31000.0, 0.005, 0
+    rho = np.zeros(len(x0))
+    rho[rng.choice(len(x0), size=8000, replace=False)] = p.rho_i_max
+    mu = p.mu * np.exp(0.3 * rng.standard_normal(len(tri)))
+    return x0, tri, p, rho, mu
+
+
+def test_ff_element_config2_within_gate():
+    """The mixed form with the float-float element (wcfe_engine_set_element_precision 1) on
+    config 2 over its 500 steps: displacement within 1e-6 of the FP64 form (per-vertex max
+    over the largest displacement), where the FP32 element reaches about 1.06e-6; the
+    float-float element's error is below the FP32 element's."""
+    x0, tri, p, rho, mu = _config2_cell()
+    xs = {}
+    for name, prec, ff in (("fp64", capi.PREC_FP64, 0), ("fp32", capi.PREC_MIXED, 0), ("ff", capi.PREC_MIXED, 1)):
+        e = capi.Engine(prec)
+        e.set_element_precision(ff)
+        assert e.element_precision() == ff
+        h = e.add_cell(x0, tri, p, state=synth.initial_state(x0))
+        h.set_integrins(rho)
+        h.set_element_mu(mu)
+        e.step(500, 5e-5)
+        assert h.status() == 0
+        xs[name] = h.get_state()[0]
+        e.close()
+    u = np.max(np.abs(xs["fp64"] - x0))
+    err32 = np.max(np.abs(xs["fp32"] - xs["fp64"])) / u
+    errff = np.max(np.abs(xs["ff"] - xs["fp64"])) / u
+    assert errff <= 1e-6, (errff, err32)
+    assert errff < err32, (errff, err32)
+
+
+def test_element_precision_flag():
+    """Mode 1 is the mixed form's only; it is neither fused nor staged; it keeps the
+    step's results within the mixed form's own bound of the FP32 element's."""
+    e = capi.Engine(capi.PREC_FP64)
+    with pytest.raises(capi.WcfeError):
+        e.set_element_precision(1)
+    e.set_element_precision(0)
+    e.close()
+    m = capi.Engine(capi.PREC_MIXED)
+    for bad in (-1, 2):
+        with pytest.raises(capi.WcfeError):
+            m.set_element_precision(bad)
+    m.set_element_precision(1)
+    m.set_fused(True)
+    x0, tri = synth.disk_mesh(900, seed=41)
+    h = m.add_cell(x0, tri, default_params("kMD"), state=synth.initial_state(x0, perturb=1.0, seed=4))
+    assert not m.fused()
+    m.set_patch_kernel(0)
+    m.step(20, 5e-5)
+    a = h.get_state()
+    m.close()
+    r = capi.Engine(capi.PREC_MIXED)
+    h2 = r.add_cell(x0, tri, default_params("kMD"), state=synth.initial_state(x0, perturb=1.0, seed=4))
+    r.step(20, 5e-5)
+    b = h2.get_state()
+    r.close()
+    d = np.max(np.abs(a[0] - b[0])) / max(np.max(np.abs(b[0] - x0)), 1e-30)
+    assert d <= 1e-5, d

@@ -97,6 +97,8 @@ SIGNATURES = {
     "wcfe_engine_get_kernels": (C.c_int, [C.c_void_p, _i, _i]),
     "wcfe_engine_set_fused": (C.c_int, [C.c_void_p, C.c_int32]),
     "wcfe_engine_get_fused": (C.c_int, [C.c_void_p]),
+    "wcfe_engine_set_element_precision": (C.c_int, [C.c_void_p, C.c_int32]),
+    "wcfe_engine_get_element_precision": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32)]),
     "wcfe_cell_set_element_mu": (C.c_int, [C.c_void_p, C.c_int32, _d]),
     "wcfe_cell_couple_substrate": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
     "wcfe_engine_step_implicit": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.c_double, C.c_int32, C.c_void_p]),
@@ -378,6 +380,15 @@ class Engine:
     def fused(self) -> bool:
         """True where a run of steps of this engine is fused."""
         return load().wcfe_engine_get_fused(self.h) == 1
+
+    def set_element_precision(self, mode: int):
+        """Mixed engines: 0 the FP32 element, 1 the float-float element."""
+        check(load().wcfe_engine_set_element_precision(self.h, int(mode)), "wcfe_engine_set_element_precision")
+
+    def element_precision(self) -> int:
+        m = C.c_int32(-1)
+        check(load().wcfe_engine_get_element_precision(self.h, C.byref(m)), "wcfe_engine_get_element_precision")
+        return int(m.value)
 
     def kernels(self):
         """(patch kernel kind, vertex kernel kind) in use."""

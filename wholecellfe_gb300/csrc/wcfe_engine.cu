@@ -215,6 +215,7 @@ struct wcfe_engine {
     int patch_emax = 320;
     int vblock = 256;             // vertices (threads) per vertex-phase block
     int vertex_kind = 0;          // mixed form: vertex-phase kernel for 5 (0), 4 (1), 6 (2) or 8 (3) blocks per SM
+    bool element_ff = false;      // mixed form: the float-float element (wcfe_engine_set_element_precision)
     int patch_kernel = 1;         // mixed form: 0 staged (bulk copies) where its plan fits, 1 plain
     bool fused = false;           // mixed form: runs of steps fold each next vertex phase into the patch phase
     // the implicit step's workspace (dense tangents, factors, solve vectors), kept between
@@ -745,7 +746,7 @@ enum { STEP_FULL = 0, STEP_FIRST = 1, STEP_MID = 2, STEP_LAST = 3 };
 // fused runs: the mixed form's plain patch kernels, no coupled substrate (whose patch phase
 // must follow its cells' before their next prediction)
 bool fused_ok(const wcfe_engine* e) {
-    return e->prec == WCFE_PREC_MIXED && e->fused && e->patch_kernel != 0 && e->n2_sub == 0;
+    return e->prec == WCFE_PREC_MIXED && e->fused && e->patch_kernel != 0 && e->n2_sub == 0 && !e->element_ff;
 }
 int step_kind(const wcfe_engine* e, int s, int n) {
     if (n < 2 || !fused_ok(e)) return STEP_FULL;
@@ -757,11 +758,11 @@ void patch_step(wcfe_engine* e, const WorkItem* k2, int n2, double dt, double dt
                 int vh_from_buf, cudaStream_t st = nullptr, int fused = 0) {
     if (!st) st = e->stream;
     if (e->prec == WCFE_PREC_MIXED) {
-        if (e->patch_kernel == 0 &&
+        if (e->patch_kernel == 0 && !e->element_ff &&
             launch_patch_staged(e->d_table, k2, n2, e->cap_ne, e->cap_nvp, e->cap_nh, e->cap_nc, dt, dt_real, apt,
                                 t_override, vh_from_buf, e->num_sms, st))
             return;
-        const int kind = e->patch_kernel == 0 ? 1 : e->patch_kernel;
+        const int kind = e->element_ff ? 6 : (e->patch_kernel == 0 ? 1 : e->patch_kernel);
         const size_t smem = mixed_smem_bytes(e->patch_emax);
         const int okind = fused ? 5 : kind;   // the fused form is its own instantiation
         launch_patch_mixed(e->d_table, k2, n2, e->patch_emax, dt, dt_real, apt, t_override, vh_from_buf,
@@ -1745,6 +1746,21 @@ int wcfe_engine_set_patch_kernel(wcfe_engine* e, int32_t kind) {
     return WCFE_OK;
 }
 
+int wcfe_engine_set_element_precision(wcfe_engine* e, int32_t mode) {
+    xjoin(e);
+    if (!e || mode < 0 || mode > 1) return fail("bad argument", WCFE_ERR_ARG);
+    if (mode == 1 && e->prec != WCFE_PREC_MIXED) return fail("the float-float element is the mixed form's", WCFE_ERR_ARG);
+    e->element_ff = mode == 1;
+    invalidate_graph(e);
+    return WCFE_OK;
+}
+
+int wcfe_engine_get_element_precision(const wcfe_engine* e, int32_t* mode) {
+    if (!e || !mode) return fail("bad argument", WCFE_ERR_ARG);
+    *mode = e->element_ff ? 1 : 0;
+    return WCFE_OK;
+}
+
 int wcfe_engine_set_fused(wcfe_engine* e, int32_t enable) {
     xjoin(e);
     if (!e || enable < 0 || enable > 1) return fail("bad argument", WCFE_ERR_ARG);
@@ -2653,7 +2669,7 @@ int wcfe_engine_autotune(wcfe_engine* e, double dt, int32_t reps) {
     // mixed engines also try the staged patch kernel (its block shape is fixed; it uses emax)
     // and the plain kernel with register caps for 6, 7 and 8 CTAs of 128 threads per SM
     std::vector<int> kinds = {1};
-    if (e->prec == WCFE_PREC_MIXED) kinds = {1, 2, 3, 4, 0};
+    if (e->prec == WCFE_PREC_MIXED && !e->element_ff) kinds = {1, 2, 3, 4, 0};
     for (int kind : kinds) {
         e->patch_kernel = kind;
         for (int em : emax_c) {

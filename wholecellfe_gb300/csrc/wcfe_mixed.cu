@@ -314,6 +314,118 @@ __device__ __forceinline__ void element2d(const float4 r[3][kRec], const ElemPar
     o.acur = 0.5f * fabsf(gc);
 }
 
+// A float-float scalar with the arithmetic operators (wcfe_ff.cuh), for element2d_ff.
+struct fq {
+    ff v;
+    __device__ __forceinline__ fq() : v{0.0f, 0.0f} {}
+    __device__ __forceinline__ fq(float x) : v{x, 0.0f} {}
+    __device__ __forceinline__ fq(ff x) : v(x) {}
+    __device__ __forceinline__ float f() const { return v.hi; }
+};
+__device__ __forceinline__ fq operator+(fq a, fq b) { return ff_add(a.v, b.v); }
+__device__ __forceinline__ fq operator-(fq a, fq b) { return ff_sub(a.v, b.v); }
+__device__ __forceinline__ fq operator*(fq a, fq b) { return ff_mul(a.v, b.v); }
+__device__ __forceinline__ fq operator/(fq a, fq b) { return ff_div(a.v, b.v); }
+__device__ __forceinline__ fq operator-(fq a) { return ff{-a.v.hi, -a.v.lo}; }
+
+// element2d with every intermediate in float-float (about 48 bits) from the same FP32
+// records, the outputs rounded to FP32 once: the mixed form's float-float element
+// (wcfe_engine_set_element_precision), for runs whose accuracy the FP32 element's own
+// roundings would limit.  The reference edges and the step's displacement differences are
+// formed exactly from the record's words (TwoSum).
+__device__ __forceinline__ void element2d_ff(const float4 r[3][kRec], const ElemParams& q, Elem2& o) {
+    const fq G1x = two_sum(r[1][0].x - r[0][0].x, r[1][0].z - r[0][0].z);
+    const fq G1y = two_sum(r[1][0].y - r[0][0].y, r[1][0].w - r[0][0].w);
+    const fq G2x = two_sum(r[2][0].x - r[0][0].x, r[2][0].z - r[0][0].z);
+    const fq G2y = two_sum(r[2][0].y - r[0][0].y, r[2][0].w - r[0][0].w);
+    const fq d1x = two_sum(r[1][1].x, -r[0][1].x), d1y = two_sum(r[1][1].y, -r[0][1].y);
+    const fq d2x = two_sum(r[2][1].x, -r[0][1].x), d2y = two_sum(r[2][1].y, -r[0][1].y);
+    const fq Gc = G1x * G2y - G1y * G2x;
+    const fq iG = fq(1.0f) / Gc;
+    const fq b1x = G2y * iG, b1y = -(G2x * iG);
+    const fq b2x = -(G1y * iG), b2y = G1x * iG;
+    const fq b0x = -(b1x + b2x), b0y = -(b1y + b2y);
+    const fq H00 = d1x * b1x + d2x * b2x, H01 = d1x * b1y + d2x * b2y;
+    const fq H10 = d1y * b1x + d2y * b2x, H11 = d1y * b1y + d2y * b2y;
+    const fq gc = (G1x + d1x) * (G2y + d2y) - (G1y + d1y) * (G2x + d2x);
+    const fq third = fq(1.0f) / fq(3.0f);
+    const fq exx = third * (fq(r[0][1].z) + r[1][1].z + r[2][1].z);
+    const fq eyy = third * (fq(r[0][1].w) + r[1][1].w + r[2][1].w);
+    const fq exy = third * (fq(r[0][2].x) + r[1][2].x + r[2][2].x);
+    const fq ezz = third * (fq(r[0][2].y) + r[1][2].y + r[2][2].y);
+    const fq one(1.0f), two(2.0f);
+    const fq m00 = one - two * exx, m11 = one - two * eyy, m01 = -(two * exy);
+    const fq dm1 = -(two * (exx + eyy)) + fq(4.0f) * (exx * eyy - exy * exy);
+    const fq idM = one / (one + dm1);
+    const fq i00 = m11 * idM, i01 = -(m01 * idM), i11 = m00 * idM;
+    const fq be00 = two * (exx * i00 + exy * i01), be01 = two * (exx * i01 + exy * i11);
+    const fq be11 = two * (exy * i01 + eyy * i11);
+    const fq de = dm1 - two * ezz * (one + dm1);
+    const fq c00 = two * H00 + (H00 * H00 + H10 * H10);
+    const fq c11 = two * H11 + (H01 * H01 + H11 * H11);
+    const fq c01 = H01 + H10 + (H00 * H01 + H10 * H11);
+    const fq dC = (one + c00) * (one + c11) - c01 * c01;
+    const fq iC = one / dC;
+    const fq ci00 = (one + c11) * iC, ci01 = -(c01 * iC), ci11 = (one + c00) * iC;
+    const fq ga00 = -(c00 * ci00 + c01 * ci01), ga01 = -(c00 * ci01 + c01 * ci11);
+    const fq ga11 = -(c01 * ci01 + c11 * ci11);
+    const fq dth = (H00 + H11) + (H00 * H11 - H01 * H10);
+    const fq g = q.grow, thg = one + g, gg2 = two * g + g * g;
+    const fq one_dth = one + dth;
+    const fq eta = (gg2 + thg * thg * de - two * dth - dth * dth) / (one_dth * one_dth);
+    const fq c0 = -(gg2 + thg * thg * eta) / thg;
+    const fq ith = one / thg, tge = thg * (one + eta);
+    const fq mu = q.mu;
+    fq S00 = mu * (c0 + be00 * ith - tge * ga00);
+    fq S01 = mu * (be01 * ith - tge * ga01);
+    fq S11 = mu * (c0 + be11 * ith - tge * ga11);
+    if (q.t_an != 0.0f) {  // anisotropic active stress t_act (1 - 2 kappa) a0 a0^T (direction in FP32)
+        float ax = (1.0f / 3.0f) * ((r[0][0].x + r[1][0].x + r[2][0].x) + (r[0][0].z + r[1][0].z + r[2][0].z) +
+                                    (r[0][1].x + r[1][1].x + r[2][1].x)) - q.cx;
+        float ay = (1.0f / 3.0f) * ((r[0][0].y + r[1][0].y + r[2][0].y) + (r[0][0].w + r[1][0].w + r[2][0].w) +
+                                    (r[0][1].y + r[1][1].y + r[2][1].y)) - q.cy;
+        const float ia = rsqrtf(ax * ax + ay * ay);
+        ax *= ia; ay *= ia;
+        S00 = S00 + fq(q.t_an) * fq(ax * ax); S01 = S01 + fq(q.t_an) * fq(ax * ay);
+        S11 = S11 + fq(q.t_an) * fq(ay * ay);
+    }
+    const fq si = q.s_iso;
+    const fq T00 = si * H00 + S00 + (H00 * S00 + H01 * S01);
+    const fq T01 = si * H01 + S01 + (H00 * S01 + H01 * S11);
+    const fq T10 = si * H10 + S01 + (H10 * S00 + H11 * S01);
+    const fq T11 = si * H11 + S11 + (H10 * S01 + H11 * S11);
+    const fq wA = fq(0.5f) * Gc * q.thick;
+    o.re[0][0] = (wA * (T00 * b0x + T01 * b0y)).f(); o.re[0][1] = (wA * (T10 * b0x + T11 * b0y)).f();
+    o.re[1][0] = (wA * (T00 * b1x + T01 * b1y)).f(); o.re[1][1] = (wA * (T10 * b1x + T11 * b1y)).f();
+    o.re[2][0] = (wA * (T00 * b2x + T01 * b2y)).f(); o.re[2][1] = (wA * (T10 * b2x + T11 * b2y)).f();
+    const fq iF = one / one_dth;
+    const fq f00 = (one + H11) * iF, f01 = -(H01 * iF), f10 = -(H10 * iF), f11 = (one + H00) * iF;
+    const fq K00 = -(H00 * f00 + H01 * f10), K01 = -(H00 * f01 + H01 * f11);
+    const fq K10 = -(H10 * f00 + H11 * f10), K11 = -(H10 * f01 + H11 * f11);
+    const fq EK00 = exx * K00 + exy * K10, EK01 = exx * K01 + exy * K11;
+    const fq EK10 = exy * K00 + eyy * K10, EK11 = exy * K01 + eyy * K11;
+    const fq KEK00 = K00 * EK00 + K10 * EK10, KEK01 = K00 * EK01 + K10 * EK11;
+    const fq KEK11 = K01 * EK01 + K11 * EK11;
+    const fq KK00 = K00 * K00 + K10 * K10, KK01 = K00 * K01 + K10 * K11, KK11 = K01 * K01 + K11 * K11;
+    const fq half(0.5f);
+    const fq D00 = two * EK00 + KEK00 - half * (two * K00 + KK00);
+    const fq D11 = two * EK11 + KEK11 - half * (two * K11 + KK11);
+    const fq D01 = (EK10 + EK01) + KEK01 - half * (K01 + K10 + KK01);
+    const fq tg2 = thg * thg, gg = tg2 - one;
+    const fq dvxx = tg2 * D00 + gg * (exx - half), dvyy = tg2 * D11 + gg * (eyy - half);
+    const fq dvxy = tg2 * D01 + gg * exy, dvzz = gg * (ezz - half);
+    const fq w3 = third * wA;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        o.rea[i][0] = (w3 * ((exx - r[i][1].z) + dvxx)).f();
+        o.rea[i][1] = (w3 * ((eyy - r[i][1].w) + dvyy)).f();
+        o.rea[i][2] = (w3 * ((exy - r[i][2].x) + dvxy)).f();
+        o.rea[i][3] = (w3 * ((ezz - r[i][2].y) + dvzz)).f();
+    }
+    o.mm = w3.f();
+    o.acur = fabsf((half * gc).f());
+}
+
 constexpr int kBndSlots = 96;    // boundary vertices a patch CTA queues for its second loop (more finish in place)
 
 // Per-cell, per-step constants of the boundary terms (computed once per patch CTA).
@@ -821,8 +933,8 @@ constexpr int kBndRec = 10;   // floats per queued boundary vertex: index, F0 an
 // FUSED: the fused form (MixedArgs::va), a separate instantiation so that its code does
 // not weigh on the register allocation of the plain one.  EMAX > 0: the element-slot
 // stride of the shared arrays as a constant (a.emax == EMAX), so that the field offsets
-// are immediates; 0: a.emax at run time.
-template <int MINB, bool FUSED, int EMAX = 0>
+// are immediates; 0: a.emax at run time.  FF: the float-float element (element2d_ff).
+template <int MINB, bool FUSED, int EMAX = 0, bool FF = false>
 __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a, const CellDev* __restrict__ cells,
                                                                  const WorkItem* __restrict__ work) {
     extern __shared__ float smf[];
@@ -876,7 +988,8 @@ __global__ void __launch_bounds__(128, MINB) k_patch_phase_mixed(MixedArgs a, co
             Elem2 o;
             ElemParams qe = q;
             if (c.mu_e) qe.mu = __ldg(reinterpret_cast<const float*>(c.mu_e) + e);
-            element2d(r, qe, o);
+            if (FF) element2d_ff(r, qe, o);
+            else element2d(r, qe, o);
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 smf[(2 * k + 0) * emax + j] = o.re[k][0];
@@ -1451,6 +1564,7 @@ const void* mixed_kernel(int kind) {
         case 3: return (const void*)k_patch_phase_mixed<7, false>;
         case 4: return (const void*)k_patch_phase_mixed<8, false>;
         case 5: return (const void*)k_patch_phase_mixed<5, true>;
+        case 6: return (const void*)k_patch_phase_mixed<2, false, 0, true>;
         default: return (const void*)k_patch_phase_mixed<5, false>;
     }
 }
@@ -1466,7 +1580,7 @@ cudaError_t configure_mixed(size_t max_smem) {
                                  (int)(max_smem > at.sharedSizeBytes ? max_smem - at.sharedSizeBytes : 0));
         if (e != cudaSuccess) return e;
     }
-    for (int kind = 1; kind <= 5; ++kind) {
+    for (int kind = 1; kind <= 6; ++kind) {
         cudaFuncAttributes at;
         cudaError_t e = cudaFuncGetAttributes(&at, mixed_kernel(kind));
         if (e != cudaSuccess) return e;
@@ -1477,7 +1591,8 @@ cudaError_t configure_mixed(size_t max_smem) {
     return configure_staged(max_smem);
 }
 
-// resident CTAs per SM of the plain kernel variant `kind` (1-4, see k_patch_phase_mixed; 5 fused)
+// resident CTAs per SM of the plain kernel variant `kind` (1-4, see k_patch_phase_mixed; 5 fused;
+// 6 the float-float element)
 int mixed_occupancy(int threads, size_t smem, int kind) { return occupancy_cached(mixed_kernel(kind), threads, smem); }
 int mixed_occupancy(int threads, size_t smem) { return mixed_occupancy(threads, smem, 1); }
 
@@ -1514,6 +1629,7 @@ void launch_patch_mixed(const CellDev* cells, const WorkItem* work, int nwork, i
         case 2: k_patch_phase_mixed<6, false><<<grid, threads, smem, st>>>(a, cells, work); break;
         case 3: k_patch_phase_mixed<7, false><<<grid, threads, smem, st>>>(a, cells, work); break;
         case 4: k_patch_phase_mixed<8, false><<<grid, threads, smem, st>>>(a, cells, work); break;
+        case 6: k_patch_phase_mixed<2, false, 0, true><<<grid, threads, smem, st>>>(a, cells, work); break;
         default:
             if (emax == 512) k_patch_phase_mixed<5, false, 512><<<grid, threads, smem, st>>>(a, cells, work);
             else k_patch_phase_mixed<5, false><<<grid, threads, smem, st>>>(a, cells, work);
