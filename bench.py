@@ -870,6 +870,7 @@ def run_phase(args):
             eng.set_patch_kernel(args.patch_kernel)
             eng.set_vertex_kernel(args.vertex_kernel)
             eng.set_fused(bool(args.fused))
+            eng.set_element_precision(args.element_ff)
         if args.shape:
             t, e_ = (int(x) for x in args.shape.split(","))
             eng.set_shape(t, e_)
@@ -883,7 +884,7 @@ def run_phase(args):
                       "vertex_ms": r["ms_v"] / args.steps, "patch_ms": r["ms_p"] / args.steps,
                       "cell_steps_per_s": ncells * args.steps / (r["total_ms"] / 1e3), "shape": [thr, emax],
                       "patch_kernel": args.patch_kernel, "vertex_kernel": args.vertex_kernel,
-                      "fused": eng.fused()}))
+                      "fused": eng.fused(), "element_ff": args.element_ff}))
     eng.close()
 
 
@@ -994,6 +995,8 @@ def main():
                          "capped for 6-8 CTAs per SM")
     ap.add_argument("--vertex-kernel", type=int, default=0, choices=[0, 1, 2, 3],
                     help="with --phase mixed: vertex kernel for 5, 4, 6 or 8 blocks per SM")
+    ap.add_argument("--element-ff", type=int, default=0, choices=[0, 1],
+                    help="--phase mixed: 1 = the float-float element (wcfe_engine_set_element_precision)")
     ap.add_argument("--fused", type=int, default=0, choices=[0, 1],
                     help="with --phase mixed: fold each next vertex phase into the patch phase (default 0)")
     args = ap.parse_args()
